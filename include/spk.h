@@ -1,0 +1,270 @@
+/*
+ * spk.h -- C ABI of the GB300 path tracer.
+ *
+ * This is the drop-in boundary for Sparkle's `cpu` pipeline. Sparkle has no C ABI: its boundary is the
+ * C++ virtual `Renderer` (libraries/include/renderer/renderer/Renderer.h:28-108) instantiated as
+ * `CPURenderer` (libraries/source/renderer/renderer/CPURenderer.cpp) for `RenderConfig::Pipeline::Cpu`,
+ * reading the render-thread scene through `SceneRenderProxy` (libraries/include/renderer/proxy/
+ * SceneRenderProxy.h:46-121). Each entry point below names the reference interface it replaces.
+ *
+ * Conventions
+ *  - Every call returns spk_status (0 = ok) and never aborts; the text of the last error of a context is
+ *    returned by spk_last_error().
+ *  - Plain pointers and sizes only. Host pointers are copied in or out before the call returns; the
+ *    *_device entry points take device pointers that stay owned by the caller.
+ *  - A context owns all device memory it allocates. One context is used by one thread at a time (the
+ *    reference renders on its render thread only, Renderer.cpp:20); several contexts may coexist.
+ *  - Coordinate system, units and constants are the reference's: Z up, Y front, X right
+ *    (libraries/include/core/math/Types.h:45-47).
+ */
+#ifndef SPK_H_
+#define SPK_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPK_ABI_VERSION 1u
+
+typedef int32_t spk_status;
+enum {
+    SPK_OK = 0,
+    SPK_ERR_INVALID_ARGUMENT = 1,
+    SPK_ERR_CUDA = 2,
+    SPK_ERR_OUT_OF_MEMORY = 3,
+    SPK_ERR_NOT_READY = 4,      /* e.g. render before set_scene / set_config */
+    SPK_ERR_DEVICE_LIMIT = 5,   /* a device-side bound (traversal stack, iteration budget) was exceeded */
+    SPK_ERR_INTERNAL = 6,
+};
+
+typedef struct spk_ctx spk_ctx;
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Scene description (render-thread proxies, copied in by spk_set_scene)                             */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* A triangle mesh as held by `Mesh` (libraries/include/io/Mesh.h:7-141): per-vertex SoA attributes and a
+ * triangle index list. normals are required (Mesh::Validate, Mesh.h:136-140); tangents may be NULL
+ * (Mesh::GetTangent then returns (1,0,0,1), Mesh.h:104-118); uvs may be NULL (zero, Mesh.h:120-134). */
+typedef struct spk_mesh {
+    const float *positions; /* [num_vertices][3] */
+    const float *normals;   /* [num_vertices][3] */
+    const float *tangents;  /* [num_vertices][4] or NULL */
+    const float *uvs;       /* [num_vertices][2] or NULL */
+    const uint32_t *indices; /* [num_faces][3] */
+    uint32_t num_vertices;
+    uint32_t num_faces;
+} spk_mesh;
+
+enum { SPK_PRIM_MESH = 0, SPK_PRIM_SPHERE = 1 };
+
+/* One `PrimitiveRenderProxy` (libraries/include/renderer/proxy/PrimitiveRenderProxy.h:14-78): a mesh
+ * instance (`MeshRenderProxy`) or an analytic sphere (`SphereRenderProxy`, SphereRenderProxy.h:9-42).
+ * `transform` is the affine matrix M (row-major 3x4: linear part | translation) of the proxy's
+ * `Transform`; `inv_transform` is the inverse the reference keeps beside it (Transform.h:141-142) and uses
+ * to move world rays into local space (MeshRenderProxy.cpp:99-100). Both are given by the caller so that
+ * every consumer uses the same bits. A sphere's centre is the translation column; `radius` is its scaled
+ * radius (SphereRenderProxy::SetRadius, SphereRenderProxy.h:32-35). */
+typedef struct spk_instance {
+    uint32_t type;        /* SPK_PRIM_MESH / SPK_PRIM_SPHERE */
+    uint32_t mesh_id;     /* index into the mesh array (mesh instances) */
+    uint32_t material_id; /* index into the material array */
+    float radius;         /* spheres only */
+    float transform[12];     /* row-major 3x4 */
+    float inv_transform[12]; /* row-major 3x4 */
+} spk_instance;
+
+enum { SPK_MAT_PBR = 0, SPK_MAT_DIELECTRIC = 1 };
+
+/* A material render proxy: `PbrMaterialRenderProxy` (PbrMaterialRenderProxy.h:10-52) or
+ * `DieletricMaterialRenderProxy` (DialetricMaterialRenderProxy.h:10-39), constant-valued
+ * (`MaterialResource`, libraries/include/io/Material.h:7-20). The reference's Lambertian and Metal
+ * materials are PBR with fixed metallic/roughness (LambertianMaterial.h:8-15, MetalMaterial.h:8-15). */
+typedef struct spk_material {
+    uint32_t type; /* SPK_MAT_PBR / SPK_MAT_DIELECTRIC */
+    float base_color[3];
+    float emissive[3];
+    float metallic;
+    float roughness;
+    float eta;
+} spk_material;
+
+enum { SPK_SKY_NONE = 0, SPK_SKY_GRADIENT = 1, SPK_SKY_CUBE = 2 };
+
+/* `SkyRenderProxy::Evaluate` input (SkyRenderProxy.cpp:50-64): no sky (misses add nothing), the
+ * white-to-colour gradient on d.z, or an RGBA float cube map sampled per face bilinearly with wrap
+ * (Image2DCube::Sample, libraries/source/io/Image.cpp:298-357). Faces are +X,-X,+Y,-Y,+Z,-Z, each
+ * cube_size x cube_size texels, row-major, 4 floats per texel. */
+typedef struct spk_sky {
+    uint32_t mode;
+    float color[3];
+    uint32_t cube_size;
+    const float *cube_rgba; /* [6][cube_size][cube_size][4] or NULL */
+} spk_sky;
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Camera and render configuration                                                                   */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* `CameraRenderProxy` posture + focus plane + attribute (CameraRenderProxy.h:30-57), i.e. the values
+ * SetupViewRay reads (CPURenderer.cpp:220-238). spk_camera_from_look() derives them the way
+ * CameraRenderProxy::Update/OnTransformDirty do (CameraRenderProxy.cpp:10-76, 118-128). */
+typedef struct spk_camera {
+    float position[3];
+    float right[3];
+    float up[3];
+    float front[3];
+    float lower_left[3];
+    float max_u[3];
+    float max_v[3];
+    float aperture_radius;
+    float exposure;
+    float far_plane;
+} spk_camera;
+
+enum { SPK_RNG_XOSHIRO128P = 0, SPK_RNG_XOSHIRO256SS = 1 };
+enum { SPK_DEBUG_COLOR = 0 };
+enum { SPK_KERNEL_AUTO = 0, SPK_KERNEL_MEGAKERNEL = 1, SPK_KERNEL_WAVEFRONT = 2 };
+
+/* The subset of `RenderConfig` (libraries/include/renderer/RenderConfig.h:28-123) the cpu pipeline reads,
+ * with the cvar names of RenderConfig.cpp:13-47 as field names. `rng` selects the per-pixel generator:
+ * the reference's Xoshiro128+ reseeded with j*W+i+frame_seed*W*H (Sampler.h:16-40,
+ * CPURenderer.cpp:436-444), or xoshiro256** seeded from (seed, pixel index, frame). `enable_nee` turns on
+ * next-event estimation (not part of the reference cpu pipeline). `kernel` selects the device
+ * schedule; both schedules compute identical results. */
+typedef struct spk_config {
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp;     /* `spp` cvar: per-frame sample weight (CPURenderer.cpp:102-105) */
+    uint32_t max_spp; /* `max_spp` cvar: accumulation cap (CameraRenderProxy.cpp:66-75) */
+    uint32_t bounce;  /* `bounce` cvar: max path segments (CPURenderer.cpp:257-259) */
+    uint32_t spatial_denoise; /* `spatial_denoise` cvar (CPURenderer.cpp:452-526) */
+    uint32_t enable_nee;
+    uint32_t rng;
+    uint32_t seed;
+    uint32_t debug_mode;
+    uint32_t kernel;
+} spk_config;
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Ray casting (ray-set parity)                                                                      */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* A ray as `Ray` holds it (libraries/include/core/math/Ray.h:8-65): origin and unit direction. */
+typedef struct spk_ray {
+    float origin[3];
+    float direction[3];
+} spk_ray;
+
+#define SPK_INVALID_ID 0xFFFFFFFFu
+
+/* The closest-hit candidate `IntersectionCandidate` (Intersection.h:90-103) after the scene walk:
+ * world-space t (Ray::InverseAt, Ray.h:43-47), barycentrics u,v of the winning triangle, the scene
+ * primitive index (the caller's instance index, not the TLAS-reordered slot) and the original face index.
+ * Misses have prim == SPK_INVALID_ID. Spheres report face == SPK_INVALID_ID and u = v = 0. For any-hit
+ * queries only `prim` != SPK_INVALID_ID is meaningful. */
+typedef struct spk_hit {
+    float t;
+    float u;
+    float v;
+    uint32_t prim;
+    uint32_t face;
+} spk_hit;
+
+/* Counters of the last spk_render / spk_trace call. */
+typedef struct spk_stats {
+    uint64_t extension_rays; /* closest-hit segments traced */
+    uint64_t shadow_rays;    /* any-hit segments traced (NEE) */
+    uint64_t paths;          /* camera paths started */
+    float device_ms;         /* device time of the call, CUDA events on the context stream */
+    float trace_kernel_ms;   /* device time of the traversal kernels alone */
+    uint32_t trace_launches; /* launches of the traversal kernels */
+    uint32_t kernel_launches; /* all kernel launches of the call */
+    uint32_t error_flags;    /* device-side error bits (stack overflow, iteration budget) */
+    uint32_t bvh_nodes;      /* wide nodes resident for the scene */
+    uint64_t bvh_bytes;      /* bytes of wide nodes + triangle records resident */
+} spk_stats;
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Entry points                                                                                      */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* ABI version of the loaded library (SPK_ABI_VERSION). */
+uint32_t spk_abi_version(void);
+
+/* Replaces Renderer::CreateRenderer(Pipeline::Cpu, ...) (Renderer.cpp:17-52) + CPURenderer's constructor
+ * (CPURenderer.cpp:22-28). Selects CUDA device `device` and creates the context stream. */
+spk_status spk_create(int32_t device, spk_ctx **out_ctx);
+
+/* Releases every device allocation of the context. */
+spk_status spk_destroy(spk_ctx *ctx);
+
+/* Text of the last error on this context ("" if none). Valid until the next call on the context. */
+const char *spk_last_error(const spk_ctx *ctx);
+
+/* Replaces SceneRenderProxy::UpdateBVH (SceneRenderProxy.cpp:269-297): builds every BLAS
+ * (MeshRenderProxy::BuildBVH, MeshRenderProxy.cpp:310-314) and the TLAS (SceneRenderProxy.cpp:31-69) on
+ * the host, flattens them into compressed 8-wide nodes and uploads them with the shading attributes.
+ * Marks the accumulation dirty, as any primitive change does. */
+spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_meshes,
+                         const spk_instance *instances, uint32_t num_instances,
+                         const spk_material *materials, uint32_t num_materials, const spk_sky *sky);
+
+/* Replaces CameraRenderProxy::OnTransformDirty/UpdateAttribute (CameraRenderProxy.cpp:118-128): a new
+ * camera marks pixels dirty, so the next frame clears the accumulation (CPURenderer.cpp:128-137). */
+spk_status spk_set_camera(spk_ctx *ctx, const spk_camera *camera);
+
+/* Derives an spk_camera from a look-at posture the way CameraRenderProxy::Update (vertical fov, focus
+ * distance, aspect ratio; CameraRenderProxy.cpp:21-34) and OnTransformDirty (:113-136) do. */
+spk_status spk_camera_from_look(const float position[3], const float target[3], const float world_up[3],
+                                float vertical_fov_rad, float focus_distance, float aperture_radius,
+                                float exposure, uint32_t width, uint32_t height, spk_camera *out);
+
+/* Replaces CPURenderer::InitRenderResources (CPURenderer.cpp:38-105): sizes the frame buffer, G-buffer
+ * and output image for `width` x `height` and derives the per-frame sample count round(sqrt(spp))^2. */
+spk_status spk_set_config(spk_ctx *ctx, const spk_config *config);
+
+/* Replaces `num_frames` calls of CPURenderer::Render (CPURenderer.cpp:119-208) on a static scene: per frame
+ * the clear (if dirty), BasePass (:419-450), DenoisePass (:506-552) and ToneMappingPass (:565-576), with
+ * the camera's cumulated-sample bookkeeping between frames (CameraRenderProxy.cpp:66-75). Asynchronous
+ * with respect to the host: results are visible to spk_read_framebuffer / spk_synchronize. */
+spk_status spk_render(spk_ctx *ctx, uint32_t num_frames);
+
+/* Copies the accumulated HDR frame buffer (`frame_buffer_`, H rows of W float4, row j = image row j from
+ * the bottom as the reference indexes it) and/or the tonemapped RGBA16F output image (`output_image_`,
+ * already flipped: row 0 is the top row, CPURenderer.cpp:573) to host memory. Either pointer may be NULL. */
+spk_status spk_read_framebuffer(spk_ctx *ctx, float *hdr_rgba, uint16_t *rgba16f);
+
+/* Device pointers of the context's frame buffer (float4 x W*H) and output image (half4 x W*H), valid
+ * until the next spk_set_config / spk_destroy. */
+spk_status spk_framebuffer_device(spk_ctx *ctx, void **hdr_rgba, void **rgba16f);
+
+/* Camera accumulation counters: samples already folded into the frame buffer (capped at max_spp), and
+ * the number of samples dispatched since the last clear (the per-frame seed base). Mirrors
+ * CameraRenderProxy::GetCumulatedSampleCount and CPURenderer::dispatched_sample_count_. */
+spk_status spk_sample_counts(const spk_ctx *ctx, uint32_t *cumulated, uint32_t *dispatched);
+
+/* Replaces CPURenderer::IsReadyForAutoScreenshot (CPURenderer.cpp:32-36): cumulated >= max_spp. */
+int32_t spk_is_converged(const spk_ctx *ctx);
+
+/* Replaces SceneRenderProxy::Intersect<AnyHit> (SceneRenderProxy.cpp:299-309) over a host ray set:
+ * closest hit (any_hit = 0) or any hit (any_hit = 1) per ray. `hits` receives num_rays records. */
+spk_status spk_trace(spk_ctx *ctx, const spk_ray *rays, uint64_t num_rays, spk_hit *hits, int32_t any_hit);
+
+/* Same query on device-resident rays/hits (arrays of spk_ray / spk_hit in device memory). */
+spk_status spk_trace_device(spk_ctx *ctx, const void *d_rays, uint64_t num_rays, void *d_hits, int32_t any_hit);
+
+/* Waits for all work queued on the context stream. */
+spk_status spk_synchronize(spk_ctx *ctx);
+
+/* Counters of the last spk_render / spk_trace / spk_trace_device call (waits for it to finish). */
+spk_status spk_get_stats(spk_ctx *ctx, spk_stats *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPK_H_ */

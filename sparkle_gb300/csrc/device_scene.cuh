@@ -1,0 +1,59 @@
+// device_scene.cuh -- layout of the resident scene in device memory.
+//
+//  nodes     : WideNode[]   80 B each, BLAS nodes of every mesh followed by the TLAS nodes
+//  tris      : float4[3*T]  48 B per triangle in BLAS leaf order: {p0.xyz, e1.x} {e1.yz, e2.xy}
+//                           {e2.z, face id, -, -}; p0/e1/e2 are BLAS::Triangle (MeshRenderProxy.cpp:78-92)
+//  tlas_items: uint32[]     instance index per TLAS leaf slot (TLAS::Build's prim_ids reorder)
+//  instances : DevInstance[] caller order
+//  verts     : float4[3*V]  48 B per vertex {n.xyz, t.x} {t.yzw, uv.x} {uv.y, -, -, -}
+//  faces     : uint4[F]     vertex indices of each face (w unused), per-mesh ranges
+//  materials : DevMaterial[]
+//  sky cube  : float4[6*N*N]
+#pragma once
+
+#include <cstdint>
+
+#include "spk_math.cuh"
+
+namespace spk {
+
+struct alignas(16) DevInstance {
+    float m[12];     // transform rows
+    float minv[12];  // inverse transform rows
+    uint32_t type;   // SPK_PRIM_MESH / SPK_PRIM_SPHERE
+    uint32_t blas_root;
+    uint32_t material;
+    float radius;
+    uint32_t vert_base;  // first vertex of the mesh in `verts`
+    uint32_t face_base;  // first face of the mesh in `faces`
+    uint32_t mesh_id;
+    uint32_t pad;
+};
+static_assert(sizeof(DevInstance) == 128, "DevInstance is 128 bytes");
+
+struct alignas(16) DevMaterial {
+    float base[3];
+    uint32_t type;
+    float emissive[3];
+    uint32_t is_emissive;  // ||emissive|| > Eps, evaluated once on the host exactly as SamplePixel does
+    float metallic, roughness, eta, pad;
+};
+static_assert(sizeof(DevMaterial) == 48, "DevMaterial is 48 bytes");
+
+struct DevScene {
+    const uint4 *nodes;
+    const float4 *tris;
+    const uint32_t *tlas_items;
+    const DevInstance *instances;
+    const float4 *verts;
+    const uint4 *faces;
+    const DevMaterial *materials;
+    const float4 *sky_cube;
+    uint32_t tlas_root;  // kInvalid for an empty scene
+    uint32_t sky_mode;
+    uint32_t sky_size;
+    float sky_color[3];
+    float scene_abs_x;  // max |x| over world bounds; bounds the x-only world-t error used for pruning
+};
+
+}  // namespace spk

@@ -1,0 +1,216 @@
+// kernels.cu -- ray-set query, one-kernel path tracer (BasePass), resolve (DenoisePass + ToneMappingPass).
+//
+// Compiled with -fmad=false: every multiply and add rounds separately, as the reference's (contraction-free)
+// host arithmetic does; the slab tests use explicit fmaf.
+#include <cuda_fp16.h>
+
+#include "kernels.cuh"
+
+namespace spk {
+namespace {
+
+__device__ __forceinline__ void warp_add_u64(unsigned long long *dst, uint32_t v) {
+    const uint32_t total = __reduce_add_sync(__activemask(), v);
+    if ((threadIdx.x & 31u) == (__ffs(__activemask()) - 1)) atomicAdd(dst, static_cast<unsigned long long>(total));
+}
+
+// ------------------------------------------------------------------------------------------------
+// Ray-set query: persistent warps pull 32-ray batches from a global counter.
+// ------------------------------------------------------------------------------------------------
+template <int kMode>
+__global__ void __launch_bounds__(128) k_trace(DevScene S, const float *__restrict__ rays, uint64_t n,
+                                               spk_hit_dev *__restrict__ hits, Counters *counters) {
+    uint32_t err = 0;
+    const uint32_t lane = threadIdx.x & 31u;
+    unsigned long long *next = &counters->queue_counters[0];
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(next, 32ull);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const uint64_t k = base + lane;
+        if (k < n) {
+            const float *r = rays + k * 6;
+            const f3 o = mk3(r[0], r[1], r[2]);
+            const f3 d = mk3(r[3], r[4], r[5]);
+            const TraceResult res = trace_ray<kMode>(S, o, d, kFltMax, err);
+            spk_hit_dev out;
+            if (res.inst == kInvalid) {
+                out = spk_hit_dev{0.f, 0.f, 0.f, kInvalid, kInvalid};
+            } else if (kMode == kTraceClosest) {
+                out = spk_hit_dev{res.t, res.u, res.v, res.inst, res.face};
+            } else {
+                out = spk_hit_dev{0.f, 0.f, 0.f, res.inst, kInvalid};
+            }
+            hits[k] = out;
+        }
+        warp_add_u64(&counters->extension_rays, k < n ? 1u : 0u);
+    }
+    if (err) atomicOr(&counters->error_flags, err);
+}
+
+// ------------------------------------------------------------------------------------------------
+// BasePass: one thread per pixel runs RenderPixel + SamplePixel (CPURenderer.cpp:240-417).
+// ------------------------------------------------------------------------------------------------
+template <int kKind>
+__global__ void __launch_bounds__(128) k_render_mega(DevScene S, DevCamera cam, FrameBuffers fb, RenderParams p,
+                                                     Counters *counters) {
+    const uint32_t i = blockIdx.x * 16u + (threadIdx.x & 15u);
+    const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 4);
+    uint32_t err = 0, rays = 0;
+    if (i < fb.width && j < fb.height) {
+        Rng rng;
+        rng_seed_pixel<kKind>(rng, p.seed, i, j, fb.width, fb.height, p.frame_seed);
+        const float pw = 1.f / static_cast<float>(fb.width - 1);
+        const float ph = 1.f / static_cast<float>(fb.height - 1);
+        const float u = (static_cast<float>(i) + rng_unit<kKind>(rng)) * pw;
+        const float v = (static_cast<float>(j) + rng_unit<kKind>(rng)) * ph;
+        f3 o, d;
+        camera_ray<kKind>(cam, rng, u, v, o, d);
+        f3 color = mk3(0.f, 0.f, 0.f), thr = mk3(1.f, 1.f, 1.f), first_normal = mk3(0.f, 0.f, 0.f);
+        float valid = 1.f;
+        for (uint32_t bounce = 0; bounce < p.bounce; ++bounce) {
+            ++rays;
+            const TraceResult hit = trace_ray<kTraceClosest>(S, o, d, kFltMax, err);
+            if (hit.inst == kInvalid) {
+                if (S.sky_mode != 0u) color = color + cmul(sky_eval(S, d), thr);
+                break;
+            }
+            const Surface surf = make_surface(S, hit, o, d);
+            const DevMaterial mat = S.materials[surf.material];
+            if (bounce == 0) first_normal = surf.normal;
+            if (mat.is_emissive) {
+                color = color + cmul(mk3(mat.emissive[0], mat.emissive[1], mat.emissive[2]), thr);
+                break;
+            }
+            f3 next_dir;
+            const f3 this_thr = sample_surface<kKind>(rng, mat, d, surf.normal, surf.tangent, next_dir);
+            thr = cmul(thr, this_thr);
+            if (sqnorm(thr) < kEps) {
+                valid = -1.f;
+                break;
+            }
+            if (bounce >= 3) {
+                float q = max_std(thr.x, max_std(thr.y, thr.z));
+                q = (q < 0.05f) ? 0.05f : (1.0f < q) ? 1.0f : q;
+                if (rng_unit<kKind>(rng) > q) break;
+                thr = mk3(thr.x / q, thr.y / q, thr.z / q);
+            }
+            o = surf.location + next_dir * kTolerance;
+            d = next_dir;
+        }
+        const size_t k = static_cast<size_t>(j) * fb.width + i;
+        fb.gcolor[k] = make_float4(min_std(color.x, kOutputLimit), min_std(color.y, kOutputLimit),
+                                   min_std(color.z, kOutputLimit), valid);
+        if (p.spatial_denoise) fb.gnormal[k] = make_float4(first_normal.x, first_normal.y, first_normal.z, 0.f);
+    }
+    warp_add_u64(&counters->extension_rays, rays);
+    if (err) atomicOr(&counters->error_flags, err);
+}
+
+// ------------------------------------------------------------------------------------------------
+// DenoisePass + ToneMappingPass (CPURenderer.cpp:452-576) as one gather kernel.
+// ------------------------------------------------------------------------------------------------
+__constant__ int c_dirs[8][2] = {{1, 0}, {0, 1}, {-1, 0}, {0, -1}, {-1, -1}, {1, -1}, {-1, 1}, {1, 1}};
+
+__device__ __forceinline__ bool px_valid(const float4 &c) { return c.w > 0.f; }
+__device__ __forceinline__ bool px_sky(const float4 &c, const float4 &n) {
+    return px_valid(c) && fabsf(n.x) <= 1e-5f && fabsf(n.y) <= 1e-5f && fabsf(n.z) <= 1e-5f;
+}
+
+__device__ __forceinline__ float aces(float c, float exposure) {
+    const float x = c * exposure;
+    float y = (x * (x * 2.51f + 0.03f)) / (x * (x * 2.43f + 0.59f) + 0.14f);
+    y = (1.f < y) ? 1.f : y;
+    y = (y < 0.f) ? 0.f : y;
+    return y;
+}
+
+__global__ void __launch_bounds__(256) k_resolve(FrameBuffers fb, float f, float exposure, uint32_t spatial) {
+    const uint32_t i = blockIdx.x * 32u + (threadIdx.x & 31u);
+    const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 5);
+    if (i >= fb.width || j >= fb.height) return;
+    const int W = static_cast<int>(fb.width), H = static_cast<int>(fb.height);
+    const size_t k = static_cast<size_t>(j) * fb.width + i;
+    float4 in = fb.gcolor[k];
+    if (spatial && !px_valid(in)) {
+        // SpatialDenoisePixel as a gather: a valid, non-sky neighbour S fills this pixel when this pixel is
+        // the first of S's 8 directions that is in bounds, invalid and has normal similarity >= 0.99. Among
+        // several such S the one last in row-major order wins (the single-threaded order of the passes).
+        long best_writer = -1;
+        float4 best_color = in;
+        for (int dk = 0; dk < 8; ++dk) {
+            const int si = static_cast<int>(i) - c_dirs[dk][0], sj = static_cast<int>(j) - c_dirs[dk][1];
+            if (si < 0 || si >= W || sj < 0 || sj >= H) continue;
+            const size_t sk = static_cast<size_t>(sj) * fb.width + si;
+            const float4 sc = fb.gcolor[sk];
+            const float4 sn = fb.gnormal[sk];
+            if (!px_valid(sc) || px_sky(sc, sn)) continue;
+            const f3 wn = mk3(sn.x, sn.y, sn.z);
+            long target = -1;
+            for (int tk = 0; tk < 8; ++tk) {
+                const int ni = si + c_dirs[tk][0], nj = sj + c_dirs[tk][1];
+                if (ni < 0 || ni >= W || nj < 0 || nj >= H) continue;
+                const size_t nk = static_cast<size_t>(nj) * fb.width + ni;
+                if (fb.gcolor[nk].w > 0.f) continue;
+                const float4 nn = fb.gnormal[nk];
+                if (dot3(mk3(nn.x, nn.y, nn.z), wn) < 0.99f) continue;
+                target = static_cast<long>(nk);
+                break;
+            }
+            if (target == static_cast<long>(k) && static_cast<long>(sk) > best_writer) {
+                best_writer = static_cast<long>(sk);
+                best_color = make_float4(sc.x, sc.y, sc.z, 1.f);
+            }
+        }
+        in = best_color;
+    }
+    float4 a = fb.fb[k];
+    a = make_float4(in.x + (a.x - in.x) * f, in.y + (a.y - in.y) * f, in.z + (a.z - in.z) * f, in.w + (a.w - in.w) * f);
+    fb.fb[k] = a;
+    ushort4 o;
+    o.x = __half_as_ushort(__float2half_rn(aces(a.x, exposure)));
+    o.y = __half_as_ushort(__float2half_rn(aces(a.y, exposure)));
+    o.z = __half_as_ushort(__float2half_rn(aces(a.z, exposure)));
+    o.w = __half_as_ushort(__float2half_rn(1.f));
+    fb.out[static_cast<size_t>(fb.height - 1 - j) * fb.width + i] = o;
+}
+
+}  // namespace
+
+cudaError_t launch_trace(const DevScene &scene, const float *rays, uint64_t n, void *hits, int mode,
+                         Counters *counters, int num_sms, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(&counters->queue_counters[0], 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    const uint64_t warps_needed = (n + 31) / 32;
+    uint64_t blocks = static_cast<uint64_t>(num_sms) * 12;  // persistent: ~12 blocks of 4 warps per SM
+    blocks = std::min<uint64_t>(blocks, (warps_needed + 3) / 4);
+    if (blocks == 0) blocks = 1;
+    auto *h = static_cast<spk_hit_dev *>(hits);
+    if (mode == kTraceClosest) {
+        k_trace<kTraceClosest><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, rays, n, h, counters);
+    } else {
+        k_trace<kTraceAnyRef><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, rays, n, h, counters);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_render_mega(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
+                               const RenderParams &p, Counters *counters, cudaStream_t stream) {
+    const dim3 grid((fbuf.width + 15) / 16, (fbuf.height + 7) / 8);
+    if (p.rng == 0) {
+        k_render_mega<0><<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
+    } else {
+        k_render_mega<1><<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resolve(const FrameBuffers &fbuf, float moving_average, float exposure, uint32_t spatial_denoise,
+                           cudaStream_t stream) {
+    const dim3 grid((fbuf.width + 31) / 32, (fbuf.height + 7) / 8);
+    k_resolve<<<grid, 256, 0, stream>>>(fbuf, moving_average, exposure, spatial_denoise);
+    return cudaGetLastError();
+}
+
+}  // namespace spk

@@ -1,0 +1,710 @@
+// spk_api.cu -- the C ABI (include/spk.h) and the host renderer behind it.
+//
+// `spk_ctx` plays CPURenderer (libraries/source/renderer/renderer/CPURenderer.cpp) for one scene: it owns
+// the resident scene (SceneRenderProxy's BVHs, flattened for the device), the camera and config snapshot,
+// the frame buffers, and the sample bookkeeping of CameraRenderProxy (CameraRenderProxy.cpp:66-75) and
+// CPURenderer::dispatched_sample_count_ (CPURenderer.cpp:128-137, 206-207).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/spk.h"
+#include "bvh_builder.h"
+#include "kernels.cuh"
+#include "wavefront.cuh"
+
+using namespace spk;
+
+namespace {
+
+template <class T>
+struct DevBuf {
+    T *ptr = nullptr;
+    size_t count = 0;
+    void reset() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        count = 0;
+    }
+};
+
+}  // namespace
+
+struct spk_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    std::vector<cudaEvent_t> trace_events;  // start/stop pairs of traversal launches of the last call
+    std::string error;
+
+    // resident scene
+    DevBuf<uint4> nodes;
+    DevBuf<float4> tris;
+    DevBuf<uint32_t> tlas_items;
+    DevBuf<DevInstance> instances;
+    DevBuf<float4> verts;
+    DevBuf<uint4> faces;
+    DevBuf<DevMaterial> materials;
+    DevBuf<float4> sky;
+    DevScene scene{};
+    bool has_scene = false;
+    uint32_t bvh_nodes = 0;
+    uint64_t bvh_bytes = 0;
+
+    // config / camera / frame buffers
+    spk_config cfg{};
+    bool has_config = false;
+    uint32_t spp_eff = 1;
+    DevCamera cam{};
+    bool has_camera = false;
+    DevBuf<float4> gcolor, gnormal, fb;
+    DevBuf<ushort4> out;
+    WavefrontState wf{};
+
+    // CameraRenderProxy / CPURenderer sample bookkeeping
+    uint32_t cumulated = 0, pending = 0, dispatched = 0;
+    bool dirty = true;
+
+    // counters
+    Counters *counters = nullptr;  // device
+    spk_stats last{};
+    bool stats_pending = false;
+    uint32_t launches_in_call = 0;
+};
+
+namespace {
+
+spk_status fail(spk_ctx *ctx, spk_status code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->error = buf;
+    return code;
+}
+
+spk_status cuda_fail(spk_ctx *ctx, cudaError_t e, const char *what) {
+    return fail(ctx, e == cudaErrorMemoryAllocation ? SPK_ERR_OUT_OF_MEMORY : SPK_ERR_CUDA, "%s: %s", what,
+                cudaGetErrorString(e));
+}
+
+template <class T>
+cudaError_t upload(DevBuf<T> &buf, const T *host, size_t count, cudaStream_t stream) {
+    buf.reset();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&buf.ptr, count * sizeof(T));
+    if (e != cudaSuccess) return e;
+    buf.count = count;
+    e = cudaMemcpyAsync(buf.ptr, host, count * sizeof(T), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(stream);
+}
+
+template <class T>
+cudaError_t alloc(DevBuf<T> &buf, size_t count) {
+    buf.reset();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&buf.ptr, count * sizeof(T));
+    if (e == cudaSuccess) buf.count = count;
+    return e;
+}
+
+int host_threads() {
+    const unsigned n = std::thread::hardware_concurrency();
+    return n == 0 ? 1 : static_cast<int>(std::min(n, 64u));
+}
+
+// Outward-rounded world box of a transformed local box (8 corners, evaluated in double).
+BuildBox world_box(const float *m, const double lo[3], const double hi[3]) {
+    BuildBox b;
+    double mn[3] = {std::numeric_limits<double>::max(), std::numeric_limits<double>::max(),
+                    std::numeric_limits<double>::max()};
+    double mx[3] = {-mn[0], -mn[1], -mn[2]};
+    for (int c = 0; c < 8; ++c) {
+        const double p[3] = {(c & 1) ? hi[0] : lo[0], (c & 2) ? hi[1] : lo[1], (c & 4) ? hi[2] : lo[2]};
+        for (int r = 0; r < 3; ++r) {
+            const double w = m[4 * r + 3] + m[4 * r] * p[0] + m[4 * r + 1] * p[1] + m[4 * r + 2] * p[2];
+            mn[r] = std::min(mn[r], w);
+            mx[r] = std::max(mx[r], w);
+        }
+    }
+    for (int r = 0; r < 3; ++r) {
+        const double pad = 1e-6 * (std::fabs(mn[r]) + std::fabs(mx[r]) + (mx[r] - mn[r])) + 1e-30;
+        b.lo[r] = std::nextafter(static_cast<float>(mn[r] - pad), -std::numeric_limits<float>::max());
+        b.hi[r] = std::nextafter(static_cast<float>(mx[r] + pad), std::numeric_limits<float>::max());
+    }
+    return b;
+}
+
+void append_wide(std::vector<WideNode> &all, const WideBvh &w, uint32_t item_offset) {
+    const uint32_t base = static_cast<uint32_t>(all.size());
+    for (WideNode n : w.nodes) {
+        n.child_base += base;
+        n.item_base += item_offset;
+        all.push_back(n);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t spk_abi_version(void) { return SPK_ABI_VERSION; }
+
+spk_status spk_create(int32_t device, spk_ctx **out_ctx) {
+    if (!out_ctx) return SPK_ERR_INVALID_ARGUMENT;
+    *out_ctx = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return SPK_ERR_CUDA;
+    if (device < 0 || device >= count) return SPK_ERR_INVALID_ARGUMENT;
+    auto *ctx = new (std::nothrow) spk_ctx();
+    if (!ctx) return SPK_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    if ((e = cudaSetDevice(device)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreate(&ctx->ev_start)) != cudaSuccess || (e = cudaEventCreate(&ctx->ev_stop)) != cudaSuccess ||
+        (e = cudaMalloc(&ctx->counters, sizeof(Counters))) != cudaSuccess ||
+        (e = cudaMemset(ctx->counters, 0, sizeof(Counters))) != cudaSuccess) {
+        spk_destroy(ctx);
+        return SPK_ERR_CUDA;
+    }
+    *out_ctx = ctx;
+    return SPK_OK;
+}
+
+spk_status spk_destroy(spk_ctx *ctx) {
+    if (!ctx) return SPK_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->nodes.reset();
+    ctx->tris.reset();
+    ctx->tlas_items.reset();
+    ctx->instances.reset();
+    ctx->verts.reset();
+    ctx->faces.reset();
+    ctx->materials.reset();
+    ctx->sky.reset();
+    ctx->gcolor.reset();
+    ctx->gnormal.reset();
+    ctx->fb.reset();
+    ctx->out.reset();
+    wavefront_free(ctx->wf);
+    if (ctx->counters) cudaFree(ctx->counters);
+    for (cudaEvent_t ev : ctx->trace_events) cudaEventDestroy(ev);
+    if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
+    if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SPK_OK;
+}
+
+const char *spk_last_error(const spk_ctx *ctx) { return ctx ? ctx->error.c_str() : "null context"; }
+
+spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_meshes, const spk_instance *instances,
+                         uint32_t num_instances, const spk_material *materials, uint32_t num_materials,
+                         const spk_sky *sky) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if ((num_meshes && !meshes) || (num_instances && !instances) || (num_materials && !materials))
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "null scene array");
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    const int threads = host_threads();
+    // Validate.
+    for (uint32_t k = 0; k < num_meshes; ++k) {
+        const spk_mesh &m = meshes[k];
+        if (m.num_faces && (!m.positions || !m.normals || !m.indices))
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "mesh %u: positions, normals and indices are required", k);
+        for (uint64_t f = 0; f < 3ull * m.num_faces; ++f) {
+            if (m.indices[f] >= m.num_vertices)
+                return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "mesh %u: index %u out of range", k, m.indices[f]);
+        }
+    }
+    for (uint32_t k = 0; k < num_instances; ++k) {
+        const spk_instance &in = instances[k];
+        if (in.type != SPK_PRIM_MESH && in.type != SPK_PRIM_SPHERE)
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: bad type", k);
+        if (in.type == SPK_PRIM_MESH && in.mesh_id >= num_meshes)
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: mesh_id out of range", k);
+        if (in.material_id >= num_materials)
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: material_id out of range", k);
+    }
+    if (sky && sky->mode == SPK_SKY_CUBE && (!sky->cube_rgba || sky->cube_size == 0))
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "cube sky without texels");
+
+    // BLAS per mesh: binned SAH BVH2 (<= 3 triangles per leaf) collapsed to 8-wide nodes.
+    std::vector<WideNode> all_nodes;
+    std::vector<float4> tri_recs;
+    std::vector<uint32_t> blas_root(num_meshes, kInvalid);
+    std::vector<uint32_t> vert_base(num_meshes, 0), face_base(num_meshes, 0);
+    std::vector<float4> vert_recs;
+    std::vector<uint4> face_recs;
+    std::vector<std::array<double, 6>> mesh_bounds(num_meshes);
+    for (uint32_t k = 0; k < num_meshes; ++k) {
+        const spk_mesh &m = meshes[k];
+        vert_base[k] = static_cast<uint32_t>(vert_recs.size() / 3);
+        face_base[k] = static_cast<uint32_t>(face_recs.size());
+        for (uint32_t v = 0; v < m.num_vertices; ++v) {
+            const float *n = m.normals + 3 * v;
+            const float t[4] = {m.tangents ? m.tangents[4 * v] : 1.f, m.tangents ? m.tangents[4 * v + 1] : 0.f,
+                                m.tangents ? m.tangents[4 * v + 2] : 0.f, m.tangents ? m.tangents[4 * v + 3] : 1.f};
+            const float uv[2] = {m.uvs ? m.uvs[2 * v] : 0.f, m.uvs ? m.uvs[2 * v + 1] : 0.f};
+            vert_recs.push_back(make_float4(n[0], n[1], n[2], t[0]));
+            vert_recs.push_back(make_float4(t[1], t[2], t[3], uv[0]));
+            vert_recs.push_back(make_float4(uv[1], 0.f, 0.f, 0.f));
+        }
+        for (uint32_t f = 0; f < m.num_faces; ++f)
+            face_recs.push_back(make_uint4(m.indices[3 * f], m.indices[3 * f + 1], m.indices[3 * f + 2], 0u));
+        auto &mb = mesh_bounds[k];
+        mb = {std::numeric_limits<double>::max(), std::numeric_limits<double>::max(),
+              std::numeric_limits<double>::max(), -std::numeric_limits<double>::max(),
+              -std::numeric_limits<double>::max(), -std::numeric_limits<double>::max()};
+        if (m.num_faces == 0) continue;
+        std::vector<BuildBox> boxes(m.num_faces);
+        for (uint32_t f = 0; f < m.num_faces; ++f) {
+            BuildBox b;
+            for (int a = 0; a < 3; ++a) {
+                b.lo[a] = std::numeric_limits<float>::max();
+                b.hi[a] = -std::numeric_limits<float>::max();
+            }
+            for (int c = 0; c < 3; ++c) {
+                const float *p = m.positions + 3 * m.indices[3 * f + c];
+                for (int a = 0; a < 3; ++a) {
+                    b.lo[a] = std::min(b.lo[a], p[a]);
+                    b.hi[a] = std::max(b.hi[a], p[a]);
+                    mb[a] = std::min(mb[a], static_cast<double>(p[a]));
+                    mb[3 + a] = std::max(mb[3 + a], static_cast<double>(p[a]));
+                }
+            }
+            boxes[f] = b;
+        }
+        const Bvh2 b2 = build_bvh2(boxes, 3, threads);
+        const WideBvh wide = collapse_wide(b2);
+        const uint32_t tri_offset = static_cast<uint32_t>(tri_recs.size() / 3);
+        blas_root[k] = static_cast<uint32_t>(all_nodes.size());
+        append_wide(all_nodes, wide, tri_offset);
+        for (uint32_t face : wide.items) {
+            const float *p0 = m.positions + 3 * m.indices[3 * face];
+            const float *p1 = m.positions + 3 * m.indices[3 * face + 1];
+            const float *p2 = m.positions + 3 * m.indices[3 * face + 2];
+            // BLAS::Triangle::Set: e1 = v1 - v0, e2 = v2 - v0 (MeshRenderProxy.cpp:80-86)
+            const float e1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+            const float e2[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+            uint32_t fbits = face;
+            float ff;
+            std::memcpy(&ff, &fbits, 4);
+            tri_recs.push_back(make_float4(p0[0], p0[1], p0[2], e1[0]));
+            tri_recs.push_back(make_float4(e1[1], e1[2], e2[0], e2[1]));
+            tri_recs.push_back(make_float4(e2[2], ff, 0.f, 0.f));
+        }
+    }
+    // Instances + TLAS over their world boxes (TLAS::Build, SceneRenderProxy.cpp:31-69).
+    std::vector<DevInstance> inst_recs(num_instances);
+    std::vector<BuildBox> inst_boxes(num_instances);
+    float abs_x = 0.f;
+    for (uint32_t k = 0; k < num_instances; ++k) {
+        const spk_instance &in = instances[k];
+        DevInstance &d = inst_recs[k];
+        std::memset(&d, 0, sizeof(d));
+        std::memcpy(d.m, in.transform, sizeof(d.m));
+        std::memcpy(d.minv, in.inv_transform, sizeof(d.minv));
+        d.type = in.type;
+        d.material = in.material_id;
+        d.radius = in.radius;
+        d.mesh_id = in.mesh_id;
+        if (in.type == SPK_PRIM_SPHERE) {
+            d.blas_root = kInvalid;
+            const double r = std::fabs(static_cast<double>(in.radius));
+            const double lo[3] = {-r, -r, -r}, hi[3] = {r, r, r};
+            const float tm[12] = {1, 0, 0, in.transform[3], 0, 1, 0, in.transform[7], 0, 0, 1, in.transform[11]};
+            inst_boxes[k] = world_box(tm, lo, hi);
+        } else {
+            d.blas_root = blas_root[in.mesh_id];
+            d.vert_base = vert_base[in.mesh_id];
+            d.face_base = face_base[in.mesh_id];
+            const auto &mb = mesh_bounds[in.mesh_id];
+            if (d.blas_root == kInvalid) {
+                const double z[3] = {0, 0, 0};
+                inst_boxes[k] = world_box(in.transform, z, z);
+            } else {
+                const double lo[3] = {mb[0], mb[1], mb[2]}, hi[3] = {mb[3], mb[4], mb[5]};
+                inst_boxes[k] = world_box(in.transform, lo, hi);
+            }
+        }
+        abs_x = std::max(abs_x, std::max(std::fabs(inst_boxes[k].lo[0]), std::fabs(inst_boxes[k].hi[0])));
+    }
+    uint32_t tlas_root = kInvalid;
+    std::vector<uint32_t> tlas_items;
+    if (num_instances > 0) {
+        const Bvh2 b2 = build_bvh2(inst_boxes, 3, threads);
+        const WideBvh wide = collapse_wide(b2);
+        tlas_root = static_cast<uint32_t>(all_nodes.size());
+        append_wide(all_nodes, wide, 0);
+        tlas_items = wide.items;
+    }
+    // Materials; the emissive test is SamplePixel's `emissive_color.norm() > Eps` (CPURenderer.cpp:286-287).
+    std::vector<DevMaterial> mat_recs(num_materials);
+    for (uint32_t k = 0; k < num_materials; ++k) {
+        const spk_material &s = materials[k];
+        DevMaterial &d = mat_recs[k];
+        std::memset(&d, 0, sizeof(d));
+        for (int c = 0; c < 3; ++c) {
+            d.base[c] = s.base_color[c];
+            d.emissive[c] = s.emissive[c];
+        }
+        d.type = s.type;
+        const volatile float e0 = s.emissive[0] * s.emissive[0], e1 = s.emissive[1] * s.emissive[1],
+                             e2 = s.emissive[2] * s.emissive[2];
+        const volatile float sn = e0 + (e1 + e2);
+        d.is_emissive = std::sqrt(static_cast<float>(sn)) > kEps ? 1u : 0u;
+        d.metallic = s.metallic;
+        d.roughness = s.roughness;
+        d.eta = s.eta;
+    }
+    std::vector<float4> cube;
+    if (sky && sky->mode == SPK_SKY_CUBE) {
+        const size_t n = 6ull * sky->cube_size * sky->cube_size;
+        cube.resize(n);
+        std::memcpy(cube.data(), sky->cube_rgba, n * sizeof(float4));
+    }
+    // Upload.
+    ctx->has_scene = false;
+    cudaError_t e;
+    static_assert(sizeof(WideNode) == 5 * sizeof(uint4), "node size");
+    if ((e = upload(ctx->nodes, reinterpret_cast<const uint4 *>(all_nodes.data()), all_nodes.size() * 5,
+                    ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->tris, tri_recs.data(), tri_recs.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->tlas_items, tlas_items.data(), tlas_items.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->instances, inst_recs.data(), inst_recs.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->verts, vert_recs.data(), vert_recs.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->faces, face_recs.data(), face_recs.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->materials, mat_recs.data(), mat_recs.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->sky, cube.data(), cube.size(), ctx->stream)) != cudaSuccess) {
+        return cuda_fail(ctx, e, "scene upload");
+    }
+    DevScene &S = ctx->scene;
+    S.nodes = ctx->nodes.ptr;
+    S.tris = ctx->tris.ptr;
+    S.tlas_items = ctx->tlas_items.ptr;
+    S.instances = ctx->instances.ptr;
+    S.verts = ctx->verts.ptr;
+    S.faces = ctx->faces.ptr;
+    S.materials = ctx->materials.ptr;
+    S.sky_cube = ctx->sky.ptr;
+    S.tlas_root = tlas_root;
+    S.sky_mode = sky ? sky->mode : SPK_SKY_NONE;
+    S.sky_size = sky ? sky->cube_size : 0;
+    for (int c = 0; c < 3; ++c) S.sky_color[c] = sky ? sky->color[c] : 0.f;
+    S.scene_abs_x = abs_x;
+    ctx->bvh_nodes = static_cast<uint32_t>(all_nodes.size());
+    ctx->bvh_bytes = all_nodes.size() * sizeof(WideNode) + tri_recs.size() * sizeof(float4);
+    ctx->has_scene = true;
+    ctx->dirty = true;
+    return SPK_OK;
+}
+
+spk_status spk_set_camera(spk_ctx *ctx, const spk_camera *camera) {
+    if (!ctx || !camera) return SPK_ERR_INVALID_ARGUMENT;
+    static_assert(sizeof(DevCamera) == sizeof(spk_camera), "camera layout");
+    std::memcpy(&ctx->cam, camera, sizeof(DevCamera));
+    ctx->has_camera = true;
+    ctx->dirty = true;
+    return SPK_OK;
+}
+
+spk_status spk_camera_from_look(const float position[3], const float target[3], const float world_up[3],
+                                float vertical_fov_rad, float focus_distance, float aperture_radius, float exposure,
+                                uint32_t width, uint32_t height, spk_camera *out) {
+    if (!position || !target || !world_up || !out || width == 0 || height == 0 || !(focus_distance > 0.f))
+        return SPK_ERR_INVALID_ARGUMENT;
+    double f[3], r[3], u[3];
+    for (int k = 0; k < 3; ++k) f[k] = static_cast<double>(target[k]) - position[k];
+    double n = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    if (!(n > 0)) return SPK_ERR_INVALID_ARGUMENT;
+    for (double &x : f) x /= n;
+    r[0] = f[1] * world_up[2] - f[2] * world_up[1];
+    r[1] = f[2] * world_up[0] - f[0] * world_up[2];
+    r[2] = f[0] * world_up[1] - f[1] * world_up[0];
+    n = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    if (!(n > 0)) return SPK_ERR_INVALID_ARGUMENT;
+    for (double &x : r) x /= n;
+    u[0] = r[1] * f[2] - r[2] * f[1];
+    u[1] = r[2] * f[0] - r[0] * f[2];
+    u[2] = r[0] * f[1] - r[1] * f[0];
+    spk_camera c{};
+    for (int k = 0; k < 3; ++k) {
+        c.position[k] = position[k];
+        c.front[k] = static_cast<float>(f[k]);
+        c.right[k] = static_cast<float>(r[k]);
+        c.up[k] = static_cast<float>(u[k]);
+    }
+    // CameraRenderProxy::Update: h = tan(fov / 2); height = 2 h focus; width = aspect * height.
+    const volatile float h = std::tan(vertical_fov_rad / 2.f);
+    const volatile float fh = 2.f * h * focus_distance;
+    const volatile float aspect = static_cast<float>(width) / static_cast<float>(height);
+    const volatile float fw = aspect * fh;
+    for (int k = 0; k < 3; ++k) {
+        c.max_u[k] = c.right[k] * fw;
+        c.max_v[k] = c.up[k] * fh;
+        const volatile float a = c.position[k] + c.front[k] * focus_distance;
+        const volatile float b = a - c.max_u[k] * .5f;
+        c.lower_left[k] = b - c.max_v[k] * .5f;
+    }
+    c.aperture_radius = aperture_radius;
+    c.exposure = exposure;
+    c.far_plane = 1000.f;
+    *out = c;
+    return SPK_OK;
+}
+
+spk_status spk_set_config(spk_ctx *ctx, const spk_config *config) {
+    if (!ctx || !config) return SPK_ERR_INVALID_ARGUMENT;
+    if (config->width < 2 || config->height < 2)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "resolution must be at least 2x2");
+    if (static_cast<uint64_t>(config->width) * config->height > (1ull << 31))
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "resolution too large");
+    if (config->rng > SPK_RNG_XOSHIRO256SS) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "unknown rng policy");
+    if (config->debug_mode != SPK_DEBUG_COLOR) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "only debug_mode 0 (color)");
+    if (config->kernel > SPK_KERNEL_WAVEFRONT) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "unknown kernel schedule");
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    const size_t n = static_cast<size_t>(config->width) * config->height;
+    cudaError_t e;
+    if ((e = alloc(ctx->gcolor, n)) != cudaSuccess || (e = alloc(ctx->gnormal, n)) != cudaSuccess ||
+        (e = alloc(ctx->fb, n)) != cudaSuccess || (e = alloc(ctx->out, n)) != cudaSuccess) {
+        ctx->has_config = false;
+        return cuda_fail(ctx, e, "frame buffer allocation");
+    }
+    if ((e = cudaMemsetAsync(ctx->gnormal.ptr, 0, n * sizeof(float4), ctx->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(ctx->fb.ptr, 0, n * sizeof(float4), ctx->stream)) != cudaSuccess) {
+        return cuda_fail(ctx, e, "frame buffer clear");
+    }
+    if ((e = wavefront_alloc(ctx->wf, static_cast<uint32_t>(n))) != cudaSuccess) {
+        ctx->has_config = false;
+        return cuda_fail(ctx, e, "path state allocation");
+    }
+    ctx->cfg = *config;
+    // sub_pixel_count_ = lround(sqrt(float(spp))); actual spp = its square (CPURenderer.cpp:102-104)
+    const auto sub = static_cast<unsigned>(std::lround(std::sqrt(static_cast<float>(config->spp))));
+    ctx->spp_eff = sub * sub;
+    ctx->has_config = true;
+    ctx->dirty = true;
+    return SPK_OK;
+}
+
+static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
+    FrameBuffers fbuf{ctx->gcolor.ptr, ctx->gnormal.ptr, ctx->fb.ptr, ctx->out.ptr, ctx->cfg.width, ctx->cfg.height};
+    cudaError_t e;
+    for (cudaEvent_t ev : ctx->trace_events) cudaEventDestroy(ev);
+    ctx->trace_events.clear();
+    ctx->launches_in_call = 0;
+    if ((e = cudaMemsetAsync(ctx->counters, 0, sizeof(Counters), ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "counter reset");
+    if ((e = cudaEventRecord(ctx->ev_start, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "event");
+    const bool wavefront = ctx->cfg.kernel == SPK_KERNEL_WAVEFRONT;
+    for (uint32_t f = 0; f < num_frames; ++f) {
+        // CameraRenderProxy::Update (CameraRenderProxy.cpp:66-75)
+        if (ctx->dirty) {
+            ctx->cumulated = 0;
+            ctx->pending = 0;
+        }
+        ctx->cumulated = std::min(ctx->cfg.max_spp, ctx->cumulated + ctx->pending);
+        ctx->pending = 0;
+        // CPURenderer::Render: clear on dirty (CPURenderer.cpp:128-137)
+        if (ctx->dirty) {
+            if ((e = cudaMemsetAsync(ctx->fb.ptr, 0, ctx->fb.count * sizeof(float4), ctx->stream)) != cudaSuccess)
+                return cuda_fail(ctx, e, "frame buffer clear");
+            ctx->dirty = false;
+            ctx->dispatched = 0;
+        }
+        RenderParams p{ctx->dispatched, ctx->cfg.bounce, ctx->cfg.rng, ctx->cfg.seed, ctx->cfg.spatial_denoise,
+                       ctx->cfg.enable_nee};
+        cudaEvent_t t0, t1;
+        cudaEventCreate(&t0);
+        cudaEventCreate(&t1);
+        ctx->trace_events.push_back(t0);
+        ctx->trace_events.push_back(t1);
+        cudaEventRecord(t0, ctx->stream);
+        uint32_t launches = 0;
+        if (wavefront) {
+            e = launch_render_wavefront(ctx->scene, ctx->cam, fbuf, p, ctx->counters, ctx->wf, ctx->num_sms,
+                                        ctx->stream, &launches);
+        } else {
+            e = launch_render_mega(ctx->scene, ctx->cam, fbuf, p, ctx->counters, ctx->stream);
+            launches = 1;
+        }
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "base pass launch");
+        cudaEventRecord(t1, ctx->stream);
+        ctx->launches_in_call += launches;
+        // DenoisePass weight: cumulated / (cumulated + actual spp) (CPURenderer.cpp:530-532)
+        const float mavg = static_cast<float>(ctx->cumulated) / static_cast<float>(ctx->cumulated + ctx->spp_eff);
+        if ((e = launch_resolve(fbuf, mavg, ctx->cam.exposure, ctx->cfg.spatial_denoise, ctx->stream)) != cudaSuccess)
+            return cuda_fail(ctx, e, "resolve launch");
+        ctx->launches_in_call += 1;
+        ctx->dispatched += ctx->spp_eff;
+        ctx->pending += ctx->spp_eff;
+    }
+    if ((e = cudaEventRecord(ctx->ev_stop, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "event");
+    ctx->last = spk_stats{};
+    ctx->last.paths = static_cast<uint64_t>(num_frames) * ctx->cfg.width * ctx->cfg.height;
+    ctx->stats_pending = true;
+    return SPK_OK;
+}
+
+spk_status spk_render(spk_ctx *ctx, uint32_t num_frames) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene || !ctx->has_config || !ctx->has_camera)
+        return fail(ctx, SPK_ERR_NOT_READY, "render needs spk_set_scene, spk_set_config and spk_set_camera first");
+    cudaSetDevice(ctx->device);
+    return render_impl(ctx, num_frames);
+}
+
+spk_status spk_read_framebuffer(spk_ctx *ctx, float *hdr_rgba, uint16_t *rgba16f) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "no frame buffer");
+    cudaSetDevice(ctx->device);
+    cudaError_t e;
+    if (hdr_rgba &&
+        (e = cudaMemcpyAsync(hdr_rgba, ctx->fb.ptr, ctx->fb.count * sizeof(float4), cudaMemcpyDeviceToHost,
+                             ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "frame buffer read");
+    if (rgba16f &&
+        (e = cudaMemcpyAsync(rgba16f, ctx->out.ptr, ctx->out.count * sizeof(ushort4), cudaMemcpyDeviceToHost,
+                             ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "output image read");
+    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
+    return SPK_OK;
+}
+
+spk_status spk_framebuffer_device(spk_ctx *ctx, void **hdr_rgba, void **rgba16f) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "no frame buffer");
+    if (hdr_rgba) *hdr_rgba = ctx->fb.ptr;
+    if (rgba16f) *rgba16f = ctx->out.ptr;
+    return SPK_OK;
+}
+
+spk_status spk_sample_counts(const spk_ctx *ctx, uint32_t *cumulated, uint32_t *dispatched) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (cumulated) *cumulated = ctx->cumulated;
+    if (dispatched) *dispatched = ctx->dispatched;
+    return SPK_OK;
+}
+
+int32_t spk_is_converged(const spk_ctx *ctx) {
+    return ctx && ctx->has_config && ctx->cumulated >= ctx->cfg.max_spp ? 1 : 0;
+}
+
+static spk_status trace_impl(spk_ctx *ctx, const void *d_rays, uint64_t num_rays, void *d_hits, int32_t any_hit) {
+    for (cudaEvent_t ev : ctx->trace_events) cudaEventDestroy(ev);
+    ctx->trace_events.clear();
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(ctx->counters, 0, sizeof(Counters), ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "counter reset");
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    ctx->trace_events.push_back(t0);
+    ctx->trace_events.push_back(t1);
+    cudaEventRecord(ctx->ev_start, ctx->stream);
+    cudaEventRecord(t0, ctx->stream);
+    e = launch_trace(ctx->scene, static_cast<const float *>(d_rays), num_rays, d_hits,
+                     any_hit ? kTraceAnyRef : kTraceClosest, ctx->counters, ctx->num_sms, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "trace launch");
+    cudaEventRecord(t1, ctx->stream);
+    cudaEventRecord(ctx->ev_stop, ctx->stream);
+    ctx->launches_in_call = 1;
+    ctx->last = spk_stats{};
+    ctx->stats_pending = true;
+    return SPK_OK;
+}
+
+spk_status spk_trace_device(spk_ctx *ctx, const void *d_rays, uint64_t num_rays, void *d_hits, int32_t any_hit) {
+    if (!ctx || (num_rays && (!d_rays || !d_hits))) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, SPK_ERR_NOT_READY, "trace needs spk_set_scene first");
+    cudaSetDevice(ctx->device);
+    return trace_impl(ctx, d_rays, num_rays, d_hits, any_hit);
+}
+
+spk_status spk_trace(spk_ctx *ctx, const spk_ray *rays, uint64_t num_rays, spk_hit *hits, int32_t any_hit) {
+    if (!ctx || (num_rays && (!rays || !hits))) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, SPK_ERR_NOT_READY, "trace needs spk_set_scene first");
+    cudaSetDevice(ctx->device);
+    if (num_rays == 0) return SPK_OK;
+    void *d_rays = nullptr, *d_hits = nullptr;
+    cudaError_t e;
+    if ((e = cudaMalloc(&d_rays, num_rays * sizeof(spk_ray))) != cudaSuccess) return cuda_fail(ctx, e, "ray buffer");
+    if ((e = cudaMalloc(&d_hits, num_rays * sizeof(spk_hit))) != cudaSuccess) {
+        cudaFree(d_rays);
+        return cuda_fail(ctx, e, "hit buffer");
+    }
+    spk_status st = SPK_OK;
+    if ((e = cudaMemcpyAsync(d_rays, rays, num_rays * sizeof(spk_ray), cudaMemcpyHostToDevice, ctx->stream)) !=
+        cudaSuccess) {
+        st = cuda_fail(ctx, e, "ray upload");
+    } else if ((st = trace_impl(ctx, d_rays, num_rays, d_hits, any_hit)) == SPK_OK) {
+        if ((e = cudaMemcpyAsync(hits, d_hits, num_rays * sizeof(spk_hit), cudaMemcpyDeviceToHost, ctx->stream)) !=
+                cudaSuccess ||
+            (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {
+            st = cuda_fail(ctx, e, "hit download");
+        }
+    }
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(d_rays);
+    cudaFree(d_hits);
+    return st;
+}
+
+spk_status spk_synchronize(spk_ctx *ctx) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? SPK_OK : cuda_fail(ctx, e, "synchronize");
+}
+
+spk_status spk_get_stats(spk_ctx *ctx, spk_stats *out) {
+    if (!ctx || !out) return SPK_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    if (ctx->stats_pending) {
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
+        Counters c{};
+        if ((e = cudaMemcpy(&c, ctx->counters, sizeof(Counters), cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return cuda_fail(ctx, e, "counter read");
+        ctx->last.extension_rays = c.extension_rays;
+        ctx->last.shadow_rays = c.shadow_rays;
+        ctx->last.error_flags = c.error_flags;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop);
+        ctx->last.device_ms = ms;
+        float tms = 0.f;
+        for (size_t k = 0; k + 1 < ctx->trace_events.size(); k += 2) {
+            float x = 0.f;
+            cudaEventElapsedTime(&x, ctx->trace_events[k], ctx->trace_events[k + 1]);
+            tms += x;
+        }
+        ctx->last.trace_kernel_ms = tms;
+        ctx->last.trace_launches = static_cast<uint32_t>(ctx->trace_events.size() / 2);
+        ctx->last.kernel_launches = ctx->launches_in_call;
+        ctx->stats_pending = false;
+    }
+    ctx->last.bvh_nodes = ctx->bvh_nodes;
+    ctx->last.bvh_bytes = ctx->bvh_bytes;
+    *out = ctx->last;
+    return SPK_OK;
+}
+
+}  // extern "C"

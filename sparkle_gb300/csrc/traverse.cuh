@@ -1,0 +1,253 @@
+// traverse.cuh -- two-level walk of the 8-wide quantised BVH (TLAS over instances, one BLAS per mesh).
+//
+// Semantics follow SceneRenderProxy::Intersect<AnyHit> (SceneRenderProxy.cpp:82-126) over
+// MeshRenderProxy's BLAS (MeshRenderProxy.cpp:94-194) and SphereRenderProxy (SphereRenderProxy.cpp:5-38):
+//  * closest hit: a triangle is accepted when Möller–Trumbore passes in local space and its world t,
+//    computed the reference's way from the x component only (Ray::InverseAt, Ray.h:43-47), satisfies
+//    0 < world_t < best (strict, so the first of equal t is kept);
+//  * any hit (reference semantics): the first Möller–Trumbore pass (local t > Eps) or sphere with a
+//    non-negative discriminant ends the walk (the reference does not test the sphere's t sign);
+//  * occlusion (for next-event estimation): a hit with Eps < t < tmax ends the walk.
+// Differences from the reference walk that cannot change a closest hit: the reference never lowers the
+// ray's tmax (every box along the ray is visited); this walk prunes boxes that start beyond the current
+// best t plus a bound on the x-only world-t rounding error, and visits children in an octant order.
+// Only which of two hits with bit-identical t wins can differ (ties are order dependent).
+#pragma once
+
+#include "device_scene.cuh"
+
+namespace spk {
+
+enum : int { kTraceClosest = 0, kTraceAnyRef = 1, kTraceOcclusion = 2 };
+enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOverflow = 4u };
+
+constexpr int kStackSize = 48;
+constexpr uint32_t kMaxIterations = 1u << 20;
+
+struct TraceResult {
+    float t, u, v;
+    uint32_t inst;  // caller instance index, kInvalid on a miss
+    uint32_t face;  // original face index, kInvalid for spheres and misses
+};
+
+struct LevelRay {
+    f3 o, d, inv;
+    uint32_t oct;  // bit k set when direction component k is negative
+};
+
+// bvh v2 safe_inverse: |x| <= FLT_EPSILON maps to +-FLT_MAX.
+__device__ __forceinline__ float safe_inverse(float x) {
+    return fabsf(x) <= 1.1920928955078125e-07f ? copysignf(kFltMax, x) : 1.f / x;
+}
+
+__device__ __forceinline__ void setup_level(LevelRay &r, f3 o, f3 d) {
+    r.o = o;
+    r.d = d;
+    r.inv = mk3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
+    r.oct = (signbit(d.x) ? 1u : 0u) | (signbit(d.y) ? 2u : 0u) | (signbit(d.z) ? 4u : 0u);
+}
+
+// Upper bound on the t a box may start at and still hold a hit closer than `best` (in world-t terms).
+__device__ __forceinline__ float prune_limit(float best, f3 wo, f3 wd, float scene_abs_x) {
+    if (!(best < kFltMax)) return kFltMax;
+    const float ax = fabsf(wd.x);
+    const float slack = ax > 0.f ? (fabsf(wo.x) + scene_abs_x) * 0x1p-18f / ax : kFltMax;
+    const float lim = best * (1.f + 0x1p-14f) + slack;
+    return isfinite(lim) ? lim : kFltMax;
+}
+
+// Slab test of the 8 children of one wide node; returns the next node group (inner children, permuted
+// slot bits 24..31 + imask in bits 0..7) and triangle group (leaf items, bits 0..23).
+__device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint32_t idx, const LevelRay &r,
+                                           float tmax, uint2 &ngroup, uint2 &tgroup) {
+    const uint4 *np = nodes + static_cast<size_t>(idx) * 5;
+    const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
+    const float sx = __uint_as_float((n0.w & 0xFFu) << 23);
+    const float sy = __uint_as_float(((n0.w >> 8) & 0xFFu) << 23);
+    const float sz = __uint_as_float(((n0.w >> 16) & 0xFFu) << 23);
+    const float ax = sx * r.inv.x, ay = sy * r.inv.y, az = sz * r.inv.z;
+    const float ox = (__uint_as_float(n0.x) - r.o.x) * r.inv.x;
+    const float oy = (__uint_as_float(n0.y) - r.o.y) * r.inv.y;
+    const float oz = (__uint_as_float(n0.z) - r.o.z) * r.inv.z;
+    uint32_t hitmask = 0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t meta4 = h ? n1.w : n1.z;
+        const uint32_t lox = h ? n2.y : n2.x, loy = h ? n2.w : n2.z, loz = h ? n3.y : n3.x;
+        const uint32_t hix = h ? n3.w : n3.z, hiy = h ? n4.y : n4.x, hiz = h ? n4.w : n4.z;
+        const uint32_t nx = (r.oct & 1u) ? hix : lox, fx = (r.oct & 1u) ? lox : hix;
+        const uint32_t ny = (r.oct & 2u) ? hiy : loy, fy = (r.oct & 2u) ? loy : hiy;
+        const uint32_t nz = (r.oct & 4u) ? hiz : loz, fz = (r.oct & 4u) ? loz : hiz;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const uint32_t m = (meta4 >> (8 * c)) & 0xFFu;
+            const float tnx = fmaf(static_cast<float>((nx >> (8 * c)) & 0xFFu), ax, ox);
+            const float tny = fmaf(static_cast<float>((ny >> (8 * c)) & 0xFFu), ay, oy);
+            const float tnz = fmaf(static_cast<float>((nz >> (8 * c)) & 0xFFu), az, oz);
+            const float tfx = fmaf(static_cast<float>((fx >> (8 * c)) & 0xFFu), ax, ox);
+            const float tfy = fmaf(static_cast<float>((fy >> (8 * c)) & 0xFFu), ay, oy);
+            const float tfz = fmaf(static_cast<float>((fz >> (8 * c)) & 0xFFu), az, oz);
+            const float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.f));
+            const float t1 = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+            if (m != 0u && t0 <= t1) {
+                uint32_t bit = m & 0x1Fu;
+                if ((m & 0x18u) == 0x18u) bit ^= r.oct;
+                hitmask |= ((m >> 5) & 7u) << bit;
+            }
+        }
+    }
+    ngroup = make_uint2(n1.x, (hitmask & 0xFF000000u) | (n0.w >> 24));
+    tgroup = make_uint2(n1.y, hitmask & 0x00FFFFFFu);
+}
+
+template <int kMode>
+__device__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd, float tmax_occl, uint32_t &err) {
+    TraceResult best{kFltMax, 0.f, 0.f, kInvalid, kInvalid};
+    if (S.tlas_root == kInvalid) return best;
+    LevelRay ray;
+    setup_level(ray, wo, wd);
+    float tmax_box = (kMode == kTraceOcclusion) ? tmax_occl : kFltMax;
+    uint2 stack[kStackSize];
+    int sp = 0;
+    uint2 ngroup = make_uint2(S.tlas_root, 1u << 24);
+    uint2 tgroup = make_uint2(0u, 0u);
+    bool in_blas = false;
+    int blas_sp = 0;
+    uint32_t cur_inst = 0;
+    uint32_t iter = 0;
+    for (;;) {
+        if (++iter > kMaxIterations) {
+            err |= kErrIterationBudget;
+            break;
+        }
+        if (ngroup.y > 0x00FFFFFFu) {
+            const uint32_t bit = __ffs(ngroup.y >> 24) - 1;
+            ngroup.y &= ~(1u << (bit + 24));
+            const uint32_t slot = bit ^ ray.oct;
+            const uint32_t node_idx = ngroup.x + __popc(ngroup.y & 0xFFu & ((1u << slot) - 1u));
+            if (ngroup.y > 0x00FFFFFFu) {
+                if (sp < kStackSize) {
+                    stack[sp++] = ngroup;
+                } else {
+                    err |= kErrStackOverflow;
+                }
+            }
+            visit_node(S.nodes, node_idx, ray, tmax_box, ngroup, tgroup);
+        } else {
+            tgroup = ngroup;
+            ngroup = make_uint2(0u, 0u);
+        }
+        while (tgroup.y != 0u) {
+            const uint32_t k = __ffs(tgroup.y) - 1;
+            tgroup.y &= tgroup.y - 1u;
+            const uint32_t idx = tgroup.x + k;
+            if (in_blas) {
+                // Möller–Trumbore (MeshRenderProxy.cpp:128-194) in the instance's local space.
+                const float4 *tp = S.tris + static_cast<size_t>(idx) * 3;
+                const float4 a4 = __ldg(tp), b4 = __ldg(tp + 1), c4 = __ldg(tp + 2);
+                const f3 p0 = mk3(a4.x, a4.y, a4.z), e1 = mk3(a4.w, b4.x, b4.y), e2 = mk3(b4.z, b4.w, c4.x);
+                const f3 h = cross(ray.d, e2);
+                const float det = dot3(e1, h);
+                if (fabsf(det) < kEps) continue;
+                const f3 s = ray.o - p0;
+                const float f = 1.f / det;
+                const float u = f * dot3(s, h);
+                if (u < 0.f || u > 1.f) continue;
+                const f3 q = cross(s, e1);
+                const float v = f * dot3(ray.d, q);
+                if (v < 0.f || u + v > 1.f) continue;
+                const float t = f * dot3(e2, q);
+                if (!(t > kEps)) continue;
+                if (kMode == kTraceAnyRef) {
+                    best.inst = cur_inst;
+                    return best;
+                }
+                if (kMode == kTraceOcclusion) {
+                    if (t < tmax_occl) {
+                        best.inst = cur_inst;
+                        return best;
+                    }
+                    continue;
+                }
+                const float *M = S.instances[cur_inst].m;
+                const f3 wp = xform_point(M, ray.o + ray.d * t);
+                const float wt = (wp.x - wo.x) / wd.x;
+                if (wt > 0.f && wt < best.t) {
+                    best.t = wt;
+                    best.u = u;
+                    best.v = v;
+                    best.inst = cur_inst;
+                    best.face = __float_as_uint(c4.y);
+                    tmax_box = prune_limit(best.t, wo, wd, S.scene_abs_x);
+                }
+            } else {
+                const uint32_t inst = __ldg(S.tlas_items + idx);
+                const DevInstance &I = S.instances[inst];
+                if (I.type == 1u) {
+                    // SphereRenderProxy::IntersectInternal (SphereRenderProxy.cpp:5-38), world space.
+                    const f3 center = mk3(I.m[3], I.m[7], I.m[11]);
+                    const f3 co = wo - center;
+                    const float half_b = dot3(wd, co);
+                    const float c = sqnorm(co) - I.radius * I.radius;
+                    const float disc = half_b * half_b - 1.f * c;
+                    if (disc < 0.f) continue;
+                    if (kMode == kTraceAnyRef) {
+                        best.inst = inst;
+                        return best;
+                    }
+                    const float sq = sqrtf(disc);
+                    const float t = (-half_b + (c >= 0.f ? -sq : sq)) / 1.f;
+                    if (kMode == kTraceOcclusion) {
+                        if (t > kEps && t < tmax_occl) {
+                            best.inst = inst;
+                            return best;
+                        }
+                        continue;
+                    }
+                    if (t > 0.f && t < best.t) {
+                        best.t = t;
+                        best.u = 0.f;
+                        best.v = 0.f;
+                        best.inst = inst;
+                        best.face = kInvalid;
+                        tmax_box = prune_limit(best.t, wo, wd, S.scene_abs_x);
+                    }
+                } else if (I.blas_root != kInvalid) {
+                    // Enter the BLAS: park the rest of this TLAS level on the stack.
+                    if (tgroup.y != 0u) {
+                        if (sp < kStackSize) {
+                            stack[sp++] = tgroup;
+                        } else {
+                            err |= kErrStackOverflow;
+                        }
+                    }
+                    if (ngroup.y > 0x00FFFFFFu) {
+                        if (sp < kStackSize) {
+                            stack[sp++] = ngroup;
+                        } else {
+                            err |= kErrStackOverflow;
+                        }
+                    }
+                    blas_sp = sp;
+                    in_blas = true;
+                    cur_inst = inst;
+                    setup_level(ray, xform_point(I.minv, wo), xform_dir(I.minv, wd));
+                    ngroup = make_uint2(I.blas_root, 1u << 24);
+                    tgroup.y = 0u;
+                    break;
+                }
+            }
+        }
+        if (ngroup.y <= 0x00FFFFFFu) {
+            if (in_blas && sp == blas_sp) {
+                in_blas = false;
+                setup_level(ray, wo, wd);
+            }
+            if (sp == 0) break;
+            ngroup = stack[--sp];
+        }
+    }
+    return best;
+}
+
+}  // namespace spk

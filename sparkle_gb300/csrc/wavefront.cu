@@ -1,0 +1,240 @@
+// wavefront.cu -- stage kernels of the wavefront BasePass (see wavefront.cuh).
+//
+// Compiled with -fmad=false like kernels.cu so every path computes bit-identically to the one-kernel form.
+#include "wavefront.cuh"
+
+namespace spk {
+namespace {
+
+// queue_counters slots
+constexpr int kLen0 = 0;     // length of queue 0
+constexpr int kLen1 = 1;     // length of queue 1
+constexpr int kCursor = 2;   // pop cursor of the running persistent stage
+
+template <int kKind>
+__device__ __forceinline__ void load_rng(const uint4 *rng, uint32_t pid, Rng &r) {
+    const uint4 a = rng[2 * static_cast<size_t>(pid)];
+    r.s[0] = a.x;
+    r.s[1] = a.y;
+    r.s[2] = a.z;
+    r.s[3] = a.w;
+    if (kKind == 1) {
+        const uint4 b = rng[2 * static_cast<size_t>(pid) + 1];
+        r.s[4] = b.x;
+        r.s[5] = b.y;
+        r.s[6] = b.z;
+        r.s[7] = b.w;
+    }
+}
+
+template <int kKind>
+__device__ __forceinline__ void store_rng(uint4 *rng, uint32_t pid, const Rng &r) {
+    rng[2 * static_cast<size_t>(pid)] = make_uint4(r.s[0], r.s[1], r.s[2], r.s[3]);
+    if (kKind == 1) rng[2 * static_cast<size_t>(pid) + 1] = make_uint4(r.s[4], r.s[5], r.s[6], r.s[7]);
+}
+
+// Warp-aggregated append to a queue: one atomic per warp.
+__device__ __forceinline__ void queue_push(uint32_t *queue, unsigned long long *len, uint32_t value, bool active) {
+    const uint32_t mask = __ballot_sync(__activemask(), active);
+    if (mask == 0) return;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t leader = __ffs(mask) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(len, static_cast<unsigned long long>(__popc(mask)));
+    base = __shfl_sync(__activemask(), base, leader);
+    if (active) queue[base + __popc(mask & ((1u << lane) - 1u))] = value;
+}
+
+template <int kKind>
+__global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers fb, RenderParams p, WavefrontState s,
+                                                     Counters *counters) {
+    const uint32_t i = blockIdx.x * 16u + (threadIdx.x & 15u);
+    const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 4);
+    if (i >= fb.width || j >= fb.height) return;
+    const uint32_t pid = j * fb.width + i;
+    Rng rng;
+    rng_seed_pixel<kKind>(rng, p.seed, i, j, fb.width, fb.height, p.frame_seed);
+    const float pw = 1.f / static_cast<float>(fb.width - 1);
+    const float ph = 1.f / static_cast<float>(fb.height - 1);
+    const float u = (static_cast<float>(i) + rng_unit<kKind>(rng)) * pw;
+    const float v = (static_cast<float>(j) + rng_unit<kKind>(rng)) * ph;
+    f3 o, d;
+    camera_ray<kKind>(cam, rng, u, v, o, d);
+    s.ray_o[pid] = make_float4(o.x, o.y, o.z, 0.f);
+    s.ray_d[pid] = make_float4(d.x, d.y, d.z, 0.f);
+    s.thr[pid] = make_float4(1.f, 1.f, 1.f, 0.f);
+    s.color[pid] = make_float4(0.f, 0.f, 0.f, 1.f);
+    store_rng<kKind>(s.rng, pid, rng);
+    if (p.spatial_denoise) fb.gnormal[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
+    s.queue[0][pid] = pid;
+    if (pid == 0) counters->queue_counters[kLen0] = static_cast<unsigned long long>(fb.width) * fb.height;
+}
+
+// Extend: persistent warps pop 32-path batches and trace their closest hit.
+__global__ void __launch_bounds__(128) k_wf_extend(DevScene S, WavefrontState s, int in_queue, Counters *counters) {
+    uint32_t err = 0;
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned long long n = counters->queue_counters[in_queue];
+    const uint32_t *queue = s.queue[in_queue];
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(&counters->queue_counters[kCursor], 32ull);
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (base >= n) break;
+        const unsigned long long q = base + lane;
+        if (q < n) {
+            const uint32_t pid = queue[q];
+            const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
+            const TraceResult h = trace_ray<kTraceClosest>(S, mk3(o4.x, o4.y, o4.z), mk3(d4.x, d4.y, d4.z), kFltMax, err);
+            s.hit[pid] = make_float4(h.t, h.u, h.v, __uint_as_float(h.inst));
+            s.hit_face[pid] = h.face;
+        }
+        const uint32_t cnt = static_cast<uint32_t>(min(32ull, n - base));
+        if (lane == 0) atomicAdd(&counters->extension_rays, static_cast<unsigned long long>(cnt));
+    }
+    if (err) atomicOr(&counters->error_flags, err);
+}
+
+template <int kKind>
+__global__ void __launch_bounds__(128) k_wf_shade(DevScene S, FrameBuffers fb, RenderParams p, WavefrontState s,
+                                                  int in_queue, uint32_t bounce, Counters *counters) {
+    const unsigned long long n = counters->queue_counters[in_queue];
+    const int out_queue = in_queue ^ 1;
+    const uint32_t *queue = s.queue[in_queue];
+    for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
+         q0 += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+        const unsigned long long q = q0 + threadIdx.x;
+        bool alive = false;
+        uint32_t pid = 0;
+        if (q < n) {
+            pid = queue[q];
+            const float4 hit4 = s.hit[pid];
+            const uint32_t inst = __float_as_uint(hit4.w);
+            const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
+            const f3 o = mk3(o4.x, o4.y, o4.z), d = mk3(d4.x, d4.y, d4.z);
+            float4 c4 = s.color[pid];
+            f3 color = mk3(c4.x, c4.y, c4.z);
+            const float4 t4 = s.thr[pid];
+            f3 thr = mk3(t4.x, t4.y, t4.z);
+            float valid = c4.w;
+            if (inst == kInvalid) {
+                if (S.sky_mode != 0u) color = color + cmul(sky_eval(S, d), thr);
+            } else {
+                const TraceResult h{hit4.x, hit4.y, hit4.z, inst, s.hit_face[pid]};
+                const Surface surf = make_surface(S, h, o, d);
+                const DevMaterial mat = S.materials[surf.material];
+                if (bounce == 0 && p.spatial_denoise)
+                    fb.gnormal[pid] = make_float4(surf.normal.x, surf.normal.y, surf.normal.z, 0.f);
+                if (mat.is_emissive) {
+                    color = color + cmul(mk3(mat.emissive[0], mat.emissive[1], mat.emissive[2]), thr);
+                } else {
+                    Rng rng;
+                    load_rng<kKind>(s.rng, pid, rng);
+                    f3 next_dir;
+                    const f3 this_thr = sample_surface<kKind>(rng, mat, d, surf.normal, surf.tangent, next_dir);
+                    thr = cmul(thr, this_thr);
+                    if (sqnorm(thr) < kEps) {
+                        valid = -1.f;
+                    } else {
+                        bool survive = true;
+                        if (bounce >= 3) {
+                            float pr = max_std(thr.x, max_std(thr.y, thr.z));
+                            pr = (pr < 0.05f) ? 0.05f : (1.0f < pr) ? 1.0f : pr;
+                            if (rng_unit<kKind>(rng) > pr) {
+                                survive = false;
+                            } else {
+                                thr = mk3(thr.x / pr, thr.y / pr, thr.z / pr);
+                            }
+                        }
+                        if (survive) {
+                            const f3 no = surf.location + next_dir * kTolerance;
+                            s.ray_o[pid] = make_float4(no.x, no.y, no.z, 0.f);
+                            s.ray_d[pid] = make_float4(next_dir.x, next_dir.y, next_dir.z, 0.f);
+                            alive = true;
+                        }
+                    }
+                    store_rng<kKind>(s.rng, pid, rng);
+                    s.thr[pid] = make_float4(thr.x, thr.y, thr.z, 0.f);
+                }
+            }
+            s.color[pid] = make_float4(color.x, color.y, color.z, valid);
+        }
+        queue_push(s.queue[out_queue], &counters->queue_counters[out_queue], pid, alive && bounce + 1 < p.bounce);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_wf_finish(FrameBuffers fb, WavefrontState s) {
+    const uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pid >= fb.width * fb.height) return;
+    const float4 c = s.color[pid];
+    fb.gcolor[pid] = make_float4(min_std(c.x, kOutputLimit), min_std(c.y, kOutputLimit), min_std(c.z, kOutputLimit), c.w);
+}
+
+template <class T>
+cudaError_t dmalloc(T *&p, size_t count) {
+    return cudaMalloc(reinterpret_cast<void **>(&p), count * sizeof(T));
+}
+
+}  // namespace
+
+cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
+    wavefront_free(s);
+    cudaError_t e;
+    if ((e = dmalloc(s.ray_o, capacity)) != cudaSuccess || (e = dmalloc(s.ray_d, capacity)) != cudaSuccess ||
+        (e = dmalloc(s.thr, capacity)) != cudaSuccess || (e = dmalloc(s.color, capacity)) != cudaSuccess ||
+        (e = dmalloc(s.rng, 2 * static_cast<size_t>(capacity))) != cudaSuccess ||
+        (e = dmalloc(s.hit, capacity)) != cudaSuccess || (e = dmalloc(s.hit_face, capacity)) != cudaSuccess ||
+        (e = dmalloc(s.queue[0], capacity)) != cudaSuccess || (e = dmalloc(s.queue[1], capacity)) != cudaSuccess ||
+        (e = dmalloc(s.sort_keys, capacity)) != cudaSuccess) {
+        wavefront_free(s);
+        return e;
+    }
+    s.capacity = capacity;
+    return cudaSuccess;
+}
+
+void wavefront_free(WavefrontState &s) {
+    void *ptrs[] = {s.ray_o, s.ray_d, s.thr, s.color, s.rng, s.hit, s.hit_face, s.queue[0], s.queue[1], s.sort_keys};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    s = WavefrontState{};
+}
+
+cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
+                                    const RenderParams &p, Counters *counters, WavefrontState &s, int num_sms,
+                                    cudaStream_t stream, uint32_t *launches) {
+    uint32_t nl = 0;
+    const uint32_t npix = fbuf.width * fbuf.height;
+    if (s.capacity < npix) return cudaErrorInvalidValue;
+    cudaError_t e;
+    unsigned long long *qc = counters->queue_counters;
+    if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
+    const dim3 ggrid((fbuf.width + 15) / 16, (fbuf.height + 7) / 8);
+    if (p.rng == 0) {
+        k_wf_generate<0><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, counters);
+    } else {
+        k_wf_generate<1><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, counters);
+    }
+    ++nl;
+    const unsigned persist_blocks = static_cast<unsigned>(num_sms) * 12u;
+    const unsigned shade_blocks = static_cast<unsigned>(num_sms) * 8u;
+    for (uint32_t b = 0; b < p.bounce; ++b) {
+        const int in = static_cast<int>(b & 1u), out = in ^ 1;
+        if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
+        if ((e = cudaMemsetAsync(qc + kCursor, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
+        k_wf_extend<<<persist_blocks, 128, 0, stream>>>(scene, s, in, counters);
+        ++nl;
+        if (p.rng == 0) {
+            k_wf_shade<0><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
+        } else {
+            k_wf_shade<1><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
+        }
+        ++nl;
+    }
+    k_wf_finish<<<(npix + 255) / 256, 256, 0, stream>>>(fbuf, s);
+    ++nl;
+    if (launches) *launches = nl;
+    return cudaGetLastError();
+}
+
+}  // namespace spk

@@ -1,0 +1,148 @@
+"""Image parity of the device BasePass/DenoisePass/ToneMappingPass (spk_render through the C ABI) against the
+CPU oracle on the same scenes, cameras and per-pixel seeds.
+
+The device and the oracle draw the same random numbers in the same order and round every multiply and
+add the same way; they differ only in the last bits of cosf/sinf/powf, so a path can occasionally take
+another branch (a Fresnel or roulette coin lands on the other side). Tolerances (written in the tests):
+ * >= 90% of pixels agree to 1e-4 relative after a few frames, and the whole image has relMSE < 1e-3;
+ * the one-kernel and wavefront schedules are bit-identical to each other;
+ * converged renders (256 frames) agree to relMSE < 1e-4.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from sparkle_gb300 import abi, native, scenes
+
+from parity import rel_mse
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = native.Context(0)
+    yield c
+    c.close()
+
+
+def gpu_render(ctx, scene, camera, cfg, frames):
+    ctx.set_scene(scene)
+    ctx.set_config(cfg)
+    ctx.set_camera(camera)
+    ctx.render(frames)
+    hdr, out = ctx.framebuffer()
+    st = ctx.stats()
+    assert st["error_flags"] == 0, st
+    return hdr, out, st
+
+
+def oracle_render(scene, camera, cfg, frames, osc=None):
+    osc = osc or oracle.OracleScene(scene)
+    r = oracle.OracleRenderer(osc, cfg, camera)
+    r.render(frames, traversal=oracle.PRUNED)
+    hdr, out = r.framebuffer()
+    return hdr, out, r
+
+
+def close_fraction(a, b, rel=1e-4):
+    d = np.abs(a[..., :3] - b[..., :3])
+    ok = np.all(d <= rel * (1.0 + np.abs(b[..., :3])), axis=-1)
+    return float(ok.mean())
+
+
+@pytest.mark.parametrize("rng", [abi.SPK_RNG_XOSHIRO128P, abi.SPK_RNG_XOSHIRO256SS])
+@pytest.mark.parametrize("spatial", [False, True])
+def test_cornell_matches_oracle(ctx, cornell, rng, spatial):
+    scene, cam_args = cornell
+    W, H, frames = 64, 48, 4
+    camera = scenes.make_camera(cam_args, W, H)
+    cfg = abi.make_config(W, H, spp=1, bounce=5, spatial_denoise=spatial, rng=rng, seed=7)
+    g_hdr, g_out, st = gpu_render(ctx, scene, camera, cfg, frames)
+    o_hdr, o_out, r = oracle_render(scene, camera, cfg, frames)
+    frac = close_fraction(g_hdr, o_hdr)
+    rm = rel_mse(g_hdr, o_hdr)
+    print(f"rng={rng} spatial={spatial} close={frac:.4f} relmse={rm:.3e} rays gpu={st['extension_rays']} "
+          f"oracle={r.counts()[0]}")
+    assert frac >= 0.90
+    assert rm < 1e-3
+    assert ctx.sample_counts() == r.sample_counts()
+    # accumulated validity channel and the tonemapped alpha
+    assert np.all(g_out[..., 3] == 0x3C00)
+    ext_o = r.counts()[0]
+    assert abs(st["extension_rays"] - ext_o) <= 0.02 * ext_o
+
+
+@pytest.mark.parametrize("spatial", [False, True])
+def test_wavefront_equals_megakernel(ctx, small_terrain, spatial):
+    scene, cam_args = small_terrain
+    W, H = 96, 64
+    camera = scenes.make_camera(cam_args, W, H)
+    outs = []
+    for kernel in (abi.SPK_KERNEL_MEGAKERNEL, abi.SPK_KERNEL_WAVEFRONT):
+        cfg = abi.make_config(W, H, spp=1, bounce=8, spatial_denoise=spatial, rng=abi.SPK_RNG_XOSHIRO256SS,
+                              kernel=kernel)
+        hdr, out, st = gpu_render(ctx, scene, camera, cfg, 3)
+        outs.append((hdr, out, st["extension_rays"]))
+    assert np.array_equal(outs[0][0].view(np.uint32), outs[1][0].view(np.uint32))
+    assert np.array_equal(outs[0][1], outs[1][1])
+    assert outs[0][2] == outs[1][2]
+
+
+def test_terrain_matches_oracle(ctx, small_terrain):
+    scene, cam_args = small_terrain
+    W, H, frames = 80, 60, 2
+    camera = scenes.make_camera(cam_args, W, H)
+    cfg = abi.make_config(W, H, spp=1, bounce=8, rng=abi.SPK_RNG_XOSHIRO256SS, kernel=abi.SPK_KERNEL_WAVEFRONT)
+    g_hdr, _, _ = gpu_render(ctx, scene, camera, cfg, frames)
+    o_hdr, _, _ = oracle_render(scene, camera, cfg, frames)
+    frac = close_fraction(g_hdr, o_hdr)
+    rm = rel_mse(g_hdr, o_hdr)
+    print(f"terrain close={frac:.4f} relmse={rm:.3e}")
+    assert frac >= 0.90
+    assert rm < 1e-3
+
+
+def test_converged_cornell_relmse(ctx, cornell):
+    scene, cam_args = cornell
+    W, H, frames = 48, 48, 256
+    camera = scenes.make_camera(cam_args, W, H)
+    cfg = abi.make_config(W, H, spp=1, bounce=5, rng=abi.SPK_RNG_XOSHIRO256SS, kernel=abi.SPK_KERNEL_WAVEFRONT)
+    g_hdr, _, _ = gpu_render(ctx, scene, camera, cfg, frames)
+    o_hdr, _, _ = oracle_render(scene, camera, cfg, frames)
+    rm = rel_mse(g_hdr, o_hdr)
+    print(f"converged relmse={rm:.3e}")
+    assert rm < 1e-4
+
+
+def test_accumulation_cap_and_reset(ctx, cornell):
+    """max_spp caps the cumulated count (then the lerp becomes an EMA); a camera change clears."""
+    scene, cam_args = cornell
+    W, H = 16, 16
+    camera = scenes.make_camera(cam_args, W, H)
+    cfg = abi.make_config(W, H, spp=1, max_spp=3, bounce=3, kernel=abi.SPK_KERNEL_MEGAKERNEL)
+    gpu_render(ctx, scene, camera, cfg, 6)
+    r = oracle.OracleRenderer(oracle.OracleScene(scene), cfg, camera)
+    r.render(6)
+    assert ctx.sample_counts() == r.sample_counts() == (3, 6)
+    assert ctx.is_converged()
+    ctx.set_camera(camera)
+    ctx.render(1)
+    assert ctx.sample_counts() == (0, 1)
+
+
+def test_full_hd_frame_is_consistent(ctx):
+    """One 1920x1080 frame of the stress scene, both schedules: identical images and ray counts, no
+    device error flags, finite output."""
+    scene, cam_args = scenes.terrain_spheres(0)
+    W, H = 1920, 1080
+    camera = scenes.make_camera(cam_args, W, H)
+    res = []
+    for kernel in (abi.SPK_KERNEL_MEGAKERNEL, abi.SPK_KERNEL_WAVEFRONT):
+        cfg = abi.make_config(W, H, spp=1, bounce=8, rng=abi.SPK_RNG_XOSHIRO256SS, kernel=kernel)
+        hdr, out, st = gpu_render(ctx, scene, camera, cfg, 1)
+        assert np.all(np.isfinite(hdr))
+        res.append((hdr, st["extension_rays"]))
+    assert np.array_equal(res[0][0].view(np.uint32), res[1][0].view(np.uint32))
+    assert res[0][1] == res[1][1]
+    assert res[0][1] >= W * H
