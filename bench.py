@@ -1,0 +1,343 @@
+"""Benchmark: Mrays/s of the path tracer on the incoherent-ray stress scene at 1920x1080, 64 spp, depth 8.
+
+A step is one 64-spp render: 64 progressive frames of one sample per pixel through spk_render (exactly the
+reference cpu pipeline's 64 Render() calls at spp=1), over the resident scene (fBm terrain 2,097,152
+triangles + 64 level-5 icospheres of 20,480 triangles, Lambertian / GGX metal / dielectric materials, sky
+cube with a baked sun). Rays = traced segments (extension + shadow).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the reference's CPU path tracer (the restated oracle: the reference itself does not
+build here) on this machine's host cores over a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WIDTH, HEIGHT, SPP, BOUNCE = 1920, 1080, 64, 8
+METRIC = "Mrays/s on 1 GB300 (path tracer, stress scene 1920x1080, 64 spp, depth 8)"
+UNIT = "Mrays/s"
+NODE_BYTES, TRI_BYTES, RAY_BYTES, HIT_BYTES = 80, 36, 32, 20
+
+
+def workload_config():
+    return {"workload": "stress scene path tracing: fBm terrain 1024^2 cells (2,097,152 tris) + 64 level-5 "
+                        "icospheres (20,480 tris each), 1920x1080, 64 spp (64 frames x 1 spp), max depth 8, "
+                        "xoshiro256** per-pixel RNG, Lambertian/GGX-metal/dielectric, sky cube with sun",
+            "width": WIDTH, "height": HEIGHT, "spp": SPP, "max_depth": BOUNCE, "triangles": 3_407_872,
+            "l2_policy": "inputs larger than L2 (BVH + triangles ~127 MB resident, frame buffers 50 MB, path "
+                         "state 180 MB per step touched), no explicit flush"}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=6)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if len(s) > 4 + k and
+                          s[4 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples),
+                "power_w_max": max((float(s[2]) for s in self.samples if re.match(r"^[0-9.]+$", s[2])), default=None)}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def init_dist(world: int, backend: str):
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group(backend)
+        return dist
+    return None
+
+
+def max_over_ranks(dist, value: float) -> float:
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, value: float) -> float:
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_ray():
+    """DRAM bytes per extension ray of the extend kernel from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "k_wf_extend_stress.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        m = re.search(r"dram_bytes_per_ray\s*=\s*([0-9.]+)", f.read())
+    return float(m.group(1)) if m else None
+
+
+def cpu_sample(scene, camera, frames: int, rows: int, threads: int, traversal: int):
+    """Times the oracle (reference cpu pipeline restated) on `rows` central rows for `frames` frames."""
+    import oracle
+    from sparkle_gb300 import abi
+    osc = oracle.OracleScene(scene)
+    cfg = abi.make_config(WIDTH, HEIGHT, spp=1, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS, seed=0)
+    r = oracle.OracleRenderer(osc, cfg, camera)
+    r0 = HEIGHT // 2 - rows // 2
+    t0 = time.perf_counter()
+    r.render(frames, traversal=traversal, threads=threads, rows=(r0, r0 + rows))
+    dt = time.perf_counter() - t0
+    ext, shadow, paths = r.counts()
+    return (ext + shadow) / dt / 1e6, ext + shadow, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    from sparkle_gb300 import scenes
+    threads = os.cpu_count() or 1
+    scene, cam_args = scenes.terrain_spheres(0)
+    camera = scenes.make_camera(cam_args, WIDTH, HEIGHT)
+    rows = 32
+    for _ in range(args.warmup):
+        cpu_sample(scene, camera, 1, rows, threads, oracle.FAITHFUL)
+    vals, rays_tot, t_tot = [], 0, 0.0
+    for _ in range(args.steps):
+        v, n, dt = cpu_sample(scene, camera, 1, rows, threads, oracle.FAITHFUL)
+        vals.append(v)
+        rays_tot += n
+        t_tot += dt
+    value = rays_tot / t_tot / 1e6
+    sample = (f"one 1-spp frame of {rows} central rows x {WIDTH} pixels per step (oracle restatement of the "
+              f"reference cpu path tracer, faithful traversal: no tmax shrink), {threads} threads")
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * t_tot / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(),
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    rank, world, local_rank = dist_env()
+    import numpy as np
+    import torch
+    from sparkle_gb300 import abi, native, scenes
+    torch.cuda.set_device(local_rank)
+    dist = init_dist(world, "nccl")
+    scene, cam_args = scenes.terrain_spheres(0)
+    camera = scenes.make_camera(cam_args, WIDTH, HEIGHT)
+    ctx = native.Context(local_rank)
+    ctx.set_scene(scene)
+    cfg = abi.make_config(WIDTH, HEIGHT, spp=1, max_spp=4096, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS,
+                          seed=rank, kernel=args.kernel)
+    ctx.set_config(cfg)
+    ctx.set_camera(camera)
+
+    # Traffic accounting (untimed): count visited wide nodes and tested triangles over 2 frames.
+    ctx.set_instrumentation(True)
+    ctx.render(2)
+    cs = ctx.stats()
+    ctx.set_instrumentation(False)
+    bytes_per_ray = (NODE_BYTES * cs["node_visits"] + TRI_BYTES * cs["triangle_tests"]) / cs["extension_rays"] \
+        + RAY_BYTES + HIT_BYTES
+
+    for _ in range(args.warmup):
+        ctx.set_camera(camera)
+        ctx.render(SPP)
+        ctx.synchronize()
+
+    # Device-timed steps (inputs resident).
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    device_ms = trace_ms = 0.0
+    rays = launches = trace_launches = errors = 0
+    with ClockSampler(local_rank) as clocks:
+        for _ in range(args.steps):
+            ctx.set_camera(camera)
+            ctx.render(SPP)
+            st = ctx.stats()
+            device_ms += st["device_ms"]
+            trace_ms += st["trace_kernel_ms"]
+            rays += st["extension_rays"] + st["shadow_rays"]
+            launches += st["kernel_launches"]
+            trace_launches += st["trace_launches"]
+            errors |= st["error_flags"]
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    elapsed_s = max_over_ranks(dist, device_ms / 1000.0)
+    total_rays = sum_over_ranks(dist, float(rays))
+    value = total_rays / elapsed_s / 1e6
+
+    # End to end through the C ABI: camera in, 64 frames, HDR + RGBA16F frame buffers out to pinned memory.
+    hdr_host = torch.empty((HEIGHT, WIDTH, 4), dtype=torch.float32, pin_memory=True)
+    out_host = torch.empty((HEIGHT, WIDTH, 4), dtype=torch.int16, pin_memory=True)
+    d2h = hdr_host.numel() * 4 + out_host.numel() * 2
+    h2d = 96  # spk_camera
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e2e_rays = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.set_camera(camera)
+        ctx.render(SPP)
+        ctx.read_framebuffer_into(hdr_host.data_ptr(), out_host.data_ptr())
+        e2e_rays += ctx.stats()["extension_rays"]
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e_value = sum_over_ranks(dist, float(e2e_rays)) / e2e_s / 1e6
+    if dist:
+        dist.barrier()
+
+    if rank != 0:
+        ctx.close()
+        return
+    peak, peak_kind = measured_peaks()
+    rays_per_launch = rays / max(1, trace_launches)
+    achieved = bytes_per_ray * rays / (trace_ms / 1000.0) / 1e9
+    traffic_per_ray = ncu_traffic_per_ray()
+    hdr = np.asarray(hdr_host)
+    assert np.all(np.isfinite(hdr)), "non-finite frame buffer"
+
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        import oracle
+        threads = os.cpu_count() or 1
+        v_f, n_f, dt_f = cpu_sample(scene, camera, 2, 64, threads, oracle.FAITHFUL)
+        v_p, n_p, dt_p = cpu_sample(scene, camera, 2, 64, threads, oracle.PRUNED)
+        cpu = {"value": round(v_f, 4), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"2 frames x 64 central rows x {WIDTH} px of the same scene/config, oracle restatement of "
+                         f"the reference cpu path tracer, faithful traversal (no tmax shrink): {n_f} rays in "
+                         f"{dt_f:.2f} s; pruned traversal: {v_p:.3f} Mrays/s",
+               "pruned_value": round(v_p, 4)}
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(elapsed_s * 1000.0 / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(workload_config(), kernel={0: "auto(wavefront)", 1: "megakernel", 2: "wavefront"}[args.kernel],
+                       parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "kernel": "k_wf_extend (closest-hit walk)" if args.kernel != 1 else "k_render_mega",
+                     "algorithmic_bytes_per_ray": round(bytes_per_ray, 1),
+                     "rays_per_launch": round(rays_per_launch, 1),
+                     "traffic": (round(traffic_per_ray * rays_per_launch) if traffic_per_ray else None),
+                     "traffic_unit": "DRAM bytes per launch (ncu per-ray figure x rays per launch)"},
+        "trace_kernel_ms_per_step": round(trace_ms / args.steps, 3),
+        "device_error_flags": errors,
+        "clocks": clocks.summary(),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_profile_small(args):
+    """The stress scene (127 MB of nodes + triangles, larger than L2) rendered at 960x540 for 2 frames: the
+    case the ncu section captures run on (one kernel, a few launches, ~0.4 GB on the device)."""
+    from sparkle_gb300 import abi, native, scenes
+    scene, cam_args = scenes.terrain_spheres(0)
+    w, h = 960, 540
+    ctx = native.Context(0)
+    ctx.set_scene(scene)
+    ctx.set_config(abi.make_config(w, h, spp=1, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS, kernel=args.kernel))
+    ctx.set_camera(scenes.make_camera(cam_args, w, h))
+    ctx.render(2)
+    st = ctx.stats()
+    assert st["error_flags"] == 0, st
+    print(json.dumps({"profile_small": True, "extension_rays": st["extension_rays"], "device_ms": st["device_ms"]}))
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--kernel", type=int, default=0, help="0 auto, 1 megakernel, 2 wavefront")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-small", action="store_true",
+                    help="ncu capture case: the same scene at 960x540, 2 frames, no timing output")
+    args = ap.parse_args()
+    if args.profile_small:
+        run_profile_small(args)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -186,7 +186,11 @@ typedef struct spk_stats {
     uint32_t error_flags;    /* device-side error bits (stack overflow, iteration budget) */
     uint32_t bvh_nodes;      /* wide nodes resident for the scene */
     uint64_t bvh_bytes;      /* bytes of wide nodes + triangle records resident */
+    uint64_t node_visits;    /* wide nodes visited (only with SPK_INSTR_COUNT_TRAFFIC) */
+    uint64_t triangle_tests; /* ray-triangle tests run (only with SPK_INSTR_COUNT_TRAFFIC) */
 } spk_stats;
+
+enum { SPK_INSTR_NONE = 0, SPK_INSTR_COUNT_TRAFFIC = 1 };
 
 /* ------------------------------------------------------------------------------------------------ */
 /* Entry points                                                                                      */
@@ -262,6 +266,11 @@ spk_status spk_synchronize(spk_ctx *ctx);
 
 /* Counters of the last spk_render / spk_trace / spk_trace_device call (waits for it to finish). */
 spk_status spk_get_stats(spk_ctx *ctx, spk_stats *out);
+
+/* Measurement hook with no reference counterpart (the reference's only instrumentation is Tracy scopes,
+ * libraries/include/core/Profiler.h:9-28): SPK_INSTR_COUNT_TRAFFIC switches the traversal kernels to
+ * variants that also count visited nodes and tested triangles (slower; results are unchanged). */
+spk_status spk_set_instrumentation(spk_ctx *ctx, uint32_t flags);
 
 #ifdef __cplusplus
 }

@@ -68,7 +68,8 @@ class spk_hit(C.Structure):
 class spk_stats(C.Structure):
     _fields_ = [("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("paths", C.c_uint64),
                 ("device_ms", _f), ("trace_kernel_ms", _f), ("trace_launches", _u32), ("kernel_launches", _u32),
-                ("error_flags", _u32), ("bvh_nodes", _u32), ("bvh_bytes", C.c_uint64)]
+                ("error_flags", _u32), ("bvh_nodes", _u32), ("bvh_bytes", C.c_uint64),
+                ("node_visits", C.c_uint64), ("triangle_tests", C.c_uint64)]
 
 
 HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4"), ("face", "<u4")])

@@ -9,18 +9,14 @@
 namespace spk {
 namespace {
 
-__device__ __forceinline__ void warp_add_u64(unsigned long long *dst, uint32_t v) {
-    const uint32_t total = __reduce_add_sync(__activemask(), v);
-    if ((threadIdx.x & 31u) == (__ffs(__activemask()) - 1)) atomicAdd(dst, static_cast<unsigned long long>(total));
-}
-
 // ------------------------------------------------------------------------------------------------
 // Ray-set query: persistent warps pull 32-ray batches from a global counter.
 // ------------------------------------------------------------------------------------------------
-template <int kMode>
+template <int kMode, bool kCount>
 __global__ void __launch_bounds__(128) k_trace(DevScene S, const float *__restrict__ rays, uint64_t n,
                                                spk_hit_dev *__restrict__ hits, Counters *counters) {
     uint32_t err = 0;
+    TraceCounts tc;
     const uint32_t lane = threadIdx.x & 31u;
     unsigned long long *next = &counters->queue_counters[0];
     for (;;) {
@@ -33,7 +29,7 @@ __global__ void __launch_bounds__(128) k_trace(DevScene S, const float *__restri
             const float *r = rays + k * 6;
             const f3 o = mk3(r[0], r[1], r[2]);
             const f3 d = mk3(r[3], r[4], r[5]);
-            const TraceResult res = trace_ray<kMode>(S, o, d, kFltMax, err);
+            const TraceResult res = trace_ray<kMode, kCount>(S, o, d, kFltMax, err, &tc);
             spk_hit_dev out;
             if (res.inst == kInvalid) {
                 out = spk_hit_dev{0.f, 0.f, 0.f, kInvalid, kInvalid};
@@ -46,18 +42,23 @@ __global__ void __launch_bounds__(128) k_trace(DevScene S, const float *__restri
         }
         warp_add_u64(&counters->extension_rays, k < n ? 1u : 0u);
     }
+    if (kCount) {
+        warp_add_u64(&counters->node_visits, tc.nodes);
+        warp_add_u64(&counters->tri_tests, tc.tris);
+    }
     if (err) atomicOr(&counters->error_flags, err);
 }
 
 // ------------------------------------------------------------------------------------------------
 // BasePass: one thread per pixel runs RenderPixel + SamplePixel (CPURenderer.cpp:240-417).
 // ------------------------------------------------------------------------------------------------
-template <int kKind>
+template <int kKind, bool kCount>
 __global__ void __launch_bounds__(128) k_render_mega(DevScene S, DevCamera cam, FrameBuffers fb, RenderParams p,
                                                      Counters *counters) {
     const uint32_t i = blockIdx.x * 16u + (threadIdx.x & 15u);
     const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 4);
     uint32_t err = 0, rays = 0;
+    TraceCounts tc;
     if (i < fb.width && j < fb.height) {
         Rng rng;
         rng_seed_pixel<kKind>(rng, p.seed, i, j, fb.width, fb.height, p.frame_seed);
@@ -71,7 +72,7 @@ __global__ void __launch_bounds__(128) k_render_mega(DevScene S, DevCamera cam, 
         float valid = 1.f;
         for (uint32_t bounce = 0; bounce < p.bounce; ++bounce) {
             ++rays;
-            const TraceResult hit = trace_ray<kTraceClosest>(S, o, d, kFltMax, err);
+            const TraceResult hit = trace_ray<kTraceClosest, kCount>(S, o, d, kFltMax, err, &tc);
             if (hit.inst == kInvalid) {
                 if (S.sky_mode != 0u) color = color + cmul(sky_eval(S, d), thr);
                 break;
@@ -105,6 +106,10 @@ __global__ void __launch_bounds__(128) k_render_mega(DevScene S, DevCamera cam, 
         if (p.spatial_denoise) fb.gnormal[k] = make_float4(first_normal.x, first_normal.y, first_normal.z, 0.f);
     }
     warp_add_u64(&counters->extension_rays, rays);
+    if (kCount) {
+        warp_add_u64(&counters->node_visits, tc.nodes);
+        warp_add_u64(&counters->tri_tests, tc.tris);
+    }
     if (err) atomicOr(&counters->error_flags, err);
 }
 
@@ -178,8 +183,8 @@ __global__ void __launch_bounds__(256) k_resolve(FrameBuffers fb, float f, float
 
 }  // namespace
 
-cudaError_t launch_trace(const DevScene &scene, const float *rays, uint64_t n, void *hits, int mode,
-                         Counters *counters, int num_sms, cudaStream_t stream) {
+cudaError_t launch_trace(const DevScene &scene, const float *rays, uint64_t n, void *hits, int mode, bool count,
+                         Counters *counters, int num_sms, cudaStream_t stream, LaunchEvents *ev) {
     cudaError_t e = cudaMemsetAsync(&counters->queue_counters[0], 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     const uint64_t warps_needed = (n + 31) / 32;
@@ -187,22 +192,44 @@ cudaError_t launch_trace(const DevScene &scene, const float *rays, uint64_t n, v
     blocks = std::min<uint64_t>(blocks, (warps_needed + 3) / 4);
     if (blocks == 0) blocks = 1;
     auto *h = static_cast<spk_hit_dev *>(hits);
+    const unsigned g = static_cast<unsigned>(blocks);
+    if (ev) ev->before(stream);
     if (mode == kTraceClosest) {
-        k_trace<kTraceClosest><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, rays, n, h, counters);
+        if (count) {
+            k_trace<kTraceClosest, true><<<g, 128, 0, stream>>>(scene, rays, n, h, counters);
+        } else {
+            k_trace<kTraceClosest, false><<<g, 128, 0, stream>>>(scene, rays, n, h, counters);
+        }
     } else {
-        k_trace<kTraceAnyRef><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(scene, rays, n, h, counters);
+        if (count) {
+            k_trace<kTraceAnyRef, true><<<g, 128, 0, stream>>>(scene, rays, n, h, counters);
+        } else {
+            k_trace<kTraceAnyRef, false><<<g, 128, 0, stream>>>(scene, rays, n, h, counters);
+        }
     }
+    if (ev) ev->after(stream);
     return cudaGetLastError();
 }
 
 cudaError_t launch_render_mega(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
-                               const RenderParams &p, Counters *counters, cudaStream_t stream) {
+                               const RenderParams &p, bool count, Counters *counters, cudaStream_t stream,
+                               LaunchEvents *ev) {
     const dim3 grid((fbuf.width + 15) / 16, (fbuf.height + 7) / 8);
+    if (ev) ev->before(stream);
     if (p.rng == 0) {
-        k_render_mega<0><<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
+        if (count) {
+            k_render_mega<0, true><<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
+        } else {
+            k_render_mega<0, false><<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
+        }
     } else {
-        k_render_mega<1><<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
+        if (count) {
+            k_render_mega<1, true><<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
+        } else {
+            k_render_mega<1, false><<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
+        }
     }
+    if (ev) ev->after(stream);
     return cudaGetLastError();
 }
 

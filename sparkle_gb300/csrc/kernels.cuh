@@ -29,7 +29,30 @@ struct Counters {
     unsigned long long shadow_rays;
     unsigned int error_flags;
     unsigned int pad;
+    unsigned long long node_visits;
+    unsigned long long tri_tests;
     unsigned long long queue_counters[8];
+};
+
+// Sum of a per-thread count over the active lanes of a warp, added once per warp.
+__device__ __forceinline__ void warp_add_u64(unsigned long long *dst, uint32_t v) {
+    const uint32_t mask = __activemask();
+    const uint32_t total = __reduce_add_sync(mask, v);
+    if ((threadIdx.x & 31u) == static_cast<uint32_t>(__ffs(mask) - 1) && total)
+        atomicAdd(dst, static_cast<unsigned long long>(total));
+}
+
+// Events bracketing each traversal launch (for per-launch device time); null = not recorded.
+struct LaunchEvents {
+    cudaEvent_t *pairs = nullptr;  // 2 * capacity events
+    int capacity = 0;
+    int used = 0;
+    void before(cudaStream_t s) {
+        if (pairs && used < capacity) cudaEventRecord(pairs[2 * used], s);
+    }
+    void after(cudaStream_t s) {
+        if (pairs && used < capacity) cudaEventRecord(pairs[2 * used++ + 1], s);
+    }
 };
 
 struct RenderParams {
@@ -42,12 +65,13 @@ struct RenderParams {
 };
 
 // Ray-set query over spk_ray records (24 B) into spk_hit records (20 B).
-cudaError_t launch_trace(const DevScene &scene, const float *rays, uint64_t n, void *hits, int mode,
-                         Counters *counters, int num_sms, cudaStream_t stream);
+cudaError_t launch_trace(const DevScene &scene, const float *rays, uint64_t n, void *hits, int mode, bool count,
+                         Counters *counters, int num_sms, cudaStream_t stream, LaunchEvents *ev);
 
 // One BasePass frame with one thread per pixel (the whole path in one kernel).
 cudaError_t launch_render_mega(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
-                               const RenderParams &p, Counters *counters, cudaStream_t stream);
+                               const RenderParams &p, bool count, Counters *counters, cudaStream_t stream,
+                               LaunchEvents *ev);
 
 // DenoisePass (spatial fill + temporal lerp with weight `moving_average`) + ToneMappingPass.
 cudaError_t launch_resolve(const FrameBuffers &fbuf, float moving_average, float exposure, uint32_t spatial_denoise,

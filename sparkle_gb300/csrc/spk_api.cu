@@ -45,7 +45,9 @@ struct spk_ctx {
     int num_sms = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
-    std::vector<cudaEvent_t> trace_events;  // start/stop pairs of traversal launches of the last call
+    std::vector<cudaEvent_t> event_pool;  // start/stop pairs around traversal launches, reused across calls
+    LaunchEvents launch_events{};
+    uint32_t instrumentation = SPK_INSTR_NONE;
     std::string error;
 
     // resident scene
@@ -148,6 +150,20 @@ BuildBox world_box(const float *m, const double lo[3], const double hi[3]) {
     return b;
 }
 
+// Makes room for `pairs` start/stop event pairs and resets the per-call launch timing.
+cudaError_t prepare_events(spk_ctx *ctx, size_t pairs) {
+    while (ctx->event_pool.size() < 2 * pairs) {
+        cudaEvent_t ev;
+        const cudaError_t e = cudaEventCreate(&ev);
+        if (e != cudaSuccess) return e;
+        ctx->event_pool.push_back(ev);
+    }
+    ctx->launch_events.pairs = ctx->event_pool.data();
+    ctx->launch_events.capacity = static_cast<int>(ctx->event_pool.size() / 2);
+    ctx->launch_events.used = 0;
+    return cudaSuccess;
+}
+
 void append_wide(std::vector<WideNode> &all, const WideBvh &w, uint32_t item_offset) {
     const uint32_t base = static_cast<uint32_t>(all.size());
     for (WideNode n : w.nodes) {
@@ -204,7 +220,7 @@ spk_status spk_destroy(spk_ctx *ctx) {
     ctx->out.reset();
     wavefront_free(ctx->wf);
     if (ctx->counters) cudaFree(ctx->counters);
-    for (cudaEvent_t ev : ctx->trace_events) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -508,13 +524,15 @@ spk_status spk_set_config(spk_ctx *ctx, const spk_config *config) {
 static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
     FrameBuffers fbuf{ctx->gcolor.ptr, ctx->gnormal.ptr, ctx->fb.ptr, ctx->out.ptr, ctx->cfg.width, ctx->cfg.height};
     cudaError_t e;
-    for (cudaEvent_t ev : ctx->trace_events) cudaEventDestroy(ev);
-    ctx->trace_events.clear();
+    const bool wavefront = ctx->cfg.kernel != SPK_KERNEL_MEGAKERNEL;
+    const bool count = (ctx->instrumentation & SPK_INSTR_COUNT_TRAFFIC) != 0;
+    const size_t launches_per_frame = wavefront ? ctx->cfg.bounce : 1;
+    if ((e = prepare_events(ctx, static_cast<size_t>(num_frames) * launches_per_frame)) != cudaSuccess)
+        return cuda_fail(ctx, e, "event pool");
     ctx->launches_in_call = 0;
     if ((e = cudaMemsetAsync(ctx->counters, 0, sizeof(Counters), ctx->stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "counter reset");
     if ((e = cudaEventRecord(ctx->ev_start, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "event");
-    const bool wavefront = ctx->cfg.kernel == SPK_KERNEL_WAVEFRONT;
     for (uint32_t f = 0; f < num_frames; ++f) {
         // CameraRenderProxy::Update (CameraRenderProxy.cpp:66-75)
         if (ctx->dirty) {
@@ -532,22 +550,16 @@ static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
         }
         RenderParams p{ctx->dispatched, ctx->cfg.bounce, ctx->cfg.rng, ctx->cfg.seed, ctx->cfg.spatial_denoise,
                        ctx->cfg.enable_nee};
-        cudaEvent_t t0, t1;
-        cudaEventCreate(&t0);
-        cudaEventCreate(&t1);
-        ctx->trace_events.push_back(t0);
-        ctx->trace_events.push_back(t1);
-        cudaEventRecord(t0, ctx->stream);
         uint32_t launches = 0;
         if (wavefront) {
-            e = launch_render_wavefront(ctx->scene, ctx->cam, fbuf, p, ctx->counters, ctx->wf, ctx->num_sms,
-                                        ctx->stream, &launches);
+            e = launch_render_wavefront(ctx->scene, ctx->cam, fbuf, p, count, ctx->counters, ctx->wf, ctx->num_sms,
+                                        ctx->stream, &launches, &ctx->launch_events);
         } else {
-            e = launch_render_mega(ctx->scene, ctx->cam, fbuf, p, ctx->counters, ctx->stream);
+            e = launch_render_mega(ctx->scene, ctx->cam, fbuf, p, count, ctx->counters, ctx->stream,
+                                   &ctx->launch_events);
             launches = 1;
         }
         if (e != cudaSuccess) return cuda_fail(ctx, e, "base pass launch");
-        cudaEventRecord(t1, ctx->stream);
         ctx->launches_in_call += launches;
         // DenoisePass weight: cumulated / (cumulated + actual spp) (CPURenderer.cpp:530-532)
         const float mavg = static_cast<float>(ctx->cumulated) / static_cast<float>(ctx->cumulated + ctx->spp_eff);
@@ -609,22 +621,15 @@ int32_t spk_is_converged(const spk_ctx *ctx) {
 }
 
 static spk_status trace_impl(spk_ctx *ctx, const void *d_rays, uint64_t num_rays, void *d_hits, int32_t any_hit) {
-    for (cudaEvent_t ev : ctx->trace_events) cudaEventDestroy(ev);
-    ctx->trace_events.clear();
     cudaError_t e;
+    if ((e = prepare_events(ctx, 1)) != cudaSuccess) return cuda_fail(ctx, e, "event pool");
     if ((e = cudaMemsetAsync(ctx->counters, 0, sizeof(Counters), ctx->stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "counter reset");
-    cudaEvent_t t0, t1;
-    cudaEventCreate(&t0);
-    cudaEventCreate(&t1);
-    ctx->trace_events.push_back(t0);
-    ctx->trace_events.push_back(t1);
     cudaEventRecord(ctx->ev_start, ctx->stream);
-    cudaEventRecord(t0, ctx->stream);
     e = launch_trace(ctx->scene, static_cast<const float *>(d_rays), num_rays, d_hits,
-                     any_hit ? kTraceAnyRef : kTraceClosest, ctx->counters, ctx->num_sms, ctx->stream);
+                     any_hit ? kTraceAnyRef : kTraceClosest, (ctx->instrumentation & SPK_INSTR_COUNT_TRAFFIC) != 0,
+                     ctx->counters, ctx->num_sms, ctx->stream, &ctx->launch_events);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "trace launch");
-    cudaEventRecord(t1, ctx->stream);
     cudaEventRecord(ctx->ev_stop, ctx->stream);
     ctx->launches_in_call = 1;
     ctx->last = spk_stats{};
@@ -687,23 +692,34 @@ spk_status spk_get_stats(spk_ctx *ctx, spk_stats *out) {
         ctx->last.extension_rays = c.extension_rays;
         ctx->last.shadow_rays = c.shadow_rays;
         ctx->last.error_flags = c.error_flags;
+        ctx->last.node_visits = c.node_visits;
+        ctx->last.triangle_tests = c.tri_tests;
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop);
         ctx->last.device_ms = ms;
         float tms = 0.f;
-        for (size_t k = 0; k + 1 < ctx->trace_events.size(); k += 2) {
+        const LaunchEvents &le = ctx->launch_events;
+        for (int k = 0; k < le.used; ++k) {
             float x = 0.f;
-            cudaEventElapsedTime(&x, ctx->trace_events[k], ctx->trace_events[k + 1]);
+            cudaEventElapsedTime(&x, le.pairs[2 * k], le.pairs[2 * k + 1]);
             tms += x;
         }
         ctx->last.trace_kernel_ms = tms;
-        ctx->last.trace_launches = static_cast<uint32_t>(ctx->trace_events.size() / 2);
+        ctx->last.trace_launches = static_cast<uint32_t>(le.used);
         ctx->last.kernel_launches = ctx->launches_in_call;
         ctx->stats_pending = false;
     }
     ctx->last.bvh_nodes = ctx->bvh_nodes;
     ctx->last.bvh_bytes = ctx->bvh_bytes;
     *out = ctx->last;
+    return SPK_OK;
+}
+
+spk_status spk_set_instrumentation(spk_ctx *ctx, uint32_t flags) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (flags & ~static_cast<uint32_t>(SPK_INSTR_COUNT_TRAFFIC))
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "unknown instrumentation flags 0x%x", flags);
+    ctx->instrumentation = flags;
     return SPK_OK;
 }
 

@@ -100,8 +100,14 @@ __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint
     tgroup = make_uint2(n1.y, hitmask & 0x00FFFFFFu);
 }
 
-template <int kMode>
-__device__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd, float tmax_occl, uint32_t &err) {
+// Per-thread traffic counters of the instrumented walk (wide nodes visited, triangles tested).
+struct TraceCounts {
+    uint32_t nodes = 0, tris = 0;
+};
+
+template <int kMode, bool kCount = false>
+__device__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd, float tmax_occl, uint32_t &err,
+                                 TraceCounts *counts = nullptr) {
     TraceResult best{kFltMax, 0.f, 0.f, kInvalid, kInvalid};
     if (S.tlas_root == kInvalid) return best;
     LevelRay ray;
@@ -133,6 +139,7 @@ __device__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd, float tmax_occ
                 }
             }
             visit_node(S.nodes, node_idx, ray, tmax_box, ngroup, tgroup);
+            if (kCount) ++counts->nodes;
         } else {
             tgroup = ngroup;
             ngroup = make_uint2(0u, 0u);
@@ -143,6 +150,7 @@ __device__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd, float tmax_occ
             const uint32_t idx = tgroup.x + k;
             if (in_blas) {
                 // Möller–Trumbore (MeshRenderProxy.cpp:128-194) in the instance's local space.
+                if (kCount) ++counts->tris;
                 const float4 *tp = S.tris + static_cast<size_t>(idx) * 3;
                 const float4 a4 = __ldg(tp), b4 = __ldg(tp + 1), c4 = __ldg(tp + 2);
                 const f3 p0 = mk3(a4.x, a4.y, a4.z), e1 = mk3(a4.w, b4.x, b4.y), e2 = mk3(b4.z, b4.w, c4.x);

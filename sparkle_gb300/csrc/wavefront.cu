@@ -8,7 +8,6 @@ namespace {
 
 // queue_counters slots
 constexpr int kLen0 = 0;     // length of queue 0
-constexpr int kLen1 = 1;     // length of queue 1
 constexpr int kCursor = 2;   // pop cursor of the running persistent stage
 
 template <int kKind>
@@ -71,8 +70,10 @@ __global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers
 }
 
 // Extend: persistent warps pop 32-path batches and trace their closest hit.
+template <bool kCount>
 __global__ void __launch_bounds__(128) k_wf_extend(DevScene S, WavefrontState s, int in_queue, Counters *counters) {
     uint32_t err = 0;
+    TraceCounts tc;
     const uint32_t lane = threadIdx.x & 31u;
     const unsigned long long n = counters->queue_counters[in_queue];
     const uint32_t *queue = s.queue[in_queue];
@@ -85,12 +86,17 @@ __global__ void __launch_bounds__(128) k_wf_extend(DevScene S, WavefrontState s,
         if (q < n) {
             const uint32_t pid = queue[q];
             const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
-            const TraceResult h = trace_ray<kTraceClosest>(S, mk3(o4.x, o4.y, o4.z), mk3(d4.x, d4.y, d4.z), kFltMax, err);
+            const TraceResult h =
+                trace_ray<kTraceClosest, kCount>(S, mk3(o4.x, o4.y, o4.z), mk3(d4.x, d4.y, d4.z), kFltMax, err, &tc);
             s.hit[pid] = make_float4(h.t, h.u, h.v, __uint_as_float(h.inst));
             s.hit_face[pid] = h.face;
         }
         const uint32_t cnt = static_cast<uint32_t>(min(32ull, n - base));
         if (lane == 0) atomicAdd(&counters->extension_rays, static_cast<unsigned long long>(cnt));
+    }
+    if (kCount) {
+        warp_add_u64(&counters->node_visits, tc.nodes);
+        warp_add_u64(&counters->tri_tests, tc.tris);
     }
     if (err) atomicOr(&counters->error_flags, err);
 }
@@ -201,8 +207,8 @@ void wavefront_free(WavefrontState &s) {
 }
 
 cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
-                                    const RenderParams &p, Counters *counters, WavefrontState &s, int num_sms,
-                                    cudaStream_t stream, uint32_t *launches) {
+                                    const RenderParams &p, bool count, Counters *counters, WavefrontState &s,
+                                    int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev) {
     uint32_t nl = 0;
     const uint32_t npix = fbuf.width * fbuf.height;
     if (s.capacity < npix) return cudaErrorInvalidValue;
@@ -222,7 +228,13 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
         const int in = static_cast<int>(b & 1u), out = in ^ 1;
         if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
         if ((e = cudaMemsetAsync(qc + kCursor, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
-        k_wf_extend<<<persist_blocks, 128, 0, stream>>>(scene, s, in, counters);
+        if (ev) ev->before(stream);
+        if (count) {
+            k_wf_extend<true><<<persist_blocks, 128, 0, stream>>>(scene, s, in, counters);
+        } else {
+            k_wf_extend<false><<<persist_blocks, 128, 0, stream>>>(scene, s, in, counters);
+        }
+        if (ev) ev->after(stream);
         ++nl;
         if (p.rng == 0) {
             k_wf_shade<0><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);

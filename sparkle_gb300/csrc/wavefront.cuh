@@ -29,7 +29,7 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity);
 void wavefront_free(WavefrontState &s);
 
 cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
-                                    const RenderParams &p, Counters *counters, WavefrontState &s, int num_sms,
-                                    cudaStream_t stream, uint32_t *launches);
+                                    const RenderParams &p, bool count, Counters *counters, WavefrontState &s,
+                                    int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev);
 
 }  // namespace spk

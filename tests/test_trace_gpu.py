@@ -53,9 +53,9 @@ def _check_closest(ctx, scene, rays, max_bad_frac=2e-5):
     assert c["hits"] > 0.2 * c["n"]
     assert c["other"] == 0
     assert c["exact"] + c["tie"] + c["gpu_closer"] + c["ref_closer"] == c["n"]
-    # every disagreement is a tie or a grazing box test, and they are rare
+    # every disagreement is a tie (bit-identical t, order-dependent winner) or a rare grazing box test
     assert c["gpu_closer"] + c["ref_closer"] <= max(2, max_bad_frac * c["n"])
-    assert c["exact"] >= (1 - 1e-3) * c["n"]
+    assert c["exact"] + c["tie"] >= (1 - max_bad_frac) * c["n"] - 2
     return got, ref, c
 
 
@@ -132,4 +132,4 @@ def test_full_size_random_rays(ctx):
     print({k: v for k, v in c.items() if k != "mismatch_idx"})
     assert c["other"] == 0
     assert c["gpu_closer"] + c["ref_closer"] <= 2e-6 * c["n"] + 4
-    assert c["exact"] >= (1 - 1e-5) * c["n"]
+    assert c["exact"] + c["tie"] >= (1 - 2e-6) * c["n"] - 4
