@@ -161,7 +161,7 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     scene, cam_args = scenes.terrain_spheres(0)
     camera = scenes.make_camera(cam_args, WIDTH, HEIGHT)
-    rows = 32
+    rows = 540
     for _ in range(args.warmup):
         cpu_sample(scene, camera, 1, rows, threads, oracle.FAITHFUL)
     vals, rays_tot, t_tot = [], 0, 0.0
@@ -271,10 +271,10 @@ def run_ours(args):
     if world == 1 and not args.no_cpu_baseline:
         import oracle
         threads = os.cpu_count() or 1
-        v_f, n_f, dt_f = cpu_sample(scene, camera, 2, 64, threads, oracle.FAITHFUL)
-        v_p, n_p, dt_p = cpu_sample(scene, camera, 2, 64, threads, oracle.PRUNED)
+        v_f, n_f, dt_f = cpu_sample(scene, camera, 16, 270, threads, oracle.FAITHFUL)
+        v_p, n_p, dt_p = cpu_sample(scene, camera, 16, 270, threads, oracle.PRUNED)
         cpu = {"value": round(v_f, 4), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"2 frames x 64 central rows x {WIDTH} px of the same scene/config, oracle restatement of "
+               "sample": f"16 frames x 270 central rows x {WIDTH} px of the same scene/config, oracle restatement of "
                          f"the reference cpu path tracer, faithful traversal (no tmax shrink): {n_f} rays in "
                          f"{dt_f:.2f} s; pruned traversal: {v_p:.3f} Mrays/s",
                "pruned_value": round(v_p, 4)}

@@ -10,26 +10,21 @@ namespace spk {
 namespace {
 
 // ------------------------------------------------------------------------------------------------
-// Ray-set query: persistent warps pull 32-ray batches from a global counter.
+// Ray-set query: persistent warps pull rays from a global counter and refill idle lanes.
 // ------------------------------------------------------------------------------------------------
 template <int kMode, bool kCount>
-__global__ void __launch_bounds__(128) k_trace(DevScene S, const float *__restrict__ rays, uint64_t n,
-                                               spk_hit_dev *__restrict__ hits, Counters *counters) {
-    uint32_t err = 0;
+__global__ void __launch_bounds__(128, 8) k_trace(DevScene S, const float *__restrict__ rays, uint64_t n,
+                                                  spk_hit_dev *__restrict__ hits, Counters *counters) {
+    uint32_t err = 0, done = 0;
     TraceCounts tc;
-    const uint32_t lane = threadIdx.x & 31u;
-    unsigned long long *next = &counters->queue_counters[0];
-    for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(next, 32ull);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        const uint64_t k = base + lane;
-        if (k < n) {
-            const float *r = rays + k * 6;
-            const f3 o = mk3(r[0], r[1], r[2]);
-            const f3 d = mk3(r[3], r[4], r[5]);
-            const TraceResult res = trace_ray<kMode, kCount>(S, o, d, kFltMax, err, &tc);
+    walk_persistent<kMode, kCount>(
+        S, &counters->queue_counters[0], n, kFltMax, err, &tc,
+        [&](unsigned long long q, f3 &o, f3 &d) {
+            const float *r = rays + q * 6;
+            o = mk3(r[0], r[1], r[2]);
+            d = mk3(r[3], r[4], r[5]);
+        },
+        [&](unsigned long long q, const TraceResult &res) {
             spk_hit_dev out;
             if (res.inst == kInvalid) {
                 out = spk_hit_dev{0.f, 0.f, 0.f, kInvalid, kInvalid};
@@ -38,10 +33,10 @@ __global__ void __launch_bounds__(128) k_trace(DevScene S, const float *__restri
             } else {
                 out = spk_hit_dev{0.f, 0.f, 0.f, res.inst, kInvalid};
             }
-            hits[k] = out;
-        }
-        warp_add_u64(&counters->extension_rays, k < n ? 1u : 0u);
-    }
+            hits[q] = out;
+            ++done;
+        });
+    warp_add_u64(&counters->extension_rays, done);
     if (kCount) {
         warp_add_u64(&counters->node_visits, tc.nodes);
         warp_add_u64(&counters->tri_tests, tc.tris);

@@ -12,6 +12,13 @@
 // ray's tmax (every box along the ray is visited); this walk prunes boxes that start beyond the current
 // best t plus a bound on the x-only world-t rounding error, and visits children in an octant order.
 // Only which of two hits with bit-identical t wins can differ (ties are order dependent).
+// One deliberate difference: for a direction component with |d| <= FLT_EPSILON, bvh v2's fast slab test
+// uses 1/d = +-FLT_MAX and its -inv*org term overflows to +-inf once |org| > 1 on that axis, which culls
+// every box of the level; here that axis is tested as an exact containment test instead.
+//
+// The walk is a resumable state machine (Walker::step) so persistent warps can replace finished rays
+// with new ones while the others are still walking (dynamic ray fetch), and it postpones triangle groups
+// when only a few lanes of the warp have triangles to test, keeping the lanes on the same kind of work.
 #pragma once
 
 #include "device_scene.cuh"
@@ -23,6 +30,7 @@ enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOve
 
 constexpr int kStackSize = 48;
 constexpr uint32_t kMaxIterations = 1u << 20;
+constexpr int kPostponeLanes = 8;  // postpone triangle groups when fewer lanes than this want triangles
 
 struct TraceResult {
     float t, u, v;
@@ -30,20 +38,26 @@ struct TraceResult {
     uint32_t face;  // original face index, kInvalid for spheres and misses
 };
 
+// Per-thread traffic counters of the instrumented walk (wide nodes visited, triangles tested).
+struct TraceCounts {
+    uint32_t nodes = 0, tris = 0;
+};
+
 struct LevelRay {
     f3 o, d, inv;
     uint32_t oct;  // bit k set when direction component k is negative
 };
 
-// bvh v2 safe_inverse: |x| <= FLT_EPSILON maps to +-FLT_MAX.
-__device__ __forceinline__ float safe_inverse(float x) {
-    return fabsf(x) <= 1.1920928955078125e-07f ? copysignf(kFltMax, x) : 1.f / x;
+// Reciprocal for the slab test; a component with |d| <= FLT_EPSILON gets +-2^100 so that
+// (bound - o) * inv keeps its exact sign without overflowing (an exact containment test on that axis).
+__device__ __forceinline__ float slab_inverse(float x) {
+    return fabsf(x) <= 1.1920928955078125e-07f ? copysignf(0x1p100f, x) : 1.f / x;
 }
 
 __device__ __forceinline__ void setup_level(LevelRay &r, f3 o, f3 d) {
     r.o = o;
     r.d = d;
-    r.inv = mk3(safe_inverse(d.x), safe_inverse(d.y), safe_inverse(d.z));
+    r.inv = mk3(slab_inverse(d.x), slab_inverse(d.y), slab_inverse(d.z));
     r.oct = (signbit(d.x) ? 1u : 0u) | (signbit(d.y) ? 2u : 0u) | (signbit(d.z) ? 4u : 0u);
 }
 
@@ -100,46 +114,63 @@ __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint
     tgroup = make_uint2(n1.y, hitmask & 0x00FFFFFFu);
 }
 
-// Per-thread traffic counters of the instrumented walk (wide nodes visited, triangles tested).
-struct TraceCounts {
-    uint32_t nodes = 0, tris = 0;
-};
-
-template <int kMode, bool kCount = false>
-__device__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd, float tmax_occl, uint32_t &err,
-                                 TraceCounts *counts = nullptr) {
-    TraceResult best{kFltMax, 0.f, 0.f, kInvalid, kInvalid};
-    if (S.tlas_root == kInvalid) return best;
+// Resumable two-level walk of one ray. init() starts it; step() advances by one node visit plus the
+// triangle tests it enables and returns true when the walk is over (result in `best`).
+template <int kMode, bool kCount>
+struct Walker {
+    f3 wo, wd;
     LevelRay ray;
-    setup_level(ray, wo, wd);
-    float tmax_box = (kMode == kTraceOcclusion) ? tmax_occl : kFltMax;
-    uint2 stack[kStackSize];
-    int sp = 0;
-    uint2 ngroup = make_uint2(S.tlas_root, 1u << 24);
-    uint2 tgroup = make_uint2(0u, 0u);
-    bool in_blas = false;
-    int blas_sp = 0;
-    uint32_t cur_inst = 0;
-    uint32_t iter = 0;
-    for (;;) {
+    uint2 ngroup, tgroup;
+    int sp, blas_sp;
+    uint32_t cur_inst;
+    uint32_t iter;
+    bool in_blas;
+    float tmax_box, tmax_occl;
+    TraceResult best;
+
+    __device__ __forceinline__ void init(const DevScene &S, f3 o, f3 d, float tmax) {
+        wo = o;
+        wd = d;
+        setup_level(ray, o, d);
+        ngroup = make_uint2(S.tlas_root, S.tlas_root == kInvalid ? 0u : (1u << 24));
+        tgroup = make_uint2(0u, 0u);
+        sp = 0;
+        blas_sp = 0;
+        cur_inst = 0;
+        iter = 0;
+        in_blas = false;
+        tmax_occl = tmax;
+        tmax_box = (kMode == kTraceOcclusion) ? tmax : kFltMax;
+        best = TraceResult{kFltMax, 0.f, 0.f, kInvalid, kInvalid};
+    }
+
+    __device__ __forceinline__ void push(uint2 *stack, uint2 v, uint32_t &err) {
+        if (sp < kStackSize) {
+            stack[sp++] = v;
+        } else {
+            err |= kErrStackOverflow;
+        }
+    }
+
+    __device__ __forceinline__ bool step(const DevScene &S, uint2 *stack, uint32_t &err, TraceCounts *counts) {
         if (++iter > kMaxIterations) {
             err |= kErrIterationBudget;
-            break;
+            return true;
         }
         if (ngroup.y > 0x00FFFFFFu) {
             const uint32_t bit = __ffs(ngroup.y >> 24) - 1;
             ngroup.y &= ~(1u << (bit + 24));
             const uint32_t slot = bit ^ ray.oct;
             const uint32_t node_idx = ngroup.x + __popc(ngroup.y & 0xFFu & ((1u << slot) - 1u));
-            if (ngroup.y > 0x00FFFFFFu) {
-                if (sp < kStackSize) {
-                    stack[sp++] = ngroup;
-                } else {
-                    err |= kErrStackOverflow;
-                }
-            }
+            if (ngroup.y > 0x00FFFFFFu) push(stack, ngroup, err);
             visit_node(S.nodes, node_idx, ray, tmax_box, ngroup, tgroup);
             if (kCount) ++counts->nodes;
+            // Triangle postponing: when few lanes have triangles, keep walking nodes and test them later.
+            const uint32_t want = __ballot_sync(__activemask(), tgroup.y != 0u);
+            if (tgroup.y != 0u && ngroup.y > 0x00FFFFFFu && __popc(want) < kPostponeLanes) {
+                push(stack, tgroup, err);
+                tgroup.y = 0u;
+            }
         } else {
             tgroup = ngroup;
             ngroup = make_uint2(0u, 0u);
@@ -168,12 +199,12 @@ __device__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd, float tmax_occ
                 if (!(t > kEps)) continue;
                 if (kMode == kTraceAnyRef) {
                     best.inst = cur_inst;
-                    return best;
+                    return true;
                 }
                 if (kMode == kTraceOcclusion) {
                     if (t < tmax_occl) {
                         best.inst = cur_inst;
-                        return best;
+                        return true;
                     }
                     continue;
                 }
@@ -201,14 +232,14 @@ __device__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd, float tmax_occ
                     if (disc < 0.f) continue;
                     if (kMode == kTraceAnyRef) {
                         best.inst = inst;
-                        return best;
+                        return true;
                     }
                     const float sq = sqrtf(disc);
                     const float t = (-half_b + (c >= 0.f ? -sq : sq)) / 1.f;
                     if (kMode == kTraceOcclusion) {
                         if (t > kEps && t < tmax_occl) {
                             best.inst = inst;
-                            return best;
+                            return true;
                         }
                         continue;
                     }
@@ -222,20 +253,8 @@ __device__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd, float tmax_occ
                     }
                 } else if (I.blas_root != kInvalid) {
                     // Enter the BLAS: park the rest of this TLAS level on the stack.
-                    if (tgroup.y != 0u) {
-                        if (sp < kStackSize) {
-                            stack[sp++] = tgroup;
-                        } else {
-                            err |= kErrStackOverflow;
-                        }
-                    }
-                    if (ngroup.y > 0x00FFFFFFu) {
-                        if (sp < kStackSize) {
-                            stack[sp++] = ngroup;
-                        } else {
-                            err |= kErrStackOverflow;
-                        }
-                    }
+                    if (tgroup.y != 0u) push(stack, tgroup, err);
+                    if (ngroup.y > 0x00FFFFFFu) push(stack, ngroup, err);
                     blas_sp = sp;
                     in_blas = true;
                     cur_inst = inst;
@@ -251,11 +270,71 @@ __device__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd, float tmax_occ
                 in_blas = false;
                 setup_level(ray, wo, wd);
             }
-            if (sp == 0) break;
+            if (sp == 0) return true;
             ngroup = stack[--sp];
         }
+        return false;
     }
-    return best;
+};
+
+// Whole walk of one ray by one thread (no lane refill).
+template <int kMode, bool kCount = false>
+__device__ __forceinline__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd, float tmax_occl, uint32_t &err,
+                                                 TraceCounts *counts = nullptr) {
+    uint2 stack[kStackSize];
+    Walker<kMode, kCount> w;
+    w.init(S, wo, wd, tmax_occl);
+    while (!w.step(S, stack, err, counts)) {
+    }
+    return w.best;
+}
+
+// Persistent walk over a work list: each warp pulls batches of items from `cursor` and refills lanes whose
+// ray has finished once fewer than `kRefillLanes` lanes are still walking. `fetch(i, o, d)` loads item i's
+// ray; `finish(i, result)` stores its result. Every lane of every warp of the block must call this.
+constexpr int kRefillLanes = 20;
+
+template <int kMode, bool kCount, class Fetch, class Finish>
+__device__ __forceinline__ void walk_persistent(const DevScene &S, unsigned long long *cursor, unsigned long long n,
+                                                float tmax, uint32_t &err, TraceCounts *counts, Fetch &&fetch,
+                                                Finish &&finish) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    uint2 stack[kStackSize];
+    Walker<kMode, kCount> w;
+    bool active = false, exhausted = false;
+    unsigned long long item = 0;
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xFFFFFFFFu, !active);
+        if (!exhausted && idle != 0u) {
+            const uint32_t cnt = __popc(idle);
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(cursor, static_cast<unsigned long long>(cnt));
+            base = __shfl_sync(0xFFFFFFFFu, base, 0);
+            if (base + cnt >= n) exhausted = true;
+            if (!active) {
+                const unsigned long long q = base + __popc(idle & lt_mask);
+                if (q < n) {
+                    item = q;
+                    f3 o, d;
+                    fetch(q, o, d);
+                    w.init(S, o, d, tmax);
+                    active = true;
+                }
+            }
+        }
+        if (__ballot_sync(0xFFFFFFFFu, active) == 0u) {
+            if (exhausted) break;
+            continue;
+        }
+        while (active) {
+            if (w.step(S, stack, err, counts)) {
+                finish(item, w.best);
+                active = false;
+            }
+            if (!exhausted && __popc(__ballot_sync(__activemask(), active)) < kRefillLanes) break;
+        }
+    }
 }
 
 }  // namespace spk

@@ -69,31 +69,29 @@ __global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers
     if (pid == 0) counters->queue_counters[kLen0] = static_cast<unsigned long long>(fb.width) * fb.height;
 }
 
-// Extend: persistent warps pop 32-path batches and trace their closest hit.
+// Extend: persistent warps pull paths from the queue, refilling lanes whose walk has finished.
 template <bool kCount>
-__global__ void __launch_bounds__(128) k_wf_extend(DevScene S, WavefrontState s, int in_queue, Counters *counters) {
-    uint32_t err = 0;
+__global__ void __launch_bounds__(128, 8) k_wf_extend(DevScene S, WavefrontState s, int in_queue,
+                                                      Counters *counters) {
+    uint32_t err = 0, done = 0;
     TraceCounts tc;
-    const uint32_t lane = threadIdx.x & 31u;
     const unsigned long long n = counters->queue_counters[in_queue];
     const uint32_t *queue = s.queue[in_queue];
-    for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&counters->queue_counters[kCursor], 32ull);
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (base >= n) break;
-        const unsigned long long q = base + lane;
-        if (q < n) {
-            const uint32_t pid = queue[q];
+    uint32_t pid = 0;
+    walk_persistent<kTraceClosest, kCount>(
+        S, &counters->queue_counters[kCursor], n, kFltMax, err, &tc,
+        [&](unsigned long long q, f3 &o, f3 &d) {
+            pid = queue[q];
             const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
-            const TraceResult h =
-                trace_ray<kTraceClosest, kCount>(S, mk3(o4.x, o4.y, o4.z), mk3(d4.x, d4.y, d4.z), kFltMax, err, &tc);
+            o = mk3(o4.x, o4.y, o4.z);
+            d = mk3(d4.x, d4.y, d4.z);
+        },
+        [&](unsigned long long, const TraceResult &h) {
             s.hit[pid] = make_float4(h.t, h.u, h.v, __uint_as_float(h.inst));
             s.hit_face[pid] = h.face;
-        }
-        const uint32_t cnt = static_cast<uint32_t>(min(32ull, n - base));
-        if (lane == 0) atomicAdd(&counters->extension_rays, static_cast<unsigned long long>(cnt));
-    }
+            ++done;
+        });
+    warp_add_u64(&counters->extension_rays, done);
     if (kCount) {
         warp_add_u64(&counters->node_visits, tc.nodes);
         warp_add_u64(&counters->tri_tests, tc.tris);
