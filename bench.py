@@ -137,11 +137,11 @@ def ncu_traffic_per_ray():
     return float(m.group(1)) if m else None
 
 
-def cpu_sample(scene, camera, frames: int, rows: int, threads: int, traversal: int):
-    """Times the oracle (reference cpu pipeline restated) on `rows` central rows for `frames` frames."""
+def cpu_sample(osc, camera, frames: int, rows: int, threads: int, traversal: int):
+    """Times the oracle (reference cpu pipeline restated, scene `osc` already built) on `rows` central rows
+    for `frames` frames; returns (Mrays/s, rays, seconds)."""
     import oracle
     from sparkle_gb300 import abi
-    osc = oracle.OracleScene(scene)
     cfg = abi.make_config(WIDTH, HEIGHT, spp=1, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS, seed=0)
     r = oracle.OracleRenderer(osc, cfg, camera)
     r0 = HEIGHT // 2 - rows // 2
@@ -161,12 +161,13 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     scene, cam_args = scenes.terrain_spheres(0)
     camera = scenes.make_camera(cam_args, WIDTH, HEIGHT)
+    osc = oracle.OracleScene(scene)
     rows = 540
     for _ in range(args.warmup):
-        cpu_sample(scene, camera, 1, rows, threads, oracle.FAITHFUL)
+        cpu_sample(osc, camera, 1, rows, threads, oracle.FAITHFUL)
     vals, rays_tot, t_tot = [], 0, 0.0
     for _ in range(args.steps):
-        v, n, dt = cpu_sample(scene, camera, 1, rows, threads, oracle.FAITHFUL)
+        v, n, dt = cpu_sample(osc, camera, 1, rows, threads, oracle.FAITHFUL)
         vals.append(v)
         rays_tot += n
         t_tot += dt
@@ -271,8 +272,9 @@ def run_ours(args):
     if world == 1 and not args.no_cpu_baseline:
         import oracle
         threads = os.cpu_count() or 1
-        v_f, n_f, dt_f = cpu_sample(scene, camera, 16, 270, threads, oracle.FAITHFUL)
-        v_p, n_p, dt_p = cpu_sample(scene, camera, 16, 270, threads, oracle.PRUNED)
+        osc = oracle.OracleScene(scene)
+        v_f, n_f, dt_f = cpu_sample(osc, camera, 16, 270, threads, oracle.FAITHFUL)
+        v_p, n_p, dt_p = cpu_sample(osc, camera, 16, 270, threads, oracle.PRUNED)
         cpu = {"value": round(v_f, 4), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"16 frames x 270 central rows x {WIDTH} px of the same scene/config, oracle restatement of "
                          f"the reference cpu path tracer, faithful traversal (no tmax shrink): {n_f} rays in "
