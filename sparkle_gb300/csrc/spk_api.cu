@@ -77,6 +77,8 @@ struct spk_ctx {
     // CameraRenderProxy / CPURenderer sample bookkeeping
     uint32_t cumulated = 0, pending = 0, dispatched = 0;
     bool dirty = true;
+    std::vector<float> frame_weights;    // multi-frame wavefront: per-frame moving-average weight
+    std::vector<uint32_t> frame_seeds;   // multi-frame wavefront: per-frame seed base
 
     // counters
     Counters *counters = nullptr;  // device
@@ -527,12 +529,52 @@ static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
     const bool wavefront = ctx->cfg.kernel != SPK_KERNEL_MEGAKERNEL;
     const bool count = (ctx->instrumentation & SPK_INSTR_COUNT_TRAFFIC) != 0;
     const size_t launches_per_frame = wavefront ? ctx->cfg.bounce : 1;
-    if ((e = prepare_events(ctx, static_cast<size_t>(num_frames) * launches_per_frame)) != cudaSuccess)
+    if ((e = prepare_events(ctx, static_cast<size_t>(num_frames) * launches_per_frame + 16)) != cudaSuccess)
         return cuda_fail(ctx, e, "event pool");
     ctx->launches_in_call = 0;
     if ((e = cudaMemsetAsync(ctx->counters, 0, sizeof(Counters), ctx->stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "counter reset");
     if ((e = cudaEventRecord(ctx->ev_start, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "event");
+    if (wavefront && !ctx->cfg.spatial_denoise && num_frames > 0) {
+        // All frames in one regenerating wavefront: run the per-frame bookkeeping ahead on the host and hand
+        // the kernels each frame's weight and seed base.
+        ctx->frame_weights.resize(num_frames);
+        ctx->frame_seeds.resize(num_frames);
+        bool clear = false;
+        for (uint32_t f = 0; f < num_frames; ++f) {
+            if (ctx->dirty) {
+                ctx->cumulated = 0;
+                ctx->pending = 0;
+            }
+            ctx->cumulated = std::min(ctx->cfg.max_spp, ctx->cumulated + ctx->pending);
+            ctx->pending = 0;
+            if (ctx->dirty) {
+                clear = true;
+                ctx->dirty = false;
+                ctx->dispatched = 0;
+            }
+            ctx->frame_seeds[f] = ctx->dispatched;
+            ctx->frame_weights[f] =
+                static_cast<float>(ctx->cumulated) / static_cast<float>(ctx->cumulated + ctx->spp_eff);
+            ctx->dispatched += ctx->spp_eff;
+            ctx->pending += ctx->spp_eff;
+        }
+        if (clear &&
+            (e = cudaMemsetAsync(ctx->fb.ptr, 0, ctx->fb.count * sizeof(float4), ctx->stream)) != cudaSuccess)
+            return cuda_fail(ctx, e, "frame buffer clear");
+        RenderParams p{0u, ctx->cfg.bounce, ctx->cfg.rng, ctx->cfg.seed, 0u, ctx->cfg.enable_nee};
+        uint32_t launches = 0;
+        e = launch_render_multiframe(ctx->scene, ctx->cam, fbuf, p, num_frames, ctx->frame_weights.data(),
+                                     ctx->frame_seeds.data(), count, ctx->counters, ctx->wf, ctx->num_sms,
+                                     ctx->stream, &launches, &ctx->launch_events);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "multi-frame wavefront");
+        ctx->launches_in_call = launches;
+        if ((e = cudaEventRecord(ctx->ev_stop, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "event");
+        ctx->last = spk_stats{};
+        ctx->last.paths = static_cast<uint64_t>(num_frames) * ctx->cfg.width * ctx->cfg.height;
+        ctx->stats_pending = true;
+        return SPK_OK;
+    }
     for (uint32_t f = 0; f < num_frames; ++f) {
         // CameraRenderProxy::Update (CameraRenderProxy.cpp:66-75)
         if (ctx->dirty) {

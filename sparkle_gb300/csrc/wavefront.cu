@@ -1,14 +1,16 @@
 // wavefront.cu -- stage kernels of the wavefront BasePass (see wavefront.cuh).
 //
 // Compiled with -fmad=false like kernels.cu so every path computes bit-identically to the one-kernel form.
+#include <cuda_fp16.h>
+
 #include "wavefront.cuh"
 
 namespace spk {
 namespace {
 
 // queue_counters slots
-constexpr int kLen0 = 0;     // length of queue 0
-constexpr int kCursor = 2;   // pop cursor of the running persistent stage
+constexpr int kLen0 = 0;    // length of queue 0 (queue 1's length is slot 1)
+constexpr int kCursor = 2;  // pop cursor of the running persistent stage
 
 template <int kKind>
 __device__ __forceinline__ void load_rng(const uint4 *rng, uint32_t pid, Rng &r) {
@@ -44,17 +46,15 @@ __device__ __forceinline__ void queue_push(uint32_t *queue, unsigned long long *
     if (active) queue[base + __popc(mask & ((1u << lane) - 1u))] = value;
 }
 
+// RenderPixel's start of a sample (CPURenderer.cpp:398-406, 436-444): reseed, jitter, camera ray.
 template <int kKind>
-__global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers fb, RenderParams p, WavefrontState s,
-                                                     Counters *counters) {
-    const uint32_t i = blockIdx.x * 16u + (threadIdx.x & 15u);
-    const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 4);
-    if (i >= fb.width || j >= fb.height) return;
-    const uint32_t pid = j * fb.width + i;
+__device__ __forceinline__ void start_path(const DevCamera &cam, const RenderParams &p, const WavefrontState &s,
+                                           uint32_t pid, uint32_t i, uint32_t j, uint32_t w, uint32_t h,
+                                           uint32_t frame_seed) {
     Rng rng;
-    rng_seed_pixel<kKind>(rng, p.seed, i, j, fb.width, fb.height, p.frame_seed);
-    const float pw = 1.f / static_cast<float>(fb.width - 1);
-    const float ph = 1.f / static_cast<float>(fb.height - 1);
+    rng_seed_pixel<kKind>(rng, p.seed, i, j, w, h, frame_seed);
+    const float pw = 1.f / static_cast<float>(w - 1);
+    const float ph = 1.f / static_cast<float>(h - 1);
     const float u = (static_cast<float>(i) + rng_unit<kKind>(rng)) * pw;
     const float v = (static_cast<float>(j) + rng_unit<kKind>(rng)) * ph;
     f3 o, d;
@@ -64,6 +64,78 @@ __global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers
     s.thr[pid] = make_float4(1.f, 1.f, 1.f, 0.f);
     s.color[pid] = make_float4(0.f, 0.f, 0.f, 1.f);
     store_rng<kKind>(s.rng, pid, rng);
+}
+
+// One bounce of SamplePixel's loop body (CPURenderer.cpp:261-368) for path `pid` whose closest hit is
+// in s.hit: sky on a miss, emission, BSDF sample, throughput cut-off, Russian roulette. Returns whether
+// the path continues (the next ray is then in s.ray_o / s.ray_d).
+template <int kKind>
+__device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontState &s, uint32_t pid,
+                                           uint32_t bounce, float4 *gnormal) {
+    bool alive = false;
+    const float4 hit4 = s.hit[pid];
+    const uint32_t inst = __float_as_uint(hit4.w);
+    const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
+    const f3 o = mk3(o4.x, o4.y, o4.z), d = mk3(d4.x, d4.y, d4.z);
+    const float4 c4 = s.color[pid];
+    f3 color = mk3(c4.x, c4.y, c4.z);
+    const float4 t4 = s.thr[pid];
+    f3 thr = mk3(t4.x, t4.y, t4.z);
+    float valid = c4.w;
+    if (inst == kInvalid) {
+        if (S.sky_mode != 0u) color = color + cmul(sky_eval(S, d), thr);
+    } else {
+        const TraceResult h{hit4.x, hit4.y, hit4.z, inst, s.hit_face[pid]};
+        const Surface surf = make_surface(S, h, o, d);
+        const DevMaterial mat = S.materials[surf.material];
+        if (bounce == 0 && gnormal) gnormal[pid] = make_float4(surf.normal.x, surf.normal.y, surf.normal.z, 0.f);
+        if (mat.is_emissive) {
+            color = color + cmul(mk3(mat.emissive[0], mat.emissive[1], mat.emissive[2]), thr);
+        } else {
+            Rng rng;
+            load_rng<kKind>(s.rng, pid, rng);
+            f3 next_dir;
+            const f3 this_thr = sample_surface<kKind>(rng, mat, d, surf.normal, surf.tangent, next_dir);
+            thr = cmul(thr, this_thr);
+            if (sqnorm(thr) < kEps) {
+                valid = -1.f;
+            } else {
+                bool survive = true;
+                if (bounce >= 3) {
+                    float pr = max_std(thr.x, max_std(thr.y, thr.z));
+                    pr = (pr < 0.05f) ? 0.05f : (1.0f < pr) ? 1.0f : pr;
+                    if (rng_unit<kKind>(rng) > pr) {
+                        survive = false;
+                    } else {
+                        thr = mk3(thr.x / pr, thr.y / pr, thr.z / pr);
+                    }
+                }
+                if (survive) {
+                    const f3 no = surf.location + next_dir * kTolerance;
+                    s.ray_o[pid] = make_float4(no.x, no.y, no.z, 0.f);
+                    s.ray_d[pid] = make_float4(next_dir.x, next_dir.y, next_dir.z, 0.f);
+                    alive = true;
+                }
+            }
+            store_rng<kKind>(s.rng, pid, rng);
+            s.thr[pid] = make_float4(thr.x, thr.y, thr.z, 0.f);
+        }
+    }
+    s.color[pid] = make_float4(color.x, color.y, color.z, valid);
+    return alive;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Frame-by-frame schedule
+// ------------------------------------------------------------------------------------------------
+template <int kKind>
+__global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers fb, RenderParams p, WavefrontState s,
+                                                     Counters *counters) {
+    const uint32_t i = blockIdx.x * 16u + (threadIdx.x & 15u);
+    const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 4);
+    if (i >= fb.width || j >= fb.height) return;
+    const uint32_t pid = j * fb.width + i;
+    start_path<kKind>(cam, p, s, pid, i, j, fb.width, fb.height, p.frame_seed);
     if (p.spatial_denoise) fb.gnormal[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
     s.queue[0][pid] = pid;
     if (pid == 0) counters->queue_counters[kLen0] = static_cast<unsigned long long>(fb.width) * fb.height;
@@ -112,56 +184,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(DevScene S, FrameBuffers fb, R
         uint32_t pid = 0;
         if (q < n) {
             pid = queue[q];
-            const float4 hit4 = s.hit[pid];
-            const uint32_t inst = __float_as_uint(hit4.w);
-            const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
-            const f3 o = mk3(o4.x, o4.y, o4.z), d = mk3(d4.x, d4.y, d4.z);
-            float4 c4 = s.color[pid];
-            f3 color = mk3(c4.x, c4.y, c4.z);
-            const float4 t4 = s.thr[pid];
-            f3 thr = mk3(t4.x, t4.y, t4.z);
-            float valid = c4.w;
-            if (inst == kInvalid) {
-                if (S.sky_mode != 0u) color = color + cmul(sky_eval(S, d), thr);
-            } else {
-                const TraceResult h{hit4.x, hit4.y, hit4.z, inst, s.hit_face[pid]};
-                const Surface surf = make_surface(S, h, o, d);
-                const DevMaterial mat = S.materials[surf.material];
-                if (bounce == 0 && p.spatial_denoise)
-                    fb.gnormal[pid] = make_float4(surf.normal.x, surf.normal.y, surf.normal.z, 0.f);
-                if (mat.is_emissive) {
-                    color = color + cmul(mk3(mat.emissive[0], mat.emissive[1], mat.emissive[2]), thr);
-                } else {
-                    Rng rng;
-                    load_rng<kKind>(s.rng, pid, rng);
-                    f3 next_dir;
-                    const f3 this_thr = sample_surface<kKind>(rng, mat, d, surf.normal, surf.tangent, next_dir);
-                    thr = cmul(thr, this_thr);
-                    if (sqnorm(thr) < kEps) {
-                        valid = -1.f;
-                    } else {
-                        bool survive = true;
-                        if (bounce >= 3) {
-                            float pr = max_std(thr.x, max_std(thr.y, thr.z));
-                            pr = (pr < 0.05f) ? 0.05f : (1.0f < pr) ? 1.0f : pr;
-                            if (rng_unit<kKind>(rng) > pr) {
-                                survive = false;
-                            } else {
-                                thr = mk3(thr.x / pr, thr.y / pr, thr.z / pr);
-                            }
-                        }
-                        if (survive) {
-                            const f3 no = surf.location + next_dir * kTolerance;
-                            s.ray_o[pid] = make_float4(no.x, no.y, no.z, 0.f);
-                            s.ray_d[pid] = make_float4(next_dir.x, next_dir.y, next_dir.z, 0.f);
-                            alive = true;
-                        }
-                    }
-                    store_rng<kKind>(s.rng, pid, rng);
-                    s.thr[pid] = make_float4(thr.x, thr.y, thr.z, 0.f);
-                }
-            }
-            s.color[pid] = make_float4(color.x, color.y, color.z, valid);
+            alive = shade_path<kKind>(S, s, pid, bounce, p.spatial_denoise ? fb.gnormal : nullptr);
         }
         queue_push(s.queue[out_queue], &counters->queue_counters[out_queue], pid, alive && bounce + 1 < p.bounce);
     }
@@ -174,9 +197,116 @@ __global__ void __launch_bounds__(256) k_wf_finish(FrameBuffers fb, WavefrontSta
     fb.gcolor[pid] = make_float4(min_std(c.x, kOutputLimit), min_std(c.y, kOutputLimit), min_std(c.z, kOutputLimit), c.w);
 }
 
+// ------------------------------------------------------------------------------------------------
+// Multi-frame schedule with path regeneration
+// ------------------------------------------------------------------------------------------------
+template <int kKind>
+__global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers fb, RenderParams p,
+                                                     WavefrontState s, Counters *counters) {
+    const uint32_t i = blockIdx.x * 16u + (threadIdx.x & 15u);
+    const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 4);
+    if (i >= fb.width || j >= fb.height) return;
+    const uint32_t pid = j * fb.width + i;
+    start_path<kKind>(cam, p, s, pid, i, j, fb.width, fb.height, s.frame_seed[0]);
+    s.slot_state[pid] = 0u;
+    s.queue[0][pid] = pid;
+    if (pid == 0) counters->queue_counters[kLen0] = static_cast<unsigned long long>(fb.width) * fb.height;
+}
+
+// Shade; a finished sample is folded into the frame buffer with its frame's weight
+// (fb = new + (fb - new) * w_k, CPURenderer.cpp:534-543, after the 6.0 clamp of RenderPixel :408) and the
+// pixel's next sample starts in the same slot.
+template <int kKind>
+__global__ void __launch_bounds__(128) k_mf_shade(DevScene S, DevCamera cam, FrameBuffers fb, RenderParams p,
+                                                  WavefrontState s, int in_queue, uint32_t num_frames,
+                                                  Counters *counters) {
+    const unsigned long long n = counters->queue_counters[in_queue];
+    const int out_queue = in_queue ^ 1;
+    const uint32_t *queue = s.queue[in_queue];
+    for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
+         q0 += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+        const unsigned long long q = q0 + threadIdx.x;
+        bool push = false;
+        uint32_t pid = 0;
+        if (q < n) {
+            pid = queue[q];
+            const uint32_t st = s.slot_state[pid];
+            const uint32_t bounce = st & 0xFFu;
+            uint32_t k = st >> 8;
+            const bool alive = shade_path<kKind>(S, s, pid, bounce, nullptr) && bounce + 1 < p.bounce;
+            if (alive) {
+                s.slot_state[pid] = (k << 8) | (bounce + 1u);
+                push = true;
+            } else {
+                const float4 c = s.color[pid];
+                const float nx = min_std(c.x, kOutputLimit), ny = min_std(c.y, kOutputLimit);
+                const float nz = min_std(c.z, kOutputLimit), nw = c.w;
+                const float f = s.frame_weight[k];
+                const float4 a = fb.fb[pid];
+                fb.fb[pid] = make_float4(nx + (a.x - nx) * f, ny + (a.y - ny) * f, nz + (a.z - nz) * f, nw + (a.w - nw) * f);
+                ++k;
+                if (k < num_frames) {
+                    const uint32_t i = pid % fb.width, j = pid / fb.width;
+                    start_path<kKind>(cam, p, s, pid, i, j, fb.width, fb.height, s.frame_seed[k]);
+                    s.slot_state[pid] = k << 8;
+                    push = true;
+                }
+            }
+        }
+        queue_push(s.queue[out_queue], &counters->queue_counters[out_queue], pid, push);
+    }
+}
+
+__device__ __forceinline__ float aces_tonemap(float c, float exposure) {
+    const float x = c * exposure;
+    float y = (x * (x * 2.51f + 0.03f)) / (x * (x * 2.43f + 0.59f) + 0.14f);
+    y = (1.f < y) ? 1.f : y;
+    y = (y < 0.f) ? 0.f : y;
+    return y;
+}
+
+// ToneMappingPass of the final frame buffer (CPURenderer.cpp:554-576).
+__global__ void __launch_bounds__(256) k_tonemap(FrameBuffers fb, float exposure) {
+    const uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pid >= fb.width * fb.height) return;
+    const uint32_t i = pid % fb.width, j = pid / fb.width;
+    const float4 a = fb.fb[pid];
+    ushort4 o;
+    o.x = __half_as_ushort(__float2half_rn(aces_tonemap(a.x, exposure)));
+    o.y = __half_as_ushort(__float2half_rn(aces_tonemap(a.y, exposure)));
+    o.z = __half_as_ushort(__float2half_rn(aces_tonemap(a.z, exposure)));
+    o.w = __half_as_ushort(__float2half_rn(1.f));
+    fb.out[static_cast<size_t>(fb.height - 1 - j) * fb.width + i] = o;
+}
+
 template <class T>
 cudaError_t dmalloc(T *&p, size_t count) {
     return cudaMalloc(reinterpret_cast<void **>(&p), count * sizeof(T));
+}
+
+unsigned extend_blocks(int num_sms) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_extend<false>, 128, 0) != cudaSuccess ||
+            per_sm <= 0)
+            per_sm = 8;
+    }
+    return static_cast<unsigned>(num_sms * per_sm);
+}
+
+cudaError_t launch_extend(const DevScene &scene, WavefrontState &s, int in, bool count, Counters *counters,
+                          int num_sms, cudaStream_t stream, LaunchEvents *ev) {
+    unsigned long long *qc = counters->queue_counters;
+    cudaError_t e = cudaMemsetAsync(qc + kCursor, 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    if (ev) ev->before(stream);
+    if (count) {
+        k_wf_extend<true><<<extend_blocks(num_sms), 128, 0, stream>>>(scene, s, in, counters);
+    } else {
+        k_wf_extend<false><<<extend_blocks(num_sms), 128, 0, stream>>>(scene, s, in, counters);
+    }
+    if (ev) ev->after(stream);
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -189,7 +319,9 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
         (e = dmalloc(s.rng, 2 * static_cast<size_t>(capacity))) != cudaSuccess ||
         (e = dmalloc(s.hit, capacity)) != cudaSuccess || (e = dmalloc(s.hit_face, capacity)) != cudaSuccess ||
         (e = dmalloc(s.queue[0], capacity)) != cudaSuccess || (e = dmalloc(s.queue[1], capacity)) != cudaSuccess ||
-        (e = dmalloc(s.sort_keys, capacity)) != cudaSuccess) {
+        (e = dmalloc(s.sort_keys, capacity)) != cudaSuccess || (e = dmalloc(s.slot_state, capacity)) != cudaSuccess ||
+        (e = cudaHostAlloc(reinterpret_cast<void **>(&s.host_len), sizeof(unsigned long long), cudaHostAllocDefault)) !=
+            cudaSuccess) {
         wavefront_free(s);
         return e;
     }
@@ -198,9 +330,11 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
 }
 
 void wavefront_free(WavefrontState &s) {
-    void *ptrs[] = {s.ray_o, s.ray_d, s.thr, s.color, s.rng, s.hit, s.hit_face, s.queue[0], s.queue[1], s.sort_keys};
+    void *ptrs[] = {s.ray_o,    s.ray_d,    s.thr,       s.color,      s.rng,          s.hit,       s.hit_face,
+                    s.queue[0], s.queue[1], s.sort_keys, s.slot_state, s.frame_weight, s.frame_seed};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    if (s.host_len) cudaFreeHost(s.host_len);
     s = WavefrontState{};
 }
 
@@ -220,19 +354,11 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
         k_wf_generate<1><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, counters);
     }
     ++nl;
-    const unsigned persist_blocks = static_cast<unsigned>(num_sms) * 12u;
     const unsigned shade_blocks = static_cast<unsigned>(num_sms) * 8u;
     for (uint32_t b = 0; b < p.bounce; ++b) {
         const int in = static_cast<int>(b & 1u), out = in ^ 1;
         if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
-        if ((e = cudaMemsetAsync(qc + kCursor, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
-        if (ev) ev->before(stream);
-        if (count) {
-            k_wf_extend<true><<<persist_blocks, 128, 0, stream>>>(scene, s, in, counters);
-        } else {
-            k_wf_extend<false><<<persist_blocks, 128, 0, stream>>>(scene, s, in, counters);
-        }
-        if (ev) ev->after(stream);
+        if ((e = launch_extend(scene, s, in, count, counters, num_sms, stream, ev)) != cudaSuccess) return e;
         ++nl;
         if (p.rng == 0) {
             k_wf_shade<0><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
@@ -242,6 +368,70 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
         ++nl;
     }
     k_wf_finish<<<(npix + 255) / 256, 256, 0, stream>>>(fbuf, s);
+    ++nl;
+    if (launches) *launches = nl;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
+                                     const RenderParams &p, uint32_t num_frames, const float *weights,
+                                     const uint32_t *seeds, bool count, Counters *counters, WavefrontState &s,
+                                     int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev) {
+    uint32_t nl = 0;
+    const uint32_t npix = fbuf.width * fbuf.height;
+    if (s.capacity < npix || num_frames == 0 || p.bounce == 0) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if (s.frame_capacity < num_frames) {
+        if (s.frame_weight) cudaFree(s.frame_weight);
+        if (s.frame_seed) cudaFree(s.frame_seed);
+        s.frame_weight = nullptr;
+        s.frame_seed = nullptr;
+        s.frame_capacity = 0;
+        if ((e = dmalloc(s.frame_weight, num_frames)) != cudaSuccess) return e;
+        if ((e = dmalloc(s.frame_seed, num_frames)) != cudaSuccess) return e;
+        s.frame_capacity = num_frames;
+    }
+    if ((e = cudaMemcpyAsync(s.frame_weight, weights, num_frames * sizeof(float), cudaMemcpyHostToDevice, stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(s.frame_seed, seeds, num_frames * sizeof(uint32_t), cudaMemcpyHostToDevice, stream)) !=
+            cudaSuccess)
+        return e;
+    unsigned long long *qc = counters->queue_counters;
+    if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
+    const dim3 ggrid((fbuf.width + 15) / 16, (fbuf.height + 7) / 8);
+    if (p.rng == 0) {
+        k_mf_generate<0><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, counters);
+    } else {
+        k_mf_generate<1><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, counters);
+    }
+    ++nl;
+    const unsigned shade_blocks = static_cast<unsigned>(num_sms) * 8u;
+    // Every iteration advances each live slot by one segment, so the loop ends within frames * bounce
+    // iterations; the queue length is read back every `kChunk` iterations.
+    constexpr uint32_t kChunk = 8;
+    const uint64_t max_iters = static_cast<uint64_t>(num_frames) * p.bounce + kChunk;
+    uint64_t iter = 0;
+    for (;;) {
+        for (uint32_t c = 0; c < kChunk; ++c, ++iter) {
+            const int in = static_cast<int>(iter & 1u), out = in ^ 1;
+            if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
+            if ((e = launch_extend(scene, s, in, count, counters, num_sms, stream, ev)) != cudaSuccess) return e;
+            if (p.rng == 0) {
+                k_mf_shade<0><<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, s, in, num_frames, counters);
+            } else {
+                k_mf_shade<1><<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, s, in, num_frames, counters);
+            }
+            nl += 2;
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = cudaMemcpyAsync(s.host_len, qc + (iter & 1u), sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                 stream)) != cudaSuccess)
+            return e;
+        if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
+        if (*s.host_len == 0) break;
+        if (iter > max_iters) return cudaErrorLaunchFailure;  // cannot happen: every slot makes progress
+    }
+    k_tonemap<<<(npix + 255) / 256, 256, 0, stream>>>(fbuf, cam.exposure);
     ++nl;
     if (launches) *launches = nl;
     return cudaGetLastError();

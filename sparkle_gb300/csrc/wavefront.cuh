@@ -23,10 +23,27 @@ struct WavefrontState {
     uint32_t *hit_face = nullptr;
     uint32_t *queue[2] = {nullptr, nullptr};  // path indices
     uint32_t *sort_keys = nullptr;            // material-sort scratch
+    uint32_t *slot_state = nullptr;           // multi-frame mode: (sample index << 8) | bounce, per pixel
+    // multi-frame mode: per-frame constants, frame k of the call
+    float *frame_weight = nullptr;      // DenoisePass moving-average weight of frame k
+    uint32_t *frame_seed = nullptr;     // dispatched sample count at frame k (per-pixel seed base)
+    uint32_t frame_capacity = 0;
+    unsigned long long *host_len = nullptr;  // pinned: queue length read back between iteration chunks
 };
 
 cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity);
 void wavefront_free(WavefrontState &s);
+
+// All `num_frames` frames of a call in one wavefront with path regeneration (valid when the spatial
+// DenoisePass is off, so pixels do not interact within a frame): a slot whose path ends folds its sample
+// into the frame buffer with that frame's weight (CPURenderer.cpp:530-543) and starts the pixel's next
+// sample. Per pixel the samples still run in frame order with the same seeds, so the frame buffer is
+// bit-identical to rendering the frames one by one. `weights[k]` / `seeds[k]` are frame k's
+// moving-average weight and seed base. Ends with the tonemap of the final frame buffer.
+cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
+                                     const RenderParams &p, uint32_t num_frames, const float *weights,
+                                     const uint32_t *seeds, bool count, Counters *counters, WavefrontState &s,
+                                     int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev);
 
 cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
                                     const RenderParams &p, bool count, Counters *counters, WavefrontState &s,

@@ -115,17 +115,26 @@ def test_converged_cornell_relmse(ctx, cornell):
     assert rm < 1e-4
 
 
-def test_accumulation_cap_and_reset(ctx, cornell):
-    """max_spp caps the cumulated count (then the lerp becomes an EMA); a camera change clears."""
+@pytest.mark.parametrize("kernel", [abi.SPK_KERNEL_MEGAKERNEL, abi.SPK_KERNEL_WAVEFRONT])
+def test_accumulation_cap_and_reset(ctx, cornell, kernel):
+    """max_spp caps the cumulated count (then the lerp becomes an EMA); a camera change clears. Frames split
+    over several calls accumulate exactly like one call."""
     scene, cam_args = cornell
     W, H = 16, 16
     camera = scenes.make_camera(cam_args, W, H)
-    cfg = abi.make_config(W, H, spp=1, max_spp=3, bounce=3, kernel=abi.SPK_KERNEL_MEGAKERNEL)
-    gpu_render(ctx, scene, camera, cfg, 6)
+    cfg = abi.make_config(W, H, spp=1, max_spp=3, bounce=3, rng=abi.SPK_RNG_XOSHIRO256SS, kernel=kernel)
+    hdr6, _, _ = gpu_render(ctx, scene, camera, cfg, 6)
     r = oracle.OracleRenderer(oracle.OracleScene(scene), cfg, camera)
-    r.render(6)
+    r.render(6, traversal=oracle.PRUNED)
     assert ctx.sample_counts() == r.sample_counts() == (3, 6)
     assert ctx.is_converged()
+    o_hdr, _ = r.framebuffer()
+    assert close_fraction(hdr6, o_hdr) >= 0.9
+    ctx.set_camera(camera)
+    ctx.render(2)
+    ctx.render(4)
+    split, _ = ctx.framebuffer()
+    assert np.array_equal(split.view(np.uint32), hdr6.view(np.uint32))
     ctx.set_camera(camera)
     ctx.render(1)
     assert ctx.sample_counts() == (0, 1)
