@@ -3,6 +3,8 @@
 // Compiled with -fmad=false like kernels.cu so every path computes bit-identically to the one-kernel form.
 #include <cuda_fp16.h>
 
+#include <algorithm>
+
 #include "wavefront.cuh"
 
 namespace spk {
@@ -200,60 +202,79 @@ __global__ void __launch_bounds__(256) k_wf_finish(FrameBuffers fb, WavefrontSta
 // ------------------------------------------------------------------------------------------------
 // Multi-frame schedule with path regeneration
 // ------------------------------------------------------------------------------------------------
+constexpr int kNextItem = 3;  // queue_counters slot: next (frame, pixel) sample item to hand out
+
+// Slot `slot` starts sample item `item` = frame * pixels + pixel of the pass.
 template <int kKind>
-__global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers fb, RenderParams p,
-                                                     WavefrontState s, Counters *counters) {
-    const uint32_t i = blockIdx.x * 16u + (threadIdx.x & 15u);
-    const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 4);
-    if (i >= fb.width || j >= fb.height) return;
-    const uint32_t pid = j * fb.width + i;
-    start_path<kKind>(cam, p, s, pid, i, j, fb.width, fb.height, s.frame_seed[0]);
-    s.slot_state[pid] = 0u;
-    s.queue[0][pid] = pid;
-    if (pid == 0) counters->queue_counters[kLen0] = static_cast<unsigned long long>(fb.width) * fb.height;
+__device__ __forceinline__ void start_item(const DevCamera &cam, const RenderParams &p, const WavefrontState &s,
+                                           uint32_t slot, uint32_t item, uint32_t w, uint32_t h,
+                                           uint32_t frame_base) {
+    const uint32_t npix = w * h;
+    const uint32_t k = item / npix, pid = item - k * npix;
+    start_path<kKind>(cam, p, s, slot, pid % w, pid / w, w, h, s.frame_seed[frame_base + k]);
+    s.slot_item[slot] = item;
+    s.slot_state[slot] = 0u;
 }
 
-// Shade; a finished sample is folded into the frame buffer with its frame's weight
-// (fb = new + (fb - new) * w_k, CPURenderer.cpp:534-543, after the 6.0 clamp of RenderPixel :408) and the
-// pixel's next sample starts in the same slot.
+template <int kKind>
+__global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers fb, RenderParams p,
+                                                     WavefrontState s, uint32_t frame_base, Counters *counters) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t npix = fb.width * fb.height;
+    if (slot >= npix) return;
+    start_item<kKind>(cam, p, s, slot, slot, fb.width, fb.height, frame_base);
+    s.queue[0][slot] = slot;
+    if (slot == 0) {
+        counters->queue_counters[kLen0] = npix;
+        counters->queue_counters[kNextItem] = npix;
+    }
+}
+
+// Shade one segment per live slot. A finished sample stores its clamped result (RenderPixel's 6.0 clamp,
+// CPURenderer.cpp:408) at its item, and the slot takes the next item from the global counter.
 template <int kKind>
 __global__ void __launch_bounds__(128) k_mf_shade(DevScene S, DevCamera cam, FrameBuffers fb, RenderParams p,
-                                                  WavefrontState s, int in_queue, uint32_t num_frames,
-                                                  Counters *counters) {
+                                                  WavefrontState s, int in_queue, uint32_t frame_base,
+                                                  uint32_t total_items, Counters *counters) {
     const unsigned long long n = counters->queue_counters[in_queue];
     const int out_queue = in_queue ^ 1;
     const uint32_t *queue = s.queue[in_queue];
+    const uint32_t lane = threadIdx.x & 31u;
     for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
          q0 += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
         const unsigned long long q = q0 + threadIdx.x;
-        bool push = false;
-        uint32_t pid = 0;
+        bool push = false, need = false;
+        uint32_t slot = 0;
         if (q < n) {
-            pid = queue[q];
-            const uint32_t st = s.slot_state[pid];
-            const uint32_t bounce = st & 0xFFu;
-            uint32_t k = st >> 8;
-            const bool alive = shade_path<kKind>(S, s, pid, bounce, nullptr) && bounce + 1 < p.bounce;
+            slot = queue[q];
+            const uint32_t bounce = s.slot_state[slot];
+            const bool alive = shade_path<kKind>(S, s, slot, bounce, nullptr) && bounce + 1 < p.bounce;
             if (alive) {
-                s.slot_state[pid] = (k << 8) | (bounce + 1u);
+                s.slot_state[slot] = bounce + 1u;
                 push = true;
             } else {
-                const float4 c = s.color[pid];
-                const float nx = min_std(c.x, kOutputLimit), ny = min_std(c.y, kOutputLimit);
-                const float nz = min_std(c.z, kOutputLimit), nw = c.w;
-                const float f = s.frame_weight[k];
-                const float4 a = fb.fb[pid];
-                fb.fb[pid] = make_float4(nx + (a.x - nx) * f, ny + (a.y - ny) * f, nz + (a.z - nz) * f, nw + (a.w - nw) * f);
-                ++k;
-                if (k < num_frames) {
-                    const uint32_t i = pid % fb.width, j = pid / fb.width;
-                    start_path<kKind>(cam, p, s, pid, i, j, fb.width, fb.height, s.frame_seed[k]);
-                    s.slot_state[pid] = k << 8;
+                const float4 c = s.color[slot];
+                s.samples[s.slot_item[slot]] =
+                    make_float4(min_std(c.x, kOutputLimit), min_std(c.y, kOutputLimit), min_std(c.z, kOutputLimit), c.w);
+                need = true;
+            }
+        }
+        // Warp-aggregated hand-out of new sample items to the lanes whose path ended.
+        const uint32_t need_mask = __ballot_sync(0xFFFFFFFFu, need);
+        if (need_mask) {
+            unsigned long long base = 0;
+            if (lane == static_cast<uint32_t>(__ffs(need_mask) - 1))
+                base = atomicAdd(&counters->queue_counters[kNextItem], static_cast<unsigned long long>(__popc(need_mask)));
+            base = __shfl_sync(0xFFFFFFFFu, base, __ffs(need_mask) - 1);
+            if (need) {
+                const unsigned long long item = base + __popc(need_mask & ((1u << lane) - 1u));
+                if (item < total_items) {
+                    start_item<kKind>(cam, p, s, slot, static_cast<uint32_t>(item), fb.width, fb.height, frame_base);
                     push = true;
                 }
             }
         }
-        queue_push(s.queue[out_queue], &counters->queue_counters[out_queue], pid, push);
+        queue_push(s.queue[out_queue], &counters->queue_counters[out_queue], slot, push);
     }
 }
 
@@ -265,12 +286,21 @@ __device__ __forceinline__ float aces_tonemap(float c, float exposure) {
     return y;
 }
 
-// ToneMappingPass of the final frame buffer (CPURenderer.cpp:554-576).
-__global__ void __launch_bounds__(256) k_tonemap(FrameBuffers fb, float exposure) {
+// DenoisePass temporal lerp of every sample of the pass, in frame order per pixel
+// (fb = new + (fb - new) * w_k, CPURenderer.cpp:534-543), then ToneMappingPass (:554-576).
+__global__ void __launch_bounds__(256) k_mf_resolve(FrameBuffers fb, WavefrontState s, uint32_t frame_base,
+                                                    uint32_t frames, float exposure) {
     const uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pid >= fb.width * fb.height) return;
+    const uint32_t npix = fb.width * fb.height;
+    if (pid >= npix) return;
+    float4 a = fb.fb[pid];
+    for (uint32_t k = 0; k < frames; ++k) {
+        const float4 n = s.samples[static_cast<size_t>(k) * npix + pid];
+        const float f = s.frame_weight[frame_base + k];
+        a = make_float4(n.x + (a.x - n.x) * f, n.y + (a.y - n.y) * f, n.z + (a.z - n.z) * f, n.w + (a.w - n.w) * f);
+    }
+    fb.fb[pid] = a;
     const uint32_t i = pid % fb.width, j = pid / fb.width;
-    const float4 a = fb.fb[pid];
     ushort4 o;
     o.x = __half_as_ushort(__float2half_rn(aces_tonemap(a.x, exposure)));
     o.y = __half_as_ushort(__float2half_rn(aces_tonemap(a.y, exposure)));
@@ -320,6 +350,7 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
         (e = dmalloc(s.hit, capacity)) != cudaSuccess || (e = dmalloc(s.hit_face, capacity)) != cudaSuccess ||
         (e = dmalloc(s.queue[0], capacity)) != cudaSuccess || (e = dmalloc(s.queue[1], capacity)) != cudaSuccess ||
         (e = dmalloc(s.sort_keys, capacity)) != cudaSuccess || (e = dmalloc(s.slot_state, capacity)) != cudaSuccess ||
+        (e = dmalloc(s.slot_item, capacity)) != cudaSuccess ||
         (e = cudaHostAlloc(reinterpret_cast<void **>(&s.host_len), sizeof(unsigned long long), cudaHostAllocDefault)) !=
             cudaSuccess) {
         wavefront_free(s);
@@ -330,8 +361,9 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
 }
 
 void wavefront_free(WavefrontState &s) {
-    void *ptrs[] = {s.ray_o,    s.ray_d,    s.thr,       s.color,      s.rng,          s.hit,       s.hit_face,
-                    s.queue[0], s.queue[1], s.sort_keys, s.slot_state, s.frame_weight, s.frame_seed};
+    void *ptrs[] = {s.ray_o,      s.ray_d,     s.thr,     s.color,        s.rng,        s.hit,
+                    s.hit_face,   s.queue[0],  s.queue[1], s.sort_keys,   s.slot_state, s.slot_item,
+                    s.samples,    s.frame_weight, s.frame_seed};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s.host_len) cudaFreeHost(s.host_len);
@@ -391,48 +423,62 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
         if ((e = dmalloc(s.frame_seed, num_frames)) != cudaSuccess) return e;
         s.frame_capacity = num_frames;
     }
+    const uint32_t pass_frames = std::min(num_frames, kFramesPerPass);
+    const size_t need = static_cast<size_t>(pass_frames) * npix;
+    if (s.sample_capacity < need) {
+        if (s.samples) cudaFree(s.samples);
+        s.samples = nullptr;
+        s.sample_capacity = 0;
+        if ((e = dmalloc(s.samples, need)) != cudaSuccess) return e;
+        s.sample_capacity = need;
+    }
     if ((e = cudaMemcpyAsync(s.frame_weight, weights, num_frames * sizeof(float), cudaMemcpyHostToDevice, stream)) !=
             cudaSuccess ||
         (e = cudaMemcpyAsync(s.frame_seed, seeds, num_frames * sizeof(uint32_t), cudaMemcpyHostToDevice, stream)) !=
             cudaSuccess)
         return e;
     unsigned long long *qc = counters->queue_counters;
-    if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
-    const dim3 ggrid((fbuf.width + 15) / 16, (fbuf.height + 7) / 8);
-    if (p.rng == 0) {
-        k_mf_generate<0><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, counters);
-    } else {
-        k_mf_generate<1><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, counters);
-    }
-    ++nl;
     const unsigned shade_blocks = static_cast<unsigned>(num_sms) * 8u;
-    // Every iteration advances each live slot by one segment, so the loop ends within frames * bounce
-    // iterations; the queue length is read back every `kChunk` iterations.
     constexpr uint32_t kChunk = 8;
-    const uint64_t max_iters = static_cast<uint64_t>(num_frames) * p.bounce + kChunk;
-    uint64_t iter = 0;
-    for (;;) {
-        for (uint32_t c = 0; c < kChunk; ++c, ++iter) {
-            const int in = static_cast<int>(iter & 1u), out = in ^ 1;
-            if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
-            if ((e = launch_extend(scene, s, in, count, counters, num_sms, stream, ev)) != cudaSuccess) return e;
-            if (p.rng == 0) {
-                k_mf_shade<0><<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, s, in, num_frames, counters);
-            } else {
-                k_mf_shade<1><<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, s, in, num_frames, counters);
-            }
-            nl += 2;
+    for (uint32_t f0 = 0; f0 < num_frames; f0 += kFramesPerPass) {
+        const uint32_t frames = std::min(kFramesPerPass, num_frames - f0);
+        const uint32_t total_items = frames * npix;
+        if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
+        if (p.rng == 0) {
+            k_mf_generate<0><<<(npix + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, counters);
+        } else {
+            k_mf_generate<1><<<(npix + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, counters);
         }
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        if ((e = cudaMemcpyAsync(s.host_len, qc + (iter & 1u), sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                                 stream)) != cudaSuccess)
-            return e;
-        if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
-        if (*s.host_len == 0) break;
-        if (iter > max_iters) return cudaErrorLaunchFailure;  // cannot happen: every slot makes progress
+        ++nl;
+        // Each iteration advances every live slot by one segment and no item is started twice, so the
+        // pass ends within frames * bounce iterations; the queue length is read back every kChunk.
+        const uint64_t max_iters = static_cast<uint64_t>(frames) * p.bounce + kChunk;
+        uint64_t iter = 0;
+        for (;;) {
+            for (uint32_t c = 0; c < kChunk; ++c, ++iter) {
+                const int in = static_cast<int>(iter & 1u), out = in ^ 1;
+                if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
+                if ((e = launch_extend(scene, s, in, count, counters, num_sms, stream, ev)) != cudaSuccess) return e;
+                if (p.rng == 0) {
+                    k_mf_shade<0><<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, s, in, f0, total_items,
+                                                                    counters);
+                } else {
+                    k_mf_shade<1><<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, s, in, f0, total_items,
+                                                                    counters);
+                }
+                nl += 2;
+            }
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            if ((e = cudaMemcpyAsync(s.host_len, qc + (iter & 1u), sizeof(unsigned long long),
+                                     cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
+                return e;
+            if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
+            if (*s.host_len == 0) break;
+            if (iter > max_iters) return cudaErrorLaunchFailure;  // cannot happen: every slot makes progress
+        }
+        k_mf_resolve<<<(npix + 255) / 256, 256, 0, stream>>>(fbuf, s, f0, frames, cam.exposure);
+        ++nl;
     }
-    k_tonemap<<<(npix + 255) / 256, 256, 0, stream>>>(fbuf, cam.exposure);
-    ++nl;
     if (launches) *launches = nl;
     return cudaGetLastError();
 }

@@ -23,7 +23,10 @@ struct WavefrontState {
     uint32_t *hit_face = nullptr;
     uint32_t *queue[2] = {nullptr, nullptr};  // path indices
     uint32_t *sort_keys = nullptr;            // material-sort scratch
-    uint32_t *slot_state = nullptr;           // multi-frame mode: (sample index << 8) | bounce, per pixel
+    uint32_t *slot_state = nullptr;           // multi-frame mode: bounce of the slot's path
+    uint32_t *slot_item = nullptr;            // multi-frame mode: sample item (frame * pixels + pixel) of the slot
+    float4 *samples = nullptr;                // multi-frame mode: clamped result of each (frame, pixel) sample
+    size_t sample_capacity = 0;               // float4 entries of `samples`
     // multi-frame mode: per-frame constants, frame k of the call
     float *frame_weight = nullptr;      // DenoisePass moving-average weight of frame k
     uint32_t *frame_seed = nullptr;     // dispatched sample count at frame k (per-pixel seed base)
@@ -31,15 +34,20 @@ struct WavefrontState {
     unsigned long long *host_len = nullptr;  // pinned: queue length read back between iteration chunks
 };
 
+// Frames per multi-frame pass: bounds the per-sample result buffer to kFramesPerPass * pixels * 16 B.
+constexpr uint32_t kFramesPerPass = 64;
+
 cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity);
 void wavefront_free(WavefrontState &s);
 
 // All `num_frames` frames of a call in one wavefront with path regeneration (valid when the spatial
-// DenoisePass is off, so pixels do not interact within a frame): a slot whose path ends folds its sample
-// into the frame buffer with that frame's weight (CPURenderer.cpp:530-543) and starts the pixel's next
-// sample. Per pixel the samples still run in frame order with the same seeds, so the frame buffer is
-// bit-identical to rendering the frames one by one. `weights[k]` / `seeds[k]` are frame k's
-// moving-average weight and seed base. Ends with the tonemap of the final frame buffer.
+// DenoisePass is off, so pixels do not interact within a frame). Slots pull (frame, pixel) sample items
+// from a global counter in frame-major order; a slot whose path ends stores the sample's clamped result
+// and starts the next item, so every iteration keeps about one frame of paths in flight and only the
+// last few paths form a tail. A resolve pass then folds each pixel's samples into the frame buffer in
+// frame order with each frame's weight (CPURenderer.cpp:530-543), so the frame buffer is bit-identical
+// to rendering the frames one by one. `weights[k]` / `seeds[k]` are frame k's moving-average weight and
+// seed base. Ends with the tonemap of the final frame buffer.
 cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
                                      const RenderParams &p, uint32_t num_frames, const float *weights,
                                      const uint32_t *seeds, bool count, Counters *counters, WavefrontState &s,
