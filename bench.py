@@ -322,6 +322,27 @@ def run_profile_small(args):
     ctx.close()
 
 
+def run_profile_rays(args):
+    """ncu capture case for the ray-set walk: 4M random rays (origins uniform in the scene box, isotropic
+    directions) on the stress scene through spk_trace_device, twice."""
+    import torch
+    from sparkle_gb300 import native, scenes
+    scene, _ = scenes.terrain_spheres(0)
+    ctx = native.Context(0)
+    ctx.set_scene(scene)
+    n = 4 * 1024 * 1024
+    rays = torch.from_numpy(scenes.random_rays(*scene.world_bounds(), n, seed=21)).cuda()
+    hits = torch.empty((n, 5), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(2):
+        ctx.trace_device(rays.data_ptr(), n, hits.data_ptr())
+        st = ctx.stats()
+        assert st["error_flags"] == 0, st
+    print(json.dumps({"profile_rays": True, "rays": n, "device_ms": st["device_ms"],
+                      "mrays_per_s": n / st["device_ms"] / 1e3}))
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -332,8 +353,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-small", action="store_true",
                     help="ncu capture case: the same scene at 960x540, 2 frames, no timing output")
+    ap.add_argument("--profile-rays", action="store_true",
+                    help="ncu capture case: 4M random rays through spk_trace_device on the stress scene")
     args = ap.parse_args()
-    if args.profile_small:
+    if args.profile_rays:
+        run_profile_rays(args)
+    elif args.profile_small:
         run_profile_small(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -37,8 +37,18 @@ def _inputs():
     return files
 
 
+STAMP = os.path.join(OUT_DIR, "defines.txt")
+
+
+def _defines() -> str:
+    return os.environ.get("SPK_BUILD_DEFINES", "").strip()
+
+
 def _stale() -> bool:
     if not os.path.exists(LIB):
+        return True
+    built_with = open(STAMP).read().strip() if os.path.exists(STAMP) else ""
+    if built_with != _defines():
         return True
     t = os.path.getmtime(LIB)
     return any(os.path.getmtime(p) > t for p in _inputs())
@@ -58,6 +68,8 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     nv = nvcc()
     common = ["-O3", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-Xcompiler", "-fPIC,-ffp-contract=off"]
+    # Tunable overrides (e.g. "-DSPK_REFILL_LANES=16"), used by the autotuner's variant builds.
+    common += [d for d in os.environ.get("SPK_BUILD_DEFINES", "").split() if d.startswith("-D")]
     jobs = []
     objs = []
     for src in CUDA_SOURCES:
@@ -76,6 +88,8 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
         logs = list(ex.map(_run, jobs))
     _run([nv, *ARCH, "-shared", *objs, "-o", LIB + ".tmp", "-lpthread"])
     os.replace(LIB + ".tmp", LIB)
+    with open(STAMP, "w") as f:
+        f.write(_defines())
     if verbose_ptxas:
         print("\n".join(l for l in logs if l.strip()))
     return LIB

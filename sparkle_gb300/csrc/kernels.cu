@@ -13,7 +13,7 @@ namespace {
 // Ray-set query: persistent warps pull rays from a global counter and refill idle lanes.
 // ------------------------------------------------------------------------------------------------
 template <int kMode, bool kCount>
-__global__ void __launch_bounds__(128, 8) k_trace(DevScene S, const float *__restrict__ rays, uint64_t n,
+__global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_trace(DevScene S, const float *__restrict__ rays, uint64_t n,
                                                   spk_hit_dev *__restrict__ hits, Counters *counters) {
     uint32_t err = 0, done = 0;
     TraceCounts tc;

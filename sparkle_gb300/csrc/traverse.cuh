@@ -11,7 +11,8 @@
 // Differences from the reference walk that cannot change a closest hit: the reference never lowers the
 // ray's tmax (every box along the ray is visited); this walk prunes boxes that start beyond the current
 // best t plus a bound on the x-only world-t rounding error, and visits children in an octant order.
-// Only which of two hits with bit-identical t wins can differ (ties are order dependent).
+// Two hits with bit-identical t go to the smaller (instance, face) rather than to the first visited, so
+// the result never depends on the visit order (the reference's winner among exact ties does).
 // One deliberate difference: for a direction component with |d| <= FLT_EPSILON, bvh v2's fast slab test
 // uses 1/d = +-FLT_MAX and its -inv*org term overflows to +-inf once |org| > 1 on that axis, which culls
 // every box of the level; here that axis is tested as an exact containment test instead.
@@ -28,9 +29,33 @@ namespace spk {
 enum : int { kTraceClosest = 0, kTraceAnyRef = 1, kTraceOcclusion = 2 };
 enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOverflow = 4u };
 
+// Tunables (compile-time; the autotuner builds variants by defining them).
+#ifndef SPK_POSTPONE_LANES
+#define SPK_POSTPONE_LANES 8  // postpone triangle groups when fewer lanes than this want triangles
+#endif
+#ifndef SPK_REFILL_LANES
+#define SPK_REFILL_LANES 20  // persistent warps refill idle lanes once fewer than this are walking
+#endif
+#ifndef SPK_BYTE_CONVERT_PRMT
+#define SPK_BYTE_CONVERT_PRMT 0  // 1: quantised plane bytes to float with a byte permute + add
+#endif
+#ifndef SPK_WALK_MIN_BLOCKS
+#define SPK_WALK_MIN_BLOCKS 8  // resident 128-thread blocks per SM the walking kernels are compiled for
+#endif
+
 constexpr int kStackSize = 48;
 constexpr uint32_t kMaxIterations = 1u << 20;
-constexpr int kPostponeLanes = 8;  // postpone triangle groups when fewer lanes than this want triangles
+constexpr int kPostponeLanes = SPK_POSTPONE_LANES;
+
+// Byte `c` of `word` as a float (exact for 0..255).
+__device__ __forceinline__ float byte_to_float(uint32_t word, int c) {
+#if SPK_BYTE_CONVERT_PRMT
+    // 0x4B0000xx is 2^23 + xx; subtracting 2^23 is exact.
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7540u | static_cast<uint32_t>(c))) - 8388608.0f;
+#else
+    return static_cast<float>((word >> (8 * c)) & 0xFFu);
+#endif
+}
 
 struct TraceResult {
     float t, u, v;
@@ -95,12 +120,12 @@ __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
             const uint32_t m = (meta4 >> (8 * c)) & 0xFFu;
-            const float tnx = fmaf(static_cast<float>((nx >> (8 * c)) & 0xFFu), ax, ox);
-            const float tny = fmaf(static_cast<float>((ny >> (8 * c)) & 0xFFu), ay, oy);
-            const float tnz = fmaf(static_cast<float>((nz >> (8 * c)) & 0xFFu), az, oz);
-            const float tfx = fmaf(static_cast<float>((fx >> (8 * c)) & 0xFFu), ax, ox);
-            const float tfy = fmaf(static_cast<float>((fy >> (8 * c)) & 0xFFu), ay, oy);
-            const float tfz = fmaf(static_cast<float>((fz >> (8 * c)) & 0xFFu), az, oz);
+            const float tnx = fmaf(byte_to_float(nx, c), ax, ox);
+            const float tny = fmaf(byte_to_float(ny, c), ay, oy);
+            const float tnz = fmaf(byte_to_float(nz, c), az, oz);
+            const float tfx = fmaf(byte_to_float(fx, c), ax, ox);
+            const float tfy = fmaf(byte_to_float(fy, c), ay, oy);
+            const float tfz = fmaf(byte_to_float(fz, c), az, oz);
             const float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.f));
             const float t1 = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
             if (m != 0u && t0 <= t1) {
@@ -142,6 +167,14 @@ struct Walker {
         tmax_occl = tmax;
         tmax_box = (kMode == kTraceOcclusion) ? tmax : kFltMax;
         best = TraceResult{kFltMax, 0.f, 0.f, kInvalid, kInvalid};
+    }
+
+    // Candidate acceptance. The reference keeps the first of equal t (IntersectionCandidate::IsCloserHit is
+    // a strict <), which depends on the visit order; this walk's order depends on warp composition, so an
+    // exact tie goes to the smaller (instance, face) instead, making every hit independent of scheduling.
+    __device__ __forceinline__ bool closer(float t, uint32_t inst, uint32_t face) const {
+        if (t < best.t) return true;
+        return t == best.t && (inst < best.inst || (inst == best.inst && face < best.face));
     }
 
     __device__ __forceinline__ void push(uint2 *stack, uint2 v, uint32_t &err) {
@@ -211,12 +244,13 @@ struct Walker {
                 const float *M = S.instances[cur_inst].m;
                 const f3 wp = xform_point(M, ray.o + ray.d * t);
                 const float wt = (wp.x - wo.x) / wd.x;
-                if (wt > 0.f && wt < best.t) {
+                const uint32_t face = __float_as_uint(c4.y);
+                if (wt > 0.f && closer(wt, cur_inst, face)) {
                     best.t = wt;
                     best.u = u;
                     best.v = v;
                     best.inst = cur_inst;
-                    best.face = __float_as_uint(c4.y);
+                    best.face = face;
                     tmax_box = prune_limit(best.t, wo, wd, S.scene_abs_x);
                 }
             } else {
@@ -243,7 +277,7 @@ struct Walker {
                         }
                         continue;
                     }
-                    if (t > 0.f && t < best.t) {
+                    if (t > 0.f && closer(t, inst, kInvalid)) {
                         best.t = t;
                         best.u = 0.f;
                         best.v = 0.f;
@@ -292,7 +326,7 @@ __device__ __forceinline__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd
 // Persistent walk over a work list: each warp pulls batches of items from `cursor` and refills lanes whose
 // ray has finished once fewer than `kRefillLanes` lanes are still walking. `fetch(i, o, d)` loads item i's
 // ray; `finish(i, result)` stores its result. Every lane of every warp of the block must call this.
-constexpr int kRefillLanes = 20;
+constexpr int kRefillLanes = SPK_REFILL_LANES;
 
 template <int kMode, bool kCount, class Fetch, class Finish>
 __device__ __forceinline__ void walk_persistent(const DevScene &S, unsigned long long *cursor, unsigned long long n,

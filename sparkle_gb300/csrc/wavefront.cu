@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers
 
 // Extend: persistent warps pull paths from the queue, refilling lanes whose walk has finished.
 template <bool kCount>
-__global__ void __launch_bounds__(128, 8) k_wf_extend(DevScene S, WavefrontState s, int in_queue,
+__global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_wf_extend(DevScene S, WavefrontState s, int in_queue,
                                                       Counters *counters) {
     uint32_t err = 0, done = 0;
     TraceCounts tc;
