@@ -306,11 +306,11 @@ def run_ours(args):
 
 
 def run_profile_small(args):
-    """The stress scene (127 MB of nodes + triangles, larger than L2) rendered at 960x540 for 2 frames: the
-    case the ncu section captures run on (one kernel, a few launches, ~0.4 GB on the device)."""
+    """The bench workload cut to 2 frames (stress scene, 127 MB of nodes + triangles, larger than L2, at
+    1920x1080): the case the ncu captures run on (one kernel, a few launches, ~0.6 GB on the device)."""
     from sparkle_gb300 import abi, native, scenes
     scene, cam_args = scenes.terrain_spheres(0)
-    w, h = 960, 540
+    w, h = WIDTH, HEIGHT
     ctx = native.Context(0)
     ctx.set_scene(scene)
     ctx.set_config(abi.make_config(w, h, spp=1, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS, kernel=args.kernel))
@@ -352,7 +352,7 @@ def main():
     ap.add_argument("--kernel", type=int, default=0, help="0 auto, 1 megakernel, 2 wavefront")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-small", action="store_true",
-                    help="ncu capture case: the same scene at 960x540, 2 frames, no timing output")
+                    help="ncu capture case: the bench workload cut to 2 frames, no timing output")
     ap.add_argument("--profile-rays", action="store_true",
                     help="ncu capture case: 4M random rays through spk_trace_device on the stress scene")
     args = ap.parse_args()

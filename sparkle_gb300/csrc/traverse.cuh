@@ -39,6 +39,9 @@ enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOve
 #ifndef SPK_BYTE_CONVERT_PRMT
 #define SPK_BYTE_CONVERT_PRMT 0  // 1: quantised plane bytes to float with a byte permute + add
 #endif
+#ifndef SPK_POSTPONE_INNER
+#define SPK_POSTPONE_INNER 0  // 1: also postpone inside the triangle loop as lanes drop out of it
+#endif
 #ifndef SPK_WALK_MIN_BLOCKS
 #define SPK_WALK_MIN_BLOCKS 8  // resident 128-thread blocks per SM the walking kernels are compiled for
 #endif
@@ -209,6 +212,16 @@ struct Walker {
             ngroup = make_uint2(0u, 0u);
         }
         while (tgroup.y != 0u) {
+#if SPK_POSTPONE_INNER
+            // Lanes drop out of this loop as their triangles run out; once too few are left, the rest park
+            // their remaining triangles and rejoin the node walk (only when a node visit is pending, so
+            // the parked group cannot come straight back).
+            if (in_blas && ngroup.y > 0x00FFFFFFu && __popc(__activemask()) < kPostponeLanes) {
+                push(stack, tgroup, err);
+                tgroup.y = 0u;
+                break;
+            }
+#endif
             const uint32_t k = __ffs(tgroup.y) - 1;
             tgroup.y &= tgroup.y - 1u;
             const uint32_t idx = tgroup.x + k;
