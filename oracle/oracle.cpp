@@ -42,6 +42,7 @@ constexpr float kEps = 1e-6f;        // Types.h:54 Eps
 constexpr float kTolerance = 1e-4f;  // Types.h:55 Tolerance
 constexpr float kPi = 3.14159265358979323846f;  // std::numbers::pi_v<float> (Types.h:51)
 constexpr float kInvSqrt3 = 0.577350269189625764509f;  // std::numbers::inv_sqrt3_v<float> (Types.h:56)
+constexpr float kInvPi = 0.318309886183790671538f;     // std::numbers::inv_pi_v<float> (Types.h:52)
 constexpr float kOutputLimit = 6.f;  // CameraRenderProxy.h:16
 
 inline V3 mk(float x, float y, float z) { return {x, y, z}; }
@@ -452,6 +453,16 @@ struct or_scene {
     spk_sky sky{};
     std::vector<float> cube;
     float scene_abs_x = 0.f;  // max |x| of any world box, bounds the x-quirk error of world t
+    // Next-event estimation: emissive triangles in world space, their area CDF, and per-instance first
+    // light index (SPK_INVALID_ID when the instance does not emit).
+    struct Light {
+        V3 p0, e1, e2, ng, emission;
+        float area;
+    };
+    std::vector<Light> lights;
+    std::vector<float> light_cdf;
+    float light_total = 0.f;
+    std::vector<uint32_t> inst_light_base;
 };
 
 namespace {
@@ -559,6 +570,74 @@ int32_t intersect_scene(const or_scene &sc, V3 o, V3 d, Candidate &cand, bool pr
     };
     traverse<AnyHit>(sc.tlas, r, leaf, overflows);
     return hit_slot;
+}
+
+// Möller–Trumbore local t of a triangle, or -1 when the test fails (same operations as intersect_triangle).
+inline float triangle_t(const Tri &tri, V3 lo, V3 ld) {
+    const V3 h = cross(ld, tri.e2);
+    const float a = dot3(tri.e1, h);
+    if (std::abs(a) < kEps) return -1.f;
+    const V3 s = lo - tri.p0;
+    const float f = 1.f / a;
+    const float u = f * dot3(s, h);
+    if (u < 0.f || u > 1.f) return -1.f;
+    const V3 q = cross(s, tri.e1);
+    const float v = f * dot3(ld, q);
+    if (v < 0.f || u + v > 1.f) return -1.f;
+    const float t = f * dot3(tri.e2, q);
+    return t > kEps ? t : -1.f;
+}
+
+// Shadow-ray occlusion for next-event estimation (the GPU shader's IsRayOccluded with TMin/TMax,
+// ray_trace.cs.slang:105-116): any triangle with Eps < t < tmax (local t; affine maps keep the ray
+// parameter) or sphere root in (Eps, tmax), walking with early exit.
+bool occluded(const or_scene &sc, V3 o, V3 d, float tmax, uint64_t &overflows) {
+    TravRay r = make_trav_ray(o, d);
+    r.tmax = tmax;
+    bool hit = false;
+    auto leaf = [&](uint32_t b, uint32_t e) {
+        for (uint32_t i = b; i < e && !hit; ++i) {
+            const Inst &in = sc.insts[sc.tlas_slot[i]];
+            if (in.desc.type == SPK_PRIM_SPHERE) {
+                const V3 center = mk(in.desc.transform[3], in.desc.transform[7], in.desc.transform[11]);
+                const V3 co = o - center;
+                const float half_b = dot3(d, co);
+                const float c = sqnorm(co) - in.desc.radius * in.desc.radius;
+                const float disc = half_b * half_b - 1.f * c;
+                if (disc < 0) continue;
+                const float sq = std::sqrt(disc);
+                const float t = (-half_b + (c >= 0 ? -sq : sq)) / 1.f;
+                if (t > kEps && t < tmax) hit = true;
+            } else {
+                const MeshData &m = sc.meshes[in.desc.mesh_id];
+                const V3 lo = xform_point(in.Minv, o), ld = xform_dir(in.Minv, d);
+                TravRay lr = make_trav_ray(lo, ld);
+                lr.tmax = tmax;
+                auto tleaf = [&](uint32_t tb, uint32_t te) {
+                    for (uint32_t k = tb; k < te; ++k) {
+                        const float t = triangle_t(m.tris[m.bvh.prim_ids[k]], lo, ld);
+                        if (t > kEps && t < tmax) {
+                            hit = true;
+                            break;
+                        }
+                    }
+                    return hit;
+                };
+                traverse<true>(m.bvh, lr, tleaf, overflows);
+            }
+        }
+        return hit;
+    };
+    traverse<true>(sc.tlas, r, leaf, overflows);
+    return hit;
+}
+
+// GetMISWeight (power heuristic, ray_trace.cs.slang:176-186).
+inline float mis_weight(float current_pdf, float compensation_pdf) {
+    if (current_pdf < kEps || compensation_pdf < kEps) return 1.f;
+    const float c2 = current_pdf * current_pdf;
+    const float o2 = compensation_pdf * compensation_pdf;
+    return c2 / (o2 + c2 + kEps);
 }
 
 // Utilities::Lerp(v0, v1, v2, u, v) = v0 + (v1 - v0) * u + (v2 - v0) * v (Utilities.h:114-117).
@@ -686,7 +765,8 @@ inline V3 sample_vndf(Rng &rng, V3 w_o, float roughness) {
 }
 
 // MaterialRenderProxy::SampleSurface; returns the throughput, writes the world w_i.
-V3 sample_surface(Rng &rng, const spk_material &mat, V3 ray_dir, V3 normal, V3 tangent, V3 &w_i_world) {
+V3 sample_surface(Rng &rng, const spk_material &mat, V3 ray_dir, V3 normal, V3 tangent, V3 &w_i_world,
+                  bool *diffuse = nullptr, float *diffuse_z = nullptr) {
     const V3 base = load3(mat.base_color);
     const V3 w_o = -ray_dir;
     V3 fu, fv, fw;
@@ -737,6 +817,8 @@ V3 sample_surface(Rng &rng, const spk_material &mat, V3 ray_dir, V3 normal, V3 t
             const float z = std::sqrt(max_std(0.f, 1.0f - sq));
             lw_i = mk(dx, dy, z);
             thr = base;
+            if (diffuse) *diffuse = true;
+            if (diffuse_z) *diffuse_z = z;
         }
     }
     V3 gu, gv, gw;
@@ -893,9 +975,70 @@ struct PixelResult {  // CPURenderer.cpp:212-217
     float valid = 1.f;
 };
 
+// Next-event estimation at a vertex where the path took the diffuse fall-through branch of the PBR
+// sampler (no counterpart in the reference cpu pipeline; the GPU shader samples only the sky,
+// ray_trace.cs.slang:118-174). One point on the emissive triangles (area CDF, uniform on the triangle) and
+// one cosine-weighted sky direction, each with an occlusion ray and the shader's power-heuristic weight
+// against the cosine pdf of the diffuse branch. The estimator is the cpu BSDF's (base/pi * L * cos / pdf),
+// so NEE converges to the plain path tracer's image.
+void nee_direct(const or_scene &sc, Rng &rng, const Hit &hit, V3 base, V3 thr, V3 &color, uint64_t &shadow_rays,
+                uint64_t &overflows) {
+    if (!sc.lights.empty()) {
+        const float u0 = rng.unit(), u1 = rng.unit(), u2 = rng.unit();
+        const float target = u0 * sc.light_total;
+        size_t k = static_cast<size_t>(std::upper_bound(sc.light_cdf.begin(), sc.light_cdf.end(), target) -
+                                       sc.light_cdf.begin());
+        if (k >= sc.lights.size()) k = sc.lights.size() - 1;
+        const or_scene::Light &L = sc.lights[k];
+        const float r1 = std::sqrt(u1);
+        const float a = r1 * (1.f - u2), b = r1 * u2;
+        const V3 x = L.p0 + L.e1 * a + L.e2 * b;
+        const V3 to = x - hit.location;
+        const float dist2 = sqnorm(to);
+        if (dist2 > 0.f) {
+            const float dist = std::sqrt(dist2);
+            const V3 w = mk(to.x / dist, to.y / dist, to.z / dist);
+            const float cos_s = dot3(hit.normal, w);
+            const float cos_l = std::abs(dot3(L.ng, w));
+            if (cos_s > 0.f && cos_l > kEps) {
+                const float pdf_l = dist2 / (sc.light_total * cos_l);
+                const float pdf_b = cos_s * kInvPi;
+                const float wl = mis_weight(pdf_l, pdf_b);
+                ++shadow_rays;
+                const V3 so = hit.location + w * kTolerance;
+                const float tmax = (dist - kTolerance) * (1.f - 1e-4f);
+                if (!occluded(sc, so, w, tmax, overflows)) {
+                    const float f = cos_s / pdf_l * wl * kInvPi;
+                    color = color + mk(thr.x * base.x * L.emission.x * f, thr.y * base.y * L.emission.y * f,
+                                       thr.z * base.z * L.emission.z * f);
+                }
+            }
+        }
+    }
+    if (sc.sky.mode != SPK_SKY_NONE) {
+        V3 fu, fv, fw;
+        local_axes(hit.normal, hit.tangent, fu, fv, fw);
+        float dx, dy;
+        unit_disk(rng, dx, dy);
+        const float z = std::sqrt(max_std(0.f, 1.0f - (dx * dx + dy * dy)));
+        const V3 w = normalized(to_world(mk(dx, dy, z), fu, fv, fw));
+        const float pdf = z * kInvPi;
+        if (pdf > 0.f) {
+            const float wl = mis_weight(pdf, pdf);
+            ++shadow_rays;
+            const V3 so = hit.location + w * kTolerance;
+            if (!occluded(sc, so, w, 1000.f, overflows)) {
+                const V3 L = sky_eval(sc, w);
+                const float f = z / pdf * wl * kInvPi;
+                color = color + mk(thr.x * base.x * L.x * f, thr.y * base.y * L.y * f, thr.z * base.z * L.z * f);
+            }
+        }
+    }
+}
+
 // SamplePixel (CPURenderer.cpp:240-396) for debug_mode == Color, with SetupViewRay (:220-238).
 PixelResult sample_pixel(const or_renderer &r, Rng &rng, float u, float v, bool pruned, uint64_t &rays,
-                         uint64_t &overflows) {
+                         uint64_t &shadow_rays, uint64_t &overflows) {
     const or_scene &sc = *r.scene;
     const spk_camera &cam = r.cam;
     PixelResult res;
@@ -908,24 +1051,45 @@ PixelResult sample_pixel(const or_renderer &r, Rng &rng, float u, float v, bool 
     const V3 focus = load3(cam.lower_left) + u * load3(cam.max_u) + v * load3(cam.max_v);
     V3 d = normalized(focus - o);
     V3 thr = mk(1, 1, 1);
+    const bool nee = r.cfg.enable_nee != 0;
+    bool prev_nee = false;  // the previous vertex sampled the lights (diffuse branch)
+    float prev_pdf = 0.f;   // cosine pdf of the direction the previous vertex continued in
     for (uint32_t bounce = 0; bounce < r.cfg.bounce; ++bounce) {
         Candidate cand;
         ++rays;
         intersect_scene<false>(sc, o, d, cand, pruned, overflows);
         const Hit hit = make_hit(sc, cand, o, d);
         if (!hit.hit) {
-            if (sc.sky.mode != SPK_SKY_NONE) res.color = res.color + cmul(sky_eval(sc, d), thr);
+            if (sc.sky.mode != SPK_SKY_NONE) {
+                V3 c = cmul(sky_eval(sc, d), thr);
+                if (prev_nee) c = c * mis_weight(prev_pdf, prev_pdf);
+                res.color = res.color + c;
+            }
             break;
         }
         const spk_material &mat = sc.materials[sc.insts[hit.prim].desc.material_id];
         if (bounce == 0) res.world_normal = hit.normal;
         const V3 emissive = load3(mat.emissive);
         if (std::sqrt(sqnorm(emissive)) > kEps) {
-            res.color = res.color + cmul(emissive, thr);
+            V3 c = cmul(emissive, thr);
+            if (prev_nee && cand.face != SPK_INVALID_ID && sc.inst_light_base[hit.prim] != SPK_INVALID_ID) {
+                const or_scene::Light &L = sc.lights[sc.inst_light_base[hit.prim] + cand.face];
+                const float cos_l = std::abs(dot3(L.ng, d));
+                if (cos_l > kEps) c = c * mis_weight(prev_pdf, (hit.t * hit.t) / (sc.light_total * cos_l));
+            }
+            res.color = res.color + c;
             break;
         }
         V3 next_dir;
-        const V3 this_thr = sample_surface(rng, mat, d, hit.normal, hit.tangent, next_dir);
+        bool diffuse = false;
+        float dz = 0.f;
+        const V3 this_thr = sample_surface(rng, mat, d, hit.normal, hit.tangent, next_dir, &diffuse, &dz);
+        prev_nee = false;
+        if (nee && diffuse) {
+            nee_direct(sc, rng, hit, load3(mat.base_color), thr, res.color, shadow_rays, overflows);
+            prev_nee = true;
+            prev_pdf = dz * kInvPi;
+        }
         thr = cmul(thr, this_thr);
         if (sqnorm(thr) < kEps) {
             res.valid = -1.f;
@@ -948,15 +1112,15 @@ void base_pass(or_renderer &r, bool pruned, int num_threads, uint32_t row_begin,
     const float pw = 1.f / static_cast<float>(r.w - 1);
     const float ph = 1.f / static_cast<float>(r.h - 1);
     const uint32_t frame_seed = r.dispatched;
-    std::atomic<uint64_t> rays{0}, ovf{0};
+    std::atomic<uint64_t> rays{0}, shadow{0}, ovf{0};
     parallel_rows(row_begin, row_end, num_threads, [&](uint32_t j, int) {
-        uint64_t my_rays = 0, my_ovf = 0;
+        uint64_t my_rays = 0, my_shadow = 0, my_ovf = 0;
         Rng rng;
         for (uint32_t i = 0; i < r.w; ++i) {
             seed_pixel(rng, static_cast<int>(r.cfg.rng), r.cfg.seed, i, j, r.w, r.h, frame_seed);
             const float u = (static_cast<float>(i) + rng.unit()) * pw;
             const float v = (static_cast<float>(j) + rng.unit()) * ph;
-            PixelResult res = sample_pixel(r, rng, u, v, pruned, my_rays, my_ovf);
+            PixelResult res = sample_pixel(r, rng, u, v, pruned, my_rays, my_shadow, my_ovf);
             res.color = mk(min_std(res.color.x, kOutputLimit), min_std(res.color.y, kOutputLimit),
                            min_std(res.color.z, kOutputLimit));
             const size_t k = static_cast<size_t>(j) * r.w + i;
@@ -964,9 +1128,11 @@ void base_pass(or_renderer &r, bool pruned, int num_threads, uint32_t row_begin,
             r.gnormal[k] = res.world_normal;
         }
         rays += my_rays;
+        shadow += my_shadow;
         ovf += my_ovf;
     });
     r.ext_rays += rays.load();
+    r.shadow_rays += shadow.load();
     r.paths += static_cast<uint64_t>(row_end - row_begin) * r.w;
 }
 
@@ -1128,6 +1294,42 @@ or_scene *or_scene_create(const spk_mesh *meshes, uint32_t num_meshes, const spk
     sc->tlas_slot = sc->tlas.prim_ids;
     for (uint32_t i = 0; i < sc->tlas.prim_ids.size(); ++i) sc->tlas.prim_ids[i] = i;
     sc->materials.assign(materials, materials + num_materials);
+    // Emissive triangles for next-event estimation, in instance then face order, world space.
+    sc->inst_light_base.assign(num_instances, SPK_INVALID_ID);
+    for (uint32_t k = 0; k < num_instances; ++k) {
+        const Inst &in = sc->insts[k];
+        if (in.desc.type != SPK_PRIM_MESH) continue;
+        const V3 em = load3(sc->materials[in.desc.material_id].emissive);
+        if (!(std::sqrt(sqnorm(em)) > kEps)) continue;
+        const MeshData &m = sc->meshes[in.desc.mesh_id];
+        sc->inst_light_base[k] = static_cast<uint32_t>(sc->lights.size());
+        for (uint32_t f = 0; f < m.tris.size(); ++f) {
+            const V3 w0 = xform_point(in.M, m.pos[m.idx[3 * f]]);
+            const V3 w1 = xform_point(in.M, m.pos[m.idx[3 * f + 1]]);
+            const V3 w2 = xform_point(in.M, m.pos[m.idx[3 * f + 2]]);
+            or_scene::Light L;
+            L.p0 = w0;
+            L.e1 = w1 - w0;
+            L.e2 = w2 - w0;
+            const V3 c = cross(L.e1, L.e2);
+            const float len = std::sqrt(sqnorm(c));
+            L.area = 0.5f * len;
+            L.ng = len > 0.f ? mk(c.x / len, c.y / len, c.z / len) : mk(0, 0, 0);
+            L.emission = em;
+            sc->lights.push_back(L);
+        }
+    }
+    float acc = 0.f;
+    for (const auto &L : sc->lights) {
+        acc = acc + L.area;
+        sc->light_cdf.push_back(acc);
+    }
+    sc->light_total = acc;
+    if (!(acc > 0.f)) {
+        sc->lights.clear();
+        sc->light_cdf.clear();
+        sc->inst_light_base.assign(num_instances, SPK_INVALID_ID);
+    }
     if (sky) {
         sc->sky = *sky;
         if (sky->mode == SPK_SKY_CUBE && sky->cube_rgba) {

@@ -27,7 +27,7 @@ struct alignas(16) DevInstance {
     uint32_t vert_base;  // first vertex of the mesh in `verts`
     uint32_t face_base;  // first face of the mesh in `faces`
     uint32_t mesh_id;
-    uint32_t pad;
+    uint32_t light_base;  // first entry of this instance's triangles in `lights`, kInvalid if it does not emit
 };
 static_assert(sizeof(DevInstance) == 128, "DevInstance is 128 bytes");
 
@@ -40,7 +40,18 @@ struct alignas(16) DevMaterial {
 };
 static_assert(sizeof(DevMaterial) == 48, "DevMaterial is 48 bytes");
 
+// An emissive triangle in world space for next-event estimation (64 B).
+struct alignas(16) DevLight {
+    float p0[3], e1[3], e2[3], ng[3], emission[3];
+    float area;
+};
+static_assert(sizeof(DevLight) == 64, "DevLight is 64 bytes");
+
 struct DevScene {
+    const DevLight *lights;   // emissive triangles of mesh instances, instance then face order
+    const float *light_cdf;   // running sum of light areas
+    uint32_t num_lights;
+    float light_total;        // total emissive area
     const uint4 *nodes;
     const float4 *tris;
     const uint32_t *tlas_items;

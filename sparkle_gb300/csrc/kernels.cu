@@ -47,12 +47,12 @@ __global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_trace(DevScene S, 
 // ------------------------------------------------------------------------------------------------
 // BasePass: one thread per pixel runs RenderPixel + SamplePixel (CPURenderer.cpp:240-417).
 // ------------------------------------------------------------------------------------------------
-template <int kKind, bool kCount>
+template <int kKind, bool kCount, bool kNee>
 __global__ void __launch_bounds__(128) k_render_mega(DevScene S, DevCamera cam, FrameBuffers fb, RenderParams p,
                                                      Counters *counters) {
     const uint32_t i = blockIdx.x * 16u + (threadIdx.x & 15u);
     const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 4);
-    uint32_t err = 0, rays = 0;
+    uint32_t err = 0, rays = 0, shadow = 0;
     TraceCounts tc;
     if (i < fb.width && j < fb.height) {
         Rng rng;
@@ -65,22 +65,37 @@ __global__ void __launch_bounds__(128) k_render_mega(DevScene S, DevCamera cam, 
         camera_ray<kKind>(cam, rng, u, v, o, d);
         f3 color = mk3(0.f, 0.f, 0.f), thr = mk3(1.f, 1.f, 1.f), first_normal = mk3(0.f, 0.f, 0.f);
         float valid = 1.f;
+        float prev_pdf = 0.f;  // NEE: cosine pdf of the continuation when the previous vertex sampled lights
         for (uint32_t bounce = 0; bounce < p.bounce; ++bounce) {
             ++rays;
             const TraceResult hit = trace_ray<kTraceClosest, kCount>(S, o, d, kFltMax, err, &tc);
             if (hit.inst == kInvalid) {
-                if (S.sky_mode != 0u) color = color + cmul(sky_eval(S, d), thr);
+                if (S.sky_mode != 0u) {
+                    f3 c = cmul(sky_eval(S, d), thr);
+                    if (kNee && prev_pdf > 0.f) c = c * mis_weight(prev_pdf, prev_pdf);
+                    color = color + c;
+                }
                 break;
             }
             const Surface surf = make_surface(S, hit, o, d);
             const DevMaterial mat = S.materials[surf.material];
             if (bounce == 0) first_normal = surf.normal;
             if (mat.is_emissive) {
-                color = color + cmul(mk3(mat.emissive[0], mat.emissive[1], mat.emissive[2]), thr);
+                f3 c = cmul(mk3(mat.emissive[0], mat.emissive[1], mat.emissive[2]), thr);
+                if (kNee && prev_pdf > 0.f) c = c * bsdf_hit_weight(S, prev_pdf, hit, d);
+                color = color + c;
                 break;
             }
             f3 next_dir;
-            const f3 this_thr = sample_surface<kKind>(rng, mat, d, surf.normal, surf.tangent, next_dir);
+            float dz = -1.f;
+            const f3 this_thr =
+                sample_surface<kKind>(rng, mat, d, surf.normal, surf.tangent, next_dir, kNee ? &dz : nullptr);
+            prev_pdf = 0.f;
+            if (kNee && dz >= 0.f) {
+                nee_direct<kKind, kCount>(S, rng, surf, mk3(mat.base[0], mat.base[1], mat.base[2]), thr, color,
+                                          shadow, err, &tc);
+                prev_pdf = dz * kInvPi;
+            }
             thr = cmul(thr, this_thr);
             if (sqnorm(thr) < kEps) {
                 valid = -1.f;
@@ -101,6 +116,7 @@ __global__ void __launch_bounds__(128) k_render_mega(DevScene S, DevCamera cam, 
         if (p.spatial_denoise) fb.gnormal[k] = make_float4(first_normal.x, first_normal.y, first_normal.z, 0.f);
     }
     warp_add_u64(&counters->extension_rays, rays);
+    warp_add_u64(&counters->shadow_rays, shadow);
     if (kCount) {
         warp_add_u64(&counters->node_visits, tc.nodes);
         warp_add_u64(&counters->tri_tests, tc.tris);
@@ -210,20 +226,15 @@ cudaError_t launch_render_mega(const DevScene &scene, const DevCamera &cam, cons
                                const RenderParams &p, bool count, Counters *counters, cudaStream_t stream,
                                LaunchEvents *ev) {
     const dim3 grid((fbuf.width + 15) / 16, (fbuf.height + 7) / 8);
+    using Kernel = void (*)(DevScene, DevCamera, FrameBuffers, RenderParams, Counters *);
+    static const Kernel table[2][2][2] = {
+        {{k_render_mega<0, false, false>, k_render_mega<0, false, true>},
+         {k_render_mega<0, true, false>, k_render_mega<0, true, true>}},
+        {{k_render_mega<1, false, false>, k_render_mega<1, false, true>},
+         {k_render_mega<1, true, false>, k_render_mega<1, true, true>}}};
+    const Kernel k = table[p.rng == 0 ? 0 : 1][count ? 1 : 0][p.enable_nee ? 1 : 0];
     if (ev) ev->before(stream);
-    if (p.rng == 0) {
-        if (count) {
-            k_render_mega<0, true><<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
-        } else {
-            k_render_mega<0, false><<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
-        }
-    } else {
-        if (count) {
-            k_render_mega<1, true><<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
-        } else {
-            k_render_mega<1, false><<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
-        }
-    }
+    k<<<grid, 128, 0, stream>>>(scene, cam, fbuf, p, counters);
     if (ev) ev->after(stream);
     return cudaGetLastError();
 }

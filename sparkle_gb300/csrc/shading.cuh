@@ -209,7 +209,7 @@ __device__ __forceinline__ f3 sample_vndf(Rng &rng, f3 w_o, float roughness) {
 // MaterialRenderProxy::SampleSurface; returns the throughput and writes the world-space w_i.
 template <int kKind>
 __device__ __forceinline__ f3 sample_surface(Rng &rng, const DevMaterial &mat, f3 ray_dir, f3 normal, f3 tangent,
-                                             f3 &w_i) {
+                                             f3 &w_i, float *diffuse_z = nullptr) {
     const f3 base = mk3(mat.base[0], mat.base[1], mat.base[2]);
     const f3 w_o = -ray_dir;
     f3 fu, fv;
@@ -260,6 +260,7 @@ __device__ __forceinline__ f3 sample_surface(Rng &rng, const DevMaterial &mat, f
             const float sq = dx * dx + dy * dy;
             lw_i = mk3(dx, dy, sqrtf(max_std(0.f, 1.0f - sq)));
             thr = base;
+            if (diffuse_z) *diffuse_z = lw_i.z;  // the diffuse fall-through branch was taken
         }
     }
     f3 gu, gv;
@@ -267,6 +268,16 @@ __device__ __forceinline__ f3 sample_surface(Rng &rng, const DevMaterial &mat, f
     w_i = normalized(gu * lw_i.x + gv * lw_i.y + normal * lw_i.z);
     return thr;
 }
+
+// GetMISWeight (power heuristic, ray_trace.cs.slang:176-186).
+__device__ __forceinline__ float mis_weight(float current_pdf, float compensation_pdf) {
+    if (current_pdf < kEps || compensation_pdf < kEps) return 1.f;
+    const float c2 = current_pdf * current_pdf;
+    const float o2 = compensation_pdf * compensation_pdf;
+    return c2 / (o2 + c2 + kEps);
+}
+
+constexpr float kInvPi = 0.318309886183790671538f;  // std::numbers::inv_pi_v<float> (Types.h:52)
 
 // ------------------------------------------------------------------------------------------------
 // Sky
@@ -333,6 +344,89 @@ __device__ __forceinline__ f3 sky_eval(const DevScene &S, f3 d) {
                    1.f + (S.sky_color[2] - 1.f) * t);
     }
     return mk3(0.f, 0.f, 0.f);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Next-event estimation (no counterpart in the reference cpu pipeline; its GPU shader samples only the
+// sky, ray_trace.cs.slang:118-174). Called at a vertex where the PBR sampler took the diffuse
+// fall-through branch: one point on the emissive triangles (area CDF, uniform on the triangle) and one
+// cosine-weighted sky direction, each with an occlusion ray and the shader's power-heuristic weight
+// against the diffuse branch's cosine pdf. The estimator is the cpu BSDF's (base/pi * L * cos / pdf), so
+// NEE converges to the plain path tracer's image. Contributions are added to `color` in that order.
+// ------------------------------------------------------------------------------------------------
+template <int kKind, bool kCount>
+__device__ __forceinline__ void nee_direct(const DevScene &S, Rng &rng, const Surface &surf, f3 base, f3 thr,
+                                           f3 &color, uint32_t &shadow_rays, uint32_t &err, TraceCounts *tc) {
+    if (S.num_lights > 0) {
+        const float u0 = rng_unit<kKind>(rng), u1 = rng_unit<kKind>(rng), u2 = rng_unit<kKind>(rng);
+        const float target = u0 * S.light_total;
+        uint32_t lo = 0, hi = S.num_lights;  // first cdf entry > target
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(S.light_cdf + mid) > target) {
+                hi = mid;
+            } else {
+                lo = mid + 1;
+            }
+        }
+        const DevLight &L = S.lights[lo < S.num_lights ? lo : S.num_lights - 1];
+        const float r1 = sqrtf(u1);
+        const float a = r1 * (1.f - u2), b = r1 * u2;
+        const f3 x = mk3(L.p0[0], L.p0[1], L.p0[2]) + mk3(L.e1[0], L.e1[1], L.e1[2]) * a +
+                     mk3(L.e2[0], L.e2[1], L.e2[2]) * b;
+        const f3 to = x - surf.location;
+        const float dist2 = sqnorm(to);
+        if (dist2 > 0.f) {
+            const float dist = sqrtf(dist2);
+            const f3 w = mk3(to.x / dist, to.y / dist, to.z / dist);
+            const float cos_s = dot3(surf.normal, w);
+            const float cos_l = fabsf(dot3(mk3(L.ng[0], L.ng[1], L.ng[2]), w));
+            if (cos_s > 0.f && cos_l > kEps) {
+                const float pdf_l = dist2 / (S.light_total * cos_l);
+                const float pdf_b = cos_s * kInvPi;
+                const float wl = mis_weight(pdf_l, pdf_b);
+                ++shadow_rays;
+                const f3 so = surf.location + w * kTolerance;
+                const float tmax = (dist - kTolerance) * (1.f - 1e-4f);
+                if (trace_ray<kTraceOcclusion, kCount>(S, so, w, tmax, err, tc).inst == kInvalid) {
+                    const float f = cos_s / pdf_l * wl * kInvPi;
+                    color = color + mk3(thr.x * base.x * L.emission[0] * f, thr.y * base.y * L.emission[1] * f,
+                                        thr.z * base.z * L.emission[2] * f);
+                }
+            }
+        }
+    }
+    if (S.sky_mode != 0u) {
+        f3 fu, fv;
+        local_axes(surf.normal, surf.tangent, fu, fv);
+        float dx, dy;
+        unit_disk<kKind>(rng, dx, dy);
+        const float z = sqrtf(max_std(0.f, 1.0f - (dx * dx + dy * dy)));
+        const f3 w = normalized(fu * dx + fv * dy + surf.normal * z);
+        const float pdf = z * kInvPi;
+        if (pdf > 0.f) {
+            const float wl = mis_weight(pdf, pdf);
+            ++shadow_rays;
+            const f3 so = surf.location + w * kTolerance;
+            if (trace_ray<kTraceOcclusion, kCount>(S, so, w, 1000.f, err, tc).inst == kInvalid) {
+                const f3 Ls = sky_eval(S, w);
+                const float f = z / pdf * wl * kInvPi;
+                color = color + mk3(thr.x * base.x * Ls.x * f, thr.y * base.y * Ls.y * f, thr.z * base.z * Ls.z * f);
+            }
+        }
+    }
+}
+
+// MIS weight of the emission a BSDF-sampled ray collects when the previous vertex also sampled the lights
+// (prev_pdf = cosine pdf of the direction it continued in; 0 when it did not sample the lights).
+__device__ __forceinline__ float bsdf_hit_weight(const DevScene &S, float prev_pdf, const TraceResult &hit, f3 d) {
+    if (!(prev_pdf > 0.f) || hit.face == kInvalid) return 1.f;
+    const uint32_t base = S.instances[hit.inst].light_base;
+    if (base == kInvalid) return 1.f;
+    const DevLight &L = S.lights[base + hit.face];
+    const float cos_l = fabsf(dot3(mk3(L.ng[0], L.ng[1], L.ng[2]), d));
+    if (!(cos_l > kEps)) return 1.f;
+    return mis_weight(prev_pdf, (hit.t * hit.t) / (S.light_total * cos_l));
 }
 
 // ------------------------------------------------------------------------------------------------

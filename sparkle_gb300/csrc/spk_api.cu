@@ -59,6 +59,8 @@ struct spk_ctx {
     DevBuf<uint4> faces;
     DevBuf<DevMaterial> materials;
     DevBuf<float4> sky;
+    DevBuf<DevLight> lights;
+    DevBuf<float> light_cdf;
     DevScene scene{};
     bool has_scene = false;
     uint32_t bvh_nodes = 0;
@@ -216,6 +218,8 @@ spk_status spk_destroy(spk_ctx *ctx) {
     ctx->faces.reset();
     ctx->materials.reset();
     ctx->sky.reset();
+    ctx->lights.reset();
+    ctx->light_cdf.reset();
     ctx->gcolor.reset();
     ctx->gnormal.reset();
     ctx->fb.reset();
@@ -392,6 +396,50 @@ spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_mesh
         d.roughness = s.roughness;
         d.eta = s.eta;
     }
+    // Emissive triangles of mesh instances in world space (instance then face order) and their area CDF,
+    // for next-event estimation.
+    std::vector<DevLight> light_recs;
+    std::vector<float> light_cdf;
+    for (uint32_t k = 0; k < num_instances; ++k) inst_recs[k].light_base = kInvalid;
+    for (uint32_t k = 0; k < num_instances; ++k) {
+        const spk_instance &in = instances[k];
+        if (in.type != SPK_PRIM_MESH || !mat_recs[in.material_id].is_emissive) continue;
+        const spk_mesh &m = meshes[in.mesh_id];
+        inst_recs[k].light_base = static_cast<uint32_t>(light_recs.size());
+        for (uint32_t f = 0; f < m.num_faces; ++f) {
+            f3 w[3];
+            for (int c = 0; c < 3; ++c) {
+                const float *p = m.positions + 3 * m.indices[3 * f + c];
+                w[c] = xform_point(in.transform, mk3(p[0], p[1], p[2]));
+            }
+            DevLight L{};
+            const f3 e1 = w[1] - w[0], e2 = w[2] - w[0];
+            const f3 cr = cross(e1, e2);
+            const float len = std::sqrt(sqnorm(cr));
+            const f3 ng = len > 0.f ? mk3(cr.x / len, cr.y / len, cr.z / len) : mk3(0.f, 0.f, 0.f);
+            const float vals[5][3] = {{w[0].x, w[0].y, w[0].z}, {e1.x, e1.y, e1.z}, {e2.x, e2.y, e2.z},
+                                      {ng.x, ng.y, ng.z},
+                                      {mat_recs[in.material_id].emissive[0], mat_recs[in.material_id].emissive[1],
+                                       mat_recs[in.material_id].emissive[2]}};
+            std::memcpy(L.p0, vals[0], 12);
+            std::memcpy(L.e1, vals[1], 12);
+            std::memcpy(L.e2, vals[2], 12);
+            std::memcpy(L.ng, vals[3], 12);
+            std::memcpy(L.emission, vals[4], 12);
+            L.area = 0.5f * len;
+            light_recs.push_back(L);
+        }
+    }
+    float light_total = 0.f;
+    for (const DevLight &L : light_recs) {
+        light_total = light_total + L.area;
+        light_cdf.push_back(light_total);
+    }
+    if (!(light_total > 0.f)) {
+        light_recs.clear();
+        light_cdf.clear();
+        for (uint32_t k = 0; k < num_instances; ++k) inst_recs[k].light_base = kInvalid;
+    }
     std::vector<float4> cube;
     if (sky && sky->mode == SPK_SKY_CUBE) {
         const size_t n = 6ull * sky->cube_size * sky->cube_size;
@@ -410,7 +458,9 @@ spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_mesh
         (e = upload(ctx->verts, vert_recs.data(), vert_recs.size(), ctx->stream)) != cudaSuccess ||
         (e = upload(ctx->faces, face_recs.data(), face_recs.size(), ctx->stream)) != cudaSuccess ||
         (e = upload(ctx->materials, mat_recs.data(), mat_recs.size(), ctx->stream)) != cudaSuccess ||
-        (e = upload(ctx->sky, cube.data(), cube.size(), ctx->stream)) != cudaSuccess) {
+        (e = upload(ctx->sky, cube.data(), cube.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->lights, light_recs.data(), light_recs.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->light_cdf, light_cdf.data(), light_cdf.size(), ctx->stream)) != cudaSuccess) {
         return cuda_fail(ctx, e, "scene upload");
     }
     DevScene &S = ctx->scene;
@@ -427,6 +477,10 @@ spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_mesh
     S.sky_size = sky ? sky->cube_size : 0;
     for (int c = 0; c < 3; ++c) S.sky_color[c] = sky ? sky->color[c] : 0.f;
     S.scene_abs_x = abs_x;
+    S.lights = ctx->lights.ptr;
+    S.light_cdf = ctx->light_cdf.ptr;
+    S.num_lights = static_cast<uint32_t>(light_recs.size());
+    S.light_total = light_total;
     ctx->bvh_nodes = static_cast<uint32_t>(all_nodes.size());
     ctx->bvh_bytes = all_nodes.size() * sizeof(WideNode) + tri_recs.size() * sizeof(float4);
     ctx->has_scene = true;

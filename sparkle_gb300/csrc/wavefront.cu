@@ -65,15 +65,18 @@ __device__ __forceinline__ void start_path(const DevCamera &cam, const RenderPar
     s.ray_d[pid] = make_float4(d.x, d.y, d.z, 0.f);
     s.thr[pid] = make_float4(1.f, 1.f, 1.f, 0.f);
     s.color[pid] = make_float4(0.f, 0.f, 0.f, 1.f);
+    s.prev_pdf[pid] = 0.f;
     store_rng<kKind>(s.rng, pid, rng);
 }
 
 // One bounce of SamplePixel's loop body (CPURenderer.cpp:261-368) for path `pid` whose closest hit is
-// in s.hit: sky on a miss, emission, BSDF sample, throughput cut-off, Russian roulette. Returns whether
-// the path continues (the next ray is then in s.ray_o / s.ray_d).
-template <int kKind>
+// in s.hit: sky on a miss, emission, BSDF sample, throughput cut-off, Russian roulette, and (with `nee`)
+// next-event estimation at diffuse-branch vertices with MIS on the emission the BSDF rays collect.
+// Returns whether the path continues (the next ray is then in s.ray_o / s.ray_d).
+template <int kKind, bool kNee>
 __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontState &s, uint32_t pid,
-                                           uint32_t bounce, float4 *gnormal) {
+                                           uint32_t bounce, float4 *gnormal, uint32_t &shadow, uint32_t &err) {
+    constexpr bool nee = kNee;
     bool alive = false;
     const float4 hit4 = s.hit[pid];
     const uint32_t inst = __float_as_uint(hit4.w);
@@ -84,20 +87,35 @@ __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontSta
     const float4 t4 = s.thr[pid];
     f3 thr = mk3(t4.x, t4.y, t4.z);
     float valid = c4.w;
+    const float prev_pdf = nee ? s.prev_pdf[pid] : 0.f;
     if (inst == kInvalid) {
-        if (S.sky_mode != 0u) color = color + cmul(sky_eval(S, d), thr);
+        if (S.sky_mode != 0u) {
+            f3 c = cmul(sky_eval(S, d), thr);
+            if (prev_pdf > 0.f) c = c * mis_weight(prev_pdf, prev_pdf);
+            color = color + c;
+        }
     } else {
         const TraceResult h{hit4.x, hit4.y, hit4.z, inst, s.hit_face[pid]};
         const Surface surf = make_surface(S, h, o, d);
         const DevMaterial mat = S.materials[surf.material];
         if (bounce == 0 && gnormal) gnormal[pid] = make_float4(surf.normal.x, surf.normal.y, surf.normal.z, 0.f);
         if (mat.is_emissive) {
-            color = color + cmul(mk3(mat.emissive[0], mat.emissive[1], mat.emissive[2]), thr);
+            f3 c = cmul(mk3(mat.emissive[0], mat.emissive[1], mat.emissive[2]), thr);
+            if (prev_pdf > 0.f) c = c * bsdf_hit_weight(S, prev_pdf, h, d);
+            color = color + c;
         } else {
             Rng rng;
             load_rng<kKind>(s.rng, pid, rng);
             f3 next_dir;
-            const f3 this_thr = sample_surface<kKind>(rng, mat, d, surf.normal, surf.tangent, next_dir);
+            float dz = -1.f;
+            const f3 this_thr =
+                sample_surface<kKind>(rng, mat, d, surf.normal, surf.tangent, next_dir, nee ? &dz : nullptr);
+            float next_pdf = 0.f;
+            if (dz >= 0.f) {
+                nee_direct<kKind, false>(S, rng, surf, mk3(mat.base[0], mat.base[1], mat.base[2]), thr, color,
+                                         shadow, err, nullptr);
+                next_pdf = dz * kInvPi;
+            }
             thr = cmul(thr, this_thr);
             if (sqnorm(thr) < kEps) {
                 valid = -1.f;
@@ -116,6 +134,7 @@ __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontSta
                     const f3 no = surf.location + next_dir * kTolerance;
                     s.ray_o[pid] = make_float4(no.x, no.y, no.z, 0.f);
                     s.ray_d[pid] = make_float4(next_dir.x, next_dir.y, next_dir.z, 0.f);
+                    if (nee) s.prev_pdf[pid] = next_pdf;
                     alive = true;
                 }
             }
@@ -173,9 +192,10 @@ __global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_wf_extend(DevScene
     if (err) atomicOr(&counters->error_flags, err);
 }
 
-template <int kKind>
+template <int kKind, bool kNee>
 __global__ void __launch_bounds__(128) k_wf_shade(DevScene S, FrameBuffers fb, RenderParams p, WavefrontState s,
                                                   int in_queue, uint32_t bounce, Counters *counters) {
+    uint32_t shadow = 0, err = 0;
     const unsigned long long n = counters->queue_counters[in_queue];
     const int out_queue = in_queue ^ 1;
     const uint32_t *queue = s.queue[in_queue];
@@ -186,10 +206,12 @@ __global__ void __launch_bounds__(128) k_wf_shade(DevScene S, FrameBuffers fb, R
         uint32_t pid = 0;
         if (q < n) {
             pid = queue[q];
-            alive = shade_path<kKind>(S, s, pid, bounce, p.spatial_denoise ? fb.gnormal : nullptr);
+            alive = shade_path<kKind, kNee>(S, s, pid, bounce, p.spatial_denoise ? fb.gnormal : nullptr, shadow, err);
         }
         queue_push(s.queue[out_queue], &counters->queue_counters[out_queue], pid, alive && bounce + 1 < p.bounce);
     }
+    warp_add_u64(&counters->shadow_rays, shadow);
+    if (err) atomicOr(&counters->error_flags, err);
 }
 
 __global__ void __launch_bounds__(256) k_wf_finish(FrameBuffers fb, WavefrontState s) {
@@ -232,10 +254,11 @@ __global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers
 
 // Shade one segment per live slot. A finished sample stores its clamped result (RenderPixel's 6.0 clamp,
 // CPURenderer.cpp:408) at its item, and the slot takes the next item from the global counter.
-template <int kKind>
+template <int kKind, bool kNee>
 __global__ void __launch_bounds__(128) k_mf_shade(DevScene S, DevCamera cam, FrameBuffers fb, RenderParams p,
                                                   WavefrontState s, int in_queue, uint32_t frame_base,
                                                   uint32_t total_items, Counters *counters) {
+    uint32_t shadow = 0, err = 0;
     const unsigned long long n = counters->queue_counters[in_queue];
     const int out_queue = in_queue ^ 1;
     const uint32_t *queue = s.queue[in_queue];
@@ -248,7 +271,8 @@ __global__ void __launch_bounds__(128) k_mf_shade(DevScene S, DevCamera cam, Fra
         if (q < n) {
             slot = queue[q];
             const uint32_t bounce = s.slot_state[slot];
-            const bool alive = shade_path<kKind>(S, s, slot, bounce, nullptr) && bounce + 1 < p.bounce;
+            const bool alive =
+                shade_path<kKind, kNee>(S, s, slot, bounce, nullptr, shadow, err) && bounce + 1 < p.bounce;
             if (alive) {
                 s.slot_state[slot] = bounce + 1u;
                 push = true;
@@ -276,6 +300,8 @@ __global__ void __launch_bounds__(128) k_mf_shade(DevScene S, DevCamera cam, Fra
         }
         queue_push(s.queue[out_queue], &counters->queue_counters[out_queue], slot, push);
     }
+    warp_add_u64(&counters->shadow_rays, shadow);
+    if (err) atomicOr(&counters->error_flags, err);
 }
 
 __device__ __forceinline__ float aces_tonemap(float c, float exposure) {
@@ -350,7 +376,7 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
         (e = dmalloc(s.hit, capacity)) != cudaSuccess || (e = dmalloc(s.hit_face, capacity)) != cudaSuccess ||
         (e = dmalloc(s.queue[0], capacity)) != cudaSuccess || (e = dmalloc(s.queue[1], capacity)) != cudaSuccess ||
         (e = dmalloc(s.sort_keys, capacity)) != cudaSuccess || (e = dmalloc(s.slot_state, capacity)) != cudaSuccess ||
-        (e = dmalloc(s.slot_item, capacity)) != cudaSuccess ||
+        (e = dmalloc(s.slot_item, capacity)) != cudaSuccess || (e = dmalloc(s.prev_pdf, capacity)) != cudaSuccess ||
         (e = cudaHostAlloc(reinterpret_cast<void **>(&s.host_len), sizeof(unsigned long long), cudaHostAllocDefault)) !=
             cudaSuccess) {
         wavefront_free(s);
@@ -363,7 +389,7 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
 void wavefront_free(WavefrontState &s) {
     void *ptrs[] = {s.ray_o,      s.ray_d,     s.thr,     s.color,        s.rng,        s.hit,
                     s.hit_face,   s.queue[0],  s.queue[1], s.sort_keys,   s.slot_state, s.slot_item,
-                    s.samples,    s.frame_weight, s.frame_seed};
+                    s.samples,    s.frame_weight, s.frame_seed, s.prev_pdf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s.host_len) cudaFreeHost(s.host_len);
@@ -393,9 +419,17 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
         if ((e = launch_extend(scene, s, in, count, counters, num_sms, stream, ev)) != cudaSuccess) return e;
         ++nl;
         if (p.rng == 0) {
-            k_wf_shade<0><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
+            if (p.enable_nee) {
+                k_wf_shade<0, true><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
+            } else {
+                k_wf_shade<0, false><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
+            }
         } else {
-            k_wf_shade<1><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
+            if (p.enable_nee) {
+                k_wf_shade<1, true><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
+            } else {
+                k_wf_shade<1, false><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
+            }
         }
         ++nl;
     }
@@ -459,13 +493,9 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 const int in = static_cast<int>(iter & 1u), out = in ^ 1;
                 if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
                 if ((e = launch_extend(scene, s, in, count, counters, num_sms, stream, ev)) != cudaSuccess) return e;
-                if (p.rng == 0) {
-                    k_mf_shade<0><<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, s, in, f0, total_items,
-                                                                    counters);
-                } else {
-                    k_mf_shade<1><<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, s, in, f0, total_items,
-                                                                    counters);
-                }
+                auto *shade = p.rng == 0 ? (p.enable_nee ? k_mf_shade<0, true> : k_mf_shade<0, false>)
+                                         : (p.enable_nee ? k_mf_shade<1, true> : k_mf_shade<1, false>);
+                shade<<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, s, in, f0, total_items, counters);
                 nl += 2;
             }
             if ((e = cudaGetLastError()) != cudaSuccess) return e;

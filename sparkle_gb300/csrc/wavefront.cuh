@@ -23,6 +23,7 @@ struct WavefrontState {
     uint32_t *hit_face = nullptr;
     uint32_t *queue[2] = {nullptr, nullptr};  // path indices
     uint32_t *sort_keys = nullptr;            // material-sort scratch
+    float *prev_pdf = nullptr;                // NEE: cosine pdf of the continuation after a light-sampling vertex
     uint32_t *slot_state = nullptr;           // multi-frame mode: bounce of the slot's path
     uint32_t *slot_item = nullptr;            // multi-frame mode: sample item (frame * pixels + pixel) of the slot
     float4 *samples = nullptr;                // multi-frame mode: clamped result of each (frame, pixel) sample

@@ -372,3 +372,24 @@ def test_spp_reweights_like_the_reference(cornell):
     r = oracle.OracleRenderer(oracle.OracleScene(scene), abi.make_config(8, 8, spp=5, bounce=2), cam)
     r.render(3)
     assert r.sample_counts() == (8, 12)  # spp 5 -> 2x2 = 4 per frame
+
+
+def test_oracle_nee_converges_to_plain(cornell):
+    """NEE + MIS (power heuristic) estimates the same image as plain path tracing once the bounce limit no
+    longer cuts paths and no sample reaches the 6.0 clamp."""
+    scene, cam_args = cornell
+    scene = abi.Scene(scene.meshes, scene.instances, list(scene.materials), scene.sky)
+    scene.materials[7] = abi.Material.light((2.0, 2.0, 2.0))
+    sc = oracle.OracleScene(scene)
+    cam = scenes.make_camera(cam_args, 12, 12)
+    means = {}
+    for nee in (False, True):
+        acc = 0.0
+        for seed in (1, 2, 3):
+            cfg = abi.make_config(12, 12, spp=1, max_spp=1 << 20, bounce=24, enable_nee=nee,
+                                  rng=abi.SPK_RNG_XOSHIRO256SS, seed=seed)
+            r = oracle.OracleRenderer(sc, cfg, cam)
+            r.render(4096, traversal=oracle.PRUNED)
+            acc += r.framebuffer()[0][..., :3].astype(np.float64).mean()
+        means[nee] = acc / 3
+    assert abs(means[True] / means[False] - 1.0) < 1e-2
