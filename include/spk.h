@@ -272,6 +272,30 @@ spk_status spk_get_stats(spk_ctx *ctx, spk_stats *out);
  * variants that also count visited nodes and tested triangles (slower; results are unchanged). */
 spk_status spk_set_instrumentation(spk_ctx *ctx, uint32_t flags);
 
+/* Largest width * height spk_render_noalloc accepts (512 x 512). */
+#define SPK_NOALLOC_MAX_PIXELS (512u * 512u)
+
+/* No counterpart in the reference. Renders `num_frames` frames exactly like spk_render does with the
+ * one-kernel schedule (SPK_KERNEL_MEGAKERNEL) -- same scene, camera, config, seeds and sample
+ * bookkeeping, bit-identical results -- but without allocating anything: no cudaMalloc, no cudaFree, no
+ * event creation. It is meant for callers that cannot allocate device memory while they render: a frame
+ * loop that must not stall on the allocator or contend for its lock mid-frame, code that runs while a
+ * stream is being captured (allocation is not allowed there), or a host whose device memory is already
+ * carved up by its own pool. Set-up still allocates once (spk_create, spk_set_scene, spk_set_config,
+ * spk_set_camera must have been called); render time does not.
+ *
+ * The caller owns the outputs: `d_hdr_rgba` (width*height float4, device memory) is the accumulated frame
+ * buffer and is read and written (it is cleared when the context is dirty, as spk_render clears its own);
+ * `d_rgba16f` (width*height half4, device memory) receives the tonemapped image. The per-frame G-buffer and
+ * the counters live in one file-scope device array sized for SPK_NOALLOC_MAX_PIXELS pixels (8 MB plus
+ * 256 bytes, held by every GPU that loads the library until the process exits); larger configs return
+ * SPK_ERR_INVALID_ARGUMENT. The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress), so make that first call before capturing any stream. Every call on a device
+ * shares the one array and it keeps the last call's contents: calls that overlap on the GPU (two contexts,
+ * two streams) race on it and must be serialised by the caller. Asynchronous like spk_render;
+ * spk_get_stats does not report these calls. */
+spk_status spk_render_noalloc(spk_ctx *ctx, uint32_t num_frames, void *d_hdr_rgba, void *d_rgba16f);
+
 #ifdef __cplusplus
 }
 #endif

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <new>
 #include <string>
 #include <thread>
@@ -820,3 +821,89 @@ spk_status spk_set_instrumentation(spk_ctx *ctx, uint32_t flags) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------------------
+// spk_render_noalloc: the one-kernel render into caller-owned buffers, with its scratch (the per-frame
+// G-buffer and the counters) in a static device array instead of context allocations, for callers that
+// must not allocate while rendering.
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoallocGbufferBytes = static_cast<size_t>(SPK_NOALLOC_MAX_PIXELS) * 2 * sizeof(float4);
+constexpr size_t kNoallocCounterBytes = 256;
+static_assert(sizeof(Counters) <= kNoallocCounterBytes, "counters fit their slot");
+
+// G-buffer colour (max pixels x float4), G-buffer normal (max pixels x float4), then the counters.
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocGbufferBytes + kNoallocCounterBytes];
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void *g_noalloc_address[kNoallocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on `device` (current), looked up once per device. The host-side
+// name of the array is only a stand-in and must never be handed to a kernel.
+cudaError_t noalloc_scratch(int device, unsigned char **out) {
+    if (device < 0 || device >= kNoallocMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_address[device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_address[device] = p;
+    }
+    *out = static_cast<unsigned char *>(g_noalloc_address[device]);
+    return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" spk_status spk_render_noalloc(spk_ctx *ctx, uint32_t num_frames, void *d_hdr_rgba, void *d_rgba16f) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (!d_hdr_rgba || !d_rgba16f) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "null output buffer");
+    if (!ctx->has_scene || !ctx->has_config || !ctx->has_camera)
+        return fail(ctx, SPK_ERR_NOT_READY, "render needs spk_set_scene, spk_set_config and spk_set_camera first");
+    const uint64_t npix = static_cast<uint64_t>(ctx->cfg.width) * ctx->cfg.height;
+    if (npix > SPK_NOALLOC_MAX_PIXELS)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT,
+                    "spk_render_noalloc supports at most %u pixels (512 x 512); the config has %llu", SPK_NOALLOC_MAX_PIXELS,
+                    static_cast<unsigned long long>(npix));
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "set device");
+    unsigned char *scratch = nullptr;
+    if ((e = noalloc_scratch(ctx->device, &scratch)) != cudaSuccess) return cuda_fail(ctx, e, "scratch address");
+    float4 *gcolor = reinterpret_cast<float4 *>(scratch);
+    float4 *gnormal = gcolor + SPK_NOALLOC_MAX_PIXELS;
+    auto *counters = reinterpret_cast<Counters *>(scratch + kNoallocGbufferBytes);
+    FrameBuffers fbuf{gcolor, gnormal, static_cast<float4 *>(d_hdr_rgba), static_cast<ushort4 *>(d_rgba16f),
+                      ctx->cfg.width, ctx->cfg.height};
+    // The array keeps the previous call's contents; only the counters must start at zero (the G-buffer is
+    // fully written by every frame before it is read).
+    if ((e = cudaMemsetAsync(counters, 0, sizeof(Counters), ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "counter reset");
+    for (uint32_t f = 0; f < num_frames; ++f) {
+        // The same per-frame bookkeeping as spk_render (CameraRenderProxy.cpp:66-75, CPURenderer.cpp:128-137).
+        if (ctx->dirty) {
+            ctx->cumulated = 0;
+            ctx->pending = 0;
+        }
+        ctx->cumulated = std::min(ctx->cfg.max_spp, ctx->cumulated + ctx->pending);
+        ctx->pending = 0;
+        if (ctx->dirty) {
+            if ((e = cudaMemsetAsync(d_hdr_rgba, 0, npix * sizeof(float4), ctx->stream)) != cudaSuccess)
+                return cuda_fail(ctx, e, "frame buffer clear");
+            ctx->dirty = false;
+            ctx->dispatched = 0;
+        }
+        const RenderParams p{ctx->dispatched, ctx->cfg.bounce, ctx->cfg.rng, ctx->cfg.seed, ctx->cfg.spatial_denoise,
+                             ctx->cfg.enable_nee};
+        if ((e = launch_render_mega(ctx->scene, ctx->cam, fbuf, p, false, counters, ctx->stream, nullptr)) !=
+            cudaSuccess)
+            return cuda_fail(ctx, e, "base pass launch");
+        const float mavg = static_cast<float>(ctx->cumulated) / static_cast<float>(ctx->cumulated + ctx->spp_eff);
+        if ((e = launch_resolve(fbuf, mavg, ctx->cam.exposure, ctx->cfg.spatial_denoise, ctx->stream)) != cudaSuccess)
+            return cuda_fail(ctx, e, "resolve launch");
+        ctx->dispatched += ctx->spp_eff;
+        ctx->pending += ctx->spp_eff;
+    }
+    return SPK_OK;
+}

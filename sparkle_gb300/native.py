@@ -21,7 +21,7 @@ SPK_ERRORS = {0: "ok", 1: "invalid argument", 2: "cuda error", 3: "out of memory
 EXPORTED = ["spk_abi_version", "spk_create", "spk_destroy", "spk_last_error", "spk_set_scene", "spk_set_camera",
             "spk_camera_from_look", "spk_set_config", "spk_render", "spk_read_framebuffer",
             "spk_framebuffer_device", "spk_sample_counts", "spk_is_converged", "spk_trace", "spk_trace_device",
-            "spk_synchronize", "spk_get_stats", "spk_set_instrumentation"]
+            "spk_synchronize", "spk_get_stats", "spk_set_instrumentation", "spk_render_noalloc"]
 
 
 class SpkError(RuntimeError):
@@ -65,6 +65,7 @@ def lib(build: bool = True):
         L.spk_synchronize.argtypes = [vp]
         L.spk_get_stats.argtypes = [vp, vp]
         L.spk_set_instrumentation.argtypes = [vp, u32]
+        L.spk_render_noalloc.argtypes = [vp, u32, vp, vp]
         for name in EXPORTED:
             if name != "spk_last_error" and getattr(L, name).restype is C.c_int:
                 getattr(L, name).restype = i32
@@ -155,6 +156,10 @@ class Context:
 
     def trace_device(self, d_rays: int, n: int, d_hits: int, any_hit: bool = False):
         self._check(self.L.spk_trace_device(self.h, C.c_void_p(d_rays), n, C.c_void_p(d_hits), int(any_hit)))
+
+    def render_noalloc(self, frames: int, d_hdr: int, d_rgba16f: int):
+        """spk_render_noalloc: renders into caller-owned device buffers without allocating (see include/spk.h)."""
+        self._check(self.L.spk_render_noalloc(self.h, frames, C.c_void_p(d_hdr), C.c_void_p(d_rgba16f)))
 
     def set_instrumentation(self, count_traffic: bool):
         self._check(self.L.spk_set_instrumentation(self.h, 1 if count_traffic else 0))
