@@ -184,6 +184,15 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def parse_tune(text: str) -> dict:
+    """"knob=value,knob=value" -> spk_tuning fields."""
+    out = {}
+    for item in filter(None, text.split(",")):
+        k, v = item.split("=")
+        out[k.strip()] = int(v)
+    return out
+
+
 def run_ours(args):
     rank, world, local_rank = dist_env()
     import numpy as np
@@ -194,6 +203,8 @@ def run_ours(args):
     scene, cam_args = scenes.terrain_spheres(0)
     camera = scenes.make_camera(cam_args, WIDTH, HEIGHT)
     ctx = native.Context(local_rank)
+    if args.tune:
+        ctx.set_tuning(**parse_tune(args.tune))
     ctx.set_scene(scene)
     cfg = abi.make_config(WIDTH, HEIGHT, spp=1, max_spp=4096, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS,
                           seed=rank, kernel=args.kernel)
@@ -285,7 +296,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": round(elapsed_s * 1000.0 / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": dict(workload_config(), kernel={0: "auto(wavefront)", 1: "megakernel", 2: "wavefront"}[args.kernel],
-                       parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+                       parallelism=f"replicas x{world}" if world > 1 else "single GPU", tuning=ctx.tuning()),
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -351,6 +362,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--kernel", type=int, default=0, help="0 auto, 1 megakernel, 2 wavefront")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tune", default="", help="spk_tuning knobs, e.g. cuda_graph=0,material_sort=1,bvh_width=4")
     ap.add_argument("--profile-small", action="store_true",
                     help="ncu capture case: the bench workload cut to 2 frames, no timing output")
     ap.add_argument("--profile-rays", action="store_true",

@@ -188,9 +188,25 @@ typedef struct spk_stats {
     uint64_t bvh_bytes;      /* bytes of wide nodes + triangle records resident */
     uint64_t node_visits;    /* wide nodes visited (only with SPK_INSTR_COUNT_TRAFFIC) */
     uint64_t triangle_tests; /* ray-triangle tests run (only with SPK_INSTR_COUNT_TRAFFIC) */
+    uint32_t graph_replays;  /* CUDA graph launches of the multi-frame iteration chunk (spk_tuning.cuda_graph) */
+    uint32_t reserved0;
 } spk_stats;
 
 enum { SPK_INSTR_NONE = 0, SPK_INSTR_COUNT_TRAFFIC = 1 };
+
+/* Performance knobs (no reference counterpart: the reference's cpu pipeline has none). None of them changes
+ * a result: closest hits are resolved with a tie-break independent of the tree's shape and every sample
+ * draws its random numbers from its own (pixel, sample) seed, so any setting renders the same bits.
+ * spk_tuning_defaults() fills the defaults; sparkle_gb300.autotune searches them per scene. */
+typedef struct spk_tuning {
+    uint32_t cuda_graph;           /* 1: replay each multi-frame iteration chunk as one CUDA graph (default 1) */
+    uint32_t material_sort;        /* 1: group each shade queue by material class before shading (default 0) */
+    uint32_t bvh_width;            /* children per wide node, 2..8 (default 8); used by the next spk_set_scene */
+    uint32_t bvh_leaf_size;        /* items per BVH leaf, 1..3 (default 3); used by the next spk_set_scene */
+    uint32_t extend_blocks_per_sm; /* traversal CTAs per SM, 0 = the occupancy maximum (default 0) */
+    uint32_t shade_blocks_per_sm;  /* shading CTAs per SM, 1..32 (default 8) */
+    uint32_t reserved[2];          /* must be 0 */
+} spk_tuning;
 
 /* ------------------------------------------------------------------------------------------------ */
 /* Entry points                                                                                      */
@@ -271,6 +287,14 @@ spk_status spk_get_stats(spk_ctx *ctx, spk_stats *out);
  * libraries/include/core/Profiler.h:9-28): SPK_INSTR_COUNT_TRAFFIC switches the traversal kernels to
  * variants that also count visited nodes and tested triangles (slower; results are unchanged). */
 spk_status spk_set_instrumentation(spk_ctx *ctx, uint32_t flags);
+
+/* Default performance knobs. */
+void spk_tuning_defaults(spk_tuning *out);
+
+/* Sets / reads the context's performance knobs (see spk_tuning). Rejects out-of-range values with
+ * SPK_ERR_INVALID_ARGUMENT and leaves the previous setting in place. */
+spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *tuning);
+spk_status spk_get_tuning(const spk_ctx *ctx, spk_tuning *out);
 
 /* Largest width * height spk_render_noalloc accepts (512 x 512). */
 #define SPK_NOALLOC_MAX_PIXELS (512u * 512u)

@@ -69,7 +69,13 @@ class spk_stats(C.Structure):
     _fields_ = [("extension_rays", C.c_uint64), ("shadow_rays", C.c_uint64), ("paths", C.c_uint64),
                 ("device_ms", _f), ("trace_kernel_ms", _f), ("trace_launches", _u32), ("kernel_launches", _u32),
                 ("error_flags", _u32), ("bvh_nodes", _u32), ("bvh_bytes", C.c_uint64),
-                ("node_visits", C.c_uint64), ("triangle_tests", C.c_uint64)]
+                ("node_visits", C.c_uint64), ("triangle_tests", C.c_uint64), ("graph_replays", _u32),
+                ("reserved0", _u32)]
+
+
+class spk_tuning(C.Structure):
+    _fields_ = [("cuda_graph", _u32), ("material_sort", _u32), ("bvh_width", _u32), ("bvh_leaf_size", _u32),
+                ("extend_blocks_per_sm", _u32), ("shade_blocks_per_sm", _u32), ("reserved", _u32 * 2)]
 
 
 HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4"), ("face", "<u4")])

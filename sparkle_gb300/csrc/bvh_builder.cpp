@@ -251,7 +251,8 @@ Bvh2 build_bvh2(const std::vector<BuildBox> &boxes, uint32_t max_leaf, int num_t
     return out;
 }
 
-WideBvh collapse_wide(const Bvh2 &bvh) {
+WideBvh collapse_wide(const Bvh2 &bvh, int max_children) {
+    max_children = std::max(2, std::min(8, max_children));
     WideBvh out;
     if (bvh.nodes.empty()) return out;
     out.nodes.reserve(bvh.nodes.size() / 4 + 1);
@@ -264,14 +265,14 @@ WideBvh collapse_wide(const Bvh2 &bvh) {
     for (size_t qi = 0; qi < queue.size(); ++qi) {
         const Job job = queue[qi];
         const Bvh2Node &root = bvh.nodes[job.bvh_node];
-        // Open the binary subtree until 8 children: always expand the inner child of largest area.
+        // Open the binary subtree until max_children children: always expand the inner child of largest area.
         std::vector<uint32_t> kids;
         if (root.count > 0) {
             kids.push_back(job.bvh_node);  // a leaf root becomes a node with a single leaf child
         } else {
             kids.push_back(root.first);
             kids.push_back(root.first + 1);
-            while (kids.size() < 8) {
+            while (static_cast<int>(kids.size()) < max_children) {
                 int best = -1;
                 float best_area = -1.f;
                 for (size_t k = 0; k < kids.size(); ++k) {

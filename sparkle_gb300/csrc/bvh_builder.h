@@ -52,6 +52,8 @@ struct WideBvh {
 };
 
 // Collapses a binary BVH (leaves of <= 3 items) into 8-wide quantised nodes.
-WideBvh collapse_wide(const Bvh2 &bvh);
+// `max_children` (2..8) caps the children opened per wide node; fewer children give smaller effective
+// fan-out (more, emptier nodes) in the same 80-byte record.
+WideBvh collapse_wide(const Bvh2 &bvh, int max_children = 8);
 
 }  // namespace spk

@@ -47,11 +47,16 @@ struct LaunchEvents {
     cudaEvent_t *pairs = nullptr;  // 2 * capacity events
     int capacity = 0;
     int used = 0;
+    float graph_ms = 0.f;   // traversal time measured inside replayed CUDA graphs
+    int graph_launches = 0;  // traversal launches inside replayed CUDA graphs
+    // cudaEventRecordExternal while a stream is captured: the record becomes a graph node that every replay
+    // performs (a plain record under capture only orders work inside the graph).
+    unsigned record_flags = cudaEventRecordDefault;
     void before(cudaStream_t s) {
-        if (pairs && used < capacity) cudaEventRecord(pairs[2 * used], s);
+        if (pairs && used < capacity) cudaEventRecordWithFlags(pairs[2 * used], s, record_flags);
     }
     void after(cudaStream_t s) {
-        if (pairs && used < capacity) cudaEventRecord(pairs[2 * used++ + 1], s);
+        if (pairs && used < capacity) cudaEventRecordWithFlags(pairs[2 * used++ + 1], s, record_flags);
     }
 };
 

@@ -39,6 +39,12 @@ struct DevBuf {
     }
 };
 
+spk_tuning default_tuning() {
+    spk_tuning t{};
+    spk_tuning_defaults(&t);
+    return t;
+}
+
 }  // namespace
 
 struct spk_ctx {
@@ -76,6 +82,8 @@ struct spk_ctx {
     DevBuf<float4> gcolor, gnormal, fb;
     DevBuf<ushort4> out;
     WavefrontState wf{};
+    ChunkGraph chunk_graph{};
+    spk_tuning tuning = default_tuning();
 
     // CameraRenderProxy / CPURenderer sample bookkeeping
     uint32_t cumulated = 0, pending = 0, dispatched = 0;
@@ -166,6 +174,8 @@ cudaError_t prepare_events(spk_ctx *ctx, size_t pairs) {
     ctx->launch_events.pairs = ctx->event_pool.data();
     ctx->launch_events.capacity = static_cast<int>(ctx->event_pool.size() / 2);
     ctx->launch_events.used = 0;
+    ctx->launch_events.graph_ms = 0.f;
+    ctx->launch_events.graph_launches = 0;
     return cudaSuccess;
 }
 
@@ -226,6 +236,7 @@ spk_status spk_destroy(spk_ctx *ctx) {
     ctx->fb.reset();
     ctx->out.reset();
     wavefront_free(ctx->wf);
+    chunk_graph_free(ctx->chunk_graph);
     if (ctx->counters) cudaFree(ctx->counters);
     for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
@@ -314,8 +325,8 @@ spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_mesh
             }
             boxes[f] = b;
         }
-        const Bvh2 b2 = build_bvh2(boxes, 3, threads);
-        const WideBvh wide = collapse_wide(b2);
+        const Bvh2 b2 = build_bvh2(boxes, ctx->tuning.bvh_leaf_size, threads);
+        const WideBvh wide = collapse_wide(b2, static_cast<int>(ctx->tuning.bvh_width));
         const uint32_t tri_offset = static_cast<uint32_t>(tri_recs.size() / 3);
         blas_root[k] = static_cast<uint32_t>(all_nodes.size());
         append_wide(all_nodes, wide, tri_offset);
@@ -372,8 +383,8 @@ spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_mesh
     uint32_t tlas_root = kInvalid;
     std::vector<uint32_t> tlas_items;
     if (num_instances > 0) {
-        const Bvh2 b2 = build_bvh2(inst_boxes, 3, threads);
-        const WideBvh wide = collapse_wide(b2);
+        const Bvh2 b2 = build_bvh2(inst_boxes, ctx->tuning.bvh_leaf_size, threads);
+        const WideBvh wide = collapse_wide(b2, static_cast<int>(ctx->tuning.bvh_width));
         tlas_root = static_cast<uint32_t>(all_nodes.size());
         append_wide(all_nodes, wide, 0);
         tlas_items = wide.items;
@@ -578,6 +589,14 @@ spk_status spk_set_config(spk_ctx *ctx, const spk_config *config) {
     return SPK_OK;
 }
 
+static WfTuning wf_tuning(const spk_ctx *ctx) {
+    WfTuning t;
+    t.extend_blocks_per_sm = ctx->tuning.extend_blocks_per_sm;
+    t.shade_blocks_per_sm = ctx->tuning.shade_blocks_per_sm;
+    t.material_sort = ctx->tuning.material_sort != 0;
+    return t;
+}
+
 static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
     FrameBuffers fbuf{ctx->gcolor.ptr, ctx->gnormal.ptr, ctx->fb.ptr, ctx->out.ptr, ctx->cfg.width, ctx->cfg.height};
     cudaError_t e;
@@ -619,14 +638,20 @@ static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
             return cuda_fail(ctx, e, "frame buffer clear");
         RenderParams p{0u, ctx->cfg.bounce, ctx->cfg.rng, ctx->cfg.seed, 0u, ctx->cfg.enable_nee};
         uint32_t launches = 0;
+        ctx->chunk_graph.enabled = ctx->tuning.cuda_graph != 0;
+        const uint32_t replays0 = ctx->chunk_graph.replays;
         e = launch_render_multiframe(ctx->scene, ctx->cam, fbuf, p, num_frames, ctx->frame_weights.data(),
                                      ctx->frame_seeds.data(), count, ctx->counters, ctx->wf, ctx->num_sms,
-                                     ctx->stream, &launches, &ctx->launch_events);
-        if (e != cudaSuccess) return cuda_fail(ctx, e, "multi-frame wavefront");
+                                     ctx->stream, &launches, &ctx->launch_events, wf_tuning(ctx), &ctx->chunk_graph);
+        if (e != cudaSuccess) {
+            const std::string what = std::string("multi-frame wavefront (") + wavefront_error_site() + ")";
+            return cuda_fail(ctx, e, what.c_str());
+        }
         ctx->launches_in_call = launches;
         if ((e = cudaEventRecord(ctx->ev_stop, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "event");
         ctx->last = spk_stats{};
         ctx->last.paths = static_cast<uint64_t>(num_frames) * ctx->cfg.width * ctx->cfg.height;
+        ctx->last.graph_replays = ctx->chunk_graph.replays - replays0;
         ctx->stats_pending = true;
         return SPK_OK;
     }
@@ -650,7 +675,7 @@ static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
         uint32_t launches = 0;
         if (wavefront) {
             e = launch_render_wavefront(ctx->scene, ctx->cam, fbuf, p, count, ctx->counters, ctx->wf, ctx->num_sms,
-                                        ctx->stream, &launches, &ctx->launch_events);
+                                        ctx->stream, &launches, &ctx->launch_events, wf_tuning(ctx));
         } else {
             e = launch_render_mega(ctx->scene, ctx->cam, fbuf, p, count, ctx->counters, ctx->stream,
                                    &ctx->launch_events);
@@ -801,14 +826,45 @@ spk_status spk_get_stats(spk_ctx *ctx, spk_stats *out) {
             cudaEventElapsedTime(&x, le.pairs[2 * k], le.pairs[2 * k + 1]);
             tms += x;
         }
-        ctx->last.trace_kernel_ms = tms;
-        ctx->last.trace_launches = static_cast<uint32_t>(le.used);
+        ctx->last.trace_kernel_ms = tms + le.graph_ms;
+        ctx->last.trace_launches = static_cast<uint32_t>(le.used + le.graph_launches);
         ctx->last.kernel_launches = ctx->launches_in_call;
         ctx->stats_pending = false;
     }
     ctx->last.bvh_nodes = ctx->bvh_nodes;
     ctx->last.bvh_bytes = ctx->bvh_bytes;
     *out = ctx->last;
+    return SPK_OK;
+}
+
+void spk_tuning_defaults(spk_tuning *out) {
+    if (!out) return;
+    *out = spk_tuning{};
+    out->cuda_graph = 1;
+    out->material_sort = 0;
+    out->bvh_width = 8;
+    out->bvh_leaf_size = 3;
+    out->extend_blocks_per_sm = 0;
+    out->shade_blocks_per_sm = 8;
+}
+
+spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
+    if (!ctx || !t) return SPK_ERR_INVALID_ARGUMENT;
+    if (t->cuda_graph > 1 || t->material_sort > 1)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "cuda_graph and material_sort take 0 or 1");
+    if (t->bvh_width < 2 || t->bvh_width > 8) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "bvh_width must be 2..8");
+    if (t->bvh_leaf_size < 1 || t->bvh_leaf_size > 3)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "bvh_leaf_size must be 1..3");
+    if (t->extend_blocks_per_sm > 32 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 32)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "blocks per SM out of range");
+    if (t->reserved[0] || t->reserved[1]) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "reserved fields must be 0");
+    ctx->tuning = *t;
+    return SPK_OK;
+}
+
+spk_status spk_get_tuning(const spk_ctx *ctx, spk_tuning *out) {
+    if (!ctx || !out) return SPK_ERR_INVALID_ARGUMENT;
+    *out = ctx->tuning;
     return SPK_OK;
 }
 

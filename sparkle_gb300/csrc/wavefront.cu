@@ -4,6 +4,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cstring>
 
 #include "wavefront.cuh"
 
@@ -304,6 +305,75 @@ __global__ void __launch_bounds__(128) k_mf_shade(DevScene S, DevCamera cam, Fra
     if (err) atomicOr(&counters->error_flags, err);
 }
 
+// ------------------------------------------------------------------------------------------------
+// Material sort: group a shade queue by the material class of each path's hit (counting sort), so the
+// warps of the shade stage run one BSDF branch and read one material record.
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t sort_class(const DevScene &S, const WavefrontState &s, uint32_t pid) {
+    const uint32_t inst = __float_as_uint(s.hit[pid].w);
+    if (inst == kInvalid) return kSortBuckets - 1;
+    return min(S.instances[inst].material, kSortBuckets - 2);
+}
+
+__global__ void __launch_bounds__(256) k_sort_hist(DevScene S, WavefrontState s, int in_queue, Counters *counters) {
+    __shared__ uint32_t h[kSortBuckets];
+    for (uint32_t b = threadIdx.x; b < kSortBuckets; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    const unsigned long long n = counters->queue_counters[in_queue];
+    const uint32_t *queue = s.queue[in_queue];
+    for (unsigned long long q = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+         q += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
+        atomicAdd(&h[sort_class(S, s, queue[q])], 1u);
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < kSortBuckets; b += blockDim.x)
+        if (h[b]) atomicAdd(&s.sort_hist[b], h[b]);
+}
+
+// Exclusive scan of the histogram into the scatter cursors; clears the histogram for the next sort.
+__global__ void __launch_bounds__(kSortBuckets) k_sort_scan(WavefrontState s) {
+    __shared__ uint32_t v[kSortBuckets];
+    const uint32_t b = threadIdx.x;
+    v[b] = s.sort_hist[b];
+    s.sort_hist[b] = 0;
+    __syncthreads();
+    uint32_t prefix = 0;
+    for (uint32_t k = 0; k < b; ++k) prefix += v[k];
+    s.sort_hist[kSortBuckets + b] = prefix;
+}
+
+__global__ void __launch_bounds__(256) k_sort_scatter(DevScene S, WavefrontState s, int in_queue, Counters *counters) {
+    const unsigned long long n = counters->queue_counters[in_queue];
+    const uint32_t *queue = s.queue[in_queue];
+    const uint32_t lane = threadIdx.x & 31u;
+    for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
+         q0 += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+        const unsigned long long q = q0 + threadIdx.x;
+        const bool active = q < n;
+        const uint32_t pid = active ? queue[q] : 0u;
+        const uint32_t key = active ? sort_class(S, s, pid) : kSortBuckets;  // inactive lanes: own group
+        // One atomic per (warp, class): lanes with the same class share a base.
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+        const uint32_t leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (active && lane == leader) base = atomicAdd(&s.sort_hist[kSortBuckets + key], __popc(peers));
+        base = __shfl_sync(0xFFFFFFFFu, base, leader);
+        if (active) s.sort_keys[base + __popc(peers & ((1u << lane) - 1u))] = pid;
+    }
+}
+
+// Enqueues the sort of queue `in`; returns the state the shade stage reads (its queue `in` replaced by
+// the grouped copy).
+WavefrontState enqueue_material_sort(const DevScene &scene, const WavefrontState &s, int in, Counters *counters,
+                                     int num_sms, cudaStream_t stream) {
+    const unsigned grid = static_cast<unsigned>(num_sms) * 4u;
+    k_sort_hist<<<grid, 256, 0, stream>>>(scene, s, in, counters);
+    k_sort_scan<<<1, kSortBuckets, 0, stream>>>(s);
+    k_sort_scatter<<<grid, 256, 0, stream>>>(scene, s, in, counters);
+    WavefrontState sorted = s;
+    sorted.queue[in] = s.sort_keys;
+    return sorted;
+}
+
 __device__ __forceinline__ float aces_tonemap(float c, float exposure) {
     const float x = c * exposure;
     float y = (x * (x * 2.51f + 0.03f)) / (x * (x * 2.43f + 0.59f) + 0.14f);
@@ -340,26 +410,28 @@ cudaError_t dmalloc(T *&p, size_t count) {
     return cudaMalloc(reinterpret_cast<void **>(&p), count * sizeof(T));
 }
 
-unsigned extend_blocks(int num_sms) {
+unsigned extend_blocks(int num_sms, uint32_t per_sm_override) {
     static int per_sm = 0;
     if (per_sm == 0) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_extend<false>, 128, 0) != cudaSuccess ||
             per_sm <= 0)
             per_sm = 8;
     }
-    return static_cast<unsigned>(num_sms * per_sm);
+    const uint32_t n = per_sm_override ? std::min<uint32_t>(per_sm_override, static_cast<uint32_t>(per_sm))
+                                       : static_cast<uint32_t>(per_sm);
+    return static_cast<unsigned>(num_sms) * n;
 }
 
 cudaError_t launch_extend(const DevScene &scene, WavefrontState &s, int in, bool count, Counters *counters,
-                          int num_sms, cudaStream_t stream, LaunchEvents *ev) {
+                          unsigned grid, cudaStream_t stream, LaunchEvents *ev) {
     unsigned long long *qc = counters->queue_counters;
     cudaError_t e = cudaMemsetAsync(qc + kCursor, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     if (ev) ev->before(stream);
     if (count) {
-        k_wf_extend<true><<<extend_blocks(num_sms), 128, 0, stream>>>(scene, s, in, counters);
+        k_wf_extend<true><<<grid, 128, 0, stream>>>(scene, s, in, counters);
     } else {
-        k_wf_extend<false><<<extend_blocks(num_sms), 128, 0, stream>>>(scene, s, in, counters);
+        k_wf_extend<false><<<grid, 128, 0, stream>>>(scene, s, in, counters);
     }
     if (ev) ev->after(stream);
     return cudaSuccess;
@@ -377,6 +449,8 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
         (e = dmalloc(s.queue[0], capacity)) != cudaSuccess || (e = dmalloc(s.queue[1], capacity)) != cudaSuccess ||
         (e = dmalloc(s.sort_keys, capacity)) != cudaSuccess || (e = dmalloc(s.slot_state, capacity)) != cudaSuccess ||
         (e = dmalloc(s.slot_item, capacity)) != cudaSuccess || (e = dmalloc(s.prev_pdf, capacity)) != cudaSuccess ||
+        (e = dmalloc(s.sort_hist, 2 * kSortBuckets)) != cudaSuccess ||
+        (e = cudaMemset(s.sort_hist, 0, 2 * kSortBuckets * sizeof(uint32_t))) != cudaSuccess ||
         (e = cudaHostAlloc(reinterpret_cast<void **>(&s.host_len), sizeof(unsigned long long), cudaHostAllocDefault)) !=
             cudaSuccess) {
         wavefront_free(s);
@@ -389,16 +463,26 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
 void wavefront_free(WavefrontState &s) {
     void *ptrs[] = {s.ray_o,      s.ray_d,     s.thr,     s.color,        s.rng,        s.hit,
                     s.hit_face,   s.queue[0],  s.queue[1], s.sort_keys,   s.slot_state, s.slot_item,
-                    s.samples,    s.frame_weight, s.frame_seed, s.prev_pdf};
+                    s.samples,    s.frame_weight, s.frame_seed, s.prev_pdf, s.sort_hist};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s.host_len) cudaFreeHost(s.host_len);
     s = WavefrontState{};
 }
 
+void chunk_graph_free(ChunkGraph &g) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    for (cudaEvent_t ev : g.events)
+        if (ev) cudaEventDestroy(ev);
+    const bool enabled = g.enabled;
+    g = ChunkGraph{};
+    g.enabled = enabled;
+}
+
 cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
                                     const RenderParams &p, bool count, Counters *counters, WavefrontState &s,
-                                    int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev) {
+                                    int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev,
+                                    const WfTuning &tuning) {
     uint32_t nl = 0;
     const uint32_t npix = fbuf.width * fbuf.height;
     if (s.capacity < npix) return cudaErrorInvalidValue;
@@ -412,25 +496,21 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
         k_wf_generate<1><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, counters);
     }
     ++nl;
-    const unsigned shade_blocks = static_cast<unsigned>(num_sms) * 8u;
+    const unsigned shade_blocks = static_cast<unsigned>(num_sms) * tuning.shade_blocks_per_sm;
+    const unsigned extend_grid = extend_blocks(num_sms, tuning.extend_blocks_per_sm);
     for (uint32_t b = 0; b < p.bounce; ++b) {
         const int in = static_cast<int>(b & 1u), out = in ^ 1;
         if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
-        if ((e = launch_extend(scene, s, in, count, counters, num_sms, stream, ev)) != cudaSuccess) return e;
+        if ((e = launch_extend(scene, s, in, count, counters, extend_grid, stream, ev)) != cudaSuccess) return e;
         ++nl;
-        if (p.rng == 0) {
-            if (p.enable_nee) {
-                k_wf_shade<0, true><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
-            } else {
-                k_wf_shade<0, false><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
-            }
-        } else {
-            if (p.enable_nee) {
-                k_wf_shade<1, true><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
-            } else {
-                k_wf_shade<1, false><<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, s, in, b, counters);
-            }
+        WavefrontState ss = s;
+        if (tuning.material_sort) {
+            ss = enqueue_material_sort(scene, s, in, counters, num_sms, stream);
+            nl += 3;
         }
+        auto *shade = p.rng == 0 ? (p.enable_nee ? k_wf_shade<0, true> : k_wf_shade<0, false>)
+                                 : (p.enable_nee ? k_wf_shade<1, true> : k_wf_shade<1, false>);
+        shade<<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, ss, in, b, counters);
         ++nl;
     }
     k_wf_finish<<<(npix + 255) / 256, 256, 0, stream>>>(fbuf, s);
@@ -439,12 +519,20 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
     return cudaGetLastError();
 }
 
+namespace {
+thread_local const char *t_site = "";
+}
+
+const char *wavefront_error_site() { return t_site; }
+
 cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
                                      const RenderParams &p, uint32_t num_frames, const float *weights,
                                      const uint32_t *seeds, bool count, Counters *counters, WavefrontState &s,
-                                     int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev) {
+                                     int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev,
+                                     const WfTuning &tuning, ChunkGraph *graph) {
     uint32_t nl = 0;
     const uint32_t npix = fbuf.width * fbuf.height;
+    t_site = "set-up";
     if (s.capacity < npix || num_frames == 0 || p.bounce == 0) return cudaErrorInvalidValue;
     cudaError_t e;
     if (s.frame_capacity < num_frames) {
@@ -472,8 +560,10 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
             cudaSuccess)
         return e;
     unsigned long long *qc = counters->queue_counters;
-    const unsigned shade_blocks = static_cast<unsigned>(num_sms) * 8u;
-    constexpr uint32_t kChunk = 8;
+    const unsigned shade_blocks = static_cast<unsigned>(num_sms) * tuning.shade_blocks_per_sm;
+    const unsigned extend_grid = extend_blocks(num_sms, tuning.extend_blocks_per_sm);
+    constexpr uint32_t kChunk = kChunkIterations;
+    static_assert(kChunk % 2 == 0, "a chunk must keep the queue parity, so one graph serves every chunk");
     for (uint32_t f0 = 0; f0 < num_frames; f0 += kFramesPerPass) {
         const uint32_t frames = std::min(kFramesPerPass, num_frames - f0);
         const uint32_t total_items = frames * npix;
@@ -484,28 +574,130 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
             k_mf_generate<1><<<(npix + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, counters);
         }
         ++nl;
+        // One chunk: kChunk iterations of (reset the output queue, extend, shade).
+        auto enqueue_chunk = [&](LaunchEvents *chunk_ev) -> cudaError_t {
+            cudaError_t ce;
+            for (uint32_t c = 0; c < kChunk; ++c) {
+                const int in = static_cast<int>(c & 1u), out = in ^ 1;
+                if ((ce = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return ce;
+                if ((ce = launch_extend(scene, s, in, count, counters, extend_grid, stream, chunk_ev)) != cudaSuccess)
+                    return ce;
+                const WavefrontState ss =
+                    tuning.material_sort ? enqueue_material_sort(scene, s, in, counters, num_sms, stream) : s;
+                auto *shade = p.rng == 0 ? (p.enable_nee ? k_mf_shade<0, true> : k_mf_shade<0, false>)
+                                         : (p.enable_nee ? k_mf_shade<1, true> : k_mf_shade<1, false>);
+                shade<<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, ss, in, f0, total_items, counters);
+            }
+            return cudaGetLastError();
+        };
+        bool use_graph = false;
+        LaunchEvents graph_ev{};
+        if (graph && graph->enabled) {
+            // The graph is keyed by every value its launches take; a new key re-captures it and updates
+            // the executable graph in place when the topology allows.
+            struct Key {
+                DevScene scene;
+                DevCamera cam;
+                FrameBuffers fbuf;
+                RenderParams p;
+                WavefrontState s;
+                uint32_t f0, total_items, count, num_sms;
+                Counters *counters;
+                cudaStream_t stream;
+                unsigned extend_grid, shade_grid, material_sort;
+            } key;
+            std::memset(&key, 0, sizeof(key));
+            key.scene = scene;
+            key.cam = cam;
+            key.fbuf = fbuf;
+            key.p = p;
+            key.s = s;
+            key.f0 = f0;
+            key.total_items = total_items;
+            key.count = count;
+            key.num_sms = static_cast<uint32_t>(num_sms);
+            key.counters = counters;
+            key.stream = stream;
+            key.extend_grid = extend_grid;
+            key.shade_grid = shade_blocks;
+            key.material_sort = tuning.material_sort;
+            const auto *kb = reinterpret_cast<const unsigned char *>(&key);
+            graph_ev.pairs = graph->events;
+            graph_ev.capacity = static_cast<int>(kChunk);
+            graph_ev.record_flags = cudaEventRecordExternal;
+            if (!graph->events[0]) {
+                for (cudaEvent_t &g_ev : graph->events)
+                    if ((e = cudaEventCreate(&g_ev)) != cudaSuccess) return e;
+            }
+            use_graph = true;
+            if (!graph->exec || graph->key.size() != sizeof(key) || std::memcmp(graph->key.data(), kb, sizeof(key))) {
+                cudaGraph_t g = nullptr;
+                t_site = "graph capture";
+                if ((e = cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) return e;
+                const cudaError_t enq = enqueue_chunk(ev ? &graph_ev : nullptr);
+                if ((e = cudaStreamEndCapture(stream, &g)) != cudaSuccess) return e;
+                if (enq != cudaSuccess) {
+                    cudaGraphDestroy(g);
+                    return enq;
+                }
+                bool updated = false;
+                if (graph->exec) {
+                    cudaGraphExecUpdateResultInfo info;
+                    updated = cudaGraphExecUpdate(graph->exec, g, &info) == cudaSuccess;
+                    if (!updated) {
+                        cudaGetLastError();
+                        cudaGraphExecDestroy(graph->exec);
+                        graph->exec = nullptr;
+                    }
+                }
+                t_site = "graph instantiate";
+                if (!updated) e = cudaGraphInstantiate(&graph->exec, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    graph->exec = nullptr;
+                    return e;
+                }
+                graph->key.assign(kb, kb + sizeof(key));
+                graph->timed = ev != nullptr;
+                ++graph->captures;
+            }
+            if (graph->timed != (ev != nullptr)) {
+                graph->key.clear();  // timing events differ: force a re-capture next time
+                use_graph = false;
+            }
+        }
         // Each iteration advances every live slot by one segment and no item is started twice, so the
         // pass ends within frames * bounce iterations; the queue length is read back every kChunk.
         const uint64_t max_iters = static_cast<uint64_t>(frames) * p.bounce + kChunk;
         uint64_t iter = 0;
         for (;;) {
-            for (uint32_t c = 0; c < kChunk; ++c, ++iter) {
-                const int in = static_cast<int>(iter & 1u), out = in ^ 1;
-                if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
-                if ((e = launch_extend(scene, s, in, count, counters, num_sms, stream, ev)) != cudaSuccess) return e;
-                auto *shade = p.rng == 0 ? (p.enable_nee ? k_mf_shade<0, true> : k_mf_shade<0, false>)
-                                         : (p.enable_nee ? k_mf_shade<1, true> : k_mf_shade<1, false>);
-                shade<<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, s, in, f0, total_items, counters);
-                nl += 2;
+            t_site = use_graph ? "graph launch" : "chunk launch";
+            if (use_graph) {
+                if ((e = cudaGraphLaunch(graph->exec, stream)) != cudaSuccess) return e;
+                ++graph->replays;
+            } else if ((e = enqueue_chunk(ev)) != cudaSuccess) {
+                return e;
             }
-            if ((e = cudaGetLastError()) != cudaSuccess) return e;
-            if ((e = cudaMemcpyAsync(s.host_len, qc + (iter & 1u), sizeof(unsigned long long),
-                                     cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
+            iter += kChunk;
+            nl += (tuning.material_sort ? 5u : 2u) * kChunk;
+            if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
+                cudaSuccess)
                 return e;
             if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
+            t_site = "graph timing events";
+            if (use_graph && ev) {
+                for (uint32_t c = 0; c < kChunk; ++c) {
+                    float x = 0.f;
+                    if ((e = cudaEventElapsedTime(&x, graph->events[2 * c], graph->events[2 * c + 1])) != cudaSuccess)
+                        return e;
+                    ev->graph_ms += x;
+                }
+                ev->graph_launches += static_cast<int>(kChunk);
+            }
             if (*s.host_len == 0) break;
             if (iter > max_iters) return cudaErrorLaunchFailure;  // cannot happen: every slot makes progress
         }
+        t_site = "resolve";
         k_mf_resolve<<<(npix + 255) / 256, 256, 0, stream>>>(fbuf, s, f0, frames, cam.exposure);
         ++nl;
     }

@@ -8,6 +8,8 @@
 // the same random numbers in the same order as the one-kernel schedule, so both write identical G-buffers.
 #pragma once
 
+#include <vector>
+
 #include "kernels.cuh"
 
 namespace spk {
@@ -22,7 +24,8 @@ struct WavefrontState {
     float4 *hit = nullptr;      // t, u, v, inst bits
     uint32_t *hit_face = nullptr;
     uint32_t *queue[2] = {nullptr, nullptr};  // path indices
-    uint32_t *sort_keys = nullptr;            // material-sort scratch
+    uint32_t *sort_keys = nullptr;            // material sort: the shade queue grouped by material class
+    uint32_t *sort_hist = nullptr;            // material sort: 2 x kSortBuckets counters (histogram, cursors)
     float *prev_pdf = nullptr;                // NEE: cosine pdf of the continuation after a light-sampling vertex
     uint32_t *slot_state = nullptr;           // multi-frame mode: bounce of the slot's path
     uint32_t *slot_item = nullptr;            // multi-frame mode: sample item (frame * pixels + pixel) of the slot
@@ -35,11 +38,34 @@ struct WavefrontState {
     unsigned long long *host_len = nullptr;  // pinned: queue length read back between iteration chunks
 };
 
+// Material-sort classes: material ids 0..kSortBuckets-3 each, larger ids share one class, misses the last.
+constexpr uint32_t kSortBuckets = 64;
+
 // Frames per multi-frame pass: bounds the per-sample result buffer to kFramesPerPass * pixels * 16 B.
 constexpr uint32_t kFramesPerPass = 64;
 
 cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity);
 void wavefront_free(WavefrontState &s);
+
+// Launch shapes and schedule options of the wavefront (spk_tuning); none changes a result.
+struct WfTuning {
+    uint32_t extend_blocks_per_sm = 0;  // 0 = occupancy maximum of the traversal kernel
+    uint32_t shade_blocks_per_sm = 8;
+    bool material_sort = false;
+};
+
+// Host-side CUDA graph of one chunk of the multi-frame loop (kChunkIterations extend + shade iterations
+// with their counter resets), captured once and replayed while the kernel parameters stay the same.
+constexpr uint32_t kChunkIterations = 8;
+struct ChunkGraph {
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t events[2 * kChunkIterations] = {};  // start/stop of each extend launch inside the graph
+    std::vector<unsigned char> key;                 // kernel parameters the graph was captured with
+    bool enabled = true;
+    bool timed = false;  // captured with the timing events
+    uint32_t replays = 0, captures = 0;
+};
+void chunk_graph_free(ChunkGraph &g);
 
 // All `num_frames` frames of a call in one wavefront with path regeneration (valid when the spatial
 // DenoisePass is off, so pixels do not interact within a frame). Slots pull (frame, pixel) sample items
@@ -52,10 +78,15 @@ void wavefront_free(WavefrontState &s);
 cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
                                      const RenderParams &p, uint32_t num_frames, const float *weights,
                                      const uint32_t *seeds, bool count, Counters *counters, WavefrontState &s,
-                                     int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev);
+                                     int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev,
+                                     const WfTuning &tuning, ChunkGraph *graph);
+
+// Step of the last launch_render_multiframe call on this thread that returned an error (for messages).
+const char *wavefront_error_site();
 
 cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
                                     const RenderParams &p, bool count, Counters *counters, WavefrontState &s,
-                                    int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev);
+                                    int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev,
+                                    const WfTuning &tuning);
 
 }  // namespace spk

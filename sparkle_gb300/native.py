@@ -10,7 +10,7 @@ import os
 import numpy as np
 
 from . import build as _build
-from .abi import (HIT_DTYPE, MarshalledScene, Scene, spk_camera, spk_config, spk_stats)
+from .abi import (HIT_DTYPE, MarshalledScene, Scene, spk_camera, spk_config, spk_stats, spk_tuning)
 
 _lib = None
 
@@ -21,7 +21,8 @@ SPK_ERRORS = {0: "ok", 1: "invalid argument", 2: "cuda error", 3: "out of memory
 EXPORTED = ["spk_abi_version", "spk_create", "spk_destroy", "spk_last_error", "spk_set_scene", "spk_set_camera",
             "spk_camera_from_look", "spk_set_config", "spk_render", "spk_read_framebuffer",
             "spk_framebuffer_device", "spk_sample_counts", "spk_is_converged", "spk_trace", "spk_trace_device",
-            "spk_synchronize", "spk_get_stats", "spk_set_instrumentation", "spk_render_noalloc"]
+            "spk_synchronize", "spk_get_stats", "spk_set_instrumentation", "spk_render_noalloc",
+            "spk_tuning_defaults", "spk_set_tuning", "spk_get_tuning"]
 
 
 class SpkError(RuntimeError):
@@ -66,6 +67,10 @@ def lib(build: bool = True):
         L.spk_get_stats.argtypes = [vp, vp]
         L.spk_set_instrumentation.argtypes = [vp, u32]
         L.spk_render_noalloc.argtypes = [vp, u32, vp, vp]
+        L.spk_tuning_defaults.argtypes = [vp]
+        L.spk_tuning_defaults.restype = None
+        L.spk_set_tuning.argtypes = [vp, vp]
+        L.spk_get_tuning.argtypes = [vp, vp]
         for name in EXPORTED:
             if name != "spk_last_error" and getattr(L, name).restype is C.c_int:
                 getattr(L, name).restype = i32
@@ -163,6 +168,21 @@ class Context:
 
     def set_instrumentation(self, count_traffic: bool):
         self._check(self.L.spk_set_instrumentation(self.h, 1 if count_traffic else 0))
+
+    def tuning(self) -> dict:
+        t = spk_tuning()
+        self._check(self.L.spk_get_tuning(self.h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in spk_tuning._fields_ if k != "reserved"}
+
+    def set_tuning(self, **knobs):
+        """Updates the named knobs of spk_tuning (the others keep their current value)."""
+        t = spk_tuning()
+        self._check(self.L.spk_get_tuning(self.h, C.byref(t)))
+        for k, v in knobs.items():
+            if k not in dict(spk_tuning._fields_) or k == "reserved":
+                raise KeyError(f"unknown tuning knob {k!r}")
+            setattr(t, k, int(v))
+        self._check(self.L.spk_set_tuning(self.h, C.byref(t)))
 
     def stats(self) -> dict:
         s = spk_stats()

@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 HEADER = os.path.join(ROOT, "include", "spk.h")
 
 STRUCTS = ["spk_mesh", "spk_instance", "spk_material", "spk_sky", "spk_camera", "spk_config", "spk_ray", "spk_hit",
-           "spk_stats"]
+           "spk_stats", "spk_tuning"]
 
 
 def header_functions():
@@ -77,3 +77,11 @@ def test_camera_from_look_matches_python_copy():
             assert va == pytest.approx(vb, rel=1e-6, abs=1e-7), name
         else:
             assert list(va) == pytest.approx(list(vb), rel=1e-6, abs=1e-6), name
+
+
+def test_tuning_defaults():
+    t = abi.spk_tuning()
+    native.lib().spk_tuning_defaults(C.byref(t))
+    assert (t.cuda_graph, t.material_sort, t.bvh_width, t.bvh_leaf_size, t.extend_blocks_per_sm,
+            t.shade_blocks_per_sm, list(t.reserved)) == (1, 0, 8, 3, 0, 8, [0, 0])
+    assert native.lib().spk_set_tuning(None, C.byref(t)) == 1

@@ -1,0 +1,113 @@
+"""Performance knobs (spk_set_tuning) never change a result: every setting renders the same bits as the
+defaults, on both schedules, and closest-hit queries return the same hits for every BVH shape.
+
+The tie-break between equal hit distances is (instance, face), independent of the tree, and every sample
+draws its random numbers from its own (pixel, sample) seed, independent of which slot or launch runs it.
+"""
+import numpy as np
+import pytest
+
+from sparkle_gb300 import abi, native, scenes
+
+pytestmark = pytest.mark.gpu
+
+DEFAULTS = dict(cuda_graph=1, material_sort=0, bvh_width=8, bvh_leaf_size=3, extend_blocks_per_sm=0,
+                shade_blocks_per_sm=8)
+
+VARIANTS = [
+    dict(cuda_graph=0),
+    dict(material_sort=1),
+    dict(bvh_width=2),
+    dict(bvh_width=4, bvh_leaf_size=1),
+    dict(bvh_leaf_size=2, extend_blocks_per_sm=2),
+    dict(shade_blocks_per_sm=3, material_sort=1, cuda_graph=0),
+]
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = native.Context(0)
+    yield c
+    c.close()
+
+
+def render(ctx, scene, camera, cfg, frames, knobs):
+    ctx.set_tuning(**{**DEFAULTS, **knobs})
+    ctx.set_scene(scene)  # BVH shape knobs apply at scene upload
+    ctx.set_config(cfg)
+    ctx.set_camera(camera)
+    ctx.render(frames)
+    hdr, out = ctx.framebuffer()
+    st = ctx.stats()
+    assert st["error_flags"] == 0, st
+    return hdr, out, st
+
+
+def test_tuning_defaults_and_validation(ctx):
+    ctx.set_tuning(**DEFAULTS)
+    assert ctx.tuning() == DEFAULTS
+    for bad in [dict(bvh_width=1), dict(bvh_width=9), dict(bvh_leaf_size=0), dict(bvh_leaf_size=4),
+                dict(cuda_graph=2), dict(shade_blocks_per_sm=0), dict(extend_blocks_per_sm=33)]:
+        with pytest.raises(native.SpkError):
+            ctx.set_tuning(**bad)
+        assert ctx.tuning() == DEFAULTS  # a rejected setting leaves the previous one
+
+
+@pytest.mark.parametrize("kernel", [abi.SPK_KERNEL_WAVEFRONT, abi.SPK_KERNEL_MEGAKERNEL])
+@pytest.mark.parametrize("nee", [False, True])
+def test_knobs_render_identical_bits(ctx, small_terrain, kernel, nee):
+    scene, cam_args = small_terrain
+    W, H = 96, 64
+    camera = scenes.make_camera(cam_args, W, H)
+    cfg = abi.make_config(W, H, spp=4, bounce=6, enable_nee=nee, seed=5, kernel=kernel)
+    # 70 frames: the multi-frame wavefront splits them into two passes (64 + 6), two chunk-graph keys
+    base_hdr, base_out, _ = render(ctx, scene, camera, cfg, 70, {})
+    for knobs in VARIANTS:
+        hdr, out, _ = render(ctx, scene, camera, cfg, 70, knobs)
+        assert np.array_equal(hdr.view(np.uint32), base_hdr.view(np.uint32)), knobs
+        assert np.array_equal(out, base_out), knobs
+    ctx.set_tuning(**DEFAULTS)
+
+
+def test_graph_replays_keep_accumulating(ctx, cornell):
+    """Split calls through the replayed chunk graph equal one call without graphs (bit-identical)."""
+    scene, cam_args = cornell
+    W, H = 64, 48
+    camera = scenes.make_camera(cam_args, W, H)
+    cfg = abi.make_config(W, H, spp=1, bounce=5, seed=11, kernel=abi.SPK_KERNEL_WAVEFRONT)
+    ref, _, _ = render(ctx, scene, camera, cfg, 24, dict(cuda_graph=0))
+    ctx.set_tuning(**DEFAULTS)
+    ctx.set_scene(scene)
+    ctx.set_config(cfg)
+    ctx.set_camera(camera)
+    for n in (5, 3, 8, 8):
+        ctx.render(n)
+    hdr, _ = ctx.framebuffer()
+    st = ctx.stats()
+    assert st["error_flags"] == 0 and st["trace_launches"] > 0 and st["trace_kernel_ms"] > 0, st
+    assert st["graph_replays"] > 0, st
+    assert np.array_equal(hdr.view(np.uint32), ref.view(np.uint32))
+    ctx.set_tuning(**{**DEFAULTS, "cuda_graph": 0})
+    ctx.render(2)
+    assert ctx.stats()["graph_replays"] == 0
+    ctx.set_tuning(**DEFAULTS)
+
+
+@pytest.mark.parametrize("width,leaf", [(2, 1), (4, 3), (8, 2)])
+def test_trace_hits_independent_of_bvh_shape(ctx, small_terrain, width, leaf):
+    scene, _ = small_terrain
+    ctx.set_tuning(**DEFAULTS)
+    ctx.set_scene(scene)
+    rays = scenes.random_rays(*scene.world_bounds(), 50_000, seed=9)
+    ref = ctx.trace(rays)
+    nodes_default = ctx.stats()["bvh_nodes"]
+    ctx.set_tuning(**{**DEFAULTS, "bvh_width": width, "bvh_leaf_size": leaf})
+    ctx.set_scene(scene)
+    got = ctx.trace(rays)
+    st = ctx.stats()
+    assert st["error_flags"] == 0
+    if width < 8:
+        assert st["bvh_nodes"] > nodes_default
+    for f in ("t", "u", "v", "prim", "face"):
+        assert np.array_equal(got[f].view(np.uint32), ref[f].view(np.uint32)), f
+    ctx.set_tuning(**DEFAULTS)
