@@ -255,7 +255,8 @@ spk_status spk_render(spk_ctx *ctx, uint32_t num_frames);
 
 /* Copies the accumulated HDR frame buffer (`frame_buffer_`, H rows of W float4, row j = image row j from
  * the bottom as the reference indexes it) and/or the tonemapped RGBA16F output image (`output_image_`,
- * already flipped: row 0 is the top row, CPURenderer.cpp:573) to host memory. Either pointer may be NULL. */
+ * already flipped: row 0 is the top row, CPURenderer.cpp:573). Either pointer may be NULL; each may be host
+ * memory or device memory of the context's GPU (the copy direction follows from the pointer). */
 spk_status spk_read_framebuffer(spk_ctx *ctx, float *hdr_rgba, uint16_t *rgba16f);
 
 /* Device pointers of the context's frame buffer (float4 x W*H) and output image (half4 x W*H), valid
@@ -295,6 +296,16 @@ void spk_tuning_defaults(spk_tuning *out);
  * SPK_ERR_INVALID_ARGUMENT and leaves the previous setting in place. */
 spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *tuning);
 spk_status spk_get_tuning(const spk_ctx *ctx, spk_tuning *out);
+
+/* Primary-hit guides for the learned denoiser (spk_denoise.h), the G-buffer the reference's GPU pipeline
+ * writes for its denoiser (WritePrimaryHitGBuffer, ray_trace.cs.slang:282-351): one pixel-centre ray per
+ * pixel from the camera position (no jitter, no lens); on a hit (t <= 1000) the unit world normal and
+ * the linear depth along normalize(cross(max_v, max_u)) (`normal_depth`, float4) and the base colour with
+ * 2 for an emissive surface else 1 (`albedo`, float4); zeros on a miss. Rows are ordered like the frame
+ * buffer. spk_render_guides is asynchronous; the buffers live until the next spk_set_config. */
+spk_status spk_render_guides(spk_ctx *ctx);
+spk_status spk_guides_device(spk_ctx *ctx, void **normal_depth, void **albedo);
+spk_status spk_read_guides(spk_ctx *ctx, float *normal_depth, float *albedo); /* host or device pointers */
 
 /* Largest width * height spk_render_noalloc accepts (512 x 512). */
 #define SPK_NOALLOC_MAX_PIXELS (512u * 512u)

@@ -36,6 +36,7 @@ def lib():
         L.or_render.argtypes = [vp, C.c_uint32, C.c_int32, C.c_int32, C.c_uint32, C.c_uint32]
         L.or_read_framebuffer.argtypes = [vp, vp, vp]
         L.or_read_gbuffer.argtypes = [vp, vp, vp]
+        L.or_guides.argtypes = [vp, vp, vp]
         L.or_counts.argtypes = [vp, vp, vp, vp]
         L.or_sample_counts.argtypes = [vp, vp, vp]
         L.or_rng_fill.argtypes = [C.c_int32, C.c_uint64, C.c_uint32, vp, vp]
@@ -108,6 +109,14 @@ class OracleRenderer:
         nrm = np.zeros((h, w, 3), np.float32)
         lib().or_read_gbuffer(self.h, _p(col), _p(nrm))
         return col, nrm
+
+    def guides(self):
+        """Primary-hit guides: (normal xyz + linear depth, albedo rgb + hit flag), rows bottom-up."""
+        w, h = self.config.width, self.config.height
+        nd = np.zeros((h, w, 4), np.float32)
+        al = np.zeros((h, w, 4), np.float32)
+        lib().or_guides(self.h, _p(nd), _p(al))
+        return nd, al
 
     def counts(self):
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()

@@ -1464,6 +1464,48 @@ void or_read_gbuffer(const or_renderer *r, float *color_rgba, float *world_norma
     if (world_normal) std::memcpy(world_normal, r->gnormal.data(), r->gnormal.size() * sizeof(V3));
 }
 
+// Primary-hit guides (WritePrimaryHitGBuffer, ray_trace.cs.slang:282-351): one pixel-centre ray from the
+// camera position (no jitter, no lens), uv = (pixel + 0.5) / (resolution - 1) with v flipped for the
+// top-down pixel row; on a hit within TMax = 1000: normalize(normal), linear depth along
+// normalize(cross(max_v, max_u)), base colour, and 2 for an emissive surface else 1. Misses are zero.
+// Rows are written bottom-up like the frame buffer (row j is top-down pixel row h - 1 - j).
+void or_guides(const or_renderer *r, float *normal_depth, float *albedo_hit) {
+    const or_scene &sc = *r->scene;
+    const spk_camera &cam = r->cam;
+    const uint32_t w = r->w, h = r->h;
+    const float pw = 1.f / static_cast<float>(w - 1), ph = 1.f / static_cast<float>(h - 1);
+    const V3 front = normalized(cross(load3(cam.max_v), load3(cam.max_u)));
+    for (uint32_t j = 0; j < h; ++j) {
+        for (uint32_t i = 0; i < w; ++i) {
+            const uint32_t py = h - 1 - j;
+            const float u = (static_cast<float>(i) + 0.5f) * pw;
+            const float v = 1.f - (static_cast<float>(py) + 0.5f) * ph;
+            const V3 o = load3(cam.position);
+            const V3 d = normalized(load3(cam.lower_left) + u * load3(cam.max_u) + v * load3(cam.max_v) - o);
+            Candidate cand;
+            uint64_t overflows = 0;
+            intersect_scene<false>(sc, o, d, cand, true, overflows);
+            const Hit hit = make_hit(sc, cand, o, d);
+            float *nd = normal_depth + 4 * (static_cast<size_t>(j) * w + i);
+            float *al = albedo_hit + 4 * (static_cast<size_t>(j) * w + i);
+            if (!hit.hit || !(hit.t <= 1000.f)) {
+                for (int c = 0; c < 4; ++c) nd[c] = al[c] = 0.f;
+                continue;
+            }
+            const spk_material &mat = sc.materials[sc.insts[hit.prim].desc.material_id];
+            const V3 n = normalized(hit.normal);
+            nd[0] = n.x;
+            nd[1] = n.y;
+            nd[2] = n.z;
+            nd[3] = dot3(hit.location - o, front);
+            al[0] = mat.base_color[0];
+            al[1] = mat.base_color[1];
+            al[2] = mat.base_color[2];
+            al[3] = std::sqrt(sqnorm(load3(mat.emissive))) > kEps ? 2.f : 1.f;
+        }
+    }
+}
+
 void or_counts(const or_renderer *r, uint64_t *extension_rays, uint64_t *shadow_rays, uint64_t *paths) {
     if (extension_rays) *extension_rays = r->ext_rays.load();
     if (shadow_rays) *shadow_rays = r->shadow_rays.load();

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libspk.so")
 
-CUDA_SOURCES = ["kernels.cu", "wavefront.cu", "spk_api.cu"]
+CUDA_SOURCES = ["kernels.cu", "wavefront.cu", "spk_api.cu", "conv_tc.cu", "unet.cu"]
 CXX_SOURCES = ["bvh_builder.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -32,7 +32,7 @@ def nvcc() -> str:
 
 def _inputs():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    files.append(os.path.join(ROOT, "include", "spk.h"))
+    files += [os.path.join(ROOT, "include", f) for f in os.listdir(os.path.join(ROOT, "include"))]
     files.append(os.path.abspath(__file__))
     return files
 

@@ -1,0 +1,472 @@
+// conv_tc.cu -- tcgen05 implicit-GEMM 3x3 convolutions (see conv_tc.cuh).
+//
+// Forward / dgrad (one CTA per 128-pixel output tile, 4 warps):
+//   warp 0 lane 0  TMA producer: per K block (tap, 32-channel chunk) one 4-D tiled load of the shifted
+//                  input box {32 ch, tw px, th rows, 1 image} (zero fill outside the image = the conv's
+//                  padding) and one 2-D load of the weight slice {32, cout}, into a 4-stage ring;
+//   warp 1 lane 0  MMA issuer: two kind::f16 MMAs (K = 16 each) per stage into a 128 x cout FP32
+//                  accumulator in TMEM, committing each stage back to the producer;
+//   all 4 warps    epilogue: tcgen05.ld of the pixel rows (warp w owns TMEM lanes 32w..32w+31), bias,
+//                  ReLU or ReLU-backward mask, BF16 pack, 16-byte stores.
+// Wgrad (one CTA per (128 rows of (tap, ci), pixel range)): all threads gather and transpose the shifted
+// input and the output gradient into K-major (pixel-contiguous) swizzled tiles, thread 0 issues the MMAs,
+// and the FP32 partial sums are added to dw with atomics.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "conv_tc.cuh"
+#include "tc_common.cuh"
+
+namespace spk {
+namespace {
+
+using namespace tc;
+
+constexpr uint32_t kTileM = 128;
+constexpr uint32_t kStages = 4;
+constexpr uint32_t kATileBytes = kTileM * 64;  // 128 rows x 32 bf16
+constexpr uint32_t kMaxCout = 256;
+
+struct FwdParams {
+    uint32_t n, h, w;
+    uint32_t cin, cout;
+    uint32_t tw, th, tiles_x, tiles_y;
+    __nv_bfloat16 *out;
+    uint32_t out_ld;
+    const float *bias;
+    uint32_t relu;
+    const __nv_bfloat16 *mask;
+    uint32_t mask_ld;
+    uint32_t *err;
+};
+
+__host__ __device__ constexpr uint32_t fwd_stage_bytes(uint32_t cout) {
+    return (kATileBytes + cout * 64u + 1023u) & ~1023u;
+}
+
+__host__ __device__ constexpr uint32_t tmem_columns(uint32_t n) {
+    return n <= 32 ? 32 : n <= 64 ? 64 : n <= 128 ? 128 : 256;
+}
+
+__device__ __forceinline__ uint8_t *align1024(uint8_t *raw) {
+    const uint32_t a = smem_u32(raw);
+    return raw + (((a + 1023u) & ~1023u) - a);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__global__ void __launch_bounds__(128, 1)
+    k_conv_fwd(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, FwdParams P) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = align1024(smem_raw);
+    const uint32_t b_bytes = P.cout * 64u;
+    const uint32_t stage_bytes = fwd_stage_bytes(P.cout);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * stage_bytes);
+    uint64_t *full = bars, *empty = bars + kStages, *accum = bars + 2 * kStages;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 1);
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t ncols = tmem_columns(P.cout);
+
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accum, 1);
+        fence_mbar_init();
+        tma_prefetch_desc(&tmx);
+        tma_prefetch_desc(&tmw);
+    }
+    if (warp == 0) tmem_alloc(tmem_slot, ncols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    uint32_t t = blockIdx.x;
+    const uint32_t tx = t % P.tiles_x;
+    t /= P.tiles_x;
+    const uint32_t ty = t % P.tiles_y;
+    const uint32_t img = t / P.tiles_y;
+    const int x0 = static_cast<int>(tx * P.tw), y0 = static_cast<int>(ty * P.th);
+    const uint32_t nch = P.cin / 32u, nk = 9u * nch;
+
+    if (warp == 0 && lane == 0) {
+        for (uint32_t kb = 0; kb < nk; ++kb) {
+            const uint32_t s = kb % kStages, u = kb / kStages;
+            if (u > 0 && !mbar_wait(&empty[s], (u - 1) & 1u, P.err)) break;
+            uint8_t *a = smem + s * stage_bytes;
+            mbar_arrive_expect_tx(&full[s], kATileBytes + b_bytes);
+            const uint32_t tap = kb / nch, c = kb - tap * nch;
+            const int dy = static_cast<int>(tap / 3u) - 1, dx = static_cast<int>(tap % 3u) - 1;
+            tma_load_4d(a, &tmx, &full[s], static_cast<int>(c * 32u), x0 + dx, y0 + dy, static_cast<int>(img));
+            tma_load_2d(a + kATileBytes, &tmw, &full[s], static_cast<int>(tap * P.cin + c * 32u), 0);
+        }
+    } else if (warp == 1 && lane == 0) {
+        const uint32_t idesc = idesc_bf16(kTileM, P.cout);
+        bool ok = true;
+        for (uint32_t kb = 0; kb < nk; ++kb) {
+            const uint32_t s = kb % kStages, u = kb / kStages;
+            if (!mbar_wait(&full[s], u & 1u, P.err)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t a = smem_u32(smem + s * stage_bytes), b = a + kATileBytes;
+#pragma unroll
+            for (uint32_t k2 = 0; k2 < 2; ++k2)
+                mma_bf16(tmem, smem_desc_sw64(a + 32u * k2), smem_desc_sw64(b + 32u * k2), idesc, (kb | k2) != 0u);
+            mma_commit(&empty[s]);
+        }
+        if (ok) mma_commit(accum);
+    }
+    __syncwarp();
+
+    // Epilogue.
+    bool ready = mbar_wait(accum, 0, P.err);
+    ready = __all_sync(0xFFFFFFFFu, ready);
+    tc_fence_after();
+    if (ready) {
+        const uint32_t r = warp * 32u + lane;
+        const uint32_t px = static_cast<uint32_t>(x0) + (r % P.tw), py = static_cast<uint32_t>(y0) + (r / P.tw);
+        const bool inb = px < P.w && py < P.h;
+        const size_t pix = (static_cast<size_t>(img) * P.h + py) * P.w + px;
+        for (uint32_t j = 0; j < P.cout / 16u; ++j) {
+            uint32_t v[16];
+            tmem_ld16(tmem + ((warp * 32u) << 16) + j * 16u, v);
+            if (!inb) continue;
+            float f[16];
+#pragma unroll
+            for (int e = 0; e < 16; ++e) f[e] = __uint_as_float(v[e]) + (P.bias ? P.bias[j * 16u + e] : 0.f);
+            if (P.mask) {
+                const uint4 *mp = reinterpret_cast<const uint4 *>(P.mask + pix * P.mask_ld + j * 16u);
+                const uint4 m0 = mp[0], m1 = mp[1];
+                const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const uint32_t bits = (mw[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
+                    // bf16 > 0: sign bit clear and not +0
+                    if ((bits & 0x8000u) || bits == 0u) f[e] = 0.f;
+                }
+            } else if (P.relu) {
+#pragma unroll
+                for (int e = 0; e < 16; ++e) f[e] = fmaxf(f[e], 0.f);
+            }
+            uint4 *op = reinterpret_cast<uint4 *>(P.out + pix * P.out_ld + j * 16u);
+            op[0] = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]),
+                               pack_bf16(f[6], f[7]));
+            op[1] = make_uint4(pack_bf16(f[8], f[9]), pack_bf16(f[10], f[11]), pack_bf16(f[12], f[13]),
+                               pack_bf16(f[14], f[15]));
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, ncols);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// wgrad
+// ------------------------------------------------------------------------------------------------
+constexpr uint32_t kWgStages = 2;
+constexpr uint32_t kWgKPix = 32;  // pixels per K block
+
+struct WgradParams {
+    uint32_t n, h, w, cin, cout;
+    const __nv_bfloat16 *x;
+    uint32_t x_ld;
+    const __nv_bfloat16 *dy;
+    uint32_t dy_ld;
+    float *dw;
+    uint32_t kblocks;    // K blocks per CTA
+    uint32_t row_tiles;  // ceil(9 * cin / 128)
+    unsigned long long npix;
+    uint32_t *err;
+};
+
+__host__ __device__ constexpr uint32_t wg_stage_bytes(uint32_t cout) {
+    return (kATileBytes + cout * 64u + 1023u) & ~1023u;
+}
+
+// Writes 8 bf16 (one 16-byte vector: channels c..c+7 of one pixel) as column `k` of rows row0..row0+7.
+__device__ __forceinline__ void scatter_column(uint8_t *tile, uint32_t row0, uint32_t k, uint4 v) {
+    const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (uint32_t e = 0; e < 8; ++e) {
+        const uint16_t h = static_cast<uint16_t>((w[e >> 1] >> (16u * (e & 1u))) & 0xFFFFu);
+        *reinterpret_cast<uint16_t *>(tile + sw64_offset(row0 + e, k >> 3) + (k & 7u) * 2u) = h;
+    }
+}
+
+__global__ void __launch_bounds__(128, 1) k_conv_wgrad(WgradParams P) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = align1024(smem_raw);
+    const uint32_t stage_bytes = wg_stage_bytes(P.cout);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kWgStages * stage_bytes);
+    uint64_t *full = bars, *empty = bars + kWgStages, *accum = bars + 2 * kWgStages;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kWgStages + 1);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31u;
+    const uint32_t ncols = tmem_columns(P.cout);
+
+    if (tid == 0) {
+        for (uint32_t s = 0; s < kWgStages; ++s) {
+            mbar_init(&full[s], 128);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accum, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) tmem_alloc(tmem_slot, ncols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const uint32_t rt = blockIdx.x % P.row_tiles, split = blockIdx.x / P.row_tiles;
+    const uint32_t krows = 9u * P.cin;
+    const unsigned long long pbase = static_cast<unsigned long long>(split) * P.kblocks * kWgKPix;
+    const uint32_t hw = P.h * P.w;
+    const uint32_t idesc = idesc_bf16(kTileM, P.cout);
+    // Lane layout of the gathers: 4 channel groups of 8 x 8 pixels per warp pass (64 contiguous bytes
+    // of each pixel's channels).
+    const uint32_t cg = lane & 3u, kk = lane >> 2;
+    // `ok` turns false on a wait timeout; the loop leaves only at a barrier, where every thread agrees.
+    bool ok = true;
+    for (uint32_t kb = 0; kb < P.kblocks; ++kb) {
+        const uint32_t s = kb % kWgStages, u = kb / kWgStages;
+        if (u > 0 && ok) ok = mbar_wait(&empty[s], (u - 1) & 1u, P.err);
+        ok = __syncthreads_and(ok);
+        if (!ok) break;
+        uint8_t *a = smem + s * stage_bytes, *b = a + kATileBytes;
+        // A: rows g = (tap, ci) of this row tile, column k = pixel pbase + kb*32 + k, value x[p + tap][ci].
+        for (uint32_t it = warp; it < 16u; it += 4u) {  // 16 passes: 4 channel-group quads x 4 pixel octets
+            const uint32_t group = (it >> 2) * 4u + cg;  // 8-row group 0..15
+            const uint32_t k = (it & 3u) * 8u + kk;
+            const uint32_t g0 = rt * kTileM + group * 8u;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            const unsigned long long p = pbase + static_cast<unsigned long long>(kb) * kWgKPix + k;
+            if (g0 < krows && p < P.npix) {
+                const uint32_t tap = g0 / P.cin, ci0 = g0 - tap * P.cin;
+                const uint32_t img = static_cast<uint32_t>(p / hw), rem = static_cast<uint32_t>(p - static_cast<unsigned long long>(img) * hw);
+                const int y = static_cast<int>(rem / P.w) + static_cast<int>(tap / 3u) - 1;
+                const int xx = static_cast<int>(rem % P.w) + static_cast<int>(tap % 3u) - 1;
+                if (y >= 0 && y < static_cast<int>(P.h) && xx >= 0 && xx < static_cast<int>(P.w)) {
+                    const size_t q = (static_cast<size_t>(img) * P.h + static_cast<uint32_t>(y)) * P.w + static_cast<uint32_t>(xx);
+                    v = *reinterpret_cast<const uint4 *>(P.x + q * P.x_ld + ci0);
+                }
+            }
+            scatter_column(a, group * 8u, k, v);
+        }
+        // B: rows co, column k, value dy[p][co].
+        const uint32_t bgroups = P.cout / 8u;  // 8-row groups; cout % 32 == 0, so bgroups passes
+        for (uint32_t it = warp; it < bgroups; it += 4u) {
+            const uint32_t group = (it >> 2) * 4u + cg;
+            const uint32_t k = (it & 3u) * 8u + kk;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            const unsigned long long p = pbase + static_cast<unsigned long long>(kb) * kWgKPix + k;
+            if (p < P.npix) v = *reinterpret_cast<const uint4 *>(P.dy + static_cast<size_t>(p) * P.dy_ld + group * 8u);
+            scatter_column(b, group * 8u, k, v);
+        }
+        fence_proxy_async_smem();
+        mbar_arrive(&full[s]);
+        if (tid == 0) {
+            if (!mbar_wait(&full[s], u & 1u, P.err)) {
+                ok = false;
+            } else {
+                tc_fence_after();
+                const uint32_t sa = smem_u32(a), sb = smem_u32(b);
+#pragma unroll
+                for (uint32_t k2 = 0; k2 < 2; ++k2)
+                    mma_bf16(tmem, smem_desc_sw64(sa + 32u * k2), smem_desc_sw64(sb + 32u * k2), idesc,
+                             (kb | k2) != 0u);
+                mma_commit(&empty[s]);
+            }
+        }
+    }
+    ok = __syncthreads_and(ok);
+    if (tid == 0 && ok) mma_commit(accum);
+    bool ready = ok && mbar_wait(accum, 0, P.err);
+    ready = __all_sync(0xFFFFFFFFu, ready);
+    tc_fence_after();
+    if (ready) {
+        const uint32_t g = rt * kTileM + warp * 32u + lane;
+        for (uint32_t j = 0; j < P.cout / 16u; ++j) {
+            uint32_t v[16];
+            tmem_ld16(tmem + ((warp * 32u) << 16) + j * 16u, v);
+            if (g >= krows) continue;
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const float f = __uint_as_float(v[e]);
+                if (f != 0.f) atomicAdd(P.dw + static_cast<size_t>(j * 16u + e) * krows + g, f);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, ncols);
+    }
+}
+
+__global__ void k_transpose_weights(const __nv_bfloat16 *w, __nv_bfloat16 *wt, uint32_t cout, uint32_t cin) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;  // index into wt [cin][9][cout]
+    if (i >= cout * cin * 9u) return;
+    const uint32_t co = i % cout, tap = (i / cout) % 9u, ci = i / (9u * cout);
+    wt[i] = w[(static_cast<size_t>(co) * 9u + (8u - tap)) * cin + ci];
+}
+
+// ------------------------------------------------------------------------------------------------
+// Host: tensor maps through the driver entry point (no libcuda link dependency).
+// ------------------------------------------------------------------------------------------------
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+constexpr int kMaxDynSmem = 227 * 1024;
+
+// Dynamic shared memory of a launch: what the kernel uses, raised so that the CTAs resident on one SM
+// never ask for more than the SM's 512 TMEM columns (an allocation beyond that would wait for another
+// CTA to finish).
+size_t launch_smem(size_t used, uint32_t tmem_cols) {
+    const size_t per_sm = 228u * 1024u;
+    const size_t ctas = 512u / tmem_cols;
+    const size_t floor_bytes = per_sm / ctas - 1024u + 1u;  // the SM reserves 1 KB per CTA
+    return std::min<size_t>(kMaxDynSmem, std::max(used, floor_bytes));
+}
+
+}  // namespace
+
+cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, const NhwcView &y, const ConvGeom &g,
+                            const ConvEpilogue &epi, uint32_t *err, cudaStream_t stream) {
+    if (x.channels == 0 || x.channels % 32u || cout == 0 || cout % 32u || cout > kMaxCout || y.channels != cout ||
+        x.ld % 8u || y.ld % 8u || x.ld < x.channels || y.ld < y.channels || !aligned16(x.ptr) || !aligned16(y.ptr) ||
+        !aligned16(w) || g.n == 0 || g.h == 0 || g.w == 0)
+        return cudaErrorInvalidValue;
+    if (epi.mask.ptr && (epi.mask.channels != cout || epi.mask.ld % 8u || !aligned16(epi.mask.ptr)))
+        return cudaErrorInvalidValue;
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return cudaErrorNotSupported;
+    uint32_t tw = 1;
+    while (tw < g.w && tw < kTileM) tw <<= 1;
+    const uint32_t th = kTileM / tw;
+    CUtensorMap tmx, tmw;
+    {
+        const cuuint64_t dims[4] = {x.channels, g.w, g.h, g.n};
+        const cuuint64_t strides[3] = {static_cast<cuuint64_t>(x.ld) * 2u, static_cast<cuuint64_t>(x.ld) * 2u * g.w,
+                                       static_cast<cuuint64_t>(x.ld) * 2u * g.w * g.h};
+        const cuuint32_t box[4] = {32u, tw, th, 1u};
+        const cuuint32_t es[4] = {1u, 1u, 1u, 1u};
+        if (enc(&tmx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, x.ptr, dims, strides, box, es,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+    }
+    {
+        const cuuint64_t dims[2] = {9u * x.channels, cout};
+        const cuuint64_t strides[1] = {9u * x.channels * 2u};
+        const cuuint32_t box[2] = {32u, cout};
+        const cuuint32_t es[2] = {1u, 1u};
+        if (enc(&tmw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(w), dims, strides, box, es,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+    }
+    FwdParams P{};
+    P.n = g.n;
+    P.h = g.h;
+    P.w = g.w;
+    P.cin = x.channels;
+    P.cout = cout;
+    P.tw = tw;
+    P.th = th;
+    P.tiles_x = (g.w + tw - 1) / tw;
+    P.tiles_y = (g.h + th - 1) / th;
+    P.out = static_cast<__nv_bfloat16 *>(y.ptr);
+    P.out_ld = y.ld;
+    P.bias = epi.bias;
+    P.relu = epi.relu ? 1u : 0u;
+    P.mask = static_cast<const __nv_bfloat16 *>(epi.mask.ptr);
+    P.mask_ld = epi.mask.ld;
+    P.err = err;
+    const size_t smem = launch_smem(kStages * fwd_stage_bytes(cout) + 1024 + 256, tmem_columns(cout));
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(k_conv_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
+    });
+    const unsigned long long tiles = static_cast<unsigned long long>(P.tiles_x) * P.tiles_y * g.n;
+    if (tiles > 0x7FFFFFFFull) return cudaErrorInvalidValue;
+    k_conv_fwd<<<static_cast<unsigned>(tiles), 128, smem, stream>>>(tmx, tmw, P);
+    return cudaGetLastError();
+}
+
+cudaError_t conv3x3_wgrad(const NhwcView &x, const NhwcView &dy, float *dw, const ConvGeom &g, uint32_t *err,
+                          cudaStream_t stream) {
+    if (x.channels == 0 || x.channels % 32u || dy.channels == 0 || dy.channels % 32u || dy.channels > kMaxCout ||
+        x.ld % 8u || dy.ld % 8u || !aligned16(x.ptr) || !aligned16(dy.ptr) || g.n == 0 || g.h == 0 || g.w == 0)
+        return cudaErrorInvalidValue;
+    WgradParams P{};
+    P.n = g.n;
+    P.h = g.h;
+    P.w = g.w;
+    P.cin = x.channels;
+    P.cout = dy.channels;
+    P.x = static_cast<const __nv_bfloat16 *>(x.ptr);
+    P.x_ld = x.ld;
+    P.dy = static_cast<const __nv_bfloat16 *>(dy.ptr);
+    P.dy_ld = dy.ld;
+    P.dw = dw;
+    P.npix = static_cast<unsigned long long>(g.n) * g.h * g.w;
+    P.row_tiles = (9u * P.cin + kTileM - 1) / kTileM;
+    P.err = err;
+    const unsigned long long kblocks_total = (P.npix + kWgKPix - 1) / kWgKPix;
+    // About 4 CTAs per SM in total, at least 8 K blocks each.
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    unsigned long long splits = std::max<unsigned long long>(1ull, (4ull * sms) / P.row_tiles);
+    splits = std::min<unsigned long long>(splits, (kblocks_total + 7) / 8);
+    splits = std::max<unsigned long long>(splits, 1ull);
+    P.kblocks = static_cast<uint32_t>((kblocks_total + splits - 1) / splits);
+    splits = (kblocks_total + P.kblocks - 1) / P.kblocks;
+    const size_t smem = launch_smem(kWgStages * wg_stage_bytes(P.cout) + 1024 + 256, tmem_columns(P.cout));
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
+    });
+    k_conv_wgrad<<<static_cast<unsigned>(splits * P.row_tiles), 128, smem, stream>>>(P);
+    return cudaGetLastError();
+}
+
+cudaError_t conv3x3_transpose_weights(const void *w, void *wt, uint32_t cout, uint32_t cin, cudaStream_t stream) {
+    const uint32_t n = cout * cin * 9u;
+    k_transpose_weights<<<(n + 255) / 256, 256, 0, stream>>>(static_cast<const __nv_bfloat16 *>(w),
+                                                            static_cast<__nv_bfloat16 *>(wt), cout, cin);
+    return cudaGetLastError();
+}
+
+}  // namespace spk

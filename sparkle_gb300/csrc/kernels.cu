@@ -239,6 +239,48 @@ cudaError_t launch_render_mega(const DevScene &scene, const DevCamera &cam, cons
     return cudaGetLastError();
 }
 
+// Primary-hit guides, the G-buffer WritePrimaryHitGBuffer writes (ray_trace.cs.slang:282-351): a
+// pixel-centre ray from the camera position (no jitter, no lens), uv = (pixel + 0.5) / (resolution - 1)
+// with v flipped for the top-down pixel row. A hit within TMax = 1000 stores normalize(normal) and the
+// linear depth along normalize(cross(max_v, max_u)), the base colour and 2 (emissive) or 1; a miss stores
+// zeros. Rows are bottom-up like the frame buffer.
+__global__ void __launch_bounds__(128) k_guides(DevScene S, DevCamera cam, uint32_t w, uint32_t h, float4 *nd,
+                                                float4 *alb, Counters *counters) {
+    const uint32_t i = blockIdx.x * 16u + (threadIdx.x & 15u);
+    const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 4);
+    if (i >= w || j >= h) return;
+    const uint32_t py = h - 1 - j;
+    const float pw = 1.f / static_cast<float>(w - 1), ph = 1.f / static_cast<float>(h - 1);
+    const float u = (static_cast<float>(i) + 0.5f) * pw;
+    const float v = 1.f - (static_cast<float>(py) + 0.5f) * ph;
+    const f3 o = mk3(cam.position[0], cam.position[1], cam.position[2]);
+    const f3 focus = mk3(cam.lower_left[0], cam.lower_left[1], cam.lower_left[2]) +
+                     u * mk3(cam.max_u[0], cam.max_u[1], cam.max_u[2]) + v * mk3(cam.max_v[0], cam.max_v[1], cam.max_v[2]);
+    const f3 d = normalized(focus - o);
+    uint32_t err = 0;
+    const TraceResult hit = trace_ray<kTraceClosest>(S, o, d, kFltMax, err);
+    const size_t pix = static_cast<size_t>(j) * w + i;
+    if (err) atomicOr(&counters->error_flags, err);
+    if (hit.inst == kInvalid || !(hit.t <= 1000.f)) {
+        nd[pix] = make_float4(0.f, 0.f, 0.f, 0.f);
+        alb[pix] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const Surface surf = make_surface(S, hit, o, d);
+    const DevMaterial mat = S.materials[surf.material];
+    const f3 n = normalized(surf.normal);
+    const f3 front = normalized(cross(mk3(cam.max_v[0], cam.max_v[1], cam.max_v[2]), mk3(cam.max_u[0], cam.max_u[1], cam.max_u[2])));
+    nd[pix] = make_float4(n.x, n.y, n.z, dot3(surf.location - o, front));
+    alb[pix] = make_float4(mat.base[0], mat.base[1], mat.base[2], mat.is_emissive ? 2.f : 1.f);
+}
+
+cudaError_t launch_guides(const DevScene &scene, const DevCamera &cam, uint32_t w, uint32_t h, float4 *nd, float4 *alb,
+                          Counters *counters, cudaStream_t stream) {
+    const dim3 grid((w + 15) / 16, (h + 7) / 8);
+    k_guides<<<grid, 128, 0, stream>>>(scene, cam, w, h, nd, alb, counters);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_resolve(const FrameBuffers &fbuf, float moving_average, float exposure, uint32_t spatial_denoise,
                            cudaStream_t stream) {
     const dim3 grid((fbuf.width + 31) / 32, (fbuf.height + 7) / 8);

@@ -78,6 +78,10 @@ cudaError_t launch_render_mega(const DevScene &scene, const DevCamera &cam, cons
                                const RenderParams &p, bool count, Counters *counters, cudaStream_t stream,
                                LaunchEvents *ev);
 
+// Primary-hit guides (normal + linear depth, albedo + hit flag) of a w x h image.
+cudaError_t launch_guides(const DevScene &scene, const DevCamera &cam, uint32_t w, uint32_t h, float4 *nd, float4 *alb,
+                          Counters *counters, cudaStream_t stream);
+
 // DenoisePass (spatial fill + temporal lerp with weight `moving_average`) + ToneMappingPass.
 cudaError_t launch_resolve(const FrameBuffers &fbuf, float moving_average, float exposure, uint32_t spatial_denoise,
                            cudaStream_t stream);

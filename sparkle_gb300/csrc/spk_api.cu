@@ -81,6 +81,7 @@ struct spk_ctx {
     bool has_camera = false;
     DevBuf<float4> gcolor, gnormal, fb;
     DevBuf<ushort4> out;
+    DevBuf<float4> guide_nd, guide_albedo;  // primary-hit guides (spk_render_guides)
     WavefrontState wf{};
     ChunkGraph chunk_graph{};
     spk_tuning tuning = default_tuning();
@@ -233,6 +234,8 @@ spk_status spk_destroy(spk_ctx *ctx) {
     ctx->light_cdf.reset();
     ctx->gcolor.reset();
     ctx->gnormal.reset();
+    ctx->guide_nd.reset();
+    ctx->guide_albedo.reset();
     ctx->fb.reset();
     ctx->out.reset();
     wavefront_free(ctx->wf);
@@ -712,11 +715,11 @@ spk_status spk_read_framebuffer(spk_ctx *ctx, float *hdr_rgba, uint16_t *rgba16f
     cudaSetDevice(ctx->device);
     cudaError_t e;
     if (hdr_rgba &&
-        (e = cudaMemcpyAsync(hdr_rgba, ctx->fb.ptr, ctx->fb.count * sizeof(float4), cudaMemcpyDeviceToHost,
+        (e = cudaMemcpyAsync(hdr_rgba, ctx->fb.ptr, ctx->fb.count * sizeof(float4), cudaMemcpyDefault,
                              ctx->stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "frame buffer read");
     if (rgba16f &&
-        (e = cudaMemcpyAsync(rgba16f, ctx->out.ptr, ctx->out.count * sizeof(ushort4), cudaMemcpyDeviceToHost,
+        (e = cudaMemcpyAsync(rgba16f, ctx->out.ptr, ctx->out.count * sizeof(ushort4), cudaMemcpyDefault,
                              ctx->stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "output image read");
     if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
@@ -834,6 +837,50 @@ spk_status spk_get_stats(spk_ctx *ctx, spk_stats *out) {
     ctx->last.bvh_nodes = ctx->bvh_nodes;
     ctx->last.bvh_bytes = ctx->bvh_bytes;
     *out = ctx->last;
+    return SPK_OK;
+}
+
+spk_status spk_render_guides(spk_ctx *ctx) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene || !ctx->has_config || !ctx->has_camera)
+        return fail(ctx, SPK_ERR_NOT_READY, "guides need spk_set_scene, spk_set_config and spk_set_camera first");
+    cudaSetDevice(ctx->device);
+    const size_t n = static_cast<size_t>(ctx->cfg.width) * ctx->cfg.height;
+    cudaError_t e;
+    if (ctx->guide_nd.count != n) {
+        ctx->guide_nd.reset();
+        ctx->guide_albedo.reset();
+        if ((e = cudaMalloc(reinterpret_cast<void **>(&ctx->guide_nd.ptr), n * sizeof(float4))) != cudaSuccess ||
+            (e = cudaMalloc(reinterpret_cast<void **>(&ctx->guide_albedo.ptr), n * sizeof(float4))) != cudaSuccess)
+            return cuda_fail(ctx, e, "guide buffers");
+        ctx->guide_nd.count = ctx->guide_albedo.count = n;
+    }
+    if ((e = launch_guides(ctx->scene, ctx->cam, ctx->cfg.width, ctx->cfg.height, ctx->guide_nd.ptr,
+                           ctx->guide_albedo.ptr, ctx->counters, ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "guides launch");
+    return SPK_OK;
+}
+
+spk_status spk_guides_device(spk_ctx *ctx, void **normal_depth, void **albedo) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->guide_nd.ptr) return fail(ctx, SPK_ERR_NOT_READY, "no guides: call spk_render_guides first");
+    if (normal_depth) *normal_depth = ctx->guide_nd.ptr;
+    if (albedo) *albedo = ctx->guide_albedo.ptr;
+    return SPK_OK;
+}
+
+spk_status spk_read_guides(spk_ctx *ctx, float *normal_depth, float *albedo) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->guide_nd.ptr) return fail(ctx, SPK_ERR_NOT_READY, "no guides: call spk_render_guides first");
+    cudaSetDevice(ctx->device);
+    cudaError_t e;
+    const size_t bytes = ctx->guide_nd.count * sizeof(float4);
+    if ((normal_depth && (e = cudaMemcpyAsync(normal_depth, ctx->guide_nd.ptr, bytes, cudaMemcpyDefault,
+                                              ctx->stream)) != cudaSuccess) ||
+        (albedo && (e = cudaMemcpyAsync(albedo, ctx->guide_albedo.ptr, bytes, cudaMemcpyDefault, ctx->stream)) !=
+                       cudaSuccess))
+        return cuda_fail(ctx, e, "guide read");
+    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
     return SPK_OK;
 }
 

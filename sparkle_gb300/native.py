@@ -22,7 +22,13 @@ EXPORTED = ["spk_abi_version", "spk_create", "spk_destroy", "spk_last_error", "s
             "spk_camera_from_look", "spk_set_config", "spk_render", "spk_read_framebuffer",
             "spk_framebuffer_device", "spk_sample_counts", "spk_is_converged", "spk_trace", "spk_trace_device",
             "spk_synchronize", "spk_get_stats", "spk_set_instrumentation", "spk_render_noalloc",
-            "spk_tuning_defaults", "spk_set_tuning", "spk_get_tuning"]
+            "spk_tuning_defaults", "spk_set_tuning", "spk_get_tuning", "spk_render_guides", "spk_guides_device",
+            "spk_read_guides",
+            # include/spk_denoise.h
+            "spk_dn_create", "spk_dn_destroy", "spk_dn_last_error", "spk_dn_init", "spk_dn_num_params",
+            "spk_dn_get_params", "spk_dn_set_params", "spk_dn_pack_features", "spk_dn_pack_halves", "spk_dn_train_step",
+            "spk_dn_gradients", "spk_dn_infer", "spk_dn_fallback", "spk_dn_synchronize", "spk_dn_last_ms",
+            "spk_dn_conv3x3"]
 
 
 class SpkError(RuntimeError):
@@ -71,8 +77,29 @@ def lib(build: bool = True):
         L.spk_tuning_defaults.restype = None
         L.spk_set_tuning.argtypes = [vp, vp]
         L.spk_get_tuning.argtypes = [vp, vp]
+        L.spk_render_guides.argtypes = [vp]
+        L.spk_guides_device.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
+        L.spk_read_guides.argtypes = [vp, vp, vp]
+        f32, pf = C.c_float, C.POINTER(C.c_float)
+        L.spk_dn_create.argtypes = [i32, u64, C.POINTER(vp)]
+        L.spk_dn_destroy.argtypes = [vp]
+        L.spk_dn_last_error.restype = C.c_char_p
+        L.spk_dn_last_error.argtypes = [vp]
+        L.spk_dn_init.argtypes = [vp, u64]
+        L.spk_dn_num_params.argtypes = [vp, C.POINTER(u64)]
+        L.spk_dn_get_params.argtypes = [vp, vp, u64]
+        L.spk_dn_set_params.argtypes = [vp, vp, u64]
+        L.spk_dn_pack_features.argtypes = [vp, vp, vp, vp, u32, u32, u32, vp]
+        L.spk_dn_pack_halves.argtypes = [vp, vp, vp, vp, vp, u32, u32, u32, vp, vp]
+        L.spk_dn_train_step.argtypes = [vp, vp, vp, u32, u32, u32, f32, pf]
+        L.spk_dn_gradients.argtypes = [vp, vp, vp, u32, u32, u32, pf, vp, u64]
+        L.spk_dn_infer.argtypes = [vp, vp, u32, u32, u32, vp]
+        L.spk_dn_fallback.argtypes = [vp, vp, vp, vp, vp, u32, u32, u32, f32, vp, C.POINTER(u32)]
+        L.spk_dn_synchronize.argtypes = [vp]
+        L.spk_dn_last_ms.argtypes = [vp, pf]
+        L.spk_dn_conv3x3.argtypes = [vp, i32, vp, u32, u32, vp, vp, vp, u32, u32, u32, u32, u32, i32, vp, u32, vp]
         for name in EXPORTED:
-            if name != "spk_last_error" and getattr(L, name).restype is C.c_int:
+            if name not in ("spk_last_error", "spk_dn_last_error") and getattr(L, name).restype is C.c_int:
                 getattr(L, name).restype = i32
         _lib = L
     return _lib
@@ -169,6 +196,26 @@ class Context:
     def set_instrumentation(self, count_traffic: bool):
         self._check(self.L.spk_set_instrumentation(self.h, 1 if count_traffic else 0))
 
+    def render_guides(self):
+        self._check(self.L.spk_render_guides(self.h))
+
+    def guides(self):
+        """Host copies of the primary-hit guides: (normal xyz + linear depth, albedo rgb + hit flag)."""
+        w, h = self.config.width, self.config.height
+        nd = np.zeros((h, w, 4), np.float32)
+        al = np.zeros((h, w, 4), np.float32)
+        self._check(self.L.spk_read_guides(self.h, _p(nd), _p(al)))
+        return nd, al
+
+    def guides_into(self, normal_depth_ptr: int, albedo_ptr: int):
+        """Copies the guides to caller buffers (host or device pointers, H*W float4 each)."""
+        self._check(self.L.spk_read_guides(self.h, C.c_void_p(normal_depth_ptr), C.c_void_p(albedo_ptr)))
+
+    def guides_device(self):
+        a, b = C.c_void_p(), C.c_void_p()
+        self._check(self.L.spk_guides_device(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def tuning(self) -> dict:
         t = spk_tuning()
         self._check(self.L.spk_get_tuning(self.h, C.byref(t)))
@@ -200,3 +247,130 @@ def camera_from_look(position, target, world_up, vfov_rad, focus_distance, apert
     if st != 0:
         raise SpkError(st, "spk_camera_from_look")
     return cam
+
+
+def _dptr(t) -> C.c_void_p:
+    """Device pointer of a torch tensor (or None)."""
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p()
+
+
+class Denoiser:
+    """One spk_denoiser (the U-Net of include/spk_denoise.h) on one CUDA device. Tensors are torch CUDA
+    tensors; each call waits for torch's current stream before it starts and for the denoiser's stream
+    before it returns, so results can be read by torch right away."""
+
+    FEATURES = 10
+    ALIGN = 16
+
+    def __init__(self, device: int = 0, seed: int = 0):
+        self.L = lib()
+        h = C.c_void_p()
+        st = self.L.spk_dn_create(device, seed, C.byref(h))
+        if st != 0:
+            raise SpkError(st, "spk_dn_create failed (no CUDA device?)")
+        self.h = h
+        n = C.c_uint64()
+        self._check(self.L.spk_dn_num_params(self.h, C.byref(n)))
+        self.num_params = n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.spk_dn_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, st: int):
+        if st != 0:
+            raise SpkError(st, self.L.spk_dn_last_error(self.h).decode())
+
+    @staticmethod
+    def _torch_sync():
+        import torch
+        torch.cuda.current_stream().synchronize()
+
+    def _done(self):
+        self._check(self.L.spk_dn_synchronize(self.h))
+
+    def init(self, seed: int):
+        self._check(self.L.spk_dn_init(self.h, seed))
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.num_params, np.float32)
+        self._check(self.L.spk_dn_get_params(self.h, _p(out), self.num_params))
+        return out
+
+    def set_params(self, params: np.ndarray):
+        params = np.ascontiguousarray(params, np.float32)
+        assert params.size == self.num_params
+        self._check(self.L.spk_dn_set_params(self.h, _p(params), self.num_params))
+
+    def pack_features(self, hdr, normal_depth, albedo, out):
+        """hdr, normal_depth, albedo: (n, h, w, 4) float32 CUDA tensors; out: (n, h, w, 10) float32."""
+        n, h, w, _ = hdr.shape
+        self._torch_sync()
+        self._check(self.L.spk_dn_pack_features(self.h, _dptr(hdr), _dptr(normal_depth), _dptr(albedo), n, h, w,
+                                                _dptr(out)))
+        self._done()
+        return out
+
+    def pack_halves(self, full, half_a, normal_depth, albedo, out_a, out_b):
+        """Features of sample half A (`half_a`) and half B (2 * full - half_a)."""
+        n, h, w, _ = full.shape
+        self._torch_sync()
+        self._check(self.L.spk_dn_pack_halves(self.h, _dptr(full), _dptr(half_a), _dptr(normal_depth),
+                                              _dptr(albedo), n, h, w, _dptr(out_a), _dptr(out_b)))
+        self._done()
+
+    def train_step(self, features, target, lr: float) -> float:
+        n, h, w, _ = features.shape
+        loss = C.c_float()
+        self._torch_sync()
+        self._check(self.L.spk_dn_train_step(self.h, _dptr(features), _dptr(target), n, h, w, lr, C.byref(loss)))
+        self._done()
+        return loss.value
+
+    def gradients(self, features, target):
+        n, h, w, _ = features.shape
+        loss = C.c_float()
+        grad = np.empty(self.num_params, np.float32)
+        self._torch_sync()
+        self._check(self.L.spk_dn_gradients(self.h, _dptr(features), _dptr(target), n, h, w, C.byref(loss),
+                                            _p(grad), self.num_params))
+        return loss.value, grad
+
+    def infer(self, features, out=None):
+        import torch
+        n, h, w, _ = features.shape
+        if out is None:
+            out = torch.empty((n, h, w, 4), dtype=torch.float32, device=features.device)
+        self._torch_sync()
+        self._check(self.L.spk_dn_infer(self.h, _dptr(features), n, h, w, _dptr(out)))
+        self._done()
+        return out
+
+    def last_ms(self) -> float:
+        ms = C.c_float()
+        self._check(self.L.spk_dn_last_ms(self.h, C.byref(ms)))
+        return ms.value
+
+    def fallback(self, denoised, den_a, den_b, plain, tile: int, threshold: float, out=None):
+        import torch
+        h, w = denoised.shape[-3], denoised.shape[-2]
+        if out is None:
+            out = torch.empty_like(denoised)
+        count = C.c_uint32()
+        self._torch_sync()
+        self._check(self.L.spk_dn_fallback(self.h, _dptr(denoised), _dptr(den_a), _dptr(den_b), _dptr(plain), h, w,
+                                           tile, threshold, _dptr(out), C.byref(count)))
+        return out, count.value
+
+    def conv3x3(self, op: int, x, x_channels: int, w, y, y_channels: int, n: int, h: int, width: int, bias=None,
+                relu: bool = False, mask=None, mask_ld: int = 0, dw=None, x_ld: int = None, y_ld: int = None):
+        """Low-level conv op on bf16 NHWC CUDA tensors (op 0 forward, 1 dgrad, 2 wgrad into dw)."""
+        self._torch_sync()
+        self._check(self.L.spk_dn_conv3x3(self.h, op, _dptr(x), x_channels, x_ld or x_channels, _dptr(w),
+                                          _dptr(bias), _dptr(y), y_channels, y_ld or y_channels, n, h, width,
+                                          1 if relu else 0, _dptr(mask), mask_ld, _dptr(dw)))
+        self._done()

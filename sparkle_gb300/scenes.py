@@ -254,3 +254,63 @@ def random_rays(lo, hi, n: int, seed: int = 0) -> np.ndarray:
 
 def make_camera(cam_args: dict, width: int, height: int):
     return camera_from_look(width=width, height=height, **cam_args)
+
+
+def _rotation(rng) -> np.ndarray:
+    """Uniform random rotation (QR of a Gaussian matrix with a sign fix)."""
+    q, r = np.linalg.qr(rng.standard_normal((3, 3)))
+    q = q @ np.diag(np.sign(np.diag(r)))
+    if np.linalg.det(q) < 0:
+        q[:, 0] = -q[:, 0]
+    return q
+
+
+def _random_material(rng):
+    kind = rng.choice(3, p=[0.55, 0.3, 0.15])
+    if kind == 0:
+        return Material.lambertian(tuple(rng.uniform(0.05, 0.9, 3)))
+    if kind == 1:
+        return Material.metal(tuple(rng.uniform(0.4, 1.0, 3)), float(rng.uniform(0.05, 0.6)))
+    return Material.glass((1.0, 1.0, 1.0), 1.5)
+
+
+def random_training_scene(seed: int, sphere_level: int = 3, grid: int = 48):
+    """A seeded procedural scene for denoiser training data: a heightfield floor, 3-12 random boxes and
+    icospheres (random scale, rotation and material: Lambertian / GGX metal / glass), 1-3 emissive boxes
+    of random colour and radiance, and either a sun-and-sky environment cube or a gradient sky.
+    Returns (scene, camera_args) with a random look-at camera above the floor."""
+    from .abi import SPK_SKY_GRADIENT
+    rng = np.random.default_rng(seed)
+    size = 20.0
+    floor = heightfield(grid, size, amplitude=float(rng.uniform(0.0, 1.5)), seed=seed + 7)
+    meshes = [floor, unit_cube(), icosphere(sphere_level)]
+    materials = [Material.lambertian(tuple(rng.uniform(0.2, 0.8, 3)))]
+    instances = [Instance(0, 0, _affine(np.eye(3), (0, 0, 0)))]
+    for _ in range(int(rng.integers(3, 13))):
+        mesh = int(rng.integers(1, 3))
+        scale = rng.uniform(0.6, 3.0, 3) if mesh == 1 else np.full(3, rng.uniform(0.5, 2.0))
+        lin = _rotation(rng) @ np.diag(scale)
+        pos = (float(rng.uniform(-6, 6)), float(rng.uniform(-6, 6)), float(rng.uniform(0.5, 3.5)))
+        materials.append(_random_material(rng))
+        instances.append(Instance(mesh, len(materials) - 1, _affine(lin, pos)))
+    for _ in range(int(rng.integers(1, 4))):
+        col = rng.uniform(0.3, 1.0, 3)
+        radiance = col / col.max() * float(rng.uniform(3.0, 20.0))
+        materials.append(Material.light(tuple(radiance)))
+        lin = _rotation(rng) @ np.diag(rng.uniform(0.3, 1.5, 3))
+        pos = (float(rng.uniform(-7, 7)), float(rng.uniform(-7, 7)), float(rng.uniform(3.0, 8.0)))
+        instances.append(Instance(1, len(materials) - 1, _affine(lin, pos)))
+    if rng.random() < 0.6:
+        sun = np.array([rng.uniform(-1, 1), rng.uniform(-1, 1), rng.uniform(0.2, 1.0)])
+        sky = Sky(SPK_SKY_CUBE, (0, 0, 0), sky_cube(32, sun_dir=sun, sun_radiance=float(rng.uniform(10, 50)),
+                                                     sun_cos=float(rng.uniform(0.995, 0.9995))))
+    else:
+        sky = Sky(SPK_SKY_GRADIENT, tuple(rng.uniform(0.1, 1.0, 3)), None)
+    scene = Scene(meshes, instances, materials, sky, name=f"train{seed}")
+    ang = rng.uniform(0, 2 * np.pi)
+    dist = rng.uniform(10, 18)
+    cam = dict(position=(float(dist * np.cos(ang)), float(dist * np.sin(ang)), float(rng.uniform(2.0, 9.0))),
+               target=(float(rng.uniform(-2, 2)), float(rng.uniform(-2, 2)), float(rng.uniform(0.0, 2.0))),
+               world_up=(0, 0, 1), vfov_rad=float(np.deg2rad(rng.uniform(35, 65))), focus_distance=10.0,
+               aperture_radius=0.035 / 22.0 / 2.0, exposure=1.0)
+    return scene, cam

@@ -13,14 +13,17 @@ from sparkle_gb300 import build as spk_build
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 HEADER = os.path.join(ROOT, "include", "spk.h")
+HEADERS = [HEADER, os.path.join(ROOT, "include", "spk_denoise.h")]
 
 STRUCTS = ["spk_mesh", "spk_instance", "spk_material", "spk_sky", "spk_camera", "spk_config", "spk_ray", "spk_hit",
            "spk_stats", "spk_tuning"]
 
 
 def header_functions():
-    text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\w[\w\s\*]*?\b(spk_\w+)\s*\(", text, re.M)))
+    names = set()
+    for h in HEADERS:
+        names |= set(re.findall(r"^\w[\w\s\*]*?\b(spk_\w+)\s*\(", open(h).read(), re.M))
+    return sorted(names)
 
 
 def test_header_functions_are_bound():
