@@ -9,6 +9,10 @@ cube with a baked sun). Rays = traced segments (extension + shadow).
 
 `--impl reference` times the reference's CPU path tracer (the restated oracle: the reference itself does not
 build here) on this machine's host cores over a bounded sample of the same workload.
+
+The line also carries `denoise`: the wall time to relMSE 0.01 / 0.003 at 1920x1080 on the same scene for
+denoised low-spp rendering (the committed U-Net) vs plain path tracing, against a 4096-spp reference
+(`--no-denoise` skips it).
 """
 from __future__ import annotations
 
@@ -312,8 +316,28 @@ def run_ours(args):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if world == 1 and not args.no_denoise:
+        line["denoise"] = denoise_metric(ctx)
     print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def denoise_metric(ctx):
+    """Second half of the metric: wall time to relMSE 0.01 (and 0.003) at 1920x1080 on the same scene,
+    denoised low-spp (committed U-Net weights, tcgen05 inference, per-tile fallback) vs plain path
+    tracing, both scored against a 4096-spp plain reference (the full 16384-spp run is
+    `python -m sparkle_gb300.eval_denoiser`)."""
+    from sparkle_gb300 import denoise, eval_denoiser
+    import os as _os
+    if not _os.path.exists(denoise.WEIGHTS):
+        return {"unavailable": "no trained weights at " + _os.path.relpath(denoise.WEIGHTS, ROOT)}
+    r = eval_denoiser.run(WIDTH, HEIGHT, ref_spp=4096, plain_max=512, den_spp=(1, 4), ctx=ctx)
+    out = {"ref_spp": r["ref_spp"], "nee": True, "threshold": r["threshold"], "tile": r["tile"],
+           "plain": [[p["spp"], round(p["relmse"], 6), p["wall_s"]] for p in r["plain"]],
+           "denoised": [[d["spp"], round(d["relmse"], 6), d["wall_s"], d["fallback_tiles"]] for d in r["denoised"]]}
+    for k in ("time_to_0.01", "time_to_0.003"):
+        out[k] = r[k]
+    return out
 
 
 def run_profile_small(args):
@@ -362,6 +386,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--kernel", type=int, default=0, help="0 auto, 1 megakernel, 2 wavefront")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-denoise", action="store_true", help="skip the denoised-vs-plain time-to-relMSE leg")
     ap.add_argument("--tune", default="", help="spk_tuning knobs, e.g. cuda_graph=0,material_sort=1,bvh_width=4")
     ap.add_argument("--profile-small", action="store_true",
                     help="ncu capture case: the bench workload cut to 2 frames, no timing output")

@@ -69,6 +69,11 @@ inline V3 normalized(V3 a) {
 inline float min_std(float a, float b) { return (b < a) ? b : a; }  // std::min(a, b)
 inline float max_std(float a, float b) { return (a < b) ? b : a; }  // std::max(a, b)
 inline V3 load3(const float *p) { return {p[0], p[1], p[2]}; }
+// RenderPixel's clamp min(c, OutputLimit) (CPURenderer.cpp:408) with one deliberate deviation: a non-finite
+// component becomes 0 instead of entering the running mean as NaN for good. NaN samples come from Refract
+// (Utilities.h:213-220, no total-internal-reflection guard) when RandomUnit() returns exactly 1.0 or when
+// FrDielectric's `sin_t >= 1` test and Refract's sin^2 round differently at the critical angle.
+inline float clamp_sample(float c) { return (c - c == 0.f) ? min_std(c, kOutputLimit) : 0.f; }
 
 // Affine transform rows (3x4, row-major). TransformPoint = t + L*p (Eigen's transform_right_product_impl:
 // res = translation; res += linear * p), TransformDirection = L*d (Transform.h:95-103).
@@ -1121,8 +1126,7 @@ void base_pass(or_renderer &r, bool pruned, int num_threads, uint32_t row_begin,
             const float u = (static_cast<float>(i) + rng.unit()) * pw;
             const float v = (static_cast<float>(j) + rng.unit()) * ph;
             PixelResult res = sample_pixel(r, rng, u, v, pruned, my_rays, my_shadow, my_ovf);
-            res.color = mk(min_std(res.color.x, kOutputLimit), min_std(res.color.y, kOutputLimit),
-                           min_std(res.color.z, kOutputLimit));
+            res.color = mk(clamp_sample(res.color.x), clamp_sample(res.color.y), clamp_sample(res.color.z));
             const size_t k = static_cast<size_t>(j) * r.w + i;
             r.gcolor[k] = {res.color.x, res.color.y, res.color.z, res.valid};
             r.gnormal[k] = res.world_normal;

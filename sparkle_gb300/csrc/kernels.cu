@@ -111,8 +111,8 @@ __global__ void __launch_bounds__(128) k_render_mega(DevScene S, DevCamera cam, 
             d = next_dir;
         }
         const size_t k = static_cast<size_t>(j) * fb.width + i;
-        fb.gcolor[k] = make_float4(min_std(color.x, kOutputLimit), min_std(color.y, kOutputLimit),
-                                   min_std(color.z, kOutputLimit), valid);
+        fb.gcolor[k] = make_float4(clamp_sample(color.x), clamp_sample(color.y),
+                                   clamp_sample(color.z), valid);
         if (p.spatial_denoise) fb.gnormal[k] = make_float4(first_normal.x, first_normal.y, first_normal.z, 0.f);
     }
     warp_add_u64(&counters->extension_rays, rays);

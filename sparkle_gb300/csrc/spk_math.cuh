@@ -51,6 +51,12 @@ SPK_HD f3 normalized(f3 a) {
 // std::min / std::max operand order (NaN in the left operand is returned by min only if b < a fails).
 SPK_HD float min_std(float a, float b) { return (b < a) ? b : a; }
 SPK_HD float max_std(float a, float b) { return (a < b) ? b : a; }
+// RenderPixel's per-sample clamp min(c, OutputLimit) (CPURenderer.cpp:408), except that a non-finite
+// component becomes 0. The reference lets a NaN through the clamp into the running mean, where it stays
+// for good; NaN samples come from its Refract (Utilities.h:213-220, no total-internal-reflection guard)
+// when RandomUnit() returns exactly 1.0 or when FrDielectric's `sin_t >= 1` test and Refract's sin^2
+// round differently at the critical angle. Every finite sample is unchanged.
+SPK_HD float clamp_sample(float c) { return (c - c == 0.f) ? min_std(c, kOutputLimit) : 0.f; }
 
 // Affine 3x4, row-major: TransformPoint = t + L*p, TransformDirection = L*d (Transform.h:95-103).
 SPK_HD f3 xform_point(const float *m, f3 p) {

@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(256) k_wf_finish(FrameBuffers fb, WavefrontSta
     const uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
     if (pid >= fb.width * fb.height) return;
     const float4 c = s.color[pid];
-    fb.gcolor[pid] = make_float4(min_std(c.x, kOutputLimit), min_std(c.y, kOutputLimit), min_std(c.z, kOutputLimit), c.w);
+    fb.gcolor[pid] = make_float4(clamp_sample(c.x), clamp_sample(c.y), clamp_sample(c.z), c.w);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(128) k_mf_shade(DevScene S, DevCamera cam, Fra
             } else {
                 const float4 c = s.color[slot];
                 s.samples[s.slot_item[slot]] =
-                    make_float4(min_std(c.x, kOutputLimit), min_std(c.y, kOutputLimit), min_std(c.z, kOutputLimit), c.w);
+                    make_float4(clamp_sample(c.x), clamp_sample(c.y), clamp_sample(c.z), c.w);
                 need = true;
             }
         }
