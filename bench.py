@@ -357,6 +357,29 @@ def run_profile_small(args):
     ctx.close()
 
 
+def run_profile_unet(args):
+    """ncu capture case for the U-Net's tcgen05 convolutions: one inference at 1920x1080 (padded to
+    1920x1088; about 1.1 GB of activations) and one training step on a 4 x 128 x 128 batch, on seeded
+    random features, with the committed weights when present."""
+    import numpy as np
+    import torch
+    from sparkle_gb300 import denoise, native
+    dn = native.Denoiser(0, seed=1)
+    if os.path.exists(denoise.WEIGHTS):
+        denoise.load_weights(dn)
+    rng = np.random.default_rng(5)
+    feat = torch.from_numpy(rng.uniform(0, 1, (1, HEIGHT, WIDTH, 10)).astype(np.float32)).cuda()
+    out = dn.infer(feat)
+    ms_infer = dn.last_ms()
+    fb = torch.from_numpy(rng.uniform(0, 1, (4, 128, 128, 10)).astype(np.float32)).cuda()
+    tb = torch.from_numpy(rng.uniform(0, 2, (4, 128, 128, 3)).astype(np.float32)).cuda()
+    loss = dn.train_step(fb, tb, 1e-4)
+    ms_train = dn.last_ms()
+    assert np.isfinite(loss) and torch.isfinite(out).all().item()
+    print(json.dumps({"profile_unet": True, "infer_ms": ms_infer, "train_step_ms": ms_train, "loss": loss}))
+    dn.close()
+
+
 def run_profile_rays(args):
     """ncu capture case for the ray-set walk: 4M random rays (origins uniform in the scene box, isotropic
     directions) on the stress scene through spk_trace_device, twice."""
@@ -390,10 +413,14 @@ def main():
     ap.add_argument("--tune", default="", help="spk_tuning knobs, e.g. cuda_graph=0,material_sort=1,bvh_width=4")
     ap.add_argument("--profile-small", action="store_true",
                     help="ncu capture case: the bench workload cut to 2 frames, no timing output")
+    ap.add_argument("--profile-unet", action="store_true",
+                    help="ncu capture case: one 1080p U-Net inference and one training step")
     ap.add_argument("--profile-rays", action="store_true",
                     help="ncu capture case: 4M random rays through spk_trace_device on the stress scene")
     args = ap.parse_args()
-    if args.profile_rays:
+    if args.profile_unet:
+        run_profile_unet(args)
+    elif args.profile_rays:
         run_profile_rays(args)
     elif args.profile_small:
         run_profile_small(args)
