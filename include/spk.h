@@ -205,7 +205,8 @@ typedef struct spk_tuning {
     uint32_t bvh_leaf_size;        /* items per BVH leaf, 1..3 (default 3); used by the next spk_set_scene */
     uint32_t extend_blocks_per_sm; /* traversal CTAs per SM, 0 = the occupancy maximum (default 0) */
     uint32_t shade_blocks_per_sm;  /* shading CTAs per SM, 1..32 (default 8) */
-    uint32_t reserved[2];          /* must be 0 */
+    uint32_t batch_slots;          /* path slots (queue capacity) of spk_render_batch, 0 = min(items, 2^21) */
+    uint32_t reserved;             /* must be 0 */
 } spk_tuning;
 
 /* ------------------------------------------------------------------------------------------------ */
@@ -232,6 +233,23 @@ const char *spk_last_error(const spk_ctx *ctx);
 spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_meshes,
                          const spk_instance *instances, uint32_t num_instances,
                          const spk_material *materials, uint32_t num_materials, const spk_sky *sky);
+
+/* One scene of a multi-scene context: the arguments of spk_set_scene. */
+typedef struct spk_scene_desc {
+    const spk_mesh *meshes;
+    uint32_t num_meshes;
+    const spk_instance *instances;
+    uint32_t num_instances;
+    const spk_material *materials;
+    uint32_t num_materials;
+    const spk_sky *sky;
+} spk_scene_desc;
+
+/* No reference counterpart (the reference renders one scene). Makes several scenes resident at once, for
+ * spk_render_batch: each is built exactly as spk_set_scene builds one, then all share the device arrays.
+ * spk_render / spk_trace / spk_render_guides see scene 0. spk_set_scene(...) is
+ * spk_set_scenes(&one, 1). */
+spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t num_scenes);
 
 /* Replaces CameraRenderProxy::OnTransformDirty/UpdateAttribute (CameraRenderProxy.cpp:118-128): a new
  * camera marks pixels dirty, so the next frame clears the accumulation (CPURenderer.cpp:128-137). */
@@ -306,6 +324,33 @@ spk_status spk_get_tuning(const spk_ctx *ctx, spk_tuning *out);
 spk_status spk_render_guides(spk_ctx *ctx);
 spk_status spk_guides_device(spk_ctx *ctx, void **normal_depth, void **albedo);
 spk_status spk_read_guides(spk_ctx *ctx, float *normal_depth, float *albedo); /* host or device pointers */
+
+/* One render request of a batch: `scene` (index of spk_set_scenes), an image of width x height, `spp`
+ * frames of one sample per pixel (like `spp` spk_render calls at spp = 1 from a cleared accumulation),
+ * path depth `bounce`, per-pixel seed `seed`, and its camera. */
+typedef struct spk_request {
+    uint32_t scene;
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp;
+    uint32_t bounce;
+    uint32_t seed;
+    spk_camera camera;
+} spk_request;
+
+/* No reference counterpart. Renders all requests in one regenerating wavefront: sample items (request,
+ * frame, pixel) of every request are handed to path slots from one counter, so requests of uneven
+ * resolution, sample count, depth and scene keep the GPU full together. `rng` and `enable_nee` apply to
+ * the whole batch. Each request's frame buffer and tonemapped image are bit-identical to spk_set_config
+ * ({width, height, spp = 1, max_spp >= spp, bounce, spatial_denoise = 0, enable_nee, rng, seed}) +
+ * spk_set_camera + spk_render(spp) on its scene. Waits for completion; spk_get_stats reports the batch. */
+spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t num_requests, uint32_t rng,
+                            uint32_t enable_nee);
+
+/* Copies request `index` of the last batch out (host or device pointers; either may be NULL): its
+ * accumulated HDR frame buffer (height rows of width float4, bottom row first) and its tonemapped RGBA16F
+ * image (top row first). */
+spk_status spk_read_batch(spk_ctx *ctx, uint32_t index, float *hdr_rgba, uint16_t *rgba16f);
 
 /* Largest width * height spk_render_noalloc accepts (512 x 512). */
 #define SPK_NOALLOC_MAX_PIXELS (512u * 512u)

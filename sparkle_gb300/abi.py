@@ -75,7 +75,18 @@ class spk_stats(C.Structure):
 
 class spk_tuning(C.Structure):
     _fields_ = [("cuda_graph", _u32), ("material_sort", _u32), ("bvh_width", _u32), ("bvh_leaf_size", _u32),
-                ("extend_blocks_per_sm", _u32), ("shade_blocks_per_sm", _u32), ("reserved", _u32 * 2)]
+                ("extend_blocks_per_sm", _u32), ("shade_blocks_per_sm", _u32), ("batch_slots", _u32),
+                ("reserved", _u32)]
+
+
+class spk_scene_desc(C.Structure):
+    _fields_ = [("meshes", C.c_void_p), ("num_meshes", _u32), ("instances", C.c_void_p), ("num_instances", _u32),
+                ("materials", C.c_void_p), ("num_materials", _u32), ("sky", C.c_void_p)]
+
+
+class spk_request(C.Structure):
+    _fields_ = [("scene", _u32), ("width", _u32), ("height", _u32), ("spp", _u32), ("bounce", _u32),
+                ("seed", _u32), ("camera", spk_camera)]
 
 
 HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4"), ("face", "<u4")])

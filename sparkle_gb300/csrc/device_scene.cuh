@@ -47,6 +47,18 @@ struct alignas(16) DevLight {
 };
 static_assert(sizeof(DevLight) == 64, "DevLight is 64 bytes");
 
+// One scene of a context holding several (spk_set_scenes): its TLAS root in the shared node array, its
+// sky, and its slice of the shared light table. Instance light_base indices are relative to the slice.
+struct DevSceneDesc {
+    uint32_t tlas_root;
+    uint32_t sky_mode, sky_size;
+    float sky_color[3];
+    uint32_t sky_offset;   // first texel of the scene's cube in sky_cube
+    uint32_t light_base;   // first entry of the scene's lights / light_cdf
+    uint32_t num_lights;
+    float light_total;
+};
+
 struct DevScene {
     const DevLight *lights;   // emissive triangles of mesh instances, instance then face order
     const float *light_cdf;   // running sum of light areas
@@ -65,6 +77,26 @@ struct DevScene {
     uint32_t sky_size;
     float sky_color[3];
     float scene_abs_x;  // max |x| over world bounds; bounds the x-only world-t error used for pruning
+    const DevSceneDesc *descs;  // every scene of the context (the fields above are scene 0's)
+    uint32_t num_scenes;
 };
+
+// The DevScene of scene `k` of a multi-scene context: scene 0's record with the TLAS root, sky and light
+// table of scene k. Everything else (nodes, triangles, instances, materials) is shared.
+__host__ __device__ inline DevScene scene_view(const DevScene &S, const DevSceneDesc &d) {
+    DevScene v = S;
+    v.tlas_root = d.tlas_root;
+    v.sky_mode = d.sky_mode;
+    v.sky_size = d.sky_size;
+    v.sky_color[0] = d.sky_color[0];
+    v.sky_color[1] = d.sky_color[1];
+    v.sky_color[2] = d.sky_color[2];
+    v.sky_cube = S.sky_cube + d.sky_offset;
+    v.lights = S.lights + d.light_base;
+    v.light_cdf = S.light_cdf + d.light_base;
+    v.num_lights = d.num_lights;
+    v.light_total = d.light_total;
+    return v;
+}
 
 }  // namespace spk

@@ -23,6 +23,7 @@ __global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_trace(DevScene S, 
             const float *r = rays + q * 6;
             o = mk3(r[0], r[1], r[2]);
             d = mk3(r[3], r[4], r[5]);
+            return S.tlas_root;
         },
         [&](unsigned long long q, const TraceResult &res) {
             spk_hit_dev out;

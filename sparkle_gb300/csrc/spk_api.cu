@@ -68,6 +68,7 @@ struct spk_ctx {
     DevBuf<float4> sky;
     DevBuf<DevLight> lights;
     DevBuf<float> light_cdf;
+    DevBuf<DevSceneDesc> scene_descs;
     DevScene scene{};
     bool has_scene = false;
     uint32_t bvh_nodes = 0;
@@ -84,6 +85,12 @@ struct spk_ctx {
     DevBuf<float4> guide_nd, guide_albedo;  // primary-hit guides (spk_render_guides)
     WavefrontState wf{};
     ChunkGraph chunk_graph{};
+    // batch (spk_render_batch)
+    WavefrontState wf_batch{};
+    DevBuf<DevRequest> batch_reqs;
+    DevBuf<float4> batch_hdr;
+    DevBuf<ushort4> batch_img;
+    std::vector<DevRequest> batch_host;
     spk_tuning tuning = default_tuning();
 
     // CameraRenderProxy / CPURenderer sample bookkeeping
@@ -191,6 +198,326 @@ void append_wide(std::vector<WideNode> &all, const WideBvh &w, uint32_t item_off
 
 }  // namespace
 
+namespace {
+
+struct HostScene {
+    std::vector<WideNode> nodes;
+    std::vector<float4> tris;
+    std::vector<uint32_t> tlas_items;
+    std::vector<DevInstance> insts;
+    std::vector<float4> verts;
+    std::vector<uint4> faces;
+    std::vector<DevMaterial> mats;
+    std::vector<float4> cube;
+    std::vector<DevLight> lights;
+    std::vector<float> light_cdf;
+    uint32_t tlas_root = kInvalid;
+    uint32_t sky_mode = SPK_SKY_NONE, sky_size = 0;
+    float sky_color[3] = {0.f, 0.f, 0.f};
+    float abs_x = 0.f, light_total = 0.f;
+};
+
+// Validates one scene description and builds its host-side records (BLAS per mesh, TLAS, vertex/face
+// records, materials, emissive-triangle light table, sky texels), with indices local to the scene.
+spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_meshes, const spk_instance *instances,
+                            uint32_t num_instances, const spk_material *materials, uint32_t num_materials,
+                            const spk_sky *sky, HostScene &hs) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if ((num_meshes && !meshes) || (num_instances && !instances) || (num_materials && !materials))
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "null scene array");
+    const int threads = host_threads();
+    // Validate.
+    for (uint32_t k = 0; k < num_meshes; ++k) {
+        const spk_mesh &m = meshes[k];
+        if (m.num_faces && (!m.positions || !m.normals || !m.indices))
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "mesh %u: positions, normals and indices are required", k);
+        for (uint64_t f = 0; f < 3ull * m.num_faces; ++f) {
+            if (m.indices[f] >= m.num_vertices)
+                return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "mesh %u: index %u out of range", k, m.indices[f]);
+        }
+    }
+    for (uint32_t k = 0; k < num_instances; ++k) {
+        const spk_instance &in = instances[k];
+        if (in.type != SPK_PRIM_MESH && in.type != SPK_PRIM_SPHERE)
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: bad type", k);
+        if (in.type == SPK_PRIM_MESH && in.mesh_id >= num_meshes)
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: mesh_id out of range", k);
+        if (in.material_id >= num_materials)
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: material_id out of range", k);
+    }
+    if (sky && sky->mode == SPK_SKY_CUBE && (!sky->cube_rgba || sky->cube_size == 0))
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "hs.cube sky without texels");
+
+    // BLAS per mesh: binned SAH BVH2 (<= 3 triangles per leaf) collapsed to 8-wide nodes.
+    std::vector<uint32_t> blas_root(num_meshes, kInvalid);
+    std::vector<uint32_t> vert_base(num_meshes, 0), face_base(num_meshes, 0);
+    std::vector<std::array<double, 6>> mesh_bounds(num_meshes);
+    for (uint32_t k = 0; k < num_meshes; ++k) {
+        const spk_mesh &m = meshes[k];
+        vert_base[k] = static_cast<uint32_t>(hs.verts.size() / 3);
+        face_base[k] = static_cast<uint32_t>(hs.faces.size());
+        for (uint32_t v = 0; v < m.num_vertices; ++v) {
+            const float *n = m.normals + 3 * v;
+            const float t[4] = {m.tangents ? m.tangents[4 * v] : 1.f, m.tangents ? m.tangents[4 * v + 1] : 0.f,
+                                m.tangents ? m.tangents[4 * v + 2] : 0.f, m.tangents ? m.tangents[4 * v + 3] : 1.f};
+            const float uv[2] = {m.uvs ? m.uvs[2 * v] : 0.f, m.uvs ? m.uvs[2 * v + 1] : 0.f};
+            hs.verts.push_back(make_float4(n[0], n[1], n[2], t[0]));
+            hs.verts.push_back(make_float4(t[1], t[2], t[3], uv[0]));
+            hs.verts.push_back(make_float4(uv[1], 0.f, 0.f, 0.f));
+        }
+        for (uint32_t f = 0; f < m.num_faces; ++f)
+            hs.faces.push_back(make_uint4(m.indices[3 * f], m.indices[3 * f + 1], m.indices[3 * f + 2], 0u));
+        auto &mb = mesh_bounds[k];
+        mb = {std::numeric_limits<double>::max(), std::numeric_limits<double>::max(),
+              std::numeric_limits<double>::max(), -std::numeric_limits<double>::max(),
+              -std::numeric_limits<double>::max(), -std::numeric_limits<double>::max()};
+        if (m.num_faces == 0) continue;
+        std::vector<BuildBox> boxes(m.num_faces);
+        for (uint32_t f = 0; f < m.num_faces; ++f) {
+            BuildBox b;
+            for (int a = 0; a < 3; ++a) {
+                b.lo[a] = std::numeric_limits<float>::max();
+                b.hi[a] = -std::numeric_limits<float>::max();
+            }
+            for (int c = 0; c < 3; ++c) {
+                const float *p = m.positions + 3 * m.indices[3 * f + c];
+                for (int a = 0; a < 3; ++a) {
+                    b.lo[a] = std::min(b.lo[a], p[a]);
+                    b.hi[a] = std::max(b.hi[a], p[a]);
+                    mb[a] = std::min(mb[a], static_cast<double>(p[a]));
+                    mb[3 + a] = std::max(mb[3 + a], static_cast<double>(p[a]));
+                }
+            }
+            boxes[f] = b;
+        }
+        const Bvh2 b2 = build_bvh2(boxes, ctx->tuning.bvh_leaf_size, threads);
+        const WideBvh wide = collapse_wide(b2, static_cast<int>(ctx->tuning.bvh_width));
+        const uint32_t tri_offset = static_cast<uint32_t>(hs.tris.size() / 3);
+        blas_root[k] = static_cast<uint32_t>(hs.nodes.size());
+        append_wide(hs.nodes, wide, tri_offset);
+        for (uint32_t face : wide.items) {
+            const float *p0 = m.positions + 3 * m.indices[3 * face];
+            const float *p1 = m.positions + 3 * m.indices[3 * face + 1];
+            const float *p2 = m.positions + 3 * m.indices[3 * face + 2];
+            // BLAS::Triangle::Set: e1 = v1 - v0, e2 = v2 - v0 (MeshRenderProxy.cpp:80-86)
+            const float e1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+            const float e2[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+            uint32_t fbits = face;
+            float ff;
+            std::memcpy(&ff, &fbits, 4);
+            hs.tris.push_back(make_float4(p0[0], p0[1], p0[2], e1[0]));
+            hs.tris.push_back(make_float4(e1[1], e1[2], e2[0], e2[1]));
+            hs.tris.push_back(make_float4(e2[2], ff, 0.f, 0.f));
+        }
+    }
+    // Instances + TLAS over their world boxes (TLAS::Build, SceneRenderProxy.cpp:31-69).
+    hs.insts.assign(num_instances, DevInstance{});
+    std::vector<BuildBox> inst_boxes(num_instances);
+    float abs_x = 0.f;
+    for (uint32_t k = 0; k < num_instances; ++k) {
+        const spk_instance &in = instances[k];
+        DevInstance &d = hs.insts[k];
+        std::memset(&d, 0, sizeof(d));
+        std::memcpy(d.m, in.transform, sizeof(d.m));
+        std::memcpy(d.minv, in.inv_transform, sizeof(d.minv));
+        d.type = in.type;
+        d.material = in.material_id;
+        d.radius = in.radius;
+        d.mesh_id = in.mesh_id;
+        if (in.type == SPK_PRIM_SPHERE) {
+            d.blas_root = kInvalid;
+            const double r = std::fabs(static_cast<double>(in.radius));
+            const double lo[3] = {-r, -r, -r}, hi[3] = {r, r, r};
+            const float tm[12] = {1, 0, 0, in.transform[3], 0, 1, 0, in.transform[7], 0, 0, 1, in.transform[11]};
+            inst_boxes[k] = world_box(tm, lo, hi);
+        } else {
+            d.blas_root = blas_root[in.mesh_id];
+            d.vert_base = vert_base[in.mesh_id];
+            d.face_base = face_base[in.mesh_id];
+            const auto &mb = mesh_bounds[in.mesh_id];
+            if (d.blas_root == kInvalid) {
+                const double z[3] = {0, 0, 0};
+                inst_boxes[k] = world_box(in.transform, z, z);
+            } else {
+                const double lo[3] = {mb[0], mb[1], mb[2]}, hi[3] = {mb[3], mb[4], mb[5]};
+                inst_boxes[k] = world_box(in.transform, lo, hi);
+            }
+        }
+        abs_x = std::max(abs_x, std::max(std::fabs(inst_boxes[k].lo[0]), std::fabs(inst_boxes[k].hi[0])));
+    }
+    if (num_instances > 0) {
+        const Bvh2 b2 = build_bvh2(inst_boxes, ctx->tuning.bvh_leaf_size, threads);
+        const WideBvh wide = collapse_wide(b2, static_cast<int>(ctx->tuning.bvh_width));
+        hs.tlas_root = static_cast<uint32_t>(hs.nodes.size());
+        append_wide(hs.nodes, wide, 0);
+        hs.tlas_items = wide.items;
+    }
+    // Materials; the emissive test is SamplePixel's `emissive_color.norm() > Eps` (CPURenderer.cpp:286-287).
+    hs.mats.assign(num_materials, DevMaterial{});
+    for (uint32_t k = 0; k < num_materials; ++k) {
+        const spk_material &s = materials[k];
+        DevMaterial &d = hs.mats[k];
+        std::memset(&d, 0, sizeof(d));
+        for (int c = 0; c < 3; ++c) {
+            d.base[c] = s.base_color[c];
+            d.emissive[c] = s.emissive[c];
+        }
+        d.type = s.type;
+        const volatile float e0 = s.emissive[0] * s.emissive[0], e1 = s.emissive[1] * s.emissive[1],
+                             e2 = s.emissive[2] * s.emissive[2];
+        const volatile float sn = e0 + (e1 + e2);
+        d.is_emissive = std::sqrt(static_cast<float>(sn)) > kEps ? 1u : 0u;
+        d.metallic = s.metallic;
+        d.roughness = s.roughness;
+        d.eta = s.eta;
+    }
+    // Emissive triangles of mesh instances in world space (instance then face order) and their area CDF,
+    // for next-event estimation.
+    for (uint32_t k = 0; k < num_instances; ++k) hs.insts[k].light_base = kInvalid;
+    for (uint32_t k = 0; k < num_instances; ++k) {
+        const spk_instance &in = instances[k];
+        if (in.type != SPK_PRIM_MESH || !hs.mats[in.material_id].is_emissive) continue;
+        const spk_mesh &m = meshes[in.mesh_id];
+        hs.insts[k].light_base = static_cast<uint32_t>(hs.lights.size());
+        for (uint32_t f = 0; f < m.num_faces; ++f) {
+            f3 w[3];
+            for (int c = 0; c < 3; ++c) {
+                const float *p = m.positions + 3 * m.indices[3 * f + c];
+                w[c] = xform_point(in.transform, mk3(p[0], p[1], p[2]));
+            }
+            DevLight L{};
+            const f3 e1 = w[1] - w[0], e2 = w[2] - w[0];
+            const f3 cr = cross(e1, e2);
+            const float len = std::sqrt(sqnorm(cr));
+            const f3 ng = len > 0.f ? mk3(cr.x / len, cr.y / len, cr.z / len) : mk3(0.f, 0.f, 0.f);
+            const float vals[5][3] = {{w[0].x, w[0].y, w[0].z}, {e1.x, e1.y, e1.z}, {e2.x, e2.y, e2.z},
+                                      {ng.x, ng.y, ng.z},
+                                      {hs.mats[in.material_id].emissive[0], hs.mats[in.material_id].emissive[1],
+                                       hs.mats[in.material_id].emissive[2]}};
+            std::memcpy(L.p0, vals[0], 12);
+            std::memcpy(L.e1, vals[1], 12);
+            std::memcpy(L.e2, vals[2], 12);
+            std::memcpy(L.ng, vals[3], 12);
+            std::memcpy(L.emission, vals[4], 12);
+            L.area = 0.5f * len;
+            hs.lights.push_back(L);
+        }
+    }
+    for (const DevLight &L : hs.lights) {
+        hs.light_total = hs.light_total + L.area;
+        hs.light_cdf.push_back(hs.light_total);
+    }
+    if (!(hs.light_total > 0.f)) {
+        hs.lights.clear();
+        hs.light_cdf.clear();
+        for (uint32_t k = 0; k < num_instances; ++k) hs.insts[k].light_base = kInvalid;
+    }
+    if (sky && sky->mode == SPK_SKY_CUBE) {
+        const size_t n = 6ull * sky->cube_size * sky->cube_size;
+        hs.cube.resize(n);
+        std::memcpy(hs.cube.data(), sky->cube_rgba, n * sizeof(float4));
+    }
+    hs.sky_mode = sky ? sky->mode : SPK_SKY_NONE;
+    hs.sky_size = sky ? sky->cube_size : 0;
+    for (int c = 0; c < 3; ++c) hs.sky_color[c] = sky ? sky->color[c] : 0.f;
+    hs.abs_x = abs_x;
+    return SPK_OK;
+}
+
+// Appends scene `s` to `all` (node, triangle, instance, vertex, face, material, texel and light indices
+// offset into the shared arrays) and describes it in `d`.
+void append_scene(HostScene &all, const HostScene &s, DevSceneDesc &d) {
+    const uint32_t node_off = static_cast<uint32_t>(all.nodes.size());
+    const uint32_t tri_off = static_cast<uint32_t>(all.tris.size() / 3);
+    const uint32_t item_off = static_cast<uint32_t>(all.tlas_items.size());
+    const uint32_t inst_off = static_cast<uint32_t>(all.insts.size());
+    const uint32_t vert_off = static_cast<uint32_t>(all.verts.size() / 3);
+    const uint32_t face_off = static_cast<uint32_t>(all.faces.size());
+    const uint32_t mat_off = static_cast<uint32_t>(all.mats.size());
+    // BLAS nodes come first, the TLAS nodes (from tlas_root on) last; items index triangles or TLAS items.
+    for (size_t k = 0; k < s.nodes.size(); ++k) {
+        WideNode n = s.nodes[k];
+        n.child_base += node_off;
+        const bool tlas = s.tlas_root != kInvalid && k >= s.tlas_root;
+        n.item_base += tlas ? item_off : tri_off;
+        all.nodes.push_back(n);
+    }
+    all.tris.insert(all.tris.end(), s.tris.begin(), s.tris.end());
+    for (uint32_t it : s.tlas_items) all.tlas_items.push_back(it + inst_off);
+    for (DevInstance in : s.insts) {
+        if (in.blas_root != kInvalid) in.blas_root += node_off;
+        in.vert_base += vert_off;
+        in.face_base += face_off;
+        in.material += mat_off;
+        all.insts.push_back(in);  // light_base stays relative to the scene's light slice
+    }
+    all.verts.insert(all.verts.end(), s.verts.begin(), s.verts.end());
+    all.faces.insert(all.faces.end(), s.faces.begin(), s.faces.end());
+    all.mats.insert(all.mats.end(), s.mats.begin(), s.mats.end());
+    d = DevSceneDesc{};
+    d.tlas_root = s.tlas_root == kInvalid ? kInvalid : s.tlas_root + node_off;
+    d.sky_mode = s.sky_mode;
+    d.sky_size = s.sky_size;
+    for (int c = 0; c < 3; ++c) d.sky_color[c] = s.sky_color[c];
+    d.sky_offset = static_cast<uint32_t>(all.cube.size());
+    all.cube.insert(all.cube.end(), s.cube.begin(), s.cube.end());
+    d.light_base = static_cast<uint32_t>(all.lights.size());
+    d.num_lights = static_cast<uint32_t>(s.lights.size());
+    d.light_total = s.light_total;
+    all.lights.insert(all.lights.end(), s.lights.begin(), s.lights.end());
+    all.light_cdf.insert(all.light_cdf.end(), s.light_cdf.begin(), s.light_cdf.end());
+    all.abs_x = std::max(all.abs_x, s.abs_x);
+}
+
+// Uploads concatenated scene records and points the context's DevScene at them (scene 0 by default).
+spk_status upload_scene(spk_ctx *ctx, const HostScene &hs, const std::vector<DevSceneDesc> &descs) {
+    ctx->has_scene = false;
+    cudaError_t e;
+    static_assert(sizeof(WideNode) == 5 * sizeof(uint4), "node size");
+    if ((e = upload(ctx->nodes, reinterpret_cast<const uint4 *>(hs.nodes.data()), hs.nodes.size() * 5,
+                    ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->tris, hs.tris.data(), hs.tris.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->tlas_items, hs.tlas_items.data(), hs.tlas_items.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->instances, hs.insts.data(), hs.insts.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->verts, hs.verts.data(), hs.verts.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->faces, hs.faces.data(), hs.faces.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->materials, hs.mats.data(), hs.mats.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->sky, hs.cube.data(), hs.cube.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->lights, hs.lights.data(), hs.lights.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->light_cdf, hs.light_cdf.data(), hs.light_cdf.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->scene_descs, descs.data(), descs.size(), ctx->stream)) != cudaSuccess) {
+        return cuda_fail(ctx, e, "scene upload");
+    }
+    DevScene &S = ctx->scene;
+    S.nodes = ctx->nodes.ptr;
+    S.tris = ctx->tris.ptr;
+    S.tlas_items = ctx->tlas_items.ptr;
+    S.instances = ctx->instances.ptr;
+    S.verts = ctx->verts.ptr;
+    S.faces = ctx->faces.ptr;
+    S.materials = ctx->materials.ptr;
+    S.sky_cube = ctx->sky.ptr;
+    S.scene_abs_x = hs.abs_x;
+    S.lights = ctx->lights.ptr;
+    S.light_cdf = ctx->light_cdf.ptr;
+    S.descs = ctx->scene_descs.ptr;
+    S.num_scenes = static_cast<uint32_t>(descs.size());
+    const DevScene v = scene_view(S, descs[0]);
+    S.tlas_root = v.tlas_root;
+    S.sky_mode = v.sky_mode;
+    S.sky_size = v.sky_size;
+    for (int c = 0; c < 3; ++c) S.sky_color[c] = v.sky_color[c];
+    S.num_lights = v.num_lights;
+    S.light_total = v.light_total;
+    ctx->bvh_nodes = static_cast<uint32_t>(hs.nodes.size());
+    ctx->bvh_bytes = hs.nodes.size() * sizeof(WideNode) + hs.tris.size() * sizeof(float4);
+    ctx->has_scene = true;
+    ctx->dirty = true;
+    return SPK_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 uint32_t spk_abi_version(void) { return SPK_ABI_VERSION; }
@@ -232,6 +559,7 @@ spk_status spk_destroy(spk_ctx *ctx) {
     ctx->sky.reset();
     ctx->lights.reset();
     ctx->light_cdf.reset();
+    ctx->scene_descs.reset();
     ctx->gcolor.reset();
     ctx->gnormal.reset();
     ctx->guide_nd.reset();
@@ -239,6 +567,10 @@ spk_status spk_destroy(spk_ctx *ctx) {
     ctx->fb.reset();
     ctx->out.reset();
     wavefront_free(ctx->wf);
+    wavefront_free(ctx->wf_batch);
+    ctx->batch_reqs.reset();
+    ctx->batch_hdr.reset();
+    ctx->batch_img.reset();
     chunk_graph_free(ctx->chunk_graph);
     if (ctx->counters) cudaFree(ctx->counters);
     for (cudaEvent_t ev : ctx->event_pool) cudaEventDestroy(ev);
@@ -255,252 +587,34 @@ spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_mesh
                          uint32_t num_instances, const spk_material *materials, uint32_t num_materials,
                          const spk_sky *sky) {
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
-    if ((num_meshes && !meshes) || (num_instances && !instances) || (num_materials && !materials))
-        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "null scene array");
+    const spk_scene_desc d{meshes, num_meshes, instances, num_instances, materials, num_materials, sky};
+    return spk_set_scenes(ctx, &d, 1);
+}
+
+spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t num_scenes) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (!scenes || num_scenes == 0) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "no scenes");
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    const int threads = host_threads();
-    // Validate.
-    for (uint32_t k = 0; k < num_meshes; ++k) {
-        const spk_mesh &m = meshes[k];
-        if (m.num_faces && (!m.positions || !m.normals || !m.indices))
-            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "mesh %u: positions, normals and indices are required", k);
-        for (uint64_t f = 0; f < 3ull * m.num_faces; ++f) {
-            if (m.indices[f] >= m.num_vertices)
-                return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "mesh %u: index %u out of range", k, m.indices[f]);
+    HostScene all;
+    std::vector<DevSceneDesc> descs(num_scenes);
+    for (uint32_t k = 0; k < num_scenes; ++k) {
+        const spk_scene_desc &d = scenes[k];
+        HostScene hs;
+        const spk_status st = build_host_scene(ctx, d.meshes, d.num_meshes, d.instances, d.num_instances,
+                                               d.materials, d.num_materials, d.sky, hs);
+        if (st != SPK_OK) {
+            if (num_scenes > 1) ctx->error = "scene " + std::to_string(k) + ": " + ctx->error;
+            return st;
         }
-    }
-    for (uint32_t k = 0; k < num_instances; ++k) {
-        const spk_instance &in = instances[k];
-        if (in.type != SPK_PRIM_MESH && in.type != SPK_PRIM_SPHERE)
-            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: bad type", k);
-        if (in.type == SPK_PRIM_MESH && in.mesh_id >= num_meshes)
-            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: mesh_id out of range", k);
-        if (in.material_id >= num_materials)
-            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: material_id out of range", k);
-    }
-    if (sky && sky->mode == SPK_SKY_CUBE && (!sky->cube_rgba || sky->cube_size == 0))
-        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "cube sky without texels");
-
-    // BLAS per mesh: binned SAH BVH2 (<= 3 triangles per leaf) collapsed to 8-wide nodes.
-    std::vector<WideNode> all_nodes;
-    std::vector<float4> tri_recs;
-    std::vector<uint32_t> blas_root(num_meshes, kInvalid);
-    std::vector<uint32_t> vert_base(num_meshes, 0), face_base(num_meshes, 0);
-    std::vector<float4> vert_recs;
-    std::vector<uint4> face_recs;
-    std::vector<std::array<double, 6>> mesh_bounds(num_meshes);
-    for (uint32_t k = 0; k < num_meshes; ++k) {
-        const spk_mesh &m = meshes[k];
-        vert_base[k] = static_cast<uint32_t>(vert_recs.size() / 3);
-        face_base[k] = static_cast<uint32_t>(face_recs.size());
-        for (uint32_t v = 0; v < m.num_vertices; ++v) {
-            const float *n = m.normals + 3 * v;
-            const float t[4] = {m.tangents ? m.tangents[4 * v] : 1.f, m.tangents ? m.tangents[4 * v + 1] : 0.f,
-                                m.tangents ? m.tangents[4 * v + 2] : 0.f, m.tangents ? m.tangents[4 * v + 3] : 1.f};
-            const float uv[2] = {m.uvs ? m.uvs[2 * v] : 0.f, m.uvs ? m.uvs[2 * v + 1] : 0.f};
-            vert_recs.push_back(make_float4(n[0], n[1], n[2], t[0]));
-            vert_recs.push_back(make_float4(t[1], t[2], t[3], uv[0]));
-            vert_recs.push_back(make_float4(uv[1], 0.f, 0.f, 0.f));
+        if (num_scenes == 1) {
+            descs[0] = DevSceneDesc{hs.tlas_root, hs.sky_mode, hs.sky_size, {hs.sky_color[0], hs.sky_color[1],
+                                    hs.sky_color[2]}, 0u, 0u, static_cast<uint32_t>(hs.lights.size()), hs.light_total};
+            return upload_scene(ctx, hs, descs);
         }
-        for (uint32_t f = 0; f < m.num_faces; ++f)
-            face_recs.push_back(make_uint4(m.indices[3 * f], m.indices[3 * f + 1], m.indices[3 * f + 2], 0u));
-        auto &mb = mesh_bounds[k];
-        mb = {std::numeric_limits<double>::max(), std::numeric_limits<double>::max(),
-              std::numeric_limits<double>::max(), -std::numeric_limits<double>::max(),
-              -std::numeric_limits<double>::max(), -std::numeric_limits<double>::max()};
-        if (m.num_faces == 0) continue;
-        std::vector<BuildBox> boxes(m.num_faces);
-        for (uint32_t f = 0; f < m.num_faces; ++f) {
-            BuildBox b;
-            for (int a = 0; a < 3; ++a) {
-                b.lo[a] = std::numeric_limits<float>::max();
-                b.hi[a] = -std::numeric_limits<float>::max();
-            }
-            for (int c = 0; c < 3; ++c) {
-                const float *p = m.positions + 3 * m.indices[3 * f + c];
-                for (int a = 0; a < 3; ++a) {
-                    b.lo[a] = std::min(b.lo[a], p[a]);
-                    b.hi[a] = std::max(b.hi[a], p[a]);
-                    mb[a] = std::min(mb[a], static_cast<double>(p[a]));
-                    mb[3 + a] = std::max(mb[3 + a], static_cast<double>(p[a]));
-                }
-            }
-            boxes[f] = b;
-        }
-        const Bvh2 b2 = build_bvh2(boxes, ctx->tuning.bvh_leaf_size, threads);
-        const WideBvh wide = collapse_wide(b2, static_cast<int>(ctx->tuning.bvh_width));
-        const uint32_t tri_offset = static_cast<uint32_t>(tri_recs.size() / 3);
-        blas_root[k] = static_cast<uint32_t>(all_nodes.size());
-        append_wide(all_nodes, wide, tri_offset);
-        for (uint32_t face : wide.items) {
-            const float *p0 = m.positions + 3 * m.indices[3 * face];
-            const float *p1 = m.positions + 3 * m.indices[3 * face + 1];
-            const float *p2 = m.positions + 3 * m.indices[3 * face + 2];
-            // BLAS::Triangle::Set: e1 = v1 - v0, e2 = v2 - v0 (MeshRenderProxy.cpp:80-86)
-            const float e1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
-            const float e2[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
-            uint32_t fbits = face;
-            float ff;
-            std::memcpy(&ff, &fbits, 4);
-            tri_recs.push_back(make_float4(p0[0], p0[1], p0[2], e1[0]));
-            tri_recs.push_back(make_float4(e1[1], e1[2], e2[0], e2[1]));
-            tri_recs.push_back(make_float4(e2[2], ff, 0.f, 0.f));
-        }
+        append_scene(all, hs, descs[k]);
     }
-    // Instances + TLAS over their world boxes (TLAS::Build, SceneRenderProxy.cpp:31-69).
-    std::vector<DevInstance> inst_recs(num_instances);
-    std::vector<BuildBox> inst_boxes(num_instances);
-    float abs_x = 0.f;
-    for (uint32_t k = 0; k < num_instances; ++k) {
-        const spk_instance &in = instances[k];
-        DevInstance &d = inst_recs[k];
-        std::memset(&d, 0, sizeof(d));
-        std::memcpy(d.m, in.transform, sizeof(d.m));
-        std::memcpy(d.minv, in.inv_transform, sizeof(d.minv));
-        d.type = in.type;
-        d.material = in.material_id;
-        d.radius = in.radius;
-        d.mesh_id = in.mesh_id;
-        if (in.type == SPK_PRIM_SPHERE) {
-            d.blas_root = kInvalid;
-            const double r = std::fabs(static_cast<double>(in.radius));
-            const double lo[3] = {-r, -r, -r}, hi[3] = {r, r, r};
-            const float tm[12] = {1, 0, 0, in.transform[3], 0, 1, 0, in.transform[7], 0, 0, 1, in.transform[11]};
-            inst_boxes[k] = world_box(tm, lo, hi);
-        } else {
-            d.blas_root = blas_root[in.mesh_id];
-            d.vert_base = vert_base[in.mesh_id];
-            d.face_base = face_base[in.mesh_id];
-            const auto &mb = mesh_bounds[in.mesh_id];
-            if (d.blas_root == kInvalid) {
-                const double z[3] = {0, 0, 0};
-                inst_boxes[k] = world_box(in.transform, z, z);
-            } else {
-                const double lo[3] = {mb[0], mb[1], mb[2]}, hi[3] = {mb[3], mb[4], mb[5]};
-                inst_boxes[k] = world_box(in.transform, lo, hi);
-            }
-        }
-        abs_x = std::max(abs_x, std::max(std::fabs(inst_boxes[k].lo[0]), std::fabs(inst_boxes[k].hi[0])));
-    }
-    uint32_t tlas_root = kInvalid;
-    std::vector<uint32_t> tlas_items;
-    if (num_instances > 0) {
-        const Bvh2 b2 = build_bvh2(inst_boxes, ctx->tuning.bvh_leaf_size, threads);
-        const WideBvh wide = collapse_wide(b2, static_cast<int>(ctx->tuning.bvh_width));
-        tlas_root = static_cast<uint32_t>(all_nodes.size());
-        append_wide(all_nodes, wide, 0);
-        tlas_items = wide.items;
-    }
-    // Materials; the emissive test is SamplePixel's `emissive_color.norm() > Eps` (CPURenderer.cpp:286-287).
-    std::vector<DevMaterial> mat_recs(num_materials);
-    for (uint32_t k = 0; k < num_materials; ++k) {
-        const spk_material &s = materials[k];
-        DevMaterial &d = mat_recs[k];
-        std::memset(&d, 0, sizeof(d));
-        for (int c = 0; c < 3; ++c) {
-            d.base[c] = s.base_color[c];
-            d.emissive[c] = s.emissive[c];
-        }
-        d.type = s.type;
-        const volatile float e0 = s.emissive[0] * s.emissive[0], e1 = s.emissive[1] * s.emissive[1],
-                             e2 = s.emissive[2] * s.emissive[2];
-        const volatile float sn = e0 + (e1 + e2);
-        d.is_emissive = std::sqrt(static_cast<float>(sn)) > kEps ? 1u : 0u;
-        d.metallic = s.metallic;
-        d.roughness = s.roughness;
-        d.eta = s.eta;
-    }
-    // Emissive triangles of mesh instances in world space (instance then face order) and their area CDF,
-    // for next-event estimation.
-    std::vector<DevLight> light_recs;
-    std::vector<float> light_cdf;
-    for (uint32_t k = 0; k < num_instances; ++k) inst_recs[k].light_base = kInvalid;
-    for (uint32_t k = 0; k < num_instances; ++k) {
-        const spk_instance &in = instances[k];
-        if (in.type != SPK_PRIM_MESH || !mat_recs[in.material_id].is_emissive) continue;
-        const spk_mesh &m = meshes[in.mesh_id];
-        inst_recs[k].light_base = static_cast<uint32_t>(light_recs.size());
-        for (uint32_t f = 0; f < m.num_faces; ++f) {
-            f3 w[3];
-            for (int c = 0; c < 3; ++c) {
-                const float *p = m.positions + 3 * m.indices[3 * f + c];
-                w[c] = xform_point(in.transform, mk3(p[0], p[1], p[2]));
-            }
-            DevLight L{};
-            const f3 e1 = w[1] - w[0], e2 = w[2] - w[0];
-            const f3 cr = cross(e1, e2);
-            const float len = std::sqrt(sqnorm(cr));
-            const f3 ng = len > 0.f ? mk3(cr.x / len, cr.y / len, cr.z / len) : mk3(0.f, 0.f, 0.f);
-            const float vals[5][3] = {{w[0].x, w[0].y, w[0].z}, {e1.x, e1.y, e1.z}, {e2.x, e2.y, e2.z},
-                                      {ng.x, ng.y, ng.z},
-                                      {mat_recs[in.material_id].emissive[0], mat_recs[in.material_id].emissive[1],
-                                       mat_recs[in.material_id].emissive[2]}};
-            std::memcpy(L.p0, vals[0], 12);
-            std::memcpy(L.e1, vals[1], 12);
-            std::memcpy(L.e2, vals[2], 12);
-            std::memcpy(L.ng, vals[3], 12);
-            std::memcpy(L.emission, vals[4], 12);
-            L.area = 0.5f * len;
-            light_recs.push_back(L);
-        }
-    }
-    float light_total = 0.f;
-    for (const DevLight &L : light_recs) {
-        light_total = light_total + L.area;
-        light_cdf.push_back(light_total);
-    }
-    if (!(light_total > 0.f)) {
-        light_recs.clear();
-        light_cdf.clear();
-        for (uint32_t k = 0; k < num_instances; ++k) inst_recs[k].light_base = kInvalid;
-    }
-    std::vector<float4> cube;
-    if (sky && sky->mode == SPK_SKY_CUBE) {
-        const size_t n = 6ull * sky->cube_size * sky->cube_size;
-        cube.resize(n);
-        std::memcpy(cube.data(), sky->cube_rgba, n * sizeof(float4));
-    }
-    // Upload.
-    ctx->has_scene = false;
-    cudaError_t e;
-    static_assert(sizeof(WideNode) == 5 * sizeof(uint4), "node size");
-    if ((e = upload(ctx->nodes, reinterpret_cast<const uint4 *>(all_nodes.data()), all_nodes.size() * 5,
-                    ctx->stream)) != cudaSuccess ||
-        (e = upload(ctx->tris, tri_recs.data(), tri_recs.size(), ctx->stream)) != cudaSuccess ||
-        (e = upload(ctx->tlas_items, tlas_items.data(), tlas_items.size(), ctx->stream)) != cudaSuccess ||
-        (e = upload(ctx->instances, inst_recs.data(), inst_recs.size(), ctx->stream)) != cudaSuccess ||
-        (e = upload(ctx->verts, vert_recs.data(), vert_recs.size(), ctx->stream)) != cudaSuccess ||
-        (e = upload(ctx->faces, face_recs.data(), face_recs.size(), ctx->stream)) != cudaSuccess ||
-        (e = upload(ctx->materials, mat_recs.data(), mat_recs.size(), ctx->stream)) != cudaSuccess ||
-        (e = upload(ctx->sky, cube.data(), cube.size(), ctx->stream)) != cudaSuccess ||
-        (e = upload(ctx->lights, light_recs.data(), light_recs.size(), ctx->stream)) != cudaSuccess ||
-        (e = upload(ctx->light_cdf, light_cdf.data(), light_cdf.size(), ctx->stream)) != cudaSuccess) {
-        return cuda_fail(ctx, e, "scene upload");
-    }
-    DevScene &S = ctx->scene;
-    S.nodes = ctx->nodes.ptr;
-    S.tris = ctx->tris.ptr;
-    S.tlas_items = ctx->tlas_items.ptr;
-    S.instances = ctx->instances.ptr;
-    S.verts = ctx->verts.ptr;
-    S.faces = ctx->faces.ptr;
-    S.materials = ctx->materials.ptr;
-    S.sky_cube = ctx->sky.ptr;
-    S.tlas_root = tlas_root;
-    S.sky_mode = sky ? sky->mode : SPK_SKY_NONE;
-    S.sky_size = sky ? sky->cube_size : 0;
-    for (int c = 0; c < 3; ++c) S.sky_color[c] = sky ? sky->color[c] : 0.f;
-    S.scene_abs_x = abs_x;
-    S.lights = ctx->lights.ptr;
-    S.light_cdf = ctx->light_cdf.ptr;
-    S.num_lights = static_cast<uint32_t>(light_recs.size());
-    S.light_total = light_total;
-    ctx->bvh_nodes = static_cast<uint32_t>(all_nodes.size());
-    ctx->bvh_bytes = all_nodes.size() * sizeof(WideNode) + tri_recs.size() * sizeof(float4);
-    ctx->has_scene = true;
-    ctx->dirty = true;
-    return SPK_OK;
+    return upload_scene(ctx, all, descs);
 }
 
 spk_status spk_set_camera(spk_ctx *ctx, const spk_camera *camera) {
@@ -884,6 +998,106 @@ spk_status spk_read_guides(spk_ctx *ctx, float *normal_depth, float *albedo) {
     return SPK_OK;
 }
 
+spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t num_requests, uint32_t rng,
+                            uint32_t enable_nee) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, SPK_ERR_NOT_READY, "batch needs spk_set_scenes first");
+    if (!requests || num_requests == 0) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "no requests");
+    if (rng > SPK_RNG_XOSHIRO256SS) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "unknown rng %u", rng);
+    cudaSetDevice(ctx->device);
+    std::vector<DevRequest> reqs(num_requests);
+    unsigned long long items = 0, pixels = 0;
+    for (uint32_t r = 0; r < num_requests; ++r) {
+        const spk_request &q = requests[r];
+        if (q.scene >= ctx->scene.num_scenes)
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "request %u: scene %u of %u", r, q.scene, ctx->scene.num_scenes);
+        if (q.width < 2 || q.height < 2 || q.spp == 0 || q.bounce == 0)
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "request %u: needs width, height >= 2 and spp, bounce >= 1", r);
+        DevRequest &d = reqs[r];
+        std::memset(&d, 0, sizeof(d));
+        std::memcpy(&d.cam, &q.camera, sizeof(DevCamera));
+        d.scene = q.scene;
+        d.width = q.width;
+        d.height = q.height;
+        d.npix = q.width * q.height;
+        d.spp = q.spp;
+        d.bounce = q.bounce;
+        d.seed = q.seed;
+        d.item_base = items;
+        d.pixel_base = pixels;
+        items += static_cast<unsigned long long>(d.npix) * q.spp;
+        pixels += d.npix;
+    }
+    if (items >= 0xFFFFFFFFull)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "batch of %llu sample items: split it below 2^32", items);
+    const uint32_t slots = static_cast<uint32_t>(
+        std::min<unsigned long long>(items, ctx->tuning.batch_slots ? ctx->tuning.batch_slots : (1u << 21)));
+    cudaError_t e;
+    WavefrontState &s = ctx->wf_batch;
+    if (s.capacity < slots && (e = wavefront_alloc(s, slots)) != cudaSuccess) return cuda_fail(ctx, e, "batch slots");
+    if (s.sample_capacity < items) {
+        if (s.samples) cudaFree(s.samples);
+        s.samples = nullptr;
+        s.sample_capacity = 0;
+        if ((e = cudaMalloc(reinterpret_cast<void **>(&s.samples), items * sizeof(float4))) != cudaSuccess)
+            return cuda_fail(ctx, e, "batch sample buffer");
+        s.sample_capacity = items;
+    }
+    if ((e = upload(ctx->batch_reqs, reqs.data(), reqs.size(), ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "batch requests");
+    if (ctx->batch_hdr.count < pixels) {
+        ctx->batch_hdr.reset();
+        ctx->batch_img.reset();
+        if ((e = cudaMalloc(reinterpret_cast<void **>(&ctx->batch_hdr.ptr), pixels * sizeof(float4))) != cudaSuccess ||
+            (e = cudaMalloc(reinterpret_cast<void **>(&ctx->batch_img.ptr), pixels * sizeof(ushort4))) != cudaSuccess)
+            return cuda_fail(ctx, e, "batch outputs");
+        ctx->batch_hdr.count = ctx->batch_img.count = pixels;
+    }
+    BatchParams b{};
+    b.reqs = ctx->batch_reqs.ptr;
+    b.num_reqs = num_requests;
+    b.rng = rng;
+    b.enable_nee = enable_nee ? 1u : 0u;
+    b.total_items = items;
+    b.total_pixels = pixels;
+    b.out_hdr = ctx->batch_hdr.ptr;
+    b.out_image = ctx->batch_img.ptr;
+    const bool count = (ctx->instrumentation & SPK_INSTR_COUNT_TRAFFIC) != 0;
+    if ((e = prepare_events(ctx, 16)) != cudaSuccess) return cuda_fail(ctx, e, "event pool");
+    if ((e = cudaMemsetAsync(ctx->counters, 0, sizeof(Counters), ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "counter reset");
+    if ((e = cudaEventRecord(ctx->ev_start, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "event");
+    uint32_t launches = 0;
+    ctx->launch_events.capacity = 0;  // per-launch traversal timing is not recorded for batches
+    e = launch_render_batch(ctx->scene, b, count, ctx->counters, s, ctx->num_sms, ctx->stream, &launches, nullptr,
+                            wf_tuning(ctx));
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "batch wavefront");
+    if ((e = cudaEventRecord(ctx->ev_stop, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "event");
+    ctx->batch_host = reqs;
+    ctx->launches_in_call = launches;
+    ctx->last = spk_stats{};
+    ctx->last.paths = items;
+    ctx->stats_pending = true;
+    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
+    return SPK_OK;
+}
+
+spk_status spk_read_batch(spk_ctx *ctx, uint32_t index, float *hdr_rgba, uint16_t *rgba16f) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (index >= ctx->batch_host.size()) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "no request %u in the last batch", index);
+    cudaSetDevice(ctx->device);
+    const DevRequest &r = ctx->batch_host[index];
+    cudaError_t e;
+    if (hdr_rgba && (e = cudaMemcpyAsync(hdr_rgba, ctx->batch_hdr.ptr + r.pixel_base, r.npix * sizeof(float4),
+                                         cudaMemcpyDefault, ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "batch read");
+    if (rgba16f && (e = cudaMemcpyAsync(rgba16f, ctx->batch_img.ptr + r.pixel_base, r.npix * sizeof(ushort4),
+                                        cudaMemcpyDefault, ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "batch read");
+    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
+    return SPK_OK;
+}
+
 void spk_tuning_defaults(spk_tuning *out) {
     if (!out) return;
     *out = spk_tuning{};
@@ -904,7 +1118,7 @@ spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "bvh_leaf_size must be 1..3");
     if (t->extend_blocks_per_sm > 32 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 32)
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "blocks per SM out of range");
-    if (t->reserved[0] || t->reserved[1]) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "reserved fields must be 0");
+    if (t->reserved) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "reserved field must be 0");
     ctx->tuning = *t;
     return SPK_OK;
 }

@@ -156,11 +156,12 @@ struct Walker {
     float tmax_box, tmax_occl;
     TraceResult best;
 
-    __device__ __forceinline__ void init(const DevScene &S, f3 o, f3 d, float tmax) {
+    // `root` is the TLAS root node of the ray's scene (S.tlas_root for a single-scene context).
+    __device__ __forceinline__ void init(const DevScene &S, uint32_t root, f3 o, f3 d, float tmax) {
         wo = o;
         wd = d;
         setup_level(ray, o, d);
-        ngroup = make_uint2(S.tlas_root, S.tlas_root == kInvalid ? 0u : (1u << 24));
+        ngroup = make_uint2(root, root == kInvalid ? 0u : (1u << 24));
         tgroup = make_uint2(0u, 0u);
         sp = 0;
         blas_sp = 0;
@@ -330,7 +331,7 @@ __device__ __forceinline__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd
                                                  TraceCounts *counts = nullptr) {
     uint2 stack[kStackSize];
     Walker<kMode, kCount> w;
-    w.init(S, wo, wd, tmax_occl);
+    w.init(S, S.tlas_root, wo, wd, tmax_occl);
     while (!w.step(S, stack, err, counts)) {
     }
     return w.best;
@@ -338,7 +339,8 @@ __device__ __forceinline__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd
 
 // Persistent walk over a work list: each warp pulls batches of items from `cursor` and refills lanes whose
 // ray has finished once fewer than `kRefillLanes` lanes are still walking. `fetch(i, o, d)` loads item i's
-// ray; `finish(i, result)` stores its result. Every lane of every warp of the block must call this.
+// ray and returns the TLAS root of its scene; `finish(i, result)` stores its result. Every lane of every
+// warp of the block must call this.
 constexpr int kRefillLanes = SPK_REFILL_LANES;
 
 template <int kMode, bool kCount, class Fetch, class Finish>
@@ -364,8 +366,8 @@ __device__ __forceinline__ void walk_persistent(const DevScene &S, unsigned long
                 if (q < n) {
                     item = q;
                     f3 o, d;
-                    fetch(q, o, d);
-                    w.init(S, o, d, tmax);
+                    const uint32_t root = fetch(q, o, d);
+                    w.init(S, root, o, d, tmax);
                     active = true;
                 }
             }

@@ -163,8 +163,9 @@ __global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers
     if (pid == 0) counters->queue_counters[kLen0] = static_cast<unsigned long long>(fb.width) * fb.height;
 }
 
-// Extend: persistent warps pull paths from the queue, refilling lanes whose walk has finished.
-template <bool kCount>
+// Extend: persistent warps pull paths from the queue, refilling lanes whose walk has finished. With
+// kBatch each path traces in its own scene (the TLAS root its slot recorded at start).
+template <bool kCount, bool kBatch = false>
 __global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_wf_extend(DevScene S, WavefrontState s, int in_queue,
                                                       Counters *counters) {
     uint32_t err = 0, done = 0;
@@ -179,6 +180,7 @@ __global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_wf_extend(DevScene
             const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
             o = mk3(o4.x, o4.y, o4.z);
             d = mk3(d4.x, d4.y, d4.z);
+            return kBatch ? s.slot_root[pid] : S.tlas_root;
         },
         [&](unsigned long long, const TraceResult &h) {
             s.hit[pid] = make_float4(h.t, h.u, h.v, __uint_as_float(h.inst));
@@ -405,6 +407,134 @@ __global__ void __launch_bounds__(256) k_mf_resolve(FrameBuffers fb, WavefrontSt
     fb.out[static_cast<size_t>(fb.height - 1 - j) * fb.width + i] = o;
 }
 
+// ------------------------------------------------------------------------------------------------
+// Batched requests: one wavefront over the sample items of every request (spk_render_batch)
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t find_request(const BatchParams &b, unsigned long long item) {
+    uint32_t lo = 0, hi = b.num_reqs;  // last request with item_base <= item
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (b.reqs[mid].item_base <= item) {
+            lo = mid;
+        } else {
+            hi = mid;
+        }
+    }
+    return lo;
+}
+
+// Slot `slot` starts global item `item`: request r, frame k, pixel; the same seed, jitter and camera ray
+// as frame k of spk_render on that request alone (frame seed base k: one sample per frame).
+template <int kKind>
+__device__ __forceinline__ void start_item_batch(const DevScene &S, const BatchParams &b, const WavefrontState &s,
+                                                 uint32_t slot, unsigned long long item) {
+    const uint32_t r = find_request(b, item);
+    const DevRequest &R = b.reqs[r];
+    const unsigned long long local = item - R.item_base;
+    const uint32_t k = static_cast<uint32_t>(local / R.npix);
+    const uint32_t pix = static_cast<uint32_t>(local - static_cast<unsigned long long>(k) * R.npix);
+    RenderParams p{k, R.bounce, b.rng, R.seed, 0u, b.enable_nee};
+    start_path<kKind>(R.cam, p, s, slot, pix % R.width, pix / R.width, R.width, R.height, k);
+    s.slot_item[slot] = static_cast<uint32_t>(item);
+    s.slot_state[slot] = 0u;
+    s.slot_req[slot] = r;
+    s.slot_root[slot] = S.descs[R.scene].tlas_root;
+}
+
+template <int kKind>
+__global__ void __launch_bounds__(128) k_b_generate(DevScene S, BatchParams b, WavefrontState s, uint32_t first,
+                                                    Counters *counters) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= first) return;
+    start_item_batch<kKind>(S, b, s, slot, slot);
+    s.queue[0][slot] = slot;
+    if (slot == 0) {
+        counters->queue_counters[kLen0] = first;
+        counters->queue_counters[kNextItem] = first;
+    }
+}
+
+template <int kKind, bool kNee>
+__global__ void __launch_bounds__(128) k_b_shade(DevScene S, BatchParams b, WavefrontState s, int in_queue,
+                                                 Counters *counters) {
+    uint32_t shadow = 0, err = 0;
+    const unsigned long long n = counters->queue_counters[in_queue];
+    const int out_queue = in_queue ^ 1;
+    const uint32_t *queue = s.queue[in_queue];
+    const uint32_t lane = threadIdx.x & 31u;
+    for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
+         q0 += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+        const unsigned long long q = q0 + threadIdx.x;
+        bool push = false, need = false;
+        uint32_t slot = 0;
+        if (q < n) {
+            slot = queue[q];
+            const DevRequest &R = b.reqs[s.slot_req[slot]];
+            const DevScene Sv = scene_view(S, S.descs[R.scene]);
+            const uint32_t bounce = s.slot_state[slot];
+            const bool alive =
+                shade_path<kKind, kNee>(Sv, s, slot, bounce, nullptr, shadow, err) && bounce + 1 < R.bounce;
+            if (alive) {
+                s.slot_state[slot] = bounce + 1u;
+                push = true;
+            } else {
+                const float4 c = s.color[slot];
+                s.samples[s.slot_item[slot]] = make_float4(clamp_sample(c.x), clamp_sample(c.y), clamp_sample(c.z), c.w);
+                need = true;
+            }
+        }
+        const uint32_t need_mask = __ballot_sync(0xFFFFFFFFu, need);
+        if (need_mask) {
+            unsigned long long base = 0;
+            if (lane == static_cast<uint32_t>(__ffs(need_mask) - 1))
+                base = atomicAdd(&counters->queue_counters[kNextItem], static_cast<unsigned long long>(__popc(need_mask)));
+            base = __shfl_sync(0xFFFFFFFFu, base, __ffs(need_mask) - 1);
+            if (need) {
+                const unsigned long long item = base + __popc(need_mask & ((1u << lane) - 1u));
+                if (item < b.total_items) {
+                    start_item_batch<kKind>(S, b, s, slot, item);
+                    push = true;
+                }
+            }
+        }
+        queue_push(s.queue[out_queue], &counters->queue_counters[out_queue], slot, push);
+    }
+    warp_add_u64(&counters->shadow_rays, shadow);
+    if (err) atomicOr(&counters->error_flags, err);
+}
+
+// Per pixel of every request: fold its samples in frame order with DenoisePass's weights from a cleared
+// frame buffer (frame k: cumulated k, weight k / (k + 1), CPURenderer.cpp:530-543), then tonemap.
+__global__ void __launch_bounds__(256) k_b_resolve(BatchParams b, WavefrontState s) {
+    const unsigned long long g = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (g >= b.total_pixels) return;
+    uint32_t lo = 0, hi = b.num_reqs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (b.reqs[mid].pixel_base <= g) {
+            lo = mid;
+        } else {
+            hi = mid;
+        }
+    }
+    const DevRequest &R = b.reqs[lo];
+    const uint32_t pix = static_cast<uint32_t>(g - R.pixel_base);
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (uint32_t k = 0; k < R.spp; ++k) {
+        const float4 n = s.samples[R.item_base + static_cast<unsigned long long>(k) * R.npix + pix];
+        const float f = static_cast<float>(k) / static_cast<float>(k + 1u);
+        a = make_float4(n.x + (a.x - n.x) * f, n.y + (a.y - n.y) * f, n.z + (a.z - n.z) * f, n.w + (a.w - n.w) * f);
+    }
+    b.out_hdr[g] = a;
+    const uint32_t i = pix % R.width, j = pix / R.width;
+    ushort4 o;
+    o.x = __half_as_ushort(__float2half_rn(aces_tonemap(a.x, R.cam.exposure)));
+    o.y = __half_as_ushort(__float2half_rn(aces_tonemap(a.y, R.cam.exposure)));
+    o.z = __half_as_ushort(__float2half_rn(aces_tonemap(a.z, R.cam.exposure)));
+    o.w = __half_as_ushort(__float2half_rn(1.f));
+    b.out_image[R.pixel_base + static_cast<unsigned long long>(R.height - 1 - j) * R.width + i] = o;
+}
+
 template <class T>
 cudaError_t dmalloc(T *&p, size_t count) {
     return cudaMalloc(reinterpret_cast<void **>(&p), count * sizeof(T));
@@ -423,16 +553,14 @@ unsigned extend_blocks(int num_sms, uint32_t per_sm_override) {
 }
 
 cudaError_t launch_extend(const DevScene &scene, WavefrontState &s, int in, bool count, Counters *counters,
-                          unsigned grid, cudaStream_t stream, LaunchEvents *ev) {
+                          unsigned grid, cudaStream_t stream, LaunchEvents *ev, bool batch = false) {
     unsigned long long *qc = counters->queue_counters;
     cudaError_t e = cudaMemsetAsync(qc + kCursor, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     if (ev) ev->before(stream);
-    if (count) {
-        k_wf_extend<true><<<grid, 128, 0, stream>>>(scene, s, in, counters);
-    } else {
-        k_wf_extend<false><<<grid, 128, 0, stream>>>(scene, s, in, counters);
-    }
+    auto *kern = batch ? (count ? k_wf_extend<true, true> : k_wf_extend<false, true>)
+                       : (count ? k_wf_extend<true, false> : k_wf_extend<false, false>);
+    kern<<<grid, 128, 0, stream>>>(scene, s, in, counters);
     if (ev) ev->after(stream);
     return cudaSuccess;
 }
@@ -450,6 +578,7 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
         (e = dmalloc(s.sort_keys, capacity)) != cudaSuccess || (e = dmalloc(s.slot_state, capacity)) != cudaSuccess ||
         (e = dmalloc(s.slot_item, capacity)) != cudaSuccess || (e = dmalloc(s.prev_pdf, capacity)) != cudaSuccess ||
         (e = dmalloc(s.sort_hist, 2 * kSortBuckets)) != cudaSuccess ||
+        (e = dmalloc(s.slot_req, capacity)) != cudaSuccess || (e = dmalloc(s.slot_root, capacity)) != cudaSuccess ||
         (e = cudaMemset(s.sort_hist, 0, 2 * kSortBuckets * sizeof(uint32_t))) != cudaSuccess ||
         (e = cudaHostAlloc(reinterpret_cast<void **>(&s.host_len), sizeof(unsigned long long), cudaHostAllocDefault)) !=
             cudaSuccess) {
@@ -463,7 +592,8 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
 void wavefront_free(WavefrontState &s) {
     void *ptrs[] = {s.ray_o,      s.ray_d,     s.thr,     s.color,        s.rng,        s.hit,
                     s.hit_face,   s.queue[0],  s.queue[1], s.sort_keys,   s.slot_state, s.slot_item,
-                    s.samples,    s.frame_weight, s.frame_seed, s.prev_pdf, s.sort_hist};
+                    s.samples,    s.frame_weight, s.frame_seed, s.prev_pdf, s.sort_hist, s.slot_req,
+                    s.slot_root};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s.host_len) cudaFreeHost(s.host_len);
@@ -701,6 +831,56 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
         k_mf_resolve<<<(npix + 255) / 256, 256, 0, stream>>>(fbuf, s, f0, frames, cam.exposure);
         ++nl;
     }
+    if (launches) *launches = nl;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, bool count, Counters *counters,
+                                WavefrontState &s, int num_sms, cudaStream_t stream, uint32_t *launches,
+                                LaunchEvents *ev, const WfTuning &tuning) {
+    if (b.num_reqs == 0 || b.total_items == 0 || s.capacity == 0 || s.sample_capacity < b.total_items)
+        return cudaErrorInvalidValue;
+    uint32_t nl = 0;
+    cudaError_t e;
+    unsigned long long *qc = counters->queue_counters;
+    const unsigned shade_blocks = static_cast<unsigned>(num_sms) * tuning.shade_blocks_per_sm;
+    const unsigned extend_grid = extend_blocks(num_sms, tuning.extend_blocks_per_sm);
+    const uint32_t first = static_cast<uint32_t>(std::min<unsigned long long>(s.capacity, b.total_items));
+    if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
+    if (b.rng == 0) {
+        k_b_generate<0><<<(first + 127) / 128, 128, 0, stream>>>(scene, b, s, first, counters);
+    } else {
+        k_b_generate<1><<<(first + 127) / 128, 128, 0, stream>>>(scene, b, s, first, counters);
+    }
+    ++nl;
+    constexpr uint32_t kChunk = kChunkIterations;
+    // A slot finishes an item within its request's bounce limit and no item starts twice, so
+    // total_items * 64 iterations (bounce < 64 in practice) is a loose guard against a runaway loop.
+    const unsigned long long max_iters = b.total_items * 64ull + kChunk;
+    unsigned long long iter = 0;
+    auto *shade = b.rng == 0 ? (b.enable_nee ? k_b_shade<0, true> : k_b_shade<0, false>)
+                             : (b.enable_nee ? k_b_shade<1, true> : k_b_shade<1, false>);
+    for (;;) {
+        for (uint32_t c = 0; c < kChunk; ++c) {
+            const int in = static_cast<int>(c & 1u), out = in ^ 1;
+            if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
+            if ((e = launch_extend(scene, s, in, count, counters, extend_grid, stream, ev, true)) != cudaSuccess)
+                return e;
+            shade<<<shade_blocks, 128, 0, stream>>>(scene, b, s, in, counters);
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        iter += kChunk;
+        nl += 2 * kChunk;
+        if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
+            cudaSuccess)
+            return e;
+        if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
+        if (*s.host_len == 0) break;
+        if (iter > max_iters) return cudaErrorLaunchFailure;
+    }
+    const unsigned blocks = static_cast<unsigned>((b.total_pixels + 255) / 256);
+    k_b_resolve<<<blocks, 256, 0, stream>>>(b, s);
+    ++nl;
     if (launches) *launches = nl;
     return cudaGetLastError();
 }

@@ -29,6 +29,8 @@ struct WavefrontState {
     float *prev_pdf = nullptr;                // NEE: cosine pdf of the continuation after a light-sampling vertex
     uint32_t *slot_state = nullptr;           // multi-frame mode: bounce of the slot's path
     uint32_t *slot_item = nullptr;            // multi-frame mode: sample item (frame * pixels + pixel) of the slot
+    uint32_t *slot_req = nullptr;             // batch mode: request of the slot's path
+    uint32_t *slot_root = nullptr;            // batch mode: TLAS root of the slot's scene
     float4 *samples = nullptr;                // multi-frame mode: clamped result of each (frame, pixel) sample
     size_t sample_capacity = 0;               // float4 entries of `samples`
     // multi-frame mode: per-frame constants, frame k of the call
@@ -80,6 +82,31 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                                      const uint32_t *seeds, bool count, Counters *counters, WavefrontState &s,
                                      int num_sms, cudaStream_t stream, uint32_t *launches, LaunchEvents *ev,
                                      const WfTuning &tuning, ChunkGraph *graph);
+
+// One request of a batch (spk_request) as the batch kernels read it.
+struct DevRequest {
+    DevCamera cam;
+    uint32_t scene, width, height, npix;
+    uint32_t spp, bounce, seed, pad;
+    unsigned long long item_base;   // first global sample item: items of request r are frame-major
+    unsigned long long pixel_base;  // first pixel of the request in the batch output images
+};
+
+struct BatchParams {
+    const DevRequest *reqs;
+    uint32_t num_reqs;
+    uint32_t rng, enable_nee;
+    unsigned long long total_items;
+    unsigned long long total_pixels;
+    float4 *out_hdr;     // accumulated frame buffers of all requests, request after request
+    ushort4 *out_image;  // tonemapped images (top row first per request)
+};
+
+// All sample items of a batch in one regenerating wavefront over `s` (capacity = path slots), then the
+// ordered per-pixel resolve and tonemap into the batch outputs. `s.samples` must hold total_items entries.
+cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, bool count, Counters *counters,
+                                WavefrontState &s, int num_sms, cudaStream_t stream, uint32_t *launches,
+                                LaunchEvents *ev, const WfTuning &tuning);
 
 // Step of the last launch_render_multiframe call on this thread that returned an error (for messages).
 const char *wavefront_error_site();

@@ -10,7 +10,8 @@ import os
 import numpy as np
 
 from . import build as _build
-from .abi import (HIT_DTYPE, MarshalledScene, Scene, spk_camera, spk_config, spk_stats, spk_tuning)
+from .abi import (HIT_DTYPE, MarshalledScene, Scene, spk_camera, spk_config, spk_request, spk_scene_desc, spk_stats,
+                  spk_tuning)
 
 _lib = None
 
@@ -23,7 +24,7 @@ EXPORTED = ["spk_abi_version", "spk_create", "spk_destroy", "spk_last_error", "s
             "spk_framebuffer_device", "spk_sample_counts", "spk_is_converged", "spk_trace", "spk_trace_device",
             "spk_synchronize", "spk_get_stats", "spk_set_instrumentation", "spk_render_noalloc",
             "spk_tuning_defaults", "spk_set_tuning", "spk_get_tuning", "spk_render_guides", "spk_guides_device",
-            "spk_read_guides",
+            "spk_read_guides", "spk_set_scenes", "spk_render_batch", "spk_read_batch",
             # include/spk_denoise.h
             "spk_dn_create", "spk_dn_destroy", "spk_dn_last_error", "spk_dn_init", "spk_dn_num_params",
             "spk_dn_get_params", "spk_dn_set_params", "spk_dn_pack_features", "spk_dn_pack_halves", "spk_dn_train_step",
@@ -77,6 +78,9 @@ def lib(build: bool = True):
         L.spk_tuning_defaults.restype = None
         L.spk_set_tuning.argtypes = [vp, vp]
         L.spk_get_tuning.argtypes = [vp, vp]
+        L.spk_set_scenes.argtypes = [vp, vp, u32]
+        L.spk_render_batch.argtypes = [vp, vp, u32, u32, u32]
+        L.spk_read_batch.argtypes = [vp, u32, vp, vp]
         L.spk_render_guides.argtypes = [vp]
         L.spk_guides_device.argtypes = [vp, C.POINTER(vp), C.POINTER(vp)]
         L.spk_read_guides.argtypes = [vp, vp, vp]
@@ -140,6 +144,34 @@ class Context:
         self._check(self.L.spk_set_scene(self.h, C.cast(a[0], C.c_void_p), a[1], C.cast(a[2], C.c_void_p), a[3],
                                          C.cast(a[4], C.c_void_p), a[5], C.cast(a[6], C.c_void_p)))
         self._scene = m
+
+    def set_scenes(self, scenes):
+        """Several resident scenes (spk_set_scenes) for render_batch; scene 0 is what render() sees."""
+        ms = [MarshalledScene(sc) for sc in scenes]
+        descs = (spk_scene_desc * len(ms))()
+        for k, m in enumerate(ms):
+            a = m.args()
+            descs[k] = spk_scene_desc(C.cast(a[0], C.c_void_p), a[1], C.cast(a[2], C.c_void_p), a[3],
+                                      C.cast(a[4], C.c_void_p), a[5], C.cast(a[6], C.c_void_p))
+        self._check(self.L.spk_set_scenes(self.h, descs, len(ms)))
+        self._scene = ms
+
+    def render_batch(self, requests, rng: int = 1, enable_nee: bool = False):
+        """requests: list of dicts with scene, width, height, spp, bounce, seed, camera (spk_camera)."""
+        arr = (spk_request * len(requests))()
+        for k, r in enumerate(requests):
+            arr[k] = spk_request(r["scene"], r["width"], r["height"], r["spp"], r["bounce"], r.get("seed", 0),
+                                 r["camera"])
+        self._check(self.L.spk_render_batch(self.h, arr, len(requests), rng, 1 if enable_nee else 0))
+        self._batch = [(r["width"], r["height"]) for r in requests]
+
+    def read_batch(self, index: int):
+        """(hdr (H, W, 4) float32 bottom row first, rgba16f (H, W, 4) uint16 top row first) of request `index`."""
+        w, h = self._batch[index]
+        hdr = np.zeros((h, w, 4), np.float32)
+        out = np.zeros((h, w, 4), np.uint16)
+        self._check(self.L.spk_read_batch(self.h, index, _p(hdr), _p(out)))
+        return hdr, out
 
     def set_camera(self, camera: spk_camera):
         self._check(self.L.spk_set_camera(self.h, C.byref(camera)))

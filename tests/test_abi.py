@@ -16,7 +16,7 @@ HEADER = os.path.join(ROOT, "include", "spk.h")
 HEADERS = [HEADER, os.path.join(ROOT, "include", "spk_denoise.h")]
 
 STRUCTS = ["spk_mesh", "spk_instance", "spk_material", "spk_sky", "spk_camera", "spk_config", "spk_ray", "spk_hit",
-           "spk_stats", "spk_tuning"]
+           "spk_stats", "spk_tuning", "spk_scene_desc", "spk_request"]
 
 
 def header_functions():
@@ -86,5 +86,5 @@ def test_tuning_defaults():
     t = abi.spk_tuning()
     native.lib().spk_tuning_defaults(C.byref(t))
     assert (t.cuda_graph, t.material_sort, t.bvh_width, t.bvh_leaf_size, t.extend_blocks_per_sm,
-            t.shade_blocks_per_sm, list(t.reserved)) == (1, 0, 8, 3, 0, 8, [0, 0])
+            t.shade_blocks_per_sm, t.batch_slots, t.reserved) == (1, 0, 8, 3, 0, 8, 0, 0)
     assert native.lib().spk_set_tuning(None, C.byref(t)) == 1
