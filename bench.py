@@ -12,7 +12,8 @@ build here) on this machine's host cores over a bounded sample of the same workl
 
 The line also carries `denoise`: the wall time to relMSE 0.01 / 0.003 at 1920x1080 on the same scene for
 denoised low-spp rendering (the committed U-Net) vs plain path tracing, against a 4096-spp reference
-(`--no-denoise` skips it).
+(`--no-denoise` skips it); and `batch`: 32 uneven render requests over 3 scenes in one batched wavefront
+against the same requests rendered one by one (`--no-batch` skips it, `--batch-autotune` adds a tuned run).
 """
 from __future__ import annotations
 
@@ -318,8 +319,59 @@ def run_ours(args):
         line["cpu_baseline"] = cpu
     if world == 1 and not args.no_denoise:
         line["denoise"] = denoise_metric(ctx)
+    if world == 1 and not args.no_batch:
+        line["batch"] = batch_metric(args.batch_autotune)
     print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def batch_metric(autotune: bool = False):
+    """Batched workload: 32 requests over 3 scenes (about 10k, 200k and 2.1M triangles), pixel counts
+    log-uniform in [128^2, 1920x1080], spp in {1, 4, 16, 64}, depth 8 with roulette, xoshiro256**. The
+    batch (spk_render_batch, one regenerating wavefront) against the same requests rendered one after
+    another (spk_render per request on per-scene contexts); both by device time (CUDA events)."""
+    from sparkle_gb300 import abi, autotune as at, native, scenes
+    sc = scenes.batch_scenes()
+    reqs = scenes.batch_requests([c for _, c in sc])
+    ctx = native.Context(0)
+    ctx.set_scenes([s for s, _ in sc])
+
+    def run_batch(c):
+        c.render_batch(reqs, rng=abi.SPK_RNG_XOSHIRO256SS, enable_nee=False)
+        return c.stats()
+
+    run_batch(ctx)  # warm-up (allocations)
+    best = at.measure(ctx, run_batch, repeats=2)
+    out = {"requests": len(reqs), "scene_triangles": [s.num_triangles for s, _ in sc],
+           "sample_items": int(sum(r["width"] * r["height"] * r["spp"] for r in reqs)),
+           "batched": {"mrays_s": round(best[0] / (best[1] * 1e3), 1), "device_ms": round(best[1], 2),
+                       "rays": int(best[0])}}
+    if autotune:
+        knobs, hist = at.autotune(ctx, run_batch, rebuild=lambda: ctx.set_scenes([s for s, _ in sc]), log=None)
+        tuned = at.measure(ctx, run_batch, repeats=2)
+        out["autotuned"] = {"knobs": knobs, "mrays_s": round(tuned[0] / (tuned[1] * 1e3), 1),
+                            "evaluations": len(hist)}
+    ctx.close()
+    singles = []
+    for s, _ in sc:
+        c = native.Context(0)
+        c.set_scene(s)
+        singles.append(c)
+    rays = ms = 0.0
+    for r in reqs:
+        c = singles[r["scene"]]
+        c.set_config(abi.make_config(r["width"], r["height"], spp=1, max_spp=4096, bounce=r["bounce"],
+                                     rng=abi.SPK_RNG_XOSHIRO256SS, seed=r["seed"], kernel=abi.SPK_KERNEL_WAVEFRONT))
+        c.set_camera(r["camera"])
+        c.render(r["spp"])
+        st = c.stats()
+        rays += st["extension_rays"] + st["shadow_rays"]
+        ms += st["device_ms"]
+    for c in singles:
+        c.close()
+    out["sequential"] = {"mrays_s": round(rays / (ms * 1e3), 1), "device_ms": round(ms, 2), "rays": int(rays)}
+    out["speedup"] = round(out["batched"]["mrays_s"] / out["sequential"]["mrays_s"], 3)
+    return out
 
 
 def denoise_metric(ctx):
@@ -410,6 +462,8 @@ def main():
     ap.add_argument("--kernel", type=int, default=0, help="0 auto, 1 megakernel, 2 wavefront")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-denoise", action="store_true", help="skip the denoised-vs-plain time-to-relMSE leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-requests leg")
+    ap.add_argument("--batch-autotune", action="store_true", help="autotune the batched leg's launch knobs")
     ap.add_argument("--tune", default="", help="spk_tuning knobs, e.g. cuda_graph=0,material_sort=1,bvh_width=4")
     ap.add_argument("--profile-small", action="store_true",
                     help="ncu capture case: the bench workload cut to 2 frames, no timing output")

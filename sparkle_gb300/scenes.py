@@ -314,3 +314,30 @@ def random_training_scene(seed: int, sphere_level: int = 3, grid: int = 48):
                world_up=(0, 0, 1), vfov_rad=float(np.deg2rad(rng.uniform(35, 65))), focus_distance=10.0,
                aperture_radius=0.035 / 22.0 / 2.0, exposure=1.0)
     return scene, cam
+
+
+def batch_scenes():
+    """The three scenes of the batched workload, about 10k, 200k and 2.1M triangles, built like the stress
+    scene (fBm heightfield + icospheres, Lambertian / GGX metal / glass, sun-and-sky cube)."""
+    small = terrain_spheres(seed=11, grid=56, num_spheres=4, sphere_level=3, size=30.0, cube_size=32)
+    mid = terrain_spheres(seed=12, grid=300, num_spheres=16, sphere_level=3, size=60.0, cube_size=32)
+    big = terrain_spheres(seed=13, grid=1024, num_spheres=8, sphere_level=2, size=100.0, cube_size=64)
+    return [small, mid, big]
+
+
+def batch_requests(scene_cams, num: int = 32, seed: int = 0):
+    """`num` render requests: scene uniform, pixel count log-uniform in [128^2, 1920 x 1080] with an aspect
+    ratio in [1, 16/9], spp uniform in {1, 4, 16, 64}, depth 8 (Russian roulette after depth 3)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    lo, hi = np.log(128 * 128), np.log(1920 * 1080)
+    for k in range(num):
+        scene = int(rng.integers(0, len(scene_cams)))
+        npix = float(np.exp(rng.uniform(lo, hi)))
+        aspect = float(rng.uniform(1.0, 16.0 / 9.0))
+        w = max(2, min(1920, int(round(np.sqrt(npix * aspect)))))
+        h = max(2, min(1080, int(round(npix / w))))
+        spp = int(rng.choice([1, 4, 16, 64]))
+        out.append(dict(scene=scene, width=w, height=h, spp=spp, bounce=8, seed=k,
+                        camera=make_camera(scene_cams[scene], w, h)))
+    return out
