@@ -79,6 +79,8 @@ struct DevScene {
     float scene_abs_x;  // max |x| over world bounds; bounds the x-only world-t error used for pruning
     const DevSceneDesc *descs;  // every scene of the context (the fields above are scene 0's)
     uint32_t num_scenes;
+    float box_lo[3];     // world bounds of all scenes (ray sort cells)
+    float box_scale[3];  // 8 / extent per axis (0 for a flat axis)
 };
 
 // The DevScene of scene `k` of a multi-scene context: scene 0's record with the TLAS root, sky and light

@@ -215,6 +215,10 @@ struct HostScene {
     uint32_t sky_mode = SPK_SKY_NONE, sky_size = 0;
     float sky_color[3] = {0.f, 0.f, 0.f};
     float abs_x = 0.f, light_total = 0.f;
+    float lo[3] = {std::numeric_limits<float>::max(), std::numeric_limits<float>::max(),
+                   std::numeric_limits<float>::max()};
+    float hi[3] = {-std::numeric_limits<float>::max(), -std::numeric_limits<float>::max(),
+                   -std::numeric_limits<float>::max()};
 };
 
 // Validates one scene description and builds its host-side records (BLAS per mesh, TLAS, vertex/face
@@ -344,6 +348,10 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
             }
         }
         abs_x = std::max(abs_x, std::max(std::fabs(inst_boxes[k].lo[0]), std::fabs(inst_boxes[k].hi[0])));
+        for (int a = 0; a < 3; ++a) {
+            hs.lo[a] = std::min(hs.lo[a], inst_boxes[k].lo[a]);
+            hs.hi[a] = std::max(hs.hi[a], inst_boxes[k].hi[a]);
+        }
     }
     if (num_instances > 0) {
         const Bvh2 b2 = build_bvh2(inst_boxes, ctx->tuning.bvh_leaf_size, threads);
@@ -467,6 +475,10 @@ void append_scene(HostScene &all, const HostScene &s, DevSceneDesc &d) {
     all.lights.insert(all.lights.end(), s.lights.begin(), s.lights.end());
     all.light_cdf.insert(all.light_cdf.end(), s.light_cdf.begin(), s.light_cdf.end());
     all.abs_x = std::max(all.abs_x, s.abs_x);
+    for (int a = 0; a < 3; ++a) {
+        all.lo[a] = std::min(all.lo[a], s.lo[a]);
+        all.hi[a] = std::max(all.hi[a], s.hi[a]);
+    }
 }
 
 // Uploads concatenated scene records and points the context's DevScene at them (scene 0 by default).
@@ -502,6 +514,11 @@ spk_status upload_scene(spk_ctx *ctx, const HostScene &hs, const std::vector<Dev
     S.light_cdf = ctx->light_cdf.ptr;
     S.descs = ctx->scene_descs.ptr;
     S.num_scenes = static_cast<uint32_t>(descs.size());
+    for (int a = 0; a < 3; ++a) {
+        const bool ok = hs.hi[a] > hs.lo[a];
+        S.box_lo[a] = ok ? hs.lo[a] : 0.f;
+        S.box_scale[a] = ok ? 8.f / (hs.hi[a] - hs.lo[a]) : 0.f;
+    }
     const DevScene v = scene_view(S, descs[0]);
     S.tlas_root = v.tlas_root;
     S.sky_mode = v.sky_mode;
@@ -711,6 +728,7 @@ static WfTuning wf_tuning(const spk_ctx *ctx) {
     t.extend_blocks_per_sm = ctx->tuning.extend_blocks_per_sm;
     t.shade_blocks_per_sm = ctx->tuning.shade_blocks_per_sm;
     t.material_sort = ctx->tuning.material_sort != 0;
+    t.ray_sort = ctx->tuning.ray_sort != 0;
     return t;
 }
 
@@ -1118,7 +1136,7 @@ spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "bvh_leaf_size must be 1..3");
     if (t->extend_blocks_per_sm > 32 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 32)
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "blocks per SM out of range");
-    if (t->reserved) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "reserved field must be 0");
+    if (t->ray_sort > 1) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "ray_sort takes 0 or 1");
     ctx->tuning = *t;
     return SPK_OK;
 }

@@ -42,6 +42,12 @@ enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOve
 #ifndef SPK_POSTPONE_INNER
 #define SPK_POSTPONE_INNER 0  // 1: also postpone inside the triangle loop as lanes drop out of it
 #endif
+#ifndef SPK_MINMAX3
+#define SPK_MINMAX3 0  // 1: slab entry/exit with three-input min/max (exact, same results)
+#endif
+#ifndef SPK_MT_RCP
+#define SPK_MT_RCP 0  // 1: Moller-Trumbore's 1/det as a correctly rounded reciprocal (same bits as 1.f/det)
+#endif
 #ifndef SPK_WALK_MIN_BLOCKS
 #define SPK_WALK_MIN_BLOCKS 8  // resident 128-thread blocks per SM the walking kernels are compiled for
 #endif
@@ -100,6 +106,19 @@ __device__ __forceinline__ float prune_limit(float best, f3 wo, f3 wd, float sce
 
 // Slab test of the 8 children of one wide node; returns the next node group (inner children, permuted
 // slot bits 24..31 + imask in bits 0..7) and triangle group (leaf items, bits 0..23).
+// Three-input max / min (PTX max.f32 / min.f32 with three operands): the same value as the two-input
+// forms applied in turn, NaN operands ignored.
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint32_t idx, const LevelRay &r,
                                            float tmax, uint2 &ngroup, uint2 &tgroup) {
     const uint4 *np = nodes + static_cast<size_t>(idx) * 5;
@@ -129,8 +148,13 @@ __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint
             const float tfx = fmaf(byte_to_float(fx, c), ax, ox);
             const float tfy = fmaf(byte_to_float(fy, c), ay, oy);
             const float tfz = fmaf(byte_to_float(fz, c), az, oz);
+#if SPK_MINMAX3
+            const float t0 = max3f(tnx, tny, fmaxf(tnz, 0.f));
+            const float t1 = min3f(tfx, tfy, fminf(tfz, tmax));
+#else
             const float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.f));
             const float t1 = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+#endif
             if (m != 0u && t0 <= t1) {
                 uint32_t bit = m & 0x1Fu;
                 if ((m & 0x18u) == 0x18u) bit ^= r.oct;
@@ -236,7 +260,11 @@ struct Walker {
                 const float det = dot3(e1, h);
                 if (fabsf(det) < kEps) continue;
                 const f3 s = ray.o - p0;
+#if SPK_MT_RCP
+                const float f = __frcp_rn(det);
+#else
                 const float f = 1.f / det;
+#endif
                 const float u = f * dot3(s, h);
                 if (u < 0.f || u > 1.f) continue;
                 const f3 q = cross(s, e1);

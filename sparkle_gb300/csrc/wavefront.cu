@@ -308,8 +308,7 @@ __global__ void __launch_bounds__(128) k_mf_shade(DevScene S, DevCamera cam, Fra
 }
 
 // ------------------------------------------------------------------------------------------------
-// Material sort: group a shade queue by the material class of each path's hit (counting sort), so the
-// warps of the shade stage run one BSDF branch and read one material record.
+// Counting sorts of a queue (material class before shading, ray key before extension)
 // ------------------------------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t sort_class(const DevScene &S, const WavefrontState &s, uint32_t pid) {
     const uint32_t inst = __float_as_uint(s.hit[pid].w);
@@ -317,33 +316,93 @@ __device__ __forceinline__ uint32_t sort_class(const DevScene &S, const Wavefron
     return min(S.instances[inst].material, kSortBuckets - 2);
 }
 
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // bits b2 b1 b0 -> b2 0 0 b1 0 0 b0
+    return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4);
+}
+
+__device__ __forceinline__ uint32_t ray_key(const DevScene &S, const WavefrontState &s, uint32_t pid) {
+    const float4 o = s.ray_o[pid], d = s.ray_d[pid];
+    uint32_t c[3];
+    const float ov[3] = {o.x, o.y, o.z};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float f = (ov[a] - S.box_lo[a]) * S.box_scale[a];
+        c[a] = f > 0.f ? min(static_cast<uint32_t>(f), 7u) : 0u;
+    }
+    const uint32_t oct = (d.x < 0.f ? 1u : 0u) | (d.y < 0.f ? 2u : 0u) | (d.z < 0.f ? 4u : 0u);
+    return ((spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2)) << 3) | oct;
+}
+
+template <int kKey>  // 0: material class of the hit, 1: ray (origin cell, direction octant)
+struct SortKey {
+    static constexpr uint32_t kBuckets = kKey == 0 ? kSortBuckets : kRaySortBuckets;
+    __device__ static uint32_t of(const DevScene &S, const WavefrontState &s, uint32_t pid) {
+        return kKey == 0 ? sort_class(S, s, pid) : ray_key(S, s, pid);
+    }
+};
+
+template <int kKey>
 __global__ void __launch_bounds__(256) k_sort_hist(DevScene S, WavefrontState s, int in_queue, Counters *counters) {
-    __shared__ uint32_t h[kSortBuckets];
-    for (uint32_t b = threadIdx.x; b < kSortBuckets; b += blockDim.x) h[b] = 0;
+    constexpr uint32_t B = SortKey<kKey>::kBuckets;
+    __shared__ uint32_t h[B];
+    for (uint32_t b = threadIdx.x; b < B; b += blockDim.x) h[b] = 0;
     __syncthreads();
     const unsigned long long n = counters->queue_counters[in_queue];
     const uint32_t *queue = s.queue[in_queue];
     for (unsigned long long q = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
          q += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
-        atomicAdd(&h[sort_class(S, s, queue[q])], 1u);
+        atomicAdd(&h[SortKey<kKey>::of(S, s, queue[q])], 1u);
     __syncthreads();
-    for (uint32_t b = threadIdx.x; b < kSortBuckets; b += blockDim.x)
+    for (uint32_t b = threadIdx.x; b < B; b += blockDim.x)
         if (h[b]) atomicAdd(&s.sort_hist[b], h[b]);
 }
 
-// Exclusive scan of the histogram into the scatter cursors; clears the histogram for the next sort.
-__global__ void __launch_bounds__(kSortBuckets) k_sort_scan(WavefrontState s) {
-    __shared__ uint32_t v[kSortBuckets];
-    const uint32_t b = threadIdx.x;
-    v[b] = s.sort_hist[b];
-    s.sort_hist[b] = 0;
+// Exclusive scan of the histogram (1024 threads, B / 1024 buckets each) into the scatter cursors; clears
+// the histogram for the next sort.
+template <int kKey>
+__global__ void __launch_bounds__(1024) k_sort_scan(WavefrontState s) {
+    constexpr uint32_t B = SortKey<kKey>::kBuckets;
+    constexpr uint32_t per = (B + 1023) / 1024;
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+    uint32_t v[per];
+    uint32_t mine = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < per; ++k) {
+        const uint32_t b = t * per + k;
+        v[k] = b < B ? s.sort_hist[b] : 0u;
+        if (b < B) s.sort_hist[b] = 0;
+        mine += v[k];
+    }
+    uint32_t incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= static_cast<uint32_t>(o)) incl += x;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
     __syncthreads();
-    uint32_t prefix = 0;
-    for (uint32_t k = 0; k < b; ++k) prefix += v[k];
-    s.sort_hist[kSortBuckets + b] = prefix;
+    if (warp == 0) {
+        uint32_t w = warp_sums[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, w, o);
+            if (lane >= static_cast<uint32_t>(o)) w += x;
+        }
+        warp_sums[lane] = w;  // inclusive prefix of warp totals
+    }
+    __syncthreads();
+    uint32_t run = incl - mine + (warp > 0 ? warp_sums[warp - 1] : 0u);
+#pragma unroll
+    for (uint32_t k = 0; k < per; ++k) {
+        const uint32_t b = t * per + k;
+        if (b < B) s.sort_hist[kRaySortBuckets + b] = run;
+        run += v[k];
+    }
 }
 
-__global__ void __launch_bounds__(256) k_sort_scatter(DevScene S, WavefrontState s, int in_queue, Counters *counters) {
+template <int kKey>
+__global__ void __launch_bounds__(256) k_sort_scatter(DevScene S, WavefrontState s, int in_queue, uint32_t *dst,
+                                                      Counters *counters) {
+    constexpr uint32_t B = SortKey<kKey>::kBuckets;
     const unsigned long long n = counters->queue_counters[in_queue];
     const uint32_t *queue = s.queue[in_queue];
     const uint32_t lane = threadIdx.x & 31u;
@@ -352,28 +411,49 @@ __global__ void __launch_bounds__(256) k_sort_scatter(DevScene S, WavefrontState
         const unsigned long long q = q0 + threadIdx.x;
         const bool active = q < n;
         const uint32_t pid = active ? queue[q] : 0u;
-        const uint32_t key = active ? sort_class(S, s, pid) : kSortBuckets;  // inactive lanes: own group
-        // One atomic per (warp, class): lanes with the same class share a base.
+        const uint32_t key = active ? SortKey<kKey>::of(S, s, pid) : B;  // inactive lanes: own group
+        // One atomic per (warp, key): lanes with the same key share a base.
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
         const uint32_t leader = __ffs(peers) - 1;
         uint32_t base = 0;
-        if (active && lane == leader) base = atomicAdd(&s.sort_hist[kSortBuckets + key], __popc(peers));
+        if (active && lane == leader) base = atomicAdd(&s.sort_hist[kRaySortBuckets + key], __popc(peers));
         base = __shfl_sync(0xFFFFFFFFu, base, leader);
-        if (active) s.sort_keys[base + __popc(peers & ((1u << lane) - 1u))] = pid;
+        if (active) dst[base + __popc(peers & ((1u << lane) - 1u))] = pid;
     }
 }
 
-// Enqueues the sort of queue `in`; returns the state the shade stage reads (its queue `in` replaced by
-// the grouped copy).
+// Enqueues a counting sort of queue `in` by key kKey into `dst`; returns the state the next stage reads
+// (its queue `in` replaced by the sorted copy).
+// The histogram holds 2 x kRaySortBuckets counters (counts, then cursors) and `dst` the queue's capacity;
+// wavefront_alloc sizes both, and sort_buffers_ok checks it before a schedule uses a sort.
+bool sort_buffers_ok(const WavefrontState &s) {
+    return s.sort_hist != nullptr && s.sort_keys != nullptr && s.sort_keys2 != nullptr;
+}
+
+template <int kKey>
+WavefrontState enqueue_sort(const DevScene &scene, const WavefrontState &s, int in, uint32_t *dst, Counters *counters,
+                            int num_sms, cudaStream_t stream) {
+    const unsigned grid = static_cast<unsigned>(num_sms) * 4u;
+    k_sort_hist<kKey><<<grid, 256, 0, stream>>>(scene, s, in, counters);
+    k_sort_scan<kKey><<<1, 1024, 0, stream>>>(s);
+    k_sort_scatter<kKey><<<grid, 256, 0, stream>>>(scene, s, in, dst, counters);
+    WavefrontState sorted = s;
+    sorted.queue[in] = dst;
+    return sorted;
+}
+
+// Material sort: group a shade queue by the material class of each path's hit, so the warps of the
+// shade stage run one BSDF branch and read one material record.
 WavefrontState enqueue_material_sort(const DevScene &scene, const WavefrontState &s, int in, Counters *counters,
                                      int num_sms, cudaStream_t stream) {
-    const unsigned grid = static_cast<unsigned>(num_sms) * 4u;
-    k_sort_hist<<<grid, 256, 0, stream>>>(scene, s, in, counters);
-    k_sort_scan<<<1, kSortBuckets, 0, stream>>>(s);
-    k_sort_scatter<<<grid, 256, 0, stream>>>(scene, s, in, counters);
-    WavefrontState sorted = s;
-    sorted.queue[in] = s.sort_keys;
-    return sorted;
+    return enqueue_sort<0>(scene, s, in, s.sort_keys, counters, num_sms, stream);
+}
+
+// Ray sort: order an extend queue by origin cell and direction octant, so the lanes of a warp walk
+// similar rays.
+WavefrontState enqueue_ray_sort(const DevScene &scene, const WavefrontState &s, int in, Counters *counters,
+                                int num_sms, cudaStream_t stream) {
+    return enqueue_sort<1>(scene, s, in, s.sort_keys2, counters, num_sms, stream);
 }
 
 __device__ __forceinline__ float aces_tonemap(float c, float exposure) {
@@ -552,7 +632,7 @@ unsigned extend_blocks(int num_sms, uint32_t per_sm_override) {
     return static_cast<unsigned>(num_sms) * n;
 }
 
-cudaError_t launch_extend(const DevScene &scene, WavefrontState &s, int in, bool count, Counters *counters,
+cudaError_t launch_extend(const DevScene &scene, const WavefrontState &s, int in, bool count, Counters *counters,
                           unsigned grid, cudaStream_t stream, LaunchEvents *ev, bool batch = false) {
     unsigned long long *qc = counters->queue_counters;
     cudaError_t e = cudaMemsetAsync(qc + kCursor, 0, sizeof(unsigned long long), stream);
@@ -577,9 +657,10 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
         (e = dmalloc(s.queue[0], capacity)) != cudaSuccess || (e = dmalloc(s.queue[1], capacity)) != cudaSuccess ||
         (e = dmalloc(s.sort_keys, capacity)) != cudaSuccess || (e = dmalloc(s.slot_state, capacity)) != cudaSuccess ||
         (e = dmalloc(s.slot_item, capacity)) != cudaSuccess || (e = dmalloc(s.prev_pdf, capacity)) != cudaSuccess ||
-        (e = dmalloc(s.sort_hist, 2 * kSortBuckets)) != cudaSuccess ||
+        (e = dmalloc(s.sort_hist, 2 * kRaySortBuckets)) != cudaSuccess ||
+        (e = dmalloc(s.sort_keys2, capacity)) != cudaSuccess ||
         (e = dmalloc(s.slot_req, capacity)) != cudaSuccess || (e = dmalloc(s.slot_root, capacity)) != cudaSuccess ||
-        (e = cudaMemset(s.sort_hist, 0, 2 * kSortBuckets * sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMemset(s.sort_hist, 0, 2 * kRaySortBuckets * sizeof(uint32_t))) != cudaSuccess ||
         (e = cudaHostAlloc(reinterpret_cast<void **>(&s.host_len), sizeof(unsigned long long), cudaHostAllocDefault)) !=
             cudaSuccess) {
         wavefront_free(s);
@@ -593,7 +674,7 @@ void wavefront_free(WavefrontState &s) {
     void *ptrs[] = {s.ray_o,      s.ray_d,     s.thr,     s.color,        s.rng,        s.hit,
                     s.hit_face,   s.queue[0],  s.queue[1], s.sort_keys,   s.slot_state, s.slot_item,
                     s.samples,    s.frame_weight, s.frame_seed, s.prev_pdf, s.sort_hist, s.slot_req,
-                    s.slot_root};
+                    s.slot_root,  s.sort_keys2};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s.host_len) cudaFreeHost(s.host_len);
@@ -616,6 +697,7 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
     uint32_t nl = 0;
     const uint32_t npix = fbuf.width * fbuf.height;
     if (s.capacity < npix) return cudaErrorInvalidValue;
+    if ((tuning.ray_sort || tuning.material_sort) && !sort_buffers_ok(s)) return cudaErrorInvalidValue;
     cudaError_t e;
     unsigned long long *qc = counters->queue_counters;
     if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
@@ -631,11 +713,16 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
     for (uint32_t b = 0; b < p.bounce; ++b) {
         const int in = static_cast<int>(b & 1u), out = in ^ 1;
         if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
-        if ((e = launch_extend(scene, s, in, count, counters, extend_grid, stream, ev)) != cudaSuccess) return e;
+        WavefrontState se = s;
+        if (tuning.ray_sort) {
+            se = enqueue_ray_sort(scene, s, in, counters, num_sms, stream);
+            nl += 3;
+        }
+        if ((e = launch_extend(scene, se, in, count, counters, extend_grid, stream, ev)) != cudaSuccess) return e;
         ++nl;
-        WavefrontState ss = s;
+        WavefrontState ss = se;
         if (tuning.material_sort) {
-            ss = enqueue_material_sort(scene, s, in, counters, num_sms, stream);
+            ss = enqueue_material_sort(scene, se, in, counters, num_sms, stream);
             nl += 3;
         }
         auto *shade = p.rng == 0 ? (p.enable_nee ? k_wf_shade<0, true> : k_wf_shade<0, false>)
@@ -664,6 +751,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
     const uint32_t npix = fbuf.width * fbuf.height;
     t_site = "set-up";
     if (s.capacity < npix || num_frames == 0 || p.bounce == 0) return cudaErrorInvalidValue;
+    if ((tuning.ray_sort || tuning.material_sort) && !sort_buffers_ok(s)) return cudaErrorInvalidValue;
     cudaError_t e;
     if (s.frame_capacity < num_frames) {
         if (s.frame_weight) cudaFree(s.frame_weight);
@@ -710,10 +798,12 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
             for (uint32_t c = 0; c < kChunk; ++c) {
                 const int in = static_cast<int>(c & 1u), out = in ^ 1;
                 if ((ce = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return ce;
-                if ((ce = launch_extend(scene, s, in, count, counters, extend_grid, stream, chunk_ev)) != cudaSuccess)
+                const WavefrontState se =
+                    tuning.ray_sort ? enqueue_ray_sort(scene, s, in, counters, num_sms, stream) : s;
+                if ((ce = launch_extend(scene, se, in, count, counters, extend_grid, stream, chunk_ev)) != cudaSuccess)
                     return ce;
                 const WavefrontState ss =
-                    tuning.material_sort ? enqueue_material_sort(scene, s, in, counters, num_sms, stream) : s;
+                    tuning.material_sort ? enqueue_material_sort(scene, se, in, counters, num_sms, stream) : se;
                 auto *shade = p.rng == 0 ? (p.enable_nee ? k_mf_shade<0, true> : k_mf_shade<0, false>)
                                          : (p.enable_nee ? k_mf_shade<1, true> : k_mf_shade<1, false>);
                 shade<<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, ss, in, f0, total_items, counters);
@@ -734,7 +824,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 uint32_t f0, total_items, count, num_sms;
                 Counters *counters;
                 cudaStream_t stream;
-                unsigned extend_grid, shade_grid, material_sort;
+                unsigned extend_grid, shade_grid, material_sort, ray_sort;
             } key;
             std::memset(&key, 0, sizeof(key));
             key.scene = scene;
@@ -751,6 +841,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
             key.extend_grid = extend_grid;
             key.shade_grid = shade_blocks;
             key.material_sort = tuning.material_sort;
+            key.ray_sort = tuning.ray_sort;
             const auto *kb = reinterpret_cast<const unsigned char *>(&key);
             graph_ev.pairs = graph->events;
             graph_ev.capacity = static_cast<int>(kChunk);
@@ -809,7 +900,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 return e;
             }
             iter += kChunk;
-            nl += (tuning.material_sort ? 5u : 2u) * kChunk;
+            nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u)) * kChunk;
             if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
                 cudaSuccess)
                 return e;
@@ -840,6 +931,7 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
                                 LaunchEvents *ev, const WfTuning &tuning) {
     if (b.num_reqs == 0 || b.total_items == 0 || s.capacity == 0 || s.sample_capacity < b.total_items)
         return cudaErrorInvalidValue;
+    if ((tuning.ray_sort || tuning.material_sort) && !sort_buffers_ok(s)) return cudaErrorInvalidValue;
     uint32_t nl = 0;
     cudaError_t e;
     unsigned long long *qc = counters->queue_counters;
@@ -864,13 +956,16 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
         for (uint32_t c = 0; c < kChunk; ++c) {
             const int in = static_cast<int>(c & 1u), out = in ^ 1;
             if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
-            if ((e = launch_extend(scene, s, in, count, counters, extend_grid, stream, ev, true)) != cudaSuccess)
+            const WavefrontState se = tuning.ray_sort ? enqueue_ray_sort(scene, s, in, counters, num_sms, stream) : s;
+            if ((e = launch_extend(scene, se, in, count, counters, extend_grid, stream, ev, true)) != cudaSuccess)
                 return e;
-            shade<<<shade_blocks, 128, 0, stream>>>(scene, b, s, in, counters);
+            const WavefrontState ss =
+                tuning.material_sort ? enqueue_material_sort(scene, se, in, counters, num_sms, stream) : se;
+            shade<<<shade_blocks, 128, 0, stream>>>(scene, b, ss, in, counters);
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         iter += kChunk;
-        nl += 2 * kChunk;
+        nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u)) * kChunk;
         if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
             cudaSuccess)
             return e;

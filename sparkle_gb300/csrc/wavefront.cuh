@@ -25,7 +25,8 @@ struct WavefrontState {
     uint32_t *hit_face = nullptr;
     uint32_t *queue[2] = {nullptr, nullptr};  // path indices
     uint32_t *sort_keys = nullptr;            // material sort: the shade queue grouped by material class
-    uint32_t *sort_hist = nullptr;            // material sort: 2 x kSortBuckets counters (histogram, cursors)
+    uint32_t *sort_hist = nullptr;            // sorts: 2 x kRaySortBuckets counters (histogram, cursors)
+    uint32_t *sort_keys2 = nullptr;           // ray sort: the extend queue ordered by ray key
     float *prev_pdf = nullptr;                // NEE: cosine pdf of the continuation after a light-sampling vertex
     uint32_t *slot_state = nullptr;           // multi-frame mode: bounce of the slot's path
     uint32_t *slot_item = nullptr;            // multi-frame mode: sample item (frame * pixels + pixel) of the slot
@@ -42,6 +43,8 @@ struct WavefrontState {
 
 // Material-sort classes: material ids 0..kSortBuckets-3 each, larger ids share one class, misses the last.
 constexpr uint32_t kSortBuckets = 64;
+// Ray-sort keys: 3-bit Morton cell per axis of the origin in the scene bounds x direction octant.
+constexpr uint32_t kRaySortBuckets = 4096;
 
 // Frames per multi-frame pass: bounds the per-sample result buffer to kFramesPerPass * pixels * 16 B.
 constexpr uint32_t kFramesPerPass = 64;
@@ -54,6 +57,7 @@ struct WfTuning {
     uint32_t extend_blocks_per_sm = 0;  // 0 = occupancy maximum of the traversal kernel
     uint32_t shade_blocks_per_sm = 8;
     bool material_sort = false;
+    bool ray_sort = false;
 };
 
 // Host-side CUDA graph of one chunk of the multi-frame loop (kChunkIterations extend + shade iterations

@@ -251,14 +251,14 @@ class Context:
     def tuning(self) -> dict:
         t = spk_tuning()
         self._check(self.L.spk_get_tuning(self.h, C.byref(t)))
-        return {k: getattr(t, k) for k, _ in spk_tuning._fields_ if k != "reserved"}
+        return {k: getattr(t, k) for k, _ in spk_tuning._fields_}
 
     def set_tuning(self, **knobs):
         """Updates the named knobs of spk_tuning (the others keep their current value)."""
         t = spk_tuning()
         self._check(self.L.spk_get_tuning(self.h, C.byref(t)))
         for k, v in knobs.items():
-            if k not in dict(spk_tuning._fields_) or k == "reserved":
+            if k not in dict(spk_tuning._fields_):
                 raise KeyError(f"unknown tuning knob {k!r}")
             setattr(t, k, int(v))
         self._check(self.L.spk_set_tuning(self.h, C.byref(t)))

@@ -12,7 +12,7 @@ from sparkle_gb300 import abi, native, scenes
 pytestmark = pytest.mark.gpu
 
 DEFAULTS = dict(cuda_graph=1, material_sort=0, bvh_width=8, bvh_leaf_size=3, extend_blocks_per_sm=0,
-                shade_blocks_per_sm=8, batch_slots=0)
+                shade_blocks_per_sm=8, batch_slots=0, ray_sort=0)
 
 VARIANTS = [
     dict(cuda_graph=0),
@@ -21,6 +21,8 @@ VARIANTS = [
     dict(bvh_width=4, bvh_leaf_size=1),
     dict(bvh_leaf_size=2, extend_blocks_per_sm=2),
     dict(shade_blocks_per_sm=3, material_sort=1, cuda_graph=0),
+    dict(ray_sort=1),
+    dict(ray_sort=1, material_sort=1),
 ]
 
 
