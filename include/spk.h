@@ -207,6 +207,7 @@ typedef struct spk_tuning {
     uint32_t shade_blocks_per_sm;  /* shading CTAs per SM, 1..32 (default 8) */
     uint32_t batch_slots;          /* path slots (queue capacity) of spk_render_batch, 0 = min(items, 2^21) */
     uint32_t ray_sort;             /* 1: order each extend queue by ray (direction octant, origin cell) (default 0) */
+    uint32_t bvh_collapse;         /* 8-wide collapse: 0 greedy largest-area (default), 1 SAH-optimal; next spk_set_scene */
 } spk_tuning;
 
 /* ------------------------------------------------------------------------------------------------ */

@@ -22,8 +22,9 @@ SPACE = {
     "cuda_graph": [1, 0],
     "bvh_width": [8, 4],
     "bvh_leaf_size": [3, 2],
+    "bvh_collapse": [0, 1],
 }
-SCENE_KNOBS = ("bvh_width", "bvh_leaf_size")
+SCENE_KNOBS = ("bvh_width", "bvh_leaf_size", "bvh_collapse")
 
 
 def measure(ctx, workload, repeats: int = 2):

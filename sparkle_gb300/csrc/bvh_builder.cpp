@@ -2,6 +2,7 @@
 #include "bvh_builder.h"
 
 #include <algorithm>
+#include <functional>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -352,6 +353,207 @@ WideBvh collapse_wide(const Bvh2 &bvh, int max_children) {
                 w.meta[s] = static_cast<uint8_t>((unary << 5) | offset);
                 for (uint32_t i = 0; i < c.count; ++i) out.items.push_back(bvh.items[c.first + i]);
                 offset += c.count;
+            }
+        }
+        out.nodes[job.wide_node] = w;
+    }
+    return out;
+}
+
+
+namespace {
+
+constexpr float kSahNodeCost = 1.0f;
+constexpr float kSahItemCost = 0.3f;
+
+// Assigns the children of one wide node to octant slots (slot s = near-most child for rays whose sign
+// bits equal s) and writes its quantised boxes: the same assignment collapse_wide uses.
+void assign_slots(const Bvh2 &bvh, const std::vector<uint32_t> &kids, int *slot_of, int *kid_in_slot) {
+    const int nk = static_cast<int>(kids.size());
+    float lo[3] = {std::numeric_limits<float>::max(), std::numeric_limits<float>::max(),
+                   std::numeric_limits<float>::max()};
+    float hi[3] = {-lo[0], -lo[1], -lo[2]};
+    for (uint32_t k : kids)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], bvh.nodes[k].lo[a]);
+            hi[a] = std::max(hi[a], bvh.nodes[k].hi[a]);
+        }
+    float pc[3];
+    for (int a = 0; a < 3; ++a) pc[a] = 0.5f * (lo[a] + hi[a]);
+    struct Cost {
+        float c;
+        int kid, slot;
+    };
+    std::vector<Cost> costs;
+    for (int k = 0; k < nk; ++k) {
+        const Bvh2Node &c = bvh.nodes[kids[k]];
+        float d[3];
+        for (int a = 0; a < 3; ++a) d[a] = 0.5f * (c.lo[a] + c.hi[a]) - pc[a];
+        for (int sl = 0; sl < 8; ++sl) {
+            const float v = (sl & 1 ? -d[0] : d[0]) + (sl & 2 ? -d[1] : d[1]) + (sl & 4 ? -d[2] : d[2]);
+            costs.push_back({v, k, sl});
+        }
+    }
+    std::stable_sort(costs.begin(), costs.end(), [](const Cost &a, const Cost &b) { return a.c < b.c; });
+    std::fill(slot_of, slot_of + 8, -1);
+    std::fill(kid_in_slot, kid_in_slot + 8, -1);
+    for (const Cost &c : costs) {
+        if (slot_of[c.kid] < 0 && kid_in_slot[c.slot] < 0) {
+            slot_of[c.kid] = c.slot;
+            kid_in_slot[c.slot] = c.kid;
+        }
+    }
+}
+
+}  // namespace
+
+WideBvh collapse_wide_sah(const Bvh2 &bvh, int max_children, int max_leaf) {
+    const int K = std::max(2, std::min(8, max_children));
+    max_leaf = std::max(1, std::min(3, max_leaf));
+    WideBvh out;
+    const size_t n = bvh.nodes.size();
+    if (n == 0) return out;
+    // Post-order of the binary tree (explicit stack: trees over millions of items are deep).
+    std::vector<uint32_t> order;
+    order.reserve(n);
+    {
+        std::vector<std::pair<uint32_t, bool>> st{{0u, false}};
+        while (!st.empty()) {
+            auto [v, expanded] = st.back();
+            st.pop_back();
+            const Bvh2Node &b = bvh.nodes[v];
+            if (b.count > 0 || expanded) {
+                order.push_back(v);
+                continue;
+            }
+            st.push_back({v, true});
+            st.push_back({b.first + 1, false});
+            st.push_back({b.first, false});
+        }
+    }
+    const float kInf = std::numeric_limits<float>::infinity();
+    std::vector<uint32_t> items_in(n, 0);
+    std::vector<float> cost(n * 9, kInf);     // cost[v * 9 + i], i = 1..K: best with at most i roots
+    std::vector<uint8_t> split(n * 9, 0);     // split[v * 9 + j]: left share k of the best j-root distribution
+    std::vector<uint8_t> use_dist(n * 9, 0);  // use_dist[v * 9 + i]: at most i roots uses the distribution
+    std::vector<uint8_t> leaf_root(n, 0);     // the single-root option is a leaf
+    for (uint32_t v : order) {
+        const Bvh2Node &b = bvh.nodes[v];
+        const float area = node_half_area(b);
+        float *C = &cost[static_cast<size_t>(v) * 9];
+        if (b.count > 0) {
+            items_in[v] = b.count;
+            const float leaf = b.count <= static_cast<uint32_t>(max_leaf) ? area * kSahItemCost * b.count : kInf;
+            for (int i = 1; i <= K; ++i) C[i] = leaf;
+            leaf_root[v] = 1;
+            continue;
+        }
+        const uint32_t L = b.first, R = b.first + 1;
+        items_in[v] = items_in[L] + items_in[R];
+        const float *CL = &cost[static_cast<size_t>(L) * 9];
+        const float *CR = &cost[static_cast<size_t>(R) * 9];
+        float dist[9];
+        for (int j = 2; j <= K; ++j) {
+            float best = kInf;
+            int bk = 1;
+            for (int k = 1; k < j; ++k) {
+                const float c = CL[k] + CR[j - k];
+                if (c < best) {
+                    best = c;
+                    bk = k;
+                }
+            }
+            dist[j] = best;
+            split[static_cast<size_t>(v) * 9 + j] = static_cast<uint8_t>(bk);
+        }
+        const float leaf =
+            items_in[v] <= static_cast<uint32_t>(max_leaf) ? area * kSahItemCost * items_in[v] : kInf;
+        const float inner = area * kSahNodeCost + dist[K];
+        leaf_root[v] = leaf <= inner ? 1 : 0;
+        C[1] = std::min(leaf, inner);
+        for (int i = 2; i <= K; ++i) {
+            if (dist[i] < C[i - 1]) {
+                C[i] = dist[i];
+                use_dist[static_cast<size_t>(v) * 9 + i] = 1;
+            } else {
+                C[i] = C[i - 1];
+            }
+        }
+    }
+    // Roots of the best representation of subtree v with at most i roots.
+    std::function<void(uint32_t, int, std::vector<uint32_t> &)> roots = [&](uint32_t v, int i,
+                                                                          std::vector<uint32_t> &outv) {
+        while (i > 1 && !use_dist[static_cast<size_t>(v) * 9 + i]) --i;
+        if (i == 1) {
+            outv.push_back(v);
+            return;
+        }
+        const int k = split[static_cast<size_t>(v) * 9 + i];
+        roots(bvh.nodes[v].first, k, outv);
+        roots(bvh.nodes[v].first + 1, i - k, outv);
+    };
+    auto collect_items = [&](uint32_t v, std::vector<uint32_t> &dst) {
+        std::vector<uint32_t> st{v};
+        while (!st.empty()) {
+            const uint32_t u = st.back();
+            st.pop_back();
+            const Bvh2Node &b = bvh.nodes[u];
+            if (b.count > 0) {
+                for (uint32_t t = 0; t < b.count; ++t) dst.push_back(bvh.items[b.first + t]);
+            } else {
+                st.push_back(b.first + 1);
+                st.push_back(b.first);
+            }
+        }
+    };
+    out.nodes.reserve(n / 4 + 1);
+    out.items.reserve(bvh.items.size());
+    out.nodes.push_back(WideNode{});
+    struct Job {
+        uint32_t bvh_node, wide_node;
+    };
+    std::vector<Job> queue{{0, 0}};
+    for (size_t qi = 0; qi < queue.size(); ++qi) {
+        const Job job = queue[qi];
+        std::vector<uint32_t> kids;
+        if (leaf_root[job.bvh_node]) {
+            kids.push_back(job.bvh_node);  // the whole tree is one leaf: a node with a single leaf child
+        } else {
+            const Bvh2Node &b = bvh.nodes[job.bvh_node];
+            const int k = split[static_cast<size_t>(job.bvh_node) * 9 + K];
+            roots(b.first, k, kids);
+            roots(b.first + 1, K - k, kids);
+        }
+        int slot_of[8], kid_in_slot[8];
+        assign_slots(bvh, kids, slot_of, kid_in_slot);
+        WideNode w{};
+        const Bvh2Node *child_ptrs[8];
+        for (size_t k = 0; k < kids.size(); ++k) child_ptrs[k] = &bvh.nodes[kids[k]];
+        quantize_node(w, child_ptrs, static_cast<int>(kids.size()), slot_of);
+        w.child_base = static_cast<uint32_t>(out.nodes.size());
+        w.item_base = static_cast<uint32_t>(out.items.size());
+        uint32_t offset = 0;
+        for (int sl = 0; sl < 8; ++sl) {
+            const int k = kid_in_slot[sl];
+            if (k < 0) {
+                w.meta[sl] = 0;
+                continue;
+            }
+            const uint32_t c = kids[k];
+            const bool as_leaf = leaf_root[c] || (kids.size() == 1 && kids[0] == job.bvh_node);
+            if (!as_leaf) {
+                w.imask |= static_cast<uint8_t>(1u << sl);
+                w.meta[sl] = static_cast<uint8_t>(0x20u | (24u + sl));
+                queue.push_back({c, static_cast<uint32_t>(out.nodes.size())});
+                out.nodes.push_back(WideNode{});
+            } else {
+                std::vector<uint32_t> its;
+                collect_items(c, its);
+                const uint32_t cnt = static_cast<uint32_t>(its.size());
+                const uint32_t unary = (1u << cnt) - 1u;
+                w.meta[sl] = static_cast<uint8_t>((unary << 5) | offset);
+                for (uint32_t it : its) out.items.push_back(it);
+                offset += cnt;
             }
         }
         out.nodes[job.wide_node] = w;

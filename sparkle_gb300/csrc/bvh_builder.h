@@ -56,4 +56,11 @@ struct WideBvh {
 // fan-out (more, emptier nodes) in the same 80-byte record.
 WideBvh collapse_wide(const Bvh2 &bvh, int max_children = 8);
 
+// SAH-optimal collapse (the dynamic program of Ylitie, Karras and Laine, "Efficient Incoherent Ray
+// Traversal on GPUs Through Compressed Wide BVHs", HPG 2017): for every binary node and every k <= 8 the
+// cheapest way to represent its subtree as at most k roots, each root a leaf of <= `max_leaf` items or a
+// wide node; cost = half area x (1 per wide node, 0.3 per item). Best on a binary BVH with one item per leaf,
+// so that the program also chooses the leaf sizes.
+WideBvh collapse_wide_sah(const Bvh2 &bvh, int max_children = 8, int max_leaf = 3);
+
 }  // namespace spk

@@ -200,6 +200,17 @@ void append_wide(std::vector<WideNode> &all, const WideBvh &w, uint32_t item_off
 
 namespace {
 
+// Binary SAH build + collapse to 8-wide nodes as the tuning asks: the SAH-optimal collapse starts from
+// one item per binary leaf and chooses the wide leaves itself; the greedy one keeps the binary leaves.
+WideBvh build_wide(const std::vector<BuildBox> &boxes, const spk_tuning &t, int threads) {
+    if (t.bvh_collapse) {
+        const Bvh2 b2 = build_bvh2(boxes, 1, threads);
+        return collapse_wide_sah(b2, static_cast<int>(t.bvh_width), static_cast<int>(t.bvh_leaf_size));
+    }
+    const Bvh2 b2 = build_bvh2(boxes, t.bvh_leaf_size, threads);
+    return collapse_wide(b2, static_cast<int>(t.bvh_width));
+}
+
 struct HostScene {
     std::vector<WideNode> nodes;
     std::vector<float4> tris;
@@ -294,8 +305,7 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
             }
             boxes[f] = b;
         }
-        const Bvh2 b2 = build_bvh2(boxes, ctx->tuning.bvh_leaf_size, threads);
-        const WideBvh wide = collapse_wide(b2, static_cast<int>(ctx->tuning.bvh_width));
+        const WideBvh wide = build_wide(boxes, ctx->tuning, threads);
         const uint32_t tri_offset = static_cast<uint32_t>(hs.tris.size() / 3);
         blas_root[k] = static_cast<uint32_t>(hs.nodes.size());
         append_wide(hs.nodes, wide, tri_offset);
@@ -354,8 +364,7 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
         }
     }
     if (num_instances > 0) {
-        const Bvh2 b2 = build_bvh2(inst_boxes, ctx->tuning.bvh_leaf_size, threads);
-        const WideBvh wide = collapse_wide(b2, static_cast<int>(ctx->tuning.bvh_width));
+        const WideBvh wide = build_wide(inst_boxes, ctx->tuning, threads);
         hs.tlas_root = static_cast<uint32_t>(hs.nodes.size());
         append_wide(hs.nodes, wide, 0);
         hs.tlas_items = wide.items;
@@ -1125,6 +1134,7 @@ void spk_tuning_defaults(spk_tuning *out) {
     out->bvh_leaf_size = 3;
     out->extend_blocks_per_sm = 0;
     out->shade_blocks_per_sm = 8;
+    out->bvh_collapse = 0;
 }
 
 spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
@@ -1136,7 +1146,8 @@ spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "bvh_leaf_size must be 1..3");
     if (t->extend_blocks_per_sm > 32 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 32)
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "blocks per SM out of range");
-    if (t->ray_sort > 1) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "ray_sort takes 0 or 1");
+    if (t->ray_sort > 1 || t->bvh_collapse > 1)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "ray_sort and bvh_collapse take 0 or 1");
     ctx->tuning = *t;
     return SPK_OK;
 }

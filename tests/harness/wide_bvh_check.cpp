@@ -9,7 +9,10 @@
 
 using namespace spk;
 
-extern "C" int wide_bvh_check(const float *boxes6, uint32_t n, int threads, uint32_t *out_stats /*4*/) {
+// mode 0: binary leaves <= 3 + greedy collapse; mode 1: one item per binary leaf + SAH-optimal collapse.
+// out_cost: SAH cost of the wide tree (half area x (1 per node + 0.3 per item)) relative to the root box.
+extern "C" int wide_bvh_check(const float *boxes6, uint32_t n, int threads, int mode, uint32_t *out_stats /*4*/,
+                              double *out_cost) {
     std::vector<BuildBox> boxes(n);
     for (uint32_t i = 0; i < n; ++i) {
         for (int k = 0; k < 3; ++k) {
@@ -17,7 +20,7 @@ extern "C" int wide_bvh_check(const float *boxes6, uint32_t n, int threads, uint
             boxes[i].hi[k] = boxes6[6 * i + 3 + k];
         }
     }
-    const Bvh2 b2 = build_bvh2(boxes, 3, threads);
+    const Bvh2 b2 = build_bvh2(boxes, mode ? 1 : 3, threads);
     if (n == 0) return b2.nodes.empty() ? 0 : 1;
     // binary tree: leaves <= 3 items, every item once
     std::vector<int> seen(n, 0);
@@ -28,7 +31,8 @@ extern "C" int wide_bvh_check(const float *boxes6, uint32_t n, int threads, uint
     }
     for (int s : seen)
         if (s != 1) return 4;
-    const WideBvh w = collapse_wide(b2);
+    const WideBvh w = mode ? collapse_wide_sah(b2) : collapse_wide(b2);
+    double cost = 0.0, root_area = 0.0;
     if (w.items.size() != n) return 5;
     std::vector<int> seen_items(n, 0);
     std::vector<int> refs(w.nodes.size(), 0);
@@ -49,6 +53,7 @@ extern "C" int wide_bvh_check(const float *boxes6, uint32_t n, int threads, uint
             sc[k] = std::ldexp(1.0, static_cast<int>(nd.e[k]) - 127);
         }
         uint32_t inner_rank = 0, item_total = 0;
+        double nlo[3] = {1e300, 1e300, 1e300}, nhi[3] = {-1e300, -1e300, -1e300};
         for (int s = 0; s < 8; ++s) {
             const uint32_t m = nd.meta[s];
             const bool inner = (nd.imask >> s) & 1u;
@@ -61,6 +66,10 @@ extern "C" int wide_bvh_check(const float *boxes6, uint32_t n, int threads, uint
             if (m == 0) {
                 if (inner) return 8;
                 continue;
+            }
+            for (int k = 0; k < 3; ++k) {
+                nlo[k] = std::fmin(nlo[k], lo[k]);
+                nhi[k] = std::fmax(nhi[k], hi[k]);
             }
             if (inner) {
                 if (m != (0x20u | (24u + s))) return 9;
@@ -97,9 +106,15 @@ extern "C" int wide_bvh_check(const float *boxes6, uint32_t n, int threads, uint
                     }
                 }
                 item_total += ni;
+                const double ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
+                cost += 0.3 * ni * (ex * ey + ey * ez + ez * ex);
             }
         }
         if (item_total > 24) return 18;
+        const double ex = nhi[0] - nlo[0], ey = nhi[1] - nlo[1], ez = nhi[2] - nlo[2];
+        const double area = ex * ey + ey * ez + ez * ex;
+        cost += area;
+        if (idx == 0) root_area = area;
     }
     for (int s : seen_items)
         if (s != 1) return 19;
@@ -108,5 +123,6 @@ extern "C" int wide_bvh_check(const float *boxes6, uint32_t n, int threads, uint
     out_stats[1] = max_depth;
     out_stats[2] = static_cast<uint32_t>(b2.nodes.size());
     out_stats[3] = static_cast<uint32_t>(w.items.size());
+    if (out_cost) *out_cost = root_area > 0 ? cost / root_area : 0.0;
     return 0;
 }

@@ -21,7 +21,7 @@ def harness(tmp_path_factory):
                     os.path.join(ROOT, "sparkle_gb300", "csrc", "bvh_builder.cpp"), "-o", str(out), "-lpthread"],
                    check=True)
     L = C.CDLL(str(out))
-    L.wide_bvh_check.argtypes = [C.c_void_p, C.c_uint32, C.c_int, C.c_void_p]
+    L.wide_bvh_check.argtypes = [C.c_void_p, C.c_uint32, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
     return L
 
 
@@ -30,13 +30,27 @@ def tri_boxes(mesh):
     return np.concatenate([p.min(1), p.max(1)], 1).astype(np.float32)
 
 
-def check(harness, boxes, threads=4):
+def check(harness, boxes, threads=4, mode=None):
+    """Checks both collapses (greedy and SAH-optimal) unless `mode` picks one; returns the greedy stats."""
+    boxes = np.ascontiguousarray(boxes, np.float32)
+    out = None
+    for m in ((0, 1) if mode is None else (mode,)):
+        stats = np.zeros(4, np.uint32)
+        cost = C.c_double()
+        rc = harness.wide_bvh_check(boxes.ctypes.data_as(C.c_void_p), len(boxes), threads, m,
+                                    stats.ctypes.data_as(C.c_void_p), C.byref(cost))
+        assert rc == 0, f"invariant {rc} violated (collapse mode {m})"
+        out = stats if out is None else out
+    return out
+
+
+def sah_cost(harness, boxes, mode, threads=4):
     boxes = np.ascontiguousarray(boxes, np.float32)
     stats = np.zeros(4, np.uint32)
-    rc = harness.wide_bvh_check(boxes.ctypes.data_as(C.c_void_p), len(boxes), threads,
-                                stats.ctypes.data_as(C.c_void_p))
-    assert rc == 0, f"invariant {rc} violated"
-    return stats
+    cost = C.c_double()
+    assert harness.wide_bvh_check(boxes.ctypes.data_as(C.c_void_p), len(boxes), threads, mode,
+                                  stats.ctypes.data_as(C.c_void_p), C.byref(cost)) == 0
+    return cost.value, stats
 
 
 def test_small_meshes(harness):
@@ -66,6 +80,16 @@ def test_cornell_and_icosphere(harness, cornell):
 
 def test_full_terrain(harness):
     mesh = scenes.heightfield(1024, 100.0, 6.0, seed=1)
-    stats = check(harness, tri_boxes(mesh), threads=8)
+    stats = check(harness, tri_boxes(mesh), threads=8, mode=0)
+    check(harness, tri_boxes(mesh), threads=8, mode=1)
     assert stats[3] == 2 * 1024 * 1024
     assert stats[1] < 40
+
+
+def test_sah_collapse_lowers_the_cost(harness):
+    """The SAH-optimal collapse has a lower SAH cost than the greedy one on the meshes of the workloads."""
+    for mesh in (scenes.heightfield(128, 40.0, 3.0, seed=2), scenes.icosphere(4)):
+        g, gs = sah_cost(harness, tri_boxes(mesh), 0)
+        s, ss = sah_cost(harness, tri_boxes(mesh), 1)
+        assert s < g, (s, g)
+        assert ss[3] == gs[3]  # every item once in both
