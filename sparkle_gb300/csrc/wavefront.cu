@@ -8,6 +8,10 @@
 
 #include "wavefront.cuh"
 
+#ifndef SPK_SHADE_MIN_BLOCKS
+#define SPK_SHADE_MIN_BLOCKS 8  // resident 128-thread blocks per SM the shading kernels are compiled for (64 registers)
+#endif
+
 namespace spk {
 namespace {
 
@@ -196,7 +200,7 @@ __global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_wf_extend(DevScene
 }
 
 template <int kKind, bool kNee>
-__global__ void __launch_bounds__(128) k_wf_shade(DevScene S, FrameBuffers fb, RenderParams p, WavefrontState s,
+__global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_wf_shade(DevScene S, FrameBuffers fb, RenderParams p, WavefrontState s,
                                                   int in_queue, uint32_t bounce, Counters *counters) {
     uint32_t shadow = 0, err = 0;
     const unsigned long long n = counters->queue_counters[in_queue];
@@ -258,7 +262,7 @@ __global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers
 // Shade one segment per live slot. A finished sample stores its clamped result (RenderPixel's 6.0 clamp,
 // CPURenderer.cpp:408) at its item, and the slot takes the next item from the global counter.
 template <int kKind, bool kNee>
-__global__ void __launch_bounds__(128) k_mf_shade(DevScene S, DevCamera cam, FrameBuffers fb, RenderParams p,
+__global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_mf_shade(DevScene S, DevCamera cam, FrameBuffers fb, RenderParams p,
                                                   WavefrontState s, int in_queue, uint32_t frame_base,
                                                   uint32_t total_items, Counters *counters) {
     uint32_t shadow = 0, err = 0;
@@ -535,7 +539,7 @@ __global__ void __launch_bounds__(128) k_b_generate(DevScene S, BatchParams b, W
 }
 
 template <int kKind, bool kNee>
-__global__ void __launch_bounds__(128) k_b_shade(DevScene S, BatchParams b, WavefrontState s, int in_queue,
+__global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_b_shade(DevScene S, BatchParams b, WavefrontState s, int in_queue,
                                                  Counters *counters) {
     uint32_t shadow = 0, err = 0;
     const unsigned long long n = counters->queue_counters[in_queue];
