@@ -1,0 +1,201 @@
+"""glTF 2.0 scene import into the path tracer's scene structs, with the reference loader's conventions.
+
+Restates Sparkle's GLTFLoader (libraries/source/io/scene/GLTFLoader.cpp), which reads the file with
+tinygltf (not in the reference tree); this module parses the glTF JSON, buffers and accessors itself.
+What the reference does and this module mirrors:
+
+* Materials (LoadMaterials, GLTFLoader.cpp:475-526): a factor is read only when its texture is present --
+  base colour with baseColorTexture, metallic/roughness with metallicRoughnessTexture, emissive with
+  emissiveTexture -- otherwise MaterialResource's defaults apply (base colour 1, emissive 0, metallic 1,
+  roughness 1; io/Material.h:9-14). Textures themselves are not sampled yet (the factors are kept).
+* Nodes (ProcessNode, GLTFLoader.cpp:528-575): rotation = 90 degrees about +X times the node's quaternion
+  (glTF is y-up, Sparkle z-up), applied at every node including children; the node's scale is baked into
+  its vertex positions only (LoadPositionArray, :192-230) and the node transform keeps scale 1; local =
+  translation * rotation (Transform.cpp:52-60), world = parent world * local (SceneNode.cpp:30-42). A
+  node's `matrix` is ignored (only translation / rotation / scale are read).
+* Primitives (LoadPrimitive, :329-473): triangle lists, fans and strips (fans and strips expanded to lists),
+  POSITION / NORMAL / TANGENT / TEXCOORD_0; points and lines are skipped; one mesh instance per primitive
+  with the primitive's material.
+* Scenes (Load, :577-645): the default scene's root nodes (scene 0 without a default); a file without
+  scenes treats every node as a root.
+
+Where the reference would assert or read out of range, this module makes a choice and says so: a
+primitive without indices gets 0..n-1, one without a material gets the default material, one without
+normals gets area-weighted vertex normals.
+"""
+from __future__ import annotations
+
+import base64
+import json
+import os
+import struct
+
+import numpy as np
+
+from .abi import Instance, Material, Mesh, Scene, Sky
+
+_COMPONENT = {5120: np.int8, 5121: np.uint8, 5122: np.int16, 5123: np.uint16, 5125: np.uint32, 5126: np.float32}
+_NCOMP = {"SCALAR": 1, "VEC2": 2, "VEC3": 3, "VEC4": 4, "MAT2": 4, "MAT3": 9, "MAT4": 16}
+MODE_TRIANGLES, MODE_STRIP, MODE_FAN = 4, 5, 6
+
+
+def _read_container(path: str):
+    data = open(path, "rb").read()
+    if data[:4] == b"glTF":  # binary container: header, JSON chunk, optional BIN chunk
+        _, _, length = struct.unpack_from("<III", data, 0)
+        off, doc, bin_chunk = 12, None, None
+        while off < length:
+            clen, ctype = struct.unpack_from("<II", data, off)
+            chunk = data[off + 8:off + 8 + clen]
+            if ctype == 0x4E4F534A:
+                doc = json.loads(chunk.decode("utf-8"))
+            elif ctype == 0x004E4942:
+                bin_chunk = chunk
+            off += 8 + clen
+        return doc, bin_chunk
+    return json.loads(data.decode("utf-8")), None
+
+
+def _buffers(doc, base_dir, bin_chunk):
+    out = []
+    for k, b in enumerate(doc.get("buffers", [])):
+        uri = b.get("uri")
+        if uri is None:
+            out.append(bin_chunk if k == 0 and bin_chunk is not None else b"")
+        elif uri.startswith("data:"):
+            out.append(base64.b64decode(uri.split(",", 1)[1]))
+        else:
+            out.append(open(os.path.join(base_dir, uri), "rb").read())
+    return out
+
+
+def _accessor(doc, buffers, index):
+    acc = doc["accessors"][index]
+    dtype = np.dtype(_COMPONENT[acc["componentType"]])
+    ncomp = _NCOMP[acc["type"]]
+    count = acc["count"]
+    if "bufferView" not in acc:  # all zeros (sparse accessors are not supported)
+        return np.zeros((count, ncomp), dtype)
+    view = doc["bufferViews"][acc["bufferView"]]
+    buf = buffers[view["buffer"]]
+    start = view.get("byteOffset", 0) + acc.get("byteOffset", 0)
+    elem = dtype.itemsize * ncomp
+    stride = view.get("byteStride", elem) or elem
+    raw = np.frombuffer(buf, np.uint8, count=(count - 1) * stride + elem if count else 0, offset=start)
+    if stride == elem:
+        arr = raw.view(dtype).reshape(count, ncomp)
+    else:
+        rows = np.lib.stride_tricks.as_strided(raw, shape=(count, elem), strides=(stride, 1))
+        arr = np.ascontiguousarray(rows).view(dtype).reshape(count, ncomp)
+    return arr.copy()
+
+
+def _quat_matrix(q):
+    """3x3 rotation of a glTF quaternion [x, y, z, w] (normalised first)."""
+    x, y, z, w = (float(v) for v in q)
+    n = np.sqrt(x * x + y * y + z * z + w * w)
+    x, y, z, w = x / n, y / n, z / n, w / n
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+ROT_X90 = np.array([[1.0, 0.0, 0.0], [0.0, 0.0, -1.0], [0.0, 1.0, 0.0]])  # AngleAxis(90 deg, +X)
+
+
+def default_material() -> Material:
+    """MaterialResource's defaults (io/Material.h:9-14): white, metallic 1, roughness 1, no emission."""
+    return Material((1.0, 1.0, 1.0), (0.0, 0.0, 0.0), 1.0, 1.0, 0.0, False)
+
+
+def _material(m) -> Material:
+    mat = default_material()
+    pbr = m.get("pbrMetallicRoughness", {})
+    base, emissive = mat.base_color, mat.emissive
+    metallic, roughness = mat.metallic, mat.roughness
+    if pbr.get("baseColorTexture", {}).get("index", -1) >= 0:
+        base = tuple(float(v) for v in pbr.get("baseColorFactor", [1, 1, 1, 1])[:3])
+    if pbr.get("metallicRoughnessTexture", {}).get("index", -1) >= 0:
+        metallic = float(pbr.get("metallicFactor", 1.0))
+        roughness = float(pbr.get("roughnessFactor", 1.0))
+    if m.get("emissiveTexture", {}).get("index", -1) >= 0:
+        emissive = tuple(float(v) for v in m.get("emissiveFactor", [0, 0, 0])[:3])
+    return Material(base, emissive, metallic, roughness, 0.0, False)
+
+
+def _vertex_normals(pos, idx):
+    n = np.zeros_like(pos, dtype=np.float64)
+    p = pos.astype(np.float64)
+    fn = np.cross(p[idx[:, 1]] - p[idx[:, 0]], p[idx[:, 2]] - p[idx[:, 0]])  # area-weighted
+    for c in range(3):
+        np.add.at(n, idx[:, c], fn)
+    ln = np.linalg.norm(n, axis=1, keepdims=True)
+    n = np.where(ln > 0, n / np.maximum(ln, 1e-30), np.array([0.0, 0.0, 1.0]))
+    return n.astype(np.float32)
+
+
+def _primitive_mesh(doc, buffers, prim, scale):
+    mode = prim.get("mode", MODE_TRIANGLES)
+    if mode not in (MODE_TRIANGLES, MODE_STRIP, MODE_FAN):
+        return None
+    attrs = prim["attributes"]
+    pos = _accessor(doc, buffers, attrs["POSITION"]).astype(np.float32) * np.asarray(scale, np.float32)
+    nv = len(pos)
+    idx = (_accessor(doc, buffers, prim["indices"]).reshape(-1).astype(np.int64) if "indices" in prim
+           else np.arange(nv, dtype=np.int64))
+    if mode == MODE_FAN:
+        idx = np.stack([np.full(len(idx) - 2, idx[0]), idx[1:-1], idx[2:]], 1).reshape(-1)
+    elif mode == MODE_STRIP:
+        idx = np.stack([idx[:-2], idx[1:-1], idx[2:]], 1).reshape(-1)
+    tris = idx[: len(idx) // 3 * 3].reshape(-1, 3)
+    if len(tris) == 0:
+        return None
+    normals = (_accessor(doc, buffers, attrs["NORMAL"]).astype(np.float32) if "NORMAL" in attrs
+               else _vertex_normals(pos, tris))
+    tangents = _accessor(doc, buffers, attrs["TANGENT"]).astype(np.float32) if "TANGENT" in attrs else None
+    uvs = _accessor(doc, buffers, attrs["TEXCOORD_0"]).astype(np.float32) if "TEXCOORD_0" in attrs else None
+    return Mesh(pos, normals, tris.astype(np.uint32), tangents, uvs)
+
+
+def load_gltf(path: str, sky: Sky | None = None) -> Scene:
+    """Reads a .gltf (JSON with external or data-URI buffers) or .glb file into a Scene."""
+    doc, bin_chunk = _read_container(path)
+    buffers = _buffers(doc, os.path.dirname(os.path.abspath(path)), bin_chunk)
+    materials = [_material(m) for m in doc.get("materials", [])]
+    default_index = None
+    meshes, instances = [], []
+
+    def process(node_id, parent):
+        nonlocal default_index
+        node = doc["nodes"][node_id]
+        rot = ROT_X90 @ (_quat_matrix(node["rotation"]) if "rotation" in node else np.eye(3))
+        t = np.asarray(node.get("translation", [0.0, 0.0, 0.0]), np.float64)
+        local = np.eye(4)
+        local[:3, :3] = rot
+        local[:3, 3] = t
+        world = parent @ local
+        scale = node.get("scale", [1.0, 1.0, 1.0])
+        if "mesh" in node:
+            for prim in doc["meshes"][node["mesh"]].get("primitives", []):
+                mesh = _primitive_mesh(doc, buffers, prim, scale)
+                if mesh is None:
+                    continue
+                mat = prim.get("material", -1)
+                if mat < 0:
+                    if default_index is None:
+                        materials.append(default_material())
+                        default_index = len(materials) - 1
+                    mat = default_index
+                meshes.append(mesh)
+                instances.append(Instance(len(meshes) - 1, mat, world[:3, :].astype(np.float32)))
+        for c in node.get("children", []):
+            process(c, world)
+
+    scenes_list = doc.get("scenes", [])
+    if scenes_list:
+        roots = scenes_list[doc.get("scene", 0) if doc.get("scene", -1) > -1 else 0].get("nodes", [])
+    else:
+        roots = list(range(len(doc.get("nodes", []))))
+    for r in roots:
+        process(r, np.eye(4))
+    return Scene(meshes, instances, materials, sky or Sky(), name=os.path.basename(path))
