@@ -235,7 +235,29 @@ spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_mesh
                          const spk_instance *instances, uint32_t num_instances,
                          const spk_material *materials, uint32_t num_materials, const spk_sky *sky);
 
-/* One scene of a multi-scene context: the arguments of spk_set_scene. */
+/* A texture as `Image2D` holds it (libraries/include/io/Image.h:112-150): width x height RGBA texels, row
+ * y = v * height, as floats (8-bit formats divided by 255, ColorToVec, Utilities.h:377-380). `srgb` marks an
+ * sRGB format, decoded after the bilinear filter (the "pseudo srgb decode" of Image2D::Sample). */
+typedef struct spk_texture {
+    uint32_t width;
+    uint32_t height;
+    uint32_t srgb;
+    const float *rgba; /* [height][width][4] */
+} spk_texture;
+
+/* Texture maps of one material (MaterialResource's *_texture fields, io/Material.h:16-19): indices into the
+ * scene's texture array, or -1 for none. With a map the material reads texture x factor (base colour,
+ * emissive), texture.z x metallic, texture.y x roughness, and the normal map perturbs the shading normal in
+ * the vertex tangent frame (MaterialRenderProxy.h:117-160, MeshRenderProxy.cpp:341-358). */
+typedef struct spk_material_maps {
+    int32_t base_color;
+    int32_t metallic_roughness;
+    int32_t emissive;
+    int32_t normal;
+} spk_material_maps;
+
+/* One scene of a multi-scene context: the arguments of spk_set_scene, plus optional textures (`maps` has
+ * num_materials entries, or is NULL for untextured materials). */
 typedef struct spk_scene_desc {
     const spk_mesh *meshes;
     uint32_t num_meshes;
@@ -244,6 +266,9 @@ typedef struct spk_scene_desc {
     const spk_material *materials;
     uint32_t num_materials;
     const spk_sky *sky;
+    const spk_texture *textures;
+    uint32_t num_textures;
+    const spk_material_maps *maps;
 } spk_scene_desc;
 
 /* No reference counterpart (the reference renders one scene). Makes several scenes resident at once, for

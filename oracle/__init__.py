@@ -37,6 +37,7 @@ def lib():
         L.or_read_framebuffer.argtypes = [vp, vp, vp]
         L.or_read_gbuffer.argtypes = [vp, vp, vp]
         L.or_guides.argtypes = [vp, vp, vp]
+        L.or_scene_set_textures.argtypes = [vp, vp, C.c_uint32, vp]
         L.or_counts.argtypes = [vp, vp, vp, vp]
         L.or_sample_counts.argtypes = [vp, vp, vp]
         L.or_rng_fill.argtypes = [C.c_int32, C.c_uint64, C.c_uint32, vp, vp]
@@ -59,6 +60,9 @@ class OracleScene:
                                        C.cast(a[4], C.c_void_p), a[5], C.cast(a[6], C.c_void_p))
         if not self.h:
             raise RuntimeError("or_scene_create failed")
+        if scene.textures or self.m.has_maps:
+            lib().or_scene_set_textures(self.h, C.cast(self.m.textures, C.c_void_p), len(scene.textures),
+                                        C.cast(self.m.maps, C.c_void_p) if self.m.has_maps else None)
 
     def __del__(self):
         if getattr(self, "h", None):

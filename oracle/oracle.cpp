@@ -468,6 +468,13 @@ struct or_scene {
     std::vector<float> light_cdf;
     float light_total = 0.f;
     std::vector<uint32_t> inst_light_base;
+    // Textures (Image2D) and per-material maps (MaterialResource's *_texture fields); empty when untextured.
+    struct Tex {
+        uint32_t w, h, srgb;
+        std::vector<V4> px;
+    };
+    std::vector<Tex> textures;
+    std::vector<spk_material_maps> maps;
 };
 
 namespace {
@@ -650,6 +657,60 @@ inline float lerp3(float a, float b, float c, float u, float v) { return a + (b 
 
 // GetIntersection for meshes (MeshRenderProxy.cpp:340-361, Mesh.h:86-134) and spheres
 // (SphereRenderProxy.h:22-31), then Intersection::Update (Intersection.h:52-71).
+// Image2D::Sample (io/Image.h:112-150): bilinear with wrap at uv * size (utilities::Decompose truncates
+// toward zero, utilities::WrapMod), u lerp then v lerp, sRGB decoded after the filter (SRGBtoLinear,
+// Utilities.h:416-425).
+inline unsigned wrap_texel(int a, unsigned b) { return (static_cast<unsigned>(a % static_cast<int>(b)) + b) % b; }
+
+inline float srgb_decode(float c) { return c < 0.04045f ? c / 12.92f : std::pow((c + 0.055f) / 1.055f, 2.4f); }
+
+V3 tex_sample(const or_scene &sc, uint32_t t, const float uv[2]) {
+    const or_scene::Tex &T = sc.textures[t];
+    const float px = uv[0] * static_cast<float>(T.w), py = uv[1] * static_cast<float>(T.h);
+    const int ui = static_cast<int>(px), vi = static_cast<int>(py);
+    const float uc = px - static_cast<float>(ui), vc = py - static_cast<float>(vi);
+    const unsigned x0 = wrap_texel(ui, T.w), x1 = wrap_texel(ui + 1, T.w);
+    const unsigned y0 = wrap_texel(vi, T.h), y1 = wrap_texel(vi + 1, T.h);
+    const V4 s00 = T.px[y0 * T.w + x0], s10 = T.px[y0 * T.w + x1], s01 = T.px[y1 * T.w + x0], s11 = T.px[y1 * T.w + x1];
+    const V3 l0 = mk(s00.x + (s10.x - s00.x) * uc, s00.y + (s10.y - s00.y) * uc, s00.z + (s10.z - s00.z) * uc);
+    const V3 l1 = mk(s01.x + (s11.x - s01.x) * uc, s01.y + (s11.y - s01.y) * uc, s01.z + (s11.z - s01.z) * uc);
+    V3 r = mk(l0.x + (l1.x - l0.x) * vc, l0.y + (l1.y - l0.y) * vc, l0.z + (l1.z - l0.z) * vc);
+    if (T.srgb) r = mk(srgb_decode(r.x), srgb_decode(r.y), srgb_decode(r.z));
+    return r;
+}
+
+// which: 0 base colour, 1 metallic-roughness, 2 emissive, 3 normal; -1 when the material has none.
+inline int32_t material_map(const or_scene &sc, uint32_t mat, int which) {
+    if (sc.maps.empty()) return -1;
+    const spk_material_maps &m = sc.maps[mat];
+    return which == 0 ? m.base_color : which == 1 ? m.metallic_roughness : which == 2 ? m.emissive : m.normal;
+}
+
+// MaterialRenderProxy::GetBaseColor / GetMetallic / GetRoughness / GetEmissive (MaterialRenderProxy.h:117-160):
+// texture x factor, metallic = texel.z x factor, roughness = texel.y x factor.
+spk_material resolve_material(const or_scene &sc, uint32_t mat_id, const float uv[2]) {
+    spk_material m = sc.materials[mat_id];
+    int32_t t = material_map(sc, mat_id, 0);
+    if (t >= 0) {
+        const V3 c = tex_sample(sc, static_cast<uint32_t>(t), uv);
+        m.base_color[0] = c.x * m.base_color[0];
+        m.base_color[1] = c.y * m.base_color[1];
+        m.base_color[2] = c.z * m.base_color[2];
+    }
+    if ((t = material_map(sc, mat_id, 1)) >= 0) {
+        const V3 c = tex_sample(sc, static_cast<uint32_t>(t), uv);
+        m.metallic = c.z * m.metallic;
+        m.roughness = c.y * m.roughness;
+    }
+    if ((t = material_map(sc, mat_id, 2)) >= 0) {
+        const V3 c = tex_sample(sc, static_cast<uint32_t>(t), uv);
+        m.emissive[0] = c.x * m.emissive[0];
+        m.emissive[1] = c.y * m.emissive[1];
+        m.emissive[2] = c.z * m.emissive[2];
+    }
+    return m;
+}
+
 Hit make_hit(const or_scene &sc, const Candidate &cand, V3 o, V3 d) {
     Hit h;
     if (cand.slot < 0) return h;
@@ -679,11 +740,22 @@ Hit make_hit(const or_scene &sc, const Candidate &cand, V3 o, V3 d) {
             h.uv[1] = lerp3(m.uv[2 * i0 + 1], m.uv[2 * i1 + 1], m.uv[2 * i2 + 1], u, v);
         }
         const V3 n0 = m.nrm[i0], n1 = m.nrm[i1], n2 = m.nrm[i2];
-        const V3 sn = mk(lerp3(n0.x, n1.x, n2.x, u, v), lerp3(n0.y, n1.y, n2.y, u, v), lerp3(n0.z, n1.z, n2.z, u, v));
+        V3 sn = mk(lerp3(n0.x, n1.x, n2.x, u, v), lerp3(n0.y, n1.y, n2.y, u, v), lerp3(n0.z, n1.z, n2.z, u, v));
         V3 tg = mk(1, 0, 0);
+        float tw = 1.f;
         if (m.has_tan) {
             const V4 t0 = m.tan[i0], t1 = m.tan[i1], t2 = m.tan[i2];
             tg = mk(lerp3(t0.x, t1.x, t2.x, u, v), lerp3(t0.y, t1.y, t2.y, u, v), lerp3(t0.z, t1.z, t2.z, u, v));
+            tw = lerp3(t0.w, t1.w, t2.w, u, v);
+        }
+        const int32_t nmap = material_map(sc, in.desc.material_id, 3);
+        if (nmap >= 0) {
+            // MeshRenderProxy::GetIntersection (MeshRenderProxy.cpp:349-355): GetNormal = texel * 2 - 1 in the
+            // tangent frame, TangentSpaceToWorldSpace (Utilities.h:403-409).
+            const V3 t = tex_sample(sc, static_cast<uint32_t>(nmap), h.uv);
+            const V3 tn = mk(t.x * 2.f - 1.f, t.y * 2.f - 1.f, t.z * 2.f - 1.f);
+            const V3 bi = cross(sn, tg) * tw;
+            sn = normalized(tg * tn.x + bi * tn.y + sn * tn.z);
         }
         // inv_transform.TransformDirectionTangentSpace(n) = M_3x3 * n (Transform.h:105-108)
         h.normal = normalized(xform_dir(in.M, sn));
@@ -1072,7 +1144,7 @@ PixelResult sample_pixel(const or_renderer &r, Rng &rng, float u, float v, bool 
             }
             break;
         }
-        const spk_material &mat = sc.materials[sc.insts[hit.prim].desc.material_id];
+        const spk_material mat = resolve_material(sc, sc.insts[hit.prim].desc.material_id, hit.uv);
         if (bounce == 0) res.world_normal = hit.normal;
         const V3 emissive = load3(mat.emissive);
         if (std::sqrt(sqnorm(emissive)) > kEps) {
@@ -1206,6 +1278,51 @@ void denoise_and_tonemap(or_renderer &r) {
 // ------------------------------------------------------------------------------------------------
 // C API
 // ------------------------------------------------------------------------------------------------
+// Emissive triangles for next-event estimation, in instance then face order, world space. A material
+// with an emissive texture varies over the triangle and is reached by BSDF sampling only.
+void build_lights(or_scene *sc) {
+    const uint32_t num_instances = static_cast<uint32_t>(sc->insts.size());
+    sc->lights.clear();
+    sc->light_cdf.clear();
+    sc->light_total = 0.f;
+    sc->inst_light_base.assign(num_instances, SPK_INVALID_ID);
+    for (uint32_t k = 0; k < num_instances; ++k) {
+        const Inst &in = sc->insts[k];
+        if (in.desc.type != SPK_PRIM_MESH) continue;
+        if (material_map(*sc, in.desc.material_id, 2) >= 0) continue;
+        const V3 em = load3(sc->materials[in.desc.material_id].emissive);
+        if (!(std::sqrt(sqnorm(em)) > kEps)) continue;
+        const MeshData &m = sc->meshes[in.desc.mesh_id];
+        sc->inst_light_base[k] = static_cast<uint32_t>(sc->lights.size());
+        for (uint32_t f = 0; f < m.tris.size(); ++f) {
+            const V3 w0 = xform_point(in.M, m.pos[m.idx[3 * f]]);
+            const V3 w1 = xform_point(in.M, m.pos[m.idx[3 * f + 1]]);
+            const V3 w2 = xform_point(in.M, m.pos[m.idx[3 * f + 2]]);
+            or_scene::Light L;
+            L.p0 = w0;
+            L.e1 = w1 - w0;
+            L.e2 = w2 - w0;
+            const V3 c = cross(L.e1, L.e2);
+            const float len = std::sqrt(sqnorm(c));
+            L.area = 0.5f * len;
+            L.ng = len > 0.f ? mk(c.x / len, c.y / len, c.z / len) : mk(0, 0, 0);
+            L.emission = em;
+            sc->lights.push_back(L);
+        }
+    }
+    float acc = 0.f;
+    for (const auto &L : sc->lights) {
+        acc = acc + L.area;
+        sc->light_cdf.push_back(acc);
+    }
+    sc->light_total = acc;
+    if (!(acc > 0.f)) {
+        sc->lights.clear();
+        sc->light_cdf.clear();
+        sc->inst_light_base.assign(num_instances, SPK_INVALID_ID);
+    }
+}
+
 extern "C" {
 
 or_scene *or_scene_create(const spk_mesh *meshes, uint32_t num_meshes, const spk_instance *instances,
@@ -1298,42 +1415,7 @@ or_scene *or_scene_create(const spk_mesh *meshes, uint32_t num_meshes, const spk
     sc->tlas_slot = sc->tlas.prim_ids;
     for (uint32_t i = 0; i < sc->tlas.prim_ids.size(); ++i) sc->tlas.prim_ids[i] = i;
     sc->materials.assign(materials, materials + num_materials);
-    // Emissive triangles for next-event estimation, in instance then face order, world space.
-    sc->inst_light_base.assign(num_instances, SPK_INVALID_ID);
-    for (uint32_t k = 0; k < num_instances; ++k) {
-        const Inst &in = sc->insts[k];
-        if (in.desc.type != SPK_PRIM_MESH) continue;
-        const V3 em = load3(sc->materials[in.desc.material_id].emissive);
-        if (!(std::sqrt(sqnorm(em)) > kEps)) continue;
-        const MeshData &m = sc->meshes[in.desc.mesh_id];
-        sc->inst_light_base[k] = static_cast<uint32_t>(sc->lights.size());
-        for (uint32_t f = 0; f < m.tris.size(); ++f) {
-            const V3 w0 = xform_point(in.M, m.pos[m.idx[3 * f]]);
-            const V3 w1 = xform_point(in.M, m.pos[m.idx[3 * f + 1]]);
-            const V3 w2 = xform_point(in.M, m.pos[m.idx[3 * f + 2]]);
-            or_scene::Light L;
-            L.p0 = w0;
-            L.e1 = w1 - w0;
-            L.e2 = w2 - w0;
-            const V3 c = cross(L.e1, L.e2);
-            const float len = std::sqrt(sqnorm(c));
-            L.area = 0.5f * len;
-            L.ng = len > 0.f ? mk(c.x / len, c.y / len, c.z / len) : mk(0, 0, 0);
-            L.emission = em;
-            sc->lights.push_back(L);
-        }
-    }
-    float acc = 0.f;
-    for (const auto &L : sc->lights) {
-        acc = acc + L.area;
-        sc->light_cdf.push_back(acc);
-    }
-    sc->light_total = acc;
-    if (!(acc > 0.f)) {
-        sc->lights.clear();
-        sc->light_cdf.clear();
-        sc->inst_light_base.assign(num_instances, SPK_INVALID_ID);
-    }
+    build_lights(sc);
     if (sky) {
         sc->sky = *sky;
         if (sky->mode == SPK_SKY_CUBE && sky->cube_rgba) {
@@ -1496,7 +1578,7 @@ void or_guides(const or_renderer *r, float *normal_depth, float *albedo_hit) {
                 for (int c = 0; c < 4; ++c) nd[c] = al[c] = 0.f;
                 continue;
             }
-            const spk_material &mat = sc.materials[sc.insts[hit.prim].desc.material_id];
+            const spk_material mat = resolve_material(sc, sc.insts[hit.prim].desc.material_id, hit.uv);
             const V3 n = normalized(hit.normal);
             nd[0] = n.x;
             nd[1] = n.y;
@@ -1508,6 +1590,23 @@ void or_guides(const or_renderer *r, float *normal_depth, float *albedo_hit) {
             al[3] = std::sqrt(sqnorm(load3(mat.emissive))) > kEps ? 2.f : 1.f;
         }
     }
+}
+
+void or_scene_set_textures(or_scene *sc, const spk_texture *textures, uint32_t num_textures,
+                           const spk_material_maps *maps) {
+    sc->textures.clear();
+    for (uint32_t k = 0; k < num_textures; ++k) {
+        or_scene::Tex T{textures[k].width, textures[k].height, textures[k].srgb ? 1u : 0u, {}};
+        const size_t n = static_cast<size_t>(T.w) * T.h;
+        T.px.resize(n);
+        for (size_t i = 0; i < n; ++i)
+            T.px[i] = V4{textures[k].rgba[4 * i], textures[k].rgba[4 * i + 1], textures[k].rgba[4 * i + 2],
+                         textures[k].rgba[4 * i + 3]};
+        sc->textures.push_back(std::move(T));
+    }
+    sc->maps.clear();
+    if (maps) sc->maps.assign(maps, maps + sc->materials.size());
+    build_lights(sc);
 }
 
 void or_counts(const or_renderer *r, uint64_t *extension_rays, uint64_t *shadow_rays, uint64_t *paths) {

@@ -52,6 +52,8 @@ void or_read_framebuffer(const or_renderer *r, float *hdr_rgba, uint16_t *rgba16
 /* Per-pixel G-buffer of the last frame: color (rgb, valid flag) and first-hit world normal. */
 void or_read_gbuffer(const or_renderer *r, float *color_rgba, float *world_normal);
 void or_guides(const or_renderer *r, float *normal_depth, float *albedo_hit);
+void or_scene_set_textures(or_scene *sc, const spk_texture *textures, uint32_t num_textures,
+                           const spk_material_maps *maps);
 void or_counts(const or_renderer *r, uint64_t *extension_rays, uint64_t *shadow_rays, uint64_t *paths);
 void or_sample_counts(const or_renderer *r, uint32_t *cumulated, uint32_t *dispatched);
 

@@ -79,9 +79,19 @@ class spk_tuning(C.Structure):
                 ("ray_sort", _u32), ("bvh_collapse", _u32)]
 
 
+class spk_texture(C.Structure):
+    _fields_ = [("width", _u32), ("height", _u32), ("srgb", _u32), ("rgba", C.POINTER(C.c_float))]
+
+
+class spk_material_maps(C.Structure):
+    _fields_ = [("base_color", C.c_int32), ("metallic_roughness", C.c_int32), ("emissive", C.c_int32),
+                ("normal", C.c_int32)]
+
+
 class spk_scene_desc(C.Structure):
     _fields_ = [("meshes", C.c_void_p), ("num_meshes", _u32), ("instances", C.c_void_p), ("num_instances", _u32),
-                ("materials", C.c_void_p), ("num_materials", _u32), ("sky", C.c_void_p)]
+                ("materials", C.c_void_p), ("num_materials", _u32), ("sky", C.c_void_p), ("textures", C.c_void_p),
+                ("num_textures", _u32), ("maps", C.c_void_p)]
 
 
 class spk_request(C.Structure):
@@ -149,6 +159,11 @@ class Material:
     roughness: float = 1.0
     eta: float = 0.0
     dielectric: bool = False
+    # texture maps: indices into Scene.textures, -1 for none (MaterialResource's *_texture fields)
+    base_color_tex: int = -1
+    metallic_roughness_tex: int = -1
+    emissive_tex: int = -1
+    normal_tex: int = -1
 
     @staticmethod
     def lambertian(color):
@@ -170,6 +185,19 @@ class Material:
 
 
 @dataclass
+class Texture:
+    """An Image2D's texels as float RGBA (8-bit data divided by 255), row y = v * height; `srgb` decodes
+    after the bilinear filter."""
+    rgba: np.ndarray  # (H, W, 4) float32
+    srgb: bool = False
+
+    def __post_init__(self):
+        self.rgba = np.ascontiguousarray(self.rgba, dtype=np.float32)
+        if self.rgba.ndim != 3 or self.rgba.shape[2] != 4:
+            raise ValueError("texture texels must be (H, W, 4)")
+
+
+@dataclass
 class Sky:
     mode: int = SPK_SKY_NONE
     color: tuple = (0.0, 0.0, 0.0)
@@ -183,6 +211,7 @@ class Scene:
     materials: List[Material]
     sky: Sky = field(default_factory=Sky)
     name: str = "scene"
+    textures: List[Texture] = field(default_factory=list)
 
     @property
     def num_triangles(self) -> int:
@@ -248,10 +277,28 @@ class MarshalledScene:
             self.sky.cube_size = self._cube.shape[1]
             self.sky.cube_rgba = _ptr(self._cube, C.c_float)
 
+        self.textures = (spk_texture * max(1, len(scene.textures)))()
+        for k, t in enumerate(scene.textures):
+            h, w, _ = t.rgba.shape
+            self.textures[k] = spk_texture(w, h, 1 if t.srgb else 0, _ptr(t.rgba, C.c_float))
+        self.has_maps = any(m.base_color_tex >= 0 or m.metallic_roughness_tex >= 0 or m.emissive_tex >= 0 or
+                            m.normal_tex >= 0 for m in scene.materials)
+        self.maps = (spk_material_maps * max(1, len(scene.materials)))()
+        for k, m in enumerate(scene.materials):
+            self.maps[k] = spk_material_maps(m.base_color_tex, m.metallic_roughness_tex, m.emissive_tex, m.normal_tex)
+
     def args(self):
         s = self.scene
         return (self.meshes, len(s.meshes), self.instances, len(s.instances), self.materials, len(s.materials),
                 C.byref(self.sky))
+
+    def desc(self) -> "spk_scene_desc":
+        """spk_scene_desc of this scene (with its textures and maps)."""
+        a = self.args()
+        s = self.scene
+        return spk_scene_desc(C.cast(a[0], C.c_void_p), a[1], C.cast(a[2], C.c_void_p), a[3], C.cast(a[4], C.c_void_p),
+                              a[5], C.cast(a[6], C.c_void_p), C.cast(self.textures, C.c_void_p), len(s.textures),
+                              C.cast(self.maps, C.c_void_p) if self.has_maps else None)
 
 
 def rays_to_array(origins: np.ndarray, directions: np.ndarray) -> np.ndarray:

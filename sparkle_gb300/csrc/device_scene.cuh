@@ -26,10 +26,17 @@ struct alignas(16) DevInstance {
     float radius;
     uint32_t vert_base;  // first vertex of the mesh in `verts`
     uint32_t face_base;  // first face of the mesh in `faces`
-    uint32_t mesh_id;
+    uint32_t normal_map;  // the material's normal-map texture (kInvalid for none), read with the instance
     uint32_t light_base;  // first entry of this instance's triangles in `lights`, kInvalid if it does not emit
 };
 static_assert(sizeof(DevInstance) == 128, "DevInstance is 128 bytes");
+
+// A texture in the shared texel array (Image2D, io/Image.h:112-150).
+struct DevTexture {
+    uint32_t offset;  // first texel in `texels`
+    uint32_t width, height;
+    uint32_t srgb;
+};
 
 struct alignas(16) DevMaterial {
     float base[3];
@@ -37,8 +44,11 @@ struct alignas(16) DevMaterial {
     float emissive[3];
     uint32_t is_emissive;  // ||emissive|| > Eps, evaluated once on the host exactly as SamplePixel does
     float metallic, roughness, eta, pad;
+    // texture maps (indices into DevScene::textures, kInvalid for none): base colour, metallic-roughness,
+    // emissive, normal
+    uint32_t tex_base, tex_mr, tex_emissive, tex_normal;
 };
-static_assert(sizeof(DevMaterial) == 48, "DevMaterial is 48 bytes");
+static_assert(sizeof(DevMaterial) == 64, "DevMaterial is 64 bytes");
 
 // An emissive triangle in world space for next-event estimation (64 B).
 struct alignas(16) DevLight {
@@ -77,6 +87,8 @@ struct DevScene {
     uint32_t sky_size;
     float sky_color[3];
     float scene_abs_x;  // max |x| over world bounds; bounds the x-only world-t error used for pruning
+    const DevTexture *textures;  // all scenes' textures
+    const float4 *texels;        // their texels, texture after texture
     const DevSceneDesc *descs;  // every scene of the context (the fields above are scene 0's)
     uint32_t num_scenes;
     float box_lo[3];     // world bounds of all scenes (ray sort cells)

@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(128) k_render_mega(DevScene S, DevCamera cam, 
                 break;
             }
             const Surface surf = make_surface(S, hit, o, d);
-            const DevMaterial mat = S.materials[surf.material];
+            const DevMaterial mat = resolve_material(S, S.materials[surf.material], surf.uv);
             if (bounce == 0) first_normal = surf.normal;
             if (mat.is_emissive) {
                 f3 c = cmul(mk3(mat.emissive[0], mat.emissive[1], mat.emissive[2]), thr);
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(128) k_guides(DevScene S, DevCamera cam, uint3
         return;
     }
     const Surface surf = make_surface(S, hit, o, d);
-    const DevMaterial mat = S.materials[surf.material];
+    const DevMaterial mat = resolve_material(S, S.materials[surf.material], surf.uv);
     const f3 n = normalized(surf.normal);
     const f3 front = normalized(cross(mk3(cam.max_v[0], cam.max_v[1], cam.max_v[2]), mk3(cam.max_u[0], cam.max_u[1], cam.max_u[2])));
     nd[pix] = make_float4(n.x, n.y, n.z, dot3(surf.location - o, front));

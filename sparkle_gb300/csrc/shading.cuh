@@ -108,6 +108,59 @@ struct Surface {
     uint32_t material;
 };
 
+// Image2D::Sample (io/Image.h:112-150): bilinear with wrap at uv * size, the integer part truncated toward
+// zero (utilities::Decompose), u lerp then v lerp, sRGB decoded after the filter.
+__device__ __forceinline__ unsigned wrap_texel(int a, unsigned b) {
+    return (static_cast<unsigned>(a % static_cast<int>(b)) + b) % b;  // utilities::WrapMod
+}
+
+__device__ __forceinline__ float srgb_decode(float c) {  // utilities::SRGBtoLinear per channel
+    return c < 0.04045f ? c / 12.92f : powf((c + 0.055f) / 1.055f, 2.4f);
+}
+
+__device__ __forceinline__ f3 tex_sample(const DevScene &S, uint32_t t, const float uv[2]) {
+    const DevTexture T = S.textures[t];
+    const float px = uv[0] * static_cast<float>(T.width), py = uv[1] * static_cast<float>(T.height);
+    const int ui = static_cast<int>(px), vi = static_cast<int>(py);
+    const float uc = px - static_cast<float>(ui), vc = py - static_cast<float>(vi);
+    const unsigned x0 = wrap_texel(ui, T.width), x1 = wrap_texel(ui + 1, T.width);
+    const unsigned y0 = wrap_texel(vi, T.height), y1 = wrap_texel(vi + 1, T.height);
+    const float4 *px4 = S.texels + T.offset;
+    const float4 s00 = __ldg(px4 + y0 * T.width + x0), s10 = __ldg(px4 + y0 * T.width + x1);
+    const float4 s01 = __ldg(px4 + y1 * T.width + x0), s11 = __ldg(px4 + y1 * T.width + x1);
+    const f3 l0 = mk3(s00.x + (s10.x - s00.x) * uc, s00.y + (s10.y - s00.y) * uc, s00.z + (s10.z - s00.z) * uc);
+    const f3 l1 = mk3(s01.x + (s11.x - s01.x) * uc, s01.y + (s11.y - s01.y) * uc, s01.z + (s11.z - s01.z) * uc);
+    f3 r = mk3(l0.x + (l1.x - l0.x) * vc, l0.y + (l1.y - l0.y) * vc, l0.z + (l1.z - l0.z) * vc);
+    if (T.srgb) r = mk3(srgb_decode(r.x), srgb_decode(r.y), srgb_decode(r.z));
+    return r;
+}
+
+// Per-hit material values: texture x factor (MaterialRenderProxy::GetBaseColor / GetMetallic / GetRoughness /
+// GetEmissive, MaterialRenderProxy.h:117-160); a textured emission is tested per hit with SamplePixel's
+// `norm() > Eps` (CPURenderer.cpp:286-287).
+__device__ __forceinline__ DevMaterial resolve_material(const DevScene &S, const DevMaterial &m, const float uv[2]) {
+    DevMaterial r = m;
+    if (m.tex_base != kInvalid) {
+        const f3 t = tex_sample(S, m.tex_base, uv);
+        r.base[0] = t.x * m.base[0];
+        r.base[1] = t.y * m.base[1];
+        r.base[2] = t.z * m.base[2];
+    }
+    if (m.tex_mr != kInvalid) {
+        const f3 t = tex_sample(S, m.tex_mr, uv);
+        r.metallic = t.z * m.metallic;
+        r.roughness = t.y * m.roughness;
+    }
+    if (m.tex_emissive != kInvalid) {
+        const f3 t = tex_sample(S, m.tex_emissive, uv);
+        r.emissive[0] = t.x * m.emissive[0];
+        r.emissive[1] = t.y * m.emissive[1];
+        r.emissive[2] = t.z * m.emissive[2];
+        r.is_emissive = sqrtf(sqnorm(mk3(r.emissive[0], r.emissive[1], r.emissive[2]))) > kEps ? 1u : 0u;
+    }
+    return r;
+}
+
 // GetIntersection + Intersection::Update for the winning candidate.
 __device__ __forceinline__ Surface make_surface(const DevScene &S, const TraceResult &hit, f3 o, f3 d) {
     Surface s;
@@ -137,8 +190,18 @@ __device__ __forceinline__ Surface make_surface(const DevScene &S, const TraceRe
         const float u = hit.u, v = hit.v;
         s.uv[0] = lerp3(b0.w, b1.w, b2.w, u, v);
         s.uv[1] = lerp3(c0.x, c1.x, c2.x, u, v);
-        const f3 sn = mk3(lerp3(a0.x, a1.x, a2.x, u, v), lerp3(a0.y, a1.y, a2.y, u, v), lerp3(a0.z, a1.z, a2.z, u, v));
+        f3 sn = mk3(lerp3(a0.x, a1.x, a2.x, u, v), lerp3(a0.y, a1.y, a2.y, u, v), lerp3(a0.z, a1.z, a2.z, u, v));
         const f3 tg = mk3(lerp3(a0.w, a1.w, a2.w, u, v), lerp3(b0.x, b1.x, b2.x, u, v), lerp3(b0.y, b1.y, b2.y, u, v));
+        const uint32_t nmap = I.normal_map;
+        if (nmap != kInvalid) {
+            // Normal map in the vertex tangent frame (MeshRenderProxy.cpp:349-355, TangentSpaceToWorldSpace,
+            // Utilities.h:403-409): tangent-space normal = texel * 2 - 1.
+            const float tw = lerp3(b0.z, b1.z, b2.z, u, v);
+            const f3 t = tex_sample(S, nmap, s.uv);
+            const f3 tn = mk3(t.x * 2.f - 1.f, t.y * 2.f - 1.f, t.z * 2.f - 1.f);
+            const f3 bi = cross(sn, tg) * tw;
+            sn = normalized(tg * tn.x + bi * tn.y + sn * tn.z);
+        }
         s.normal = normalized(xform_dir(I.m, sn));
         s.tangent = xform_dir(I.m, tg);
     }

@@ -69,6 +69,8 @@ struct spk_ctx {
     DevBuf<DevLight> lights;
     DevBuf<float> light_cdf;
     DevBuf<DevSceneDesc> scene_descs;
+    DevBuf<DevTexture> textures;
+    DevBuf<float4> texels;
     DevScene scene{};
     bool has_scene = false;
     uint32_t bvh_nodes = 0;
@@ -222,6 +224,8 @@ struct HostScene {
     std::vector<float4> cube;
     std::vector<DevLight> lights;
     std::vector<float> light_cdf;
+    std::vector<DevTexture> textures;
+    std::vector<float4> texels;
     uint32_t tlas_root = kInvalid;
     uint32_t sky_mode = SPK_SKY_NONE, sky_size = 0;
     float sky_color[3] = {0.f, 0.f, 0.f};
@@ -236,7 +240,8 @@ struct HostScene {
 // records, materials, emissive-triangle light table, sky texels), with indices local to the scene.
 spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_meshes, const spk_instance *instances,
                             uint32_t num_instances, const spk_material *materials, uint32_t num_materials,
-                            const spk_sky *sky, HostScene &hs) {
+                            const spk_sky *sky, const spk_texture *textures, uint32_t num_textures,
+                            const spk_material_maps *maps, HostScene &hs) {
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     if ((num_meshes && !meshes) || (num_instances && !instances) || (num_materials && !materials))
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "null scene array");
@@ -261,7 +266,26 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
             return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: material_id out of range", k);
     }
     if (sky && sky->mode == SPK_SKY_CUBE && (!sky->cube_rgba || sky->cube_size == 0))
-        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "hs.cube sky without texels");
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "cube sky without texels");
+    if (num_textures && !textures) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "null texture array");
+    for (uint32_t k = 0; k < num_textures; ++k)
+        if (textures[k].width == 0 || textures[k].height == 0 || !textures[k].rgba)
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "texture %u: empty", k);
+    if (maps) {
+        for (uint32_t k = 0; k < num_materials; ++k) {
+            const int32_t t[4] = {maps[k].base_color, maps[k].metallic_roughness, maps[k].emissive, maps[k].normal};
+            for (int32_t i : t)
+                if (i < -1 || i >= static_cast<int32_t>(num_textures))
+                    return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "material %u: texture index %d out of range", k, i);
+        }
+    }
+    for (uint32_t k = 0; k < num_textures; ++k) {
+        const spk_texture &t = textures[k];
+        hs.textures.push_back(DevTexture{static_cast<uint32_t>(hs.texels.size()), t.width, t.height, t.srgb ? 1u : 0u});
+        const size_t nt = static_cast<size_t>(t.width) * t.height;
+        for (size_t i = 0; i < nt; ++i)
+            hs.texels.push_back(make_float4(t.rgba[4 * i], t.rgba[4 * i + 1], t.rgba[4 * i + 2], t.rgba[4 * i + 3]));
+    }
 
     // BLAS per mesh: binned SAH BVH2 (<= 3 triangles per leaf) collapsed to 8-wide nodes.
     std::vector<uint32_t> blas_root(num_meshes, kInvalid);
@@ -337,7 +361,7 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
         d.type = in.type;
         d.material = in.material_id;
         d.radius = in.radius;
-        d.mesh_id = in.mesh_id;
+        d.normal_map = kInvalid;  // set once the materials are built
         if (in.type == SPK_PRIM_SPHERE) {
             d.blas_root = kInvalid;
             const double r = std::fabs(static_cast<double>(in.radius));
@@ -387,13 +411,24 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
         d.metallic = s.metallic;
         d.roughness = s.roughness;
         d.eta = s.eta;
+        auto tex = [](int32_t i) { return i < 0 ? kInvalid : static_cast<uint32_t>(i); };
+        d.tex_base = maps ? tex(maps[k].base_color) : kInvalid;
+        d.tex_mr = maps ? tex(maps[k].metallic_roughness) : kInvalid;
+        d.tex_emissive = maps ? tex(maps[k].emissive) : kInvalid;
+        d.tex_normal = maps ? tex(maps[k].normal) : kInvalid;
     }
     // Emissive triangles of mesh instances in world space (instance then face order) and their area CDF,
     // for next-event estimation.
     for (uint32_t k = 0; k < num_instances; ++k) hs.insts[k].light_base = kInvalid;
     for (uint32_t k = 0; k < num_instances; ++k) {
         const spk_instance &in = instances[k];
-        if (in.type != SPK_PRIM_MESH || !hs.mats[in.material_id].is_emissive) continue;
+        for (uint32_t k = 0; k < num_instances; ++k)
+        if (instances[k].type == SPK_PRIM_MESH) hs.insts[k].normal_map = hs.mats[instances[k].material_id].tex_normal;
+    // A textured emission varies over the triangle: such emitters are reached by BSDF sampling only
+        // (no light-table entry, so their hits take the full emission).
+        if (in.type != SPK_PRIM_MESH || !hs.mats[in.material_id].is_emissive ||
+            hs.mats[in.material_id].tex_emissive != kInvalid)
+            continue;
         const spk_mesh &m = meshes[in.mesh_id];
         hs.insts[k].light_base = static_cast<uint32_t>(hs.lights.size());
         for (uint32_t f = 0; f < m.num_faces; ++f) {
@@ -466,11 +501,23 @@ void append_scene(HostScene &all, const HostScene &s, DevSceneDesc &d) {
         in.vert_base += vert_off;
         in.face_base += face_off;
         in.material += mat_off;
+        if (in.normal_map != kInvalid) in.normal_map += static_cast<uint32_t>(all.textures.size());
         all.insts.push_back(in);  // light_base stays relative to the scene's light slice
     }
     all.verts.insert(all.verts.end(), s.verts.begin(), s.verts.end());
     all.faces.insert(all.faces.end(), s.faces.begin(), s.faces.end());
-    all.mats.insert(all.mats.end(), s.mats.begin(), s.mats.end());
+    const uint32_t tex_off = static_cast<uint32_t>(all.textures.size());
+    const uint32_t texel_off = static_cast<uint32_t>(all.texels.size());
+    for (DevMaterial m : s.mats) {
+        for (uint32_t *t : {&m.tex_base, &m.tex_mr, &m.tex_emissive, &m.tex_normal})
+            if (*t != kInvalid) *t += tex_off;
+        all.mats.push_back(m);
+    }
+    for (DevTexture t : s.textures) {
+        t.offset += texel_off;
+        all.textures.push_back(t);
+    }
+    all.texels.insert(all.texels.end(), s.texels.begin(), s.texels.end());
     d = DevSceneDesc{};
     d.tlas_root = s.tlas_root == kInvalid ? kInvalid : s.tlas_root + node_off;
     d.sky_mode = s.sky_mode;
@@ -506,7 +553,9 @@ spk_status upload_scene(spk_ctx *ctx, const HostScene &hs, const std::vector<Dev
         (e = upload(ctx->sky, hs.cube.data(), hs.cube.size(), ctx->stream)) != cudaSuccess ||
         (e = upload(ctx->lights, hs.lights.data(), hs.lights.size(), ctx->stream)) != cudaSuccess ||
         (e = upload(ctx->light_cdf, hs.light_cdf.data(), hs.light_cdf.size(), ctx->stream)) != cudaSuccess ||
-        (e = upload(ctx->scene_descs, descs.data(), descs.size(), ctx->stream)) != cudaSuccess) {
+        (e = upload(ctx->scene_descs, descs.data(), descs.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->textures, hs.textures.data(), hs.textures.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->texels, hs.texels.data(), hs.texels.size(), ctx->stream)) != cudaSuccess) {
         return cuda_fail(ctx, e, "scene upload");
     }
     DevScene &S = ctx->scene;
@@ -522,6 +571,8 @@ spk_status upload_scene(spk_ctx *ctx, const HostScene &hs, const std::vector<Dev
     S.lights = ctx->lights.ptr;
     S.light_cdf = ctx->light_cdf.ptr;
     S.descs = ctx->scene_descs.ptr;
+    S.textures = ctx->textures.ptr;
+    S.texels = ctx->texels.ptr;
     S.num_scenes = static_cast<uint32_t>(descs.size());
     for (int a = 0; a < 3; ++a) {
         const bool ok = hs.hi[a] > hs.lo[a];
@@ -586,6 +637,8 @@ spk_status spk_destroy(spk_ctx *ctx) {
     ctx->lights.reset();
     ctx->light_cdf.reset();
     ctx->scene_descs.reset();
+    ctx->textures.reset();
+    ctx->texels.reset();
     ctx->gcolor.reset();
     ctx->gnormal.reset();
     ctx->guide_nd.reset();
@@ -613,7 +666,8 @@ spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_mesh
                          uint32_t num_instances, const spk_material *materials, uint32_t num_materials,
                          const spk_sky *sky) {
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
-    const spk_scene_desc d{meshes, num_meshes, instances, num_instances, materials, num_materials, sky};
+    const spk_scene_desc d{meshes, num_meshes, instances, num_instances, materials, num_materials, sky,
+                           nullptr, 0, nullptr};
     return spk_set_scenes(ctx, &d, 1);
 }
 
@@ -628,7 +682,8 @@ spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t n
         const spk_scene_desc &d = scenes[k];
         HostScene hs;
         const spk_status st = build_host_scene(ctx, d.meshes, d.num_meshes, d.instances, d.num_instances,
-                                               d.materials, d.num_materials, d.sky, hs);
+                                               d.materials, d.num_materials, d.sky, d.textures, d.num_textures,
+                                               d.maps, hs);
         if (st != SPK_OK) {
             if (num_scenes > 1) ctx->error = "scene " + std::to_string(k) + ": " + ctx->error;
             return st;

@@ -102,7 +102,7 @@ __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontSta
     } else {
         const TraceResult h{hit4.x, hit4.y, hit4.z, inst, s.hit_face[pid]};
         const Surface surf = make_surface(S, h, o, d);
-        const DevMaterial mat = S.materials[surf.material];
+        const DevMaterial mat = resolve_material(S, S.materials[surf.material], surf.uv);
         if (bounce == 0 && gnormal) gnormal[pid] = make_float4(surf.normal.x, surf.normal.y, surf.normal.z, 0.f);
         if (mat.is_emissive) {
             f3 c = cmul(mk3(mat.emissive[0], mat.emissive[1], mat.emissive[2]), thr);

@@ -7,7 +7,8 @@ What the reference does and this module mirrors:
 * Materials (LoadMaterials, GLTFLoader.cpp:475-526): a factor is read only when its texture is present --
   base colour with baseColorTexture, metallic/roughness with metallicRoughnessTexture, emissive with
   emissiveTexture -- otherwise MaterialResource's defaults apply (base colour 1, emissive 0, metallic 1,
-  roughness 1; io/Material.h:9-14). Textures themselves are not sampled yet (the factors are kept).
+  roughness 1; io/Material.h:9-14). Textures (PNG images, embedded or external) become Scene textures:
+  base colour and emissive as sRGB, metallic-roughness and normal maps as linear data.
 * Nodes (ProcessNode, GLTFLoader.cpp:528-575): rotation = 90 degrees about +X times the node's quaternion
   (glTF is y-up, Sparkle z-up), applied at every node including children; the node's scale is baked into
   its vertex positions only (LoadPositionArray, :192-230) and the node transform keeps scale 1; local =
@@ -29,10 +30,11 @@ import base64
 import json
 import os
 import struct
+import zlib
 
 import numpy as np
 
-from .abi import Instance, Material, Mesh, Scene, Sky
+from .abi import Instance, Material, Mesh, Scene, Sky, Texture
 
 _COMPONENT = {5120: np.int8, 5121: np.uint8, 5122: np.int16, 5123: np.uint16, 5125: np.uint32, 5126: np.float32}
 _NCOMP = {"SCALAR": 1, "VEC2": 2, "VEC3": 3, "VEC4": 4, "MAT2": 4, "MAT3": 9, "MAT4": 16}
@@ -90,6 +92,72 @@ def _accessor(doc, buffers, index):
     return arr.copy()
 
 
+def decode_png(data: bytes) -> np.ndarray:
+    """8-bit non-interlaced PNG (grey, grey+alpha, RGB, RGBA) -> (H, W, 4) float32 in [0, 1] (ColorToVec)."""
+    if data[:8] != b"\x89PNG\r\n\x1a\n":
+        raise ValueError("not a PNG image (only PNG textures are decoded)")
+    off, idat = 8, []
+    w = h = ctype = None
+    while off < len(data):
+        n, = struct.unpack(">I", data[off:off + 4])
+        kind = data[off + 4:off + 8]
+        body = data[off + 8:off + 8 + n]
+        off += 12 + n
+        if kind == b"IHDR":
+            w, h, depth, ctype, _, _, interlace = struct.unpack(">IIBBBBB", body)
+            if depth != 8 or interlace != 0 or ctype not in (0, 2, 4, 6):
+                raise ValueError("only 8-bit non-interlaced grey/RGB(A) PNGs are decoded")
+        elif kind == b"IDAT":
+            idat.append(body)
+        elif kind == b"IEND":
+            break
+    ch = {0: 1, 2: 3, 4: 2, 6: 4}[ctype]
+    raw = np.frombuffer(zlib.decompress(b"".join(idat)), np.uint8).reshape(h, 1 + w * ch)
+    out = np.zeros((h, w * ch), np.int32)
+    prev = np.zeros(w * ch, np.int32)
+    for y in range(h):
+        f, line = raw[y, 0], raw[y, 1:].astype(np.int32)
+        cur = np.zeros(w * ch, np.int32)
+        for x in range(w * ch):
+            a = cur[x - ch] if x >= ch else 0
+            b = prev[x]
+            c = prev[x - ch] if x >= ch else 0
+            if f == 0:
+                pred = 0
+            elif f == 1:
+                pred = a
+            elif f == 2:
+                pred = b
+            elif f == 3:
+                pred = (a + b) // 2
+            else:  # Paeth
+                pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
+                pred = a if pa <= pb and pa <= pc else (b if pb <= pc else c)
+            cur[x] = (line[x] + pred) & 0xFF
+        out[y] = cur
+        prev = cur
+    px = out.reshape(h, w, ch).astype(np.float32) / 255.0
+    rgba = np.ones((h, w, 4), np.float32)
+    if ch in (1, 2):
+        rgba[..., :3] = px[..., :1]
+    else:
+        rgba[..., :3] = px[..., :3]
+    if ch in (2, 4):
+        rgba[..., 3] = px[..., -1]
+    return rgba
+
+
+def _image_bytes(doc, buffers, base_dir, image):
+    if "bufferView" in image:
+        v = doc["bufferViews"][image["bufferView"]]
+        start = v.get("byteOffset", 0)
+        return bytes(buffers[v["buffer"]][start:start + v["byteLength"]])
+    uri = image["uri"]
+    if uri.startswith("data:"):
+        return base64.b64decode(uri.split(",", 1)[1])
+    return open(os.path.join(base_dir, uri), "rb").read()
+
+
 def _quat_matrix(q):
     """3x3 rotation of a glTF quaternion [x, y, z, w] (normalised first)."""
     x, y, z, w = (float(v) for v in q)
@@ -108,19 +176,26 @@ def default_material() -> Material:
     return Material((1.0, 1.0, 1.0), (0.0, 0.0, 0.0), 1.0, 1.0, 0.0, False)
 
 
-def _material(m) -> Material:
+def _material(m, texture) -> Material:
+    """`texture(index, srgb)` returns the Scene texture index of glTF texture `index` (decoding it once)."""
     mat = default_material()
     pbr = m.get("pbrMetallicRoughness", {})
     base, emissive = mat.base_color, mat.emissive
     metallic, roughness = mat.metallic, mat.roughness
+    maps = dict(base_color_tex=-1, metallic_roughness_tex=-1, emissive_tex=-1, normal_tex=-1)
     if pbr.get("baseColorTexture", {}).get("index", -1) >= 0:
         base = tuple(float(v) for v in pbr.get("baseColorFactor", [1, 1, 1, 1])[:3])
+        maps["base_color_tex"] = texture(pbr["baseColorTexture"]["index"], True)
+    if m.get("normalTexture", {}).get("index", -1) >= 0:
+        maps["normal_tex"] = texture(m["normalTexture"]["index"], False)
     if pbr.get("metallicRoughnessTexture", {}).get("index", -1) >= 0:
         metallic = float(pbr.get("metallicFactor", 1.0))
         roughness = float(pbr.get("roughnessFactor", 1.0))
+        maps["metallic_roughness_tex"] = texture(pbr["metallicRoughnessTexture"]["index"], False)
     if m.get("emissiveTexture", {}).get("index", -1) >= 0:
         emissive = tuple(float(v) for v in m.get("emissiveFactor", [0, 0, 0])[:3])
-    return Material(base, emissive, metallic, roughness, 0.0, False)
+        maps["emissive_tex"] = texture(m["emissiveTexture"]["index"], True)
+    return Material(base, emissive, metallic, roughness, 0.0, False, **maps)
 
 
 def _vertex_normals(pos, idx):
@@ -161,7 +236,19 @@ def load_gltf(path: str, sky: Sky | None = None) -> Scene:
     """Reads a .gltf (JSON with external or data-URI buffers) or .glb file into a Scene."""
     doc, bin_chunk = _read_container(path)
     buffers = _buffers(doc, os.path.dirname(os.path.abspath(path)), bin_chunk)
-    materials = [_material(m) for m in doc.get("materials", [])]
+    base_dir = os.path.dirname(os.path.abspath(path))
+    textures, tex_index = [], {}
+
+    def texture(index, srgb):
+        # CreateTexture (GLTFLoader.cpp:273-327): colour maps are sRGB, normal and metallic-roughness data
+        key = (index, srgb)
+        if key not in tex_index:
+            image = doc["images"][doc["textures"][index]["source"]]
+            textures.append(Texture(decode_png(_image_bytes(doc, buffers, base_dir, image)), srgb=srgb))
+            tex_index[key] = len(textures) - 1
+        return tex_index[key]
+
+    materials = [_material(m, texture) for m in doc.get("materials", [])]
     default_index = None
     meshes, instances = [], []
 
@@ -198,4 +285,4 @@ def load_gltf(path: str, sky: Sky | None = None) -> Scene:
         roots = list(range(len(doc.get("nodes", []))))
     for r in roots:
         process(r, np.eye(4))
-    return Scene(meshes, instances, materials, sky or Sky(), name=os.path.basename(path))
+    return Scene(meshes, instances, materials, sky or Sky(), name=os.path.basename(path), textures=textures)

@@ -140,9 +140,13 @@ class Context:
 
     def set_scene(self, scene: Scene):
         m = MarshalledScene(scene)
-        a = m.args()
-        self._check(self.L.spk_set_scene(self.h, C.cast(a[0], C.c_void_p), a[1], C.cast(a[2], C.c_void_p), a[3],
-                                         C.cast(a[4], C.c_void_p), a[5], C.cast(a[6], C.c_void_p)))
+        if scene.textures or m.has_maps:  # spk_set_scene has no texture arguments
+            d = m.desc()
+            self._check(self.L.spk_set_scenes(self.h, C.byref(d), 1))
+        else:
+            a = m.args()
+            self._check(self.L.spk_set_scene(self.h, C.cast(a[0], C.c_void_p), a[1], C.cast(a[2], C.c_void_p), a[3],
+                                             C.cast(a[4], C.c_void_p), a[5], C.cast(a[6], C.c_void_p)))
         self._scene = m
 
     def set_scenes(self, scenes):
@@ -150,9 +154,7 @@ class Context:
         ms = [MarshalledScene(sc) for sc in scenes]
         descs = (spk_scene_desc * len(ms))()
         for k, m in enumerate(ms):
-            a = m.args()
-            descs[k] = spk_scene_desc(C.cast(a[0], C.c_void_p), a[1], C.cast(a[2], C.c_void_p), a[3],
-                                      C.cast(a[4], C.c_void_p), a[5], C.cast(a[6], C.c_void_p))
+            descs[k] = m.desc()
         self._check(self.L.spk_set_scenes(self.h, descs, len(ms)))
         self._scene = ms
 

@@ -16,7 +16,7 @@ HEADER = os.path.join(ROOT, "include", "spk.h")
 HEADERS = [HEADER, os.path.join(ROOT, "include", "spk_denoise.h")]
 
 STRUCTS = ["spk_mesh", "spk_instance", "spk_material", "spk_sky", "spk_camera", "spk_config", "spk_ray", "spk_hit",
-           "spk_stats", "spk_tuning", "spk_scene_desc", "spk_request"]
+           "spk_stats", "spk_tuning", "spk_scene_desc", "spk_request", "spk_texture", "spk_material_maps"]
 
 
 def header_functions():

@@ -11,6 +11,21 @@ import pytest
 
 from sparkle_gb300 import abi, gltf, scenes
 
+
+def png_bytes(rgba8):
+    """A minimal RGBA PNG (filter 0 rows) for the embedded textures."""
+    import zlib
+    h, w, _ = rgba8.shape
+    raw = b"".join(b"\x00" + rgba8[y].tobytes() for y in range(h))
+
+    def chunk(t, b):
+        return struct.pack(">I", len(b)) + t + b + struct.pack(">I", zlib.crc32(t + b) & 0xFFFFFFFF)
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 0)) +
+            chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b""))
+
+
+TEX = np.array([[[255, 0, 0, 255], [0, 255, 0, 255]], [[0, 0, 255, 255], [255, 255, 255, 128]]], np.uint8)
+
 QUAD_POS = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], np.float32)
 QUAD_NRM = np.tile(np.array([[0, 0, 1]], np.float32), (4, 1))
 
@@ -28,7 +43,9 @@ def build_doc(nodes, scenes_=None, materials=None, prims=None, glb=False):
                  dict(bufferView=3, componentType=5123, count=4, type="SCALAR")]
     prims = prims or [dict(attributes=dict(POSITION=0, NORMAL=1), indices=2, material=0)]
     doc = dict(asset=dict(version="2.0"), bufferViews=views, accessors=accessors, nodes=nodes,
-               meshes=[dict(primitives=prims)], materials=materials or [dict()])
+               meshes=[dict(primitives=prims)], materials=materials or [dict()],
+               images=[dict(uri="data:image/png;base64," + base64.b64encode(png_bytes(TEX)).decode())],
+               textures=[dict(source=0)])
     if scenes_ is not None:
         doc["scenes"] = scenes_
         doc["scene"] = 0
@@ -102,6 +119,10 @@ def test_material_factors_need_their_texture(tmp_path):
     assert m1.base_color == pytest.approx((0.2, 0.3, 0.4)) and (m1.metallic, m1.roughness) == (0.0, 0.5)
     assert m1.emissive == (1.0, 2.0, 3.0)
     assert sc.instances[2].material_id == 2 and sc.materials[2].metallic == 1.0  # default material appended
+    # texture 0 decoded once per colour space: sRGB for base colour / emissive, linear for metallic-roughness
+    assert (m1.base_color_tex, m1.emissive_tex) == (0, 0) and m1.metallic_roughness_tex == 1
+    assert sc.textures[0].srgb and not sc.textures[1].srgb
+    np.testing.assert_allclose(sc.textures[0].rgba, TEX / 255.0, atol=1e-7)
 
 
 @pytest.mark.parametrize("mode,ntri", [(6, 2), (5, 2)])
