@@ -277,6 +277,32 @@ typedef struct spk_scene_desc {
  * spk_set_scenes(&one, 1). */
 spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t num_scenes);
 
+/* Incremental scene changes on a context whose scene came from spk_set_scene (one scene). Each replaces
+ * SceneRenderProxy::UpdateBVH for one kind of PrimitiveChangeType (SceneRenderProxy.cpp:269-297): every
+ * BLAS stays resident, the TLAS, the instance records and the emissive-triangle light table are rebuilt
+ * (on the host: the TLAS is as small as the instance list), and the accumulation is marked dirty. The
+ * result of any sequence of updates equals spk_set_scene with the updated arguments.
+ *
+ * spk_set_instances: New / Remove / Move (index swap) -- the whole instance list, over the resident
+ * meshes and materials. */
+spk_status spk_set_instances(spk_ctx *ctx, const spk_instance *instances, uint32_t num_instances);
+
+/* Update (PrimitiveRenderProxy::IsTransformDirty, SceneRenderProxy.cpp:213-226): new transforms and inverse
+ * transforms (row-major 3x4 each, 12 floats per instance) for instances first .. first + count - 1. */
+spk_status spk_set_instance_transforms(spk_ctx *ctx, uint32_t first, uint32_t count, const float *transforms,
+                                       const float *inv_transforms);
+
+/* No reference counterpart (Sparkle builds a BLAS once per mesh): new vertex positions (and optionally
+ * normals [n][3] and tangents [n][4]) for mesh `mesh_id`, same vertex count and faces. The device rewrites
+ * the mesh's triangle records and refits its BLAS level by level, re-quantising every child box as the
+ * host builder does; then the TLAS is rebuilt. Host or device pointers. */
+spk_status spk_update_mesh(spk_ctx *ctx, uint32_t mesh_id, uint32_t num_vertices, const float *positions,
+                           const float *normals, const float *tangents);
+
+/* The resident BVH node array (80-byte compressed 8-wide nodes: every BLAS, then the TLAS): sets *count to
+ * its length and copies min(capacity, *count) nodes into `nodes` (host or device) when it is not NULL. */
+spk_status spk_read_bvh_nodes(spk_ctx *ctx, void *nodes, uint64_t capacity, uint64_t *count);
+
 /* Replaces CameraRenderProxy::OnTransformDirty/UpdateAttribute (CameraRenderProxy.cpp:118-128): a new
  * camera marks pixels dirty, so the next frame clears the accumulation (CPURenderer.cpp:128-137). */
 spk_status spk_set_camera(spk_ctx *ctx, const spk_camera *camera);

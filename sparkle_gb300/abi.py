@@ -240,6 +240,21 @@ def _ptr(a: Optional[np.ndarray], ctype):
     return a.ctypes.data_as(C.POINTER(ctype))
 
 
+def instance_array(instances):
+    """spk_instance records of a list of Instance (at least one slot, so the pointer is never NULL)."""
+    arr = (spk_instance * max(1, len(instances)))()
+    for k, inst in enumerate(instances):
+        rec = spk_instance()
+        rec.type = SPK_PRIM_SPHERE if inst.sphere else SPK_PRIM_MESH
+        rec.mesh_id = inst.mesh_id
+        rec.material_id = inst.material_id
+        rec.radius = inst.radius
+        rec.transform[:] = inst.transform.reshape(-1).tolist()
+        rec.inv_transform[:] = affine_inverse(inst.transform).reshape(-1).tolist()
+        arr[k] = rec
+    return arr
+
+
 class MarshalledScene:
     """ctypes arrays for spk_set_scene / or_scene_create; keeps the numpy buffers alive."""
 
@@ -250,16 +265,7 @@ class MarshalledScene:
             self.meshes[k] = spk_mesh(_ptr(m.positions, C.c_float), _ptr(m.normals, C.c_float),
                                       _ptr(m.tangents, C.c_float), _ptr(m.uvs, C.c_float),
                                       _ptr(m.indices, C.c_uint32), m.positions.shape[0], m.indices.shape[0])
-        self.instances = (spk_instance * max(1, len(scene.instances)))()
-        for k, inst in enumerate(scene.instances):
-            rec = spk_instance()
-            rec.type = SPK_PRIM_SPHERE if inst.sphere else SPK_PRIM_MESH
-            rec.mesh_id = inst.mesh_id
-            rec.material_id = inst.material_id
-            rec.radius = inst.radius
-            rec.transform[:] = inst.transform.reshape(-1).tolist()
-            rec.inv_transform[:] = affine_inverse(inst.transform).reshape(-1).tolist()
-            self.instances[k] = rec
+        self.instances = instance_array(scene.instances)
         self.materials = (spk_material * max(1, len(scene.materials)))()
         for k, mat in enumerate(scene.materials):
             rec = spk_material()

@@ -21,6 +21,7 @@
 
 #include "../../include/spk.h"
 #include "bvh_builder.h"
+#include "bvh_device.cuh"
 #include "kernels.cuh"
 #include "wavefront.cuh"
 
@@ -37,6 +38,32 @@ struct DevBuf {
         ptr = nullptr;
         count = 0;
     }
+};
+
+// What a mesh's BLAS occupies in the scene arrays; kept to refit it after the vertices move.
+struct MeshBlas {
+    uint32_t root = kInvalid;  // node index of the BLAS root, kInvalid for an empty mesh
+    uint32_t node_count = 0;
+    std::vector<uint32_t> levels;  // first node (relative to root) of each BFS depth, then node_count
+    uint32_t tri_first = 0, tri_count = 0;  // triangle records, in triangles
+    uint32_t vert_base = 0, face_base = 0;
+    double bounds[6] = {0, 0, 0, 0, 0, 0};  // local-space box (lo, hi)
+};
+
+// The instance list, mesh geometry and BLAS placement of a single-scene context, kept on the host so that
+// spk_set_instances / spk_set_instance_transforms / spk_update_mesh can rebuild the TLAS and the light table
+// (SceneRenderProxy::UpdateBVH, SceneRenderProxy.cpp:269-297) without rebuilding any BLAS.
+struct DynScene {
+    bool valid = false;
+    std::vector<spk_instance> instances;
+    std::vector<std::vector<float>> positions;   // per mesh, 3 floats per vertex
+    std::vector<std::vector<uint32_t>> indices;  // per mesh, 3 per face
+    std::vector<MeshBlas> blas;
+    std::vector<DevMaterial> mats;
+    std::vector<DevInstance> insts;
+    DevSceneDesc desc{};
+    uint32_t tlas_root = 0;      // first TLAS node = number of BLAS nodes
+    uint32_t node_capacity = 0;  // nodes allocated on the device
 };
 
 spk_tuning default_tuning() {
@@ -73,6 +100,8 @@ struct spk_ctx {
     DevBuf<float4> texels;
     DevScene scene{};
     bool has_scene = false;
+    DynScene dyn;                          // single-scene contexts: what the incremental updates need
+    DevBuf<float> dyn_pos, dyn_attr, dyn_boxes;  // refit scratch: positions, normals + tangents, node boxes
     uint32_t bvh_nodes = 0;
     uint64_t bvh_bytes = 0;
 
@@ -134,6 +163,23 @@ cudaError_t upload(DevBuf<T> &buf, const T *host, size_t count, cudaStream_t str
     buf.count = count;
     e = cudaMemcpyAsync(buf.ptr, host, count * sizeof(T), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(stream);
+}
+
+// As upload, into an allocation of max(count, capacity) elements (the tail is zeroed).
+template <class T>
+cudaError_t upload_with_capacity(DevBuf<T> &buf, const T *host, size_t count, size_t capacity, cudaStream_t stream) {
+    buf.reset();
+    capacity = std::max(capacity, count);
+    if (capacity == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&buf.ptr, capacity * sizeof(T));
+    if (e != cudaSuccess) return e;
+    buf.count = capacity;
+    if (capacity > count &&
+        (e = cudaMemsetAsync(buf.ptr + count, 0, (capacity - count) * sizeof(T), stream)) != cudaSuccess)
+        return e;
+    if (count && (e = cudaMemcpyAsync(buf.ptr, host, count * sizeof(T), cudaMemcpyHostToDevice, stream)) != cudaSuccess)
+        return e;
     return cudaStreamSynchronize(stream);
 }
 
@@ -213,6 +259,145 @@ WideBvh build_wide(const std::vector<BuildBox> &boxes, const spk_tuning &t, int 
     return collapse_wide(b2, static_cast<int>(t.bvh_width));
 }
 
+// Node ranges of the BFS depths of a collapsed BVH (children always follow their parent, depth by depth).
+std::vector<uint32_t> wide_levels(const WideBvh &w) {
+    std::vector<uint32_t> depth(w.nodes.size(), 0), levels{0};
+    for (uint32_t i = 0; i < w.nodes.size(); ++i) {
+        const WideNode &n = w.nodes[i];
+        if (i > 0 && depth[i] != depth[i - 1]) levels.push_back(i);
+        for (uint32_t r = 0; r < static_cast<uint32_t>(__builtin_popcount(n.imask)); ++r)
+            depth[n.child_base + r] = depth[i] + 1;
+    }
+    levels.push_back(static_cast<uint32_t>(w.nodes.size()));
+    return levels;
+}
+
+// Materials; the emissive test is SamplePixel's `emissive_color.norm() > Eps` (CPURenderer.cpp:286-287).
+std::vector<DevMaterial> build_materials(const spk_material *materials, uint32_t num_materials,
+                                         const spk_material_maps *maps) {
+    std::vector<DevMaterial> out(num_materials);
+    for (uint32_t k = 0; k < num_materials; ++k) {
+        const spk_material &s = materials[k];
+        DevMaterial &d = out[k];
+        std::memset(&d, 0, sizeof(d));
+        for (int c = 0; c < 3; ++c) {
+            d.base[c] = s.base_color[c];
+            d.emissive[c] = s.emissive[c];
+        }
+        d.type = s.type;
+        const volatile float e0 = s.emissive[0] * s.emissive[0], e1 = s.emissive[1] * s.emissive[1],
+                             e2 = s.emissive[2] * s.emissive[2];
+        const volatile float sn = e0 + (e1 + e2);
+        d.is_emissive = std::sqrt(static_cast<float>(sn)) > kEps ? 1u : 0u;
+        d.metallic = s.metallic;
+        d.roughness = s.roughness;
+        d.eta = s.eta;
+        auto tex = [](int32_t i) { return i < 0 ? kInvalid : static_cast<uint32_t>(i); };
+        d.tex_base = maps ? tex(maps[k].base_color) : kInvalid;
+        d.tex_mr = maps ? tex(maps[k].metallic_roughness) : kInvalid;
+        d.tex_emissive = maps ? tex(maps[k].emissive) : kInvalid;
+        d.tex_normal = maps ? tex(maps[k].normal) : kInvalid;
+    }
+    return out;
+}
+
+// Instance records and their world boxes (the TLAS build input, SceneRenderProxy.cpp:31-69).
+void instance_records(const spk_instance *instances, uint32_t num_instances, const std::vector<MeshBlas> &blas,
+                      const std::vector<DevMaterial> &mats, std::vector<DevInstance> &insts,
+                      std::vector<BuildBox> &boxes, float &abs_x, float lo_out[3], float hi_out[3]) {
+    insts.assign(num_instances, DevInstance{});
+    boxes.assign(num_instances, BuildBox{});
+    abs_x = 0.f;
+    for (uint32_t k = 0; k < num_instances; ++k) {
+        const spk_instance &in = instances[k];
+        DevInstance &d = insts[k];
+        std::memset(&d, 0, sizeof(d));
+        std::memcpy(d.m, in.transform, sizeof(d.m));
+        std::memcpy(d.minv, in.inv_transform, sizeof(d.minv));
+        d.type = in.type;
+        d.material = in.material_id;
+        d.radius = in.radius;
+        d.normal_map = kInvalid;
+        d.light_base = kInvalid;
+        if (in.type == SPK_PRIM_SPHERE) {
+            d.blas_root = kInvalid;
+            const double r = std::fabs(static_cast<double>(in.radius));
+            const double lo[3] = {-r, -r, -r}, hi[3] = {r, r, r};
+            const float tm[12] = {1, 0, 0, in.transform[3], 0, 1, 0, in.transform[7], 0, 0, 1, in.transform[11]};
+            boxes[k] = world_box(tm, lo, hi);
+        } else {
+            const MeshBlas &b = blas[in.mesh_id];
+            d.blas_root = b.root;
+            d.vert_base = b.vert_base;
+            d.face_base = b.face_base;
+            d.normal_map = mats[in.material_id].tex_normal;
+            if (d.blas_root == kInvalid) {
+                const double z[3] = {0, 0, 0};
+                boxes[k] = world_box(in.transform, z, z);
+            } else {
+                boxes[k] = world_box(in.transform, b.bounds, b.bounds + 3);
+            }
+        }
+        abs_x = std::max(abs_x, std::max(std::fabs(boxes[k].lo[0]), std::fabs(boxes[k].hi[0])));
+        for (int a = 0; a < 3; ++a) {
+            lo_out[a] = std::min(lo_out[a], boxes[k].lo[a]);
+            hi_out[a] = std::max(hi_out[a], boxes[k].hi[a]);
+        }
+    }
+}
+
+// Emissive triangles of mesh instances in world space (instance then face order) and their area CDF, for
+// next-event estimation. A textured emission varies over the triangle: such emitters are reached by BSDF
+// sampling only (no light-table entry, so their hits take the full emission).
+void light_table(const spk_instance *instances, uint32_t num_instances, const spk_mesh *meshes,
+                 const std::vector<DevMaterial> &mats, std::vector<DevInstance> &insts, std::vector<DevLight> &lights,
+                 std::vector<float> &cdf, float &total) {
+    lights.clear();
+    cdf.clear();
+    total = 0.f;
+    for (uint32_t k = 0; k < num_instances; ++k) {
+        const spk_instance &in = instances[k];
+        insts[k].light_base = kInvalid;
+        if (in.type != SPK_PRIM_MESH || !mats[in.material_id].is_emissive || mats[in.material_id].tex_emissive != kInvalid)
+            continue;
+        const spk_mesh &m = meshes[in.mesh_id];
+        insts[k].light_base = static_cast<uint32_t>(lights.size());
+        for (uint32_t f = 0; f < m.num_faces; ++f) {
+            f3 w[3];
+            for (int c = 0; c < 3; ++c) {
+                const float *p = m.positions + 3 * m.indices[3 * f + c];
+                w[c] = xform_point(in.transform, mk3(p[0], p[1], p[2]));
+            }
+            DevLight L{};
+            const f3 e1 = w[1] - w[0], e2 = w[2] - w[0];
+            const f3 cr = cross(e1, e2);
+            const float len = std::sqrt(sqnorm(cr));
+            const f3 ng = len > 0.f ? mk3(cr.x / len, cr.y / len, cr.z / len) : mk3(0.f, 0.f, 0.f);
+            const float vals[5][3] = {{w[0].x, w[0].y, w[0].z}, {e1.x, e1.y, e1.z}, {e2.x, e2.y, e2.z},
+                                      {ng.x, ng.y, ng.z},
+                                      {mats[in.material_id].emissive[0], mats[in.material_id].emissive[1],
+                                       mats[in.material_id].emissive[2]}};
+            std::memcpy(L.p0, vals[0], 12);
+            std::memcpy(L.e1, vals[1], 12);
+            std::memcpy(L.e2, vals[2], 12);
+            std::memcpy(L.ng, vals[3], 12);
+            std::memcpy(L.emission, vals[4], 12);
+            L.area = 0.5f * len;
+            lights.push_back(L);
+        }
+    }
+    for (const DevLight &L : lights) {
+        total = total + L.area;
+        cdf.push_back(total);
+    }
+    if (!(total > 0.f)) {
+        lights.clear();
+        cdf.clear();
+        total = 0.f;
+        for (uint32_t k = 0; k < num_instances; ++k) insts[k].light_base = kInvalid;
+    }
+}
+
 struct HostScene {
     std::vector<WideNode> nodes;
     std::vector<float4> tris;
@@ -226,6 +411,7 @@ struct HostScene {
     std::vector<float> light_cdf;
     std::vector<DevTexture> textures;
     std::vector<float4> texels;
+    std::vector<MeshBlas> blas;  // per mesh (single-scene builds)
     uint32_t tlas_root = kInvalid;
     uint32_t sky_mode = SPK_SKY_NONE, sky_size = 0;
     float sky_color[3] = {0.f, 0.f, 0.f};
@@ -288,13 +474,12 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
     }
 
     // BLAS per mesh: binned SAH BVH2 (<= 3 triangles per leaf) collapsed to 8-wide nodes.
-    std::vector<uint32_t> blas_root(num_meshes, kInvalid);
-    std::vector<uint32_t> vert_base(num_meshes, 0), face_base(num_meshes, 0);
-    std::vector<std::array<double, 6>> mesh_bounds(num_meshes);
+    hs.blas.assign(num_meshes, MeshBlas{});
     for (uint32_t k = 0; k < num_meshes; ++k) {
         const spk_mesh &m = meshes[k];
-        vert_base[k] = static_cast<uint32_t>(hs.verts.size() / 3);
-        face_base[k] = static_cast<uint32_t>(hs.faces.size());
+        MeshBlas &mbl = hs.blas[k];
+        mbl.vert_base = static_cast<uint32_t>(hs.verts.size() / 3);
+        mbl.face_base = static_cast<uint32_t>(hs.faces.size());
         for (uint32_t v = 0; v < m.num_vertices; ++v) {
             const float *n = m.normals + 3 * v;
             const float t[4] = {m.tangents ? m.tangents[4 * v] : 1.f, m.tangents ? m.tangents[4 * v + 1] : 0.f,
@@ -306,10 +491,11 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
         }
         for (uint32_t f = 0; f < m.num_faces; ++f)
             hs.faces.push_back(make_uint4(m.indices[3 * f], m.indices[3 * f + 1], m.indices[3 * f + 2], 0u));
-        auto &mb = mesh_bounds[k];
-        mb = {std::numeric_limits<double>::max(), std::numeric_limits<double>::max(),
-              std::numeric_limits<double>::max(), -std::numeric_limits<double>::max(),
-              -std::numeric_limits<double>::max(), -std::numeric_limits<double>::max()};
+        double *mb = mbl.bounds;
+        for (int a = 0; a < 3; ++a) {
+            mb[a] = std::numeric_limits<double>::max();
+            mb[3 + a] = -std::numeric_limits<double>::max();
+        }
         if (m.num_faces == 0) continue;
         std::vector<BuildBox> boxes(m.num_faces);
         for (uint32_t f = 0; f < m.num_faces; ++f) {
@@ -331,7 +517,11 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
         }
         const WideBvh wide = build_wide(boxes, ctx->tuning, threads);
         const uint32_t tri_offset = static_cast<uint32_t>(hs.tris.size() / 3);
-        blas_root[k] = static_cast<uint32_t>(hs.nodes.size());
+        mbl.root = static_cast<uint32_t>(hs.nodes.size());
+        mbl.node_count = static_cast<uint32_t>(wide.nodes.size());
+        mbl.levels = wide_levels(wide);
+        mbl.tri_first = tri_offset;
+        mbl.tri_count = static_cast<uint32_t>(wide.items.size());
         append_wide(hs.nodes, wide, tri_offset);
         for (uint32_t face : wide.items) {
             const float *p0 = m.positions + 3 * m.indices[3 * face];
@@ -348,122 +538,18 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
             hs.tris.push_back(make_float4(e2[2], ff, 0.f, 0.f));
         }
     }
+    hs.mats = build_materials(materials, num_materials, maps);
     // Instances + TLAS over their world boxes (TLAS::Build, SceneRenderProxy.cpp:31-69).
-    hs.insts.assign(num_instances, DevInstance{});
-    std::vector<BuildBox> inst_boxes(num_instances);
+    std::vector<BuildBox> inst_boxes;
     float abs_x = 0.f;
-    for (uint32_t k = 0; k < num_instances; ++k) {
-        const spk_instance &in = instances[k];
-        DevInstance &d = hs.insts[k];
-        std::memset(&d, 0, sizeof(d));
-        std::memcpy(d.m, in.transform, sizeof(d.m));
-        std::memcpy(d.minv, in.inv_transform, sizeof(d.minv));
-        d.type = in.type;
-        d.material = in.material_id;
-        d.radius = in.radius;
-        d.normal_map = kInvalid;  // set once the materials are built
-        if (in.type == SPK_PRIM_SPHERE) {
-            d.blas_root = kInvalid;
-            const double r = std::fabs(static_cast<double>(in.radius));
-            const double lo[3] = {-r, -r, -r}, hi[3] = {r, r, r};
-            const float tm[12] = {1, 0, 0, in.transform[3], 0, 1, 0, in.transform[7], 0, 0, 1, in.transform[11]};
-            inst_boxes[k] = world_box(tm, lo, hi);
-        } else {
-            d.blas_root = blas_root[in.mesh_id];
-            d.vert_base = vert_base[in.mesh_id];
-            d.face_base = face_base[in.mesh_id];
-            const auto &mb = mesh_bounds[in.mesh_id];
-            if (d.blas_root == kInvalid) {
-                const double z[3] = {0, 0, 0};
-                inst_boxes[k] = world_box(in.transform, z, z);
-            } else {
-                const double lo[3] = {mb[0], mb[1], mb[2]}, hi[3] = {mb[3], mb[4], mb[5]};
-                inst_boxes[k] = world_box(in.transform, lo, hi);
-            }
-        }
-        abs_x = std::max(abs_x, std::max(std::fabs(inst_boxes[k].lo[0]), std::fabs(inst_boxes[k].hi[0])));
-        for (int a = 0; a < 3; ++a) {
-            hs.lo[a] = std::min(hs.lo[a], inst_boxes[k].lo[a]);
-            hs.hi[a] = std::max(hs.hi[a], inst_boxes[k].hi[a]);
-        }
-    }
+    instance_records(instances, num_instances, hs.blas, hs.mats, hs.insts, inst_boxes, abs_x, hs.lo, hs.hi);
     if (num_instances > 0) {
         const WideBvh wide = build_wide(inst_boxes, ctx->tuning, threads);
         hs.tlas_root = static_cast<uint32_t>(hs.nodes.size());
         append_wide(hs.nodes, wide, 0);
         hs.tlas_items = wide.items;
     }
-    // Materials; the emissive test is SamplePixel's `emissive_color.norm() > Eps` (CPURenderer.cpp:286-287).
-    hs.mats.assign(num_materials, DevMaterial{});
-    for (uint32_t k = 0; k < num_materials; ++k) {
-        const spk_material &s = materials[k];
-        DevMaterial &d = hs.mats[k];
-        std::memset(&d, 0, sizeof(d));
-        for (int c = 0; c < 3; ++c) {
-            d.base[c] = s.base_color[c];
-            d.emissive[c] = s.emissive[c];
-        }
-        d.type = s.type;
-        const volatile float e0 = s.emissive[0] * s.emissive[0], e1 = s.emissive[1] * s.emissive[1],
-                             e2 = s.emissive[2] * s.emissive[2];
-        const volatile float sn = e0 + (e1 + e2);
-        d.is_emissive = std::sqrt(static_cast<float>(sn)) > kEps ? 1u : 0u;
-        d.metallic = s.metallic;
-        d.roughness = s.roughness;
-        d.eta = s.eta;
-        auto tex = [](int32_t i) { return i < 0 ? kInvalid : static_cast<uint32_t>(i); };
-        d.tex_base = maps ? tex(maps[k].base_color) : kInvalid;
-        d.tex_mr = maps ? tex(maps[k].metallic_roughness) : kInvalid;
-        d.tex_emissive = maps ? tex(maps[k].emissive) : kInvalid;
-        d.tex_normal = maps ? tex(maps[k].normal) : kInvalid;
-    }
-    // Emissive triangles of mesh instances in world space (instance then face order) and their area CDF,
-    // for next-event estimation.
-    for (uint32_t k = 0; k < num_instances; ++k) hs.insts[k].light_base = kInvalid;
-    for (uint32_t k = 0; k < num_instances; ++k) {
-        const spk_instance &in = instances[k];
-        for (uint32_t k = 0; k < num_instances; ++k)
-        if (instances[k].type == SPK_PRIM_MESH) hs.insts[k].normal_map = hs.mats[instances[k].material_id].tex_normal;
-    // A textured emission varies over the triangle: such emitters are reached by BSDF sampling only
-        // (no light-table entry, so their hits take the full emission).
-        if (in.type != SPK_PRIM_MESH || !hs.mats[in.material_id].is_emissive ||
-            hs.mats[in.material_id].tex_emissive != kInvalid)
-            continue;
-        const spk_mesh &m = meshes[in.mesh_id];
-        hs.insts[k].light_base = static_cast<uint32_t>(hs.lights.size());
-        for (uint32_t f = 0; f < m.num_faces; ++f) {
-            f3 w[3];
-            for (int c = 0; c < 3; ++c) {
-                const float *p = m.positions + 3 * m.indices[3 * f + c];
-                w[c] = xform_point(in.transform, mk3(p[0], p[1], p[2]));
-            }
-            DevLight L{};
-            const f3 e1 = w[1] - w[0], e2 = w[2] - w[0];
-            const f3 cr = cross(e1, e2);
-            const float len = std::sqrt(sqnorm(cr));
-            const f3 ng = len > 0.f ? mk3(cr.x / len, cr.y / len, cr.z / len) : mk3(0.f, 0.f, 0.f);
-            const float vals[5][3] = {{w[0].x, w[0].y, w[0].z}, {e1.x, e1.y, e1.z}, {e2.x, e2.y, e2.z},
-                                      {ng.x, ng.y, ng.z},
-                                      {hs.mats[in.material_id].emissive[0], hs.mats[in.material_id].emissive[1],
-                                       hs.mats[in.material_id].emissive[2]}};
-            std::memcpy(L.p0, vals[0], 12);
-            std::memcpy(L.e1, vals[1], 12);
-            std::memcpy(L.e2, vals[2], 12);
-            std::memcpy(L.ng, vals[3], 12);
-            std::memcpy(L.emission, vals[4], 12);
-            L.area = 0.5f * len;
-            hs.lights.push_back(L);
-        }
-    }
-    for (const DevLight &L : hs.lights) {
-        hs.light_total = hs.light_total + L.area;
-        hs.light_cdf.push_back(hs.light_total);
-    }
-    if (!(hs.light_total > 0.f)) {
-        hs.lights.clear();
-        hs.light_cdf.clear();
-        for (uint32_t k = 0; k < num_instances; ++k) hs.insts[k].light_base = kInvalid;
-    }
+    light_table(instances, num_instances, meshes, hs.mats, hs.insts, hs.lights, hs.light_cdf, hs.light_total);
     if (sky && sky->mode == SPK_SKY_CUBE) {
         const size_t n = 6ull * sky->cube_size * sky->cube_size;
         hs.cube.resize(n);
@@ -538,12 +624,14 @@ void append_scene(HostScene &all, const HostScene &s, DevSceneDesc &d) {
 }
 
 // Uploads concatenated scene records and points the context's DevScene at them (scene 0 by default).
-spk_status upload_scene(spk_ctx *ctx, const HostScene &hs, const std::vector<DevSceneDesc> &descs) {
+// `node_capacity` reserves room for a TLAS that grows on a later incremental update.
+spk_status upload_scene(spk_ctx *ctx, const HostScene &hs, const std::vector<DevSceneDesc> &descs,
+                        size_t node_capacity = 0) {
     ctx->has_scene = false;
     cudaError_t e;
     static_assert(sizeof(WideNode) == 5 * sizeof(uint4), "node size");
-    if ((e = upload(ctx->nodes, reinterpret_cast<const uint4 *>(hs.nodes.data()), hs.nodes.size() * 5,
-                    ctx->stream)) != cudaSuccess ||
+    if ((e = upload_with_capacity(ctx->nodes, reinterpret_cast<const uint4 *>(hs.nodes.data()), hs.nodes.size() * 5,
+                                  node_capacity * 5, ctx->stream)) != cudaSuccess ||
         (e = upload(ctx->tris, hs.tris.data(), hs.tris.size(), ctx->stream)) != cudaSuccess ||
         (e = upload(ctx->tlas_items, hs.tlas_items.data(), hs.tlas_items.size(), ctx->stream)) != cudaSuccess ||
         (e = upload(ctx->instances, hs.insts.data(), hs.insts.size(), ctx->stream)) != cudaSuccess ||
@@ -590,6 +678,104 @@ spk_status upload_scene(spk_ctx *ctx, const HostScene &hs, const std::vector<Dev
     ctx->bvh_bytes = hs.nodes.size() * sizeof(WideNode) + hs.tris.size() * sizeof(float4);
     ctx->has_scene = true;
     ctx->dirty = true;
+    return SPK_OK;
+}
+
+// SceneRenderProxy::UpdateBVH's `tlas_ = std::make_unique<TLAS>(primitives_); tlas_->Build()`
+// (SceneRenderProxy.cpp:292-296) for a single-scene context whose BLASes are resident: rebuilds the instance
+// records, the TLAS and the emissive-triangle light table on the host from the kept instance list and mesh
+// positions, and uploads them (the TLAS into the nodes behind the BLASes).
+spk_status rebuild_top(spk_ctx *ctx) {
+    DynScene &dy = ctx->dyn;
+    const uint32_t n = static_cast<uint32_t>(dy.instances.size());
+    std::vector<BuildBox> boxes;
+    float abs_x = 0.f;
+    float lo[3] = {std::numeric_limits<float>::max(), std::numeric_limits<float>::max(),
+                   std::numeric_limits<float>::max()};
+    float hi[3] = {-lo[0], -lo[1], -lo[2]};
+    instance_records(dy.instances.data(), n, dy.blas, dy.mats, dy.insts, boxes, abs_x, lo, hi);
+    std::vector<WideNode> tlas;
+    std::vector<uint32_t> items;
+    if (n > 0) {
+        const WideBvh wide = build_wide(boxes, ctx->tuning, host_threads());
+        for (WideNode w : wide.nodes) {
+            w.child_base += dy.tlas_root;
+            tlas.push_back(w);
+        }
+        items = wide.items;
+    }
+    std::vector<spk_mesh> views(dy.positions.size());
+    for (size_t m = 0; m < views.size(); ++m) {
+        views[m] = spk_mesh{};
+        views[m].positions = dy.positions[m].data();
+        views[m].indices = dy.indices[m].data();
+        views[m].num_vertices = static_cast<uint32_t>(dy.positions[m].size() / 3);
+        views[m].num_faces = static_cast<uint32_t>(dy.indices[m].size() / 3);
+    }
+    std::vector<DevLight> lights;
+    std::vector<float> cdf;
+    float total = 0.f;
+    light_table(dy.instances.data(), n, views.data(), dy.mats, dy.insts, lights, cdf, total);
+
+    cudaError_t e;
+    const size_t need = static_cast<size_t>(dy.tlas_root) + tlas.size();
+    if (need > dy.node_capacity) {  // grow: keep the BLAS nodes, double the TLAS room
+        const size_t cap = static_cast<size_t>(dy.tlas_root) + 2 * std::max<size_t>(tlas.size(), 1);
+        DevBuf<uint4> grown;
+        if ((e = cudaMalloc(&grown.ptr, cap * 5 * sizeof(uint4))) != cudaSuccess) return cuda_fail(ctx, e, "TLAS nodes");
+        grown.count = cap * 5;
+        if (dy.tlas_root &&
+            (e = cudaMemcpyAsync(grown.ptr, ctx->nodes.ptr, dy.tlas_root * 5ull * sizeof(uint4), cudaMemcpyDeviceToDevice,
+                                 ctx->stream)) != cudaSuccess) {
+            grown.reset();
+            return cuda_fail(ctx, e, "TLAS nodes");
+        }
+        cudaStreamSynchronize(ctx->stream);
+        ctx->nodes.reset();
+        ctx->nodes = grown;
+        dy.node_capacity = static_cast<uint32_t>(cap);
+    }
+    dy.desc.tlas_root = n > 0 ? dy.tlas_root : kInvalid;
+    dy.desc.num_lights = static_cast<uint32_t>(lights.size());
+    dy.desc.light_total = total;
+    if ((!tlas.empty() && (e = cudaMemcpyAsync(ctx->nodes.ptr + 5ull * dy.tlas_root, tlas.data(),
+                                               tlas.size() * sizeof(WideNode), cudaMemcpyHostToDevice, ctx->stream)) !=
+                              cudaSuccess) ||
+        (e = upload(ctx->tlas_items, items.data(), items.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->instances, dy.insts.data(), dy.insts.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->lights, lights.data(), lights.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->light_cdf, cdf.data(), cdf.size(), ctx->stream)) != cudaSuccess ||
+        (e = upload(ctx->scene_descs, &dy.desc, 1, ctx->stream)) != cudaSuccess) {
+        ctx->has_scene = false;
+        return cuda_fail(ctx, e, "scene update");
+    }
+    DevScene &S = ctx->scene;
+    S.nodes = ctx->nodes.ptr;
+    S.tlas_items = ctx->tlas_items.ptr;
+    S.instances = ctx->instances.ptr;
+    S.lights = ctx->lights.ptr;
+    S.light_cdf = ctx->light_cdf.ptr;
+    S.descs = ctx->scene_descs.ptr;
+    S.tlas_root = dy.desc.tlas_root;
+    S.num_lights = dy.desc.num_lights;
+    S.light_total = total;
+    S.scene_abs_x = abs_x;
+    for (int a = 0; a < 3; ++a) {
+        const bool ok = hi[a] > lo[a];
+        S.box_lo[a] = ok ? lo[a] : 0.f;
+        S.box_scale[a] = ok ? 8.f / (hi[a] - lo[a]) : 0.f;
+    }
+    ctx->bvh_nodes = static_cast<uint32_t>(need);
+    ctx->dirty = true;  // any primitive change clears the accumulation (SceneRenderProxy.cpp:198-202)
+    return SPK_OK;
+}
+
+spk_status require_dynamic(spk_ctx *ctx) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene || !ctx->dyn.valid)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "incremental updates need a scene set by spk_set_scene");
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
     return SPK_OK;
 }
 
@@ -676,6 +862,7 @@ spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t n
     if (!scenes || num_scenes == 0) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "no scenes");
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    ctx->dyn = DynScene{};
     HostScene all;
     std::vector<DevSceneDesc> descs(num_scenes);
     for (uint32_t k = 0; k < num_scenes; ++k) {
@@ -691,11 +878,151 @@ spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t n
         if (num_scenes == 1) {
             descs[0] = DevSceneDesc{hs.tlas_root, hs.sky_mode, hs.sky_size, {hs.sky_color[0], hs.sky_color[1],
                                     hs.sky_color[2]}, 0u, 0u, static_cast<uint32_t>(hs.lights.size()), hs.light_total};
-            return upload_scene(ctx, hs, descs);
+            // A wide TLAS over n instances has at most max(1, n) nodes: reserve that much behind the BLASes.
+            const uint32_t blas_nodes = hs.tlas_root == kInvalid ? static_cast<uint32_t>(hs.nodes.size()) : hs.tlas_root;
+            const size_t capacity = static_cast<size_t>(blas_nodes) +
+                                    std::max<size_t>(hs.nodes.size() - blas_nodes, std::max(1u, d.num_instances));
+            const spk_status up = upload_scene(ctx, hs, descs, capacity);
+            if (up != SPK_OK) return up;
+            DynScene &dy = ctx->dyn;
+            dy.instances.assign(d.instances, d.instances + d.num_instances);
+            dy.positions.resize(d.num_meshes);
+            dy.indices.resize(d.num_meshes);
+            for (uint32_t m = 0; m < d.num_meshes; ++m) {
+                const spk_mesh &mesh = d.meshes[m];
+                dy.positions[m].assign(mesh.positions, mesh.positions + (mesh.positions ? 3ull * mesh.num_vertices : 0));
+                dy.indices[m].assign(mesh.indices, mesh.indices + (mesh.indices ? 3ull * mesh.num_faces : 0));
+            }
+            dy.blas = std::move(hs.blas);
+            dy.mats = std::move(hs.mats);
+            dy.insts = std::move(hs.insts);
+            dy.desc = descs[0];
+            dy.tlas_root = blas_nodes;
+            dy.node_capacity = static_cast<uint32_t>(capacity);
+            dy.valid = true;
+            return SPK_OK;
         }
         append_scene(all, hs, descs[k]);
     }
     return upload_scene(ctx, all, descs);
+}
+
+spk_status spk_set_instances(spk_ctx *ctx, const spk_instance *instances, uint32_t num_instances) {
+    spk_status st = require_dynamic(ctx);
+    if (st != SPK_OK) return st;
+    if (num_instances && !instances) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "null instance array");
+    DynScene &dy = ctx->dyn;
+    for (uint32_t k = 0; k < num_instances; ++k) {
+        const spk_instance &in = instances[k];
+        if (in.type != SPK_PRIM_MESH && in.type != SPK_PRIM_SPHERE)
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: bad type", k);
+        if (in.type == SPK_PRIM_MESH && in.mesh_id >= dy.blas.size())
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: mesh_id out of range", k);
+        if (in.material_id >= dy.mats.size())
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instance %u: material_id out of range", k);
+    }
+    dy.instances.assign(instances, instances + num_instances);
+    return rebuild_top(ctx);
+}
+
+spk_status spk_set_instance_transforms(spk_ctx *ctx, uint32_t first, uint32_t count, const float *transforms,
+                                       const float *inv_transforms) {
+    spk_status st = require_dynamic(ctx);
+    if (st != SPK_OK) return st;
+    DynScene &dy = ctx->dyn;
+    if (count && (!transforms || !inv_transforms)) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "null transforms");
+    if (static_cast<uint64_t>(first) + count > dy.instances.size())
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "instances %u..%u out of range (%zu instances)", first,
+                    first + count, dy.instances.size());
+    for (uint32_t k = 0; k < count; ++k) {
+        std::memcpy(dy.instances[first + k].transform, transforms + 12ull * k, 12 * sizeof(float));
+        std::memcpy(dy.instances[first + k].inv_transform, inv_transforms + 12ull * k, 12 * sizeof(float));
+    }
+    return rebuild_top(ctx);
+}
+
+spk_status spk_update_mesh(spk_ctx *ctx, uint32_t mesh_id, uint32_t num_vertices, const float *positions,
+                           const float *normals, const float *tangents) {
+    spk_status st = require_dynamic(ctx);
+    if (st != SPK_OK) return st;
+    DynScene &dy = ctx->dyn;
+    if (mesh_id >= dy.blas.size()) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "mesh_id %u out of range", mesh_id);
+    std::vector<float> &pos = dy.positions[mesh_id];
+    if (num_vertices != pos.size() / 3)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "mesh %u: %u vertices given, the mesh has %zu", mesh_id,
+                    num_vertices, pos.size() / 3);
+    if (num_vertices && !positions) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "null positions");
+    const MeshBlas &b = dy.blas[mesh_id];
+    const uint32_t num_faces = static_cast<uint32_t>(dy.indices[mesh_id].size() / 3);
+    cudaError_t e;
+    const size_t nv3 = 3ull * num_vertices;
+    // The host copy (bounds, light table) and the device copy (refit) of the new positions.
+    if (nv3 && (e = cudaMemcpy(pos.data(), positions, nv3 * sizeof(float), cudaMemcpyDefault)) != cudaSuccess)
+        return cuda_fail(ctx, e, "positions");
+    if (ctx->dyn_pos.count < nv3 && (e = alloc(ctx->dyn_pos, nv3)) != cudaSuccess) return cuda_fail(ctx, e, "positions");
+    if (nv3 && (e = cudaMemcpyAsync(ctx->dyn_pos.ptr, pos.data(), nv3 * sizeof(float), cudaMemcpyHostToDevice,
+                                    ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "positions");
+    if (normals || tangents) {
+        const size_t na = (normals ? nv3 : 0) + (tangents ? 4ull * num_vertices : 0);
+        if (ctx->dyn_attr.count < na && (e = alloc(ctx->dyn_attr, na)) != cudaSuccess)
+            return cuda_fail(ctx, e, "vertex attributes");
+        float *dn = normals ? ctx->dyn_attr.ptr : nullptr;
+        float *dt = tangents ? ctx->dyn_attr.ptr + (normals ? nv3 : 0) : nullptr;
+        if ((normals && (e = cudaMemcpyAsync(dn, normals, nv3 * sizeof(float), cudaMemcpyDefault, ctx->stream)) !=
+                            cudaSuccess) ||
+            (tangents && (e = cudaMemcpyAsync(dt, tangents, 4ull * num_vertices * sizeof(float), cudaMemcpyDefault,
+                                              ctx->stream)) != cudaSuccess) ||
+            (e = launch_update_vertices(ctx->verts.ptr, b.vert_base, num_vertices, dn, dt, ctx->stream)) != cudaSuccess)
+            return cuda_fail(ctx, e, "vertex attributes");
+    }
+    if (b.root != kInvalid) {
+        if (ctx->dyn_boxes.count < 6ull * b.node_count && (e = alloc(ctx->dyn_boxes, 6ull * b.node_count)) != cudaSuccess)
+            return cuda_fail(ctx, e, "refit scratch");
+        BlasRefit r{};
+        r.nodes = ctx->nodes.ptr;
+        r.boxes = ctx->dyn_boxes.ptr;
+        r.tris = ctx->tris.ptr;
+        r.faces = ctx->faces.ptr + b.face_base;
+        r.positions = ctx->dyn_pos.ptr;
+        r.root = b.root;
+        r.node_count = b.node_count;
+        r.tri_first = b.tri_first;
+        r.tri_count = b.tri_count;
+        r.num_faces = num_faces;
+        r.num_vertices = num_vertices;
+        if ((e = launch_refit_triangles(r, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "refit");
+        for (size_t l = b.levels.size() - 1; l-- > 0;)
+            if ((e = launch_refit_nodes(r, b.levels[l], b.levels[l + 1], ctx->stream)) != cudaSuccess)
+                return cuda_fail(ctx, e, "refit");
+    }
+    // The mesh's local box over its faces' vertices, as the BLAS build takes it.
+    MeshBlas &mb = dy.blas[mesh_id];
+    for (int a = 0; a < 3; ++a) {
+        mb.bounds[a] = std::numeric_limits<double>::max();
+        mb.bounds[3 + a] = -std::numeric_limits<double>::max();
+    }
+    for (uint32_t i : dy.indices[mesh_id])
+        for (int a = 0; a < 3; ++a) {
+            mb.bounds[a] = std::min(mb.bounds[a], static_cast<double>(pos[3ull * i + a]));
+            mb.bounds[3 + a] = std::max(mb.bounds[3 + a], static_cast<double>(pos[3ull * i + a]));
+        }
+    st = rebuild_top(ctx);
+    if (st != SPK_OK) return st;
+    if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "refit");
+    return SPK_OK;
+}
+
+spk_status spk_read_bvh_nodes(spk_ctx *ctx, void *nodes, uint64_t capacity, uint64_t *count) {
+    if (!ctx || !count) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene) return fail(ctx, SPK_ERR_NOT_READY, "no scene");
+    *count = ctx->bvh_nodes;
+    if (!nodes) return SPK_OK;
+    const uint64_t n = std::min<uint64_t>(capacity, ctx->bvh_nodes);
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaMemcpyAsync(nodes, ctx->nodes.ptr, n * sizeof(WideNode), cudaMemcpyDefault, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return e == cudaSuccess ? SPK_OK : cuda_fail(ctx, e, "read nodes");
 }
 
 spk_status spk_set_camera(spk_ctx *ctx, const spk_camera *camera) {

@@ -10,8 +10,8 @@ import os
 import numpy as np
 
 from . import build as _build
-from .abi import (HIT_DTYPE, MarshalledScene, Scene, spk_camera, spk_config, spk_request, spk_scene_desc, spk_stats,
-                  spk_tuning)
+from .abi import (HIT_DTYPE, MarshalledScene, Scene, affine_inverse, instance_array, spk_camera, spk_config,
+                  spk_request, spk_scene_desc, spk_stats, spk_tuning)
 
 _lib = None
 
@@ -24,7 +24,8 @@ EXPORTED = ["spk_abi_version", "spk_create", "spk_destroy", "spk_last_error", "s
             "spk_framebuffer_device", "spk_sample_counts", "spk_is_converged", "spk_trace", "spk_trace_device",
             "spk_synchronize", "spk_get_stats", "spk_set_instrumentation", "spk_render_noalloc",
             "spk_tuning_defaults", "spk_set_tuning", "spk_get_tuning", "spk_render_guides", "spk_guides_device",
-            "spk_read_guides", "spk_set_scenes", "spk_render_batch", "spk_read_batch",
+            "spk_read_guides", "spk_set_scenes", "spk_render_batch", "spk_read_batch", "spk_set_instances",
+            "spk_set_instance_transforms", "spk_update_mesh", "spk_read_bvh_nodes",
             # include/spk_denoise.h
             "spk_dn_create", "spk_dn_destroy", "spk_dn_last_error", "spk_dn_init", "spk_dn_num_params",
             "spk_dn_get_params", "spk_dn_set_params", "spk_dn_pack_features", "spk_dn_pack_halves", "spk_dn_train_step",
@@ -79,6 +80,10 @@ def lib(build: bool = True):
         L.spk_set_tuning.argtypes = [vp, vp]
         L.spk_get_tuning.argtypes = [vp, vp]
         L.spk_set_scenes.argtypes = [vp, vp, u32]
+        L.spk_set_instances.argtypes = [vp, vp, u32]
+        L.spk_set_instance_transforms.argtypes = [vp, u32, u32, vp, vp]
+        L.spk_update_mesh.argtypes = [vp, u32, u32, vp, vp, vp]
+        L.spk_read_bvh_nodes.argtypes = [vp, vp, u64, C.POINTER(u64)]
         L.spk_render_batch.argtypes = [vp, vp, u32, u32, u32]
         L.spk_read_batch.argtypes = [vp, u32, vp, vp]
         L.spk_render_guides.argtypes = [vp]
@@ -157,6 +162,33 @@ class Context:
             descs[k] = m.desc()
         self._check(self.L.spk_set_scenes(self.h, descs, len(ms)))
         self._scene = ms
+
+    def set_instances(self, instances):
+        """spk_set_instances: replaces the instance list (add / remove / reorder) over the resident meshes."""
+        arr = instance_array(instances)
+        self._check(self.L.spk_set_instances(self.h, arr, len(instances)))
+
+    def set_instance_transforms(self, first: int, transforms):
+        """spk_set_instance_transforms: new 3x4 transforms for instances first, first + 1, ..."""
+        t = np.ascontiguousarray(np.asarray(transforms, np.float32).reshape(-1, 3, 4))
+        inv = np.ascontiguousarray(np.stack([affine_inverse(m) for m in t]).astype(np.float32)) if len(t) else t
+        self._check(self.L.spk_set_instance_transforms(self.h, first, len(t), _p(t), _p(inv)))
+
+    def update_mesh(self, mesh_id: int, positions, normals=None, tangents=None):
+        """spk_update_mesh: new vertex positions (and optionally normals / tangents) of a resident mesh."""
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+        nrm = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        tan = None if tangents is None else np.ascontiguousarray(tangents, np.float32).reshape(-1, 4)
+        self._check(self.L.spk_update_mesh(self.h, mesh_id, pos.shape[0], _p(pos), None if nrm is None else _p(nrm),
+                                           None if tan is None else _p(tan)))
+
+    def bvh_nodes(self) -> np.ndarray:
+        """The resident node array as (n, 80) bytes (spk_read_bvh_nodes)."""
+        n = C.c_uint64()
+        self._check(self.L.spk_read_bvh_nodes(self.h, None, 0, C.byref(n)))
+        out = np.zeros((n.value, 80), np.uint8)
+        self._check(self.L.spk_read_bvh_nodes(self.h, _p(out), n.value, C.byref(n)))
+        return out
 
     def render_batch(self, requests, rng: int = 1, enable_nee: bool = False):
         """requests: list of dicts with scene, width, height, spp, bounce, seed, camera (spk_camera)."""
