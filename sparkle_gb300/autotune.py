@@ -23,8 +23,9 @@ SPACE = {
     "bvh_width": [8, 4],
     "bvh_leaf_size": [3, 2],
     "bvh_collapse": [0, 1],
+    "bvh_builder": [0, 1],
 }
-SCENE_KNOBS = ("bvh_width", "bvh_leaf_size", "bvh_collapse")
+SCENE_KNOBS = ("bvh_width", "bvh_leaf_size", "bvh_collapse", "bvh_builder")
 
 
 def measure(ctx, workload, repeats: int = 2):

@@ -1,7 +1,9 @@
-// bvh_device.cu -- BLAS refit kernels (bvh_device.cuh).
+// bvh_device.cu -- BLAS refit and device BLAS build (bvh_device.cuh).
 #include "bvh_device.cuh"
 
+#include <algorithm>
 #include <cfloat>
+#include <cstring>
 
 namespace spk {
 namespace {
@@ -61,6 +63,36 @@ __device__ int quant_exponent(double ext) {
     return e;
 }
 
+// Quantises as the host builder does (bvh_builder.cpp quantize_node): origin = the node box's low corner,
+// the smallest power-of-two scale that spans the box in 255 steps, child boxes rounded outwards, flat
+// children widened by a step. Slots with meta 0 are empty.
+__device__ void quantize(NodeBytes &n, const float clo[8][3], const float chi[8][3], const float lo[3],
+                         const float hi[3]) {
+    for (int a = 0; a < 3; ++a) {
+        const double origin = lo[a];
+        const int e = quant_exponent(static_cast<double>(hi[a]) - origin);
+        const double scale = ldexp(1.0, e);
+        n.f[a] = lo[a];
+        n.b[12 + a] = static_cast<uint8_t>(e + 127);
+        for (int s = 0; s < 8; ++s) {
+            if (n.b[24 + s] == 0) continue;
+            double ql = floor((static_cast<double>(clo[s][a]) - origin) / scale);
+            double qh = ceil((static_cast<double>(chi[s][a]) - origin) / scale);
+            ql = fmax(0.0, fmin(255.0, ql));
+            qh = fmax(0.0, fmin(255.0, qh));
+            if (qh <= ql) {
+                if (qh < 255.0) {
+                    qh = ql + 1.0;
+                } else {
+                    ql = qh - 1.0;
+                }
+            }
+            n.b[32 + 8 * a + s] = static_cast<uint8_t>(ql);
+            n.b[56 + 8 * a + s] = static_cast<uint8_t>(qh);
+        }
+    }
+}
+
 __global__ void k_refit_nodes(BlasRefit r, uint32_t first, uint32_t last) {
     const uint32_t i = first + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= last) return;
@@ -107,31 +139,7 @@ __global__ void k_refit_nodes(BlasRefit r, uint32_t first, uint32_t last) {
         mb[a] = lo[a];
         mb[3 + a] = hi[a];
     }
-    // Quantise as the host builder does: origin = the node box's low corner, the smallest power-of-two
-    // scale that spans the box in 255 steps, child boxes rounded outwards, flat children widened by a step.
-    for (int a = 0; a < 3; ++a) {
-        const double origin = lo[a];
-        const int e = quant_exponent(static_cast<double>(hi[a]) - origin);
-        const double scale = ldexp(1.0, e);
-        n.f[a] = lo[a];
-        n.b[12 + a] = static_cast<uint8_t>(e + 127);
-        for (int s = 0; s < 8; ++s) {
-            if (n.b[24 + s] == 0) continue;
-            double ql = floor((static_cast<double>(clo[s][a]) - origin) / scale);
-            double qh = ceil((static_cast<double>(chi[s][a]) - origin) / scale);
-            ql = fmax(0.0, fmin(255.0, ql));
-            qh = fmax(0.0, fmin(255.0, qh));
-            if (qh <= ql) {
-                if (qh < 255.0) {
-                    qh = ql + 1.0;
-                } else {
-                    ql = qh - 1.0;
-                }
-            }
-            n.b[32 + 8 * a + s] = static_cast<uint8_t>(ql);
-            n.b[56 + 8 * a + s] = static_cast<uint8_t>(qh);
-        }
-    }
+    quantize(n, clo, chi, lo, hi);
 #pragma unroll
     for (int k = 0; k < 5; ++k) np[k] = n.q[k];
 }
@@ -156,6 +164,384 @@ __global__ void k_update_vertices(float4 *verts, uint32_t num_vertices, const fl
     r[1] = b;
 }
 
+
+// ---------------------------------------------------------------------------------------------------------
+// Device BLAS build.
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr int kSortThreads = 256;
+constexpr int kSortRounds = 8;  // keys per thread per tile
+constexpr uint32_t kTile = kSortThreads * kSortRounds;
+constexpr int kScanThreads = 1024;
+
+// Order-preserving map of floats to unsigned integers (for atomicMin / atomicMax of bounds).
+__device__ __forceinline__ uint32_t float_key(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key_float(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+// Per face: its box and centroid; the centroid bounds reduced into cb[0..5] (min xyz, max xyz as float keys).
+__global__ void k_face_boxes(const float *pos, const uint32_t *idx, uint32_t n, float4 *flo, float4 *fhi,
+                             uint32_t *cb) {
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    float c[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, d[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    if (f < n) {
+        float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (int v = 0; v < 3; ++v) {
+            const float *p = pos + 3ull * idx[3ull * f + v];
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = fminf(lo[a], p[a]);
+                hi[a] = fmaxf(hi[a], p[a]);
+            }
+        }
+        flo[f] = make_float4(lo[0], lo[1], lo[2], 0.f);
+        fhi[f] = make_float4(hi[0], hi[1], hi[2], 0.f);
+        for (int a = 0; a < 3; ++a) c[a] = d[a] = __fmul_rn(0.5f, __fadd_rn(lo[a], hi[a]));
+    }
+    for (int off = 16; off > 0; off >>= 1)
+        for (int a = 0; a < 3; ++a) {
+            c[a] = fminf(c[a], __shfl_xor_sync(0xFFFFFFFFu, c[a], off));
+            d[a] = fmaxf(d[a], __shfl_xor_sync(0xFFFFFFFFu, d[a], off));
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int a = 0; a < 3; ++a) {
+            atomicMin(cb + a, float_key(c[a]));
+            atomicMax(cb + 3 + a, float_key(d[a]));
+        }
+}
+
+__device__ __forceinline__ uint64_t spread21(uint32_t v) {  // bit i of v -> bit 3i
+    uint64_t x = v & 0x1FFFFFu;
+    x = (x | x << 32) & 0x1F00000000FFFFull;
+    x = (x | x << 16) & 0x1F0000FF0000FFull;
+    x = (x | x << 8) & 0x100F00F00F00F00Full;
+    x = (x | x << 4) & 0x10C30C30C30C30C3ull;
+    x = (x | x << 2) & 0x1249249249249249ull;
+    return x;
+}
+
+__global__ void k_morton(const float4 *flo, const float4 *fhi, uint32_t n, const uint32_t *cb, uint64_t *keys,
+                         uint32_t *vals) {
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n) return;
+    const float4 lo = flo[f], hi = fhi[f];
+    const float c[3] = {__fmul_rn(0.5f, __fadd_rn(lo.x, hi.x)), __fmul_rn(0.5f, __fadd_rn(lo.y, hi.y)),
+                        __fmul_rn(0.5f, __fadd_rn(lo.z, hi.z))};
+    uint32_t q[3];
+    for (int a = 0; a < 3; ++a) {
+        const float b0 = key_float(cb[a]), b1 = key_float(cb[3 + a]);
+        const float ext = b1 - b0;
+        const float t = ext > 0.f ? (c[a] - b0) / ext : 0.f;
+        q[a] = static_cast<uint32_t>(fminf(fmaxf(t * 2097152.f, 0.f), 2097151.f));
+    }
+    keys[f] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
+    vals[f] = f;
+}
+
+// Stable LSD radix sort, 8 bits per pass: per-tile digit counts, one exclusive scan over (digit, tile),
+// then each tile scatters its keys in order (ranks from warp match masks and per-warp digit counts).
+__global__ void k_radix_count(const uint64_t *keys, uint32_t n, int shift, uint32_t num_tiles, uint32_t *hist) {
+    __shared__ uint32_t cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kTile;
+    for (int r = 0; r < kSortRounds; ++r) {
+        const uint64_t i = base + static_cast<uint64_t>(r) * kSortThreads + threadIdx.x;
+        if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[static_cast<uint64_t>(threadIdx.x) * num_tiles + blockIdx.x] = cnt[threadIdx.x];
+}
+
+__global__ void k_radix_scatter(const uint64_t *keys, const uint32_t *vals, uint32_t n, int shift,
+                                uint32_t num_tiles, const uint32_t *offsets, uint64_t *keys_out,
+                                uint32_t *vals_out) {
+    __shared__ uint32_t running[256];
+    __shared__ uint32_t warp_cnt[kSortThreads / 32][256];
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    running[tid] = offsets[static_cast<uint64_t>(tid) * num_tiles + blockIdx.x];
+    for (int w = 0; w < kSortThreads / 32; ++w) warp_cnt[w][tid] = 0;
+    __syncthreads();
+    const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kTile;
+    for (int r = 0; r < kSortRounds; ++r) {
+        const uint64_t i = base + static_cast<uint64_t>(r) * kSortThreads + tid;
+        const bool valid = i < n;
+        const uint64_t key = valid ? keys[i] : 0;
+        const uint32_t val = valid ? vals[i] : 0;
+        const uint32_t digit = valid ? static_cast<uint32_t>((key >> shift) & 255u) : 256u + lane;  // unique if invalid
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, digit);
+        const uint32_t rank_in_warp = __popc(peers & ((1u << lane) - 1u));
+        if (valid && rank_in_warp == 0) warp_cnt[warp][digit] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t before = 0;
+            for (uint32_t w = 0; w < warp; ++w) before += warp_cnt[w][digit];
+            const uint32_t dst = running[digit] + before + rank_in_warp;
+            keys_out[dst] = key;
+            vals_out[dst] = val;
+        }
+        __syncthreads();
+        uint32_t total = 0;
+        for (int w = 0; w < kSortThreads / 32; ++w) {
+            total += warp_cnt[w][tid];
+            warp_cnt[w][tid] = 0;
+        }
+        running[tid] += total;
+        __syncthreads();
+    }
+}
+
+// In-place exclusive scan of data[0..n) by one block; *total receives the sum.
+__global__ void k_scan(uint32_t *data, uint32_t n, uint32_t *total) {
+    __shared__ uint32_t part[kScanThreads];
+    const uint32_t tid = threadIdx.x;
+    const uint32_t chunk = (n + kScanThreads - 1) / kScanThreads;
+    const uint64_t b = static_cast<uint64_t>(tid) * chunk;
+    const uint64_t e = min(static_cast<uint64_t>(n), b + chunk);
+    uint32_t sum = 0;
+    for (uint64_t i = b; i < e; ++i) sum += data[i];
+    part[tid] = sum;
+    __syncthreads();
+    for (uint32_t off = 1; off < kScanThreads; off <<= 1) {
+        const uint32_t v = tid >= off ? part[tid - off] : 0u;
+        __syncthreads();
+        part[tid] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[tid] - sum;
+    for (uint64_t i = b; i < e; ++i) {
+        const uint32_t v = data[i];
+        data[i] = run;
+        run += v;
+    }
+    if (tid == kScanThreads - 1 && total) *total = part[tid];
+}
+
+// Karras 2012 binary radix tree over the sorted codes (ties broken by position). Internal node i in
+// [0, n-1), leaf m is node n-1+m; node 0 is the root. Writes children, parent links and each internal
+// node's leaf range.
+__device__ __forceinline__ int common_prefix(const uint64_t *k, int64_t n, int64_t i, int64_t j) {
+    if (j < 0 || j >= n) return -1;
+    const uint64_t a = k[i], b = k[j];
+    return a != b ? __clzll(a ^ b) : 64 + __clzll(static_cast<uint64_t>(i ^ j));
+}
+
+__global__ void k_karras(const uint64_t *keys, uint32_t n, uint32_t *left, uint32_t *right, uint32_t *parent,
+                         uint32_t *first, uint32_t *count) {
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    const int64_t N = n;
+    if (i >= N - 1) return;
+    const int d = common_prefix(keys, N, i, i + 1) - common_prefix(keys, N, i, i - 1) >= 0 ? 1 : -1;
+    const int dmin = common_prefix(keys, N, i, i - d);
+    int64_t lmax = 2;
+    while (common_prefix(keys, N, i, i + lmax * d) > dmin) lmax *= 2;
+    int64_t l = 0;
+    for (int64_t t = lmax / 2; t >= 1; t /= 2)
+        if (common_prefix(keys, N, i, i + (l + t) * d) > dmin) l += t;
+    const int64_t j = i + l * d;
+    const int dnode = common_prefix(keys, N, i, j);
+    int64_t s = 0;
+    for (int64_t t = (l + 1) / 2;; t = (t + 1) / 2) {
+        if (common_prefix(keys, N, i, i + (s + t) * d) > dnode) s += t;
+        if (t == 1) break;
+    }
+    const int64_t gamma = i + s * d + min(d, 0);
+    const int64_t lo = min(i, j), hi = max(i, j);
+    const uint32_t lc = static_cast<uint32_t>(lo == gamma ? (N - 1) + gamma : gamma);
+    const uint32_t rc = static_cast<uint32_t>(hi == gamma + 1 ? (N - 1) + gamma + 1 : gamma + 1);
+    left[i] = lc;
+    right[i] = rc;
+    parent[lc] = static_cast<uint32_t>(i);
+    parent[rc] = static_cast<uint32_t>(i);
+    first[i] = static_cast<uint32_t>(lo);
+    count[i] = static_cast<uint32_t>(hi - lo + 1);
+}
+
+// Leaf boxes, then up the tree: the second child to arrive at a node writes its box and goes on.
+__global__ void k_bottom_up(const uint32_t *sorted_faces, const float4 *flo, const float4 *fhi, uint32_t n,
+                            const uint32_t *left, const uint32_t *right, const uint32_t *parent, uint32_t *arrivals,
+                            float4 *nlo, float4 *nhi) {
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    uint32_t node = n - 1 + m;
+    float4 lo = flo[sorted_faces[m]], hi = fhi[sorted_faces[m]];
+    nlo[node] = lo;
+    nhi[node] = hi;
+    for (uint32_t steps = 0; steps < n; ++steps) {
+        const uint32_t p = parent[node];
+        if (p == kNone) break;
+        __threadfence();
+        if (atomicAdd(&arrivals[p], 1u) == 0) break;
+        const uint32_t other = left[p] == node ? right[p] : left[p];
+        const float4 ol = __ldcg(nlo + other), oh = __ldcg(nhi + other);
+        lo = make_float4(fminf(lo.x, ol.x), fminf(lo.y, ol.y), fminf(lo.z, ol.z), 0.f);
+        hi = make_float4(fmaxf(hi.x, oh.x), fmaxf(hi.y, oh.y), fmaxf(hi.z, oh.z), 0.f);
+        nlo[p] = lo;
+        nhi[p] = hi;
+        node = p;
+    }
+}
+
+struct BinaryTree {
+    const uint32_t *left, *right, *first, *count;
+    const float4 *nlo, *nhi;
+    uint32_t n;  // leaves
+    __device__ uint32_t leaves(uint32_t x) const { return x >= n - 1 ? 1u : count[x]; }
+    __device__ uint32_t first_leaf(uint32_t x) const { return x >= n - 1 ? x - (n - 1) : first[x]; }
+    __device__ float half_area(uint32_t x) const {
+        const float4 a = nlo[x], b = nhi[x];
+        const float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+        return dx * dy + dy * dz + dz * dx;
+    }
+};
+
+// One breadth-first level of the collapse, pass 1: open each job's binary subtree into at most
+// `max_children` kids (always the inner kid of largest area; kids of <= max_leaf leaves stay closed) and
+// count the inner kids and leaf items.
+__global__ void k_collapse_open(BinaryTree t, const uint32_t *jobs, uint32_t num_jobs, int max_children, int max_leaf,
+                                uint32_t *kids, uint32_t *inner_count, uint32_t *item_count) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= num_jobs) return;
+    const uint32_t b = jobs[j];
+    uint32_t k[8];
+    int nk = 0;
+    const uint32_t ml = static_cast<uint32_t>(max_leaf);
+    if (b >= 2 * t.n - 1) {  // not a node: emit an empty job (the host then reports the item count mismatch)
+        for (int q = 0; q < 8; ++q) kids[8ull * j + q] = kNone;
+        inner_count[j] = item_count[j] = 0;
+        return;
+    }
+    if (t.leaves(b) <= ml) {
+        k[nk++] = b;
+    } else {
+        k[nk++] = t.left[b];
+        k[nk++] = t.right[b];
+        while (nk < max_children) {
+            int best = -1;
+            float best_area = -1.f;
+            for (int q = 0; q < nk; ++q) {
+                if (t.leaves(k[q]) > ml) {
+                    const float a = t.half_area(k[q]);
+                    if (a > best_area) {
+                        best_area = a;
+                        best = q;
+                    }
+                }
+            }
+            if (best < 0) break;
+            const uint32_t x = k[best];
+            k[best] = t.left[x];
+            k[nk++] = t.right[x];
+        }
+    }
+    uint32_t inner = 0, items = 0;
+    for (int q = 0; q < 8; ++q) {
+        kids[8ull * j + q] = q < nk ? k[q] : kNone;
+        if (q < nk) {
+            if (t.leaves(k[q]) > ml && k[q] != b) {
+                ++inner;
+            } else {
+                items += t.leaves(k[q]);
+            }
+        }
+    }
+    inner_count[j] = inner;
+    item_count[j] = items;
+}
+
+// Pass 2: octant slot order, quantised boxes, children and items. Job j is node level_base + j; its inner
+// kids become next-level jobs inner_off[j].. (nodes next_base + inner_off[j] ..) in slot order; its leaf
+// items go to items[item_base + item_off[j] ..] in slot order.
+__global__ void k_collapse_emit(BinaryTree t, uint32_t num_jobs, int max_leaf, const uint32_t *jobs, const uint32_t *kids,
+                                const uint32_t *inner_off, const uint32_t *item_off, uint32_t level_base,
+                                uint32_t next_base, uint32_t item_base, const uint32_t *sorted_faces, uint4 *nodes,
+                                uint32_t *items, uint32_t *next_jobs) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= num_jobs) return;
+    const uint32_t b = jobs[j];
+    const uint32_t ml = static_cast<uint32_t>(max_leaf);
+    uint32_t k[8];
+    int nk = 0;
+    for (int q = 0; q < 8; ++q) {
+        k[q] = kids[8ull * j + q];
+        if (k[q] != kNone) nk = q + 1;
+    }
+    float clo[8][3], chi[8][3], blo[8][3], bhi[8][3];
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int q = 0; q < nk; ++q) {
+        const float4 a = t.nlo[k[q]], c = t.nhi[k[q]];
+        blo[q][0] = a.x, blo[q][1] = a.y, blo[q][2] = a.z;
+        bhi[q][0] = c.x, bhi[q][1] = c.y, bhi[q][2] = c.z;
+        for (int x = 0; x < 3; ++x) {
+            lo[x] = fminf(lo[x], blo[q][x]);
+            hi[x] = fmaxf(hi[x], bhi[q][x]);
+        }
+    }
+    // Slot s is the near-most kid for rays whose direction sign bits equal s: pairs (kid, slot) taken in
+    // ascending order of the kid centre's projection on the slot's diagonal, each kid and slot once.
+    float pc[3];
+    for (int x = 0; x < 3; ++x) pc[x] = __fmul_rn(0.5f, __fadd_rn(lo[x], hi[x]));
+    float dk[8][3];
+    for (int q = 0; q < nk; ++q)
+        for (int x = 0; x < 3; ++x) dk[q][x] = __fsub_rn(__fmul_rn(0.5f, __fadd_rn(blo[q][x], bhi[q][x])), pc[x]);
+    int slot_of[8], kid_in_slot[8];
+    for (int q = 0; q < 8; ++q) slot_of[q] = kid_in_slot[q] = -1;
+    for (int round = 0; round < nk; ++round) {
+        float best = FLT_MAX;
+        int bq = -1, bs = -1;
+        for (int q = 0; q < nk; ++q) {
+            if (slot_of[q] >= 0) continue;
+            for (int s = 0; s < 8; ++s) {
+                if (kid_in_slot[s] >= 0) continue;
+                const float v = __fadd_rn(__fadd_rn(s & 1 ? -dk[q][0] : dk[q][0], s & 2 ? -dk[q][1] : dk[q][1]),
+                                          s & 4 ? -dk[q][2] : dk[q][2]);
+                if (bq < 0 || v < best) {  // first minimum in (kid, slot) order
+                    best = v;
+                    bq = q;
+                    bs = s;
+                }
+            }
+        }
+        slot_of[bq] = bs;
+        kid_in_slot[bs] = bq;
+    }
+    NodeBytes n;
+    for (int w = 0; w < 20; ++w) n.u[w] = 0;
+    const uint32_t child_base = next_base + inner_off[j];
+    const uint32_t ibase = item_base + item_off[j];
+    n.u[4] = child_base;
+    n.u[5] = ibase;
+    uint32_t inner = 0, offset = 0, imask = 0;
+    for (int s = 0; s < 8; ++s) {
+        const int q = kid_in_slot[s];
+        if (q < 0) continue;
+        for (int x = 0; x < 3; ++x) {
+            clo[s][x] = blo[q][x];
+            chi[s][x] = bhi[q][x];
+        }
+        const uint32_t kid = k[q];
+        const uint32_t cnt = t.leaves(kid);
+        if (cnt > ml && kid != b) {
+            imask |= 1u << s;
+            n.b[24 + s] = static_cast<uint8_t>(0x20u | (24u + s));
+            if (inner_off[j] + inner < t.n) next_jobs[inner_off[j] + inner] = kid;
+            ++inner;
+        } else {
+            n.b[24 + s] = static_cast<uint8_t>((((1u << cnt) - 1u) << 5) | offset);
+            const uint32_t f0 = t.first_leaf(kid);
+            for (uint32_t i = 0; i < cnt; ++i)
+                if (ibase + offset + i < t.n && f0 + i < t.n) items[ibase + offset + i] = sorted_faces[f0 + i];
+            offset += cnt;
+        }
+    }
+    n.b[15] = static_cast<uint8_t>(imask);
+    quantize(n, clo, chi, lo, hi);
+    uint4 *dst = nodes + 5ull * (level_base + j);
+    for (int w = 0; w < 5; ++w) dst[w] = n.q[w];
+}
 }  // namespace
 
 cudaError_t launch_refit_triangles(const BlasRefit &r, cudaStream_t stream) {
@@ -176,6 +562,141 @@ cudaError_t launch_update_vertices(float4 *verts, uint32_t vert_base, uint32_t n
     k_update_vertices<<<(num_vertices + 255) / 256, 256, 0, stream>>>(verts + 3ull * vert_base, num_vertices, normals,
                                                                          tangents);
     return cudaGetLastError();
+}
+
+}  // namespace spk
+
+namespace spk {
+namespace {
+
+// Device scratch freed on every exit path.
+struct Scratch {
+    std::vector<void *> ptrs;
+    template <class T>
+    cudaError_t get(T *&p, size_t count) {
+        p = nullptr;
+        void *q = nullptr;
+        const cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+        if (e != cudaSuccess) return e;
+        ptrs.push_back(q);
+        p = static_cast<T *>(q);
+        return cudaSuccess;
+    }
+    ~Scratch() {
+        for (void *q : ptrs) cudaFree(q);
+    }
+};
+
+#define SPK_TRY(x)                              \
+    do {                                        \
+        const cudaError_t e_ = (x);             \
+        if (e_ != cudaSuccess) return e_;       \
+    } while (0)
+
+inline uint32_t blocks(uint64_t n, uint32_t threads) { return static_cast<uint32_t>((n + threads - 1) / threads); }
+
+}  // namespace
+
+cudaError_t build_wide_device(const float *positions, uint32_t num_vertices, const uint32_t *indices,
+                              uint32_t num_faces, int max_children, int max_leaf, cudaStream_t stream, WideBvh &out,
+                              std::vector<uint32_t> &levels) {
+    out = WideBvh{};
+    levels.clear();
+    if (num_faces == 0) return cudaSuccess;
+    max_children = std::max(2, std::min(8, max_children));
+    max_leaf = std::max(1, std::min(3, max_leaf));
+    const uint32_t n = num_faces;
+    const uint32_t tiles = blocks(n, kTile);
+    Scratch sc;
+    float *d_pos;
+    uint32_t *d_idx, *cb, *hist, *vals[2], *left, *right, *parent, *first, *count, *arrivals, *jobs[2], *kids,
+        *inner_cnt, *item_cnt, *totals, *items;
+    uint64_t *keys[2];
+    float4 *flo, *fhi, *nlo, *nhi;
+    uint4 *nodes;
+    SPK_TRY(sc.get(d_pos, 3ull * num_vertices));
+    SPK_TRY(sc.get(d_idx, 3ull * n));
+    SPK_TRY(sc.get(cb, 6));
+    SPK_TRY(sc.get(flo, n));
+    SPK_TRY(sc.get(fhi, n));
+    SPK_TRY(sc.get(keys[0], n));
+    SPK_TRY(sc.get(keys[1], n));
+    SPK_TRY(sc.get(vals[0], n));
+    SPK_TRY(sc.get(vals[1], n));
+    SPK_TRY(sc.get(hist, 256ull * tiles));
+    SPK_TRY(sc.get(left, n));
+    SPK_TRY(sc.get(right, n));
+    SPK_TRY(sc.get(first, n));
+    SPK_TRY(sc.get(count, n));
+    SPK_TRY(sc.get(parent, 2ull * n));
+    SPK_TRY(sc.get(arrivals, n));
+    SPK_TRY(sc.get(nlo, 2ull * n));
+    SPK_TRY(sc.get(nhi, 2ull * n));
+    SPK_TRY(sc.get(jobs[0], n));
+    SPK_TRY(sc.get(jobs[1], n));
+    SPK_TRY(sc.get(kids, 8ull * n));
+    SPK_TRY(sc.get(inner_cnt, n));
+    SPK_TRY(sc.get(item_cnt, n));
+    SPK_TRY(sc.get(totals, 2));
+    SPK_TRY(sc.get(items, n));
+    SPK_TRY(sc.get(nodes, 5ull * n));
+
+    SPK_TRY(cudaMemcpyAsync(d_pos, positions, 3ull * num_vertices * sizeof(float), cudaMemcpyHostToDevice, stream));
+    SPK_TRY(cudaMemcpyAsync(d_idx, indices, 3ull * n * sizeof(uint32_t), cudaMemcpyHostToDevice, stream));
+    const uint32_t cb_init[6] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u};
+    SPK_TRY(cudaMemcpyAsync(cb, cb_init, sizeof(cb_init), cudaMemcpyHostToDevice, stream));
+    k_face_boxes<<<blocks(n, 256), 256, 0, stream>>>(d_pos, d_idx, n, flo, fhi, cb);
+    k_morton<<<blocks(n, 256), 256, 0, stream>>>(flo, fhi, n, cb, keys[0], vals[0]);
+    int cur = 0;
+    for (int shift = 0; shift < 64; shift += 8) {
+        k_radix_count<<<tiles, kSortThreads, 0, stream>>>(keys[cur], n, shift, tiles, hist);
+        k_scan<<<1, kScanThreads, 0, stream>>>(hist, 256u * tiles, nullptr);
+        k_radix_scatter<<<tiles, kSortThreads, 0, stream>>>(keys[cur], vals[cur], n, shift, tiles, hist, keys[cur ^ 1],
+                                                            vals[cur ^ 1]);
+        cur ^= 1;
+    }
+    SPK_TRY(cudaGetLastError());
+    const uint64_t *skeys = keys[cur];
+    const uint32_t *sfaces = vals[cur];
+    SPK_TRY(cudaMemsetAsync(parent, 0xFF, 2ull * n * sizeof(uint32_t), stream));
+    SPK_TRY(cudaMemsetAsync(arrivals, 0, n * sizeof(uint32_t), stream));
+    if (n > 1) k_karras<<<blocks(n - 1, 256), 256, 0, stream>>>(skeys, n, left, right, parent, first, count);
+    k_bottom_up<<<blocks(n, 256), 256, 0, stream>>>(sfaces, flo, fhi, n, left, right, parent, arrivals, nlo, nhi);
+    SPK_TRY(cudaGetLastError());
+
+    BinaryTree t{left, right, first, count, nlo, nhi, n};
+    const uint32_t root = 0;  // internal node 0, or leaf 0 (= node 0) when n == 1
+    SPK_TRY(cudaMemcpyAsync(jobs[0], &root, sizeof(root), cudaMemcpyHostToDevice, stream));
+    uint32_t num_jobs = 1, level_base = 0, item_base = 0;
+    int jc = 0;
+    levels.push_back(0);
+    while (num_jobs > 0) {
+        if (static_cast<uint64_t>(level_base) + num_jobs > n) return cudaErrorUnknown;  // cannot happen: <= n nodes
+        k_collapse_open<<<blocks(num_jobs, 128), 128, 0, stream>>>(t, jobs[jc], num_jobs, max_children, max_leaf, kids,
+                                                                   inner_cnt, item_cnt);
+        k_scan<<<1, kScanThreads, 0, stream>>>(inner_cnt, num_jobs, totals);
+        k_scan<<<1, kScanThreads, 0, stream>>>(item_cnt, num_jobs, totals + 1);
+        const uint32_t next_base = level_base + num_jobs;
+        k_collapse_emit<<<blocks(num_jobs, 128), 128, 0, stream>>>(t, num_jobs, max_leaf, jobs[jc], kids, inner_cnt,
+                                                                   item_cnt, level_base, next_base, item_base, sfaces,
+                                                                   nodes, items, jobs[jc ^ 1]);
+        SPK_TRY(cudaGetLastError());
+        uint32_t tot[2];
+        SPK_TRY(cudaMemcpyAsync(tot, totals, sizeof(tot), cudaMemcpyDeviceToHost, stream));
+        SPK_TRY(cudaStreamSynchronize(stream));
+        level_base = next_base;
+        item_base += tot[1];
+        num_jobs = tot[0];
+        jc ^= 1;
+        levels.push_back(level_base);
+    }
+    if (item_base != n) return cudaErrorUnknown;
+    out.nodes.resize(level_base);
+    out.items.resize(n);
+    static_assert(sizeof(WideNode) == 5 * sizeof(uint4), "node size");
+    SPK_TRY(cudaMemcpyAsync(out.nodes.data(), nodes, level_base * sizeof(WideNode), cudaMemcpyDeviceToHost, stream));
+    SPK_TRY(cudaMemcpyAsync(out.items.data(), items, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream));
+    return cudaStreamSynchronize(stream);
 }
 
 }  // namespace spk

@@ -1,4 +1,4 @@
-// bvh_device.cuh -- BVH work on the device: refitting a mesh's BLAS after its vertices move.
+// bvh_device.cuh -- BVH work on the device: refitting a mesh's BLAS after its vertices move, and building one.
 //
 // Sparkle builds a mesh's BLAS once, in local space, when the primitive is created and rebuilds the TLAS on
 // every primitive change (SceneRenderProxy.cpp:269-297, MeshRenderProxy.cpp:52-92). A deforming mesh (same
@@ -6,11 +6,22 @@
 // positions and the 8-wide nodes are refitted level by level, deepest first, each child box re-quantised
 // exactly as the host builder quantises it (so a refit with unchanged positions reproduces the nodes bit
 // for bit). Traversal results never depend on the tree's shape, only its conservativeness.
+//
+// It also builds a mesh's BLAS on the device (spk_tuning.bvh_builder = 1) in place of the host's binned SAH
+// build: a linear BVH (Karras, "Maximizing Parallelism in the Construction of BVHs, Octrees, and k-d Trees",
+// HPG 2012) over 63-bit Morton codes of the triangle centroids, sorted by a stable LSD radix sort (face index
+// breaks ties), boxes propagated bottom-up with one atomic counter per node, then collapsed into 8-wide nodes
+// breadth first, one launch per level, with the host collapse's rules (open the largest-area inner child
+// until 8, subtrees of <= leaf-size triangles become leaves, octant slot order, the same quantisation).
+// Every step is deterministic: the same mesh gives the same nodes.
 #pragma once
 
 #include <cstdint>
+#include <vector>
 
 #include <cuda_runtime.h>
+
+#include "bvh_builder.h"
 
 namespace spk {
 
@@ -38,5 +49,14 @@ cudaError_t launch_refit_nodes(const BlasRefit &r, uint32_t first, uint32_t last
 // Writes new normals (and, when given, tangents xyzw) into the vertex records verts[3*(vert_base + v)].
 cudaError_t launch_update_vertices(float4 *verts, uint32_t vert_base, uint32_t num_vertices, const float *normals,
                                    const float *tangents, cudaStream_t stream);
+
+// Builds the 8-wide BLAS of one mesh on the device. positions [num_vertices][3] and indices [num_faces][3]
+// are host arrays (indices already checked against num_vertices). `out` receives the nodes (node 0 the
+// root, children after their parent depth by depth) and the leaf items (face indices) as the host builder
+// returns them; `levels` the first node of each depth, then the node count. `max_children` 2..8,
+// `max_leaf` 1..3.
+cudaError_t build_wide_device(const float *positions, uint32_t num_vertices, const uint32_t *indices,
+                              uint32_t num_faces, int max_children, int max_leaf, cudaStream_t stream, WideBvh &out,
+                              std::vector<uint32_t> &levels);
 
 }  // namespace spk

@@ -497,7 +497,8 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
             mb[3 + a] = -std::numeric_limits<double>::max();
         }
         if (m.num_faces == 0) continue;
-        std::vector<BuildBox> boxes(m.num_faces);
+        const bool device_build = ctx->tuning.bvh_builder == 1;
+        std::vector<BuildBox> boxes(device_build ? 0 : m.num_faces);
         for (uint32_t f = 0; f < m.num_faces; ++f) {
             BuildBox b;
             for (int a = 0; a < 3; ++a) {
@@ -513,9 +514,18 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
                     mb[3 + a] = std::max(mb[3 + a], static_cast<double>(p[a]));
                 }
             }
-            boxes[f] = b;
+            if (!device_build) boxes[f] = b;
         }
-        const WideBvh wide = build_wide(boxes, ctx->tuning, threads);
+        WideBvh wide;
+        if (device_build) {
+            std::vector<uint32_t> lv;
+            const cudaError_t e = build_wide_device(m.positions, m.num_vertices, m.indices, m.num_faces,
+                                                    static_cast<int>(ctx->tuning.bvh_width),
+                                                    static_cast<int>(ctx->tuning.bvh_leaf_size), ctx->stream, wide, lv);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "device BVH build");
+        } else {
+            wide = build_wide(boxes, ctx->tuning, threads);
+        }
         const uint32_t tri_offset = static_cast<uint32_t>(hs.tris.size() / 3);
         mbl.root = static_cast<uint32_t>(hs.nodes.size());
         mbl.node_count = static_cast<uint32_t>(wide.nodes.size());
@@ -1517,6 +1527,7 @@ void spk_tuning_defaults(spk_tuning *out) {
     out->extend_blocks_per_sm = 0;
     out->shade_blocks_per_sm = 8;
     out->bvh_collapse = 0;
+    out->bvh_builder = 0;
 }
 
 spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
@@ -1528,8 +1539,8 @@ spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "bvh_leaf_size must be 1..3");
     if (t->extend_blocks_per_sm > 32 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 32)
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "blocks per SM out of range");
-    if (t->ray_sort > 1 || t->bvh_collapse > 1)
-        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "ray_sort and bvh_collapse take 0 or 1");
+    if (t->ray_sort > 1 || t->bvh_collapse > 1 || t->bvh_builder > 1)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "ray_sort, bvh_collapse and bvh_builder take 0 or 1");
     ctx->tuning = *t;
     return SPK_OK;
 }

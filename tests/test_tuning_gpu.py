@@ -12,7 +12,7 @@ from sparkle_gb300 import abi, native, scenes
 pytestmark = pytest.mark.gpu
 
 DEFAULTS = dict(cuda_graph=1, material_sort=0, bvh_width=8, bvh_leaf_size=3, extend_blocks_per_sm=0,
-                shade_blocks_per_sm=8, batch_slots=0, ray_sort=0, bvh_collapse=0)
+                shade_blocks_per_sm=8, batch_slots=0, ray_sort=0, bvh_collapse=0, bvh_builder=0)
 
 VARIANTS = [
     dict(cuda_graph=0),
@@ -25,6 +25,8 @@ VARIANTS = [
     dict(bvh_collapse=1),
     dict(bvh_collapse=1, bvh_width=4, bvh_leaf_size=2),
     dict(ray_sort=1, material_sort=1),
+    dict(bvh_builder=1),
+    dict(bvh_builder=1, bvh_width=4, bvh_leaf_size=1),
 ]
 
 
@@ -97,20 +99,22 @@ def test_graph_replays_keep_accumulating(ctx, cornell):
     ctx.set_tuning(**DEFAULTS)
 
 
-@pytest.mark.parametrize("width,leaf,collapse", [(2, 1, 1), (4, 3, 1), (8, 2, 1), (8, 3, 0), (4, 2, 0)])
-def test_trace_hits_independent_of_bvh_shape(ctx, small_terrain, width, leaf, collapse):
+@pytest.mark.parametrize("width,leaf,collapse,builder", [(2, 1, 1, 0), (4, 3, 1, 0), (8, 2, 1, 0), (8, 3, 0, 0),
+                                                        (4, 2, 0, 0), (8, 3, 0, 1), (2, 1, 0, 1), (8, 1, 0, 1)])
+def test_trace_hits_independent_of_bvh_shape(ctx, small_terrain, width, leaf, collapse, builder):
     scene, _ = small_terrain
     ctx.set_tuning(**DEFAULTS)
     ctx.set_scene(scene)
     rays = scenes.random_rays(*scene.world_bounds(), 50_000, seed=9)
     ref = ctx.trace(rays)
     nodes_default = ctx.stats()["bvh_nodes"]
-    ctx.set_tuning(**{**DEFAULTS, "bvh_width": width, "bvh_leaf_size": leaf, "bvh_collapse": collapse})
+    ctx.set_tuning(**{**DEFAULTS, "bvh_width": width, "bvh_leaf_size": leaf, "bvh_collapse": collapse,
+                      "bvh_builder": builder})
     ctx.set_scene(scene)
     got = ctx.trace(rays)
     st = ctx.stats()
     assert st["error_flags"] == 0
-    if width < 8 and not collapse:
+    if width < 8 and not collapse and not builder:
         assert st["bvh_nodes"] > nodes_default
     for f in ("t", "u", "v", "prim", "face"):
         assert np.array_equal(got[f].view(np.uint32), ref[f].view(np.uint32)), f
