@@ -38,6 +38,7 @@ enum {
     SPK_ERR_NOT_READY = 4,      /* e.g. render before set_scene / set_config */
     SPK_ERR_DEVICE_LIMIT = 5,   /* a device-side bound (traversal stack, iteration budget) was exceeded */
     SPK_ERR_INTERNAL = 6,
+    SPK_ERR_IO = 7,             /* a file could not be written */
 };
 
 typedef struct spk_ctx spk_ctx;
@@ -429,6 +430,51 @@ spk_status spk_read_batch(spk_ctx *ctx, uint32_t index, float *hdr_rgba, uint16_
  * two streams) race on it and must be serialised by the caller. Asynchronous like spk_render;
  * spk_get_stats does not report these calls. */
 spk_status spk_render_noalloc(spk_ctx *ctx, uint32_t num_frames, void *d_hdr_rgba, void *d_rgba16f);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Image output (the reference's screenshot flow)                                                   */
+/* ------------------------------------------------------------------------------------------------ */
+
+enum { SPK_IMAGE_PNG = 0, SPK_IMAGE_HDR = 1, SPK_IMAGE_EXR = 2 };
+
+/* Image2D::CreateFromRawPixels of the RGBA16F output (ConvertPixelsToRGBA8, libraries/source/io/Image.cpp:
+ * 30-67): every colour channel clamped to [0, 1], raised to 0.45 (utilities::LinearToSrgb) and stored as
+ * lround(x * 255); alpha without the power. Converted on the device; `rgba8` (width*height*4 bytes, rows
+ * top first) is a host or device pointer. */
+spk_status spk_read_rgba8(spk_ctx *ctx, uint8_t *rgba8);
+
+/* Renderer::RequestSaveScreenshot + ReadbackFinalOutputIfRequested + Image2D::WriteToFile
+ * (libraries/source/renderer/renderer/Renderer.cpp:94-181, Image.cpp:221-275) without the UI: writes
+ * `path` as SPK_IMAGE_PNG (the spk_read_rgba8 image, 8-bit RGBA), SPK_IMAGE_HDR (Radiance RGBE of the
+ * linear frame buffer, as WriteToFile writes HDR images) or SPK_IMAGE_EXR (the linear frame buffer as
+ * half RGBA, uncompressed scanlines). The path is used as given. */
+spk_status spk_save_image(spk_ctx *ctx, const char *path, uint32_t format);
+
+/* The encoders on caller images (rows top first): RGBA8 to PNG, float RGBA to Radiance HDR, RGBA16F to
+ * OpenEXR; and the RGBA16F -> RGBA8 conversion of spk_read_rgba8 on the host. */
+spk_status spk_write_png(const char *path, const uint8_t *rgba8, uint32_t width, uint32_t height);
+spk_status spk_write_hdr(const char *path, const float *rgba, uint32_t width, uint32_t height);
+spk_status spk_write_exr(const char *path, const uint16_t *rgba16f, uint32_t width, uint32_t height);
+spk_status spk_convert_rgba8(const uint16_t *rgba16f, uint64_t pixels, uint8_t *rgba8);
+
+/* ------------------------------------------------------------------------------------------------ */
+/* Image evaluation                                                                                   */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* The reference's rendering-test score (tests/rendering/render_test_support.py:43-59: mean FLIP of a
+ * screenshot against a ground-truth PNG, both read as RGB / 255, LDR-FLIP with sRGB inputs and default
+ * parameters) on device `device`: the published LDR-FLIP (Andersson et al. 2020) of two width x height RGB
+ * float images in [0, 1] (sRGB-encoded, 3 floats per pixel, host or device pointers).
+ * `pixels_per_degree` is the viewing condition (67.02 = 0.7 m from a 0.7 m wide 3840-pixel screen, FLIP's
+ * default). Writes the per-pixel error to `error_map` (width*height floats, host or device) when it is
+ * not NULL and the mean to *mean_error. */
+spk_status spk_flip(int32_t device, const float *reference_rgb, const float *test_rgb, uint32_t width,
+                    uint32_t height, float pixels_per_degree, float *error_map, double *mean_error);
+
+/* relMSE = mean over the `count` values of (x - ref)^2 / (ref^2 + eps) (the metric of the denoiser
+ * benchmark, eps = 0.01), on device `device`; host or device pointers. */
+spk_status spk_relmse(int32_t device, const float *x, const float *reference, uint64_t count, float eps,
+                      double *out);
 
 #ifdef __cplusplus
 }

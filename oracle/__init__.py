@@ -43,6 +43,7 @@ def lib():
         L.or_rng_fill.argtypes = [C.c_int32, C.c_uint64, C.c_uint32, vp, vp]
         L.or_float_to_half.restype = C.c_uint32
         L.or_float_to_half.argtypes = [C.c_float]
+        L.or_rgba16f_to_rgba8.argtypes = [vp, C.c_uint64, vp]
         L.or_sample_surface.argtypes = [vp, vp, vp, vp, C.c_uint32, vp]
         _lib = L
     return _lib
@@ -142,6 +143,14 @@ def rng_fill(kind: int, seed: int, n: int):
 
 def float_to_half(x: float) -> int:
     return int(lib().or_float_to_half(x))
+
+
+def rgba16f_to_rgba8(rgba16f) -> np.ndarray:
+    """The reference's screenshot conversion (ConvertPixelsToRGBA8, Image.cpp:54-67) of half bits."""
+    src = np.ascontiguousarray(rgba16f, np.uint16)
+    out = np.zeros(src.shape, np.uint8)
+    lib().or_rgba16f_to_rgba8(_p(src), src.size // 4, _p(out))
+    return out
 
 
 def sample_surface(mat: spk_material, ray_dir, normal, tangent, seed: int):

@@ -1637,6 +1637,40 @@ void or_rng_fill(int32_t kind, uint64_t seed, uint32_t n, uint32_t *out_u32, flo
 
 uint32_t or_float_to_half(float f) { return f32_to_f16(f); }
 
+// Eigen::half -> float: sign, 5-bit exponent, 10-bit mantissa; subnormals scaled by 2^-24.
+static float f16_to_f32(uint16_t h) {
+    const int e = (h >> 10) & 31, m = h & 1023;
+    float v;
+    if (e == 0) {
+        v = std::ldexp(static_cast<float>(m), -24);
+    } else if (e == 31) {
+        v = m ? std::numeric_limits<float>::quiet_NaN() : std::numeric_limits<float>::infinity();
+    } else {
+        v = std::ldexp(static_cast<float>(1024 + m), e - 25);
+    }
+    return (h & 0x8000) ? -v : v;
+}
+
+// FloatToUint8 (Image.cpp:31-34). lround of a NaN is unspecified; it is taken as 0 here.
+static uint8_t float_to_uint8(float v) {
+    if (std::isnan(v)) return 0;
+    return static_cast<uint8_t>(std::lround(std::clamp(v, 0.f, 1.f) * 255.f));
+}
+
+// ConvertPixelsToRGBA8, the RGBAFloat16 case (Image.cpp:54-67): rgb.cwiseMax(0).cwiseMin(1), then
+// utilities::LinearToSrgb = pow(x, 0.45f) (Utilities.h:411-414), each channel through FloatToUint8; alpha
+// through FloatToUint8 alone.
+void or_rgba16f_to_rgba8(const uint16_t *in, uint64_t pixels, uint8_t *out) {
+    for (uint64_t i = 0; i < pixels; ++i) {
+        for (int c = 0; c < 3; ++c) {
+            float v = f16_to_f32(in[4 * i + c]);
+            if (!std::isnan(v)) v = std::min(std::max(v, 0.f), 1.f);
+            out[4 * i + c] = float_to_uint8(std::pow(v, 0.45f));
+        }
+        out[4 * i + 3] = float_to_uint8(f16_to_f32(in[4 * i + 3]));
+    }
+}
+
 void or_sample_surface(const spk_material *m, const float ray_dir[3], const float normal[3], const float tangent[3],
                        uint32_t seed, float out[7]) {
     Rng rng;

@@ -19,6 +19,7 @@ SPK_MAT_PBR, SPK_MAT_DIELECTRIC = 0, 1
 SPK_SKY_NONE, SPK_SKY_GRADIENT, SPK_SKY_CUBE = 0, 1, 2
 SPK_RNG_XOSHIRO128P, SPK_RNG_XOSHIRO256SS = 0, 1
 SPK_KERNEL_AUTO, SPK_KERNEL_MEGAKERNEL, SPK_KERNEL_WAVEFRONT = 0, 1, 2
+SPK_IMAGE_PNG, SPK_IMAGE_HDR, SPK_IMAGE_EXR = 0, 1, 2
 
 _f = C.c_float
 _u32 = C.c_uint32

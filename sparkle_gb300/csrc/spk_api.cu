@@ -22,6 +22,7 @@
 #include "../../include/spk.h"
 #include "bvh_builder.h"
 #include "bvh_device.cuh"
+#include "image_io.h"
 #include "kernels.cuh"
 #include "wavefront.cuh"
 
@@ -114,6 +115,9 @@ struct spk_ctx {
     DevBuf<float4> gcolor, gnormal, fb;
     DevBuf<ushort4> out;
     DevBuf<float4> guide_nd, guide_albedo;  // primary-hit guides (spk_render_guides)
+    DevBuf<uint8_t> rgba8_tables;           // half -> RGBA8 tables of the screenshot conversion (colour, alpha)
+    DevBuf<uchar4> rgba8;                   // spk_read_rgba8 scratch
+    DevBuf<ushort4> fb_half;                // spk_save_image (EXR) scratch
     WavefrontState wf{};
     ChunkGraph chunk_graph{};
     // batch (spk_render_batch)
@@ -839,6 +843,9 @@ spk_status spk_destroy(spk_ctx *ctx) {
     ctx->gnormal.reset();
     ctx->guide_nd.reset();
     ctx->guide_albedo.reset();
+    ctx->rgba8_tables.reset();
+    ctx->rgba8.reset();
+    ctx->fb_half.reset();
     ctx->fb.reset();
     ctx->out.reset();
     wavefront_free(ctx->wf);
@@ -1256,6 +1263,90 @@ spk_status spk_read_framebuffer(spk_ctx *ctx, float *hdr_rgba, uint16_t *rgba16f
                              ctx->stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "output image read");
     if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
+    return SPK_OK;
+}
+
+spk_status spk_read_rgba8(spk_ctx *ctx, uint8_t *rgba8) {
+    if (!ctx || !rgba8) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "no frame buffer");
+    cudaSetDevice(ctx->device);
+    cudaError_t e;
+    if (!ctx->rgba8_tables.ptr) {
+        std::vector<uint8_t> tab(2 * 65536);
+        std::memcpy(tab.data(), rgba8_table(true), 65536);
+        std::memcpy(tab.data() + 65536, rgba8_table(false), 65536);
+        if ((e = upload(ctx->rgba8_tables, tab.data(), tab.size(), ctx->stream)) != cudaSuccess)
+            return cuda_fail(ctx, e, "conversion tables");
+    }
+    const uint64_t n = ctx->out.count;
+    if (ctx->rgba8.count != n && (e = alloc(ctx->rgba8, n)) != cudaSuccess) return cuda_fail(ctx, e, "RGBA8 image");
+    if ((e = launch_rgba16f_to_rgba8(ctx->out.ptr, n, ctx->rgba8_tables.ptr, ctx->rgba8.ptr, ctx->stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(rgba8, ctx->rgba8.ptr, n * sizeof(uchar4), cudaMemcpyDefault, ctx->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "RGBA8 conversion");
+    return SPK_OK;
+}
+
+spk_status spk_save_image(spk_ctx *ctx, const char *path, uint32_t format) {
+    if (!ctx || !path || !*path) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "no frame buffer");
+    if (format > SPK_IMAGE_EXR) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "unknown image format %u", format);
+    const uint32_t w = ctx->cfg.width, h = ctx->cfg.height;
+    const uint64_t n = static_cast<uint64_t>(w) * h;
+    std::vector<uint8_t> bytes;
+    cudaError_t e;
+    if (format == SPK_IMAGE_PNG) {
+        std::vector<uint8_t> px(4 * n);
+        const spk_status st = spk_read_rgba8(ctx, px.data());
+        if (st != SPK_OK) return st;
+        bytes = encode_png(px.data(), w, h);
+    } else if (format == SPK_IMAGE_HDR) {
+        std::vector<float> fb(4 * n), top(4 * n);
+        if ((e = cudaMemcpyAsync(fb.data(), ctx->fb.ptr, n * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream)) !=
+                cudaSuccess ||
+            (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+            return cuda_fail(ctx, e, "frame buffer read");
+        for (uint32_t y = 0; y < h; ++y)  // frame buffer rows run bottom up
+            std::memcpy(&top[4ull * y * w], &fb[4ull * (h - 1 - y) * w], 4ull * w * sizeof(float));
+        bytes = encode_hdr(top.data(), w, h);
+    } else {
+        if (ctx->fb_half.count != n && (e = alloc(ctx->fb_half, n)) != cudaSuccess)
+            return cuda_fail(ctx, e, "half image");
+        std::vector<uint16_t> px(4 * n);
+        if ((e = launch_fb_to_half(ctx->fb.ptr, w, h, ctx->fb_half.ptr, ctx->stream)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(px.data(), ctx->fb_half.ptr, n * sizeof(ushort4), cudaMemcpyDeviceToHost,
+                                 ctx->stream)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+            return cuda_fail(ctx, e, "half image");
+        bytes = encode_exr(px.data(), w, h);
+    }
+    std::string err;
+    if (!write_file(path, bytes, err)) return fail(ctx, SPK_ERR_IO, "%s", err.c_str());
+    return SPK_OK;
+}
+
+spk_status spk_write_png(const char *path, const uint8_t *rgba8, uint32_t width, uint32_t height) {
+    if (!path || !rgba8 || width == 0 || height == 0) return SPK_ERR_INVALID_ARGUMENT;
+    std::string err;
+    return write_file(path, encode_png(rgba8, width, height), err) ? SPK_OK : SPK_ERR_IO;
+}
+
+spk_status spk_write_hdr(const char *path, const float *rgba, uint32_t width, uint32_t height) {
+    if (!path || !rgba || width == 0 || height == 0) return SPK_ERR_INVALID_ARGUMENT;
+    std::string err;
+    return write_file(path, encode_hdr(rgba, width, height), err) ? SPK_OK : SPK_ERR_IO;
+}
+
+spk_status spk_write_exr(const char *path, const uint16_t *rgba16f, uint32_t width, uint32_t height) {
+    if (!path || !rgba16f || width == 0 || height == 0) return SPK_ERR_INVALID_ARGUMENT;
+    std::string err;
+    return write_file(path, encode_exr(rgba16f, width, height), err) ? SPK_OK : SPK_ERR_IO;
+}
+
+spk_status spk_convert_rgba8(const uint16_t *rgba16f, uint64_t pixels, uint8_t *rgba8) {
+    if (pixels && (!rgba16f || !rgba8)) return SPK_ERR_INVALID_ARGUMENT;
+    rgba16f_to_rgba8(rgba16f, pixels, rgba8);
     return SPK_OK;
 }
 

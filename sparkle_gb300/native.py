@@ -16,7 +16,7 @@ from .abi import (HIT_DTYPE, MarshalledScene, Scene, affine_inverse, instance_ar
 _lib = None
 
 SPK_ERRORS = {0: "ok", 1: "invalid argument", 2: "cuda error", 3: "out of memory", 4: "not ready",
-              5: "device limit", 6: "internal"}
+              5: "device limit", 6: "internal", 7: "i/o"}
 
 # Every symbol include/spk.h declares.
 EXPORTED = ["spk_abi_version", "spk_create", "spk_destroy", "spk_last_error", "spk_set_scene", "spk_set_camera",
@@ -25,7 +25,9 @@ EXPORTED = ["spk_abi_version", "spk_create", "spk_destroy", "spk_last_error", "s
             "spk_synchronize", "spk_get_stats", "spk_set_instrumentation", "spk_render_noalloc",
             "spk_tuning_defaults", "spk_set_tuning", "spk_get_tuning", "spk_render_guides", "spk_guides_device",
             "spk_read_guides", "spk_set_scenes", "spk_render_batch", "spk_read_batch", "spk_set_instances",
-            "spk_set_instance_transforms", "spk_update_mesh", "spk_read_bvh_nodes",
+            "spk_set_instance_transforms", "spk_update_mesh", "spk_read_bvh_nodes", "spk_read_rgba8",
+            "spk_save_image", "spk_write_png", "spk_write_hdr", "spk_write_exr", "spk_convert_rgba8",
+            "spk_flip", "spk_relmse",
             # include/spk_denoise.h
             "spk_dn_create", "spk_dn_destroy", "spk_dn_last_error", "spk_dn_init", "spk_dn_num_params",
             "spk_dn_get_params", "spk_dn_set_params", "spk_dn_pack_features", "spk_dn_pack_halves", "spk_dn_train_step",
@@ -84,6 +86,14 @@ def lib(build: bool = True):
         L.spk_set_instance_transforms.argtypes = [vp, u32, u32, vp, vp]
         L.spk_update_mesh.argtypes = [vp, u32, u32, vp, vp, vp]
         L.spk_read_bvh_nodes.argtypes = [vp, vp, u64, C.POINTER(u64)]
+        L.spk_read_rgba8.argtypes = [vp, vp]
+        L.spk_save_image.argtypes = [vp, C.c_char_p, u32]
+        L.spk_write_png.argtypes = [C.c_char_p, vp, u32, u32]
+        L.spk_write_hdr.argtypes = [C.c_char_p, vp, u32, u32]
+        L.spk_write_exr.argtypes = [C.c_char_p, vp, u32, u32]
+        L.spk_convert_rgba8.argtypes = [vp, u64, vp]
+        L.spk_flip.argtypes = [i32, vp, vp, u32, u32, C.c_float, vp, C.POINTER(C.c_double)]
+        L.spk_relmse.argtypes = [i32, vp, vp, u64, C.c_float, C.POINTER(C.c_double)]
         L.spk_render_batch.argtypes = [vp, vp, u32, u32, u32]
         L.spk_read_batch.argtypes = [vp, u32, vp, vp]
         L.spk_render_guides.argtypes = [vp]
@@ -116,6 +126,40 @@ def lib(build: bool = True):
 
 def _p(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def _image_call(fn, path, img, dtype, channels=4):
+    img = np.ascontiguousarray(img, dtype)
+    if img.ndim != 3 or img.shape[2] != channels:
+        raise ValueError(f"expected an (H, W, {channels}) image")
+    st = fn(os.fsencode(path), _p(img), img.shape[1], img.shape[0])
+    if st != 0:
+        raise SpkError(st, f"cannot write {path}")
+
+
+def write_png(path, rgba8):
+    """spk_write_png: an (H, W, 4) uint8 image, rows top first."""
+    _image_call(lib().spk_write_png, path, rgba8, np.uint8)
+
+
+def write_hdr(path, rgba):
+    """spk_write_hdr: an (H, W, 4) float32 image (alpha ignored), rows top first, as Radiance RGBE."""
+    _image_call(lib().spk_write_hdr, path, rgba, np.float32)
+
+
+def write_exr(path, rgba16f):
+    """spk_write_exr: an (H, W, 4) uint16 (half bits) image, rows top first, as uncompressed OpenEXR."""
+    _image_call(lib().spk_write_exr, path, rgba16f, np.uint16)
+
+
+def convert_rgba8(rgba16f) -> np.ndarray:
+    """spk_convert_rgba8: the screenshot conversion of an RGBA16F image (uint16 half bits) on the host."""
+    src = np.ascontiguousarray(rgba16f, np.uint16)
+    out = np.zeros(src.shape, np.uint8)
+    st = lib().spk_convert_rgba8(_p(src), src.size // 4, _p(out))
+    if st != 0:
+        raise SpkError(st, "spk_convert_rgba8 failed")
+    return out
 
 
 class Context:
@@ -181,6 +225,16 @@ class Context:
         tan = None if tangents is None else np.ascontiguousarray(tangents, np.float32).reshape(-1, 4)
         self._check(self.L.spk_update_mesh(self.h, mesh_id, pos.shape[0], _p(pos), None if nrm is None else _p(nrm),
                                            None if tan is None else _p(tan)))
+
+    def read_rgba8(self) -> np.ndarray:
+        """spk_read_rgba8: the screenshot image, (H, W, 4) uint8, rows top first."""
+        out = np.zeros((self.config.height, self.config.width, 4), np.uint8)
+        self._check(self.L.spk_read_rgba8(self.h, _p(out)))
+        return out
+
+    def save_image(self, path, fmt: int = 0):
+        """spk_save_image: SPK_IMAGE_PNG (0), SPK_IMAGE_HDR (1) or SPK_IMAGE_EXR (2)."""
+        self._check(self.L.spk_save_image(self.h, os.fsencode(path), fmt))
 
     def bvh_nodes(self) -> np.ndarray:
         """The resident node array as (n, 80) bytes (spk_read_bvh_nodes)."""
