@@ -56,7 +56,7 @@ def test_device_relmse_and_compare_images(tmp_path, cornell):
     x = rng.lognormal(0, 1, 100_003).astype(np.float32)
     r = rng.lognormal(0, 1, 100_003).astype(np.float32)
     ref = np.mean((x.astype(np.float64) - r) ** 2 / (r.astype(np.float64) ** 2 + 0.01))
-    assert abs(evaluate.rel_mse(x, r) - ref) < 1e-9 * max(1.0, ref)
+    assert abs(evaluate.rel_mse(x, r) - ref) < 1e-6 * ref  # fp32 terms, float64 sum
     # the reference's screenshot test flow: two renders at different sample counts written as PNGs
     scene, cam_args = cornell
     W, H = 96, 72
