@@ -1,11 +1,15 @@
 // conv_tc.cu -- tcgen05 implicit-GEMM 3x3 convolutions (see conv_tc.cuh).
 //
-// Forward / dgrad (one CTA per 128-pixel output tile, 4 warps):
-//   warp 0 lane 0  TMA producer: per K block (tap, 32-channel chunk) one 4-D tiled load of the shifted
-//                  input box {32 ch, tw px, th rows, 1 image} (zero fill outside the image = the conv's
-//                  padding) and one 2-D load of the weight slice {32, cout}, into a 4-stage ring;
-//   warp 1 lane 0  MMA issuer: two kind::f16 MMAs (K = 16 each) per stage into a 128 x cout FP32
-//                  accumulator in TMEM, committing each stage back to the producer;
+// Forward / dgrad (one CTA per output tile of tw x th = 128 pixels, tw a multiple of 8, 4 warps):
+//   warp 0 lane 0  TMA producer: per K block (column tap dx, 32-channel chunk) one 4-D tiled load of the
+//                  input box {32 ch, tw px, th + 2 rows, 1 image} shifted by dx and reaching one row above
+//                  and below the tile (zero fill outside the image = the conv's padding), and three 2-D
+//                  loads of the weight slices {32, cout} of the taps (dy, dx), dy = -1, 0, 1, into a ring
+//                  of 2-4 stages;
+//   warp 1 lane 0  MMA issuer: per stage and row tap dy, two kind::f16 MMAs (K = 16 each) whose A operand
+//                  starts (dy + 1) * tw rows into the input box -- a whole number of 8-row swizzle atoms, so
+//                  one box serves all three row taps -- into a 128 x cout FP32 accumulator in TMEM,
+//                  committing each stage back to the producer;
 //   all 4 warps    epilogue: tcgen05.ld of the pixel rows (warp w owns TMEM lanes 32w..32w+31), bias,
 //                  ReLU or ReLU-backward mask, BF16 pack, 16-byte stores.
 // Wgrad (one CTA per (128 rows of (tap, ci), pixel range)): all threads gather and transpose the shifted
@@ -34,6 +38,7 @@ struct FwdParams {
     uint32_t n, h, w;
     uint32_t cin, cout;
     uint32_t tw, th, tiles_x, tiles_y;
+    uint32_t stages, a_bytes, stage_bytes;  // ring depth; input box and stage sizes (1024-byte multiples)
     __nv_bfloat16 *out;
     uint32_t out_ld;
     const float *bias;
@@ -43,8 +48,12 @@ struct FwdParams {
     uint32_t *err;
 };
 
-__host__ __device__ constexpr uint32_t fwd_stage_bytes(uint32_t cout) {
-    return (kATileBytes + cout * 64u + 1023u) & ~1023u;
+// Input box {32 ch, tw, th + 2} and the three weight slices of one column tap, each 1024-byte aligned.
+__host__ __device__ constexpr uint32_t fwd_a_bytes(uint32_t tw, uint32_t th) {
+    return (64u * tw * (th + 2u) + 1023u) & ~1023u;
+}
+__host__ __device__ constexpr uint32_t fwd_stage_bytes(uint32_t tw, uint32_t th, uint32_t cout) {
+    return fwd_a_bytes(tw, th) + ((3u * cout * 64u + 1023u) & ~1023u);
 }
 
 __host__ __device__ constexpr uint32_t tmem_columns(uint32_t n) {
@@ -65,16 +74,16 @@ __global__ void __launch_bounds__(128, 1)
     k_conv_fwd(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, FwdParams P) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = align1024(smem_raw);
-    const uint32_t b_bytes = P.cout * 64u;
-    const uint32_t stage_bytes = fwd_stage_bytes(P.cout);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kStages * stage_bytes);
+    const uint32_t b_bytes = P.cout * 64u;  // one weight slice
+    const uint32_t stage_bytes = P.stage_bytes, nst = P.stages;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + nst * stage_bytes);
     uint64_t *full = bars, *empty = bars + kStages, *accum = bars + 2 * kStages;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 1);
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t ncols = tmem_columns(P.cout);
 
     if (threadIdx.x == 0) {
-        for (uint32_t s = 0; s < kStages; ++s) {
+        for (uint32_t s = 0; s < nst; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
@@ -95,33 +104,40 @@ __global__ void __launch_bounds__(128, 1)
     const uint32_t ty = t % P.tiles_y;
     const uint32_t img = t / P.tiles_y;
     const int x0 = static_cast<int>(tx * P.tw), y0 = static_cast<int>(ty * P.th);
-    const uint32_t nch = P.cin / 32u, nk = 9u * nch;
+    const uint32_t nch = P.cin / 32u, nk = 3u * nch;  // K blocks: (column tap, channel chunk)
 
     if (warp == 0 && lane == 0) {
         for (uint32_t kb = 0; kb < nk; ++kb) {
-            const uint32_t s = kb % kStages, u = kb / kStages;
+            const uint32_t s = kb % nst, u = kb / nst;
             if (u > 0 && !mbar_wait(&empty[s], (u - 1) & 1u, P.err)) break;
             uint8_t *a = smem + s * stage_bytes;
-            mbar_arrive_expect_tx(&full[s], kATileBytes + b_bytes);
-            const uint32_t tap = kb / nch, c = kb - tap * nch;
-            const int dy = static_cast<int>(tap / 3u) - 1, dx = static_cast<int>(tap % 3u) - 1;
-            tma_load_4d(a, &tmx, &full[s], static_cast<int>(c * 32u), x0 + dx, y0 + dy, static_cast<int>(img));
-            tma_load_2d(a + kATileBytes, &tmw, &full[s], static_cast<int>(tap * P.cin + c * 32u), 0);
+            uint8_t *b = a + P.a_bytes;
+            mbar_arrive_expect_tx(&full[s], 64u * P.tw * (P.th + 2u) + 3u * b_bytes);
+            const uint32_t dx3 = kb / nch, c = kb - dx3 * nch;
+            tma_load_4d(a, &tmx, &full[s], static_cast<int>(c * 32u), x0 + static_cast<int>(dx3) - 1, y0 - 1,
+                        static_cast<int>(img));
+            for (uint32_t dy3 = 0; dy3 < 3; ++dy3)
+                tma_load_2d(b + dy3 * b_bytes, &tmw, &full[s], static_cast<int>((dy3 * 3u + dx3) * P.cin + c * 32u), 0);
         }
     } else if (warp == 1 && lane == 0) {
         const uint32_t idesc = idesc_bf16(kTileM, P.cout);
         bool ok = true;
         for (uint32_t kb = 0; kb < nk; ++kb) {
-            const uint32_t s = kb % kStages, u = kb / kStages;
+            const uint32_t s = kb % nst, u = kb / nst;
             if (!mbar_wait(&full[s], u & 1u, P.err)) {
                 ok = false;
                 break;
             }
             tc_fence_after();
-            const uint32_t a = smem_u32(smem + s * stage_bytes), b = a + kATileBytes;
+            const uint32_t a = smem_u32(smem + s * stage_bytes), b = a + P.a_bytes;
 #pragma unroll
-            for (uint32_t k2 = 0; k2 < 2; ++k2)
-                mma_bf16(tmem, smem_desc_sw64(a + 32u * k2), smem_desc_sw64(b + 32u * k2), idesc, (kb | k2) != 0u);
+            for (uint32_t dy3 = 0; dy3 < 3; ++dy3) {
+                const uint32_t ad = a + dy3 * P.tw * 64u, bd = b + dy3 * b_bytes;
+#pragma unroll
+                for (uint32_t k2 = 0; k2 < 2; ++k2)
+                    mma_bf16(tmem, smem_desc_sw64(ad + 32u * k2), smem_desc_sw64(bd + 32u * k2), idesc,
+                             (kb | dy3 | k2) != 0u);
+            }
             mma_commit(&empty[s]);
         }
         if (ok) mma_commit(accum);
@@ -355,7 +371,7 @@ constexpr int kMaxDynSmem = 227 * 1024;
 size_t launch_smem(size_t used, uint32_t tmem_cols) {
     const size_t per_sm = 228u * 1024u;
     const size_t ctas = 512u / tmem_cols;
-    const size_t floor_bytes = per_sm / ctas - 1024u + 1u;  // the SM reserves 1 KB per CTA
+    const size_t floor_bytes = per_sm / (ctas + 1u) - 1024u + 1u;  // the SM reserves 1 KB per CTA: ctas + 1 do not fit
     return std::min<size_t>(kMaxDynSmem, std::max(used, floor_bytes));
 }
 
@@ -371,15 +387,16 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
         return cudaErrorInvalidValue;
     EncodeTiledFn enc = encode_fn();
     if (!enc) return cudaErrorNotSupported;
-    uint32_t tw = 1;
-    while (tw < g.w && tw < kTileM) tw <<= 1;
+    // Tiles of 16 x 8 pixels (8 x 16 below 16 columns): a multiple of 8 columns, so that the row taps'
+    // A operands start on 8-row swizzle atoms of the shared input box.
+    const uint32_t tw = g.w >= 16u ? 16u : 8u;
     const uint32_t th = kTileM / tw;
     CUtensorMap tmx, tmw;
     {
         const cuuint64_t dims[4] = {x.channels, g.w, g.h, g.n};
         const cuuint64_t strides[3] = {static_cast<cuuint64_t>(x.ld) * 2u, static_cast<cuuint64_t>(x.ld) * 2u * g.w,
                                        static_cast<cuuint64_t>(x.ld) * 2u * g.w * g.h};
-        const cuuint32_t box[4] = {32u, tw, th, 1u};
+        const cuuint32_t box[4] = {32u, tw, th + 2u, 1u};
         const cuuint32_t es[4] = {1u, 1u, 1u, 1u};
         if (enc(&tmx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, x.ptr, dims, strides, box, es,
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -406,6 +423,10 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
     P.th = th;
     P.tiles_x = (g.w + tw - 1) / tw;
     P.tiles_y = (g.h + th - 1) / th;
+    P.a_bytes = fwd_a_bytes(tw, th);
+    P.stage_bytes = fwd_stage_bytes(tw, th, cout);
+    // Ring depth: up to 4 stages within 96 KB, never more than the K blocks of a tile (3 per 32 channels).
+    P.stages = std::max(2u, std::min({kStages, 3u * (x.channels / 32u), (96u * 1024u) / P.stage_bytes}));
     P.out = static_cast<__nv_bfloat16 *>(y.ptr);
     P.out_ld = y.ld;
     P.bias = epi.bias;
@@ -413,13 +434,13 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
     P.mask = static_cast<const __nv_bfloat16 *>(epi.mask.ptr);
     P.mask_ld = epi.mask.ld;
     P.err = err;
-    const size_t smem = launch_smem(kStages * fwd_stage_bytes(cout) + 1024 + 256, tmem_columns(cout));
     static std::once_flag attr;
     std::call_once(attr, [] {
         cudaFuncSetAttribute(k_conv_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
     });
     const unsigned long long tiles = static_cast<unsigned long long>(P.tiles_x) * P.tiles_y * g.n;
     if (tiles > 0x7FFFFFFFull) return cudaErrorInvalidValue;
+    const size_t smem = launch_smem(P.stages * P.stage_bytes + 1024 + 256, tmem_columns(cout));
     k_conv_fwd<<<static_cast<unsigned>(tiles), 128, smem, stream>>>(tmx, tmw, P);
     return cudaGetLastError();
 }
