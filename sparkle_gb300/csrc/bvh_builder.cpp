@@ -14,7 +14,10 @@
 namespace spk {
 namespace {
 
-constexpr int kBins = 32;
+#ifndef SPK_SAH_BINS
+#define SPK_SAH_BINS 32  // SAH bins per axis of the binned host build
+#endif
+constexpr int kBins = SPK_SAH_BINS;
 
 inline void box_reset(BuildBox &b) {
     for (int k = 0; k < 3; ++k) {
