@@ -321,8 +321,54 @@ def run_ours(args):
         line["denoise"] = denoise_metric(ctx)
     if world == 1 and not args.no_batch:
         line["batch"] = batch_metric(args.batch_autotune)
+    if world == 1 and not args.no_scene_update:
+        line["scene_update"] = scene_update_metric(scene, camera)
     print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def scene_update_metric(scene, camera):
+    """Scene build and incremental updates on the stress scene (wall time through the C ABI, host arrays in):
+    spk_set_scene with the host SAH and with the device LBVH BLAS builder and the Mrays/s each tree traces at
+    (16 frames of the bench workload, device time), spk_update_mesh of the 2.1M-triangle terrain (device
+    refit of its BLAS + TLAS rebuild) and spk_set_instance_transforms of the 64 spheres (TLAS rebuild)."""
+    import numpy as np
+    from sparkle_gb300 import abi, native
+    c = native.Context(0)
+    cfg = abi.make_config(WIDTH, HEIGHT, spp=1, max_spp=4096, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS, seed=0)
+    out = {}
+    for name, builder in (("host_sah", 0), ("device_lbvh", 1)):
+        c.set_tuning(bvh_builder=builder)
+        c.set_scene(scene)  # warm (allocations, table set-up)
+        t0 = time.perf_counter()
+        c.set_scene(scene)
+        build_ms = (time.perf_counter() - t0) * 1e3
+        c.set_config(cfg)
+        c.set_camera(camera)
+        c.render(4)
+        c.set_camera(camera)
+        c.render(16)
+        st = c.stats()
+        out[name] = {"set_scene_ms": round(build_ms, 1), "bvh_nodes": st["bvh_nodes"],
+                     "mrays": round((st["extension_rays"] + st["shadow_rays"]) / (st["device_ms"] * 1e3), 1)}
+    c.set_tuning(bvh_builder=0)
+    c.set_scene(scene)
+    terrain = scene.meshes[0]
+    moved = terrain.positions.copy()
+    moved[:, 2] += np.float32(0.5) * np.sin(moved[:, 0] * np.float32(0.3)).astype(np.float32)
+    c.update_mesh(0, moved)  # warm
+    t0 = time.perf_counter()
+    c.update_mesh(0, terrain.positions)
+    refit_ms = (time.perf_counter() - t0) * 1e3
+    xf = np.stack([i.transform for i in scene.instances[1:]])
+    t0 = time.perf_counter()
+    c.set_instance_transforms(1, xf)
+    c.synchronize()
+    xf_ms = (time.perf_counter() - t0) * 1e3
+    out["update_mesh_ms"] = {"terrain_triangles": int(terrain.num_faces), "value": round(refit_ms, 2)}
+    out["set_instance_transforms_ms"] = {"instances": len(xf), "value": round(xf_ms, 3)}
+    c.close()
+    return out
 
 
 def batch_metric(autotune: bool = False):
@@ -432,6 +478,35 @@ def run_profile_unet(args):
     dn.close()
 
 
+def run_profile_scene(args):
+    """ncu capture case for the scene-build kernels: the stress scene's BLASes built on the device (LBVH),
+    then the terrain's BLAS refitted once and the 1080p output converted for a screenshot and scored with
+    FLIP against itself. `--grid` shrinks the terrain (cells per side) for multi-pass captures."""
+    import numpy as np
+    from sparkle_gb300 import abi, evaluate, native, scenes
+    scene, cam_args = scenes.terrain_spheres(0, grid=args.grid)
+    ctx = native.Context(0)
+    ctx.set_tuning(bvh_builder=1)
+    t0 = time.perf_counter()
+    ctx.set_scene(scene)
+    build_ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    ctx.update_mesh(0, scene.meshes[0].positions)
+    refit_ms = (time.perf_counter() - t0) * 1e3
+    ctx.set_config(abi.make_config(WIDTH, HEIGHT, spp=1, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS))
+    ctx.set_camera(scenes.make_camera(cam_args, WIDTH, HEIGHT))
+    ctx.render(1)
+    shot = ctx.read_rgba8()
+    rgb = shot[..., :3].astype(np.float32) / np.float32(255)
+    t0 = time.perf_counter()
+    mean = evaluate.flip(rgb, rgb[::-1].copy())
+    flip_ms = (time.perf_counter() - t0) * 1e3
+    print(json.dumps({"profile_scene": True, "triangles": scene.num_triangles, "set_scene_ms": round(build_ms, 1),
+                      "update_mesh_ms": round(refit_ms, 2), "flip_1080p_ms": round(flip_ms, 2),
+                      "flip_mean": round(mean, 5)}), flush=True)
+    ctx.close()
+
+
 def run_profile_rays(args):
     """ncu capture case for the ray-set walk: 4M random rays (origins uniform in the scene box, isotropic
     directions) on the stress scene through spk_trace_device, twice."""
@@ -464,11 +539,15 @@ def main():
     ap.add_argument("--no-denoise", action="store_true", help="skip the denoised-vs-plain time-to-relMSE leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-requests leg")
     ap.add_argument("--batch-autotune", action="store_true", help="autotune the batched leg's launch knobs")
+    ap.add_argument("--no-scene-update", action="store_true", help="skip the scene build / incremental update leg")
     ap.add_argument("--tune", default="", help="spk_tuning knobs, e.g. cuda_graph=0,material_sort=1,bvh_width=4")
     ap.add_argument("--profile-small", action="store_true",
                     help="ncu capture case: the bench workload cut to 2 frames, no timing output")
     ap.add_argument("--profile-unet", action="store_true",
                     help="ncu capture case: one 1080p U-Net inference and one training step")
+    ap.add_argument("--profile-scene", action="store_true",
+                    help="ncu capture case: device BLAS build + refit of the stress scene, screenshot + FLIP")
+    ap.add_argument("--grid", type=int, default=1024, help="terrain cells per side for --profile-scene")
     ap.add_argument("--profile-rays", action="store_true",
                     help="ncu capture case: 4M random rays through spk_trace_device on the stress scene")
     args = ap.parse_args()
@@ -476,6 +555,8 @@ def main():
         run_profile_unet(args)
     elif args.profile_rays:
         run_profile_rays(args)
+    elif args.profile_scene:
+        run_profile_scene(args)
     elif args.profile_small:
         run_profile_small(args)
     elif args.impl == "reference":

@@ -71,13 +71,14 @@ __device__ void quantize(NodeBytes &n, const float clo[8][3], const float chi[8]
     for (int a = 0; a < 3; ++a) {
         const double origin = lo[a];
         const int e = quant_exponent(static_cast<double>(hi[a]) - origin);
-        const double scale = ldexp(1.0, e);
+        // Multiplying by 2^-e is exact, so it gives the host's (x - origin) / 2^e bit for bit.
+        const double inv_scale = ldexp(1.0, -e);
         n.f[a] = lo[a];
         n.b[12 + a] = static_cast<uint8_t>(e + 127);
         for (int s = 0; s < 8; ++s) {
             if (n.b[24 + s] == 0) continue;
-            double ql = floor((static_cast<double>(clo[s][a]) - origin) / scale);
-            double qh = ceil((static_cast<double>(chi[s][a]) - origin) / scale);
+            double ql = floor((static_cast<double>(clo[s][a]) - origin) * inv_scale);
+            double qh = ceil((static_cast<double>(chi[s][a]) - origin) * inv_scale);
             ql = fmax(0.0, fmin(255.0, ql));
             qh = fmax(0.0, fmin(255.0, qh));
             if (qh <= ql) {
@@ -292,6 +293,50 @@ __global__ void k_radix_scatter(const uint64_t *keys, const uint32_t *vals, uint
         running[tid] += total;
         __syncthreads();
     }
+}
+
+// Block-level pass of the exclusive scan: block b scans data[b*kScanChunk ..) in place (coalesced, four
+// values per thread) and writes its total to sums[b].
+constexpr uint32_t kScanChunk = 4u * kScanThreads;
+
+__global__ void k_scan_blocks(uint32_t *data, uint32_t n, uint32_t *sums) {
+    __shared__ uint32_t warp_tot[kScanThreads / 32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint64_t base = static_cast<uint64_t>(blockIdx.x) * kScanChunk + 4ull * tid;
+    uint32_t v[4], run = 0;
+    for (int k = 0; k < 4; ++k) {
+        v[k] = base + k < n ? data[base + k] : 0u;
+        run += v[k];
+    }
+    uint32_t incl = run;  // inclusive scan of the thread sums within the warp
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t o = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+        if (lane >= static_cast<uint32_t>(off)) incl += o;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t t = lane < kScanThreads / 32 ? warp_tot[lane] : 0u, x = t;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t o = __shfl_up_sync(0xFFFFFFFFu, x, off);
+            if (lane >= static_cast<uint32_t>(off)) x += o;
+        }
+        if (lane < kScanThreads / 32) warp_tot[lane] = x - t;  // exclusive warp offsets
+        if (lane == kScanThreads / 32 - 1) sums[blockIdx.x] = x;
+    }
+    __syncthreads();
+    uint32_t acc = warp_tot[warp] + incl - run;
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < n) data[base + k] = acc;
+        acc += v[k];
+    }
+}
+
+__global__ void k_scan_add(uint32_t *data, uint32_t n, const uint32_t *offsets) {
+    const uint64_t i = static_cast<uint64_t>(blockIdx.x) * kScanChunk + threadIdx.x;
+    const uint32_t o = offsets[blockIdx.x];
+    for (int k = 0; k < 4; ++k)
+        if (i + k * kScanThreads < n) data[i + k * kScanThreads] += o;
 }
 
 // In-place exclusive scan of data[0..n) by one block; *total receives the sum.
@@ -595,6 +640,19 @@ struct Scratch {
 
 inline uint32_t blocks(uint64_t n, uint32_t threads) { return static_cast<uint32_t>((n + threads - 1) / threads); }
 
+// Exclusive scan of data[0..n) in place; *total (device) receives the sum. One block for short arrays,
+// else block scans, one scan of the block totals (scratch: blocks(n, kScanChunk) + 1 words) and an add.
+void scan(uint32_t *data, uint32_t n, uint32_t *total, uint32_t *scratch, cudaStream_t stream) {
+    if (n <= kScanChunk) {
+        k_scan<<<1, kScanThreads, 0, stream>>>(data, n, total);
+        return;
+    }
+    const uint32_t nb = blocks(n, kScanChunk);
+    k_scan_blocks<<<nb, kScanThreads, 0, stream>>>(data, n, scratch);
+    k_scan<<<1, kScanThreads, 0, stream>>>(scratch, nb, total);
+    k_scan_add<<<nb, kScanThreads, 0, stream>>>(data, n, scratch);
+}
+
 }  // namespace
 
 cudaError_t build_wide_device(const float *positions, uint32_t num_vertices, const uint32_t *indices,
@@ -637,7 +695,9 @@ cudaError_t build_wide_device(const float *positions, uint32_t num_vertices, con
     SPK_TRY(sc.get(kids, 8ull * n));
     SPK_TRY(sc.get(inner_cnt, n));
     SPK_TRY(sc.get(item_cnt, n));
+    uint32_t *scan_tmp;
     SPK_TRY(sc.get(totals, 2));
+    SPK_TRY(sc.get(scan_tmp, blocks(256ull * tiles > n ? 256ull * tiles : n, kScanChunk) + 1));
     SPK_TRY(sc.get(items, n));
     SPK_TRY(sc.get(nodes, 5ull * n));
 
@@ -650,7 +710,7 @@ cudaError_t build_wide_device(const float *positions, uint32_t num_vertices, con
     int cur = 0;
     for (int shift = 0; shift < 64; shift += 8) {
         k_radix_count<<<tiles, kSortThreads, 0, stream>>>(keys[cur], n, shift, tiles, hist);
-        k_scan<<<1, kScanThreads, 0, stream>>>(hist, 256u * tiles, nullptr);
+        scan(hist, 256u * tiles, nullptr, scan_tmp, stream);
         k_radix_scatter<<<tiles, kSortThreads, 0, stream>>>(keys[cur], vals[cur], n, shift, tiles, hist, keys[cur ^ 1],
                                                             vals[cur ^ 1]);
         cur ^= 1;
@@ -674,8 +734,8 @@ cudaError_t build_wide_device(const float *positions, uint32_t num_vertices, con
         if (static_cast<uint64_t>(level_base) + num_jobs > n) return cudaErrorUnknown;  // cannot happen: <= n nodes
         k_collapse_open<<<blocks(num_jobs, 128), 128, 0, stream>>>(t, jobs[jc], num_jobs, max_children, max_leaf, kids,
                                                                    inner_cnt, item_cnt);
-        k_scan<<<1, kScanThreads, 0, stream>>>(inner_cnt, num_jobs, totals);
-        k_scan<<<1, kScanThreads, 0, stream>>>(item_cnt, num_jobs, totals + 1);
+        scan(inner_cnt, num_jobs, totals, scan_tmp, stream);
+        scan(item_cnt, num_jobs, totals + 1, scan_tmp, stream);
         const uint32_t next_base = level_base + num_jobs;
         k_collapse_emit<<<blocks(num_jobs, 128), 128, 0, stream>>>(t, num_jobs, max_leaf, jobs[jc], kids, inner_cnt,
                                                                    item_cnt, level_base, next_base, item_base, sfaces,
