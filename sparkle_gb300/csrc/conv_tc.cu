@@ -33,6 +33,10 @@ constexpr uint32_t kTileM = 128;
 constexpr uint32_t kStages = 4;
 constexpr uint32_t kATileBytes = kTileM * 64;  // 128 rows x 32 bf16
 constexpr uint32_t kMaxCout = 256;
+#ifndef SPK_CONV_STAGE_BUDGET_KB
+#define SPK_CONV_STAGE_BUDGET_KB 32  // shared memory for the forward kernel's ring (KB): 2 stages, more CTAs per SM
+#endif
+constexpr uint32_t kStageBudget = SPK_CONV_STAGE_BUDGET_KB;
 
 struct FwdParams {
     uint32_t n, h, w;
@@ -425,8 +429,9 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
     P.tiles_y = (g.h + th - 1) / th;
     P.a_bytes = fwd_a_bytes(tw, th);
     P.stage_bytes = fwd_stage_bytes(tw, th, cout);
-    // Ring depth: up to 4 stages within 96 KB, never more than the K blocks of a tile (3 per 32 channels).
-    P.stages = std::max(2u, std::min({kStages, 3u * (x.channels / 32u), (96u * 1024u) / P.stage_bytes}));
+    // Ring depth: up to 4 stages within the stage budget, never more than the K blocks of a tile (3 per 32
+    // channels). A smaller ring leaves room for more CTAs per SM.
+    P.stages = std::max(2u, std::min({kStages, 3u * (x.channels / 32u), (kStageBudget * 1024u) / P.stage_bytes}));
     P.out = static_cast<__nv_bfloat16 *>(y.ptr);
     P.out_ld = y.ld;
     P.bias = epi.bias;
