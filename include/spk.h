@@ -457,6 +457,15 @@ spk_status spk_write_hdr(const char *path, const float *rgba, uint32_t width, ui
 spk_status spk_write_exr(const char *path, const uint16_t *rgba16f, uint32_t width, uint32_t height);
 spk_status spk_convert_rgba8(const uint16_t *rgba16f, uint64_t pixels, uint8_t *rgba8);
 
+/* SkyLight::SetSkyMap's cube cook (SkyLightCookJob::Execute, scene/component/light/SkyLight.cpp:83-113) on
+ * device `device`: the cube_size x cube_size faces (+X, -X, +Y, -Y, +Z, -Z) of the SPK_SKY_CUBE sky the
+ * reference samples on a miss, from a width x height equirectangular sky map (RGBA floats as Image2D holds
+ * them; `srgb` for an sRGB format, decoded after the filter): each texel centre's direction mapped by
+ * CartesianToEquirectangular, the map sampled bilinearly with wrap, rounded to half (RGBAFloat16) with
+ * alpha 1. `cube_rgba` receives 6 * cube_size^2 * 4 floats (host or device). The reference cooks 1024. */
+spk_status spk_sky_from_equirect(int32_t device, const float *rgba, uint32_t width, uint32_t height, uint32_t srgb,
+                                 uint32_t cube_size, float *cube_rgba);
+
 /* ------------------------------------------------------------------------------------------------ */
 /* Image evaluation                                                                                   */
 /* ------------------------------------------------------------------------------------------------ */

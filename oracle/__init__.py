@@ -44,6 +44,7 @@ def lib():
         L.or_float_to_half.restype = C.c_uint32
         L.or_float_to_half.argtypes = [C.c_float]
         L.or_rgba16f_to_rgba8.argtypes = [vp, C.c_uint64, vp]
+        L.or_sky_from_equirect.argtypes = [vp, C.c_uint32, C.c_uint32, C.c_int32, C.c_uint32, vp]
         L.or_sample_surface.argtypes = [vp, vp, vp, vp, C.c_uint32, vp]
         _lib = L
     return _lib
@@ -143,6 +144,14 @@ def rng_fill(kind: int, seed: int, n: int):
 
 def float_to_half(x: float) -> int:
     return int(lib().or_float_to_half(x))
+
+
+def sky_from_equirect(rgba, srgb: bool, n: int) -> np.ndarray:
+    """The reference's sky cube cook (SkyLightCookJob::Execute, SkyLight.cpp:83-113) of an (H, W, 4) map."""
+    src = np.ascontiguousarray(rgba, np.float32)
+    out = np.zeros((6, n, n, 4), np.float32)
+    lib().or_sky_from_equirect(_p(src), src.shape[1], src.shape[0], int(srgb), n, _p(out))
+    return out
 
 
 def rgba16f_to_rgba8(rgba16f) -> np.ndarray:

@@ -1657,6 +1657,49 @@ static uint8_t float_to_uint8(float v) {
     return static_cast<uint8_t>(std::lround(std::clamp(v, 0.f, 1.f) * 255.f));
 }
 
+// SkyLightCookJob::Execute (SkyLight.cpp:83-113): face f texel (i, j) of an n x n cube holds the sky map's
+// Image2D::Sample (Image.h:112-152) at CartesianToEquirectangular (Utilities.h:510-518) of
+// TextureCoordinateToDirection(f, u, v) (Image.h:287-314) at the texel centre, stored through SetPixel
+// into RGBAFloat16 (half RGB, alpha 1). `map` is w x h RGBA floats; `cube` receives 6 x n x n RGBA floats.
+void or_sky_from_equirect(const float *map, uint32_t w, uint32_t h, int32_t srgb, uint32_t n, float *cube) {
+    auto wrap = [](int a, unsigned b) { return (static_cast<unsigned>(a % static_cast<int>(b)) + b) % b; };
+    auto decode = [](float c) { return c < 0.04045f ? c / 12.92f : std::pow((c + 0.055f) / 1.055f, 2.4f); };
+    const float inv_pi = static_cast<float>(0.318309886183790671538);
+    for (uint32_t f = 0; f < 6; ++f)
+        for (uint32_t j = 0; j < n; ++j)
+            for (uint32_t i = 0; i < n; ++i) {
+                const float u = (static_cast<float>(i) + 0.5f) / static_cast<float>(n) * 2.f - 1.f;
+                const float v = (static_cast<float>(j) + 0.5f) / static_cast<float>(n) * 2.f - 1.f;
+                V3 d;
+                switch (f) {
+                case 0: d = V3{1.f, -v, -u}; break;
+                case 1: d = V3{-1.f, -v, u}; break;
+                case 2: d = V3{u, 1.f, v}; break;
+                case 3: d = V3{u, -1.f, -v}; break;
+                case 4: d = V3{u, -v, 1.f}; break;
+                default: d = V3{-u, -v, -1.f}; break;
+                }
+                d = normalized(d);
+                const float eu = std::atan2(d.y, d.x) * (inv_pi * 0.5f) + 0.5f;
+                const float ev = std::asin(-d.z) * inv_pi + 0.5f;
+                const float px = eu * static_cast<float>(w), py = ev * static_cast<float>(h);
+                const int ui = static_cast<int>(px), vi = static_cast<int>(py);  // utilities::Decompose
+                const float uc = px - static_cast<float>(ui), vc = py - static_cast<float>(vi);
+                const float *s00 = map + 4ull * (wrap(vi, h) * w + wrap(ui, w));
+                const float *s10 = map + 4ull * (wrap(vi, h) * w + wrap(ui + 1, w));
+                const float *s01 = map + 4ull * (wrap(vi + 1, h) * w + wrap(ui, w));
+                const float *s11 = map + 4ull * (wrap(vi + 1, h) * w + wrap(ui + 1, w));
+                float *o = cube + 4ull * ((static_cast<uint64_t>(f) * n + j) * n + i);
+                for (int c = 0; c < 3; ++c) {
+                    const float l0 = s00[c] + (s10[c] - s00[c]) * uc, l1 = s01[c] + (s11[c] - s01[c]) * uc;
+                    float r = l0 + (l1 - l0) * vc;
+                    if (srgb) r = decode(r);
+                    o[c] = f16_to_f32(static_cast<uint16_t>(f32_to_f16(r)));
+                }
+                o[3] = 1.f;
+            }
+}
+
 // ConvertPixelsToRGBA8, the RGBAFloat16 case (Image.cpp:54-67): rgb.cwiseMax(0).cwiseMin(1), then
 // utilities::LinearToSrgb = pow(x, 0.45f) (Utilities.h:411-414), each channel through FloatToUint8; alpha
 // through FloatToUint8 alone.

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libspk.so")
 
-CUDA_SOURCES = ["kernels.cu", "wavefront.cu", "spk_api.cu", "conv_tc.cu", "unet.cu", "bvh_device.cu", "image_io.cu", "flip.cu"]
+CUDA_SOURCES = ["kernels.cu", "wavefront.cu", "spk_api.cu", "conv_tc.cu", "unet.cu", "bvh_device.cu", "image_io.cu", "flip.cu", "sky.cu"]
 CXX_SOURCES = ["bvh_builder.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

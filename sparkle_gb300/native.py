@@ -27,7 +27,7 @@ EXPORTED = ["spk_abi_version", "spk_create", "spk_destroy", "spk_last_error", "s
             "spk_read_guides", "spk_set_scenes", "spk_render_batch", "spk_read_batch", "spk_set_instances",
             "spk_set_instance_transforms", "spk_update_mesh", "spk_read_bvh_nodes", "spk_read_rgba8",
             "spk_save_image", "spk_write_png", "spk_write_hdr", "spk_write_exr", "spk_convert_rgba8",
-            "spk_flip", "spk_relmse",
+            "spk_flip", "spk_relmse", "spk_sky_from_equirect",
             # include/spk_denoise.h
             "spk_dn_create", "spk_dn_destroy", "spk_dn_last_error", "spk_dn_init", "spk_dn_num_params",
             "spk_dn_get_params", "spk_dn_set_params", "spk_dn_pack_features", "spk_dn_pack_halves", "spk_dn_train_step",
@@ -94,6 +94,7 @@ def lib(build: bool = True):
         L.spk_convert_rgba8.argtypes = [vp, u64, vp]
         L.spk_flip.argtypes = [i32, vp, vp, u32, u32, C.c_float, vp, C.POINTER(C.c_double)]
         L.spk_relmse.argtypes = [i32, vp, vp, u64, C.c_float, C.POINTER(C.c_double)]
+        L.spk_sky_from_equirect.argtypes = [i32, vp, u32, u32, u32, u32, vp]
         L.spk_render_batch.argtypes = [vp, vp, u32, u32, u32]
         L.spk_read_batch.argtypes = [vp, u32, vp, vp]
         L.spk_render_guides.argtypes = [vp]

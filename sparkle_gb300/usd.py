@@ -21,13 +21,17 @@ mirrors:
   metallic-roughness texture (G roughness, B metallic), a connected normal the normal map. Unauthored
   inputs take UsdPreviewSurface's defaults (diffuse 0.18, emissive 0, metallic 0, roughness 0.5,
   opacity 1, ior 1.5).
-* Cameras and lights are not imported: the path tracer's camera and sky are the caller's.
+* Dome lights (LoadSkyLight, :474-496) become the sky: with a texture file (relative to the USD file) the
+  cube SkyLight cooks from that map (sparkle_gb300.sky), else the gradient sky of its colour x intensity x
+  2^exposure (GetLightColor, :455-458). Distant lights and cameras are not read: the CPU path ignores the
+  directional light and the camera is the caller's.
 
 Where the reference would assert (missing normals), this module computes area-weighted vertex normals.
 faceVarying / uniform / constant primvars are expanded to one vertex per face corner. The exporter writes
 what USDExporter writes: a Z-up stage, one Xform (xformOp:transform) per mesh instance holding its Mesh,
 materials under /_materials as UsdPreviewSurface networks with UsdUVTexture shaders, textures as PNG files
-in textures/ beside the file, spheres skipped (the exporter handles mesh primitives only).
+in textures/ beside the file, a gradient sky as a colour-only dome light, spheres skipped (the exporter
+handles mesh primitives only) and cube skies skipped (their source map is not kept).
 """
 from __future__ import annotations
 
@@ -36,7 +40,7 @@ import re
 
 import numpy as np
 
-from .abi import Instance, Material, Mesh, Scene, Sky, Texture
+from .abi import SPK_SKY_GRADIENT, Instance, Material, Mesh, Scene, Sky, Texture
 
 # --------------------------------------------------------------------------------------------------------
 # Tokenizer and parser of the USDA subset.
@@ -490,8 +494,26 @@ def _index(prims, prefix=""):
     return out
 
 
-def load_usda(path, sky: Sky = None) -> Scene:
-    """Scene (meshes, instances, materials, textures) of a USDA file; `sky` is the caller's."""
+def _dome_sky(p, base_dir, sky_size):
+    def get(*names, default=None):
+        for n in names:
+            if p.attrs.get(n) is not None:
+                return p.attrs[n]
+        return default
+    tex = get("inputs:texture:file", "texture:file")
+    if tex:
+        from .sky import sky_from_file
+        return sky_from_file(os.path.normpath(os.path.join(base_dir, tex[1])), sky_size)
+    color = np.asarray(get("inputs:color", "color", default=(1.0, 1.0, 1.0)), np.float32)
+    scale = np.float32(get("inputs:intensity", "intensity", default=1.0)) * np.float32(
+        2.0 ** float(get("inputs:exposure", "exposure", default=0.0)))
+    return Sky(SPK_SKY_GRADIENT, tuple(float(x) for x in color * scale), None)
+
+
+def load_usda(path, sky: Sky = None, sky_size: int = 1024) -> Scene:
+    """Scene (meshes, instances, materials, textures, sky) of a USDA file. The first dome light of the
+    default prim's subtree gives the sky unless `sky` is given; a textured dome light's cube has
+    sky_size x sky_size faces (the reference cooks 1024)."""
     with open(path, "r", encoding="utf-8") as f:
         layer_meta, roots = _parse(f.read())
     roots = [r for r in roots if r.spec == "def"]
@@ -501,6 +523,7 @@ def load_usda(path, sky: Sky = None) -> Scene:
     meshes, instances, materials, textures = [], [], [], []
     tex_cache, mat_cache = {}, {}
     base_dir = os.path.dirname(os.path.abspath(path))
+    domes = []
 
     def walk(node, parent_world):
         world = parent_world @ _local_matrix(node)
@@ -509,6 +532,8 @@ def load_usda(path, sky: Sky = None) -> Scene:
                 continue
             if c.type == "Xform" or c.type == "":
                 walk(c, world)
+            elif c.type == "DomeLight":
+                domes.append(c)
             elif c.type == "Mesh":
                 mesh, mat_id = _load_mesh(c, prims_by_path, base_dir, textures, tex_cache, mat_cache, materials)
                 if mesh is not None:
@@ -517,7 +542,9 @@ def load_usda(path, sky: Sky = None) -> Scene:
 
     if root is not None:
         walk(root, np.eye(4))
-    return Scene(meshes, instances, materials, sky or Sky(), name=os.path.basename(path), textures=textures)
+    if sky is None:
+        sky = _dome_sky(domes[0], base_dir, sky_size) if domes else Sky()
+    return Scene(meshes, instances, materials, sky, name=os.path.basename(path), textures=textures)
 
 
 # --------------------------------------------------------------------------------------------------------
@@ -612,6 +639,9 @@ def save_usda(scene: Scene, path) -> None:
         mat_names[mid] = mp
         return mp
 
+    if scene.sky is not None and scene.sky.mode == SPK_SKY_GRADIENT:  # procedural: a colour-only dome light
+        lines += ['    def DomeLight "sky"', "    {", f"        color3f inputs:color = ({', '.join(_f(x) for x in scene.sky.color)})",
+                  "        float inputs:intensity = 1", "    }"]
     for k, inst in enumerate(scene.instances):
         if inst.sphere:
             continue  # the exporter writes mesh primitives only
