@@ -432,6 +432,29 @@ spk_status spk_read_batch(spk_ctx *ctx, uint32_t index, float *hdr_rgba, uint16_
 spk_status spk_render_noalloc(spk_ctx *ctx, uint32_t num_frames, void *d_hdr_rgba, void *d_rgba16f);
 
 /* ------------------------------------------------------------------------------------------------ */
+/* Checkpoint / resume and test hooks                                                               */
+/* ------------------------------------------------------------------------------------------------ */
+
+/* No reference counterpart (SessionManager, include/application/SessionManager.h:12-29, keeps the camera
+ * and the config only): a render checkpoint holds the accumulation state -- the frame buffer, the output
+ * image and CameraRenderProxy / CPURenderer's sample bookkeeping -- so that a long render stops and
+ * resumes bit for bit. spk_checkpoint_size gives its byte size for the context's config;
+ * spk_save_checkpoint writes it (host or device buffer of at least that size); spk_load_checkpoint
+ * restores it into a context with the same spk_config (scene and camera set as at the save, before the
+ * load: setting them afterwards restarts the accumulation, as any change does). */
+spk_status spk_checkpoint_size(const spk_ctx *ctx, uint64_t *bytes);
+spk_status spk_save_checkpoint(spk_ctx *ctx, void *buffer, uint64_t size);
+spk_status spk_load_checkpoint(spk_ctx *ctx, const void *buffer, uint64_t size);
+
+/* Test hooks for failure handling, no GPU fault involved. spk_debug_fail_allocation(n): the nth device
+ * allocation the library makes from now on fails as out of memory, once (0 disarms); the entry point
+ * that made it returns SPK_ERR_OUT_OF_MEMORY and its context stays usable. spk_debug_walk_budget(ctx, n):
+ * every ray walk of the context may take at most n node steps (0 = the default 2^20); a walk that runs out
+ * ends and sets the iteration-budget bit of spk_stats.error_flags. */
+void spk_debug_fail_allocation(uint32_t nth);
+spk_status spk_debug_walk_budget(spk_ctx *ctx, uint32_t steps);
+
+/* ------------------------------------------------------------------------------------------------ */
 /* Image output (the reference's screenshot flow)                                                   */
 /* ------------------------------------------------------------------------------------------------ */
 

@@ -85,6 +85,17 @@ spk_status spk_dn_fallback(spk_denoiser *dn, const float *d_denoised, const floa
                            const float *d_plain, uint32_t h, uint32_t w, uint32_t tile, float threshold,
                            float *d_out, uint32_t *fallback_tiles);
 
+/* Training checkpoint: the FP32 parameters, both Adam moments and the step count (spk_dn_state_size
+ * bytes, host buffer), so that training stops and resumes where it was. */
+spk_status spk_dn_state_size(const spk_denoiser *dn, uint64_t *bytes);
+spk_status spk_dn_save_state(spk_denoiser *dn, void *host, uint64_t size);
+spk_status spk_dn_load_state(spk_denoiser *dn, const void *host, uint64_t size);
+
+/* Test hook: one kernel waits on an mbarrier that nothing arrives at. Its bounded wait gives up after 1 s
+ * like every tensor-core kernel's; the call returns SPK_ERR_DEVICE_LIMIT with the time-out bit and the
+ * denoiser stays usable. */
+spk_status spk_dn_debug_wait_timeout(spk_denoiser *dn);
+
 /* Waits for the denoiser's stream. */
 spk_status spk_dn_synchronize(spk_denoiser *dn);
 

@@ -1,5 +1,6 @@
 // bvh_device.cu -- BLAS refit and device BLAS build (bvh_device.cuh).
 #include "bvh_device.cuh"
+#include "fault.h"
 
 #include <algorithm>
 #include <cfloat>
@@ -621,7 +622,8 @@ struct Scratch {
     cudaError_t get(T *&p, size_t count) {
         p = nullptr;
         void *q = nullptr;
-        const cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+        const cudaError_t e =
+            fault_allocation() ? cudaErrorMemoryAllocation : cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
         if (e != cudaSuccess) return e;
         ptrs.push_back(q);
         p = static_cast<T *>(q);

@@ -379,7 +379,25 @@ size_t launch_smem(size_t used, uint32_t tmem_cols) {
     return std::min<size_t>(kMaxDynSmem, std::max(used, floor_bytes));
 }
 
+// Waits on an mbarrier that nothing arrives at: the bounded wait gives up after 1 s and sets
+// kErrWaitTimeout, the failure path every tensor-core kernel takes when its pipeline stalls.
+__global__ void k_wait_probe(uint32_t *err) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_wait(&bar, 0, err);
+    __syncthreads();
+}
+
 }  // namespace
+
+cudaError_t conv_wait_probe(uint32_t *err, cudaStream_t stream) {
+    k_wait_probe<<<1, 32, 0, stream>>>(err);
+    return cudaGetLastError();
+}
 
 cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, const NhwcView &y, const ConvGeom &g,
                             const ConvEpilogue &epi, uint32_t *err, cudaStream_t stream) {

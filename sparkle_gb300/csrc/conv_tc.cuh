@@ -41,6 +41,10 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
 cudaError_t conv3x3_wgrad(const NhwcView &x, const NhwcView &dy, float *dw, const ConvGeom &g, uint32_t *err,
                           cudaStream_t stream);
 
+// One CTA waits on an mbarrier nothing arrives at; the wait gives up after 1 s and ORs kErrWaitTimeout into
+// *err (tests of the bounded-wait failure path).
+cudaError_t conv_wait_probe(uint32_t *err, cudaStream_t stream);
+
 // wt[ci][tap][co] = w[co][8 - tap][ci] (bf16), the dgrad weights.
 cudaError_t conv3x3_transpose_weights(const void *w, void *wt, uint32_t cout, uint32_t cin, cudaStream_t stream);
 

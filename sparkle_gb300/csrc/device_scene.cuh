@@ -93,6 +93,7 @@ struct DevScene {
     uint32_t num_scenes;
     float box_lo[3];     // world bounds of all scenes (ray sort cells)
     float box_scale[3];  // 8 / extent per axis (0 for a flat axis)
+    uint32_t walk_budget;  // node steps a walk may take before it reports kErrIterationBudget; 0 = 2^20
 };
 
 // The DevScene of scene `k` of a multi-scene context: scene 0's record with the TLAS root, sky and light

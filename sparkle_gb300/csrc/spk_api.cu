@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <array>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -22,11 +23,28 @@
 #include "../../include/spk.h"
 #include "bvh_builder.h"
 #include "bvh_device.cuh"
+#include "fault.h"
 #include "image_io.h"
 #include "kernels.cuh"
 #include "wavefront.cuh"
 
 using namespace spk;
+
+namespace spk {
+namespace {
+std::atomic<unsigned> g_fail_allocation{0};  // the nth next device allocation fails; 0: none
+}  // namespace
+
+void fault_arm_allocation(unsigned nth) { g_fail_allocation.store(nth); }
+
+bool fault_allocation() {
+    unsigned c = g_fail_allocation.load();
+    while (c > 0) {
+        if (g_fail_allocation.compare_exchange_weak(c, c - 1)) return c == 1;
+    }
+    return false;
+}
+}  // namespace spk
 
 namespace {
 
@@ -162,7 +180,7 @@ template <class T>
 cudaError_t upload(DevBuf<T> &buf, const T *host, size_t count, cudaStream_t stream) {
     buf.reset();
     if (count == 0) return cudaSuccess;
-    cudaError_t e = cudaMalloc(&buf.ptr, count * sizeof(T));
+    cudaError_t e = fault_allocation() ? cudaErrorMemoryAllocation : cudaMalloc(&buf.ptr, count * sizeof(T));
     if (e != cudaSuccess) return e;
     buf.count = count;
     e = cudaMemcpyAsync(buf.ptr, host, count * sizeof(T), cudaMemcpyHostToDevice, stream);
@@ -176,7 +194,7 @@ cudaError_t upload_with_capacity(DevBuf<T> &buf, const T *host, size_t count, si
     buf.reset();
     capacity = std::max(capacity, count);
     if (capacity == 0) return cudaSuccess;
-    cudaError_t e = cudaMalloc(&buf.ptr, capacity * sizeof(T));
+    cudaError_t e = fault_allocation() ? cudaErrorMemoryAllocation : cudaMalloc(&buf.ptr, capacity * sizeof(T));
     if (e != cudaSuccess) return e;
     buf.count = capacity;
     if (capacity > count &&
@@ -191,7 +209,7 @@ template <class T>
 cudaError_t alloc(DevBuf<T> &buf, size_t count) {
     buf.reset();
     if (count == 0) return cudaSuccess;
-    cudaError_t e = cudaMalloc(&buf.ptr, count * sizeof(T));
+    cudaError_t e = fault_allocation() ? cudaErrorMemoryAllocation : cudaMalloc(&buf.ptr, count * sizeof(T));
     if (e == cudaSuccess) buf.count = count;
     return e;
 }
@@ -1263,6 +1281,93 @@ spk_status spk_read_framebuffer(spk_ctx *ctx, float *hdr_rgba, uint16_t *rgba16f
                              ctx->stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "output image read");
     if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
+    return SPK_OK;
+}
+
+// Render checkpoint: a header (magic, version, the spk_config, the sample bookkeeping), then the frame
+// buffer (width * height float4) and the output image (width * height half4).
+namespace {
+struct CheckpointHeader {
+    char magic[8];
+    uint32_t version;
+    uint32_t reserved;
+    spk_config config;
+    uint32_t cumulated, pending, dispatched, dirty;
+};
+constexpr char kCheckpointMagic[8] = {'S', 'P', 'K', 'C', 'K', 'P', 'T', '1'};
+
+uint64_t checkpoint_bytes(const spk_ctx *ctx) {
+    const uint64_t n = static_cast<uint64_t>(ctx->cfg.width) * ctx->cfg.height;
+    return sizeof(CheckpointHeader) + n * (sizeof(float4) + sizeof(ushort4));
+}
+}  // namespace
+
+spk_status spk_checkpoint_size(const spk_ctx *ctx, uint64_t *bytes) {
+    if (!ctx || !bytes) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_config) return SPK_ERR_NOT_READY;
+    *bytes = checkpoint_bytes(ctx);
+    return SPK_OK;
+}
+
+spk_status spk_save_checkpoint(spk_ctx *ctx, void *buffer, uint64_t size) {
+    if (!ctx || !buffer) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "no frame buffer");
+    if (size < checkpoint_bytes(ctx)) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "checkpoint buffer too small");
+    cudaSetDevice(ctx->device);
+    CheckpointHeader h{};
+    std::memcpy(h.magic, kCheckpointMagic, 8);
+    h.version = 1;
+    h.config = ctx->cfg;
+    h.cumulated = ctx->cumulated;
+    h.pending = ctx->pending;
+    h.dispatched = ctx->dispatched;
+    h.dirty = ctx->dirty ? 1u : 0u;
+    auto *out = static_cast<uint8_t *>(buffer);
+    std::memcpy(out, &h, sizeof(h));
+    const uint64_t n = static_cast<uint64_t>(ctx->cfg.width) * ctx->cfg.height;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(out + sizeof(h), ctx->fb.ptr, n * sizeof(float4), cudaMemcpyDefault, ctx->stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(out + sizeof(h) + n * sizeof(float4), ctx->out.ptr, n * sizeof(ushort4), cudaMemcpyDefault,
+                             ctx->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "checkpoint read");
+    return SPK_OK;
+}
+
+spk_status spk_load_checkpoint(spk_ctx *ctx, const void *buffer, uint64_t size) {
+    if (!ctx || !buffer) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "set the checkpoint's config first");
+    CheckpointHeader h{};
+    if (size < sizeof(h)) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "checkpoint truncated");
+    std::memcpy(&h, buffer, sizeof(h));
+    if (std::memcmp(h.magic, kCheckpointMagic, 8) != 0 || h.version != 1)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "not a render checkpoint of this version");
+    if (std::memcmp(&h.config, &ctx->cfg, sizeof(spk_config)) != 0)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "checkpoint config differs from the context's");
+    if (size < checkpoint_bytes(ctx)) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "checkpoint truncated");
+    cudaSetDevice(ctx->device);
+    const uint64_t n = static_cast<uint64_t>(ctx->cfg.width) * ctx->cfg.height;
+    const auto *in = static_cast<const uint8_t *>(buffer);
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(ctx->fb.ptr, in + sizeof(h), n * sizeof(float4), cudaMemcpyDefault, ctx->stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(ctx->out.ptr, in + sizeof(h) + n * sizeof(float4), n * sizeof(ushort4), cudaMemcpyDefault,
+                             ctx->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+        return cuda_fail(ctx, e, "checkpoint write");
+    ctx->cumulated = h.cumulated;
+    ctx->pending = h.pending;
+    ctx->dispatched = h.dispatched;
+    ctx->dirty = h.dirty != 0;  // the accumulation continues from the saved state, not from a cleared one
+    return SPK_OK;
+}
+
+void spk_debug_fail_allocation(uint32_t nth) { fault_arm_allocation(nth); }
+
+spk_status spk_debug_walk_budget(spk_ctx *ctx, uint32_t steps) {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    ctx->scene.walk_budget = steps;
     return SPK_OK;
 }
 

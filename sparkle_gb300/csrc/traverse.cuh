@@ -175,7 +175,7 @@ struct Walker {
     uint2 ngroup, tgroup;
     int sp, blas_sp;
     uint32_t cur_inst;
-    uint32_t iter;
+    uint32_t iter, budget;
     bool in_blas;
     float tmax_box, tmax_occl;
     TraceResult best;
@@ -191,6 +191,7 @@ struct Walker {
         blas_sp = 0;
         cur_inst = 0;
         iter = 0;
+        budget = S.walk_budget ? S.walk_budget : kMaxIterations;
         in_blas = false;
         tmax_occl = tmax;
         tmax_box = (kMode == kTraceOcclusion) ? tmax : kFltMax;
@@ -214,7 +215,7 @@ struct Walker {
     }
 
     __device__ __forceinline__ bool step(const DevScene &S, uint2 *stack, uint32_t &err, TraceCounts *counts) {
-        if (++iter > kMaxIterations) {
+        if (++iter > budget) {
             err |= kErrIterationBudget;
             return true;
         }

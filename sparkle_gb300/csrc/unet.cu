@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "conv_tc.cuh"
+#include "fault.h"
 #include "spk_denoise.h"
 
 using bf16 = __nv_bfloat16;
@@ -82,7 +83,8 @@ struct DBuf {
         if (p) cudaFree(p);
         p = nullptr;
         n = 0;
-        const cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&p), std::max<size_t>(count, 1) * sizeof(T));
+        const cudaError_t e = fault_allocation() ? cudaErrorMemoryAllocation
+                                                 : cudaMalloc(reinterpret_cast<void **>(&p), std::max<size_t>(count, 1) * sizeof(T));
         if (e == cudaSuccess) n = count;
         return e;
     }
@@ -736,6 +738,69 @@ spk_status spk_dn_set_params(spk_denoiser *dn, const float *host, uint64_t count
     DN_TRY(refresh_weights(dn), "weight conversion");
     DN_TRY(cudaStreamSynchronize(dn->stream), "synchronize");
     return SPK_OK;
+}
+
+namespace {
+struct DnStateHeader {
+    char magic[8];
+    uint32_t version, reserved;
+    uint64_t nparams, adam_t;
+};
+constexpr char kDnStateMagic[8] = {'S', 'P', 'K', 'D', 'N', 'S', 'T', '1'};
+}  // namespace
+
+spk_status spk_dn_state_size(const spk_denoiser *dn, uint64_t *bytes) {
+    if (!dn || !bytes) return SPK_ERR_INVALID_ARGUMENT;
+    *bytes = sizeof(DnStateHeader) + 3ull * dn->nparams * sizeof(float);
+    return SPK_OK;
+}
+
+spk_status spk_dn_save_state(spk_denoiser *dn, void *host, uint64_t size) {
+    if (!dn || !host) return SPK_ERR_INVALID_ARGUMENT;
+    const uint64_t nb = dn->nparams * sizeof(float);
+    if (size < sizeof(DnStateHeader) + 3 * nb) return dn_fail(dn, SPK_ERR_INVALID_ARGUMENT, "state buffer too small");
+    cudaSetDevice(dn->device);
+    DnStateHeader h{};
+    std::memcpy(h.magic, kDnStateMagic, 8);
+    h.version = 1;
+    h.nparams = dn->nparams;
+    h.adam_t = dn->adam_t;
+    auto *out = static_cast<uint8_t *>(host);
+    std::memcpy(out, &h, sizeof(h));
+    out += sizeof(h);
+    DN_TRY(cudaMemcpyAsync(out, dn->params.p, nb, cudaMemcpyDeviceToHost, dn->stream), "state read");
+    DN_TRY(cudaMemcpyAsync(out + nb, dn->adam_m.p, nb, cudaMemcpyDeviceToHost, dn->stream), "state read");
+    DN_TRY(cudaMemcpyAsync(out + 2 * nb, dn->adam_v.p, nb, cudaMemcpyDeviceToHost, dn->stream), "state read");
+    DN_TRY(cudaStreamSynchronize(dn->stream), "synchronize");
+    return SPK_OK;
+}
+
+spk_status spk_dn_load_state(spk_denoiser *dn, const void *host, uint64_t size) {
+    if (!dn || !host) return SPK_ERR_INVALID_ARGUMENT;
+    DnStateHeader h{};
+    if (size < sizeof(h)) return dn_fail(dn, SPK_ERR_INVALID_ARGUMENT, "state truncated");
+    std::memcpy(&h, host, sizeof(h));
+    if (std::memcmp(h.magic, kDnStateMagic, 8) != 0 || h.version != 1)
+        return dn_fail(dn, SPK_ERR_INVALID_ARGUMENT, "not a denoiser training state of this version");
+    if (h.nparams != dn->nparams) return dn_fail(dn, SPK_ERR_INVALID_ARGUMENT, "state holds another network size");
+    const uint64_t nb = dn->nparams * sizeof(float);
+    if (size < sizeof(h) + 3 * nb) return dn_fail(dn, SPK_ERR_INVALID_ARGUMENT, "state truncated");
+    cudaSetDevice(dn->device);
+    const auto *in = static_cast<const uint8_t *>(host) + sizeof(h);
+    DN_TRY(cudaMemcpyAsync(dn->params.p, in, nb, cudaMemcpyHostToDevice, dn->stream), "state write");
+    DN_TRY(cudaMemcpyAsync(dn->adam_m.p, in + nb, nb, cudaMemcpyHostToDevice, dn->stream), "state write");
+    DN_TRY(cudaMemcpyAsync(dn->adam_v.p, in + 2 * nb, nb, cudaMemcpyHostToDevice, dn->stream), "state write");
+    DN_TRY(refresh_weights(dn), "weight conversion");
+    DN_TRY(cudaStreamSynchronize(dn->stream), "synchronize");
+    dn->adam_t = h.adam_t;
+    return SPK_OK;
+}
+
+spk_status spk_dn_debug_wait_timeout(spk_denoiser *dn) {
+    if (!dn) return SPK_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(dn->device);
+    DN_TRY(conv_wait_probe(dn->err.p, dn->stream), "wait probe");
+    return check_errors(dn);
 }
 
 spk_status spk_dn_pack_features(spk_denoiser *dn, const float *d_hdr, const float *d_nd, const float *d_alb,

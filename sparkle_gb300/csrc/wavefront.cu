@@ -7,6 +7,7 @@
 #include <cstring>
 
 #include "wavefront.cuh"
+#include "fault.h"
 
 #ifndef SPK_SHADE_MIN_BLOCKS
 #define SPK_SHADE_MIN_BLOCKS 8  // resident 128-thread blocks per SM the shading kernels are compiled for (64 registers)
@@ -621,6 +622,7 @@ __global__ void __launch_bounds__(256) k_b_resolve(BatchParams b, WavefrontState
 
 template <class T>
 cudaError_t dmalloc(T *&p, size_t count) {
+    if (fault_allocation()) return cudaErrorMemoryAllocation;
     return cudaMalloc(reinterpret_cast<void **>(&p), count * sizeof(T));
 }
 

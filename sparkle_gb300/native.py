@@ -32,7 +32,9 @@ EXPORTED = ["spk_abi_version", "spk_create", "spk_destroy", "spk_last_error", "s
             "spk_dn_create", "spk_dn_destroy", "spk_dn_last_error", "spk_dn_init", "spk_dn_num_params",
             "spk_dn_get_params", "spk_dn_set_params", "spk_dn_pack_features", "spk_dn_pack_halves", "spk_dn_train_step",
             "spk_dn_gradients", "spk_dn_infer", "spk_dn_fallback", "spk_dn_synchronize", "spk_dn_last_ms",
-            "spk_dn_conv3x3"]
+            "spk_dn_conv3x3", "spk_dn_state_size", "spk_dn_save_state", "spk_dn_load_state",
+            "spk_dn_debug_wait_timeout", "spk_checkpoint_size", "spk_save_checkpoint", "spk_load_checkpoint",
+            "spk_debug_fail_allocation", "spk_debug_walk_budget"]
 
 
 class SpkError(RuntimeError):
@@ -95,6 +97,16 @@ def lib(build: bool = True):
         L.spk_flip.argtypes = [i32, vp, vp, u32, u32, C.c_float, vp, C.POINTER(C.c_double)]
         L.spk_relmse.argtypes = [i32, vp, vp, u64, C.c_float, C.POINTER(C.c_double)]
         L.spk_sky_from_equirect.argtypes = [i32, vp, u32, u32, u32, u32, vp]
+        L.spk_checkpoint_size.argtypes = [vp, C.POINTER(u64)]
+        L.spk_save_checkpoint.argtypes = [vp, vp, u64]
+        L.spk_load_checkpoint.argtypes = [vp, vp, u64]
+        L.spk_debug_fail_allocation.argtypes = [u32]
+        L.spk_debug_fail_allocation.restype = None
+        L.spk_debug_walk_budget.argtypes = [vp, u32]
+        L.spk_dn_state_size.argtypes = [vp, C.POINTER(u64)]
+        L.spk_dn_save_state.argtypes = [vp, vp, u64]
+        L.spk_dn_load_state.argtypes = [vp, vp, u64]
+        L.spk_dn_debug_wait_timeout.argtypes = [vp]
         L.spk_render_batch.argtypes = [vp, vp, u32, u32, u32]
         L.spk_read_batch.argtypes = [vp, u32, vp, vp]
         L.spk_render_guides.argtypes = [vp]
@@ -127,6 +139,11 @@ def lib(build: bool = True):
 
 def _p(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def debug_fail_allocation(nth: int):
+    """spk_debug_fail_allocation: the nth device allocation from now fails once (0 disarms)."""
+    lib().spk_debug_fail_allocation(nth)
 
 
 def _image_call(fn, path, img, dtype, channels=4):
@@ -236,6 +253,23 @@ class Context:
     def save_image(self, path, fmt: int = 0):
         """spk_save_image: SPK_IMAGE_PNG (0), SPK_IMAGE_HDR (1) or SPK_IMAGE_EXR (2)."""
         self._check(self.L.spk_save_image(self.h, os.fsencode(path), fmt))
+
+    def save_checkpoint(self) -> bytes:
+        """spk_save_checkpoint: the accumulation state (frame buffer, output image, sample bookkeeping)."""
+        n = C.c_uint64()
+        self._check(self.L.spk_checkpoint_size(self.h, C.byref(n)))
+        buf = np.zeros(n.value, np.uint8)
+        self._check(self.L.spk_save_checkpoint(self.h, _p(buf), n.value))
+        return buf.tobytes()
+
+    def load_checkpoint(self, data: bytes):
+        """spk_load_checkpoint: resume from save_checkpoint() bytes (same config; scene and camera set)."""
+        buf = np.frombuffer(data, np.uint8)
+        self._check(self.L.spk_load_checkpoint(self.h, _p(buf), buf.size))
+
+    def debug_walk_budget(self, steps: int):
+        """spk_debug_walk_budget: at most `steps` node steps per ray walk (0 = the default)."""
+        self._check(self.L.spk_debug_walk_budget(self.h, steps))
 
     def bvh_nodes(self) -> np.ndarray:
         """The resident node array as (n, 80) bytes (spk_read_bvh_nodes)."""
@@ -416,6 +450,23 @@ class Denoiser:
 
     def init(self, seed: int):
         self._check(self.L.spk_dn_init(self.h, seed))
+
+    def save_state(self) -> bytes:
+        """spk_dn_save_state: parameters, Adam moments and step count (a training checkpoint)."""
+        n = C.c_uint64()
+        self._check(self.L.spk_dn_state_size(self.h, C.byref(n)))
+        buf = np.zeros(n.value, np.uint8)
+        self._check(self.L.spk_dn_save_state(self.h, _p(buf), n.value))
+        return buf.tobytes()
+
+    def load_state(self, data: bytes):
+        """spk_dn_load_state: resume training from save_state() bytes."""
+        buf = np.frombuffer(data, np.uint8)
+        self._check(self.L.spk_dn_load_state(self.h, _p(buf), buf.size))
+
+    def debug_wait_timeout(self):
+        """spk_dn_debug_wait_timeout: a kernel whose bounded mbarrier wait runs out (raises SpkError 5)."""
+        self._check(self.L.spk_dn_debug_wait_timeout(self.h))
 
     def get_params(self) -> np.ndarray:
         out = np.empty(self.num_params, np.float32)
