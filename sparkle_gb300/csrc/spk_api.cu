@@ -5,6 +5,7 @@
 // the frame buffers, and the sample bookkeeping of CameraRenderProxy (CameraRenderProxy.cpp:66-75) and
 // CPURenderer::dispatched_sample_count_ (CPURenderer.cpp:128-137, 206-207).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <array>
@@ -47,6 +48,15 @@ bool fault_allocation() {
 }  // namespace spk
 
 namespace {
+
+// An NVTX range around one entry point (shown by Nsight tools; free when no tool is attached), the
+// PROFILE_SCOPE of the reference's passes (core/Profiler.h:9-28).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 template <class T>
 struct DevBuf {
@@ -893,6 +903,7 @@ spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_mesh
 }
 
 spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t num_scenes) {
+    NvtxRange range("spk_set_scenes");
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     if (!scenes || num_scenes == 0) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "no scenes");
     cudaSetDevice(ctx->device);
@@ -943,6 +954,7 @@ spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t n
 }
 
 spk_status spk_set_instances(spk_ctx *ctx, const spk_instance *instances, uint32_t num_instances) {
+    NvtxRange range("spk_set_instances");
     spk_status st = require_dynamic(ctx);
     if (st != SPK_OK) return st;
     if (num_instances && !instances) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "null instance array");
@@ -962,6 +974,7 @@ spk_status spk_set_instances(spk_ctx *ctx, const spk_instance *instances, uint32
 
 spk_status spk_set_instance_transforms(spk_ctx *ctx, uint32_t first, uint32_t count, const float *transforms,
                                        const float *inv_transforms) {
+    NvtxRange range("spk_set_instance_transforms");
     spk_status st = require_dynamic(ctx);
     if (st != SPK_OK) return st;
     DynScene &dy = ctx->dyn;
@@ -978,6 +991,7 @@ spk_status spk_set_instance_transforms(spk_ctx *ctx, uint32_t first, uint32_t co
 
 spk_status spk_update_mesh(spk_ctx *ctx, uint32_t mesh_id, uint32_t num_vertices, const float *positions,
                            const float *normals, const float *tangents) {
+    NvtxRange range("spk_update_mesh");
     spk_status st = require_dynamic(ctx);
     if (st != SPK_OK) return st;
     DynScene &dy = ctx->dyn;
@@ -1260,6 +1274,7 @@ static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
 }
 
 spk_status spk_render(spk_ctx *ctx, uint32_t num_frames) {
+    NvtxRange range("spk_render");
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_scene || !ctx->has_config || !ctx->has_camera)
         return fail(ctx, SPK_ERR_NOT_READY, "render needs spk_set_scene, spk_set_config and spk_set_camera first");
@@ -1394,6 +1409,7 @@ spk_status spk_read_rgba8(spk_ctx *ctx, uint8_t *rgba8) {
 }
 
 spk_status spk_save_image(spk_ctx *ctx, const char *path, uint32_t format) {
+    NvtxRange range("spk_save_image");
     if (!ctx || !path || !*path) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "no frame buffer");
     if (format > SPK_IMAGE_EXR) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "unknown image format %u", format);
@@ -1499,6 +1515,7 @@ spk_status spk_trace_device(spk_ctx *ctx, const void *d_rays, uint64_t num_rays,
 }
 
 spk_status spk_trace(spk_ctx *ctx, const spk_ray *rays, uint64_t num_rays, spk_hit *hits, int32_t any_hit) {
+    NvtxRange range("spk_trace");
     if (!ctx || (num_rays && (!rays || !hits))) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_scene) return fail(ctx, SPK_ERR_NOT_READY, "trace needs spk_set_scene first");
     cudaSetDevice(ctx->device);
@@ -1570,6 +1587,7 @@ spk_status spk_get_stats(spk_ctx *ctx, spk_stats *out) {
 }
 
 spk_status spk_render_guides(spk_ctx *ctx) {
+    NvtxRange range("spk_render_guides");
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_scene || !ctx->has_config || !ctx->has_camera)
         return fail(ctx, SPK_ERR_NOT_READY, "guides need spk_set_scene, spk_set_config and spk_set_camera first");
@@ -1615,6 +1633,7 @@ spk_status spk_read_guides(spk_ctx *ctx, float *normal_depth, float *albedo) {
 
 spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t num_requests, uint32_t rng,
                             uint32_t enable_nee) {
+    NvtxRange range("spk_render_batch");
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_scene) return fail(ctx, SPK_ERR_NOT_READY, "batch needs spk_set_scenes first");
     if (!requests || num_requests == 0) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "no requests");

@@ -6,6 +6,7 @@
 // upsampled input fills channels [0, W[l+1]) and the encoder's second conv writes its output straight into
 // channels [W[l+1], W[l+1] + W[l]), so concatenation costs nothing.
 #include <cuda_bf16.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -382,6 +383,12 @@ struct NormalGen {
 }  // namespace spk
 
 using namespace spk;
+
+// An NVTX range around one denoiser entry point (shown by Nsight tools; free when none is attached).
+struct DnRange {
+    explicit DnRange(const char *name) { nvtxRangePushA(name); }
+    ~DnRange() { nvtxRangePop(); }
+};
 
 struct spk_denoiser {
     int device = 0;
@@ -849,6 +856,7 @@ spk_status spk_dn_gradients(spk_denoiser *dn, const float *d_features, const flo
 
 spk_status spk_dn_train_step(spk_denoiser *dn, const float *d_features, const float *d_target, uint32_t n, uint32_t h,
                              uint32_t w, float lr, float *loss) {
+    const DnRange range("spk_dn_train_step");
     if (!dn) return SPK_ERR_INVALID_ARGUMENT;
     if (!(lr > 0.f)) return dn_fail(dn, SPK_ERR_INVALID_ARGUMENT, "learning rate must be positive");
     cudaSetDevice(dn->device);
@@ -867,6 +875,7 @@ spk_status spk_dn_train_step(spk_denoiser *dn, const float *d_features, const fl
 }
 
 spk_status spk_dn_infer(spk_denoiser *dn, const float *d_features, uint32_t n, uint32_t h, uint32_t w, float *d_out) {
+    const DnRange range("spk_dn_infer");
     if (!dn || !d_features || !d_out || n == 0 || h == 0 || w == 0) return SPK_ERR_INVALID_ARGUMENT;
     cudaSetDevice(dn->device);
     const uint32_t hp = (h + SPK_DN_ALIGN - 1) / SPK_DN_ALIGN * SPK_DN_ALIGN;
