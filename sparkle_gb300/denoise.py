@@ -95,15 +95,36 @@ def generate(ctx: native.Context, dn: native.Denoiser, num_scenes: int, size: in
                    dict(scenes=num_scenes, size=size, spp_in=spp_in, spp_target=spp_target, seed=seed))
 
 
+def save_checkpoint(path: str, dn: native.Denoiser, generator, step: int, losses):
+    """Training checkpoint: the denoiser state (parameters, Adam moments, step), the crop generator's state,
+    the step reached and the losses so far; written to a temporary file, then renamed."""
+    tmp = path + ".tmp"
+    with open(tmp, "wb") as f:
+        np.savez(f, dn_state=np.frombuffer(dn.save_state(), np.uint8), generator=generator.get_state().numpy(),
+                 step=np.int64(step), losses=np.asarray(losses, np.float64))
+    os.replace(tmp, path)
+
+
 def train(dn: native.Denoiser, data: DataSet, steps: int, batch: int = 16, crop: int = 128, lr: float = 1e-3,
-          seed: int = 0, log_every: int = 0):
-    """Adam on random crops; returns (losses, seconds, device ms per step)."""
+          seed: int = 0, log_every: int = 0, checkpoint: str = None, checkpoint_every: int = 0, resume: bool = False,
+          stop_at: int = None):
+    """Adam on random crops; returns (losses, seconds, device ms per step). With `checkpoint`, the state is
+    saved every `checkpoint_every` steps and at the end (or at `stop_at`); `resume` continues from it, so an
+    interrupted run ends where the uninterrupted one would (to the rounding of the atomic gradient sums)."""
     torch = _torch()
     g = torch.Generator(device="cpu").manual_seed(seed)
     n, h, w, _ = data.features.shape
     losses, dev_ms = [], []
+    first = 0
+    if resume and checkpoint and os.path.exists(checkpoint):
+        z = np.load(checkpoint)
+        dn.load_state(z["dn_state"].tobytes())
+        g.set_state(torch.from_numpy(z["generator"]))
+        first = int(z["step"])
+        losses = [float(x) for x in z["losses"]]
     t0 = time.perf_counter()
-    for step in range(steps):
+    last = steps if stop_at is None else min(steps, stop_at)
+    for step in range(first, last):
         idx = torch.randint(0, n, (batch,), generator=g)
         ys = torch.randint(0, h - crop + 1, (batch,), generator=g)
         xs = torch.randint(0, w - crop + 1, (batch,), generator=g)
@@ -114,7 +135,11 @@ def train(dn: native.Denoiser, data: DataSet, steps: int, batch: int = 16, crop:
         dev_ms.append(dn.last_ms())
         if log_every and (step + 1) % log_every == 0:
             print(f"step {step + 1}: loss {np.mean(losses[-log_every:]):.5f}", flush=True)
-    return losses, time.perf_counter() - t0, float(np.median(dev_ms))
+        if checkpoint and checkpoint_every and (step + 1) % checkpoint_every == 0:
+            save_checkpoint(checkpoint, dn, g, step + 1, losses)
+    if checkpoint and last > first:
+        save_checkpoint(checkpoint, dn, g, last, losses)
+    return losses, time.perf_counter() - t0, float(np.median(dev_ms)) if dev_ms else 0.0
 
 
 def save_weights(dn: native.Denoiser, path: str = WEIGHTS, **meta):

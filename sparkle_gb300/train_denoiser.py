@@ -46,6 +46,9 @@ def main(argv=None):
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=denoise.WEIGHTS)
+    ap.add_argument("--checkpoint", default=None, help="training checkpoint file (written every --checkpoint-every)")
+    ap.add_argument("--checkpoint-every", type=int, default=500)
+    ap.add_argument("--resume", action="store_true", help="continue from --checkpoint")
     args = ap.parse_args(argv)
 
     ctx = native.Context(0)
@@ -56,7 +59,9 @@ def main(argv=None):
     train_data = denoise.DataSet(data.features[:args.scenes], data.targets[:args.scenes])
     untrained = holdout_scores(dn, data, args.scenes)
     losses, train_s, step_ms = denoise.train(dn, train_data, args.steps, batch=args.batch, crop=args.crop,
-                                             lr=args.lr, seed=args.seed, log_every=max(1, args.steps // 10))
+                                             lr=args.lr, seed=args.seed, log_every=max(1, args.steps // 10),
+                                             checkpoint=args.checkpoint, checkpoint_every=args.checkpoint_every,
+                                             resume=args.resume)
     trained = holdout_scores(dn, data, args.scenes)
     meta = dict(scenes=args.scenes, holdout=args.holdout, size=args.size, spp_in=args.spp_in,
                 spp_target=args.spp_target, steps=args.steps, batch=args.batch, crop=args.crop, lr=args.lr,

@@ -161,3 +161,24 @@ def test_bounded_wait_times_out_and_the_denoiser_recovers():
     dn.infer(g2)
     assert np.array_equal(dn.infer(f).cpu().numpy(), ref)
     dn.close()
+
+
+def test_training_run_resumes_from_its_checkpoint(tmp_path):
+    import torch
+    from sparkle_gb300 import denoise
+    f, t = batch(4, n=4, h=64, w=64)
+    data = denoise.DataSet(f, t)
+    kw = dict(batch=2, crop=32, lr=1e-3, seed=3)
+    a = native.Denoiser(0, seed=5)
+    la, _, _ = denoise.train(a, data, 6, **kw)
+    ck = str(tmp_path / "train.ckpt")
+    b = native.Denoiser(0, seed=5)
+    lb, _, _ = denoise.train(b, data, 6, checkpoint=ck, checkpoint_every=2, stop_at=3, **kw)
+    assert len(lb) == 3
+    c = native.Denoiser(0, seed=11)  # other initial weights: the checkpoint replaces them
+    lc, _, _ = denoise.train(c, data, 6, checkpoint=ck, resume=True, **kw)
+    assert len(lc) == 6
+    np.testing.assert_allclose(lc, la, rtol=1e-4)
+    np.testing.assert_allclose(c.get_params(), a.get_params(), rtol=1e-3, atol=1e-6)
+    for d in (a, b, c):
+        d.close()
