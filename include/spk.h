@@ -209,8 +209,9 @@ typedef struct spk_tuning {
     uint32_t batch_slots;          /* path slots (queue capacity) of spk_render_batch, 0 = min(items, 2^21) */
     uint32_t ray_sort;             /* 1: order each extend queue by ray (direction octant, origin cell) (default 0) */
     uint32_t bvh_collapse;         /* 8-wide collapse: 0 greedy largest-area (default), 1 SAH-optimal; next spk_set_scene */
-    uint32_t bvh_builder;          /* BLAS builder: 0 host binned SAH (default), 1 device LBVH (Morton order, greedy
-                                      collapse; bvh_collapse ignored), milliseconds instead of seconds for large meshes */
+    uint32_t bvh_builder;          /* BLAS builder: 0 host binned SAH (default), 1 device LBVH (Karras radix tree over
+                                      Morton order), 2 device PLOC clustering over Morton order; 1 and 2 use the greedy
+                                      collapse (bvh_collapse ignored) and take milliseconds where the host takes seconds */
 } spk_tuning;
 
 /* ------------------------------------------------------------------------------------------------ */

@@ -23,7 +23,7 @@ SPACE = {
     "bvh_width": [8, 4],
     "bvh_leaf_size": [3, 2],
     "bvh_collapse": [0, 1],
-    "bvh_builder": [0, 1],
+    "bvh_builder": [0, 1, 2],
 }
 SCENE_KNOBS = ("bvh_width", "bvh_leaf_size", "bvh_collapse", "bvh_builder")
 

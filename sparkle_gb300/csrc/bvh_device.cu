@@ -406,14 +406,34 @@ __global__ void k_karras(const uint64_t *keys, uint32_t n, uint32_t *left, uint3
     count[i] = static_cast<uint32_t>(hi - lo + 1);
 }
 
+// Bottom-up SAH cost of a binary node (traversal cost 1 : triangle cost 1, as the host build): a subtree of
+// at most max_leaf triangles may stay one leaf when that is not dearer than keeping it split. The cost goes
+// to the low corner's w, the "one leaf" decision (1 / 0) to the high corner's w; the collapse reads it.
+__device__ __forceinline__ void node_cost(float4 &lo, float4 &hi, float cost_a, float cost_b, uint32_t count,
+                                          uint32_t max_leaf) {
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    const float area = dx * dy + dy * dz + dz * dx;
+    const float inner = area + cost_a + cost_b;
+    const float leaf = count <= max_leaf ? area * static_cast<float>(count) : FLT_MAX;
+    lo.w = fminf(inner, leaf);
+    hi.w = leaf <= inner ? 1.f : 0.f;
+}
+
+__device__ __forceinline__ void leaf_cost(float4 &lo, float4 &hi) {
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    lo.w = dx * dy + dy * dz + dz * dx;
+    hi.w = 1.f;
+}
+
 // Leaf boxes, then up the tree: the second child to arrive at a node writes its box and goes on.
 __global__ void k_bottom_up(const uint32_t *sorted_faces, const float4 *flo, const float4 *fhi, uint32_t n,
-                            const uint32_t *left, const uint32_t *right, const uint32_t *parent, uint32_t *arrivals,
-                            float4 *nlo, float4 *nhi) {
+                            const uint32_t *left, const uint32_t *right, const uint32_t *parent, const uint32_t *count,
+                            uint32_t max_leaf, uint32_t *arrivals, float4 *nlo, float4 *nhi) {
     const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= n) return;
     uint32_t node = n - 1 + m;
     float4 lo = flo[sorted_faces[m]], hi = fhi[sorted_faces[m]];
+    leaf_cost(lo, hi);
     nlo[node] = lo;
     nhi[node] = hi;
     for (uint32_t steps = 0; steps < n; ++steps) {
@@ -423,12 +443,110 @@ __global__ void k_bottom_up(const uint32_t *sorted_faces, const float4 *flo, con
         if (atomicAdd(&arrivals[p], 1u) == 0) break;
         const uint32_t other = left[p] == node ? right[p] : left[p];
         const float4 ol = __ldcg(nlo + other), oh = __ldcg(nhi + other);
+        const float ca = lo.w, cb = ol.w;
         lo = make_float4(fminf(lo.x, ol.x), fminf(lo.y, ol.y), fminf(lo.z, ol.z), 0.f);
         hi = make_float4(fmaxf(hi.x, oh.x), fmaxf(hi.y, oh.y), fmaxf(hi.z, oh.z), 0.f);
+        node_cost(lo, hi, ca, cb, count[p], max_leaf);
         nlo[p] = lo;
         nhi[p] = hi;
         node = p;
     }
+}
+
+// PLOC (Meister and Bittner, "Parallel Locally-Ordered Clustering for Bounding Volume Hierarchy
+// Construction", 2018): starting from the leaves in Morton order, every cluster finds the neighbour within
+// kPlocRadius positions whose merged box has the smallest area; mutual nearest neighbours merge into a new
+// node (ids handed out downwards from n - 2, so the last merge is the root, node 0), and the survivors are
+// compacted in order. Ties go to the lower position, merge ids come from a scan: deterministic.
+constexpr int kPlocRadius = 16;
+constexpr int kPlocThreads = 256;
+
+__global__ void k_leaf_init(const uint32_t *sorted_faces, const float4 *flo, const float4 *fhi, uint32_t n,
+                            float4 *nlo, float4 *nhi, uint32_t *clusters) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t node = n - 1 + i;
+    float4 lo = flo[sorted_faces[i]], hi = fhi[sorted_faces[i]];
+    leaf_cost(lo, hi);
+    nlo[node] = lo;
+    nhi[node] = hi;
+    clusters[i] = node;
+}
+
+__device__ __forceinline__ float merged_half_area(float4 al, float4 ah, float4 bl, float4 bh) {
+    const float dx = fmaxf(ah.x, bh.x) - fminf(al.x, bl.x);
+    const float dy = fmaxf(ah.y, bh.y) - fminf(al.y, bl.y);
+    const float dz = fmaxf(ah.z, bh.z) - fminf(al.z, bl.z);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__global__ void k_ploc_nn(const uint32_t *clusters, uint32_t m, const float4 *nlo, const float4 *nhi, uint32_t *nn) {
+    __shared__ float4 slo[kPlocThreads + 2 * kPlocRadius], shi[kPlocThreads + 2 * kPlocRadius];
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * kPlocThreads - kPlocRadius;
+    for (int k = threadIdx.x; k < kPlocThreads + 2 * kPlocRadius; k += blockDim.x) {
+        const int64_t i = base + k;
+        if (i >= 0 && i < m) {
+            const uint32_t c = clusters[i];
+            slo[k] = nlo[c];
+            shi[k] = nhi[c];
+        }
+    }
+    __syncthreads();
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * kPlocThreads + threadIdx.x;
+    if (i >= m) return;
+    const int li = static_cast<int>(threadIdx.x) + kPlocRadius;
+    float best = FLT_MAX;
+    int64_t bj = i;
+    for (int d = -kPlocRadius; d <= kPlocRadius; ++d) {
+        const int64_t j = i + d;
+        if (d == 0 || j < 0 || j >= m) continue;
+        const float a = merged_half_area(slo[li], shi[li], slo[li + d], shi[li + d]);
+        if (a < best) {  // ascending j: the first of equal areas is kept
+            best = a;
+            bj = j;
+        }
+    }
+    nn[i] = static_cast<uint32_t>(bj);
+}
+
+// keep[i]: cluster i survives this round (merged into a new node or unchanged); merge[i]: it is the lower
+// position of a mutual pair and makes the new node.
+__global__ void k_ploc_flags(const uint32_t *nn, uint32_t m, uint32_t *keep, uint32_t *merge) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const uint32_t j = nn[i];
+    const bool mutual = j != i && j < m && nn[j] == i;
+    merge[i] = mutual && i < j ? 1u : 0u;
+    keep[i] = mutual && i > j ? 0u : 1u;
+}
+
+__global__ void k_ploc_write(const uint32_t *clusters, uint32_t m, const uint32_t *nn, const uint32_t *merge_off,
+                             const uint32_t *pos, uint32_t id_base, uint32_t n, uint32_t max_leaf, float4 *nlo, float4 *nhi,
+                             uint32_t *left, uint32_t *right, uint32_t *count, uint32_t *out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    const uint32_t j = nn[i];
+    const bool mutual = j != i && j < m && nn[j] == i;
+    if (mutual && i > j) return;  // merged into the node made at position j
+    uint32_t c = clusters[i];
+    if (mutual) {
+        const uint32_t id = id_base - merge_off[i];
+        const uint32_t a = c, b = clusters[j];
+        if (id < n - 1) {
+            left[id] = a;
+            right[id] = b;
+            const uint32_t cnt = (a >= n - 1 ? 1u : count[a]) + (b >= n - 1 ? 1u : count[b]);
+            count[id] = cnt;
+            const float4 al = nlo[a], ah = nhi[a], bl = nlo[b], bh = nhi[b];
+            float4 lo = make_float4(fminf(al.x, bl.x), fminf(al.y, bl.y), fminf(al.z, bl.z), 0.f);
+            float4 hi = make_float4(fmaxf(ah.x, bh.x), fmaxf(ah.y, bh.y), fmaxf(ah.z, bh.z), 0.f);
+            node_cost(lo, hi, al.w, bl.w, cnt, max_leaf);
+            nlo[id] = lo;
+            nhi[id] = hi;
+        }
+        c = id;
+    }
+    out[pos[i]] = c;
 }
 
 struct BinaryTree {
@@ -436,7 +554,8 @@ struct BinaryTree {
     const float4 *nlo, *nhi;
     uint32_t n;  // leaves
     __device__ uint32_t leaves(uint32_t x) const { return x >= n - 1 ? 1u : count[x]; }
-    __device__ uint32_t first_leaf(uint32_t x) const { return x >= n - 1 ? x - (n - 1) : first[x]; }
+    // One wide-BVH leaf: a triangle, or a subtree the bottom-up SAH costs chose to keep whole.
+    __device__ bool is_leaf(uint32_t x) const { return x >= n - 1 || nhi[x].w != 0.f; }
     __device__ float half_area(uint32_t x) const {
         const float4 a = nlo[x], b = nhi[x];
         const float dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
@@ -460,7 +579,7 @@ __global__ void k_collapse_open(BinaryTree t, const uint32_t *jobs, uint32_t num
         inner_count[j] = item_count[j] = 0;
         return;
     }
-    if (t.leaves(b) <= ml) {
+    if (t.is_leaf(b)) {
         k[nk++] = b;
     } else {
         k[nk++] = t.left[b];
@@ -469,7 +588,7 @@ __global__ void k_collapse_open(BinaryTree t, const uint32_t *jobs, uint32_t num
             int best = -1;
             float best_area = -1.f;
             for (int q = 0; q < nk; ++q) {
-                if (t.leaves(k[q]) > ml) {
+                if (!t.is_leaf(k[q])) {
                     const float a = t.half_area(k[q]);
                     if (a > best_area) {
                         best_area = a;
@@ -487,7 +606,7 @@ __global__ void k_collapse_open(BinaryTree t, const uint32_t *jobs, uint32_t num
     for (int q = 0; q < 8; ++q) {
         kids[8ull * j + q] = q < nk ? k[q] : kNone;
         if (q < nk) {
-            if (t.leaves(k[q]) > ml && k[q] != b) {
+            if (!t.is_leaf(k[q]) && k[q] != b) {
                 ++inner;
             } else {
                 items += t.leaves(k[q]);
@@ -570,16 +689,28 @@ __global__ void k_collapse_emit(BinaryTree t, uint32_t num_jobs, int max_leaf, c
         }
         const uint32_t kid = k[q];
         const uint32_t cnt = t.leaves(kid);
-        if (cnt > ml && kid != b) {
+        if (!t.is_leaf(kid) && kid != b) {
             imask |= 1u << s;
             n.b[24 + s] = static_cast<uint8_t>(0x20u | (24u + s));
             if (inner_off[j] + inner < t.n) next_jobs[inner_off[j] + inner] = kid;
             ++inner;
         } else {
             n.b[24 + s] = static_cast<uint8_t>((((1u << cnt) - 1u) << 5) | offset);
-            const uint32_t f0 = t.first_leaf(kid);
-            for (uint32_t i = 0; i < cnt; ++i)
-                if (ibase + offset + i < t.n && f0 + i < t.n) items[ibase + offset + i] = sorted_faces[f0 + i];
+            // The leaves of the kid's subtree (<= 3), left first: a Morton-ordered range for the radix tree,
+            // any leaves for the clustered one.
+            uint32_t st[4], sp = 0, o = 0;
+            st[sp++] = kid;
+            while (sp > 0 && o < cnt) {
+                const uint32_t x = st[--sp];
+                if (x >= t.n - 1) {
+                    const uint32_t m = x - (t.n - 1);
+                    if (ibase + offset + o < t.n && m < t.n) items[ibase + offset + o] = sorted_faces[m];
+                    ++o;
+                } else if (sp + 2 <= 4) {
+                    st[sp++] = t.right[x];
+                    st[sp++] = t.left[x];
+                }
+            }
             offset += cnt;
         }
     }
@@ -658,8 +789,8 @@ void scan(uint32_t *data, uint32_t n, uint32_t *total, uint32_t *scratch, cudaSt
 }  // namespace
 
 cudaError_t build_wide_device(const float *positions, uint32_t num_vertices, const uint32_t *indices,
-                              uint32_t num_faces, int max_children, int max_leaf, cudaStream_t stream, WideBvh &out,
-                              std::vector<uint32_t> &levels) {
+                              uint32_t num_faces, int max_children, int max_leaf, bool clustered, cudaStream_t stream,
+                              WideBvh &out, std::vector<uint32_t> &levels) {
     out = WideBvh{};
     levels.clear();
     if (num_faces == 0) return cudaSuccess;
@@ -720,10 +851,37 @@ cudaError_t build_wide_device(const float *positions, uint32_t num_vertices, con
     SPK_TRY(cudaGetLastError());
     const uint64_t *skeys = keys[cur];
     const uint32_t *sfaces = vals[cur];
-    SPK_TRY(cudaMemsetAsync(parent, 0xFF, 2ull * n * sizeof(uint32_t), stream));
-    SPK_TRY(cudaMemsetAsync(arrivals, 0, n * sizeof(uint32_t), stream));
-    if (n > 1) k_karras<<<blocks(n - 1, 256), 256, 0, stream>>>(skeys, n, left, right, parent, first, count);
-    k_bottom_up<<<blocks(n, 256), 256, 0, stream>>>(sfaces, flo, fhi, n, left, right, parent, arrivals, nlo, nhi);
+    if (clustered) {
+        // PLOC rounds until one cluster is left; clusters ping-pong between jobs[0] and jobs[1], the nearest
+        // neighbours live in kids, the keep / merge flags (scanned in place) in item_cnt / inner_cnt.
+        k_leaf_init<<<blocks(n, 256), 256, 0, stream>>>(sfaces, flo, fhi, n, nlo, nhi, jobs[0]);
+        uint32_t m = n, merged = 0;
+        int cc = 0;
+        for (uint32_t round = 0; m > 1; ++round) {
+            if (round > n) return cudaErrorUnknown;  // cannot happen: every round merges at least one pair
+            k_ploc_nn<<<blocks(m, kPlocThreads), kPlocThreads, 0, stream>>>(jobs[cc], m, nlo, nhi, kids);
+            k_ploc_flags<<<blocks(m, 256), 256, 0, stream>>>(kids, m, item_cnt, inner_cnt);
+            scan(inner_cnt, m, totals, scan_tmp, stream);
+            scan(item_cnt, m, totals + 1, scan_tmp, stream);
+            k_ploc_write<<<blocks(m, 256), 256, 0, stream>>>(jobs[cc], m, kids, inner_cnt, item_cnt, n - 2 - merged, n,
+                                                             static_cast<uint32_t>(max_leaf), nlo, nhi, left, right,
+                                                             count, jobs[cc ^ 1]);
+            SPK_TRY(cudaGetLastError());
+            uint32_t tot[2];
+            SPK_TRY(cudaMemcpyAsync(tot, totals, sizeof(tot), cudaMemcpyDeviceToHost, stream));
+            SPK_TRY(cudaStreamSynchronize(stream));
+            if (tot[0] == 0 || tot[1] != m - tot[0]) return cudaErrorUnknown;
+            merged += tot[0];
+            m = tot[1];
+            cc ^= 1;
+        }
+    } else {
+        SPK_TRY(cudaMemsetAsync(parent, 0xFF, 2ull * n * sizeof(uint32_t), stream));
+        SPK_TRY(cudaMemsetAsync(arrivals, 0, n * sizeof(uint32_t), stream));
+        if (n > 1) k_karras<<<blocks(n - 1, 256), 256, 0, stream>>>(skeys, n, left, right, parent, first, count);
+        k_bottom_up<<<blocks(n, 256), 256, 0, stream>>>(sfaces, flo, fhi, n, left, right, parent, count,
+                                                        static_cast<uint32_t>(max_leaf), arrivals, nlo, nhi);
+    }
     SPK_TRY(cudaGetLastError());
 
     BinaryTree t{left, right, first, count, nlo, nhi, n};

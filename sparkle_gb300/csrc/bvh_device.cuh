@@ -13,7 +13,8 @@
 // breaks ties), boxes propagated bottom-up with one atomic counter per node, then collapsed into 8-wide nodes
 // breadth first, one launch per level, with the host collapse's rules (open the largest-area inner child
 // until 8, subtrees of <= leaf-size triangles become leaves, octant slot order, the same quantisation).
-// Every step is deterministic: the same mesh gives the same nodes.
+// Every step is deterministic: the same mesh gives the same nodes. spk_tuning.bvh_builder = 2 replaces the
+// radix tree by PLOC clustering (Meister and Bittner 2018) over the same Morton order.
 #pragma once
 
 #include <cstdint>
@@ -50,13 +51,14 @@ cudaError_t launch_refit_nodes(const BlasRefit &r, uint32_t first, uint32_t last
 cudaError_t launch_update_vertices(float4 *verts, uint32_t vert_base, uint32_t num_vertices, const float *normals,
                                    const float *tangents, cudaStream_t stream);
 
-// Builds the 8-wide BLAS of one mesh on the device. positions [num_vertices][3] and indices [num_faces][3]
+// Builds the 8-wide BLAS of one mesh on the device, from the Karras radix tree of the Morton-sorted faces
+// or, with `clustered`, from a PLOC agglomerative clustering of them (tighter trees, a few more rounds). positions [num_vertices][3] and indices [num_faces][3]
 // are host arrays (indices already checked against num_vertices). `out` receives the nodes (node 0 the
 // root, children after their parent depth by depth) and the leaf items (face indices) as the host builder
 // returns them; `levels` the first node of each depth, then the node count. `max_children` 2..8,
 // `max_leaf` 1..3.
 cudaError_t build_wide_device(const float *positions, uint32_t num_vertices, const uint32_t *indices,
-                              uint32_t num_faces, int max_children, int max_leaf, cudaStream_t stream, WideBvh &out,
-                              std::vector<uint32_t> &levels);
+                              uint32_t num_faces, int max_children, int max_leaf, bool clustered, cudaStream_t stream,
+                              WideBvh &out, std::vector<uint32_t> &levels);
 
 }  // namespace spk

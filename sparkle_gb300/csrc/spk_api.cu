@@ -529,7 +529,7 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
             mb[3 + a] = -std::numeric_limits<double>::max();
         }
         if (m.num_faces == 0) continue;
-        const bool device_build = ctx->tuning.bvh_builder == 1;
+        const bool device_build = ctx->tuning.bvh_builder != 0;
         std::vector<BuildBox> boxes(device_build ? 0 : m.num_faces);
         for (uint32_t f = 0; f < m.num_faces; ++f) {
             BuildBox b;
@@ -553,7 +553,8 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
             std::vector<uint32_t> lv;
             const cudaError_t e = build_wide_device(m.positions, m.num_vertices, m.indices, m.num_faces,
                                                     static_cast<int>(ctx->tuning.bvh_width),
-                                                    static_cast<int>(ctx->tuning.bvh_leaf_size), ctx->stream, wide, lv);
+                                                    static_cast<int>(ctx->tuning.bvh_leaf_size),
+                                                    ctx->tuning.bvh_builder == 2, ctx->stream, wide, lv);
             if (e != cudaSuccess) return cuda_fail(ctx, e, "device BVH build");
         } else {
             wide = build_wide(boxes, ctx->tuning, threads);
@@ -1754,8 +1755,9 @@ spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "bvh_leaf_size must be 1..3");
     if (t->extend_blocks_per_sm > 32 || t->shade_blocks_per_sm < 1 || t->shade_blocks_per_sm > 32)
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "blocks per SM out of range");
-    if (t->ray_sort > 1 || t->bvh_collapse > 1 || t->bvh_builder > 1)
-        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "ray_sort, bvh_collapse and bvh_builder take 0 or 1");
+    if (t->ray_sort > 1 || t->bvh_collapse > 1)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "ray_sort and bvh_collapse take 0 or 1");
+    if (t->bvh_builder > 2) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "bvh_builder takes 0, 1 or 2");
     ctx->tuning = *t;
     return SPK_OK;
 }

@@ -1,5 +1,5 @@
-"""Device BLAS builder (spk_tuning.bvh_builder = 1): Karras LBVH over Morton codes, collapsed to the same
-8-wide node format as the host builder. Results never depend on the tree, so hits and images must equal
+"""Device BLAS builders (spk_tuning.bvh_builder = 1: Karras LBVH over Morton codes; 2: PLOC clustering over
+the same order), collapsed to the same 8-wide node format as the host builder. Results never depend on the tree, so hits and images must equal
 the host-built scene's bit for bit; the build is deterministic, and a refit of a device-built tree with
 unchanged positions reproduces it."""
 import time
@@ -24,14 +24,15 @@ def hits_equal(a, b):
         assert np.array_equal(a[f].view(np.uint32), b[f].view(np.uint32)), f
 
 
+@pytest.mark.parametrize("builder", [1, 2])
 @pytest.mark.parametrize("width,leaf", [(8, 3), (4, 2), (2, 1), (8, 1)])
-def test_device_build_hits_equal_host_build(ctx, small_terrain, width, leaf):
+def test_device_build_hits_equal_host_build(ctx, small_terrain, width, leaf, builder):
     scene, _ = small_terrain
     rays = scenes.random_rays(*scene.world_bounds(), 50_000, seed=12)
     ctx.set_tuning(bvh_builder=0, bvh_width=8, bvh_leaf_size=3, bvh_collapse=0)
     ctx.set_scene(scene)
     ref = ctx.trace(rays)
-    ctx.set_tuning(bvh_builder=1, bvh_width=width, bvh_leaf_size=leaf)
+    ctx.set_tuning(bvh_builder=builder, bvh_width=width, bvh_leaf_size=leaf)
     ctx.set_scene(scene)
     got = ctx.trace(rays)
     assert ctx.stats()["error_flags"] == 0
@@ -39,9 +40,10 @@ def test_device_build_hits_equal_host_build(ctx, small_terrain, width, leaf):
     ctx.set_tuning(bvh_builder=0, bvh_width=8, bvh_leaf_size=3)
 
 
-def test_device_build_is_deterministic_and_refits(ctx, small_terrain):
+@pytest.mark.parametrize("builder", [1, 2])
+def test_device_build_is_deterministic_and_refits(ctx, small_terrain, builder):
     scene, _ = small_terrain
-    ctx.set_tuning(bvh_builder=1)
+    ctx.set_tuning(bvh_builder=builder)
     ctx.set_scene(scene)
     a = ctx.bvh_nodes()
     ctx.set_scene(scene)
@@ -53,8 +55,9 @@ def test_device_build_is_deterministic_and_refits(ctx, small_terrain):
     ctx.set_tuning(bvh_builder=0)
 
 
+@pytest.mark.parametrize("builder", [1, 2])
 @pytest.mark.parametrize("n", [1, 2, 3, 4, 9, 25])
-def test_tiny_meshes(ctx, n):
+def test_tiny_meshes(ctx, n, builder):
     """Meshes of a few triangles: a single leaf root, a root with only leaf children, one level below."""
     rng = np.random.default_rng(n)
     pos = rng.uniform(-1, 1, (3 * n, 3)).astype(np.float32)
@@ -66,14 +69,15 @@ def test_tiny_meshes(ctx, n):
     ctx.set_tuning(bvh_builder=0)
     ctx.set_scene(scene)
     ref = ctx.trace(rays)
-    ctx.set_tuning(bvh_builder=1)
+    ctx.set_tuning(bvh_builder=builder)
     ctx.set_scene(scene)
     hits_equal(ctx.trace(rays), ref)
     assert (ref["prim"] != 0xFFFFFFFF).any()
     ctx.set_tuning(bvh_builder=0)
 
 
-def test_large_mesh_builds_fast_and_equal(ctx):
+@pytest.mark.parametrize("builder", [1, 2])
+def test_large_mesh_builds_fast_and_equal(ctx, builder):
     """A 512x512 heightfield (524,288 triangles): same hits as the host build, built in far less time."""
     mesh = scenes.heightfield(512, 100.0, 6.0, seed=2)
     scene = abi.Scene([mesh], [abi.Instance(0, 0, np.eye(3, 4))], [abi.Material.lambertian((0.5, 0.5, 0.5))],
@@ -84,14 +88,14 @@ def test_large_mesh_builds_fast_and_equal(ctx):
     ctx.set_scene(scene)
     host_s = time.perf_counter() - t0
     ref = ctx.trace(rays)
-    ctx.set_tuning(bvh_builder=1)
+    ctx.set_tuning(bvh_builder=builder)
     ctx.set_scene(scene)  # warm
     t0 = time.perf_counter()
     ctx.set_scene(scene)
     dev_s = time.perf_counter() - t0
     got = ctx.trace(rays)
     hits_equal(got, ref)
-    print(f"set_scene 524k triangles: host SAH {host_s * 1e3:.0f} ms, device LBVH {dev_s * 1e3:.0f} ms")
+    print(f"set_scene 524k triangles: host SAH {host_s * 1e3:.0f} ms, device builder {builder}: {dev_s * 1e3:.0f} ms")
     assert dev_s < host_s
     ctx.set_tuning(bvh_builder=0)
 
@@ -101,7 +105,7 @@ def test_device_built_render_equals_host_built(ctx, small_terrain):
     camera = scenes.make_camera(cam_args, 64, 48)
     cfg = abi.make_config(64, 48, spp=2, bounce=4, seed=1)
     out = []
-    for builder in (0, 1):
+    for builder in (0, 1, 2):
         ctx.set_tuning(bvh_builder=builder)
         ctx.set_scene(scene)
         ctx.set_config(cfg)
@@ -109,4 +113,5 @@ def test_device_built_render_equals_host_built(ctx, small_terrain):
         ctx.render(3)
         out.append(ctx.framebuffer()[0])
     assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
+    assert np.array_equal(out[0].view(np.uint32), out[2].view(np.uint32))
     ctx.set_tuning(bvh_builder=0)

@@ -27,6 +27,7 @@ VARIANTS = [
     dict(ray_sort=1, material_sort=1),
     dict(bvh_builder=1),
     dict(bvh_builder=1, bvh_width=4, bvh_leaf_size=1),
+    dict(bvh_builder=2),
 ]
 
 
