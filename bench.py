@@ -142,6 +142,23 @@ def ncu_traffic_per_ray():
     return float(m.group(1)) if m else None
 
 
+def ncu_issue_profile():
+    """The extend kernel's issue-slot use and lanes per instruction from the committed ncu summary (its
+    bulk-iteration table), which say what bounds the walk: it is issue-bound, not HBM-bound."""
+    path = os.path.join(ROOT, "profiles", "k_wf_extend_stress.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        text = f.read()
+    issue = re.search(r"smsp__issue_active \(% of peak\) \| ([0-9.]+) %", text)
+    lanes = re.search(r"smsp__thread_inst_executed_per_inst_executed \| ([0-9.]+)", text)
+    dram = re.search(r"gpu__dram_throughput \(% of peak\) \| ([0-9.]+) %", text)
+    if not (issue and lanes and dram):
+        return None
+    return {"issue_active": round(float(issue.group(1)) / 100.0, 3), "lanes_per_instruction": float(lanes.group(1)),
+            "dram_throughput": round(float(dram.group(1)) / 100.0, 3), "source": "profiles/k_wf_extend_stress.md"}
+
+
 def cpu_sample(osc, camera, frames: int, rows: int, threads: int, traversal: int):
     """Times the oracle (reference cpu pipeline restated, scene `osc` already built) on `rows` central rows
     for `frames` frames; returns (Mrays/s, rays, seconds)."""
@@ -310,7 +327,8 @@ def run_ours(args):
                      "algorithmic_bytes_per_ray": round(bytes_per_ray, 1),
                      "rays_per_launch": round(rays_per_launch, 1),
                      "traffic": (round(traffic_per_ray * rays_per_launch) if traffic_per_ray else None),
-                     "traffic_unit": "DRAM bytes per launch (ncu per-ray figure x rays per launch)"},
+                     "traffic_unit": "DRAM bytes per launch (ncu per-ray figure x rays per launch)",
+                     "ncu_issue": ncu_issue_profile()},
         "trace_kernel_ms_per_step": round(trace_ms / args.steps, 3),
         "device_error_flags": errors,
         "clocks": clocks.summary(),
