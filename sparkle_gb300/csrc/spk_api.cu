@@ -14,6 +14,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <limits>
 #include <mutex>
 #include <new>
@@ -896,14 +897,18 @@ const char *spk_last_error(const spk_ctx *ctx) { return ctx ? ctx->error.c_str()
 
 spk_status spk_set_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_meshes, const spk_instance *instances,
                          uint32_t num_instances, const spk_material *materials, uint32_t num_materials,
-                         const spk_sky *sky) {
+                         const spk_sky *sky) try {
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     const spk_scene_desc d{meshes, num_meshes, instances, num_instances, materials, num_materials, sky,
                            nullptr, 0, nullptr};
     return spk_set_scenes(ctx, &d, 1);
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
-spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t num_scenes) {
+spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t num_scenes) try {
     NvtxRange range("spk_set_scenes");
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     if (!scenes || num_scenes == 0) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "no scenes");
@@ -952,9 +957,13 @@ spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t n
         append_scene(all, hs, descs[k]);
     }
     return upload_scene(ctx, all, descs);
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
-spk_status spk_set_instances(spk_ctx *ctx, const spk_instance *instances, uint32_t num_instances) {
+spk_status spk_set_instances(spk_ctx *ctx, const spk_instance *instances, uint32_t num_instances) try {
     NvtxRange range("spk_set_instances");
     spk_status st = require_dynamic(ctx);
     if (st != SPK_OK) return st;
@@ -971,10 +980,14 @@ spk_status spk_set_instances(spk_ctx *ctx, const spk_instance *instances, uint32
     }
     dy.instances.assign(instances, instances + num_instances);
     return rebuild_top(ctx);
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
 spk_status spk_set_instance_transforms(spk_ctx *ctx, uint32_t first, uint32_t count, const float *transforms,
-                                       const float *inv_transforms) {
+                                       const float *inv_transforms) try {
     NvtxRange range("spk_set_instance_transforms");
     spk_status st = require_dynamic(ctx);
     if (st != SPK_OK) return st;
@@ -988,10 +1001,14 @@ spk_status spk_set_instance_transforms(spk_ctx *ctx, uint32_t first, uint32_t co
         std::memcpy(dy.instances[first + k].inv_transform, inv_transforms + 12ull * k, 12 * sizeof(float));
     }
     return rebuild_top(ctx);
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
 spk_status spk_update_mesh(spk_ctx *ctx, uint32_t mesh_id, uint32_t num_vertices, const float *positions,
-                           const float *normals, const float *tangents) {
+                           const float *normals, const float *tangents) try {
     NvtxRange range("spk_update_mesh");
     spk_status st = require_dynamic(ctx);
     if (st != SPK_OK) return st;
@@ -1061,9 +1078,13 @@ spk_status spk_update_mesh(spk_ctx *ctx, uint32_t mesh_id, uint32_t num_vertices
     if (st != SPK_OK) return st;
     if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "refit");
     return SPK_OK;
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
-spk_status spk_read_bvh_nodes(spk_ctx *ctx, void *nodes, uint64_t capacity, uint64_t *count) {
+spk_status spk_read_bvh_nodes(spk_ctx *ctx, void *nodes, uint64_t capacity, uint64_t *count) try {
     if (!ctx || !count) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_scene) return fail(ctx, SPK_ERR_NOT_READY, "no scene");
     *count = ctx->bvh_nodes;
@@ -1073,6 +1094,10 @@ spk_status spk_read_bvh_nodes(spk_ctx *ctx, void *nodes, uint64_t capacity, uint
     cudaError_t e = cudaMemcpyAsync(nodes, ctx->nodes.ptr, n * sizeof(WideNode), cudaMemcpyDefault, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     return e == cudaSuccess ? SPK_OK : cuda_fail(ctx, e, "read nodes");
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
 spk_status spk_set_camera(spk_ctx *ctx, const spk_camera *camera) {
@@ -1129,7 +1154,7 @@ spk_status spk_camera_from_look(const float position[3], const float target[3], 
     return SPK_OK;
 }
 
-spk_status spk_set_config(spk_ctx *ctx, const spk_config *config) {
+spk_status spk_set_config(spk_ctx *ctx, const spk_config *config) try {
     if (!ctx || !config) return SPK_ERR_INVALID_ARGUMENT;
     if (config->width < 2 || config->height < 2)
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "resolution must be at least 2x2");
@@ -1162,6 +1187,10 @@ spk_status spk_set_config(spk_ctx *ctx, const spk_config *config) {
     ctx->has_config = true;
     ctx->dirty = true;
     return SPK_OK;
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
 static WfTuning wf_tuning(const spk_ctx *ctx) {
@@ -1274,13 +1303,17 @@ static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
     return SPK_OK;
 }
 
-spk_status spk_render(spk_ctx *ctx, uint32_t num_frames) {
+spk_status spk_render(spk_ctx *ctx, uint32_t num_frames) try {
     NvtxRange range("spk_render");
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_scene || !ctx->has_config || !ctx->has_camera)
         return fail(ctx, SPK_ERR_NOT_READY, "render needs spk_set_scene, spk_set_config and spk_set_camera first");
     cudaSetDevice(ctx->device);
     return render_impl(ctx, num_frames);
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
 spk_status spk_read_framebuffer(spk_ctx *ctx, float *hdr_rgba, uint16_t *rgba16f) {
@@ -1387,7 +1420,7 @@ spk_status spk_debug_walk_budget(spk_ctx *ctx, uint32_t steps) {
     return SPK_OK;
 }
 
-spk_status spk_read_rgba8(spk_ctx *ctx, uint8_t *rgba8) {
+spk_status spk_read_rgba8(spk_ctx *ctx, uint8_t *rgba8) try {
     if (!ctx || !rgba8) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "no frame buffer");
     cudaSetDevice(ctx->device);
@@ -1407,9 +1440,13 @@ spk_status spk_read_rgba8(spk_ctx *ctx, uint8_t *rgba8) {
         (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "RGBA8 conversion");
     return SPK_OK;
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
-spk_status spk_save_image(spk_ctx *ctx, const char *path, uint32_t format) {
+spk_status spk_save_image(spk_ctx *ctx, const char *path, uint32_t format) try {
     NvtxRange range("spk_save_image");
     if (!ctx || !path || !*path) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "no frame buffer");
@@ -1446,30 +1483,54 @@ spk_status spk_save_image(spk_ctx *ctx, const char *path, uint32_t format) {
     std::string err;
     if (!write_file(path, bytes, err)) return fail(ctx, SPK_ERR_IO, "%s", err.c_str());
     return SPK_OK;
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
-spk_status spk_write_png(const char *path, const uint8_t *rgba8, uint32_t width, uint32_t height) {
+spk_status spk_write_png(const char *path, const uint8_t *rgba8, uint32_t width, uint32_t height) try {
     if (!path || !rgba8 || width == 0 || height == 0) return SPK_ERR_INVALID_ARGUMENT;
     std::string err;
     return write_file(path, encode_png(rgba8, width, height), err) ? SPK_OK : SPK_ERR_IO;
+} catch (const std::bad_alloc &) {
+    return SPK_ERR_OUT_OF_MEMORY;
+} catch (const std::exception &ex) {
+    (void)ex;
+    return SPK_ERR_INTERNAL;
 }
 
-spk_status spk_write_hdr(const char *path, const float *rgba, uint32_t width, uint32_t height) {
+spk_status spk_write_hdr(const char *path, const float *rgba, uint32_t width, uint32_t height) try {
     if (!path || !rgba || width == 0 || height == 0) return SPK_ERR_INVALID_ARGUMENT;
     std::string err;
     return write_file(path, encode_hdr(rgba, width, height), err) ? SPK_OK : SPK_ERR_IO;
+} catch (const std::bad_alloc &) {
+    return SPK_ERR_OUT_OF_MEMORY;
+} catch (const std::exception &ex) {
+    (void)ex;
+    return SPK_ERR_INTERNAL;
 }
 
-spk_status spk_write_exr(const char *path, const uint16_t *rgba16f, uint32_t width, uint32_t height) {
+spk_status spk_write_exr(const char *path, const uint16_t *rgba16f, uint32_t width, uint32_t height) try {
     if (!path || !rgba16f || width == 0 || height == 0) return SPK_ERR_INVALID_ARGUMENT;
     std::string err;
     return write_file(path, encode_exr(rgba16f, width, height), err) ? SPK_OK : SPK_ERR_IO;
+} catch (const std::bad_alloc &) {
+    return SPK_ERR_OUT_OF_MEMORY;
+} catch (const std::exception &ex) {
+    (void)ex;
+    return SPK_ERR_INTERNAL;
 }
 
-spk_status spk_convert_rgba8(const uint16_t *rgba16f, uint64_t pixels, uint8_t *rgba8) {
+spk_status spk_convert_rgba8(const uint16_t *rgba16f, uint64_t pixels, uint8_t *rgba8) try {
     if (pixels && (!rgba16f || !rgba8)) return SPK_ERR_INVALID_ARGUMENT;
     rgba16f_to_rgba8(rgba16f, pixels, rgba8);
     return SPK_OK;
+} catch (const std::bad_alloc &) {
+    return SPK_ERR_OUT_OF_MEMORY;
+} catch (const std::exception &ex) {
+    (void)ex;
+    return SPK_ERR_INTERNAL;
 }
 
 spk_status spk_framebuffer_device(spk_ctx *ctx, void **hdr_rgba, void **rgba16f) {
@@ -1515,7 +1576,7 @@ spk_status spk_trace_device(spk_ctx *ctx, const void *d_rays, uint64_t num_rays,
     return trace_impl(ctx, d_rays, num_rays, d_hits, any_hit);
 }
 
-spk_status spk_trace(spk_ctx *ctx, const spk_ray *rays, uint64_t num_rays, spk_hit *hits, int32_t any_hit) {
+spk_status spk_trace(spk_ctx *ctx, const spk_ray *rays, uint64_t num_rays, spk_hit *hits, int32_t any_hit) try {
     NvtxRange range("spk_trace");
     if (!ctx || (num_rays && (!rays || !hits))) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_scene) return fail(ctx, SPK_ERR_NOT_READY, "trace needs spk_set_scene first");
@@ -1543,6 +1604,10 @@ spk_status spk_trace(spk_ctx *ctx, const spk_ray *rays, uint64_t num_rays, spk_h
     cudaFree(d_rays);
     cudaFree(d_hits);
     return st;
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
 spk_status spk_synchronize(spk_ctx *ctx) {
@@ -1587,7 +1652,7 @@ spk_status spk_get_stats(spk_ctx *ctx, spk_stats *out) {
     return SPK_OK;
 }
 
-spk_status spk_render_guides(spk_ctx *ctx) {
+spk_status spk_render_guides(spk_ctx *ctx) try {
     NvtxRange range("spk_render_guides");
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_scene || !ctx->has_config || !ctx->has_camera)
@@ -1607,6 +1672,10 @@ spk_status spk_render_guides(spk_ctx *ctx) {
                            ctx->guide_albedo.ptr, ctx->counters, ctx->stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "guides launch");
     return SPK_OK;
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
 spk_status spk_guides_device(spk_ctx *ctx, void **normal_depth, void **albedo) {
@@ -1633,7 +1702,7 @@ spk_status spk_read_guides(spk_ctx *ctx, float *normal_depth, float *albedo) {
 }
 
 spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t num_requests, uint32_t rng,
-                            uint32_t enable_nee) {
+                            uint32_t enable_nee) try {
     NvtxRange range("spk_render_batch");
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_scene) return fail(ctx, SPK_ERR_NOT_READY, "batch needs spk_set_scenes first");
@@ -1715,9 +1784,13 @@ spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t 
     ctx->stats_pending = true;
     if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
     return SPK_OK;
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
-spk_status spk_read_batch(spk_ctx *ctx, uint32_t index, float *hdr_rgba, uint16_t *rgba16f) {
+spk_status spk_read_batch(spk_ctx *ctx, uint32_t index, float *hdr_rgba, uint16_t *rgba16f) try {
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     if (index >= ctx->batch_host.size()) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "no request %u in the last batch", index);
     cudaSetDevice(ctx->device);
@@ -1731,6 +1804,10 @@ spk_status spk_read_batch(spk_ctx *ctx, uint32_t index, float *hdr_rgba, uint16_
         return cuda_fail(ctx, e, "batch read");
     if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
     return SPK_OK;
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
 void spk_tuning_defaults(spk_tuning *out) {
