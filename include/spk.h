@@ -190,7 +190,7 @@ typedef struct spk_stats {
     uint64_t node_visits;    /* wide nodes visited (only with SPK_INSTR_COUNT_TRAFFIC) */
     uint64_t triangle_tests; /* ray-triangle tests run (only with SPK_INSTR_COUNT_TRAFFIC) */
     uint32_t graph_replays;  /* CUDA graph launches of the multi-frame iteration chunk (spk_tuning.cuda_graph) */
-    uint32_t reserved0;
+    uint32_t blas_reused;    /* BLASes the last spk_set_scene took from a spk_set_bvh blob instead of building */
 } spk_stats;
 
 enum { SPK_INSTR_NONE = 0, SPK_INSTR_COUNT_TRAFFIC = 1 };
@@ -446,6 +446,16 @@ spk_status spk_render_noalloc(spk_ctx *ctx, uint32_t num_frames, void *d_hdr_rgb
 spk_status spk_checkpoint_size(const spk_ctx *ctx, uint64_t *bytes);
 spk_status spk_save_checkpoint(spk_ctx *ctx, void *buffer, uint64_t size);
 spk_status spk_load_checkpoint(spk_ctx *ctx, const void *buffer, uint64_t size);
+
+/* The acceleration structure of a single-scene context as a blob: every mesh's BLAS (flattened 8-wide
+ * nodes and leaf order) tagged with its face / vertex counts, a hash of its positions and indices and the
+ * BVH knobs it was built with. spk_set_bvh hands such a blob to a context (host memory, copied): its next
+ * spk_set_scene takes each mesh's BLAS from the blob when that mesh and the knobs match, and builds the
+ * others; spk_stats.blas_reused counts the reused ones; spk_set_bvh(ctx, NULL, 0) drops the blob. A scene
+ * reloaded this way skips the BLAS builds (seconds for large meshes) and gets the same nodes. */
+spk_status spk_bvh_blob_size(spk_ctx *ctx, uint64_t *bytes);
+spk_status spk_save_bvh(spk_ctx *ctx, void *blob, uint64_t size);
+spk_status spk_set_bvh(spk_ctx *ctx, const void *blob, uint64_t size);
 
 /* Test hooks for failure handling, no GPU fault involved. spk_debug_fail_allocation(n): the nth device
  * allocation the library makes from now on fails as out of memory, once (0 disarms); the entry point

@@ -71,7 +71,7 @@ class spk_stats(C.Structure):
                 ("device_ms", _f), ("trace_kernel_ms", _f), ("trace_launches", _u32), ("kernel_launches", _u32),
                 ("error_flags", _u32), ("bvh_nodes", _u32), ("bvh_bytes", C.c_uint64),
                 ("node_visits", C.c_uint64), ("triangle_tests", C.c_uint64), ("graph_replays", _u32),
-                ("reserved0", _u32)]
+                ("blas_reused", _u32)]
 
 
 class spk_tuning(C.Structure):

@@ -80,6 +80,26 @@ struct MeshBlas {
     double bounds[6] = {0, 0, 0, 0, 0, 0};  // local-space box (lo, hi)
 };
 
+// One mesh's BLAS from a BVH blob (spk_set_bvh): its wide nodes and leaf items as the builders return them,
+// the mesh it was built for (face and vertex counts, a hash of positions and indices) and the BVH knobs.
+struct CachedBlas {
+    uint32_t num_faces = 0, num_vertices = 0;
+    uint64_t hash = 0;
+    WideBvh bvh;
+};
+
+// 64-bit FNV-1a over the 32-bit words of a mesh's positions and indices.
+uint64_t geometry_hash(const float *positions, uint32_t num_vertices, const uint32_t *indices, uint32_t num_faces) {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](const void *p, size_t words) {
+        const auto *w = static_cast<const uint32_t *>(p);
+        for (size_t i = 0; i < words; ++i) h = (h ^ w[i]) * 1099511628211ull;
+    };
+    if (positions) mix(positions, 3ull * num_vertices);
+    if (indices) mix(indices, 3ull * num_faces);
+    return h;
+}
+
 // The instance list, mesh geometry and BLAS placement of a single-scene context, kept on the host so that
 // spk_set_instances / spk_set_instance_transforms / spk_update_mesh can rebuild the TLAS and the light table
 // (SceneRenderProxy::UpdateBVH, SceneRenderProxy.cpp:269-297) without rebuilding any BLAS.
@@ -92,6 +112,7 @@ struct DynScene {
     std::vector<DevMaterial> mats;
     std::vector<DevInstance> insts;
     DevSceneDesc desc{};
+    spk_tuning built_with{};     // the BVH knobs of the build (spk_save_bvh records them)
     uint32_t tlas_root = 0;      // first TLAS node = number of BLAS nodes
     uint32_t node_capacity = 0;  // nodes allocated on the device
 };
@@ -131,6 +152,9 @@ struct spk_ctx {
     DevScene scene{};
     bool has_scene = false;
     DynScene dyn;                          // single-scene contexts: what the incremental updates need
+    std::vector<CachedBlas> bvh_cache;     // BLASes handed in by spk_set_bvh, by mesh index
+    uint32_t bvh_cache_knobs[4] = {0, 0, 0, 0};  // width, leaf size, collapse, builder they were built with
+    uint32_t blas_reused = 0;              // BLASes the last scene build took from bvh_cache
     DevBuf<float> dyn_pos, dyn_attr, dyn_boxes;  // refit scratch: positions, normals + tangents, node boxes
     uint32_t bvh_nodes = 0;
     uint64_t bvh_bytes = 0;
@@ -550,7 +574,19 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
             if (!device_build) boxes[f] = b;
         }
         WideBvh wide;
-        if (device_build) {
+        const uint32_t knobs[4] = {ctx->tuning.bvh_width, ctx->tuning.bvh_leaf_size, ctx->tuning.bvh_collapse,
+                                   ctx->tuning.bvh_builder};
+        const CachedBlas *cached = nullptr;
+        if (k < ctx->bvh_cache.size() && std::memcmp(knobs, ctx->bvh_cache_knobs, sizeof(knobs)) == 0) {
+            const CachedBlas &c = ctx->bvh_cache[k];
+            if (c.num_faces == m.num_faces && c.num_vertices == m.num_vertices &&
+                c.hash == geometry_hash(m.positions, m.num_vertices, m.indices, m.num_faces))
+                cached = &c;
+        }
+        if (cached) {
+            wide = cached->bvh;
+            ++ctx->blas_reused;
+        } else if (device_build) {
             std::vector<uint32_t> lv;
             const cudaError_t e = build_wide_device(m.positions, m.num_vertices, m.indices, m.num_faces,
                                                     static_cast<int>(ctx->tuning.bvh_width),
@@ -915,6 +951,7 @@ spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t n
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     ctx->dyn = DynScene{};
+    ctx->blas_reused = 0;
     HostScene all;
     std::vector<DevSceneDesc> descs(num_scenes);
     for (uint32_t k = 0; k < num_scenes; ++k) {
@@ -950,6 +987,7 @@ spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t n
             dy.insts = std::move(hs.insts);
             dy.desc = descs[0];
             dy.tlas_root = blas_nodes;
+            dy.built_with = ctx->tuning;
             dy.node_capacity = static_cast<uint32_t>(capacity);
             dy.valid = true;
             return SPK_OK;
@@ -1412,6 +1450,130 @@ spk_status spk_load_checkpoint(spk_ctx *ctx, const void *buffer, uint64_t size) 
     return SPK_OK;
 }
 
+// BVH blob: header {magic, version, mesh count, knobs[4]}, per mesh {faces, vertices, hash, node count,
+// item count}, then per mesh its nodes (80 B, child and item bases relative to the mesh's BLAS) and items.
+namespace {
+struct BvhBlobHeader {
+    char magic[8];
+    uint32_t version, num_meshes;
+    uint32_t knobs[4];
+};
+struct BvhBlobMesh {
+    uint32_t num_faces, num_vertices;
+    uint64_t hash;
+    uint32_t node_count, item_count;
+};
+constexpr char kBvhMagic[8] = {'S', 'P', 'K', 'B', 'V', 'H', '0', '1'};
+}  // namespace
+
+spk_status spk_bvh_blob_size(spk_ctx *ctx, uint64_t *bytes) {
+    if (!ctx || !bytes) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_scene || !ctx->dyn.valid)
+        return fail(ctx, SPK_ERR_NOT_READY, "BVH blobs are saved from a scene set by spk_set_scene");
+    uint64_t n = sizeof(BvhBlobHeader);
+    for (const MeshBlas &b : ctx->dyn.blas)
+        n += sizeof(BvhBlobMesh) + static_cast<uint64_t>(b.node_count) * sizeof(WideNode) + 4ull * b.tri_count;
+    *bytes = n;
+    return SPK_OK;
+}
+
+spk_status spk_save_bvh(spk_ctx *ctx, void *blob, uint64_t size) try {
+    uint64_t need = 0;
+    spk_status st = spk_bvh_blob_size(ctx, &need);
+    if (st != SPK_OK) return st;
+    if (!blob || size < need) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "BVH blob buffer too small");
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    const DynScene &dy = ctx->dyn;
+    auto *out = static_cast<uint8_t *>(blob);
+    BvhBlobHeader h{};
+    std::memcpy(h.magic, kBvhMagic, 8);
+    h.version = 1;
+    h.num_meshes = static_cast<uint32_t>(dy.blas.size());
+    const uint32_t knobs[4] = {dy.built_with.bvh_width, dy.built_with.bvh_leaf_size, dy.built_with.bvh_collapse,
+                               dy.built_with.bvh_builder};
+    std::memcpy(h.knobs, knobs, sizeof(knobs));
+    std::memcpy(out, &h, sizeof(h));
+    uint8_t *meta = out + sizeof(h);
+    uint8_t *data = meta + dy.blas.size() * sizeof(BvhBlobMesh);
+    for (size_t k = 0; k < dy.blas.size(); ++k) {
+        const MeshBlas &b = dy.blas[k];
+        BvhBlobMesh mm{};
+        mm.num_faces = static_cast<uint32_t>(dy.indices[k].size() / 3);
+        mm.num_vertices = static_cast<uint32_t>(dy.positions[k].size() / 3);
+        mm.hash = geometry_hash(dy.positions[k].data(), mm.num_vertices, dy.indices[k].data(), mm.num_faces);
+        mm.node_count = b.root == kInvalid ? 0 : b.node_count;
+        mm.item_count = b.root == kInvalid ? 0 : b.tri_count;
+        std::memcpy(meta + k * sizeof(BvhBlobMesh), &mm, sizeof(mm));
+        if (mm.node_count) {
+            std::vector<WideNode> nodes(mm.node_count);
+            std::vector<float4> tris(3ull * mm.item_count);
+            cudaError_t e;
+            if ((e = cudaMemcpy(nodes.data(), ctx->nodes.ptr + 5ull * b.root, nodes.size() * sizeof(WideNode),
+                                cudaMemcpyDeviceToHost)) != cudaSuccess ||
+                (e = cudaMemcpy(tris.data(), ctx->tris.ptr + 3ull * b.tri_first, tris.size() * sizeof(float4),
+                                cudaMemcpyDeviceToHost)) != cudaSuccess)
+                return cuda_fail(ctx, e, "BVH read");
+            for (WideNode &w : nodes) {
+                w.child_base -= b.root;
+                w.item_base -= b.tri_first;
+            }
+            std::memcpy(data, nodes.data(), nodes.size() * sizeof(WideNode));
+            data += nodes.size() * sizeof(WideNode);
+            for (uint32_t i = 0; i < mm.item_count; ++i) {
+                uint32_t face;
+                std::memcpy(&face, &tris[3ull * i + 2].y, 4);
+                std::memcpy(data + 4ull * i, &face, 4);
+            }
+            data += 4ull * mm.item_count;
+        }
+    }
+    return SPK_OK;
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+}
+
+spk_status spk_set_bvh(spk_ctx *ctx, const void *blob, uint64_t size) try {
+    if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
+    ctx->bvh_cache.clear();
+    if (!blob || size == 0) return SPK_OK;
+    const auto *in = static_cast<const uint8_t *>(blob);
+    BvhBlobHeader h{};
+    if (size < sizeof(h)) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "BVH blob truncated");
+    std::memcpy(&h, in, sizeof(h));
+    if (std::memcmp(h.magic, kBvhMagic, 8) != 0 || h.version != 1)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "not a BVH blob of this version");
+    uint64_t pos = sizeof(h) + static_cast<uint64_t>(h.num_meshes) * sizeof(BvhBlobMesh);
+    if (pos > size) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "BVH blob truncated");
+    std::vector<CachedBlas> cache(h.num_meshes);
+    for (uint32_t k = 0; k < h.num_meshes; ++k) {
+        BvhBlobMesh mm{};
+        std::memcpy(&mm, in + sizeof(h) + k * sizeof(BvhBlobMesh), sizeof(mm));
+        const uint64_t bytes = static_cast<uint64_t>(mm.node_count) * sizeof(WideNode) + 4ull * mm.item_count;
+        if (pos + bytes > size || mm.item_count > mm.num_faces)
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "BVH blob: mesh %u does not fit", k);
+        CachedBlas &c = cache[k];
+        c.num_faces = mm.num_faces;
+        c.num_vertices = mm.num_vertices;
+        c.hash = mm.hash;
+        c.bvh.nodes.resize(mm.node_count);
+        c.bvh.items.resize(mm.item_count);
+        std::memcpy(c.bvh.nodes.data(), in + pos, c.bvh.nodes.size() * sizeof(WideNode));
+        std::memcpy(c.bvh.items.data(), in + pos + c.bvh.nodes.size() * sizeof(WideNode), 4ull * mm.item_count);
+        for (const WideNode &w : c.bvh.nodes)  // every reference stays inside this BLAS
+            if (w.child_base > mm.node_count || w.item_base > mm.item_count)
+                return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "BVH blob: mesh %u has an out-of-range node", k);
+        for (uint32_t f : c.bvh.items)
+            if (f >= mm.num_faces) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "BVH blob: mesh %u has a bad item", k);
+        pos += bytes;
+    }
+    std::memcpy(ctx->bvh_cache_knobs, h.knobs, sizeof(h.knobs));
+    ctx->bvh_cache = std::move(cache);
+    return SPK_OK;
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+}
+
 void spk_debug_fail_allocation(uint32_t nth) { fault_arm_allocation(nth); }
 
 spk_status spk_debug_walk_budget(spk_ctx *ctx, uint32_t steps) {
@@ -1649,6 +1811,7 @@ spk_status spk_get_stats(spk_ctx *ctx, spk_stats *out) {
     ctx->last.bvh_nodes = ctx->bvh_nodes;
     ctx->last.bvh_bytes = ctx->bvh_bytes;
     *out = ctx->last;
+    out->blas_reused = ctx->blas_reused;
     return SPK_OK;
 }
 

@@ -34,7 +34,7 @@ EXPORTED = ["spk_abi_version", "spk_create", "spk_destroy", "spk_last_error", "s
             "spk_dn_gradients", "spk_dn_infer", "spk_dn_fallback", "spk_dn_synchronize", "spk_dn_last_ms",
             "spk_dn_conv3x3", "spk_dn_state_size", "spk_dn_save_state", "spk_dn_load_state",
             "spk_dn_debug_wait_timeout", "spk_checkpoint_size", "spk_save_checkpoint", "spk_load_checkpoint",
-            "spk_debug_fail_allocation", "spk_debug_walk_budget"]
+            "spk_debug_fail_allocation", "spk_debug_walk_budget", "spk_bvh_blob_size", "spk_save_bvh", "spk_set_bvh"]
 
 
 class SpkError(RuntimeError):
@@ -103,6 +103,9 @@ def lib(build: bool = True):
         L.spk_debug_fail_allocation.argtypes = [u32]
         L.spk_debug_fail_allocation.restype = None
         L.spk_debug_walk_budget.argtypes = [vp, u32]
+        L.spk_bvh_blob_size.argtypes = [vp, C.POINTER(u64)]
+        L.spk_save_bvh.argtypes = [vp, vp, u64]
+        L.spk_set_bvh.argtypes = [vp, vp, u64]
         L.spk_dn_state_size.argtypes = [vp, C.POINTER(u64)]
         L.spk_dn_save_state.argtypes = [vp, vp, u64]
         L.spk_dn_load_state.argtypes = [vp, vp, u64]
@@ -266,6 +269,22 @@ class Context:
         """spk_load_checkpoint: resume from save_checkpoint() bytes (same config; scene and camera set)."""
         buf = np.frombuffer(data, np.uint8)
         self._check(self.L.spk_load_checkpoint(self.h, _p(buf), buf.size))
+
+    def save_bvh(self) -> bytes:
+        """spk_save_bvh: the scene's BLASes as a blob for a later spk_set_bvh."""
+        n = C.c_uint64()
+        self._check(self.L.spk_bvh_blob_size(self.h, C.byref(n)))
+        buf = np.zeros(n.value, np.uint8)
+        self._check(self.L.spk_save_bvh(self.h, _p(buf), n.value))
+        return buf.tobytes()
+
+    def set_bvh(self, blob):
+        """spk_set_bvh: reuse a saved blob's BLASes at the next set_scene (None drops it)."""
+        if blob is None:
+            self._check(self.L.spk_set_bvh(self.h, None, 0))
+            return
+        buf = np.frombuffer(blob, np.uint8)
+        self._check(self.L.spk_set_bvh(self.h, _p(buf), buf.size))
 
     def debug_walk_budget(self, steps: int):
         """spk_debug_walk_budget: at most `steps` node steps per ray walk (0 = the default)."""
