@@ -348,8 +348,9 @@ def run_ours(args):
 def scene_update_metric(scene, camera):
     """Scene build and incremental updates on the stress scene (wall time through the C ABI, host arrays in):
     spk_set_scene with the host SAH and with the device LBVH BLAS builder and the Mrays/s each tree traces at
-    (16 frames of the bench workload, device time), spk_update_mesh of the 2.1M-triangle terrain (device
-    refit of its BLAS + TLAS rebuild) and spk_set_instance_transforms of the 64 spheres (TLAS rebuild)."""
+    (16 frames of the bench workload, device time), spk_set_scene reusing a spk_save_bvh blob, spk_update_mesh
+    of the 2.1M-triangle terrain (device refit of its BLAS + TLAS rebuild) and spk_set_instance_transforms of
+    the 64 spheres (TLAS rebuild)."""
     import numpy as np
     from sparkle_gb300 import abi, native
     c = native.Context(0)
@@ -371,6 +372,14 @@ def scene_update_metric(scene, camera):
                      "mrays": round((st["extension_rays"] + st["shadow_rays"]) / (st["device_ms"] * 1e3), 1)}
     c.set_tuning(bvh_builder=0)
     c.set_scene(scene)
+    blob = c.save_bvh()
+    r = native.Context(0)
+    r.set_bvh(blob)
+    t0 = time.perf_counter()
+    r.set_scene(scene)
+    out["set_scene_from_bvh_blob_ms"] = {"value": round((time.perf_counter() - t0) * 1e3, 1),
+                                         "blas_reused": r.stats()["blas_reused"], "blob_bytes": len(blob)}
+    r.close()
     terrain = scene.meshes[0]
     moved = terrain.positions.copy()
     moved[:, 2] += np.float32(0.5) * np.sin(moved[:, 0] * np.float32(0.3)).astype(np.float32)
