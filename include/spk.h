@@ -321,6 +321,9 @@ spk_status spk_camera_from_look(const float position[3], const float target[3], 
  * and output image for `width` x `height` and derives the per-frame sample count round(sqrt(spp))^2. */
 spk_status spk_set_config(spk_ctx *ctx, const spk_config *config);
 
+/* The context's current spk_config (SPK_ERR_NOT_READY before spk_set_config). */
+spk_status spk_get_config(const spk_ctx *ctx, spk_config *out);
+
 /* Replaces `num_frames` calls of CPURenderer::Render (CPURenderer.cpp:119-208) on a static scene: per frame
  * the clear (if dirty), BasePass (:419-450), DenoisePass (:506-552) and ToneMappingPass (:565-576), with
  * the camera's cumulated-sample bookkeeping between frames (CameraRenderProxy.cpp:66-75). Asynchronous

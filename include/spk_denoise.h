@@ -85,6 +85,15 @@ spk_status spk_dn_fallback(spk_denoiser *dn, const float *d_denoised, const floa
                            const float *d_plain, uint32_t h, uint32_t w, uint32_t tile, float threshold,
                            float *d_out, uint32_t *fallback_tiles);
 
+/* The denoised frame of sparkle_gb300/denoise.py's render_denoised in one call: renders `spp` samples per
+ * pixel on `ctx` (camera, config and scene set; the accumulation continues as spk_render's does) in two
+ * halves, renders the primary-hit guides, denoises the full mean and, when spp >= 2, each half, and
+ * replaces the tiles (tile x tile pixels) whose two denoised halves disagree by more than `threshold` with
+ * the plain mean (spk_dn_fallback). `denoised_rgba` (width*height float4, rows bottom up like the frame
+ * buffer, host or device) receives the result and *fallback_tiles (may be NULL) the replaced tiles. */
+spk_status spk_render_denoised(spk_ctx *ctx, spk_denoiser *dn, uint32_t spp, uint32_t tile, float threshold,
+                               float *denoised_rgba, uint32_t *fallback_tiles);
+
 /* Training checkpoint: the FP32 parameters, both Adam moments and the step count (spk_dn_state_size
  * bytes, host buffer), so that training stops and resumes where it was. */
 spk_status spk_dn_state_size(const spk_denoiser *dn, uint64_t *bytes);

@@ -1138,6 +1138,13 @@ spk_status spk_read_bvh_nodes(spk_ctx *ctx, void *nodes, uint64_t capacity, uint
     return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
 
+spk_status spk_get_config(const spk_ctx *ctx, spk_config *out) {
+    if (!ctx || !out) return SPK_ERR_INVALID_ARGUMENT;
+    if (!ctx->has_config) return SPK_ERR_NOT_READY;
+    *out = ctx->cfg;
+    return SPK_OK;
+}
+
 spk_status spk_set_camera(spk_ctx *ctx, const spk_camera *camera) {
     if (!ctx || !camera) return SPK_ERR_INVALID_ARGUMENT;
     static_assert(sizeof(DevCamera) == sizeof(spk_camera), "camera layout");

@@ -19,6 +19,7 @@
 #include "conv_tc.cuh"
 #include "fault.h"
 #include "spk_denoise.h"
+#include "../../include/spk.h"
 
 using bf16 = __nv_bfloat16;
 
@@ -401,6 +402,7 @@ struct spk_denoiser {
     DBuf<bf16> wb, wt;  // BF16 weights [cout][9][cin] and dgrad weights [cin][9][cout]
     uint64_t adam_t = 0;
     DBuf<uint32_t> err;
+    DBuf<float> frame;  // spk_render_denoised scratch
     DBuf<double> loss;
     // activations (forward) and gradients (backward), sized for the largest batch seen
     DBuf<bf16> x0, out, gout;
@@ -691,7 +693,7 @@ spk_status spk_dn_destroy(spk_denoiser *dn) {
     if (!dn) return SPK_OK;
     cudaSetDevice(dn->device);
     if (dn->stream) cudaStreamSynchronize(dn->stream);
-    DBuf<float> *fb[] = {&dn->params, &dn->grads, &dn->adam_m, &dn->adam_v};
+    DBuf<float> *fb[] = {&dn->params, &dn->grads, &dn->adam_m, &dn->adam_v, &dn->frame};
     for (auto *b : fb) b->release();
     DBuf<bf16> *bb[] = {&dn->wb, &dn->wt, &dn->x0, &dn->out, &dn->gout, &dn->eb4, &dn->conv_wt_scratch};
     for (auto *b : bb) b->release();
@@ -801,6 +803,57 @@ spk_status spk_dn_load_state(spk_denoiser *dn, const void *host, uint64_t size) 
     DN_TRY(cudaStreamSynchronize(dn->stream), "synchronize");
     dn->adam_t = h.adam_t;
     return SPK_OK;
+}
+
+spk_status spk_render_denoised(spk_ctx *ctx, spk_denoiser *dn, uint32_t spp, uint32_t tile, float threshold,
+                               float *denoised_rgba, uint32_t *fallback_tiles) try {
+    if (!ctx || !dn || !denoised_rgba || spp == 0 || tile == 0) return SPK_ERR_INVALID_ARGUMENT;
+    const DnRange range("spk_render_denoised");
+    spk_config cfg{};
+    spk_status st = spk_get_config(ctx, &cfg);
+    if (st != SPK_OK) return st;
+    const uint32_t w = cfg.width, h = cfg.height;
+    const size_t px = static_cast<size_t>(w) * h;
+    cudaSetDevice(dn->device);
+    // scratch: half A, three feature sets, three denoised images, the output
+    DN_TRY(dn->frame.ensure(px * (4 + 3 * SPK_DN_FEATURES + 3 * 4 + 4)), "frame scratch");
+    float *half_a = dn->frame.p, *feat = half_a + 4 * px, *feat_a = feat + SPK_DN_FEATURES * px,
+          *feat_b = feat_a + SPK_DN_FEATURES * px, *den = feat_b + SPK_DN_FEATURES * px, *den_a = den + 4 * px,
+          *den_b = den_a + 4 * px, *out = den_b + 4 * px;
+    void *fb = nullptr, *img = nullptr, *nd = nullptr, *alb = nullptr;
+    const uint32_t half = spp / 2;
+    if (half >= 1) {
+        if ((st = spk_render(ctx, half)) != SPK_OK || (st = spk_synchronize(ctx)) != SPK_OK ||
+            (st = spk_framebuffer_device(ctx, &fb, &img)) != SPK_OK)
+            return dn_fail(dn, st, "render (first half): %s", spk_last_error(ctx));
+        DN_TRY(cudaMemcpyAsync(half_a, fb, px * 4 * sizeof(float), cudaMemcpyDeviceToDevice, dn->stream), "half copy");
+        DN_TRY(cudaStreamSynchronize(dn->stream), "synchronize");
+    }
+    if ((st = spk_render(ctx, spp - half)) != SPK_OK || (st = spk_render_guides(ctx)) != SPK_OK ||
+        (st = spk_synchronize(ctx)) != SPK_OK || (st = spk_framebuffer_device(ctx, &fb, &img)) != SPK_OK ||
+        (st = spk_guides_device(ctx, &nd, &alb)) != SPK_OK)
+        return dn_fail(dn, st, "render: %s", spk_last_error(ctx));
+    const auto *ffb = static_cast<const float *>(fb), *fnd = static_cast<const float *>(nd),
+               *falb = static_cast<const float *>(alb);
+    if ((st = spk_dn_pack_features(dn, ffb, fnd, falb, 1, h, w, feat)) != SPK_OK ||
+        (st = spk_dn_infer(dn, feat, 1, h, w, den)) != SPK_OK)
+        return st;
+    uint32_t tiles = 0;
+    const float *result = den;
+    if (half >= 1) {
+        if ((st = spk_dn_pack_halves(dn, ffb, half_a, fnd, falb, 1, h, w, feat_a, feat_b)) != SPK_OK ||
+            (st = spk_dn_infer(dn, feat_a, 1, h, w, den_a)) != SPK_OK ||
+            (st = spk_dn_infer(dn, feat_b, 1, h, w, den_b)) != SPK_OK ||
+            (st = spk_dn_fallback(dn, den, den_a, den_b, ffb, h, w, tile, threshold, out, &tiles)) != SPK_OK)
+            return st;
+        result = out;
+    }
+    DN_TRY(cudaMemcpyAsync(denoised_rgba, result, px * 4 * sizeof(float), cudaMemcpyDefault, dn->stream), "output");
+    DN_TRY(cudaStreamSynchronize(dn->stream), "synchronize");
+    if (fallback_tiles) *fallback_tiles = tiles;
+    return SPK_OK;
+} catch (const std::bad_alloc &) {
+    return dn_fail(dn, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
 }
 
 spk_status spk_dn_debug_wait_timeout(spk_denoiser *dn) {

@@ -34,7 +34,8 @@ EXPORTED = ["spk_abi_version", "spk_create", "spk_destroy", "spk_last_error", "s
             "spk_dn_gradients", "spk_dn_infer", "spk_dn_fallback", "spk_dn_synchronize", "spk_dn_last_ms",
             "spk_dn_conv3x3", "spk_dn_state_size", "spk_dn_save_state", "spk_dn_load_state",
             "spk_dn_debug_wait_timeout", "spk_checkpoint_size", "spk_save_checkpoint", "spk_load_checkpoint",
-            "spk_debug_fail_allocation", "spk_debug_walk_budget", "spk_bvh_blob_size", "spk_save_bvh", "spk_set_bvh"]
+            "spk_debug_fail_allocation", "spk_debug_walk_budget", "spk_bvh_blob_size", "spk_save_bvh", "spk_set_bvh",
+            "spk_get_config", "spk_render_denoised"]
 
 
 class SpkError(RuntimeError):
@@ -103,6 +104,8 @@ def lib(build: bool = True):
         L.spk_debug_fail_allocation.argtypes = [u32]
         L.spk_debug_fail_allocation.restype = None
         L.spk_debug_walk_budget.argtypes = [vp, u32]
+        L.spk_get_config.argtypes = [vp, vp]
+        L.spk_render_denoised.argtypes = [vp, vp, u32, u32, C.c_float, vp, C.POINTER(u32)]
         L.spk_bvh_blob_size.argtypes = [vp, C.POINTER(u64)]
         L.spk_save_bvh.argtypes = [vp, vp, u64]
         L.spk_set_bvh.argtypes = [vp, vp, u64]
@@ -482,6 +485,14 @@ class Denoiser:
         """spk_dn_load_state: resume training from save_state() bytes."""
         buf = np.frombuffer(data, np.uint8)
         self._check(self.L.spk_dn_load_state(self.h, _p(buf), buf.size))
+
+    def render_denoised(self, ctx, spp: int, tile: int = 16, threshold: float = 0.02):
+        """spk_render_denoised: (denoised (H, W, 4) float32 bottom row first, fallback tile count)."""
+        w, h = ctx.config.width, ctx.config.height
+        out = np.zeros((h, w, 4), np.float32)
+        tiles = C.c_uint32()
+        self._check(self.L.spk_render_denoised(ctx.h, self.h, spp, tile, threshold, _p(out), C.byref(tiles)))
+        return out, tiles.value
 
     def debug_wait_timeout(self):
         """spk_dn_debug_wait_timeout: a kernel whose bounded mbarrier wait runs out (raises SpkError 5)."""
