@@ -185,3 +185,25 @@ def test_update_validation(ctx, small_terrain, cornell):
     ctx.set_scenes([scene, cornell[0]])  # several scenes: no incremental updates
     with pytest.raises(native.SpkError):
         ctx.set_instance_transforms(0, np.eye(3, 4)[None])
+
+
+def test_empty_instance_list_and_back(ctx, cornell):
+    scene, cam_args = cornell
+    cfg = abi.make_config(32, 24, spp=1, bounce=3, seed=5)
+    ctx.set_scene(scene)
+    ref = render(ctx, (scene, cam_args), cfg)
+    ctx.set_instances([])
+    empty = render(ctx, (scene, cam_args), cfg)
+    assert np.all(empty[..., :3] == 0)  # no geometry, no sky
+    hits = ctx.trace(scenes.random_rays(np.zeros(3), np.ones(3), 1000, seed=1))
+    assert np.all(hits["prim"] == 0xFFFFFFFF)
+    ctx.set_instances(scene.instances)
+    assert np.array_equal(render(ctx, (scene, cam_args), cfg).view(np.uint32), ref.view(np.uint32))
+    # a mesh with no faces updates without a BLAS
+    empty_mesh = abi.Mesh(np.zeros((3, 3), np.float32), np.tile([[0, 0, 1]], (3, 1)).astype(np.float32),
+                          np.zeros((0, 3), np.uint32))
+    sc = abi.Scene(scene.meshes + [empty_mesh], scene.instances + [abi.Instance(len(scene.meshes), 0, np.eye(3, 4))],
+                   scene.materials, scene.sky)
+    ctx.set_scene(sc)
+    ctx.update_mesh(len(scene.meshes), np.ones((3, 3), np.float32))
+    assert np.array_equal(render(ctx, (sc, cam_args), cfg).view(np.uint32), ref.view(np.uint32))
