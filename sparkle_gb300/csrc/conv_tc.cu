@@ -1,15 +1,17 @@
 // conv_tc.cu -- tcgen05 implicit-GEMM 3x3 convolutions (see conv_tc.cuh).
 //
-// Forward / dgrad (one CTA per output tile of tw x th = 128 pixels, tw a multiple of 8, 4 warps):
+// Forward / dgrad (one CTA per output tile of tw x (mt * th) pixels: mt M tiles of tw x th = 128 pixels
+// stacked vertically, tw a multiple of 8, 4 warps):
 //   warp 0 lane 0  TMA producer: per K block (column tap dx, 32-channel chunk) one 4-D tiled load of the
-//                  input box {32 ch, tw px, th + 2 rows, 1 image} shifted by dx and reaching one row above
-//                  and below the tile (zero fill outside the image = the conv's padding), and three 2-D
-//                  loads of the weight slices {32, cout} of the taps (dy, dx), dy = -1, 0, 1, into a ring
-//                  of 2-4 stages;
-//   warp 1 lane 0  MMA issuer: per stage and row tap dy, two kind::f16 MMAs (K = 16 each) whose A operand
-//                  starts (dy + 1) * tw rows into the input box -- a whole number of 8-row swizzle atoms, so
-//                  one box serves all three row taps -- into a 128 x cout FP32 accumulator in TMEM,
-//                  committing each stage back to the producer;
+//                  input box {32 ch, tw px, mt * th + 2 rows, 1 image} shifted by dx and reaching one row
+//                  above and below the tile (zero fill outside the image = the conv's padding), and three
+//                  2-D loads of the weight slices {32, cout} of the taps (dy, dx), dy = -1, 0, 1, into a
+//                  ring of 2-4 stages;
+//   warp 1 lane 0  MMA issuer: per stage, row tap dy and M tile m, two kind::f16 MMAs (K = 16 each) whose A
+//                  operand starts (m * th + dy + 1) * tw rows into the input box -- a whole number of 8-row
+//                  swizzle atoms, so one box serves all three row taps of all M tiles and one weight slice
+//                  serves all M tiles -- into M tile m's 128 x cout FP32 accumulator in TMEM (columns
+//                  m * cout ...), committing each stage back to the producer;
 //   all 4 warps    epilogue: tcgen05.ld of the pixel rows (warp w owns TMEM lanes 32w..32w+31), bias,
 //                  ReLU or ReLU-backward mask, BF16 pack, 16-byte stores.
 // Wgrad (one CTA per (128 rows of (tap, ci), pixel range)): all threads gather and transpose the shifted
@@ -38,26 +40,40 @@ constexpr uint32_t kMaxCout = 256;
 #endif
 constexpr uint32_t kStageBudget = SPK_CONV_STAGE_BUDGET_KB;
 
-struct FwdParams {
-    uint32_t n, h, w;
-    uint32_t cin, cout;
-    uint32_t tw, th, tiles_x, tiles_y;
-    uint32_t stages, a_bytes, stage_bytes;  // ring depth; input box and stage sizes (1024-byte multiples)
+#ifndef SPK_CONV_TMA_STORE
+#define SPK_CONV_TMA_STORE 1  // 1: forward epilogue staged in shared memory and written by TMA stores
+#endif
+#ifndef SPK_CONV_MTILES
+#define SPK_CONV_MTILES 0  // M tiles (128 pixels each) per forward CTA: 1, 2 or 4; 0 = chosen per layer
+#endif
+
+// Where and how the forward kernels write a pixel's output channels.
+struct OutSpec {
     __nv_bfloat16 *out;
     uint32_t out_ld;
     const float *bias;
     uint32_t relu;
     const __nv_bfloat16 *mask;
     uint32_t mask_ld;
+};
+
+struct FwdParams {
+    uint32_t n, h, w;
+    uint32_t cin, cout;
+    uint32_t tw, th, mt, tiles_x, tiles_y;  // M tile tw x th; mt M tiles per CTA; CTA tiles of tw x mt*th
+    uint32_t stages, a_bytes, stage_bytes;  // ring depth; input box and stage sizes (1024-byte multiples)
+    uint32_t stage_out;                     // 1: epilogue through shared memory and TMA stores
+    OutSpec out_spec;
     uint32_t *err;
 };
 
-// Input box {32 ch, tw, th + 2} and the three weight slices of one column tap, each 1024-byte aligned.
-__host__ __device__ constexpr uint32_t fwd_a_bytes(uint32_t tw, uint32_t th) {
-    return (64u * tw * (th + 2u) + 1023u) & ~1023u;
+// Input box {32 ch, tw, rows + 2} (rows = mt * th) and the three weight slices of one column tap, each
+// 1024-byte aligned.
+__host__ __device__ constexpr uint32_t fwd_a_bytes(uint32_t tw, uint32_t rows) {
+    return (64u * tw * (rows + 2u) + 1023u) & ~1023u;
 }
-__host__ __device__ constexpr uint32_t fwd_stage_bytes(uint32_t tw, uint32_t th, uint32_t cout) {
-    return fwd_a_bytes(tw, th) + ((3u * cout * 64u + 1023u) & ~1023u);
+__host__ __device__ constexpr uint32_t fwd_stage_bytes(uint32_t tw, uint32_t rows, uint32_t cout) {
+    return fwd_a_bytes(tw, rows) + ((3u * cout * 64u + 1023u) & ~1023u);
 }
 
 __host__ __device__ constexpr uint32_t tmem_columns(uint32_t n) {
@@ -74,8 +90,35 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return *reinterpret_cast<const uint32_t *>(&v);
 }
 
+// Output channels col0..col0+15 of pixel `pix` from 16 FP32 accumulator columns: + bias (`bias16`, or
+// none), then the ReLU-backward mask (keep where mask > 0; read only for pixels inside the image) or ReLU,
+// packed to BF16 pairs.
+__device__ __forceinline__ void epilogue_pack(const OutSpec &O, const uint32_t (&v)[16], const float *bias16,
+                                              size_t pix, uint32_t col0, bool inb, uint32_t (&pk)[8]) {
+    float f[16];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) f[e] = __uint_as_float(v[e]) + (bias16 ? bias16[e] : 0.f);
+    if (O.mask && inb) {
+        const uint4 *mp = reinterpret_cast<const uint4 *>(O.mask + pix * O.mask_ld + col0);
+        const uint4 m0 = mp[0], m1 = mp[1];
+        const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+            const uint32_t bits = (mw[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
+            // bf16 > 0: sign bit clear and not +0
+            if ((bits & 0x8000u) || bits == 0u) f[e] = 0.f;
+        }
+    } else if (O.relu) {
+#pragma unroll
+        for (int e = 0; e < 16; ++e) f[e] = fmaxf(f[e], 0.f);
+    }
+#pragma unroll
+    for (int e = 0; e < 8; ++e) pk[e] = pack_bf16(f[2 * e], f[2 * e + 1]);
+}
+
 __global__ void __launch_bounds__(128, 1)
-    k_conv_fwd(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw, FwdParams P) {
+    k_conv_fwd(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw,
+               const __grid_constant__ CUtensorMap tmy, FwdParams P) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = align1024(smem_raw);
     const uint32_t b_bytes = P.cout * 64u;  // one weight slice
@@ -84,7 +127,8 @@ __global__ void __launch_bounds__(128, 1)
     uint64_t *full = bars, *empty = bars + kStages, *accum = bars + 2 * kStages;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kStages + 1);
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    const uint32_t ncols = tmem_columns(P.cout);
+    const uint32_t ncols = tmem_columns(P.mt * P.cout);
+    const uint32_t rows = P.mt * P.th;  // output rows of the CTA tile
 
     if (threadIdx.x == 0) {
         for (uint32_t s = 0; s < nst; ++s) {
@@ -107,7 +151,7 @@ __global__ void __launch_bounds__(128, 1)
     t /= P.tiles_x;
     const uint32_t ty = t % P.tiles_y;
     const uint32_t img = t / P.tiles_y;
-    const int x0 = static_cast<int>(tx * P.tw), y0 = static_cast<int>(ty * P.th);
+    const int x0 = static_cast<int>(tx * P.tw), y0 = static_cast<int>(ty * rows);
     const uint32_t nch = P.cin / 32u, nk = 3u * nch;  // K blocks: (column tap, channel chunk)
 
     if (warp == 0 && lane == 0) {
@@ -116,7 +160,7 @@ __global__ void __launch_bounds__(128, 1)
             if (u > 0 && !mbar_wait(&empty[s], (u - 1) & 1u, P.err)) break;
             uint8_t *a = smem + s * stage_bytes;
             uint8_t *b = a + P.a_bytes;
-            mbar_arrive_expect_tx(&full[s], 64u * P.tw * (P.th + 2u) + 3u * b_bytes);
+            mbar_arrive_expect_tx(&full[s], 64u * P.tw * (rows + 2u) + 3u * b_bytes);
             const uint32_t dx3 = kb / nch, c = kb - dx3 * nch;
             tma_load_4d(a, &tmx, &full[s], static_cast<int>(c * 32u), x0 + static_cast<int>(dx3) - 1, y0 - 1,
                         static_cast<int>(img));
@@ -136,11 +180,14 @@ __global__ void __launch_bounds__(128, 1)
             const uint32_t a = smem_u32(smem + s * stage_bytes), b = a + P.a_bytes;
 #pragma unroll
             for (uint32_t dy3 = 0; dy3 < 3; ++dy3) {
-                const uint32_t ad = a + dy3 * P.tw * 64u, bd = b + dy3 * b_bytes;
+                const uint32_t bd = b + dy3 * b_bytes;
+                for (uint32_t m = 0; m < P.mt; ++m) {
+                    const uint32_t ad = a + (m * P.th + dy3) * P.tw * 64u;
 #pragma unroll
-                for (uint32_t k2 = 0; k2 < 2; ++k2)
-                    mma_bf16(tmem, smem_desc_sw64(ad + 32u * k2), smem_desc_sw64(bd + 32u * k2), idesc,
-                             (kb | dy3 | k2) != 0u);
+                    for (uint32_t k2 = 0; k2 < 2; ++k2)
+                        mma_bf16(tmem + m * P.cout, smem_desc_sw64(ad + 32u * k2), smem_desc_sw64(bd + 32u * k2),
+                                 idesc, (kb | dy3 | k2) != 0u);
+                }
             }
             mma_commit(&empty[s]);
         }
@@ -152,37 +199,44 @@ __global__ void __launch_bounds__(128, 1)
     bool ready = mbar_wait(accum, 0, P.err);
     ready = __all_sync(0xFFFFFFFFu, ready);
     tc_fence_after();
-    if (ready) {
-        const uint32_t r = warp * 32u + lane;
-        const uint32_t px = static_cast<uint32_t>(x0) + (r % P.tw), py = static_cast<uint32_t>(y0) + (r / P.tw);
+    // With P.stage_out the tile goes through shared memory (the ring, idle once every MMA has completed):
+    // per M tile and 32-channel chunk a 128-row x 64-byte region in the 64-byte-swizzled layout (rows =
+    // pixels of the M tile in box order), written by a 4-D TMA store that writes whole lines and drops the
+    // pixels outside the image. Otherwise each thread stores its pixel's channels itself.
+    const uint32_t r = warp * 32u + lane;
+    const uint32_t chunks = P.cout / 32u;
+    for (uint32_t m = 0; ready && m < P.mt; ++m) {
+        const uint32_t px = static_cast<uint32_t>(x0) + (r % P.tw);
+        const uint32_t py = static_cast<uint32_t>(y0) + m * P.th + (r / P.tw);
         const bool inb = px < P.w && py < P.h;
         const size_t pix = (static_cast<size_t>(img) * P.h + py) * P.w + px;
         for (uint32_t j = 0; j < P.cout / 16u; ++j) {
-            uint32_t v[16];
-            tmem_ld16(tmem + ((warp * 32u) << 16) + j * 16u, v);
-            if (!inb) continue;
-            float f[16];
-#pragma unroll
-            for (int e = 0; e < 16; ++e) f[e] = __uint_as_float(v[e]) + (P.bias ? P.bias[j * 16u + e] : 0.f);
-            if (P.mask) {
-                const uint4 *mp = reinterpret_cast<const uint4 *>(P.mask + pix * P.mask_ld + j * 16u);
-                const uint4 m0 = mp[0], m1 = mp[1];
-                const uint32_t mw[8] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
-#pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    const uint32_t bits = (mw[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
-                    // bf16 > 0: sign bit clear and not +0
-                    if ((bits & 0x8000u) || bits == 0u) f[e] = 0.f;
-                }
-            } else if (P.relu) {
-#pragma unroll
-                for (int e = 0; e < 16; ++e) f[e] = fmaxf(f[e], 0.f);
+            uint32_t v[16], pk[8];
+            tmem_ld16(tmem + ((warp * 32u) << 16) + m * P.cout + j * 16u, v);
+            epilogue_pack(P.out_spec, v, P.out_spec.bias ? P.out_spec.bias + j * 16u : nullptr, pix, j * 16u, inb,
+                          pk);
+            if (P.stage_out) {
+                uint8_t *region = smem + (m * chunks + (j >> 1)) * (kTileM * 64u);
+                const uint32_t c0 = (j & 1u) * 2u;
+                *reinterpret_cast<uint4 *>(region + sw64_offset(r, c0)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                *reinterpret_cast<uint4 *>(region + sw64_offset(r, c0 + 1u)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            } else if (inb) {
+                uint4 *op = reinterpret_cast<uint4 *>(P.out_spec.out + pix * P.out_spec.out_ld + j * 16u);
+                op[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                op[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
             }
-            uint4 *op = reinterpret_cast<uint4 *>(P.out + pix * P.out_ld + j * 16u);
-            op[0] = make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]),
-                               pack_bf16(f[6], f[7]));
-            op[1] = make_uint4(pack_bf16(f[8], f[9]), pack_bf16(f[10], f[11]), pack_bf16(f[12], f[13]),
-                               pack_bf16(f[14], f[15]));
+        }
+    }
+    if (P.stage_out) {
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0 && ready) {
+            for (uint32_t m = 0; m < P.mt; ++m)
+                for (uint32_t cc = 0; cc < chunks; ++cc)
+                    tma_store_4d(&tmy, smem + (m * chunks + cc) * (kTileM * 64u), static_cast<int>(cc * 32u), x0,
+                                 y0 + static_cast<int>(m * P.th), static_cast<int>(img));
+            tma_store_commit();
+            tma_store_wait_read();
         }
     }
     tc_fence_before();
@@ -392,6 +446,40 @@ __global__ void k_wait_probe(uint32_t *err) {
     __syncthreads();
 }
 
+int device_sms() {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+// M tiles per forward CTA. Two M tiles share each weight slice and each input box row between more
+// pixels (fewer bytes staged per pixel, fewer CTAs paying the fixed set-up and epilogue), as long as the
+// accumulators fit 256 TMEM columns and the layer still gives every SM several CTAs. Four (explicit
+// SPK_CONV_MTILES=4 only) leave too few CTAs per SM to hide each CTA's load latency: slower on GB300.
+uint32_t conv_mtiles(const ConvGeom &g, uint32_t tw, uint32_t th, uint32_t cout) {
+    const unsigned long long tiles_x = (g.w + tw - 1) / tw;
+    if (SPK_CONV_MTILES == 1 || SPK_CONV_MTILES == 2 || SPK_CONV_MTILES == 4)
+        return (SPK_CONV_MTILES * cout <= 256u) ? SPK_CONV_MTILES : 1u;
+    static const int sms = device_sms();
+    for (uint32_t mt = 2; mt > 1; mt /= 2) {
+        const unsigned long long ctas = tiles_x * ((g.h + mt * th - 1) / (mt * th)) * g.n;
+        if (mt * cout <= 256u && ctas >= 4ull * static_cast<unsigned long long>(sms)) return mt;
+    }
+    return 1;
+}
+
+OutSpec out_spec(const NhwcView &y, const ConvEpilogue &epi) {
+    OutSpec o{};
+    o.out = static_cast<__nv_bfloat16 *>(y.ptr);
+    o.out_ld = y.ld;
+    o.bias = epi.bias;
+    o.relu = epi.relu ? 1u : 0u;
+    o.mask = static_cast<const __nv_bfloat16 *>(epi.mask.ptr);
+    o.mask_ld = epi.mask.ld;
+    return o;
+}
+
 }  // namespace
 
 cudaError_t conv_wait_probe(uint32_t *err, cudaStream_t stream) {
@@ -413,12 +501,14 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
     // A operands start on 8-row swizzle atoms of the shared input box.
     const uint32_t tw = g.w >= 16u ? 16u : 8u;
     const uint32_t th = kTileM / tw;
+    const uint32_t mt = conv_mtiles(g, tw, th, cout);
+    const uint32_t rows = mt * th;
     CUtensorMap tmx, tmw;
     {
         const cuuint64_t dims[4] = {x.channels, g.w, g.h, g.n};
         const cuuint64_t strides[3] = {static_cast<cuuint64_t>(x.ld) * 2u, static_cast<cuuint64_t>(x.ld) * 2u * g.w,
                                        static_cast<cuuint64_t>(x.ld) * 2u * g.w * g.h};
-        const cuuint32_t box[4] = {32u, tw, th + 2u, 1u};
+        const cuuint32_t box[4] = {32u, tw, rows + 2u, 1u};
         const cuuint32_t es[4] = {1u, 1u, 1u, 1u};
         if (enc(&tmx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, x.ptr, dims, strides, box, es,
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -435,6 +525,18 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return cudaErrorInvalidValue;
     }
+    CUtensorMap tmy;
+    {
+        const cuuint64_t dims[4] = {cout, g.w, g.h, g.n};
+        const cuuint64_t strides[3] = {static_cast<cuuint64_t>(y.ld) * 2u, static_cast<cuuint64_t>(y.ld) * 2u * g.w,
+                                       static_cast<cuuint64_t>(y.ld) * 2u * g.w * g.h};
+        const cuuint32_t box[4] = {32u, tw, th, 1u};
+        const cuuint32_t es[4] = {1u, 1u, 1u, 1u};
+        if (enc(&tmy, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, y.ptr, dims, strides, box, es,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+    }
     FwdParams P{};
     P.n = g.n;
     P.h = g.h;
@@ -443,19 +545,17 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
     P.cout = cout;
     P.tw = tw;
     P.th = th;
+    P.mt = mt;
     P.tiles_x = (g.w + tw - 1) / tw;
-    P.tiles_y = (g.h + th - 1) / th;
-    P.a_bytes = fwd_a_bytes(tw, th);
-    P.stage_bytes = fwd_stage_bytes(tw, th, cout);
+    P.tiles_y = (g.h + rows - 1) / rows;
+    P.a_bytes = fwd_a_bytes(tw, rows);
+    P.stage_bytes = fwd_stage_bytes(tw, rows, cout);
     // Ring depth: up to 4 stages within the stage budget, never more than the K blocks of a tile (3 per 32
     // channels). A smaller ring leaves room for more CTAs per SM.
     P.stages = std::max(2u, std::min({kStages, 3u * (x.channels / 32u), (kStageBudget * 1024u) / P.stage_bytes}));
-    P.out = static_cast<__nv_bfloat16 *>(y.ptr);
-    P.out_ld = y.ld;
-    P.bias = epi.bias;
-    P.relu = epi.relu ? 1u : 0u;
-    P.mask = static_cast<const __nv_bfloat16 *>(epi.mask.ptr);
-    P.mask_ld = epi.mask.ld;
+    P.out_spec = out_spec(y, epi);
+    // The staged tile (mt x 128 pixels x cout BF16) must fit in the ring it reuses.
+    P.stage_out = (SPK_CONV_TMA_STORE && kTileM * 2u * mt * cout <= P.stages * P.stage_bytes) ? 1u : 0u;
     P.err = err;
     static std::once_flag attr;
     std::call_once(attr, [] {
@@ -463,8 +563,8 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
     });
     const unsigned long long tiles = static_cast<unsigned long long>(P.tiles_x) * P.tiles_y * g.n;
     if (tiles > 0x7FFFFFFFull) return cudaErrorInvalidValue;
-    const size_t smem = launch_smem(P.stages * P.stage_bytes + 1024 + 256, tmem_columns(cout));
-    k_conv_fwd<<<static_cast<unsigned>(tiles), 128, smem, stream>>>(tmx, tmw, P);
+    const size_t smem = launch_smem(P.stages * P.stage_bytes + 1024 + 256, tmem_columns(mt * cout));
+    k_conv_fwd<<<static_cast<unsigned>(tiles), 128, smem, stream>>>(tmx, tmw, tmy, P);
     return cudaGetLastError();
 }
 

@@ -103,6 +103,22 @@ __device__ __forceinline__ void tma_load_4d(void *dst, const void *tmap, uint64_
         : "memory");
 }
 
+// Tiled store shared -> global (bulk-group completion). Elements of the box outside the tensor are not
+// written. The source must stay unchanged until tma_store_wait_read() returns.
+__device__ __forceinline__ void tma_store_4d(const void *tmap, const void *src, int c0, int c1, int c2, int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5}], [%1];" ::"l"(tmap),
+        "r"(smem_u32(src)), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_store_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+
+// Waits until every committed bulk store of this thread has finished reading shared memory.
+__device__ __forceinline__ void tma_store_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
 __device__ __forceinline__ void tma_prefetch_desc(const void *tmap) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(tmap) : "memory");
 }

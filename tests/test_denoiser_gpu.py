@@ -52,9 +52,17 @@ CONV_SHAPES = [
     (1, 4, 4, 256, 32),
     (1, 12, 20, 128, 256),
 ]
+# Layers large enough that the forward kernel stacks 2 or 4 M tiles per CTA (32-64 output rows sharing one
+# input box per column tap and one set of weight slices), including ragged bottom tiles and 8-column tiles.
+LARGE_SHAPES = [
+    (1, 300, 520, 32, 64),   # 2 M tiles
+    (1, 1000, 520, 32, 64),  # 4 M tiles
+    (1, 600, 520, 64, 128),  # 2 M tiles at 128 output channels
+    (20, 1000, 12, 32, 32),  # 4 M tiles of 8 x 16 pixels
+]
 
 
-@pytest.mark.parametrize("shape", CONV_SHAPES)
+@pytest.mark.parametrize("shape", CONV_SHAPES + LARGE_SHAPES)
 def test_conv_forward(dn, shape):
     n, h, w, cin, cout = shape
     rng = np.random.default_rng(hash(shape) & 0xFFFF)
@@ -84,7 +92,7 @@ def test_conv_forward_channel_slices(dn):
     assert np.all(got[..., :32] == 7.0) and np.all(got[..., 96:] == 7.0)  # untouched channels
 
 
-@pytest.mark.parametrize("shape", CONV_SHAPES[:4])
+@pytest.mark.parametrize("shape", CONV_SHAPES[:4] + LARGE_SHAPES[1:3])
 def test_conv_dgrad_with_mask(dn, shape):
     n, h, w, cin, cout = shape
     rng = np.random.default_rng(11 + cin)

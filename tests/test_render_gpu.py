@@ -155,3 +155,27 @@ def test_full_hd_frame_is_consistent(ctx):
     assert np.array_equal(res[0][0].view(np.uint32), res[1][0].view(np.uint32))
     assert res[0][1] == res[1][1]
     assert res[0][1] >= W * H
+
+
+def test_full_hd_stress_rows_match_oracle(ctx):
+    """The benchmark workload itself (stress scene, 1920x1080, depth 8, xoshiro256**, seed 0) rendered for
+    4 frames in one call (the multi-frame wavefront schedule the benchmark times); the oracle renders
+    three bands of rows of the same frames (rows are independent without the spatial DenoisePass). Same
+    tolerances as the small scenes: >= 90% of pixels within 1e-4 relative, relMSE < 1e-3 per band."""
+    scene, cam_args = scenes.terrain_spheres(0)
+    W, H, frames = 1920, 1080, 4
+    camera = scenes.make_camera(cam_args, W, H)
+    cfg = abi.make_config(W, H, spp=1, bounce=8, rng=abi.SPK_RNG_XOSHIRO256SS, seed=0,
+                          kernel=abi.SPK_KERNEL_WAVEFRONT)
+    g_hdr, g_out, _ = gpu_render(ctx, scene, camera, cfg, frames)
+    osc = oracle.OracleScene(scene)
+    for r0, r1 in ((0, 6), (H // 2 - 4, H // 2 + 4), (H - 6, H)):
+        r = oracle.OracleRenderer(osc, cfg, camera)
+        r.render(frames, traversal=oracle.PRUNED, rows=(r0, r1))
+        o_hdr, _ = r.framebuffer()
+        frac = close_fraction(g_hdr[r0:r1], o_hdr[r0:r1])
+        rm = rel_mse(g_hdr[r0:r1], o_hdr[r0:r1])
+        print(f"rows {r0}-{r1}: close={frac:.4f} relmse={rm:.3e}")
+        assert frac >= 0.90
+        assert rm < 1e-3
+    assert np.all(g_out[..., 3] == 0x3C00)
