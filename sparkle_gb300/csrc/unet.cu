@@ -102,42 +102,61 @@ struct DBuf {
 // ------------------------------------------------------------------------------------------------
 __device__ __forceinline__ float bf(const bf16 v) { return __bfloat162float(v); }
 
-// features fp32 [n][h][w][10] -> X0 bf16 [n][hp][wp][32], edge replication into the padding.
+// features fp32 [n][h][w][10] -> X0 bf16 [n][hp][wp][32], edge replication into the padding. One thread
+// per (pixel, 8-channel group), so a warp writes 512 contiguous bytes.
 __global__ void k_input(const float *feat, bf16 *x0, uint32_t n, uint32_t h, uint32_t w, uint32_t hp, uint32_t wp) {
-    const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    const size_t total = static_cast<size_t>(n) * hp * wp;
+    const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;  // (pixel, channel group)
+    const size_t total = static_cast<size_t>(n) * hp * wp * (kInPad / 8u);
     if (i >= total) return;
-    const uint32_t x = static_cast<uint32_t>(i % wp), y = static_cast<uint32_t>((i / wp) % hp);
-    const uint32_t img = static_cast<uint32_t>(i / (static_cast<size_t>(wp) * hp));
+    const uint32_t grp = static_cast<uint32_t>(i % (kInPad / 8u));
+    const size_t q = i / (kInPad / 8u);
+    const uint32_t x = static_cast<uint32_t>(q % wp), y = static_cast<uint32_t>((q / wp) % hp);
+    const uint32_t img = static_cast<uint32_t>(q / (static_cast<size_t>(wp) * hp));
     const uint32_t sx = min(x, w - 1), sy = min(y, h - 1);
     const float *f = feat + ((static_cast<size_t>(img) * h + sy) * w + sx) * SPK_DN_FEATURES;
-    bf16 *o = x0 + i * kInPad;
-    for (uint32_t c = 0; c < kInPad; c += 2) {
+    uint32_t pk[4];
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k) {
+        const uint32_t c = grp * 8u + 2u * k;
         const float a = c < SPK_DN_FEATURES ? f[c] : 0.f, b = c + 1 < SPK_DN_FEATURES ? f[c + 1] : 0.f;
-        *reinterpret_cast<__nv_bfloat162 *>(o + c) = __floats2bfloat162_rn(a, b);
+        const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+        pk[k] = *reinterpret_cast<const uint32_t *>(&v);
     }
+    *reinterpret_cast<uint4 *>(x0 + q * kInPad + grp * 8u) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
 }
 
-// 2x2 average pooling: src view [n][2h][2w] (ld_s) -> dst [n][h][w][c] (dense).
+// 2x2 average pooling: src view [n][2h][2w] (ld_s) -> dst [n][h][w][c] (dense). One thread per (pixel,
+// 8-channel group): four 16-byte loads, one 16-byte store; per channel the sum runs in (dy, dx) order.
 __global__ void k_pool(const bf16 *src, uint32_t ld_s, bf16 *dst, uint32_t n, uint32_t h, uint32_t w, uint32_t c) {
-    const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;  // (pixel, channel pair)
-    const uint32_t cp = c / 2;
-    const size_t total = static_cast<size_t>(n) * h * w * cp;
+    const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;  // (pixel, channel group)
+    const uint32_t cg = c / 8;
+    const size_t total = static_cast<size_t>(n) * h * w * cg;
     if (i >= total) return;
-    const uint32_t ch = static_cast<uint32_t>(i % cp) * 2;
-    const size_t q = i / cp;
+    const uint32_t ch = static_cast<uint32_t>(i % cg) * 8;
+    const size_t q = i / cg;
     const uint32_t x = static_cast<uint32_t>(q % w), y = static_cast<uint32_t>((q / w) % h);
     const uint32_t img = static_cast<uint32_t>(q / (static_cast<size_t>(w) * h));
     const uint32_t W2 = 2 * w;
-    float a = 0.f, b = 0.f;
+    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (uint32_t dy = 0; dy < 2; ++dy)
         for (uint32_t dx = 0; dx < 2; ++dx) {
             const size_t p = (static_cast<size_t>(img) * 2 * h + 2 * y + dy) * W2 + 2 * x + dx;
-            const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162 *>(src + p * ld_s + ch);
-            a += __low2float(v);
-            b += __high2float(v);
+            const uint4 raw = *reinterpret_cast<const uint4 *>(src + p * ld_s + ch);
+            const uint32_t wv[4] = {raw.x, raw.y, raw.z, raw.w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162 *>(&wv[k]);
+                acc[2 * k] += __low2float(v);
+                acc[2 * k + 1] += __high2float(v);
+            }
         }
-    *reinterpret_cast<__nv_bfloat162 *>(dst + q * c + ch) = __floats2bfloat162_rn(0.25f * a, 0.25f * b);
+    uint32_t pk[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const __nv_bfloat162 v = __floats2bfloat162_rn(0.25f * acc[2 * k], 0.25f * acc[2 * k + 1]);
+        pk[k] = *reinterpret_cast<const uint32_t *>(&v);
+    }
+    *reinterpret_cast<uint4 *>(dst + q * c + ch) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
 }
 
 // Nearest 2x upsampling: src [n][h][w][c] (dense) -> dst view [n][2h][2w] (ld_d, first c channels).
@@ -537,7 +556,7 @@ cudaError_t forward(spk_denoiser *dn, const float *feat, uint32_t n, uint32_t h,
                     uint32_t wp) {
     cudaError_t e;
     const size_t p0 = static_cast<size_t>(n) * hp * wp;
-    k_input<<<blocks_for(p0, 256), 256, 0, dn->stream>>>(feat, dn->x0.p, n, h, w, hp, wp);
+    k_input<<<blocks_for(p0 * (kInPad / 8u), 256), 256, 0, dn->stream>>>(feat, dn->x0.p, n, h, w, hp, wp);
     auto G = [&](uint32_t l) { return ConvGeom{n, hp >> l, wp >> l}; };
     NhwcView in = dense(dn->x0.p, kInPad);
     for (uint32_t l = 0; l < kLevels; ++l) {
@@ -546,7 +565,7 @@ cudaError_t forward(spk_denoiser *dn, const float *feat, uint32_t n, uint32_t h,
         if ((e = conv_fwd(dn, enc_b(l), dense(dn->ea[l].p, kW[l]), eo, G(l))) != cudaSuccess) return e;
         if (l < 4) {
             const ConvGeom c = G(l + 1);
-            const size_t work = static_cast<size_t>(n) * c.h * c.w * (kW[l] / 2);
+            const size_t work = static_cast<size_t>(n) * c.h * c.w * (kW[l] / 8);
             k_pool<<<blocks_for(work, 256), 256, 0, dn->stream>>>(static_cast<const bf16 *>(eo.ptr), eo.ld,
                                                                    dn->pool[l].p, n, c.h, c.w, kW[l]);
             in = dense(dn->pool[l].p, kW[l]);
