@@ -308,11 +308,16 @@ def run_ours(args):
         osc = oracle.OracleScene(scene)
         v_f, n_f, dt_f = cpu_sample(osc, camera, 16, 270, threads, oracle.FAITHFUL)
         v_p, n_p, dt_p = cpu_sample(osc, camera, 16, 270, threads, oracle.PRUNED)
+        # the reference's own pool size: min(max_threads = 64, hardware threads) minus the main and render
+        # threads it reserves (TaskDispatcher.cpp:18-20, AppFramework.cpp:129-130)
+        ref_workers = max(1, min(64, threads) - 2)
+        v_w, _, _ = cpu_sample(osc, camera, 16, 270, ref_workers, oracle.FAITHFUL)
         cpu = {"value": round(v_f, 4), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"16 frames x 270 central rows x {WIDTH} px of the same scene/config, oracle restatement of "
                          f"the reference cpu path tracer, faithful traversal (no tmax shrink): {n_f} rays in "
                          f"{dt_f:.2f} s; pruned traversal: {v_p:.3f} Mrays/s",
-               "pruned_value": round(v_p, 4)}
+               "pruned_value": round(v_p, 4),
+               "reference_workers": {"threads": ref_workers, "value": round(v_w, 4)}}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(elapsed_s * 1000.0 / args.steps, 3), "higher_is_better": True,
