@@ -254,6 +254,45 @@ int host_threads() {
     return n == 0 ? 1 : static_cast<int>(std::min(n, 64u));
 }
 
+// Host loops over large meshes run in chunks on up to host_threads() threads. Every chunk writes a disjoint
+// range (or its own partial result), so the output never depends on the thread count.
+struct ChunkPlan {
+    uint64_t n = 0, step = 0, chunks = 0;
+};
+
+ChunkPlan plan_chunks(uint64_t n) {
+    constexpr uint64_t kMinChunk = 1u << 16;
+    ChunkPlan p;
+    p.n = n;
+    p.chunks = std::max<uint64_t>(1, std::min<uint64_t>(static_cast<uint64_t>(host_threads()), (n + kMinChunk - 1) / kMinChunk));
+    p.step = (n + p.chunks - 1) / p.chunks;
+    return p;
+}
+
+// Runs fn(chunk, begin, end) over the chunks of `p`; a thread that cannot be started runs inline.
+template <class F>
+void run_chunks(const ChunkPlan &p, F &&fn) {
+    if (p.n == 0) return;
+    std::vector<std::thread> pool;
+    pool.reserve(p.chunks);
+    for (uint64_t c = 1; c < p.chunks; ++c) {
+        const uint64_t lo = c * p.step, hi = std::min(p.n, lo + p.step);
+        if (lo >= hi) continue;
+        try {
+            pool.emplace_back([&fn, c, lo, hi] { fn(c, lo, hi); });
+        } catch (const std::exception &) {
+            fn(c, lo, hi);
+        }
+    }
+    fn(uint64_t{0}, uint64_t{0}, std::min(p.n, p.step));
+    for (std::thread &t : pool) t.join();
+}
+
+template <class F>
+void parallel_for(uint64_t n, F &&fn) {
+    run_chunks(plan_chunks(n), [&fn](uint64_t, uint64_t lo, uint64_t hi) { fn(lo, hi); });
+}
+
 // Outward-rounded world box of a transformed local box (8 corners, evaluated in double).
 BuildBox world_box(const float *m, const double lo[3], const double hi[3]) {
     BuildBox b;
@@ -494,10 +533,20 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
         const spk_mesh &m = meshes[k];
         if (m.num_faces && (!m.positions || !m.normals || !m.indices))
             return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "mesh %u: positions, normals and indices are required", k);
-        for (uint64_t f = 0; f < 3ull * m.num_faces; ++f) {
-            if (m.indices[f] >= m.num_vertices)
-                return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "mesh %u: index %u out of range", k, m.indices[f]);
-        }
+        const uint64_t ni = m.indices ? 3ull * m.num_faces : 0;
+        std::atomic<uint64_t> first_bad{ni};
+        parallel_for(ni, [&](uint64_t lo, uint64_t hi) {
+            for (uint64_t f = lo; f < hi; ++f) {
+                if (m.indices[f] >= m.num_vertices) {
+                    uint64_t cur = first_bad.load();
+                    while (f < cur && !first_bad.compare_exchange_weak(cur, f)) {
+                    }
+                    break;
+                }
+            }
+        });
+        if (first_bad.load() < ni)
+            return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "mesh %u: index %u out of range", k, m.indices[first_bad.load()]);
     }
     for (uint32_t k = 0; k < num_instances; ++k) {
         const spk_instance &in = instances[k];
@@ -522,32 +571,51 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
                     return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "material %u: texture index %d out of range", k, i);
         }
     }
+    static_assert(sizeof(float4) == 4 * sizeof(float), "texel layout");
     for (uint32_t k = 0; k < num_textures; ++k) {
         const spk_texture &t = textures[k];
-        hs.textures.push_back(DevTexture{static_cast<uint32_t>(hs.texels.size()), t.width, t.height, t.srgb ? 1u : 0u});
+        const size_t base = hs.texels.size();
+        hs.textures.push_back(DevTexture{static_cast<uint32_t>(base), t.width, t.height, t.srgb ? 1u : 0u});
         const size_t nt = static_cast<size_t>(t.width) * t.height;
-        for (size_t i = 0; i < nt; ++i)
-            hs.texels.push_back(make_float4(t.rgba[4 * i], t.rgba[4 * i + 1], t.rgba[4 * i + 2], t.rgba[4 * i + 3]));
+        hs.texels.resize(base + nt);
+        std::memcpy(hs.texels.data() + base, t.rgba, nt * sizeof(float4));
     }
 
     // BLAS per mesh: binned SAH BVH2 (<= 3 triangles per leaf) collapsed to 8-wide nodes.
     hs.blas.assign(num_meshes, MeshBlas{});
+    size_t total_verts = 0, total_faces = 0;
+    for (uint32_t k = 0; k < num_meshes; ++k) {
+        total_verts += meshes[k].num_vertices;
+        total_faces += meshes[k].num_faces;
+    }
+    hs.verts.resize(3 * total_verts);
+    hs.faces.resize(total_faces);
+    size_t vert_base = 0, face_base = 0;
     for (uint32_t k = 0; k < num_meshes; ++k) {
         const spk_mesh &m = meshes[k];
         MeshBlas &mbl = hs.blas[k];
-        mbl.vert_base = static_cast<uint32_t>(hs.verts.size() / 3);
-        mbl.face_base = static_cast<uint32_t>(hs.faces.size());
-        for (uint32_t v = 0; v < m.num_vertices; ++v) {
-            const float *n = m.normals + 3 * v;
-            const float t[4] = {m.tangents ? m.tangents[4 * v] : 1.f, m.tangents ? m.tangents[4 * v + 1] : 0.f,
-                                m.tangents ? m.tangents[4 * v + 2] : 0.f, m.tangents ? m.tangents[4 * v + 3] : 1.f};
-            const float uv[2] = {m.uvs ? m.uvs[2 * v] : 0.f, m.uvs ? m.uvs[2 * v + 1] : 0.f};
-            hs.verts.push_back(make_float4(n[0], n[1], n[2], t[0]));
-            hs.verts.push_back(make_float4(t[1], t[2], t[3], uv[0]));
-            hs.verts.push_back(make_float4(uv[1], 0.f, 0.f, 0.f));
-        }
-        for (uint32_t f = 0; f < m.num_faces; ++f)
-            hs.faces.push_back(make_uint4(m.indices[3 * f], m.indices[3 * f + 1], m.indices[3 * f + 2], 0u));
+        mbl.vert_base = static_cast<uint32_t>(vert_base);
+        mbl.face_base = static_cast<uint32_t>(face_base);
+        float4 *vrec = hs.verts.data() + 3 * vert_base;
+        uint4 *frec = hs.faces.data() + face_base;
+        parallel_for(m.num_vertices, [&](uint64_t lo, uint64_t hi) {
+            static const float kNoNormal[3] = {0.f, 0.f, 0.f};  // face-less meshes may come without normals
+            for (uint64_t v = lo; v < hi; ++v) {
+                const float *n = m.normals ? m.normals + 3 * v : kNoNormal;
+                const float t[4] = {m.tangents ? m.tangents[4 * v] : 1.f, m.tangents ? m.tangents[4 * v + 1] : 0.f,
+                                    m.tangents ? m.tangents[4 * v + 2] : 0.f, m.tangents ? m.tangents[4 * v + 3] : 1.f};
+                const float uv[2] = {m.uvs ? m.uvs[2 * v] : 0.f, m.uvs ? m.uvs[2 * v + 1] : 0.f};
+                vrec[3 * v] = make_float4(n[0], n[1], n[2], t[0]);
+                vrec[3 * v + 1] = make_float4(t[1], t[2], t[3], uv[0]);
+                vrec[3 * v + 2] = make_float4(uv[1], 0.f, 0.f, 0.f);
+            }
+        });
+        parallel_for(m.num_faces, [&](uint64_t lo, uint64_t hi) {
+            for (uint64_t f = lo; f < hi; ++f)
+                frec[f] = make_uint4(m.indices[3 * f], m.indices[3 * f + 1], m.indices[3 * f + 2], 0u);
+        });
+        vert_base += m.num_vertices;
+        face_base += m.num_faces;
         double *mb = mbl.bounds;
         for (int a = 0; a < 3; ++a) {
             mb[a] = std::numeric_limits<double>::max();
@@ -556,22 +624,40 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
         if (m.num_faces == 0) continue;
         const bool device_build = ctx->tuning.bvh_builder != 0;
         std::vector<BuildBox> boxes(device_build ? 0 : m.num_faces);
-        for (uint32_t f = 0; f < m.num_faces; ++f) {
-            BuildBox b;
+        // Face boxes (host build) and the mesh bounds, per chunk; min / max are exact, so combining the
+        // chunks' bounds gives the same bounds in any order.
+        const ChunkPlan plan = plan_chunks(m.num_faces);
+        std::vector<std::array<double, 6>> part(plan.chunks);
+        run_chunks(plan, [&](uint64_t c, uint64_t lo, uint64_t hi) {
+            std::array<double, 6> pb;
             for (int a = 0; a < 3; ++a) {
-                b.lo[a] = std::numeric_limits<float>::max();
-                b.hi[a] = -std::numeric_limits<float>::max();
+                pb[a] = std::numeric_limits<double>::max();
+                pb[3 + a] = -std::numeric_limits<double>::max();
             }
-            for (int c = 0; c < 3; ++c) {
-                const float *p = m.positions + 3 * m.indices[3 * f + c];
+            for (uint64_t f = lo; f < hi; ++f) {
+                BuildBox b;
                 for (int a = 0; a < 3; ++a) {
-                    b.lo[a] = std::min(b.lo[a], p[a]);
-                    b.hi[a] = std::max(b.hi[a], p[a]);
-                    mb[a] = std::min(mb[a], static_cast<double>(p[a]));
-                    mb[3 + a] = std::max(mb[3 + a], static_cast<double>(p[a]));
+                    b.lo[a] = std::numeric_limits<float>::max();
+                    b.hi[a] = -std::numeric_limits<float>::max();
                 }
+                for (int cc = 0; cc < 3; ++cc) {
+                    const float *p = m.positions + 3 * m.indices[3 * f + cc];
+                    for (int a = 0; a < 3; ++a) {
+                        b.lo[a] = std::min(b.lo[a], p[a]);
+                        b.hi[a] = std::max(b.hi[a], p[a]);
+                        pb[a] = std::min(pb[a], static_cast<double>(p[a]));
+                        pb[3 + a] = std::max(pb[3 + a], static_cast<double>(p[a]));
+                    }
+                }
+                if (!device_build) boxes[f] = b;
             }
-            if (!device_build) boxes[f] = b;
+            part[c] = pb;
+        });
+        for (const std::array<double, 6> &pb : part) {
+            for (int a = 0; a < 3; ++a) {
+                mb[a] = std::min(mb[a], pb[a]);
+                mb[3 + a] = std::max(mb[3 + a], pb[3 + a]);
+            }
         }
         WideBvh wide;
         const uint32_t knobs[4] = {ctx->tuning.bvh_width, ctx->tuning.bvh_leaf_size, ctx->tuning.bvh_collapse,
@@ -603,20 +689,26 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
         mbl.tri_first = tri_offset;
         mbl.tri_count = static_cast<uint32_t>(wide.items.size());
         append_wide(hs.nodes, wide, tri_offset);
-        for (uint32_t face : wide.items) {
-            const float *p0 = m.positions + 3 * m.indices[3 * face];
-            const float *p1 = m.positions + 3 * m.indices[3 * face + 1];
-            const float *p2 = m.positions + 3 * m.indices[3 * face + 2];
-            // BLAS::Triangle::Set: e1 = v1 - v0, e2 = v2 - v0 (MeshRenderProxy.cpp:80-86)
-            const float e1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
-            const float e2[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
-            uint32_t fbits = face;
-            float ff;
-            std::memcpy(&ff, &fbits, 4);
-            hs.tris.push_back(make_float4(p0[0], p0[1], p0[2], e1[0]));
-            hs.tris.push_back(make_float4(e1[1], e1[2], e2[0], e2[1]));
-            hs.tris.push_back(make_float4(e2[2], ff, 0.f, 0.f));
-        }
+        const size_t t0 = hs.tris.size();
+        hs.tris.resize(t0 + 3 * wide.items.size());
+        float4 *trec = hs.tris.data() + t0;
+        parallel_for(wide.items.size(), [&](uint64_t lo, uint64_t hi) {
+            for (uint64_t i = lo; i < hi; ++i) {
+                const uint32_t face = wide.items[i];
+                const float *p0 = m.positions + 3 * m.indices[3 * face];
+                const float *p1 = m.positions + 3 * m.indices[3 * face + 1];
+                const float *p2 = m.positions + 3 * m.indices[3 * face + 2];
+                // BLAS::Triangle::Set: e1 = v1 - v0, e2 = v2 - v0 (MeshRenderProxy.cpp:80-86)
+                const float e1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+                const float e2[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+                uint32_t fbits = face;
+                float ff;
+                std::memcpy(&ff, &fbits, 4);
+                trec[3 * i] = make_float4(p0[0], p0[1], p0[2], e1[0]);
+                trec[3 * i + 1] = make_float4(e1[1], e1[2], e2[0], e2[1]);
+                trec[3 * i + 2] = make_float4(e2[2], ff, 0.f, 0.f);
+            }
+        });
     }
     hs.mats = build_materials(materials, num_materials, maps);
     // Instances + TLAS over their world boxes (TLAS::Build, SceneRenderProxy.cpp:31-69).
@@ -979,8 +1071,16 @@ spk_status spk_set_scenes(spk_ctx *ctx, const spk_scene_desc *scenes, uint32_t n
             dy.indices.resize(d.num_meshes);
             for (uint32_t m = 0; m < d.num_meshes; ++m) {
                 const spk_mesh &mesh = d.meshes[m];
-                dy.positions[m].assign(mesh.positions, mesh.positions + (mesh.positions ? 3ull * mesh.num_vertices : 0));
-                dy.indices[m].assign(mesh.indices, mesh.indices + (mesh.indices ? 3ull * mesh.num_faces : 0));
+                const size_t np = mesh.positions ? 3ull * mesh.num_vertices : 0;
+                const size_t nx = mesh.indices ? 3ull * mesh.num_faces : 0;
+                dy.positions[m].resize(np);
+                dy.indices[m].resize(nx);
+                parallel_for(np, [&](uint64_t lo, uint64_t hi) {
+                    std::memcpy(dy.positions[m].data() + lo, mesh.positions + lo, (hi - lo) * sizeof(float));
+                });
+                parallel_for(nx, [&](uint64_t lo, uint64_t hi) {
+                    std::memcpy(dy.indices[m].data() + lo, mesh.indices + lo, (hi - lo) * sizeof(uint32_t));
+                });
             }
             dy.blas = std::move(hs.blas);
             dy.mats = std::move(hs.mats);
