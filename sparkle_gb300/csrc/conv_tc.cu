@@ -425,8 +425,9 @@ constexpr int kMaxDynSmem = 227 * 1024;
 
 // Dynamic shared memory of a launch: what the kernel uses, raised so that the CTAs resident on one SM
 // never ask for more than the SM's 512 TMEM columns (an allocation beyond that would wait for another
-// CTA to finish).
+// CTA to finish). 0 when the kernel would use more than a CTA may have: the caller refuses the launch.
 size_t launch_smem(size_t used, uint32_t tmem_cols) {
+    if (used > static_cast<size_t>(kMaxDynSmem)) return 0;
     const size_t per_sm = 228u * 1024u;
     const size_t ctas = 512u / tmem_cols;
     const size_t floor_bytes = per_sm / (ctas + 1u) - 1024u + 1u;  // the SM reserves 1 KB per CTA: ctas + 1 do not fit
@@ -564,6 +565,7 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
     const unsigned long long tiles = static_cast<unsigned long long>(P.tiles_x) * P.tiles_y * g.n;
     if (tiles > 0x7FFFFFFFull) return cudaErrorInvalidValue;
     const size_t smem = launch_smem(P.stages * P.stage_bytes + 1024 + 256, tmem_columns(mt * cout));
+    if (smem == 0) return cudaErrorInvalidConfiguration;
     k_conv_fwd<<<static_cast<unsigned>(tiles), 128, smem, stream>>>(tmx, tmw, tmy, P);
     return cudaGetLastError();
 }
@@ -598,6 +600,7 @@ cudaError_t conv3x3_wgrad(const NhwcView &x, const NhwcView &dy, float *dw, cons
     P.kblocks = static_cast<uint32_t>((kblocks_total + splits - 1) / splits);
     splits = (kblocks_total + P.kblocks - 1) / P.kblocks;
     const size_t smem = launch_smem(kWgStages * wg_stage_bytes(P.cout) + 1024 + 256, tmem_columns(P.cout));
+    if (smem == 0) return cudaErrorInvalidConfiguration;
     static std::once_flag attr;
     std::call_once(attr, [] {
         cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
