@@ -118,7 +118,16 @@ __device__ __forceinline__ float srgb_decode(float c) {  // utilities::SRGBtoLin
     return c < 0.04045f ? c / 12.92f : powf((c + 0.055f) / 1.055f, 2.4f);
 }
 
+// One out-of-line copy: a material samples up to four textures (each with three sRGB powf), and inlining
+// every call site would grow the shading kernels' code for scenes that have no textures at all.
+#ifndef SPK_TEX_NOINLINE
+#define SPK_TEX_NOINLINE 1
+#endif
+#if SPK_TEX_NOINLINE
+__device__ __noinline__ f3 tex_sample(const DevScene &S, uint32_t t, const float uv[2]) {
+#else
 __device__ __forceinline__ f3 tex_sample(const DevScene &S, uint32_t t, const float uv[2]) {
+#endif
     const DevTexture T = S.textures[t];
     const float px = uv[0] * static_cast<float>(T.width), py = uv[1] * static_cast<float>(T.height);
     const int ui = static_cast<int>(px), vi = static_cast<int>(py);
