@@ -124,7 +124,7 @@ __device__ __forceinline__ float srgb_decode(float c) {  // utilities::SRGBtoLin
 #define SPK_TEX_NOINLINE 1
 #endif
 #if SPK_TEX_NOINLINE
-__device__ __noinline__ f3 tex_sample(const DevScene &S, uint32_t t, const float uv[2]) {
+static __device__ __noinline__ f3 tex_sample(const DevScene &S, uint32_t t, const float uv[2]) {
 #else
 __device__ __forceinline__ f3 tex_sample(const DevScene &S, uint32_t t, const float uv[2]) {
 #endif
