@@ -116,7 +116,13 @@ __device__ __forceinline__ void epilogue_pack(const OutSpec &O, const uint32_t (
     for (int e = 0; e < 8; ++e) pk[e] = pack_bf16(f[2 * e], f[2 * e + 1]);
 }
 
-__global__ void __launch_bounds__(128, 1)
+#ifndef SPK_CONV_EPI_WARPS
+#define SPK_CONV_EPI_WARPS 8  // warps per forward CTA (4 or 8); all of them drain TMEM in the epilogue
+#endif
+constexpr uint32_t kFwdThreads = 32u * SPK_CONV_EPI_WARPS;
+static_assert(SPK_CONV_EPI_WARPS == 4 || SPK_CONV_EPI_WARPS == 8, "4 or 8 warps");
+
+__global__ void __launch_bounds__(kFwdThreads, 1)
     k_conv_fwd(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw,
                const __grid_constant__ CUtensorMap tmy, FwdParams P) {
     extern __shared__ uint8_t smem_raw[];
@@ -203,16 +209,23 @@ __global__ void __launch_bounds__(128, 1)
     // per M tile and 32-channel chunk a 128-row x 64-byte region in the 64-byte-swizzled layout (rows =
     // pixels of the M tile in box order), written by a 4-D TMA store that writes whole lines and drops the
     // pixels outside the image. Otherwise each thread stores its pixel's channels itself.
-    const uint32_t r = warp * 32u + lane;
+    // Warp w reads TMEM lane group w % 4 (the lanes it may access). With 8 warps the second four take the
+    // odd M tiles, or (one M tile) the upper half of the output channels.
+    const uint32_t lgrp = warp & 3u, part = warp >> 2, nparts = SPK_CONV_EPI_WARPS / 4u;
+    const uint32_t r = lgrp * 32u + lane;
     const uint32_t chunks = P.cout / 32u;
-    for (uint32_t m = 0; ready && m < P.mt; ++m) {
+    const uint32_t m_step = P.mt >= nparts ? nparts : 1u;
+    const uint32_t m_first = P.mt >= nparts ? part : 0u;
+    const uint32_t j_count = P.mt >= nparts ? P.cout / 16u : P.cout / 16u / nparts;
+    const uint32_t j_first = P.mt >= nparts ? 0u : part * j_count;
+    for (uint32_t m = m_first; ready && m < P.mt; m += m_step) {
         const uint32_t px = static_cast<uint32_t>(x0) + (r % P.tw);
         const uint32_t py = static_cast<uint32_t>(y0) + m * P.th + (r / P.tw);
         const bool inb = px < P.w && py < P.h;
         const size_t pix = (static_cast<size_t>(img) * P.h + py) * P.w + px;
-        for (uint32_t j = 0; j < P.cout / 16u; ++j) {
+        for (uint32_t j = j_first; j < j_first + j_count; ++j) {
             uint32_t v[16], pk[8];
-            tmem_ld16(tmem + ((warp * 32u) << 16) + m * P.cout + j * 16u, v);
+            tmem_ld16(tmem + ((lgrp * 32u) << 16) + m * P.cout + j * 16u, v);
             epilogue_pack(P.out_spec, v, P.out_spec.bias ? P.out_spec.bias + j * 16u : nullptr, pix, j * 16u, inb,
                           pk);
             if (P.stage_out) {
@@ -566,7 +579,7 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
     if (tiles > 0x7FFFFFFFull) return cudaErrorInvalidValue;
     const size_t smem = launch_smem(P.stages * P.stage_bytes + 1024 + 256, tmem_columns(mt * cout));
     if (smem == 0) return cudaErrorInvalidConfiguration;
-    k_conv_fwd<<<static_cast<unsigned>(tiles), 128, smem, stream>>>(tmx, tmw, tmy, P);
+    k_conv_fwd<<<static_cast<unsigned>(tiles), kFwdThreads, smem, stream>>>(tmx, tmw, tmy, P);
     return cudaGetLastError();
 }
 
