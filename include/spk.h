@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define SPK_ABI_VERSION 1u
+#define SPK_ABI_VERSION 2u
 
 typedef int32_t spk_status;
 enum {
@@ -212,6 +212,10 @@ typedef struct spk_tuning {
     uint32_t bvh_builder;          /* BLAS builder: 0 host binned SAH (default), 1 device LBVH (Karras radix tree over
                                       Morton order), 2 device PLOC clustering over Morton order; 1 and 2 use the greedy
                                       collapse (bvh_collapse ignored) and take milliseconds where the host takes seconds */
+    uint32_t path_slots_per_pixel; /* multi-frame schedule: paths in flight per pixel, 1..64 (default 64: every sample
+                                      of a 64-frame call at once, at most 2^27 paths, ~152 B of state each). More paths
+                                      per extend launch spread each launch's tail (its last, longest walks) over more
+                                      rays; spk_render(1) uses one path per pixel whatever the setting */
 } spk_tuning;
 
 /* ------------------------------------------------------------------------------------------------ */

@@ -16,6 +16,7 @@ import time
 
 SPACE = {
     "batch_slots": [1 << 19, 1 << 20, 1 << 21, 1 << 22],
+    "path_slots_per_pixel": [64, 16, 4, 1],
     "shade_blocks_per_sm": [4, 8, 16],
     "extend_blocks_per_sm": [0, 6],
     "material_sort": [0, 1],

@@ -1321,7 +1321,7 @@ spk_status spk_set_config(spk_ctx *ctx, const spk_config *config) try {
         (e = cudaMemsetAsync(ctx->fb.ptr, 0, n * sizeof(float4), ctx->stream)) != cudaSuccess) {
         return cuda_fail(ctx, e, "frame buffer clear");
     }
-    if ((e = wavefront_alloc(ctx->wf, static_cast<uint32_t>(n))) != cudaSuccess) {
+    if (ctx->wf.capacity < n && (e = wavefront_alloc(ctx->wf, static_cast<uint32_t>(n))) != cudaSuccess) {
         ctx->has_config = false;
         return cuda_fail(ctx, e, "path state allocation");
     }
@@ -1344,6 +1344,7 @@ static WfTuning wf_tuning(const spk_ctx *ctx) {
     t.shade_blocks_per_sm = ctx->tuning.shade_blocks_per_sm;
     t.material_sort = ctx->tuning.material_sort != 0;
     t.ray_sort = ctx->tuning.ray_sort != 0;
+    t.slots_per_pixel = ctx->tuning.path_slots_per_pixel;
     return t;
 }
 
@@ -1390,6 +1391,13 @@ static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
         uint32_t launches = 0;
         ctx->chunk_graph.enabled = ctx->tuning.cuda_graph != 0;
         const uint32_t replays0 = ctx->chunk_graph.replays;
+        // Path slots for the multi-frame schedule: pixels x path_slots_per_pixel, no more than the frames of
+        // one pass can use and at most kMaxPathSlots (about 20 GB of path state); grown on demand and kept.
+        const uint64_t npix = static_cast<uint64_t>(ctx->cfg.width) * ctx->cfg.height;
+        const uint64_t per_pixel = std::min<uint64_t>({ctx->tuning.path_slots_per_pixel, num_frames, kFramesPerPass});
+        const uint64_t slots = std::max<uint64_t>(npix, std::min<uint64_t>(npix * per_pixel, kMaxPathSlots));
+        if (ctx->wf.capacity < slots && (e = wavefront_alloc(ctx->wf, static_cast<uint32_t>(slots))) != cudaSuccess)
+            return cuda_fail(ctx, e, "path state allocation");
         e = launch_render_multiframe(ctx->scene, ctx->cam, fbuf, p, num_frames, ctx->frame_weights.data(),
                                      ctx->frame_seeds.data(), count, ctx->counters, ctx->wf, ctx->num_sms,
                                      ctx->stream, &launches, &ctx->launch_events, wf_tuning(ctx), &ctx->chunk_graph);
@@ -2091,6 +2099,7 @@ void spk_tuning_defaults(spk_tuning *out) {
     out->shade_blocks_per_sm = 8;
     out->bvh_collapse = 0;
     out->bvh_builder = 0;
+    out->path_slots_per_pixel = 64;
 }
 
 spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
@@ -2105,6 +2114,8 @@ spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
     if (t->ray_sort > 1 || t->bvh_collapse > 1)
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "ray_sort and bvh_collapse take 0 or 1");
     if (t->bvh_builder > 2) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "bvh_builder takes 0, 1 or 2");
+    if (t->path_slots_per_pixel < 1 || t->path_slots_per_pixel > 64)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "path_slots_per_pixel must be 1..64");
     ctx->tuning = *t;
     return SPK_OK;
 }

@@ -246,17 +246,18 @@ __device__ __forceinline__ void start_item(const DevCamera &cam, const RenderPar
     s.slot_state[slot] = 0u;
 }
 
+// Starts the first `initial` sample items of the pass, item i in slot i.
 template <int kKind>
 __global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers fb, RenderParams p,
-                                                     WavefrontState s, uint32_t frame_base, Counters *counters) {
+                                                     WavefrontState s, uint32_t frame_base, uint32_t initial,
+                                                     Counters *counters) {
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t npix = fb.width * fb.height;
-    if (slot >= npix) return;
+    if (slot >= initial) return;
     start_item<kKind>(cam, p, s, slot, slot, fb.width, fb.height, frame_base);
     s.queue[0][slot] = slot;
     if (slot == 0) {
-        counters->queue_counters[kLen0] = npix;
-        counters->queue_counters[kNextItem] = npix;
+        counters->queue_counters[kLen0] = initial;
+        counters->queue_counters[kNextItem] = initial;
     }
 }
 
@@ -791,11 +792,15 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
     for (uint32_t f0 = 0; f0 < num_frames; f0 += kFramesPerPass) {
         const uint32_t frames = std::min(kFramesPerPass, num_frames - f0);
         const uint32_t total_items = frames * npix;
+        // Paths in flight: slots_per_pixel x pixels, within the state's capacity and the pass's items.
+        const uint64_t want = static_cast<uint64_t>(npix) * std::max(1u, tuning.slots_per_pixel);
+        const uint32_t initial = static_cast<uint32_t>(
+            std::min<uint64_t>({want, static_cast<uint64_t>(s.capacity), static_cast<uint64_t>(total_items)}));
         if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
         if (p.rng == 0) {
-            k_mf_generate<0><<<(npix + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, counters);
+            k_mf_generate<0><<<(initial + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, initial, counters);
         } else {
-            k_mf_generate<1><<<(npix + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, counters);
+            k_mf_generate<1><<<(initial + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, initial, counters);
         }
         ++nl;
         // One chunk: kChunk iterations of (reset the output queue, extend, shade).

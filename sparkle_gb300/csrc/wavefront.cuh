@@ -48,6 +48,9 @@ constexpr uint32_t kRaySortBuckets = 4096;
 
 // Frames per multi-frame pass: bounds the per-sample result buffer to kFramesPerPass * pixels * 16 B.
 constexpr uint32_t kFramesPerPass = 64;
+// Most path slots a multi-frame schedule allocates (2^27 slots: about 20 GB of path state; a 1080p pass of
+// 64 frames has 132.7 M sample items).
+constexpr uint64_t kMaxPathSlots = 1ull << 27;
 
 cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity);
 void wavefront_free(WavefrontState &s);
@@ -58,6 +61,7 @@ struct WfTuning {
     uint32_t shade_blocks_per_sm = 8;
     bool material_sort = false;
     bool ray_sort = false;
+    uint32_t slots_per_pixel = 1;  // multi-frame schedule: path slots per pixel (bounded by the state's capacity)
 };
 
 // Host-side CUDA graph of one chunk of the multi-frame loop (kChunkIterations extend + shade iterations

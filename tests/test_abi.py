@@ -86,6 +86,6 @@ def test_tuning_defaults():
     t = abi.spk_tuning()
     native.lib().spk_tuning_defaults(C.byref(t))
     assert (t.cuda_graph, t.material_sort, t.bvh_width, t.bvh_leaf_size, t.extend_blocks_per_sm,
-            t.shade_blocks_per_sm, t.batch_slots, t.ray_sort, t.bvh_collapse, t.bvh_builder) == \
-        (1, 0, 8, 3, 0, 8, 0, 0, 0, 0)
+            t.shade_blocks_per_sm, t.batch_slots, t.ray_sort, t.bvh_collapse, t.bvh_builder,
+            t.path_slots_per_pixel) == (1, 0, 8, 3, 0, 8, 0, 0, 0, 0, 64)
     assert native.lib().spk_set_tuning(None, C.byref(t)) == 1

@@ -12,7 +12,8 @@ from sparkle_gb300 import abi, native, scenes
 pytestmark = pytest.mark.gpu
 
 DEFAULTS = dict(cuda_graph=1, material_sort=0, bvh_width=8, bvh_leaf_size=3, extend_blocks_per_sm=0,
-                shade_blocks_per_sm=8, batch_slots=0, ray_sort=0, bvh_collapse=0, bvh_builder=0)
+                shade_blocks_per_sm=8, batch_slots=0, ray_sort=0, bvh_collapse=0, bvh_builder=0,
+                path_slots_per_pixel=64)
 
 VARIANTS = [
     dict(cuda_graph=0),
@@ -28,6 +29,9 @@ VARIANTS = [
     dict(bvh_builder=1),
     dict(bvh_builder=1, bvh_width=4, bvh_leaf_size=1),
     dict(bvh_builder=2),
+    dict(path_slots_per_pixel=1),
+    dict(path_slots_per_pixel=4, cuda_graph=0),
+    dict(path_slots_per_pixel=3, material_sort=1),
 ]
 
 
@@ -54,7 +58,8 @@ def test_tuning_defaults_and_validation(ctx):
     ctx.set_tuning(**DEFAULTS)
     assert ctx.tuning() == DEFAULTS
     for bad in [dict(bvh_width=1), dict(bvh_width=9), dict(bvh_leaf_size=0), dict(bvh_leaf_size=4),
-                dict(cuda_graph=2), dict(shade_blocks_per_sm=0), dict(extend_blocks_per_sm=33)]:
+                dict(cuda_graph=2), dict(shade_blocks_per_sm=0), dict(extend_blocks_per_sm=33),
+                dict(path_slots_per_pixel=0), dict(path_slots_per_pixel=65)]:
         with pytest.raises(native.SpkError):
             ctx.set_tuning(**bad)
         assert ctx.tuning() == DEFAULTS  # a rejected setting leaves the previous one
