@@ -206,7 +206,7 @@ typedef struct spk_tuning {
     uint32_t bvh_leaf_size;        /* items per BVH leaf, 1..3 (default 3); used by the next spk_set_scene */
     uint32_t extend_blocks_per_sm; /* traversal CTAs per SM, 0 = the occupancy maximum (default 0) */
     uint32_t shade_blocks_per_sm;  /* shading CTAs per SM, 1..32 (default 8) */
-    uint32_t batch_slots;          /* path slots (queue capacity) of spk_render_batch, 0 = min(items, 2^21) */
+    uint32_t batch_slots;          /* path slots (queue capacity) of spk_render_batch, 0 = min(items, 2^27) */
     uint32_t ray_sort;             /* 1: order each extend queue by ray (direction octant, origin cell) (default 0) */
     uint32_t bvh_collapse;         /* 8-wide collapse: 0 greedy largest-area (default), 1 SAH-optimal; next spk_set_scene */
     uint32_t bvh_builder;          /* BLAS builder: 0 host binned SAH (default), 1 device LBVH (Karras radix tree over

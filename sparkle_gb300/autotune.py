@@ -15,7 +15,7 @@ from __future__ import annotations
 import time
 
 SPACE = {
-    "batch_slots": [1 << 19, 1 << 20, 1 << 21, 1 << 22],
+    "batch_slots": [1 << 27, 1 << 25, 1 << 23, 1 << 21],
     "path_slots_per_pixel": [64, 16, 4, 1],
     "shade_blocks_per_sm": [4, 8, 16],
     "extend_blocks_per_sm": [0, 6],

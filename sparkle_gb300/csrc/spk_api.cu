@@ -2013,7 +2013,7 @@ spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t 
     if (items >= 0xFFFFFFFFull)
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "batch of %llu sample items: split it below 2^32", items);
     const uint32_t slots = static_cast<uint32_t>(
-        std::min<unsigned long long>(items, ctx->tuning.batch_slots ? ctx->tuning.batch_slots : (1u << 21)));
+        std::min<unsigned long long>(items, ctx->tuning.batch_slots ? ctx->tuning.batch_slots : kMaxPathSlots));
     cudaError_t e;
     WavefrontState &s = ctx->wf_batch;
     if (s.capacity < slots && (e = wavefront_alloc(s, slots)) != cudaSuccess) return cuda_fail(ctx, e, "batch slots");
@@ -2051,8 +2051,9 @@ spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t 
     if ((e = cudaEventRecord(ctx->ev_start, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "event");
     uint32_t launches = 0;
     ctx->launch_events.capacity = 0;  // per-launch traversal timing is not recorded for batches
-    e = launch_render_batch(ctx->scene, b, count, ctx->counters, s, ctx->num_sms, ctx->stream, &launches, nullptr,
-                            wf_tuning(ctx));
+    WfTuning bt = wf_tuning(ctx);
+    bt.batch_slots = slots;  // the state may be larger (it only grows): use the requested number of paths
+    e = launch_render_batch(ctx->scene, b, count, ctx->counters, s, ctx->num_sms, ctx->stream, &launches, nullptr, bt);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "batch wavefront");
     if ((e = cudaEventRecord(ctx->ev_stop, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "event");
     ctx->batch_host = reqs;

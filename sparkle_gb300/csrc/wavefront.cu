@@ -948,7 +948,8 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
     unsigned long long *qc = counters->queue_counters;
     const unsigned shade_blocks = static_cast<unsigned>(num_sms) * tuning.shade_blocks_per_sm;
     const unsigned extend_grid = extend_blocks(num_sms, tuning.extend_blocks_per_sm);
-    const uint32_t first = static_cast<uint32_t>(std::min<unsigned long long>(s.capacity, b.total_items));
+    const unsigned long long want = tuning.batch_slots ? tuning.batch_slots : s.capacity;
+    const uint32_t first = static_cast<uint32_t>(std::min<unsigned long long>({want, s.capacity, b.total_items}));
     if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
     if (b.rng == 0) {
         k_b_generate<0><<<(first + 127) / 128, 128, 0, stream>>>(scene, b, s, first, counters);

@@ -62,6 +62,7 @@ struct WfTuning {
     bool material_sort = false;
     bool ray_sort = false;
     uint32_t slots_per_pixel = 1;  // multi-frame schedule: path slots per pixel (bounded by the state's capacity)
+    uint32_t batch_slots = 0;      // batch schedule: paths in flight (0 = the state's capacity)
 };
 
 // Host-side CUDA graph of one chunk of the multi-frame loop (kChunkIterations extend + shade iterations
