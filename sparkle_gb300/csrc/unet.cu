@@ -854,16 +854,17 @@ spk_status spk_render_denoised(spk_ctx *ctx, spk_denoiser *dn, uint32_t spp, uin
         return dn_fail(dn, st, "render: %s", spk_last_error(ctx));
     const auto *ffb = static_cast<const float *>(fb), *fnd = static_cast<const float *>(nd),
                *falb = static_cast<const float *>(alb);
-    if ((st = spk_dn_pack_features(dn, ffb, fnd, falb, 1, h, w, feat)) != SPK_OK ||
-        (st = spk_dn_infer(dn, feat, 1, h, w, den)) != SPK_OK)
+    // The mean and the two halves are consecutive images of one feature batch (feat, feat_a, feat_b) and
+    // come out as consecutive images (den, den_a, den_b): one inference of three images, whose coarse
+    // levels then give the GPU three times the tiles. Each image's result is the same as alone.
+    if ((st = spk_dn_pack_features(dn, ffb, fnd, falb, 1, h, w, feat)) != SPK_OK) return st;
+    if (half >= 1 && (st = spk_dn_pack_halves(dn, ffb, half_a, fnd, falb, 1, h, w, feat_a, feat_b)) != SPK_OK)
         return st;
+    if ((st = spk_dn_infer(dn, feat, half >= 1 ? 3u : 1u, h, w, den)) != SPK_OK) return st;
     uint32_t tiles = 0;
     const float *result = den;
     if (half >= 1) {
-        if ((st = spk_dn_pack_halves(dn, ffb, half_a, fnd, falb, 1, h, w, feat_a, feat_b)) != SPK_OK ||
-            (st = spk_dn_infer(dn, feat_a, 1, h, w, den_a)) != SPK_OK ||
-            (st = spk_dn_infer(dn, feat_b, 1, h, w, den_b)) != SPK_OK ||
-            (st = spk_dn_fallback(dn, den, den_a, den_b, ffb, h, w, tile, threshold, out, &tiles)) != SPK_OK)
+        if ((st = spk_dn_fallback(dn, den, den_a, den_b, ffb, h, w, tile, threshold, out, &tiles)) != SPK_OK)
             return st;
         result = out;
     }
