@@ -46,7 +46,7 @@ enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOve
 #define SPK_MINMAX3 0  // 1: slab entry/exit with three-input min/max (exact, same results)
 #endif
 #ifndef SPK_MT_RCP
-#define SPK_MT_RCP 0  // 1: Moller-Trumbore's 1/det as a correctly rounded reciprocal (same bits as 1.f/det)
+#define SPK_MT_RCP 1  // 1: Moller-Trumbore's 1/det as a correctly rounded reciprocal (same bits as 1.f/det)
 #endif
 #ifndef SPK_WALK_MIN_BLOCKS
 #define SPK_WALK_MIN_BLOCKS 8  // resident 128-thread blocks per SM the walking kernels are compiled for
