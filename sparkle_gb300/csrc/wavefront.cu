@@ -234,15 +234,31 @@ __global__ void __launch_bounds__(256) k_wf_finish(FrameBuffers fb, WavefrontSta
 // ------------------------------------------------------------------------------------------------
 constexpr int kNextItem = 3;  // queue_counters slot: next (frame, pixel) sample item to hand out
 
-// Slot `slot` starts sample item `item` = frame * pixels + pixel of the pass.
+#ifndef SPK_ITEM_TILES
+#define SPK_ITEM_TILES 1  // 1: a frame's items walk the image in 8 x 4 pixel tiles (0: row by row)
+#endif
+
+// Pixel of the q-th sample item of a frame. With SPK_ITEM_TILES the items go through the image in 8 x 4
+// pixel tiles, tile after tile in row-major order, so the 32 lanes of a warp trace a compact block of
+// pixels (tighter primary-ray bundles than 32 pixels of one row); row-major order when the image is not a
+// whole number of tiles. Results never depend on this order: each sample keeps its own pixel and seed.
+__device__ __forceinline__ uint32_t item_pixel(uint32_t q, uint32_t w, uint32_t h) {
+    if (!SPK_ITEM_TILES || (w & 7u) || (h & 3u)) return q;
+    const uint32_t tile = q >> 5, j = q & 31u, tiles_x = w >> 3;
+    const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
+    return (ty * 4u + (j >> 3)) * w + tx * 8u + (j & 7u);
+}
+
+// Slot `slot` starts sample item `item` = frame * pixels + q of the pass (pixel item_pixel(q)); the slot
+// records the sample's index frame * pixels + pixel, where its result is stored.
 template <int kKind>
 __device__ __forceinline__ void start_item(const DevCamera &cam, const RenderParams &p, const WavefrontState &s,
                                            uint32_t slot, uint32_t item, uint32_t w, uint32_t h,
                                            uint32_t frame_base) {
     const uint32_t npix = w * h;
-    const uint32_t k = item / npix, pid = item - k * npix;
+    const uint32_t k = item / npix, pid = item_pixel(item - k * npix, w, h);
     start_path<kKind>(cam, p, s, slot, pid % w, pid / w, w, h, s.frame_seed[frame_base + k]);
-    s.slot_item[slot] = item;
+    s.slot_item[slot] = k * npix + pid;
     s.slot_state[slot] = 0u;
 }
 
