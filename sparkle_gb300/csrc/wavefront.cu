@@ -235,7 +235,10 @@ __global__ void __launch_bounds__(256) k_wf_finish(FrameBuffers fb, WavefrontSta
 constexpr int kNextItem = 3;  // queue_counters slot: next (frame, pixel) sample item to hand out
 
 #ifndef SPK_ITEM_TILES
-#define SPK_ITEM_TILES 1  // 1: a frame's items walk the image in 8 x 4 pixel tiles (0: row by row)
+#define SPK_ITEM_TILES 1  // 1: a frame's items walk the image in 32-pixel tiles (0: row by row)
+#endif
+#ifndef SPK_ITEM_TILE_W
+#define SPK_ITEM_TILE_W 4  // tile width (4, 8 or 16); the height is 32 / width
 #endif
 
 // Pixel of the q-th sample item of a frame. With SPK_ITEM_TILES the items go through the image in 8 x 4
@@ -243,10 +246,12 @@ constexpr int kNextItem = 3;  // queue_counters slot: next (frame, pixel) sample
 // pixels (tighter primary-ray bundles than 32 pixels of one row); row-major order when the image is not a
 // whole number of tiles. Results never depend on this order: each sample keeps its own pixel and seed.
 __device__ __forceinline__ uint32_t item_pixel(uint32_t q, uint32_t w, uint32_t h) {
-    if (!SPK_ITEM_TILES || (w & 7u) || (h & 3u)) return q;
-    const uint32_t tile = q >> 5, j = q & 31u, tiles_x = w >> 3;
+    constexpr uint32_t tw = SPK_ITEM_TILE_W, th = 32u / SPK_ITEM_TILE_W;
+    static_assert(tw * th == 32u && (tw & (tw - 1u)) == 0u, "32-pixel tiles");
+    if (!SPK_ITEM_TILES || (w % tw) || (h % th)) return q;
+    const uint32_t tile = q >> 5, j = q & 31u, tiles_x = w / tw;
     const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
-    return (ty * 4u + (j >> 3)) * w + tx * 8u + (j & 7u);
+    return (ty * th + j / tw) * w + tx * tw + (j % tw);
 }
 
 // Slot `slot` starts sample item `item` = frame * pixels + q of the pass (pixel item_pixel(q)); the slot
