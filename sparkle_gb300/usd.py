@@ -23,8 +23,16 @@ mirrors:
   opacity 1, ior 1.5).
 * Dome lights (LoadSkyLight, :474-496) become the sky: with a texture file (relative to the USD file) the
   cube SkyLight cooks from that map (sparkle_gb300.sky), else the gradient sky of its colour x intensity x
-  2^exposure (GetLightColor, :455-458). Distant lights and cameras are not read: the CPU path ignores the
-  directional light and the camera is the caller's.
+  2^exposure (GetLightColor, :455-458). Distant lights are not read: the CPU path ignores the
+  directional light.
+* Cameras (LoadCamera, :80-126; load_usda_camera): a perspective Camera prim is a component of its parent
+  node, like a mesh; the last one loaded is the main camera (SetMainCamera). focalLength and
+  verticalAperture are millimetres (35 and 24 when unauthored, the loader's initial values), fStop and
+  focusDistance replace the defaults (f/22, 1 m) only when positive; an orthographic camera is refused (the
+  reference asserts). The render attributes follow CalculateRenderAttribute (CameraComponent.cpp:120-128)
+  and the posture CameraRenderProxy::OnTransformDirty (CameraRenderProxy.cpp:113-128): position = the
+  node's translation, right / front / up = rows 0 / 1 / 2 of its world matrix (Transform::
+  ExtractLocalBasis), focus plane from tan(vfov / 2), the frame's aspect ratio and the focus distance.
 
 Where the reference would assert (missing normals), this module computes area-weighted vertex normals.
 faceVarying / uniform / constant primvars are expanded to one vertex per face corner. The exporter writes
@@ -40,7 +48,7 @@ import re
 
 import numpy as np
 
-from .abi import SPK_SKY_GRADIENT, Instance, Material, Mesh, Scene, Sky, Texture
+from .abi import SPK_SKY_GRADIENT, Instance, Material, Mesh, Scene, Sky, Texture, spk_camera
 
 # --------------------------------------------------------------------------------------------------------
 # Tokenizer and parser of the USDA subset.
@@ -545,6 +553,68 @@ def load_usda(path, sky: Sky = None, sky_size: int = 1024) -> Scene:
     if sky is None:
         sky = _dome_sky(domes[0], base_dir, sky_size) if domes else Sky()
     return Scene(meshes, instances, materials, sky, name=os.path.basename(path), textures=textures)
+
+
+def _camera_prims(root):
+    """(Camera prim, its parent node's world matrix) in LoadNode's traversal order."""
+    out = []
+
+    def walk(node, parent_world):
+        world = parent_world @ _local_matrix(node)
+        for c in node.children:
+            if c.spec != "def":
+                continue
+            if c.type == "Xform" or c.type == "":
+                walk(c, world)
+            elif c.type == "Camera":
+                out.append((c, world))
+
+    walk(root, np.eye(4))
+    return out
+
+
+def load_usda_camera(path, width: int, height: int):
+    """The main camera of a USDA file (the last Camera prim loaded) as an spk_camera for a width x height
+    frame, or None when the file has no camera. Float32 arithmetic in the reference's order."""
+    with open(path, "r", encoding="utf-8") as f:
+        layer_meta, roots = _parse(f.read())
+    roots = [r for r in roots if r.spec == "def"]
+    default = layer_meta.get("defaultPrim")
+    root = next((r for r in roots if r.name == default), roots[0] if roots else None)
+    cams = _camera_prims(root) if root is not None else []
+    if not cams:
+        return None
+    prim, world = cams[-1]
+    if (prim.attrs.get("projection") or "perspective") != "perspective":
+        raise UsdError(f"camera {prim.name!r}: only perspective cameras are supported")
+    f32 = np.float32
+
+    def scalar(name, default):
+        v = prim.attrs.get(name)
+        return f32(default if v is None else v)
+
+    focal = scalar("focalLength", 35.0) * f32(0.001)
+    sensor = scalar("verticalAperture", 24.0) * f32(0.001)
+    f_stop, focus = scalar("fStop", 0.0), scalar("focusDistance", 0.0)
+    aperture = f_stop if f_stop > 0 else f32(22.0)
+    fd = focus if focus > 0 else f32(1.0)
+    vfov = f32(2.0) * f32(np.arctan(sensor / (f32(2.0) * focal)))
+    m = world.astype(np.float32)
+    position = m[:3, 3]
+    right, front, up = m[0, :3], m[1, :3], m[2, :3]
+    aspect = f32(width) / f32(height)
+    plane_h = f32(2.0) * f32(np.tan(vfov / f32(2.0))) * fd
+    plane_w = aspect * plane_h
+    max_u, max_v = right * plane_w, up * plane_h
+    lower_left = position + front * fd - max_u * f32(0.5) - max_v * f32(0.5)
+    cam = spk_camera()
+    for name, v in (("position", position), ("right", right), ("up", up), ("front", front),
+                    ("lower_left", lower_left), ("max_u", max_u), ("max_v", max_v)):
+        getattr(cam, name)[:] = [float(x) for x in v]
+    cam.aperture_radius = float(focal / aperture * f32(0.5))
+    cam.exposure = 1.0
+    cam.far_plane = 1000.0
+    return cam
 
 
 # --------------------------------------------------------------------------------------------------------

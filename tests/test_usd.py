@@ -7,7 +7,7 @@ back; one GPU test renders an imported scene against the oracle."""
 import numpy as np
 import pytest
 
-from sparkle_gb300 import abi, scenes, usd
+from sparkle_gb300 import abi, native, scenes, usd
 
 
 def write(tmp_path, text, name="s.usda"):
@@ -242,3 +242,87 @@ def test_imported_scene_renders_like_the_oracle(tmp_path):
     close = np.all(np.abs(hdr[..., :3] - ref[..., :3]) <= 1e-4 * (1 + np.abs(ref[..., :3])), axis=-1)
     assert close.mean() > 0.95
     ctx.close()
+
+
+CAMERA_USDA = '''#usda 1.0
+(
+    defaultPrim = "root"
+)
+def Xform "root"
+{
+    def Xform "first"
+    {
+        double3 xformOp:translate = (9, 9, 9)
+        uniform token[] xformOpOrder = ["xformOp:translate"]
+        def Camera "unused"
+        {
+        }
+    }
+    def Xform "cam_node"
+    {
+        double3 xformOp:translate = (1, 2, 3)
+        uniform token[] xformOpOrder = ["xformOp:translate"]
+        def Camera "cam"
+        {
+            float focalLength = 50
+            float verticalAperture = 24
+            float fStop = 2.8
+            float focusDistance = 5
+            double3 xformOp:translate = (100, 0, 0)
+            uniform token[] xformOpOrder = ["xformOp:translate"]
+        }
+    }
+}
+'''
+
+
+def _cam_fields(c):
+    return {k: np.array(getattr(c, k), np.float32) for k in
+            ("position", "right", "up", "front", "lower_left", "max_u", "max_v")}
+
+
+def test_usd_camera_matches_the_library_camera(tmp_path):
+    """The last camera wins, its own xformOps are not read (the parent node's transform is the camera's),
+    and with an unrotated node the result equals spk_camera_from_look for the same posture and lens."""
+    p = tmp_path / "cam.usda"
+    p.write_text(CAMERA_USDA)
+    c = usd.load_usda_camera(str(p), 640, 480)
+    vfov = 2 * np.arctan(np.float32(0.024) / (2 * np.float32(0.05)))
+    ref = native.camera_from_look((1, 2, 3), (1, 3, 3), (0, 0, 1), float(vfov), 5.0,
+                                  float(np.float32(0.05) / np.float32(2.8) * np.float32(0.5)), 1.0, 640, 480)
+    got, want = _cam_fields(c), _cam_fields(ref)
+    for k in got:
+        np.testing.assert_allclose(got[k], want[k], rtol=1e-6, atol=1e-6, err_msg=k)
+    assert c.aperture_radius == pytest.approx(ref.aperture_radius, rel=1e-6)
+    assert c.far_plane == ref.far_plane and c.exposure == 1.0
+
+
+def test_usd_camera_defaults_rows_and_refusals(tmp_path):
+    text = CAMERA_USDA.replace('''            float focalLength = 50
+            float verticalAperture = 24
+            float fStop = 2.8
+            float focusDistance = 5
+''', "").replace('double3 xformOp:translate = (1, 2, 3)\n        uniform token[] xformOpOrder = ["xformOp:translate"]',
+                 'float3 xformOp:rotateXYZ = (0, 0, 30)\n        uniform token[] xformOpOrder = ["xformOp:rotateXYZ"]')
+    p = tmp_path / "d.usda"
+    p.write_text(text)
+    c = usd.load_usda_camera(str(p), 100, 50)
+    # unauthored lens: 35 mm, 24 mm sensor, f/22, focus distance 1
+    assert c.aperture_radius == pytest.approx(0.035 / 22 * 0.5, rel=1e-6)
+    m = np.eye(3)
+    a = np.deg2rad(30)
+    m[0, 0], m[0, 1], m[1, 0], m[1, 1] = np.cos(a), -np.sin(a), np.sin(a), np.cos(a)
+    # right / front / up are the rows of the node's matrix (Transform::ExtractLocalBasis)
+    np.testing.assert_allclose(_cam_fields(c)["right"], m[0], atol=1e-6)
+    np.testing.assert_allclose(_cam_fields(c)["front"], m[1], atol=1e-6)
+    vfov = 2 * np.arctan(0.024 / 0.07)
+    plane_h = 2 * np.tan(vfov / 2)
+    np.testing.assert_allclose(_cam_fields(c)["max_v"], m[2] * plane_h, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(_cam_fields(c)["max_u"], m[0] * plane_h * 2, rtol=1e-5, atol=1e-6)
+    ortho = text.replace('def Camera "cam"\n        {', 'def Camera "cam"\n        {\n            token projection = "orthographic"')
+    (tmp_path / "o.usda").write_text(ortho)
+    with pytest.raises(usd.UsdError):
+        usd.load_usda_camera(str(tmp_path / "o.usda"), 100, 50)
+    none = '#usda 1.0\ndef Xform "root"\n{\n}\n'
+    (tmp_path / "n.usda").write_text(none)
+    assert usd.load_usda_camera(str(tmp_path / "n.usda"), 100, 50) is None
