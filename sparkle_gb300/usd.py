@@ -639,9 +639,32 @@ def _matrix(m4):
     return "( " + ", ".join("(" + ", ".join(_f(x) for x in r) + ")" for r in rows) + " )"
 
 
-def save_usda(scene: Scene, path) -> None:
+def _camera_lines(cam):
+    """ExportCamera (USDExporter.cpp:392-406) of an spk_camera under an Xform holding its posture: the node
+    matrix has rows right / front / up and the position as translation (what load_usda_camera reads back),
+    the lens is the 24 mm sensor of CameraComponent's defaults with the focal length, f-stop and focus
+    distance that reproduce the camera's focus plane and aperture radius (fStop 0, unauthored, for a
+    pinhole camera: it reads back as f/22, the reference's default)."""
+    f64 = lambda name: np.array(getattr(cam, name), np.float64)
+    pos, right, front, up = f64("position"), f64("right"), f64("front"), f64("up")
+    max_u, max_v, ll = f64("max_u"), f64("max_v"), f64("lower_left")
+    plane_h = np.linalg.norm(max_v) / np.linalg.norm(up)
+    fd = np.linalg.norm(ll + max_u * 0.5 + max_v * 0.5 - pos) / np.linalg.norm(front)
+    sensor = 0.024
+    focal = sensor * fd / plane_h  # tan(vfov / 2) = plane_h / (2 fd) = sensor / (2 focal)
+    f_stop = focal / (2.0 * cam.aperture_radius) if cam.aperture_radius > 0 else 0.0
+    node = np.eye(4)
+    node[0, :3], node[1, :3], node[2, :3], node[:3, 3] = right, front, up, pos
+    return ['    def Xform "camera_node"', "    {", f"        matrix4d xformOp:transform = {_matrix(node)}",
+            '        uniform token[] xformOpOrder = ["xformOp:transform"]', '        def Camera "camera"', "        {",
+            '            token projection = "perspective"', f"            float focalLength = {_f(focal * 1000.0)}",
+            f"            float verticalAperture = {_f(sensor * 1000.0)}", f"            float fStop = {_f(f_stop)}",
+            f"            float focusDistance = {_f(fd)}", "        }", "    }"]
+
+
+def save_usda(scene: Scene, path, camera=None) -> None:
     """USDExporter::Export of a Scene: Z-up stage, one Xform per mesh instance, materials under /_materials,
-    textures as PNG files in textures/ beside `path`."""
+    textures as PNG files in textures/ beside `path`; with `camera` (an spk_camera) also the camera."""
     from .native import write_png
     if not str(path).endswith(".usda"):
         raise UsdError("only .usda output is supported")
@@ -731,6 +754,8 @@ def save_usda(scene: Scene, path) -> None:
             lines += [f"            float4[] primvars:tangents = {_vec_array(mesh.tangents)} (",
                       '                interpolation = "vertex"', "            )"]
         lines += [f"            rel material:binding = <{material_path(inst.material_id)}>", "        }", "    }"]
+    if camera is not None:
+        lines += _camera_lines(camera)
     lines.append("}")
     if mat_lines:
         lines += ["", 'def Scope "_materials"', "{"] + mat_lines + ["}"]

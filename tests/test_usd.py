@@ -326,3 +326,19 @@ def test_usd_camera_defaults_rows_and_refusals(tmp_path):
     none = '#usda 1.0\ndef Xform "root"\n{\n}\n'
     (tmp_path / "n.usda").write_text(none)
     assert usd.load_usda_camera(str(tmp_path / "n.usda"), 100, 50) is None
+
+
+def test_camera_export_round_trip(tmp_path, cornell):
+    """save_usda(..., camera) writes ExportCamera's prim; load_usda_camera reads back the same camera."""
+    scene, cam_args = cornell
+    W, H = 320, 240
+    cam = scenes.make_camera(cam_args, W, H)
+    p = tmp_path / "with_cam.usda"
+    usd.save_usda(scene, str(p), camera=cam)
+    back = usd.load_usda_camera(str(p), W, H)
+    got, want = _cam_fields(back), _cam_fields(cam)
+    for k in got:
+        np.testing.assert_allclose(got[k], want[k], rtol=1e-5, atol=1e-5, err_msg=k)
+    if cam.aperture_radius > 0:
+        assert back.aperture_radius == pytest.approx(cam.aperture_radius, rel=1e-5)
+    assert len(usd.load_usda(str(p)).meshes) == len([i for i in scene.instances if not i.sphere])
