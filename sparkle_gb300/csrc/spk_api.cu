@@ -727,7 +727,7 @@ spk_status build_host_scene(spk_ctx *ctx, const spk_mesh *meshes, uint32_t num_m
         hs.cube.resize(n);
         std::memcpy(hs.cube.data(), sky->cube_rgba, n * sizeof(float4));
     }
-    hs.sky_mode = sky ? sky->mode : SPK_SKY_NONE;
+    hs.sky_mode = sky ? sky->mode : static_cast<uint32_t>(SPK_SKY_NONE);
     hs.sky_size = sky ? sky->cube_size : 0;
     for (int c = 0; c < 3; ++c) hs.sky_color[c] = sky ? sky->color[c] : 0.f;
     hs.abs_x = abs_x;

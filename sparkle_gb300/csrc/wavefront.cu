@@ -858,7 +858,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 cudaStream_t stream;
                 unsigned extend_grid, shade_grid, material_sort, ray_sort;
             } key;
-            std::memset(&key, 0, sizeof(key));
+            std::memset(static_cast<void *>(&key), 0, sizeof(key));  // padding too: the key is compared bytewise
             key.scene = scene;
             key.cam = cam;
             key.fbuf = fbuf;
