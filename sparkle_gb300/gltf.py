@@ -92,12 +92,56 @@ def _accessor(doc, buffers, index):
     return arr.copy()
 
 
+def _unfilter(raw: np.ndarray, h: int, stride: int, bpp: int) -> np.ndarray:
+    """Undoes the PNG row filters (None, Sub, Up, Average, Paeth; bpp = bytes per complete pixel, at least
+    1). None / Sub / Up rows are vectorised (Sub is a running sum mod 256 per byte lane); Average and Paeth
+    depend on the reconstructed byte to the left and run as a plain loop over the row."""
+    out = np.zeros((h, stride), np.uint8)
+    prev = np.zeros(stride, np.uint8)
+    for y in range(h):
+        f, line = int(raw[y, 0]), raw[y, 1:]
+        if f == 0:
+            cur = line.copy()
+        elif f == 1:
+            pad = (-stride) % bpp
+            lanes = np.concatenate([line, np.zeros(pad, np.uint8)]).reshape(-1, bpp).astype(np.uint32)
+            cur = (np.cumsum(lanes, axis=0) & 0xFF).astype(np.uint8).reshape(-1)[:stride]
+        elif f == 2:
+            cur = (line.astype(np.uint16) + prev).astype(np.uint8)
+        elif f in (3, 4):
+            ln, pv = line.tolist(), prev.tolist()
+            cb = [0] * stride
+            if f == 3:
+                for x in range(stride):
+                    left = cb[x - bpp] if x >= bpp else 0
+                    cb[x] = (ln[x] + ((left + pv[x]) >> 1)) & 0xFF
+            else:
+                for x in range(stride):
+                    if x >= bpp:
+                        a_, c_ = cb[x - bpp], pv[x - bpp]
+                    else:
+                        a_ = c_ = 0
+                    b_ = pv[x]
+                    pa, pb, pc = abs(b_ - c_), abs(a_ - c_), abs(a_ + b_ - 2 * c_)
+                    pred = a_ if pa <= pb and pa <= pc else (b_ if pb <= pc else c_)
+                    cb[x] = (ln[x] + pred) & 0xFF
+            cur = np.array(cb, np.uint8)
+        else:
+            raise ValueError(f"bad PNG filter type {f}")
+        out[y] = cur
+        prev = cur
+    return out
+
+
 def decode_png(data: bytes) -> np.ndarray:
-    """8-bit non-interlaced PNG (grey, grey+alpha, RGB, RGBA) -> (H, W, 4) float32 in [0, 1] (ColorToVec)."""
+    """Non-interlaced PNG -> (H, W, 4) float32 in [0, 1] (ColorToVec): grey and palette at 1, 2, 4 or 8 bits
+    (palette alpha from tRNS), grey+alpha / RGB / RGBA at 8 or 16 bits (16-bit samples keep their high byte,
+    as the reference's image loader reduces them to 8 bits). Adam7-interlaced files are refused."""
     if data[:8] != b"\x89PNG\r\n\x1a\n":
         raise ValueError("not a PNG image (only PNG textures are decoded)")
     off, idat = 8, []
-    w = h = ctype = None
+    w = h = ctype = depth = None
+    palette = trns = None
     while off < len(data):
         n, = struct.unpack(">I", data[off:off + 4])
         kind = data[off + 4:off + 8]
@@ -105,39 +149,51 @@ def decode_png(data: bytes) -> np.ndarray:
         off += 12 + n
         if kind == b"IHDR":
             w, h, depth, ctype, _, _, interlace = struct.unpack(">IIBBBBB", body)
-            if depth != 8 or interlace != 0 or ctype not in (0, 2, 4, 6):
-                raise ValueError("only 8-bit non-interlaced grey/RGB(A) PNGs are decoded")
+            ok = {0: (1, 2, 4, 8, 16), 2: (8, 16), 3: (1, 2, 4, 8), 4: (8, 16), 6: (8, 16)}
+            if ctype not in ok or depth not in ok[ctype]:
+                raise ValueError(f"unsupported PNG colour type {ctype} at {depth} bits")
+            if interlace != 0:
+                raise ValueError("interlaced (Adam7) PNGs are not decoded")
+        elif kind == b"PLTE":
+            palette = np.frombuffer(body, np.uint8).reshape(-1, 3)
+        elif kind == b"tRNS":
+            trns = np.frombuffer(body, np.uint8)
         elif kind == b"IDAT":
             idat.append(body)
         elif kind == b"IEND":
             break
-    ch = {0: 1, 2: 3, 4: 2, 6: 4}[ctype]
-    raw = np.frombuffer(zlib.decompress(b"".join(idat)), np.uint8).reshape(h, 1 + w * ch)
-    out = np.zeros((h, w * ch), np.int32)
-    prev = np.zeros(w * ch, np.int32)
-    for y in range(h):
-        f, line = raw[y, 0], raw[y, 1:].astype(np.int32)
-        cur = np.zeros(w * ch, np.int32)
-        for x in range(w * ch):
-            a = cur[x - ch] if x >= ch else 0
-            b = prev[x]
-            c = prev[x - ch] if x >= ch else 0
-            if f == 0:
-                pred = 0
-            elif f == 1:
-                pred = a
-            elif f == 2:
-                pred = b
-            elif f == 3:
-                pred = (a + b) // 2
-            else:  # Paeth
-                pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
-                pred = a if pa <= pb and pa <= pc else (b if pb <= pc else c)
-            cur[x] = (line[x] + pred) & 0xFF
-        out[y] = cur
-        prev = cur
-    px = out.reshape(h, w, ch).astype(np.float32) / 255.0
+    if w is None:
+        raise ValueError("PNG without IHDR")
+    ch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    bits = ch * depth
+    stride = (w * bits + 7) // 8
+    raw = np.frombuffer(zlib.decompress(b"".join(idat)), np.uint8)[:h * (1 + stride)].reshape(h, 1 + stride)
+    rows = _unfilter(raw, h, stride, max(1, bits // 8))
+    if depth == 16:
+        samples = rows.reshape(h, w * ch, 2)[..., 0]  # high byte of each big-endian sample
+    elif depth == 8:
+        samples = rows.reshape(h, w * ch)
+    else:  # 1, 2 or 4 bits, one channel: unpack MSB first
+        per = 8 // depth
+        shifts = np.arange(per - 1, -1, -1, dtype=np.uint8) * depth
+        unpacked = (rows[:, :, None] >> shifts) & ((1 << depth) - 1)
+        samples = unpacked.reshape(h, stride * per)[:, :w]
+        if ctype == 0:  # grey scaled to 8 bits
+            samples = (samples.astype(np.uint32) * (255 // ((1 << depth) - 1))).astype(np.uint8)
     rgba = np.ones((h, w, 4), np.float32)
+    if ctype == 3:
+        if palette is None:
+            raise ValueError("palette PNG without PLTE")
+        idx = samples.reshape(h, w).astype(np.int64)
+        if idx.max(initial=0) >= len(palette):
+            raise ValueError("PNG palette index out of range")
+        rgba[..., :3] = palette[idx].astype(np.float32) / 255.0
+        if trns is not None:
+            alpha = np.full(len(palette), 255, np.uint8)
+            alpha[:min(len(trns), len(palette))] = trns[:len(palette)]
+            rgba[..., 3] = alpha[idx].astype(np.float32) / 255.0
+        return rgba
+    px = samples.reshape(h, w, ch).astype(np.float32) / 255.0
     if ch in (1, 2):
         rgba[..., :3] = px[..., :1]
     else:
