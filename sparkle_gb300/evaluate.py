@@ -8,7 +8,7 @@ import ctypes as C
 import numpy as np
 
 from . import native
-from .gltf import decode_png
+from .gltf import decode_image
 
 PIXELS_PER_DEGREE = 0.7 * (3840 / 0.7) * np.pi / 180.0  # FLIP's default viewing condition
 
@@ -44,9 +44,9 @@ def rel_mse(x, reference, eps: float = 0.01, device: int = 0) -> float:
 
 
 def load_image(path) -> np.ndarray:
-    """A PNG as (H, W, 3) float32 RGB / 255 (render_test_support.load_image)."""
+    """A PNG (or baseline JPEG) as (H, W, 3) float32 RGB / 255 (render_test_support.load_image)."""
     with open(path, "rb") as f:
-        return decode_png(f.read())[..., :3]
+        return decode_image(f.read())[..., :3]
 
 
 def compare_images(ground_truth, screenshot, device: int = 0) -> float:

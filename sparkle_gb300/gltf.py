@@ -7,7 +7,7 @@ What the reference does and this module mirrors:
 * Materials (LoadMaterials, GLTFLoader.cpp:475-526): a factor is read only when its texture is present --
   base colour with baseColorTexture, metallic/roughness with metallicRoughnessTexture, emissive with
   emissiveTexture -- otherwise MaterialResource's defaults apply (base colour 1, emissive 0, metallic 1,
-  roughness 1; io/Material.h:9-14). Textures (PNG images, embedded or external) become Scene textures:
+  roughness 1; io/Material.h:9-14). Textures (PNG or baseline JPEG images, embedded or external) become Scene textures:
   base colour and emissive as sRGB, metallic-roughness and normal maps as linear data.
 * Nodes (ProcessNode, GLTFLoader.cpp:528-575): rotation = 90 degrees about +X times the node's quaternion
   (glTF is y-up, Sparkle z-up), applied at every node including children; the node's scale is baked into
@@ -203,6 +203,14 @@ def decode_png(data: bytes) -> np.ndarray:
     return rgba
 
 
+def decode_image(data: bytes) -> np.ndarray:
+    """A PNG or baseline JPEG file (told apart by their signatures) -> (H, W, 4) float32 in [0, 1]."""
+    if data[:2] == b"\xff\xd8":
+        from .jpeg import decode_jpeg
+        return decode_jpeg(data)
+    return decode_png(data)
+
+
 def _image_bytes(doc, buffers, base_dir, image):
     if "bufferView" in image:
         v = doc["bufferViews"][image["bufferView"]]
@@ -300,7 +308,7 @@ def load_gltf(path: str, sky: Sky | None = None) -> Scene:
         key = (index, srgb)
         if key not in tex_index:
             image = doc["images"][doc["textures"][index]["source"]]
-            textures.append(Texture(decode_png(_image_bytes(doc, buffers, base_dir, image)), srgb=srgb))
+            textures.append(Texture(decode_image(_image_bytes(doc, buffers, base_dir, image)), srgb=srgb))
             tex_index[key] = len(textures) - 1
         return tex_index[key]
 

@@ -14,7 +14,7 @@ import os
 import numpy as np
 
 from . import abi, native
-from .gltf import decode_png
+from .gltf import decode_image
 
 CUBE_SIZE = 1024  # SkyLight.cpp:24
 
@@ -67,11 +67,11 @@ def decode_hdr(data: bytes) -> np.ndarray:
 
 
 def load_sky_map(path) -> np.ndarray:
-    """(H, W, 4) float32 texels of a .hdr or .png sky map (Image2D::LoadFromFile)."""
+    """(H, W, 4) float32 texels of a .hdr, .png or .jpg sky map (Image2D::LoadFromFile)."""
     with open(path, "rb") as f:
         data = f.read()
-    if data[:8] == b"\x89PNG\r\n\x1a\n":
-        return decode_png(data)
+    if data[:8] == b"\x89PNG\r\n\x1a\n" or data[:2] == b"\xff\xd8":
+        return decode_image(data)
     return decode_hdr(data)
 
 

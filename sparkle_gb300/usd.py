@@ -427,7 +427,7 @@ def _surface_shader(mat, prims_by_path):
 
 
 def _load_texture(shader_path, prims_by_path, base_dir, srgb, textures, tex_cache):
-    from .gltf import decode_png
+    from .gltf import decode_image
     tex = prims_by_path.get(shader_path)
     if tex is None or tex.attrs.get("info:id") != "UsdUVTexture":
         raise UsdError(f"input connected to {shader_path!r}, which is not a UsdUVTexture")
@@ -438,7 +438,7 @@ def _load_texture(shader_path, prims_by_path, base_dir, srgb, textures, tex_cach
     key = (file, srgb)
     if key not in tex_cache:
         with open(file, "rb") as f:
-            rgba = decode_png(f.read())
+            rgba = decode_image(f.read())
         tex_cache[key] = len(textures)
         textures.append(Texture(rgba, srgb=srgb))
     return tex_cache[key]

@@ -168,3 +168,17 @@ def test_imported_scene_renders_like_the_oracle(tmp_path):
     close = np.all(np.abs(hdr[..., :3] - ref[..., :3]) <= 1e-4 * (1 + np.abs(ref[..., :3])), axis=-1)
     assert close.mean() > 0.95
     ctx.close()
+
+
+def test_jpeg_texture(tmp_path):
+    """An embedded JPEG image (image/jpeg) decodes like a PNG one, within the JPEG's own rounding."""
+    from test_jpeg import encode_jpeg, smooth_rgb
+    img = smooth_rgb(16, 24, 7)
+    jpg = encode_jpeg(img, q=1)
+    mats = [dict(pbrMetallicRoughness=dict(baseColorTexture=dict(index=0)))]
+    doc = json.loads(build_doc([dict(mesh=0)], scenes_=[dict(nodes=[0])], materials=mats))
+    doc["images"] = [dict(uri="data:image/jpeg;base64," + base64.b64encode(jpg).decode())]
+    sc = gltf.load_gltf(write(tmp_path, json.dumps(doc).encode()))
+    tex = sc.textures[0].rgba
+    assert tex.shape == (16, 24, 4)
+    assert np.abs(np.rint(tex[..., :3] * 255) - img).max() <= 3.0
