@@ -105,3 +105,17 @@ def test_large_texture_decodes_in_seconds():
     got = decode_png(png)
     assert time.perf_counter() - t0 < 5.0
     np.testing.assert_array_equal(np.rint(got * 255).astype(np.uint8), img)
+
+
+def test_decodes_the_library_png_writer(tmp_path):
+    """spk_write_png picks a filter per row (least absolute residual): random and smooth images read back."""
+    from sparkle_gb300 import native
+    rng = np.random.default_rng(6)
+    yy, xx = np.mgrid[0:40, 0:70]
+    smooth = np.stack([(xx * 3) % 256, (yy * 5) % 256, ((xx + yy) * 2) % 256, np.full_like(xx, 200)],
+                      -1).astype(np.uint8)
+    for k, img in enumerate((rng.integers(0, 256, (40, 70, 4), np.uint8), smooth)):
+        p = tmp_path / f"w{k}.png"
+        native.write_png(p, img)
+        got = decode_png(p.read_bytes())
+        np.testing.assert_array_equal(np.rint(got * 255).astype(np.uint8), img)
