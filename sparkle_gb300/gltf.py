@@ -133,14 +133,36 @@ def _unfilter(raw: np.ndarray, h: int, stride: int, bpp: int) -> np.ndarray:
     return out
 
 
+def _png_samples(rows: np.ndarray, w: int, h: int, ch: int, depth: int, ctype: int) -> np.ndarray:
+    """Unfiltered scanlines -> (h, w, ch) uint8 samples (16-bit: high byte; 1/2/4-bit grey scaled to 8 bits,
+    palette indices as they are)."""
+    stride = rows.shape[1]
+    if depth == 16:
+        samples = rows.reshape(h, w * ch, 2)[..., 0]  # high byte of each big-endian sample
+    elif depth == 8:
+        samples = rows.reshape(h, w * ch)
+    else:  # 1, 2 or 4 bits, one channel: unpack MSB first
+        per = 8 // depth
+        shifts = np.arange(per - 1, -1, -1, dtype=np.uint8) * depth
+        unpacked = (rows[:, :, None] >> shifts) & ((1 << depth) - 1)
+        samples = unpacked.reshape(h, stride * per)[:, :w]
+        if ctype == 0:  # grey scaled to 8 bits
+            samples = (samples.astype(np.uint32) * (255 // ((1 << depth) - 1))).astype(np.uint8)
+    return samples.reshape(h, w, ch)
+
+
+# Adam7 passes: (first column, first row, column step, row step).
+_ADAM7 = ((0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2))
+
+
 def decode_png(data: bytes) -> np.ndarray:
-    """Non-interlaced PNG -> (H, W, 4) float32 in [0, 1] (ColorToVec): grey and palette at 1, 2, 4 or 8 bits
-    (palette alpha from tRNS), grey+alpha / RGB / RGBA at 8 or 16 bits (16-bit samples keep their high byte,
-    as the reference's image loader reduces them to 8 bits). Adam7-interlaced files are refused."""
+    """PNG -> (H, W, 4) float32 in [0, 1] (ColorToVec): grey and palette at 1, 2, 4 or 8 bits (palette alpha
+    from tRNS), grey+alpha / RGB / RGBA at 8 or 16 bits (16-bit samples keep their high byte, as the
+    reference's image loader reduces them to 8 bits), non-interlaced or Adam7-interlaced."""
     if data[:8] != b"\x89PNG\r\n\x1a\n":
         raise ValueError("not a PNG image (only PNG textures are decoded)")
     off, idat = 8, []
-    w = h = ctype = depth = None
+    w = h = ctype = depth = interlace = None
     palette = trns = None
     while off < len(data):
         n, = struct.unpack(">I", data[off:off + 4])
@@ -152,8 +174,8 @@ def decode_png(data: bytes) -> np.ndarray:
             ok = {0: (1, 2, 4, 8, 16), 2: (8, 16), 3: (1, 2, 4, 8), 4: (8, 16), 6: (8, 16)}
             if ctype not in ok or depth not in ok[ctype]:
                 raise ValueError(f"unsupported PNG colour type {ctype} at {depth} bits")
-            if interlace != 0:
-                raise ValueError("interlaced (Adam7) PNGs are not decoded")
+            if interlace not in (0, 1):
+                raise ValueError(f"unknown PNG interlace method {interlace}")
         elif kind == b"PLTE":
             palette = np.frombuffer(body, np.uint8).reshape(-1, 3)
         elif kind == b"tRNS":
@@ -166,25 +188,30 @@ def decode_png(data: bytes) -> np.ndarray:
         raise ValueError("PNG without IHDR")
     ch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
     bits = ch * depth
-    stride = (w * bits + 7) // 8
-    raw = np.frombuffer(zlib.decompress(b"".join(idat)), np.uint8)[:h * (1 + stride)].reshape(h, 1 + stride)
-    rows = _unfilter(raw, h, stride, max(1, bits // 8))
-    if depth == 16:
-        samples = rows.reshape(h, w * ch, 2)[..., 0]  # high byte of each big-endian sample
-    elif depth == 8:
-        samples = rows.reshape(h, w * ch)
-    else:  # 1, 2 or 4 bits, one channel: unpack MSB first
-        per = 8 // depth
-        shifts = np.arange(per - 1, -1, -1, dtype=np.uint8) * depth
-        unpacked = (rows[:, :, None] >> shifts) & ((1 << depth) - 1)
-        samples = unpacked.reshape(h, stride * per)[:, :w]
-        if ctype == 0:  # grey scaled to 8 bits
-            samples = (samples.astype(np.uint32) * (255 // ((1 << depth) - 1))).astype(np.uint8)
+    bpp = max(1, bits // 8)
+    try:
+        stream = np.frombuffer(zlib.decompress(b"".join(idat)), np.uint8)
+    except zlib.error as e:
+        raise ValueError(f"corrupt PNG image data: {e}") from None
+    samples = np.zeros((h, w, ch), np.uint8)
+    passes = _ADAM7 if interlace else ((0, 0, 1, 1),)
+    pos = 0
+    for x0, y0, dx, dy in passes:
+        pw, ph = -(-(w - x0) // dx) if w > x0 else 0, -(-(h - y0) // dy) if h > y0 else 0
+        if pw == 0 or ph == 0:
+            continue  # an empty pass has no scanlines, not even filter bytes
+        stride = (pw * bits + 7) // 8
+        raw = stream[pos:pos + ph * (1 + stride)]
+        if raw.size < ph * (1 + stride):
+            raise ValueError("corrupt PNG: image data too short")
+        pos += ph * (1 + stride)
+        rows = _unfilter(raw.reshape(ph, 1 + stride), ph, stride, bpp)
+        samples[y0::dy, x0::dx] = _png_samples(rows, pw, ph, ch, depth, ctype)
     rgba = np.ones((h, w, 4), np.float32)
     if ctype == 3:
         if palette is None:
             raise ValueError("palette PNG without PLTE")
-        idx = samples.reshape(h, w).astype(np.int64)
+        idx = samples[..., 0].astype(np.int64)
         if idx.max(initial=0) >= len(palette):
             raise ValueError("PNG palette index out of range")
         rgba[..., :3] = palette[idx].astype(np.float32) / 255.0
@@ -193,7 +220,7 @@ def decode_png(data: bytes) -> np.ndarray:
             alpha[:min(len(trns), len(palette))] = trns[:len(palette)]
             rgba[..., 3] = alpha[idx].astype(np.float32) / 255.0
         return rgba
-    px = samples.reshape(h, w, ch).astype(np.float32) / 255.0
+    px = samples.astype(np.float32) / 255.0
     if ch in (1, 2):
         rgba[..., :3] = px[..., :1]
     else:

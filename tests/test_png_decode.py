@@ -1,7 +1,7 @@
 """The PNG texture decoder (sparkle_gb300.gltf.decode_png) on files built here byte by byte from the PNG
 specification: every row filter (None, Sub, Up, Average, Paeth), palette images with tRNS alpha, 16-bit
-samples (high byte kept, as the reference's loader reduces 16-bit images), 1-bit grey, grey + alpha, and the
-refusal of interlaced files."""
+samples (high byte kept, as the reference's loader reduces 16-bit images), 1-bit grey, grey + alpha,
+Adam7-interlaced files, and the library's own PNG writer."""
 import struct
 import time
 import zlib
@@ -92,9 +92,25 @@ def test_grey_1bit_and_grey_alpha():
     np.testing.assert_array_equal(np.rint(got[..., 3] * 255).astype(np.uint8), ga[..., 1])
 
 
-def test_interlaced_is_refused():
+def test_adam7_interlaced():
+    """Seven passes of sub-images (x0, y0, dx, dy), each filtered on its own; empty passes carry no bytes."""
+    adam7 = ((0, 0, 8, 8), (4, 0, 8, 8), (0, 4, 4, 8), (2, 0, 4, 4), (0, 2, 2, 4), (1, 0, 2, 2), (0, 1, 1, 2))
+    for h, w in ((9, 13), (3, 2), (1, 1), (16, 17)):
+        img = np.random.default_rng(h * w).integers(0, 256, (h, w, 4), np.uint8)
+        stream = b""
+        for k, (x0, y0, dx, dy) in enumerate(adam7):
+            sub = img[y0::dy, x0::dx]
+            if sub.size == 0:
+                continue
+            stream += _filter_rows([sub[y].tobytes() for y in range(sub.shape[0])], 4, (k % 5, 4, 1))
+        png = (b"\x89PNG\r\n\x1a\n" + _chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 6, 0, 0, 1)) +
+               _chunk(b"IDAT", zlib.compress(stream)) + _chunk(b"IEND", b""))
+        np.testing.assert_array_equal(np.rint(decode_png(png) * 255).astype(np.uint8), img, err_msg=f"{h}x{w}")
+
+
+def test_truncated_data_is_refused():
     with pytest.raises(ValueError):
-        decode_png(make_png(2, 2, 6, 8, [bytes(8), bytes(8)], 4, interlace=1))
+        decode_png(make_png(2, 2, 6, 8, [bytes(8), bytes(8)], 4, interlace=1)[:-40] + _chunk(b"IEND", b""))
 
 
 def test_large_texture_decodes_in_seconds():
