@@ -428,15 +428,25 @@ spk_status spk_read_batch(spk_ctx *ctx, uint32_t index, float *hdr_rgba, uint16_
  * spk_set_camera must have been called); render time does not.
  *
  * The caller owns the outputs: `d_hdr_rgba` (width*height float4, device memory) is the accumulated frame
- * buffer and is read and written (it is cleared when the context is dirty, as spk_render clears its own);
- * `d_rgba16f` (width*height half4, device memory) receives the tonemapped image. The per-frame G-buffer and
- * the counters live in one file-scope device array sized for SPK_NOALLOC_MAX_PIXELS pixels (8 MB plus
- * 256 bytes, held by every GPU that loads the library until the process exits); larger configs return
- * SPK_ERR_INVALID_ARGUMENT. The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress), so make that first call before capturing any stream. Every call on a device
- * shares the one array and it keeps the last call's contents: calls that overlap on the GPU (two contexts,
- * two streams) race on it and must be serialised by the caller. Asynchronous like spk_render;
- * spk_get_stats does not report these calls. */
+ * buffer and is read and written; `d_rgba16f` (width*height half4, device memory) receives the tonemapped
+ * image. The context's sample bookkeeping follows one frame buffer at a time: a call whose `d_hdr_rgba`
+ * differs from the previous call's (or that follows spk_render) clears it and starts the accumulation
+ * over, as a dirty context does; and after such calls spk_render starts over in the context's own buffer,
+ * while spk_read_framebuffer, spk_read_rgba8, spk_save_image and spk_save_checkpoint return
+ * SPK_ERR_NOT_READY (the context's own buffer holds none of those frames) until spk_render or
+ * spk_load_checkpoint runs.
+ *
+ * The per-frame G-buffer and the counters live in one file-scope device array sized for
+ * SPK_NOALLOC_MAX_PIXELS pixels (8 MB plus 256 bytes, held by every GPU that loads the library until the
+ * process exits); larger configs return SPK_ERR_INVALID_ARGUMENT. The first call on a device, and the
+ * first after that device's context was torn down and created again (cudaDeviceReset), looks up the
+ * array's device address (cudaGetSymbolAddress), so make that call before capturing any stream. Every
+ * call on a device shares the one array and it keeps the last call's contents (the counters are cleared
+ * by each call): calls that overlap on the GPU (two contexts, two streams) race on it and must be
+ * serialised by the caller. Asynchronous like spk_render. spk_get_stats after it waits for the stream and
+ * reports the call's counters -- rays, paths, launches and spk_stats.error_flags (walk stack bound and
+ * iteration budget) -- read from the shared array, so read them before another context's call on the
+ * same device; it records no events, so device_ms and trace_kernel_ms are 0. */
 spk_status spk_render_noalloc(spk_ctx *ctx, uint32_t num_frames, void *d_hdr_rgba, void *d_rgba16f);
 
 /* ------------------------------------------------------------------------------------------------ */

@@ -4,6 +4,7 @@
 // the resident scene (SceneRenderProxy's BVHs, flattened for the device), the camera and config snapshot,
 // the frame buffers, and the sample bookkeeping of CameraRenderProxy (CameraRenderProxy.cpp:66-75) and
 // CPURenderer::dispatched_sample_count_ (CPURenderer.cpp:128-137, 206-207).
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
@@ -184,11 +185,15 @@ struct spk_ctx {
     // CameraRenderProxy / CPURenderer sample bookkeeping
     uint32_t cumulated = 0, pending = 0, dispatched = 0;
     bool dirty = true;
+    // The frame buffer that bookkeeping belongs to: nullptr = fb; otherwise the caller's buffer that
+    // spk_render_noalloc accumulated into last. Rendering into another buffer restarts the accumulation.
+    const void *accum_target = nullptr;
     std::vector<float> frame_weights;    // multi-frame wavefront: per-frame moving-average weight
     std::vector<uint32_t> frame_seeds;   // multi-frame wavefront: per-frame seed base
 
     // counters
     Counters *counters = nullptr;  // device
+    const Counters *noalloc_counters = nullptr;  // set when the last call was spk_render_noalloc: its counters
     spk_stats last{};
     bool stats_pending = false;
     uint32_t launches_in_call = 0;
@@ -209,6 +214,16 @@ spk_status fail(spk_ctx *ctx, spk_status code, const char *fmt, ...) {
 spk_status cuda_fail(spk_ctx *ctx, cudaError_t e, const char *what) {
     return fail(ctx, e == cudaErrorMemoryAllocation ? SPK_ERR_OUT_OF_MEMORY : SPK_ERR_CUDA, "%s: %s", what,
                 cudaGetErrorString(e));
+}
+
+// The context's own frame buffers hold the accumulation unless the last frames went into a caller's
+// buffer (spk_render_noalloc); reading or saving them then would return frames the counts do not describe.
+spk_status require_own_buffers(spk_ctx *ctx) {
+    if (ctx->accum_target)
+        return fail(ctx, SPK_ERR_NOT_READY,
+                    "the last frames were rendered into the caller's buffers by spk_render_noalloc; the context's "
+                    "frame buffer holds none of them (spk_render restarts it)");
+    return SPK_OK;
 }
 
 template <class T>
@@ -1356,6 +1371,13 @@ static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
     const size_t launches_per_frame = wavefront ? ctx->cfg.bounce : 1;
     if ((e = prepare_events(ctx, static_cast<size_t>(num_frames) * launches_per_frame + 16)) != cudaSuccess)
         return cuda_fail(ctx, e, "event pool");
+    if (ctx->accum_target) {
+        // The last frames went into a caller's buffer (spk_render_noalloc): fb holds none of them, so the
+        // accumulation starts over here.
+        ctx->dirty = true;
+        ctx->accum_target = nullptr;
+    }
+    ctx->noalloc_counters = nullptr;
     ctx->launches_in_call = 0;
     if ((e = cudaMemsetAsync(ctx->counters, 0, sizeof(Counters), ctx->stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "counter reset");
@@ -1472,6 +1494,7 @@ spk_status spk_render(spk_ctx *ctx, uint32_t num_frames) try {
 spk_status spk_read_framebuffer(spk_ctx *ctx, float *hdr_rgba, uint16_t *rgba16f) {
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "no frame buffer");
+    if (const spk_status st = require_own_buffers(ctx)) return st;
     cudaSetDevice(ctx->device);
     cudaError_t e;
     if (hdr_rgba &&
@@ -1515,6 +1538,7 @@ spk_status spk_save_checkpoint(spk_ctx *ctx, void *buffer, uint64_t size) {
     if (!ctx || !buffer) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "no frame buffer");
     if (size < checkpoint_bytes(ctx)) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "checkpoint buffer too small");
+    if (const spk_status st = require_own_buffers(ctx)) return st;
     cudaSetDevice(ctx->device);
     CheckpointHeader h{};
     std::memcpy(h.magic, kCheckpointMagic, 8);
@@ -1562,6 +1586,7 @@ spk_status spk_load_checkpoint(spk_ctx *ctx, const void *buffer, uint64_t size) 
     ctx->pending = h.pending;
     ctx->dispatched = h.dispatched;
     ctx->dirty = h.dirty != 0;  // the accumulation continues from the saved state, not from a cleared one
+    ctx->accum_target = nullptr;
     return SPK_OK;
 }
 
@@ -1700,6 +1725,7 @@ spk_status spk_debug_walk_budget(spk_ctx *ctx, uint32_t steps) {
 spk_status spk_read_rgba8(spk_ctx *ctx, uint8_t *rgba8) try {
     if (!ctx || !rgba8) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "no frame buffer");
+    if (const spk_status st = require_own_buffers(ctx)) return st;
     cudaSetDevice(ctx->device);
     cudaError_t e;
     if (!ctx->rgba8_tables.ptr) {
@@ -1728,6 +1754,7 @@ spk_status spk_save_image(spk_ctx *ctx, const char *path, uint32_t format) try {
     if (!ctx || !path || !*path) return SPK_ERR_INVALID_ARGUMENT;
     if (!ctx->has_config) return fail(ctx, SPK_ERR_NOT_READY, "no frame buffer");
     if (format > SPK_IMAGE_EXR) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "unknown image format %u", format);
+    if (const spk_status st = require_own_buffers(ctx)) return st;
     const uint32_t w = ctx->cfg.width, h = ctx->cfg.height;
     const uint64_t n = static_cast<uint64_t>(w) * h;
     std::vector<uint8_t> bytes;
@@ -1842,6 +1869,7 @@ static spk_status trace_impl(spk_ctx *ctx, const void *d_rays, uint64_t num_rays
     cudaEventRecord(ctx->ev_stop, ctx->stream);
     ctx->launches_in_call = 1;
     ctx->last = spk_stats{};
+    ctx->noalloc_counters = nullptr;
     ctx->stats_pending = true;
     return SPK_OK;
 }
@@ -1901,13 +1929,23 @@ spk_status spk_get_stats(spk_ctx *ctx, spk_stats *out) {
         cudaError_t e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
         Counters c{};
-        if ((e = cudaMemcpy(&c, ctx->counters, sizeof(Counters), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        const Counters *src = ctx->noalloc_counters ? ctx->noalloc_counters : ctx->counters;
+        if ((e = cudaMemcpy(&c, src, sizeof(Counters), cudaMemcpyDeviceToHost)) != cudaSuccess)
             return cuda_fail(ctx, e, "counter read");
         ctx->last.extension_rays = c.extension_rays;
         ctx->last.shadow_rays = c.shadow_rays;
         ctx->last.error_flags = c.error_flags;
         ctx->last.node_visits = c.node_visits;
         ctx->last.triangle_tests = c.tri_tests;
+        ctx->stats_pending = false;
+        if (ctx->noalloc_counters) {  // no events are recorded by spk_render_noalloc: counters only
+            ctx->last.kernel_launches = ctx->launches_in_call;
+            ctx->last.bvh_nodes = ctx->bvh_nodes;
+            ctx->last.bvh_bytes = ctx->bvh_bytes;
+            *out = ctx->last;
+            out->blas_reused = ctx->blas_reused;
+            return SPK_OK;
+        }
         float ms = 0.f;
         cudaEventElapsedTime(&ms, ctx->ev_start, ctx->ev_stop);
         ctx->last.device_ms = ms;
@@ -2060,6 +2098,7 @@ spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t 
     ctx->launches_in_call = launches;
     ctx->last = spk_stats{};
     ctx->last.paths = items;
+    ctx->noalloc_counters = nullptr;
     ctx->stats_pending = true;
     if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
     return SPK_OK;
@@ -2153,26 +2192,62 @@ __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocGbufferBytes +
 
 constexpr int kNoallocMaxDevices = 64;
 std::mutex g_noalloc_mutex;
-void *g_noalloc_address[kNoallocMaxDevices] = {};
+struct NoallocAddress {
+    unsigned long long context_id = 0;  // the CUDA context the address belongs to (0: none looked up)
+    void *address = nullptr;
+};
+NoallocAddress g_noalloc_address[kNoallocMaxDevices];
 
-// Device address of g_noalloc_scratch on `device` (current), looked up once per device. The host-side
-// name of the array is only a stand-in and must never be handed to a kernel.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+
+// The current CUDA context's unique id (cuCtxGetId, through the driver entry point: no libcuda link
+// dependency). A device's primary context that was torn down (cudaDeviceReset) and created again gets a
+// new id, and its module -- with g_noalloc_scratch -- is loaded again at another address.
+cudaError_t current_context_id(unsigned long long *id) {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr, *q = nullptr;
+        cudaDriverEntryPointQueryResult r1, r2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &r1) == cudaSuccess &&
+            r1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &q, 12000, cudaEnableDefault, &r2) == cudaSuccess &&
+            r2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<CtxGetCurrentFn>(p);
+            get_id = reinterpret_cast<CtxGetIdFn>(q);
+        }
+    });
+    if (!get_current || !get_id) return cudaErrorNotSupported;
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS || !c || get_id(c, id) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+    return cudaSuccess;
+}
+
+// Device address of g_noalloc_scratch on `device` (current, its context initialised), looked up once per
+// device and context. The host-side name of the array is only a stand-in and must never be handed to a
+// kernel.
 cudaError_t noalloc_scratch(int device, unsigned char **out) {
     if (device < 0 || device >= kNoallocMaxDevices) return cudaErrorInvalidDevice;
+    unsigned long long id = 0;
+    cudaError_t e = current_context_id(&id);
+    if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_address[device]) {
+    NoallocAddress &slot = g_noalloc_address[device];
+    if (slot.context_id != id || !slot.address) {
         void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_noalloc_address[device] = p;
+        if ((e = cudaGetSymbolAddress(&p, g_noalloc_scratch)) != cudaSuccess) return e;
+        slot.address = p;
+        slot.context_id = id;
     }
-    *out = static_cast<unsigned char *>(g_noalloc_address[device]);
+    *out = static_cast<unsigned char *>(slot.address);
     return cudaSuccess;
 }
 
 }  // namespace
 
-extern "C" spk_status spk_render_noalloc(spk_ctx *ctx, uint32_t num_frames, void *d_hdr_rgba, void *d_rgba16f) {
+extern "C" spk_status spk_render_noalloc(spk_ctx *ctx, uint32_t num_frames, void *d_hdr_rgba, void *d_rgba16f) try {
     if (!ctx) return SPK_ERR_INVALID_ARGUMENT;
     if (!d_hdr_rgba || !d_rgba16f) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "null output buffer");
     if (!ctx->has_scene || !ctx->has_config || !ctx->has_camera)
@@ -2191,10 +2266,21 @@ extern "C" spk_status spk_render_noalloc(spk_ctx *ctx, uint32_t num_frames, void
     auto *counters = reinterpret_cast<Counters *>(scratch + kNoallocGbufferBytes);
     FrameBuffers fbuf{gcolor, gnormal, static_cast<float4 *>(d_hdr_rgba), static_cast<ushort4 *>(d_rgba16f),
                       ctx->cfg.width, ctx->cfg.height};
+    // The sample bookkeeping belongs to one frame buffer: frames accumulated so far in another one (the
+    // context's own, or another caller buffer) are not in this one, so it starts over.
+    if (ctx->accum_target != d_hdr_rgba) {
+        ctx->dirty = true;
+        ctx->accum_target = d_hdr_rgba;
+    }
     // The array keeps the previous call's contents; only the counters must start at zero (the G-buffer is
     // fully written by every frame before it is read).
     if ((e = cudaMemsetAsync(counters, 0, sizeof(Counters), ctx->stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "counter reset");
+    ctx->noalloc_counters = counters;
+    ctx->launches_in_call = 0;
+    ctx->last = spk_stats{};
+    ctx->last.paths = static_cast<uint64_t>(num_frames) * npix;
+    ctx->stats_pending = true;
     for (uint32_t f = 0; f < num_frames; ++f) {
         // The same per-frame bookkeeping as spk_render (CameraRenderProxy.cpp:66-75, CPURenderer.cpp:128-137).
         if (ctx->dirty) {
@@ -2217,8 +2303,13 @@ extern "C" spk_status spk_render_noalloc(spk_ctx *ctx, uint32_t num_frames, void
         const float mavg = static_cast<float>(ctx->cumulated) / static_cast<float>(ctx->cumulated + ctx->spp_eff);
         if ((e = launch_resolve(fbuf, mavg, ctx->cam.exposure, ctx->cfg.spatial_denoise, ctx->stream)) != cudaSuccess)
             return cuda_fail(ctx, e, "resolve launch");
+        ctx->launches_in_call += 2;
         ctx->dispatched += ctx->spp_eff;
         ctx->pending += ctx->spp_eff;
     }
     return SPK_OK;
+} catch (const std::bad_alloc &) {
+    return fail(ctx, SPK_ERR_OUT_OF_MEMORY, "host memory exhausted");
+} catch (const std::exception &ex) {
+    return fail(ctx, SPK_ERR_INTERNAL, "%s", ex.what());
 }
