@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define SPK_ABI_VERSION 2u
+#define SPK_ABI_VERSION 3u
 
 typedef int32_t spk_status;
 enum {
@@ -135,7 +135,10 @@ enum { SPK_KERNEL_AUTO = 0, SPK_KERNEL_MEGAKERNEL = 1, SPK_KERNEL_WAVEFRONT = 2 
  * the reference's Xoshiro128+ reseeded with j*W+i+frame_seed*W*H (Sampler.h:16-40,
  * CPURenderer.cpp:436-444), or xoshiro256** seeded from (seed, pixel index, frame). `enable_nee` turns on
  * next-event estimation (not part of the reference cpu pipeline). `kernel` selects the device
- * schedule; both schedules compute identical results. */
+ * schedule; both schedules compute identical results. `sample_offset` (0 in the reference) is the sample
+ * count a clear resets dispatched_sample_count_ to: the seed base of the first frame after it. Replica r of
+ * several that each render F frames of one view sets it to r * F * spp_eff, so the replicas together draw
+ * exactly the samples one renderer draws in N * F frames, under either generator. */
 typedef struct spk_config {
     uint32_t width;
     uint32_t height;
@@ -148,6 +151,7 @@ typedef struct spk_config {
     uint32_t seed;
     uint32_t debug_mode;
     uint32_t kernel;
+    uint32_t sample_offset;
 } spk_config;
 
 /* ------------------------------------------------------------------------------------------------ */

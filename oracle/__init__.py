@@ -34,6 +34,7 @@ def lib():
         L.or_renderer_create.argtypes = [vp, vp, vp]
         L.or_renderer_destroy.argtypes = [vp]
         L.or_render.argtypes = [vp, C.c_uint32, C.c_int32, C.c_int32, C.c_uint32, C.c_uint32]
+        L.or_render_rows.argtypes = [vp, C.c_uint32, C.c_int32, C.c_int32, C.c_uint32, C.c_uint32, C.c_uint32]
         L.or_read_framebuffer.argtypes = [vp, vp, vp]
         L.or_read_gbuffer.argtypes = [vp, vp, vp]
         L.or_guides.argtypes = [vp, vp, vp]
@@ -98,9 +99,10 @@ class OracleRenderer:
             lib().or_renderer_destroy(self.h)
             self.h = None
 
-    def render(self, frames: int = 1, traversal: int = FAITHFUL, threads: int = 0, rows=None):
+    def render(self, frames: int = 1, traversal: int = FAITHFUL, threads: int = 0, rows=None, row_step: int = 1):
+        """Renders `frames` frames; only rows range(*rows)[::row_step] when `rows` is given (timing samples)."""
         r0, r1 = (0, 0) if rows is None else rows
-        lib().or_render(self.h, frames, traversal, threads, r0, r1)
+        lib().or_render_rows(self.h, frames, traversal, threads, r0, r1, row_step)
 
     def framebuffer(self):
         w, h = self.config.width, self.config.height

@@ -5,7 +5,9 @@
 // Every function cites the reference lines it restates (paths relative to the Sparkle tree; a bare file
 // name lives under libraries/). PARITY UNPINNED against upstream: the reference does not build here
 // (thirdparty/bvh, Xoshiro-cpp and Eigen are empty submodules) and its tests hold no golden vectors for
-// this path; see oracle/README.md for what pins this file instead.
+// this path. What pins this file instead: an independent numpy / pure-Python restatement of the same
+// reference lines (tests/test_oracle.py) and the committed golden streams, hits and images it must keep
+// reproducing (tests/golden/).
 //
 // Floating-point conventions (compiled with -ffp-contract=off, no -ffast-math):
 //  * Eigen 3.x evaluates a fixed-size 3-term reduction (dot, squaredNorm, a row of a 3x3 product) as
@@ -1185,12 +1187,15 @@ PixelResult sample_pixel(const or_renderer &r, Rng &rng, float u, float v, bool 
 }
 
 // BasePass + RenderPixel (CPURenderer.cpp:398-450).
-void base_pass(or_renderer &r, bool pruned, int num_threads, uint32_t row_begin, uint32_t row_end) {
+// Rows row_begin, row_begin + row_step, ... below row_end (all rows: 0, h, 1).
+void base_pass(or_renderer &r, bool pruned, int num_threads, uint32_t row_begin, uint32_t row_end, uint32_t row_step) {
     const float pw = 1.f / static_cast<float>(r.w - 1);
     const float ph = 1.f / static_cast<float>(r.h - 1);
     const uint32_t frame_seed = r.dispatched;
+    const uint32_t num_rows = (row_end - row_begin + row_step - 1) / row_step;
     std::atomic<uint64_t> rays{0}, shadow{0}, ovf{0};
-    parallel_rows(row_begin, row_end, num_threads, [&](uint32_t j, int) {
+    parallel_rows(0, num_rows, num_threads, [&](uint32_t row, int) {
+        const uint32_t j = row_begin + row * row_step;
         uint64_t my_rays = 0, my_shadow = 0, my_ovf = 0;
         Rng rng;
         for (uint32_t i = 0; i < r.w; ++i) {
@@ -1209,7 +1214,7 @@ void base_pass(or_renderer &r, bool pruned, int num_threads, uint32_t row_begin,
     });
     r.ext_rays += rays.load();
     r.shadow_rays += shadow.load();
-    r.paths += static_cast<uint64_t>(row_end - row_begin) * r.w;
+    r.paths += static_cast<uint64_t>(num_rows) * r.w;
 }
 
 inline bool is_valid_px(const or_renderer &r, size_t k) { return r.gcolor[k].w > 0; }
@@ -1514,11 +1519,17 @@ void or_renderer_destroy(or_renderer *r) { delete r; }
 
 void or_render(or_renderer *r, uint32_t num_frames, int32_t traversal, int32_t num_threads, uint32_t row_begin,
                uint32_t row_end) {
+    or_render_rows(r, num_frames, traversal, num_threads, row_begin, row_end, 1);
+}
+
+void or_render_rows(or_renderer *r, uint32_t num_frames, int32_t traversal, int32_t num_threads, uint32_t row_begin,
+                    uint32_t row_end, uint32_t row_step) {
     if (!(row_end > row_begin)) {
         row_begin = 0;
         row_end = r->h;
     }
     row_end = std::min(row_end, r->h);
+    row_step = std::max(row_step, 1u);
     for (uint32_t f = 0; f < num_frames; ++f) {
         // CameraRenderProxy::Update sample bookkeeping (CameraRenderProxy.cpp:66-75)
         if (r->dirty) {
@@ -1531,9 +1542,9 @@ void or_render(or_renderer *r, uint32_t num_frames, int32_t traversal, int32_t n
         if (r->dirty) {
             for (auto &a : r->fb) a = V4{0, 0, 0, 0};
             r->dirty = false;
-            r->dispatched = 0;
+            r->dispatched = r->cfg.sample_offset;
         }
-        base_pass(*r, traversal == OR_TRAVERSAL_PRUNED, num_threads, row_begin, row_end);
+        base_pass(*r, traversal == OR_TRAVERSAL_PRUNED, num_threads, row_begin, row_end, row_step);
         denoise_and_tonemap(*r);
         r->dispatched += r->spp_eff;
         r->pending += r->spp_eff;

@@ -48,6 +48,10 @@ void or_renderer_destroy(or_renderer *r);
  * the other rows are left untouched and the accumulation bookkeeping still advances). */
 void or_render(or_renderer *r, uint32_t num_frames, int32_t traversal, int32_t num_threads, uint32_t row_begin,
                uint32_t row_end);
+/* As or_render over rows row_begin, row_begin + row_step, ... below row_end (timing samples spread over
+ * the image). */
+void or_render_rows(or_renderer *r, uint32_t num_frames, int32_t traversal, int32_t num_threads, uint32_t row_begin,
+                    uint32_t row_end, uint32_t row_step);
 void or_read_framebuffer(const or_renderer *r, float *hdr_rgba, uint16_t *rgba16f);
 /* Per-pixel G-buffer of the last frame: color (rgb, valid flag) and first-hit world normal. */
 void or_read_gbuffer(const or_renderer *r, float *color_rgba, float *world_normal);

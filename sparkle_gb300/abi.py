@@ -11,7 +11,7 @@ from typing import List, Optional
 
 import numpy as np
 
-SPK_ABI_VERSION = 2
+SPK_ABI_VERSION = 3
 SPK_INVALID_ID = 0xFFFFFFFF
 
 SPK_PRIM_MESH, SPK_PRIM_SPHERE = 0, 1
@@ -55,7 +55,7 @@ class spk_camera(C.Structure):
 class spk_config(C.Structure):
     _fields_ = [("width", _u32), ("height", _u32), ("spp", _u32), ("max_spp", _u32), ("bounce", _u32),
                 ("spatial_denoise", _u32), ("enable_nee", _u32), ("rng", _u32), ("seed", _u32),
-                ("debug_mode", _u32), ("kernel", _u32)]
+                ("debug_mode", _u32), ("kernel", _u32), ("sample_offset", _u32)]
 
 
 class spk_ray(C.Structure):
@@ -105,9 +105,9 @@ HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4"),
 
 def make_config(width: int, height: int, spp: int = 1, max_spp: int = 2048, bounce: int = 8,
                 spatial_denoise: bool = False, enable_nee: bool = False, rng: int = SPK_RNG_XOSHIRO128P,
-                seed: int = 0, kernel: int = SPK_KERNEL_AUTO) -> spk_config:
+                seed: int = 0, kernel: int = SPK_KERNEL_AUTO, sample_offset: int = 0) -> spk_config:
     return spk_config(width, height, spp, max_spp, bounce, int(spatial_denoise), int(enable_nee), rng, seed, 0,
-                      kernel)
+                      kernel, sample_offset)
 
 
 def affine_inverse(m: np.ndarray) -> np.ndarray:

@@ -1398,7 +1398,7 @@ static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
             if (ctx->dirty) {
                 clear = true;
                 ctx->dirty = false;
-                ctx->dispatched = 0;
+                ctx->dispatched = ctx->cfg.sample_offset;
             }
             ctx->frame_seeds[f] = ctx->dispatched;
             ctx->frame_weights[f] =
@@ -1448,7 +1448,7 @@ static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
             if ((e = cudaMemsetAsync(ctx->fb.ptr, 0, ctx->fb.count * sizeof(float4), ctx->stream)) != cudaSuccess)
                 return cuda_fail(ctx, e, "frame buffer clear");
             ctx->dirty = false;
-            ctx->dispatched = 0;
+            ctx->dispatched = ctx->cfg.sample_offset;
         }
         RenderParams p{ctx->dispatched, ctx->cfg.bounce, ctx->cfg.rng, ctx->cfg.seed, ctx->cfg.spatial_denoise,
                        ctx->cfg.enable_nee};
@@ -2293,7 +2293,7 @@ extern "C" spk_status spk_render_noalloc(spk_ctx *ctx, uint32_t num_frames, void
             if ((e = cudaMemsetAsync(d_hdr_rgba, 0, npix * sizeof(float4), ctx->stream)) != cudaSuccess)
                 return cuda_fail(ctx, e, "frame buffer clear");
             ctx->dirty = false;
-            ctx->dispatched = 0;
+            ctx->dispatched = ctx->cfg.sample_offset;
         }
         const RenderParams p{ctx->dispatched, ctx->cfg.bounce, ctx->cfg.rng, ctx->cfg.seed, ctx->cfg.spatial_denoise,
                              ctx->cfg.enable_nee};
