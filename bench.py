@@ -159,19 +159,44 @@ def ncu_issue_profile():
             "dram_throughput": round(float(dram.group(1)) / 100.0, 3), "source": "profiles/k_wf_extend_stress.md"}
 
 
-def cpu_sample(osc, camera, frames: int, rows: int, threads: int, traversal: int):
-    """Times the oracle (reference cpu pipeline restated, scene `osc` already built) on `rows` central rows
-    for `frames` frames; returns (Mrays/s, rays, seconds)."""
+# The CPU sample both CPU figures time (the reference arm's steps and the line's cpu_baseline): every
+# CPU_ROW_STEP-th row of the 1920x1080 frame (rows spread over the whole image, not a central band) for
+# CPU_FRAMES frames of 1 spp, i.e. 270 x 1920 x 4 = 2,073,600 path samples of the 132.7 M of one 64-spp step.
+CPU_ROW_STEP, CPU_FRAMES = 4, 4
+
+
+def cpu_sample_text(threads: int) -> str:
+    rows = len(range(0, HEIGHT, CPU_ROW_STEP))
+    return (f"{CPU_FRAMES} frames x every {CPU_ROW_STEP}th row ({rows} rows spread over the image) x {WIDTH} px of "
+            f"the same scene/config ({CPU_FRAMES * rows * WIDTH} of the {WIDTH * HEIGHT * SPP} path samples of a "
+            f"64-spp step; Mrays/s over the traced segments, which extrapolates to the step at the same rate), "
+            f"oracle restatement of the reference cpu path tracer, faithful traversal (no tmax shrink), "
+            f"{threads} threads")
+
+
+def cpu_sample(osc, camera, threads: int, traversal: int):
+    """Times the oracle (reference cpu pipeline restated, scene `osc` already built) on the CPU sample;
+    returns (Mrays/s, rays, seconds)."""
     import oracle
     from sparkle_gb300 import abi
     cfg = abi.make_config(WIDTH, HEIGHT, spp=1, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS, seed=0)
     r = oracle.OracleRenderer(osc, cfg, camera)
-    r0 = HEIGHT // 2 - rows // 2
     t0 = time.perf_counter()
-    r.render(frames, traversal=traversal, threads=threads, rows=(r0, r0 + rows))
+    r.render(CPU_FRAMES, traversal=traversal, threads=threads, rows=(0, HEIGHT), row_step=CPU_ROW_STEP)
     dt = time.perf_counter() - t0
     ext, shadow, paths = r.counts()
     return (ext + shadow) / dt / 1e6, ext + shadow, dt
+
+
+def cpu_rate(osc, camera, threads: int, traversal: int, repeats: int):
+    """One untimed sample, then `repeats` timed ones: (Mrays/s over them, rays, seconds)."""
+    cpu_sample(osc, camera, threads, traversal)
+    rays, secs = 0, 0.0
+    for _ in range(repeats):
+        _, n, dt = cpu_sample(osc, camera, threads, traversal)
+        rays += n
+        secs += dt
+    return rays / secs / 1e6, rays, secs
 
 
 def run_reference(args):
@@ -184,18 +209,15 @@ def run_reference(args):
     scene, cam_args = scenes.terrain_spheres(0)
     camera = scenes.make_camera(cam_args, WIDTH, HEIGHT)
     osc = oracle.OracleScene(scene)
-    rows = 540
     for _ in range(args.warmup):
-        cpu_sample(osc, camera, 1, rows, threads, oracle.FAITHFUL)
-    vals, rays_tot, t_tot = [], 0, 0.0
+        cpu_sample(osc, camera, threads, oracle.FAITHFUL)
+    rays_tot, t_tot = 0, 0.0
     for _ in range(args.steps):
-        v, n, dt = cpu_sample(osc, camera, 1, rows, threads, oracle.FAITHFUL)
-        vals.append(v)
+        _, n, dt = cpu_sample(osc, camera, threads, oracle.FAITHFUL)
         rays_tot += n
         t_tot += dt
     value = rays_tot / t_tot / 1e6
-    sample = (f"one 1-spp frame of {rows} central rows x {WIDTH} pixels per step (oracle restatement of the "
-              f"reference cpu path tracer, faithful traversal: no tmax shrink), {threads} threads")
+    sample = "per step: " + cpu_sample_text(threads)
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * t_tot / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -228,8 +250,11 @@ def run_ours(args):
     if args.tune:
         ctx.set_tuning(**parse_tune(args.tune))
     ctx.set_scene(scene)
+    # Replica `rank` renders samples rank*64 .. rank*64+63 of the view (same seed, its own sample offset): N
+    # replicas draw what one renderer draws in 64*N frames.
+    from sparkle_gb300 import replicas
     cfg = abi.make_config(WIDTH, HEIGHT, spp=1, max_spp=4096, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS,
-                          seed=rank, kernel=args.kernel)
+                          seed=0, kernel=args.kernel, sample_offset=replicas.replica_sample_offset(rank, SPP))
     ctx.set_config(cfg)
     ctx.set_camera(camera)
 
@@ -306,16 +331,15 @@ def run_ours(args):
         import oracle
         threads = os.cpu_count() or 1
         osc = oracle.OracleScene(scene)
-        v_f, n_f, dt_f = cpu_sample(osc, camera, 16, 270, threads, oracle.FAITHFUL)
-        v_p, n_p, dt_p = cpu_sample(osc, camera, 16, 270, threads, oracle.PRUNED)
+        v_f, n_f, dt_f = cpu_rate(osc, camera, threads, oracle.FAITHFUL, 4)
+        v_p, _, _ = cpu_rate(osc, camera, threads, oracle.PRUNED, 2)
         # the reference's own pool size: min(max_threads = 64, hardware threads) minus the main and render
         # threads it reserves (TaskDispatcher.cpp:18-20, AppFramework.cpp:129-130)
         ref_workers = max(1, min(64, threads) - 2)
-        v_w, _, _ = cpu_sample(osc, camera, 16, 270, ref_workers, oracle.FAITHFUL)
+        v_w, _, _ = cpu_rate(osc, camera, ref_workers, oracle.FAITHFUL, 2)
         cpu = {"value": round(v_f, 4), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"16 frames x 270 central rows x {WIDTH} px of the same scene/config, oracle restatement of "
-                         f"the reference cpu path tracer, faithful traversal (no tmax shrink): {n_f} rays in "
-                         f"{dt_f:.2f} s; pruned traversal: {v_p:.3f} Mrays/s",
+               "sample": f"4 repeats (after one untimed) of the reference arm's step, {cpu_sample_text(threads)}: "
+                         f"{n_f} rays in {dt_f:.2f} s; pruned traversal: {v_p:.3f} Mrays/s",
                "pruned_value": round(v_p, 4),
                "reference_workers": {"threads": ref_workers, "value": round(v_w, 4)}}
     line = {
