@@ -1,10 +1,14 @@
 """Batched requests (spk_set_scenes + spk_render_batch): each request of a batch over several resident
 scenes renders bit-identically to the same request rendered alone through spk_set_scene / spk_set_config /
-spk_render (frame buffer and tonemapped image), for both RNG policies, with and without NEE."""
+spk_render (frame buffer and tonemapped image), for both RNG policies, with and without NEE; and every
+request matches the CPU oracle's render of it (parity tolerances of tests/parity.py)."""
 import numpy as np
 import pytest
 
+import oracle
 from sparkle_gb300 import abi, native, scenes
+
+from parity import assert_image_parity, compare_images, oracle_image
 
 pytestmark = pytest.mark.gpu
 
@@ -38,10 +42,12 @@ def test_batch_matches_single_renders(three_scenes, rng, nee):
     assert st["paths"] == sum(w * h * spp for _, w, h, spp, _, _ in REQS)
     assert st["extension_rays"] > 0 and (st["shadow_rays"] > 0) == nee
     single = native.Context(0)
+    osc = [oracle.OracleScene(sc) for sc, _ in three_scenes]
     for k, (scene, w, h, spp, bounce, seed) in enumerate(REQS):
+        cfg = abi.make_config(w, h, spp=1, max_spp=4096, bounce=bounce, enable_nee=nee, rng=rng, seed=seed,
+                              kernel=abi.SPK_KERNEL_WAVEFRONT)
         single.set_scene(three_scenes[scene][0])
-        single.set_config(abi.make_config(w, h, spp=1, max_spp=4096, bounce=bounce, enable_nee=nee, rng=rng,
-                                          seed=seed, kernel=abi.SPK_KERNEL_WAVEFRONT))
+        single.set_config(cfg)
         single.set_camera(requests[k]["camera"])
         single.render(spp)
         ref_hdr, ref_out = single.framebuffer()
@@ -49,6 +55,11 @@ def test_batch_matches_single_renders(three_scenes, rng, nee):
         assert np.array_equal(hdr.view(np.uint32), ref_hdr.view(np.uint32)), k
         assert np.array_equal(out, ref_out), k
         assert np.isfinite(hdr).all()
+        o_hdr, o_out = oracle_image(three_scenes[scene][0], requests[k]["camera"], cfg, spp, osc=osc[scene])
+        # with more frames more pixels hold at least one diverged sample (each weighing 1/spp): the 70-spp
+        # request keeps >= 98.5% of its pixels within 1e-4 relative
+        assert_image_parity(compare_images(hdr, out, o_hdr, o_out), f"batch request {k} vs oracle",
+                            min_close=0.995 if spp <= 16 else 0.985)
     single.close()
     batch.close()
 

@@ -9,6 +9,8 @@ import pytest
 
 from sparkle_gb300 import abi, native, scenes
 
+from parity import assert_hits_match_oracle, assert_image_parity, compare_images, oracle_image
+
 pytestmark = pytest.mark.gpu
 
 
@@ -37,6 +39,8 @@ def test_device_build_hits_equal_host_build(ctx, small_terrain, width, leaf, bui
     got = ctx.trace(rays)
     assert ctx.stats()["error_flags"] == 0
     hits_equal(got, ref)
+    if width == 8 and leaf == 3:
+        assert_hits_match_oracle(got, scene, rays, f"device builder {builder} vs oracle")
     ctx.set_tuning(bvh_builder=0, bvh_width=8, bvh_leaf_size=3)
 
 
@@ -111,7 +115,9 @@ def test_device_built_render_equals_host_built(ctx, small_terrain):
         ctx.set_config(cfg)
         ctx.set_camera(camera)
         ctx.render(3)
-        out.append(ctx.framebuffer()[0])
-    assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
-    assert np.array_equal(out[0].view(np.uint32), out[2].view(np.uint32))
+        out.append(ctx.framebuffer())
+    assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32))
+    assert np.array_equal(out[0][0].view(np.uint32), out[2][0].view(np.uint32))
+    o_hdr, o_out = oracle_image(scene, camera, cfg, 3)
+    assert_image_parity(compare_images(out[1][0], out[1][1], o_hdr, o_out), "device-built render vs oracle")
     ctx.set_tuning(bvh_builder=0)

@@ -1,10 +1,12 @@
 """Incremental scene changes (spk_set_instances, spk_set_instance_transforms, spk_update_mesh) against a
-fresh spk_set_scene of the changed scene.
+fresh spk_set_scene of the changed scene, and against the CPU oracle on the changed scene.
 
 SceneRenderProxy::UpdateBVH rebuilds the TLAS on every primitive change and keeps each mesh's BLAS
 (SceneRenderProxy.cpp:269-297); here a deformed mesh keeps its tree too and the device refits it. Hits and
 images never depend on the tree's shape, so every update must give the same bits as building the changed
-scene from scratch; a refit with unchanged positions must reproduce the node array byte for byte.
+scene from scratch; a refit with unchanged positions must reproduce the node array byte for byte. The
+updated context's hits and images are also compared with the oracle's for the changed scene (parity
+tolerances of tests/parity.py).
 """
 import copy
 
@@ -12,6 +14,8 @@ import numpy as np
 import pytest
 
 from sparkle_gb300 import abi, native, scenes
+
+from parity import assert_hits_match_oracle, assert_image_parity, compare_images, oracle_image
 
 pytestmark = pytest.mark.gpu
 
@@ -28,7 +32,7 @@ def hits_equal(a, b):
         assert np.array_equal(a[f].view(np.uint32), b[f].view(np.uint32)), f
 
 
-def render(c, scene_cam, cfg, frames=3, scene=None):
+def render(c, scene_cam, cfg, frames=3, scene=None, with_image=False):
     sc, cam_args = scene_cam
     camera = scenes.make_camera(cam_args, cfg.width, cfg.height)
     if scene is not None:
@@ -37,7 +41,14 @@ def render(c, scene_cam, cfg, frames=3, scene=None):
     c.set_camera(camera)
     c.render(frames)
     assert c.stats()["error_flags"] == 0
-    return c.framebuffer()[0]
+    hdr, out = c.framebuffer()
+    return (hdr, out) if with_image else hdr
+
+
+def assert_render_matches_oracle(hdr, out, scene, cam_args, cfg, frames, label):
+    camera = scenes.make_camera(cam_args, cfg.width, cfg.height)
+    o_hdr, o_out = oracle_image(scene, camera, cfg, frames)
+    assert_image_parity(compare_images(hdr, out, o_hdr, o_out), label)
 
 
 def deform(positions, seed, amount):
@@ -74,11 +85,13 @@ def test_deformed_mesh_equals_fresh_build(ctx, small_terrain):
     got = ctx.trace(rays)
     hits_equal(got, ref)
     assert (got["prim"] != 0xFFFFFFFF).mean() > 0.2  # the rays do hit geometry
+    assert_hits_match_oracle(got, moved, rays, "refit vs oracle")
     # the refitted tree is a valid tree for the new geometry: same images as the fresh build
     cfg = abi.make_config(64, 48, spp=2, bounce=4, seed=3)
-    a = render(ctx, (scene, cam_args), cfg)
+    a, a_out = render(ctx, (scene, cam_args), cfg, with_image=True)
     b = render(fresh, (moved, cam_args), cfg)
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert_render_matches_oracle(a, a_out, moved, cam_args, cfg, 3, "refit render vs oracle")
     fresh.close()
 
 
@@ -115,13 +128,16 @@ def test_transforms_equal_fresh_build(ctx, small_terrain):
     fresh = native.Context(0)
     fresh.set_scene(moved)
     rays = scenes.random_rays(*moved.world_bounds(), 40_000, seed=6)
-    hits_equal(ctx.trace(rays), fresh.trace(rays))
+    got = ctx.trace(rays)
+    hits_equal(got, fresh.trace(rays))
+    assert_hits_match_oracle(got, moved, rays, "moved instances vs oracle")
     assert ctx.stats()["bvh_nodes"] == fresh.stats()["bvh_nodes"]
     assert np.array_equal(ctx.bvh_nodes(), fresh.bvh_nodes())  # same TLAS build from the same boxes
     cfg = abi.make_config(64, 48, spp=2, bounce=4, seed=2)
-    a = render(ctx, (scene, cam_args), cfg)
+    a, a_out = render(ctx, (scene, cam_args), cfg, with_image=True)
     b = render(fresh, (moved, cam_args), cfg)
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert_render_matches_oracle(a, a_out, moved, cam_args, cfg, 3, "moved instances render vs oracle")
     fresh.close()
 
 
@@ -142,10 +158,11 @@ def test_instance_list_changes_equal_fresh_build(ctx, cornell, nee):
     ctx.set_scene(scene)
     render(ctx, (scene, cam_args), cfg, frames=2)
     ctx.set_instances(changed.instances)
-    a = render(ctx, (scene, cam_args), cfg)
+    a, a_out = render(ctx, (scene, cam_args), cfg, with_image=True)
     fresh = native.Context(0)
     b = render(fresh, (changed, cam_args), cfg, scene=changed)
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert_render_matches_oracle(a, a_out, changed, cam_args, cfg, 3, f"instance list nee={nee} vs oracle")
     # the change cleared the accumulation: 3 frames after the update, not 5
     assert ctx.sample_counts()[0] == fresh.sample_counts()[0]
     fresh.close()
