@@ -10,7 +10,8 @@ cube with a baked sun). Rays = traced segments (extension + shadow).
 `--impl reference` times the reference's CPU path tracer (the restated oracle: the reference itself does not
 build here) on this machine's host cores over a bounded sample of the same workload.
 
-The line also carries `denoise`: the wall time to relMSE 0.01 / 0.003 at 1920x1080 on the same scene for
+The line also carries `nee`: the same workload with next-event estimation on, the occlusion rays in the
+wavefront's shadow stage and walked inline (`--no-nee` skips it); `denoise`: the wall time to relMSE 0.01 / 0.003 at 1920x1080 on the same scene for
 denoised low-spp rendering (the committed U-Net) vs plain path tracing, against a 4096-spp reference
 (`--no-denoise` skips it); and `batch`: 32 uneven render requests over 3 scenes in one batched wavefront
 against the same requests rendered one by one (`--no-batch` skips it, `--batch-autotune` adds a tuned run).
@@ -364,6 +365,8 @@ def run_ours(args):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if world == 1 and not args.no_nee:
+        line["nee"] = nee_metric(ctx, camera)
     if world == 1 and not args.no_denoise:
         line["denoise"] = denoise_metric(ctx)
     if world == 1 and not args.no_batch:
@@ -372,6 +375,37 @@ def run_ours(args):
         line["scene_update"] = scene_update_metric(scene, camera)
     print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def nee_metric(ctx, camera, steps: int = 3):
+    """The same workload with next-event estimation on (a light and a sky occlusion ray per diffuse vertex):
+    Mrays/s over extension + shadow rays by device time, with the occlusion rays in the wavefront's shadow
+    stage (persistent any-hit walk with lane refill, the default) and walked inline by the shade kernel."""
+    from sparkle_gb300 import abi
+    cfg = abi.make_config(WIDTH, HEIGHT, spp=1, max_spp=4096, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS,
+                          seed=0, enable_nee=True)
+    ctx.set_config(cfg)
+    out = {"spp": SPP, "steps": steps}
+    for name, stage in (("shadow_stage", 1), ("inline", 0)):
+        ctx.set_tuning(shadow_stage=stage)
+        ctx.set_camera(camera)
+        ctx.render(SPP)  # warm-up (allocations, graph capture)
+        ms = ext = shadow = 0.0
+        errors = 0
+        for _ in range(steps):
+            ctx.set_camera(camera)
+            ctx.render(SPP)
+            st = ctx.stats()
+            ms += st["device_ms"]
+            ext += st["extension_rays"]
+            shadow += st["shadow_rays"]
+            errors |= st["error_flags"]
+        out[name] = {"mrays_s": round((ext + shadow) / (ms * 1e3), 1), "ms_per_step": round(ms / steps, 2),
+                     "extension_rays_per_step": int(ext / steps), "shadow_rays_per_step": int(shadow / steps),
+                     "error_flags": errors}
+    ctx.set_tuning(shadow_stage=1)
+    out["speedup"] = round(out["shadow_stage"]["mrays_s"] / out["inline"]["mrays_s"], 3)
+    return out
 
 
 def scene_update_metric(scene, camera):
@@ -599,6 +633,7 @@ def main():
     ap.add_argument("--kernel", type=int, default=0, help="0 auto, 1 megakernel, 2 wavefront")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-denoise", action="store_true", help="skip the denoised-vs-plain time-to-relMSE leg")
+    ap.add_argument("--no-nee", action="store_true", help="skip the next-event-estimation leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-requests leg")
     ap.add_argument("--batch-autotune", action="store_true", help="autotune the batched leg's launch knobs")
     ap.add_argument("--no-scene-update", action="store_true", help="skip the scene build / incremental update leg")

@@ -220,6 +220,9 @@ typedef struct spk_tuning {
                                       of a 64-frame call at once, at most 2^27 paths, ~152 B of state each). More paths
                                       per extend launch spread each launch's tail (its last, longest walks) over more
                                       rays; spk_render(1) uses one path per pixel whatever the setting */
+    uint32_t shadow_stage;         /* wavefront NEE: 1 (default) queues the light and sky occlusion rays of each
+                                      light-sampling vertex for a persistent any-hit stage with lane refill, then adds
+                                      their radiance in order; 0 walks them inline in the shade kernel, one per thread */
 } spk_tuning;
 
 /* ------------------------------------------------------------------------------------------------ */

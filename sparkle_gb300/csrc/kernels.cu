@@ -19,7 +19,7 @@ __global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_trace(DevScene S, 
     TraceCounts tc;
     walk_persistent<kMode, kCount>(
         S, &counters->queue_counters[0], n, kFltMax, err, &tc,
-        [&](unsigned long long q, f3 &o, f3 &d) {
+        [&](unsigned long long q, f3 &o, f3 &d, float &) {
             const float *r = rays + q * 6;
             o = mk3(r[0], r[1], r[2]);
             d = mk3(r[3], r[4], r[5]);

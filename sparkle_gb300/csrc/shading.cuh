@@ -425,10 +425,24 @@ __device__ __forceinline__ f3 sky_eval(const DevScene &S, f3 d) {
 // cosine-weighted sky direction, each with an occlusion ray and the shader's power-heuristic weight
 // against the diffuse branch's cosine pdf. The estimator is the cpu BSDF's (base/pi * L * cos / pdf), so
 // NEE converges to the plain path tracer's image. Contributions are added to `color` in that order.
+//
+// nee_prepare draws the random numbers and computes both occlusion rays and the radiance each adds when
+// it is unoccluded; nee_direct walks the two rays inline and adds. The wavefront's shadow stage walks the
+// prepared rays in their own persistent kernel and adds the same contributions in the same order, so
+// both give the same bits.
 // ------------------------------------------------------------------------------------------------
-template <int kKind, bool kCount>
-__device__ __forceinline__ void nee_direct(const DevScene &S, Rng &rng, const Surface &surf, f3 base, f3 thr,
-                                           f3 &color, uint32_t &shadow_rays, uint32_t &err, TraceCounts *tc) {
+struct NeeRay {
+    f3 o, d;
+    float tmax;
+    f3 contrib;  // added to the path's colour when the ray is unoccluded
+    bool valid;  // false: no ray (no light / sky, or a back-facing sample)
+};
+
+template <int kKind>
+__device__ __forceinline__ void nee_prepare(const DevScene &S, Rng &rng, const Surface &surf, f3 base, f3 thr,
+                                            NeeRay &light, NeeRay &sky) {
+    light.valid = false;
+    sky.valid = false;
     if (S.num_lights > 0) {
         const float u0 = rng_unit<kKind>(rng), u1 = rng_unit<kKind>(rng), u2 = rng_unit<kKind>(rng);
         const float target = u0 * S.light_total;
@@ -457,14 +471,13 @@ __device__ __forceinline__ void nee_direct(const DevScene &S, Rng &rng, const Su
                 const float pdf_l = dist2 / (S.light_total * cos_l);
                 const float pdf_b = cos_s * kInvPi;
                 const float wl = mis_weight(pdf_l, pdf_b);
-                ++shadow_rays;
-                const f3 so = surf.location + w * kTolerance;
-                const float tmax = (dist - kTolerance) * (1.f - 1e-4f);
-                if (trace_ray<kTraceOcclusion, kCount>(S, so, w, tmax, err, tc).inst == kInvalid) {
-                    const float f = cos_s / pdf_l * wl * kInvPi;
-                    color = color + mk3(thr.x * base.x * L.emission[0] * f, thr.y * base.y * L.emission[1] * f,
-                                        thr.z * base.z * L.emission[2] * f);
-                }
+                light.o = surf.location + w * kTolerance;
+                light.d = w;
+                light.tmax = (dist - kTolerance) * (1.f - 1e-4f);
+                const float f = cos_s / pdf_l * wl * kInvPi;
+                light.contrib = mk3(thr.x * base.x * L.emission[0] * f, thr.y * base.y * L.emission[1] * f,
+                                    thr.z * base.z * L.emission[2] * f);
+                light.valid = true;
             }
         }
     }
@@ -478,14 +491,28 @@ __device__ __forceinline__ void nee_direct(const DevScene &S, Rng &rng, const Su
         const float pdf = z * kInvPi;
         if (pdf > 0.f) {
             const float wl = mis_weight(pdf, pdf);
-            ++shadow_rays;
-            const f3 so = surf.location + w * kTolerance;
-            if (trace_ray<kTraceOcclusion, kCount>(S, so, w, 1000.f, err, tc).inst == kInvalid) {
-                const f3 Ls = sky_eval(S, w);
-                const float f = z / pdf * wl * kInvPi;
-                color = color + mk3(thr.x * base.x * Ls.x * f, thr.y * base.y * Ls.y * f, thr.z * base.z * Ls.z * f);
-            }
+            sky.o = surf.location + w * kTolerance;
+            sky.d = w;
+            sky.tmax = 1000.f;
+            const f3 Ls = sky_eval(S, w);
+            const float f = z / pdf * wl * kInvPi;
+            sky.contrib = mk3(thr.x * base.x * Ls.x * f, thr.y * base.y * Ls.y * f, thr.z * base.z * Ls.z * f);
+            sky.valid = true;
         }
+    }
+}
+
+template <int kKind, bool kCount>
+__device__ __forceinline__ void nee_direct(const DevScene &S, Rng &rng, const Surface &surf, f3 base, f3 thr,
+                                           f3 &color, uint32_t &shadow_rays, uint32_t &err, TraceCounts *tc) {
+    NeeRay rays[2];
+    nee_prepare<kKind>(S, rng, surf, base, thr, rays[0], rays[1]);
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        if (!rays[k].valid) continue;
+        ++shadow_rays;
+        if (trace_ray<kTraceOcclusion, kCount>(S, rays[k].o, rays[k].d, rays[k].tmax, err, tc).inst == kInvalid)
+            color = color + rays[k].contrib;
     }
 }
 

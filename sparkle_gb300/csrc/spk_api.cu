@@ -1360,6 +1360,7 @@ static WfTuning wf_tuning(const spk_ctx *ctx) {
     t.material_sort = ctx->tuning.material_sort != 0;
     t.ray_sort = ctx->tuning.ray_sort != 0;
     t.slots_per_pixel = ctx->tuning.path_slots_per_pixel;
+    t.shadow_stage = ctx->tuning.shadow_stage != 0;
     return t;
 }
 
@@ -2140,6 +2141,7 @@ void spk_tuning_defaults(spk_tuning *out) {
     out->bvh_collapse = 0;
     out->bvh_builder = 0;
     out->path_slots_per_pixel = 64;
+    out->shadow_stage = 1;
 }
 
 spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
@@ -2156,6 +2158,7 @@ spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
     if (t->bvh_builder > 2) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "bvh_builder takes 0, 1 or 2");
     if (t->path_slots_per_pixel < 1 || t->path_slots_per_pixel > 64)
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "path_slots_per_pixel must be 1..64");
+    if (t->shadow_stage > 1) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "shadow_stage takes 0 or 1");
     ctx->tuning = *t;
     return SPK_OK;
 }

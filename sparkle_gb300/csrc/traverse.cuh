@@ -367,9 +367,10 @@ __device__ __forceinline__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd
 }
 
 // Persistent walk over a work list: each warp pulls batches of items from `cursor` and refills lanes whose
-// ray has finished once fewer than `kRefillLanes` lanes are still walking. `fetch(i, o, d)` loads item i's
-// ray and returns the TLAS root of its scene; `finish(i, result)` stores its result. Every lane of every
-// warp of the block must call this.
+// ray has finished once fewer than `kRefillLanes` lanes are still walking. `fetch(i, o, d, tmax)` loads item
+// i's ray (tmax starts at the call's `tmax`; an occlusion walk may lower it per ray) and returns the TLAS
+// root of its scene; `finish(i, result)` stores its result. Every lane of every warp of the block must call
+// this.
 constexpr int kRefillLanes = SPK_REFILL_LANES;
 
 template <int kMode, bool kCount, class Fetch, class Finish>
@@ -395,8 +396,9 @@ __device__ __forceinline__ void walk_persistent(const DevScene &S, unsigned long
                 if (q < n) {
                     item = q;
                     f3 o, d;
-                    const uint32_t root = fetch(q, o, d);
-                    w.init(S, root, o, d, tmax);
+                    float tm = tmax;
+                    const uint32_t root = fetch(q, o, d, tm);
+                    w.init(S, root, o, d, tm);
                     active = true;
                 }
             }

@@ -17,8 +17,11 @@ namespace spk {
 namespace {
 
 // queue_counters slots
-constexpr int kLen0 = 0;    // length of queue 0 (queue 1's length is slot 1)
-constexpr int kCursor = 2;  // pop cursor of the running persistent stage
+constexpr int kLen0 = 0;          // length of queue 0 (queue 1's length is slot 1)
+constexpr int kCursor = 2;        // pop cursor of the running persistent stage
+constexpr int kShadowLen = 4;     // occlusion rays queued by the iteration's shade stage
+constexpr int kNeeLen = 5;        // light-sampling vertices of the iteration's shade stage
+constexpr int kShadowCursor = 6;  // pop cursor of the shadow stage
 
 template <int kKind>
 __device__ __forceinline__ void load_rng(const uint4 *rng, uint32_t pid, Rng &r) {
@@ -54,6 +57,16 @@ __device__ __forceinline__ void queue_push(uint32_t *queue, unsigned long long *
     if (active) queue[base + __popc(mask & ((1u << lane) - 1u))] = value;
 }
 
+// Queues the occlusion rays a deferred light-sampling vertex prepared (bit k of `nee_rays`: ray k) and the
+// vertex itself, flagged when its path ended there. Every lane of the warp calls it.
+__device__ __forceinline__ void queue_nee(const WavefrontState &s, Counters *counters, uint32_t slot,
+                                          uint32_t nee_rays, bool ended) {
+    unsigned long long *qc = counters->queue_counters;
+    queue_push(s.shadow_queue, &qc[kShadowLen], 2u * slot, (nee_rays & 1u) != 0u);
+    queue_push(s.shadow_queue, &qc[kShadowLen], 2u * slot + 1u, (nee_rays & 2u) != 0u);
+    queue_push(s.nee_list, &qc[kNeeLen], slot | (ended ? 0x80000000u : 0u), nee_rays != 0u);
+}
+
 // RenderPixel's start of a sample (CPURenderer.cpp:398-406, 436-444): reseed, jitter, camera ray.
 template <int kKind>
 __device__ __forceinline__ void start_path(const DevCamera &cam, const RenderParams &p, const WavefrontState &s,
@@ -75,14 +88,21 @@ __device__ __forceinline__ void start_path(const DevCamera &cam, const RenderPar
     store_rng<kKind>(s.rng, pid, rng);
 }
 
+// Next-event estimation modes of the shading kernels.
+enum : int { kNeeOff = 0, kNeeInline = 1, kNeeDeferred = 2 };
+
 // One bounce of SamplePixel's loop body (CPURenderer.cpp:261-368) for path `pid` whose closest hit is
-// in s.hit: sky on a miss, emission, BSDF sample, throughput cut-off, Russian roulette, and (with `nee`)
+// in s.hit: sky on a miss, emission, BSDF sample, throughput cut-off, Russian roulette, and (with NEE)
 // next-event estimation at diffuse-branch vertices with MIS on the emission the BSDF rays collect.
+// kNeeInline walks the two occlusion rays here; kNeeDeferred stores them with their radiance for the
+// shadow stage and returns in `nee_rays` which were queued (bit k: ray k), the colour still without them.
 // Returns whether the path continues (the next ray is then in s.ray_o / s.ray_d).
-template <int kKind, bool kNee>
+template <int kKind, int kNee>
 __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontState &s, uint32_t pid,
-                                           uint32_t bounce, float4 *gnormal, uint32_t &shadow, uint32_t &err) {
-    constexpr bool nee = kNee;
+                                           uint32_t bounce, float4 *gnormal, uint32_t &shadow, uint32_t &err,
+                                           uint32_t &nee_rays) {
+    constexpr bool nee = kNee != kNeeOff;
+    nee_rays = 0u;
     bool alive = false;
     const float4 hit4 = s.hit[pid];
     const uint32_t inst = __float_as_uint(hit4.w);
@@ -118,8 +138,28 @@ __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontSta
                 sample_surface<kKind>(rng, mat, d, surf.normal, surf.tangent, next_dir, nee ? &dz : nullptr);
             float next_pdf = 0.f;
             if (dz >= 0.f) {
-                nee_direct<kKind, false>(S, rng, surf, mk3(mat.base[0], mat.base[1], mat.base[2]), thr, color,
-                                         shadow, err, nullptr);
+                const f3 base = mk3(mat.base[0], mat.base[1], mat.base[2]);
+                if (kNee == kNeeDeferred) {
+                    NeeRay r[2];
+                    nee_prepare<kKind>(S, rng, surf, base, thr, r[0], r[1]);
+                    if (r[0].valid || r[1].valid) {
+#pragma unroll
+                        for (int k = 0; k < 2; ++k) {
+                            const size_t e = 2 * static_cast<size_t>(pid) + k;
+                            if (r[k].valid) {
+                                s.shadow_o[e] = make_float4(r[k].o.x, r[k].o.y, r[k].o.z, r[k].tmax);
+                                s.shadow_d[e] = make_float4(r[k].d.x, r[k].d.y, r[k].d.z, 0.f);
+                                s.nee_contrib[e] = make_float4(r[k].contrib.x, r[k].contrib.y, r[k].contrib.z, 1.f);
+                                nee_rays |= 1u << k;
+                                ++shadow;
+                            } else {
+                                s.nee_contrib[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+                            }
+                        }
+                    }
+                } else {
+                    nee_direct<kKind, false>(S, rng, surf, base, thr, color, shadow, err, nullptr);
+                }
                 next_pdf = dz * kInvPi;
             }
             thr = cmul(thr, this_thr);
@@ -180,7 +220,7 @@ __global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_wf_extend(DevScene
     uint32_t pid = 0;
     walk_persistent<kTraceClosest, kCount>(
         S, &counters->queue_counters[kCursor], n, kFltMax, err, &tc,
-        [&](unsigned long long q, f3 &o, f3 &d) {
+        [&](unsigned long long q, f3 &o, f3 &d, float &) {
             pid = queue[q];
             const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
             o = mk3(o4.x, o4.y, o4.z);
@@ -200,7 +240,7 @@ __global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_wf_extend(DevScene
     if (err) atomicOr(&counters->error_flags, err);
 }
 
-template <int kKind, bool kNee>
+template <int kKind, int kNee>
 __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_wf_shade(DevScene S, FrameBuffers fb, RenderParams p, WavefrontState s,
                                                   int in_queue, uint32_t bounce, Counters *counters) {
     uint32_t shadow = 0, err = 0;
@@ -211,11 +251,13 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_wf_shade(DevScene
          q0 += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
         const unsigned long long q = q0 + threadIdx.x;
         bool alive = false;
-        uint32_t pid = 0;
+        uint32_t pid = 0, nee_rays = 0;
         if (q < n) {
             pid = queue[q];
-            alive = shade_path<kKind, kNee>(S, s, pid, bounce, p.spatial_denoise ? fb.gnormal : nullptr, shadow, err);
+            alive = shade_path<kKind, kNee>(S, s, pid, bounce, p.spatial_denoise ? fb.gnormal : nullptr, shadow, err,
+                                             nee_rays);
         }
+        if constexpr (kNee == kNeeDeferred) queue_nee(s, counters, pid, nee_rays, false);
         queue_push(s.queue[out_queue], &counters->queue_counters[out_queue], pid, alive && bounce + 1 < p.bounce);
     }
     warp_add_u64(&counters->shadow_rays, shadow);
@@ -284,7 +326,7 @@ __global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers
 
 // Shade one segment per live slot. A finished sample stores its clamped result (RenderPixel's 6.0 clamp,
 // CPURenderer.cpp:408) at its item, and the slot takes the next item from the global counter.
-template <int kKind, bool kNee>
+template <int kKind, int kNee>
 __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_mf_shade(DevScene S, DevCamera cam, FrameBuffers fb, RenderParams p,
                                                   WavefrontState s, int in_queue, uint32_t frame_base,
                                                   uint32_t total_items, Counters *counters) {
@@ -296,23 +338,25 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_mf_shade(DevScene
     for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
          q0 += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
         const unsigned long long q = q0 + threadIdx.x;
-        bool push = false, need = false;
-        uint32_t slot = 0;
+        bool push = false, need = false, alive = false;
+        uint32_t slot = 0, nee_rays = 0;
         if (q < n) {
             slot = queue[q];
             const uint32_t bounce = s.slot_state[slot];
-            const bool alive =
-                shade_path<kKind, kNee>(S, s, slot, bounce, nullptr, shadow, err) && bounce + 1 < p.bounce;
+            alive = shade_path<kKind, kNee>(S, s, slot, bounce, nullptr, shadow, err, nee_rays) && bounce + 1 < p.bounce;
             if (alive) {
                 s.slot_state[slot] = bounce + 1u;
                 push = true;
-            } else {
+            } else if (nee_rays == 0u) {
                 const float4 c = s.color[slot];
                 s.samples[s.slot_item[slot]] =
                     make_float4(clamp_sample(c.x), clamp_sample(c.y), clamp_sample(c.z), c.w);
                 need = true;
             }
+            // else: the path ended at a light-sampling vertex; the accumulate stage adds its NEE radiance,
+            // stores the sample and starts the slot's next item
         }
+        if constexpr (kNee == kNeeDeferred) queue_nee(s, counters, slot, nee_rays, !alive);
         // Warp-aggregated hand-out of new sample items to the lanes whose path ended.
         const uint32_t need_mask = __ballot_sync(0xFFFFFFFFu, need);
         if (need_mask) {
@@ -561,7 +605,7 @@ __global__ void __launch_bounds__(128) k_b_generate(DevScene S, BatchParams b, W
     }
 }
 
-template <int kKind, bool kNee>
+template <int kKind, int kNee>
 __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_b_shade(DevScene S, BatchParams b, WavefrontState s, int in_queue,
                                                  Counters *counters) {
     uint32_t shadow = 0, err = 0;
@@ -572,24 +616,24 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_b_shade(DevScene 
     for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
          q0 += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
         const unsigned long long q = q0 + threadIdx.x;
-        bool push = false, need = false;
-        uint32_t slot = 0;
+        bool push = false, need = false, alive = false;
+        uint32_t slot = 0, nee_rays = 0;
         if (q < n) {
             slot = queue[q];
             const DevRequest &R = b.reqs[s.slot_req[slot]];
             const DevScene Sv = scene_view(S, S.descs[R.scene]);
             const uint32_t bounce = s.slot_state[slot];
-            const bool alive =
-                shade_path<kKind, kNee>(Sv, s, slot, bounce, nullptr, shadow, err) && bounce + 1 < R.bounce;
+            alive = shade_path<kKind, kNee>(Sv, s, slot, bounce, nullptr, shadow, err, nee_rays) && bounce + 1 < R.bounce;
             if (alive) {
                 s.slot_state[slot] = bounce + 1u;
                 push = true;
-            } else {
+            } else if (nee_rays == 0u) {
                 const float4 c = s.color[slot];
                 s.samples[s.slot_item[slot]] = make_float4(clamp_sample(c.x), clamp_sample(c.y), clamp_sample(c.z), c.w);
                 need = true;
             }
         }
+        if constexpr (kNee == kNeeDeferred) queue_nee(s, counters, slot, nee_rays, !alive);
         const uint32_t need_mask = __ballot_sync(0xFFFFFFFFu, need);
         if (need_mask) {
             unsigned long long base = 0;
@@ -608,6 +652,90 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_b_shade(DevScene 
     }
     warp_add_u64(&counters->shadow_rays, shadow);
     if (err) atomicOr(&counters->error_flags, err);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Shadow stage of next-event estimation: a persistent occlusion walk over the rays the shade stage queued
+// (lane refill as in extend), then the in-order addition of the unoccluded radiance.
+// ------------------------------------------------------------------------------------------------
+template <bool kBatch>
+__global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_wf_shadow(DevScene S, WavefrontState s,
+                                                                       Counters *counters) {
+    uint32_t err = 0;
+    const unsigned long long n = counters->queue_counters[kShadowLen];
+    uint32_t e = 0;
+    walk_persistent<kTraceOcclusion, false>(
+        S, &counters->queue_counters[kShadowCursor], n, kFltMax, err, nullptr,
+        [&](unsigned long long q, f3 &o, f3 &d, float &tmax) {
+            e = s.shadow_queue[q];
+            const float4 o4 = s.shadow_o[e], d4 = s.shadow_d[e];
+            o = mk3(o4.x, o4.y, o4.z);
+            d = mk3(d4.x, d4.y, d4.z);
+            tmax = o4.w;
+            return kBatch ? s.slot_root[e >> 1] : S.tlas_root;
+        },
+        [&](unsigned long long, const TraceResult &h) {
+            if (h.inst == kInvalid) reinterpret_cast<float *>(s.nee_contrib + e)[3] = 2.f;
+        });
+    if (err) atomicOr(&counters->error_flags, err);
+}
+
+// Adds each light-sampling vertex's unoccluded radiance to its path's colour, light before sky (the order
+// nee_direct adds them in). kMode 0 (frame by frame): nothing else. kMode 1 (multi-frame) and 2 (batch):
+// a path that ended at the vertex stores its clamped sample and its slot starts the next item, as the
+// shade stage does for paths that end without pending radiance.
+template <int kKind, int kMode>
+__global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_nee_accumulate(DevCamera cam, FrameBuffers fb, RenderParams p,
+                                                                            DevScene S, BatchParams b, WavefrontState s,
+                                                                            int out_queue, uint32_t frame_base,
+                                                                            uint32_t total_items, Counters *counters) {
+    const unsigned long long n = counters->queue_counters[kNeeLen];
+    const uint32_t lane = threadIdx.x & 31u;
+    for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
+         q0 += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
+        const unsigned long long q = q0 + threadIdx.x;
+        bool push = false, need = false;
+        uint32_t slot = 0;
+        if (q < n) {
+            const uint32_t entry = s.nee_list[q];
+            slot = entry & 0x7FFFFFFFu;
+            const float4 c4 = s.color[slot];
+            f3 color = mk3(c4.x, c4.y, c4.z);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const float4 a = s.nee_contrib[2 * static_cast<size_t>(slot) + k];
+                if (a.w == 2.f) color = color + mk3(a.x, a.y, a.z);
+            }
+            s.color[slot] = make_float4(color.x, color.y, color.z, c4.w);
+            if (kMode != 0 && (entry >> 31)) {
+                s.samples[s.slot_item[slot]] =
+                    make_float4(clamp_sample(color.x), clamp_sample(color.y), clamp_sample(color.z), c4.w);
+                need = true;
+            }
+        }
+        if constexpr (kMode != 0) {
+            const uint32_t need_mask = __ballot_sync(0xFFFFFFFFu, need);
+            if (need_mask) {
+                unsigned long long base = 0;
+                if (lane == static_cast<uint32_t>(__ffs(need_mask) - 1))
+                    base = atomicAdd(&counters->queue_counters[kNextItem],
+                                     static_cast<unsigned long long>(__popc(need_mask)));
+                base = __shfl_sync(0xFFFFFFFFu, base, __ffs(need_mask) - 1);
+                if (need) {
+                    const unsigned long long item = base + __popc(need_mask & ((1u << lane) - 1u));
+                    if (kMode == 1 && item < total_items) {
+                        start_item<kKind>(cam, p, s, slot, static_cast<uint32_t>(item), fb.width, fb.height,
+                                          frame_base);
+                        push = true;
+                    } else if (kMode == 2 && item < b.total_items) {
+                        start_item_batch<kKind>(S, b, s, slot, item);
+                        push = true;
+                    }
+                }
+            }
+            queue_push(s.queue[out_queue], &counters->queue_counters[out_queue], slot, push);
+        }
+    }
 }
 
 // Per pixel of every request: fold its samples in frame order with DenoisePass's weights from a cleared
@@ -673,7 +801,71 @@ cudaError_t launch_extend(const DevScene &scene, const WavefrontState &s, int in
     return cudaSuccess;
 }
 
+int nee_mode(uint32_t enable_nee, const WfTuning &tuning) {
+    return !enable_nee ? kNeeOff : (tuning.shadow_stage ? kNeeDeferred : kNeeInline);
+}
+
+using WfShadeFn = void (*)(DevScene, FrameBuffers, RenderParams, WavefrontState, int, uint32_t, Counters *);
+WfShadeFn pick_wf_shade(uint32_t rng, int nee) {
+    if (rng == 0) return nee == kNeeOff ? k_wf_shade<0, kNeeOff> : nee == kNeeInline ? k_wf_shade<0, kNeeInline> : k_wf_shade<0, kNeeDeferred>;
+    return nee == kNeeOff ? k_wf_shade<1, kNeeOff> : nee == kNeeInline ? k_wf_shade<1, kNeeInline> : k_wf_shade<1, kNeeDeferred>;
+}
+
+using MfShadeFn = void (*)(DevScene, DevCamera, FrameBuffers, RenderParams, WavefrontState, int, uint32_t, uint32_t,
+                           Counters *);
+MfShadeFn pick_mf_shade(uint32_t rng, int nee) {
+    if (rng == 0) return nee == kNeeOff ? k_mf_shade<0, kNeeOff> : nee == kNeeInline ? k_mf_shade<0, kNeeInline> : k_mf_shade<0, kNeeDeferred>;
+    return nee == kNeeOff ? k_mf_shade<1, kNeeOff> : nee == kNeeInline ? k_mf_shade<1, kNeeInline> : k_mf_shade<1, kNeeDeferred>;
+}
+
+using BShadeFn = void (*)(DevScene, BatchParams, WavefrontState, int, Counters *);
+BShadeFn pick_b_shade(uint32_t rng, int nee) {
+    if (rng == 0) return nee == kNeeOff ? k_b_shade<0, kNeeOff> : nee == kNeeInline ? k_b_shade<0, kNeeInline> : k_b_shade<0, kNeeDeferred>;
+    return nee == kNeeOff ? k_b_shade<1, kNeeOff> : nee == kNeeInline ? k_b_shade<1, kNeeInline> : k_b_shade<1, kNeeDeferred>;
+}
+
+// The shadow stage of one iteration (deferred NEE): the occlusion walk, then the accumulation of mode
+// kMode (0 frame by frame, 1 multi-frame, 2 batch). Two launches.
+template <int kMode>
+void enqueue_shadow_stage(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf, const RenderParams &p,
+                          const BatchParams &b, const WavefrontState &s, uint32_t rng, int out_queue,
+                          uint32_t frame_base, uint32_t total_items, Counters *counters, unsigned walk_grid,
+                          unsigned shade_grid, cudaStream_t stream) {
+    k_wf_shadow<kMode == 2><<<walk_grid, 128, 0, stream>>>(scene, s, counters);
+    auto *acc = rng == 0 ? k_nee_accumulate<0, kMode> : k_nee_accumulate<1, kMode>;
+    acc<<<shade_grid, 128, 0, stream>>>(cam, fbuf, p, scene, b, s, out_queue, frame_base, total_items, counters);
+}
+
+// Resets the shadow stage's counters (queued rays, vertices, walk cursor) before a shade stage.
+cudaError_t reset_shadow_counters(Counters *counters, cudaStream_t stream) {
+    return cudaMemsetAsync(counters->queue_counters + kShadowLen, 0, 3 * sizeof(unsigned long long), stream);
+}
+
 }  // namespace
+
+cudaError_t wavefront_alloc_nee(WavefrontState &s) {
+    if (s.nee_capacity >= s.capacity && s.shadow_o) return cudaSuccess;
+    void *ptrs[] = {s.shadow_o, s.shadow_d, s.nee_contrib, s.shadow_queue, s.nee_list};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    s.shadow_o = s.shadow_d = s.nee_contrib = nullptr;
+    s.shadow_queue = s.nee_list = nullptr;
+    s.nee_capacity = 0;
+    const size_t n = s.capacity;
+    cudaError_t e;
+    if ((e = dmalloc(s.shadow_o, 2 * n)) != cudaSuccess || (e = dmalloc(s.shadow_d, 2 * n)) != cudaSuccess ||
+        (e = dmalloc(s.nee_contrib, 2 * n)) != cudaSuccess || (e = dmalloc(s.shadow_queue, 2 * n)) != cudaSuccess ||
+        (e = dmalloc(s.nee_list, n)) != cudaSuccess) {
+        void *got[] = {s.shadow_o, s.shadow_d, s.nee_contrib, s.shadow_queue, s.nee_list};
+        for (void *p : got)
+            if (p) cudaFree(p);
+        s.shadow_o = s.shadow_d = s.nee_contrib = nullptr;
+        s.shadow_queue = s.nee_list = nullptr;
+        return e;
+    }
+    s.nee_capacity = s.capacity;
+    return cudaSuccess;
+}
 
 cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
     wavefront_free(s);
@@ -702,7 +894,8 @@ void wavefront_free(WavefrontState &s) {
     void *ptrs[] = {s.ray_o,      s.ray_d,     s.thr,     s.color,        s.rng,        s.hit,
                     s.hit_face,   s.queue[0],  s.queue[1], s.sort_keys,   s.slot_state, s.slot_item,
                     s.samples,    s.frame_weight, s.frame_seed, s.prev_pdf, s.sort_hist, s.slot_req,
-                    s.slot_root,  s.sort_keys2};
+                    s.slot_root,  s.sort_keys2, s.shadow_o, s.shadow_d, s.nee_contrib, s.shadow_queue,
+                    s.nee_list};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s.host_len) cudaFreeHost(s.host_len);
@@ -727,6 +920,8 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
     if (s.capacity < npix) return cudaErrorInvalidValue;
     if ((tuning.ray_sort || tuning.material_sort) && !sort_buffers_ok(s)) return cudaErrorInvalidValue;
     cudaError_t e;
+    const int nee = nee_mode(p.enable_nee, tuning);
+    if (nee == kNeeDeferred && (e = wavefront_alloc_nee(s)) != cudaSuccess) return e;
     unsigned long long *qc = counters->queue_counters;
     if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
     const dim3 ggrid((fbuf.width + 15) / 16, (fbuf.height + 7) / 8);
@@ -753,10 +948,14 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
             ss = enqueue_material_sort(scene, se, in, counters, num_sms, stream);
             nl += 3;
         }
-        auto *shade = p.rng == 0 ? (p.enable_nee ? k_wf_shade<0, true> : k_wf_shade<0, false>)
-                                 : (p.enable_nee ? k_wf_shade<1, true> : k_wf_shade<1, false>);
-        shade<<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, ss, in, b, counters);
+        if (nee == kNeeDeferred && (e = reset_shadow_counters(counters, stream)) != cudaSuccess) return e;
+        pick_wf_shade(p.rng, nee)<<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, ss, in, b, counters);
         ++nl;
+        if (nee == kNeeDeferred) {
+            enqueue_shadow_stage<0>(scene, cam, fbuf, p, BatchParams{}, ss, p.rng, out, 0u, 0u, counters, extend_grid,
+                                    shade_blocks, stream);
+            nl += 2;
+        }
     }
     k_wf_finish<<<(npix + 255) / 256, 256, 0, stream>>>(fbuf, s);
     ++nl;
@@ -781,6 +980,8 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
     if (s.capacity < npix || num_frames == 0 || p.bounce == 0) return cudaErrorInvalidValue;
     if ((tuning.ray_sort || tuning.material_sort) && !sort_buffers_ok(s)) return cudaErrorInvalidValue;
     cudaError_t e;
+    const int nee = nee_mode(p.enable_nee, tuning);
+    if (nee == kNeeDeferred && (e = wavefront_alloc_nee(s)) != cudaSuccess) return e;
     if (s.frame_capacity < num_frames) {
         if (s.frame_weight) cudaFree(s.frame_weight);
         if (s.frame_seed) cudaFree(s.frame_seed);
@@ -836,9 +1037,12 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                     return ce;
                 const WavefrontState ss =
                     tuning.material_sort ? enqueue_material_sort(scene, se, in, counters, num_sms, stream) : se;
-                auto *shade = p.rng == 0 ? (p.enable_nee ? k_mf_shade<0, true> : k_mf_shade<0, false>)
-                                         : (p.enable_nee ? k_mf_shade<1, true> : k_mf_shade<1, false>);
-                shade<<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, ss, in, f0, total_items, counters);
+                if (nee == kNeeDeferred && (ce = reset_shadow_counters(counters, stream)) != cudaSuccess) return ce;
+                pick_mf_shade(p.rng, nee)<<<shade_blocks, 128, 0, stream>>>(scene, cam, fbuf, p, ss, in, f0,
+                                                                            total_items, counters);
+                if (nee == kNeeDeferred)
+                    enqueue_shadow_stage<1>(scene, cam, fbuf, p, BatchParams{}, ss, p.rng, out, f0, total_items,
+                                            counters, extend_grid, shade_blocks, stream);
             }
             return cudaGetLastError();
         };
@@ -856,7 +1060,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 uint32_t f0, total_items, count, num_sms;
                 Counters *counters;
                 cudaStream_t stream;
-                unsigned extend_grid, shade_grid, material_sort, ray_sort;
+                unsigned extend_grid, shade_grid, material_sort, ray_sort, nee_mode;
             } key;
             std::memset(static_cast<void *>(&key), 0, sizeof(key));  // padding too: the key is compared bytewise
             key.scene = scene;
@@ -874,6 +1078,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
             key.shade_grid = shade_blocks;
             key.material_sort = tuning.material_sort;
             key.ray_sort = tuning.ray_sort;
+            key.nee_mode = static_cast<unsigned>(nee);
             const auto *kb = reinterpret_cast<const unsigned char *>(&key);
             graph_ev.pairs = graph->events;
             graph_ev.capacity = static_cast<int>(kChunk);
@@ -932,7 +1137,8 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 return e;
             }
             iter += kChunk;
-            nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u)) * kChunk;
+            nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
+                   (nee == kNeeDeferred ? 2u : 0u)) * kChunk;
             if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
                 cudaSuccess)
                 return e;
@@ -966,6 +1172,8 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
     if ((tuning.ray_sort || tuning.material_sort) && !sort_buffers_ok(s)) return cudaErrorInvalidValue;
     uint32_t nl = 0;
     cudaError_t e;
+    const int nee = nee_mode(b.enable_nee, tuning);
+    if (nee == kNeeDeferred && (e = wavefront_alloc_nee(s)) != cudaSuccess) return e;
     unsigned long long *qc = counters->queue_counters;
     const unsigned shade_blocks = static_cast<unsigned>(num_sms) * tuning.shade_blocks_per_sm;
     const unsigned extend_grid = extend_blocks(num_sms, tuning.extend_blocks_per_sm);
@@ -983,8 +1191,7 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
     // total_items * 64 iterations (bounce < 64 in practice) is a loose guard against a runaway loop.
     const unsigned long long max_iters = b.total_items * 64ull + kChunk;
     unsigned long long iter = 0;
-    auto *shade = b.rng == 0 ? (b.enable_nee ? k_b_shade<0, true> : k_b_shade<0, false>)
-                             : (b.enable_nee ? k_b_shade<1, true> : k_b_shade<1, false>);
+    auto *shade = pick_b_shade(b.rng, nee);
     for (;;) {
         for (uint32_t c = 0; c < kChunk; ++c) {
             const int in = static_cast<int>(c & 1u), out = in ^ 1;
@@ -994,11 +1201,16 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
                 return e;
             const WavefrontState ss =
                 tuning.material_sort ? enqueue_material_sort(scene, se, in, counters, num_sms, stream) : se;
+            if (nee == kNeeDeferred && (e = reset_shadow_counters(counters, stream)) != cudaSuccess) return e;
             shade<<<shade_blocks, 128, 0, stream>>>(scene, b, ss, in, counters);
+            if (nee == kNeeDeferred)
+                enqueue_shadow_stage<2>(scene, DevCamera{}, FrameBuffers{}, RenderParams{}, b, ss, b.rng, out, 0u, 0u,
+                                        counters, extend_grid, shade_blocks, stream);
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         iter += kChunk;
-        nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u)) * kChunk;
+        nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) + (nee == kNeeDeferred ? 2u : 0u)) *
+              kChunk;
         if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
             cudaSuccess)
             return e;

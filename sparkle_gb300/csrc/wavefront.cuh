@@ -3,7 +3,9 @@
 // The per-pixel path loop of SamplePixel (CPURenderer.cpp:240-396) is split into stage kernels that run
 // over queues of live paths: generate (camera rays + RNG), then per bounce extend (closest hit) and shade
 // (emission / sky / BSDF sample / Russian roulette, compacting survivors into the next queue with
-// warp-aggregated atomics), then finish (G-buffer write). Queue lengths live in device memory, so one
+// warp-aggregated atomics) and, with next-event estimation, shadow (a persistent occlusion walk of the
+// light and sky rays shade queued) and accumulate (their radiance added in the one-kernel order), then
+// finish (G-buffer write). Queue lengths live in device memory, so one
 // frame is a fixed launch sequence with no host round trip. Each path runs the same arithmetic and draws
 // the same random numbers in the same order as the one-kernel schedule, so both write identical G-buffers.
 #pragma once
@@ -39,6 +41,14 @@ struct WavefrontState {
     uint32_t *frame_seed = nullptr;     // dispatched sample count at frame k (per-pixel seed base)
     uint32_t frame_capacity = 0;
     unsigned long long *host_len = nullptr;  // pinned: queue length read back between iteration chunks
+    // Shadow stage of next-event estimation (allocated on first use, `nee_capacity` slots): the two
+    // occlusion rays of a light-sampling vertex (k = 0 light, 1 sky) and the radiance each adds unoccluded.
+    float4 *shadow_o = nullptr;        // 2 per slot: origin xyz, w = tmax
+    float4 *shadow_d = nullptr;        // 2 per slot: direction xyz
+    float4 *nee_contrib = nullptr;     // 2 per slot: radiance xyz; w = 0 no ray, 1 queued, 2 unoccluded
+    uint32_t *shadow_queue = nullptr;  // occlusion rays of the iteration, entry 2 * slot + k
+    uint32_t *nee_list = nullptr;      // light-sampling vertices of the iteration, slot | (path ended) << 31
+    uint32_t nee_capacity = 0;
 };
 
 // Material-sort classes: material ids 0..kSortBuckets-3 each, larger ids share one class, misses the last.
@@ -63,7 +73,11 @@ struct WfTuning {
     bool ray_sort = false;
     uint32_t slots_per_pixel = 1;  // multi-frame schedule: path slots per pixel (bounded by the state's capacity)
     uint32_t batch_slots = 0;      // batch schedule: paths in flight (0 = the state's capacity)
+    bool shadow_stage = true;      // NEE occlusion rays walked by their own persistent stage (false: inline in shade)
 };
+
+// Allocates the shadow-stage buffers of `s` for its capacity (no-op when they are large enough).
+cudaError_t wavefront_alloc_nee(WavefrontState &s);
 
 // Host-side CUDA graph of one chunk of the multi-frame loop (kChunkIterations extend + shade iterations
 // with their counter resets), captured once and replayed while the kernel parameters stay the same.

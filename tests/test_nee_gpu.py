@@ -86,3 +86,28 @@ def test_nee_is_unbiased_and_reduces_noise(ctx, cornell):
     assert abs(ratio - 1.0) < 5e-3
     assert rel_mse(nee, plain) < 2e-4
     assert noise_nee < 0.25 * noise_plain
+
+
+@pytest.mark.parametrize("spatial", [False, True])
+def test_shadow_stage_equals_inline_walks(ctx, small_terrain, cornell, spatial):
+    """The wavefront's shadow stage (occlusion rays queued by shade, walked by their own persistent kernel,
+    radiance added light before sky) renders the same bits as walking them inline in the shade kernel and
+    as the one-kernel schedule, with the same shadow-ray count, on the frame-by-frame (spatial fill) and the
+    multi-frame schedules; sky NEE on the terrain, triangle lights and sky-less on the Cornell box."""
+    for scene, cam_args in (small_terrain, cornell):
+        W, H = 64, 48
+        camera = scenes.make_camera(cam_args, W, H)
+        res = []
+        for kernel, stage in ((abi.SPK_KERNEL_WAVEFRONT, 1), (abi.SPK_KERNEL_WAVEFRONT, 0),
+                              (abi.SPK_KERNEL_MEGAKERNEL, 1)):
+            ctx.set_tuning(shadow_stage=stage)
+            cfg = abi.make_config(W, H, spp=1, bounce=6, enable_nee=True, spatial_denoise=spatial,
+                                  rng=abi.SPK_RNG_XOSHIRO256SS, seed=4, kernel=kernel)
+            g, st, out = render_gpu(ctx, scene, camera, cfg, 5)
+            res.append((g, out, st["shadow_rays"], st["extension_rays"]))
+        ctx.set_tuning(shadow_stage=1)
+        assert res[0][2] > 0
+        for g, out, shadow, ext in res[1:]:
+            assert np.array_equal(g.view(np.uint32), res[0][0].view(np.uint32))
+            assert np.array_equal(out, res[0][1])
+            assert (shadow, ext) == (res[0][2], res[0][3])

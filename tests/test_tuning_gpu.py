@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 DEFAULTS = dict(cuda_graph=1, material_sort=0, bvh_width=8, bvh_leaf_size=3, extend_blocks_per_sm=0,
                 shade_blocks_per_sm=8, batch_slots=0, ray_sort=0, bvh_collapse=0, bvh_builder=0,
-                path_slots_per_pixel=64)
+                path_slots_per_pixel=64, shadow_stage=1)
 
 VARIANTS = [
     dict(cuda_graph=0),
@@ -32,6 +32,8 @@ VARIANTS = [
     dict(path_slots_per_pixel=1),
     dict(path_slots_per_pixel=4, cuda_graph=0),
     dict(path_slots_per_pixel=3, material_sort=1),
+    dict(shadow_stage=0),
+    dict(shadow_stage=0, material_sort=1, path_slots_per_pixel=2),
 ]
 
 
@@ -59,7 +61,7 @@ def test_tuning_defaults_and_validation(ctx):
     assert ctx.tuning() == DEFAULTS
     for bad in [dict(bvh_width=1), dict(bvh_width=9), dict(bvh_leaf_size=0), dict(bvh_leaf_size=4),
                 dict(cuda_graph=2), dict(shade_blocks_per_sm=0), dict(extend_blocks_per_sm=33),
-                dict(path_slots_per_pixel=0), dict(path_slots_per_pixel=65)]:
+                dict(path_slots_per_pixel=0), dict(path_slots_per_pixel=65), dict(shadow_stage=2)]:
         with pytest.raises(native.SpkError):
             ctx.set_tuning(**bad)
         assert ctx.tuning() == DEFAULTS  # a rejected setting leaves the previous one
