@@ -12,7 +12,7 @@ build here) on this machine's host cores over a bounded sample of the same workl
 
 The line also carries `nee`: the same workload with next-event estimation on, the occlusion rays in the
 wavefront's shadow stage and walked inline (`--no-nee` skips it); `denoise`: the wall time to relMSE 0.01 / 0.003 at 1920x1080 on the same scene for
-denoised low-spp rendering (the committed U-Net) vs plain path tracing, against a 4096-spp reference
+denoised 1 / 4 / 16 spp rendering (the committed U-Net) vs plain path tracing, against a 16384-spp reference
 (`--no-denoise` skips it); and `batch`: 32 uneven render requests over 3 scenes in one batched wavefront
 against the same requests rendered one by one (`--no-batch` skips it, `--batch-autotune` adds a tuned run).
 """
@@ -166,6 +166,31 @@ def ncu_issue_profile():
 CPU_ROW_STEP, CPU_FRAMES = 4, 4
 
 
+def ncu_warp_inst_per_ray():
+    """Warp instructions the extend kernel issues per extension ray, from the committed ncu summary of the
+    same walk (smsp__inst_executed.sum over its launches / the rays they walked)."""
+    path = os.path.join(ROOT, "profiles", "k_wf_extend_stress.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        m = re.search(r"warp_inst_per_ray\s*=\s*([0-9.]+)", f.read())
+    return float(m.group(1)) if m else None
+
+
+def issue_roofline(rays: float, trace_s: float, sm_mhz, num_sms: int):
+    """The walk's issue-side bound: warp instructions issued per second (ncu's instructions per ray x the
+    timed rays / the extend kernels' time) against the SMs' issue peak (4 schedulers x 1 warp instruction
+    per cycle per SM at the sampled SM clock)."""
+    ipr = ncu_warp_inst_per_ray()
+    if ipr is None or not sm_mhz or trace_s <= 0:
+        return None
+    achieved = ipr * rays / trace_s / 1e9
+    peak = num_sms * 4 * sm_mhz * 1e6 / 1e9
+    return {"bound": "issue", "achieved": round(achieved, 1), "peak": round(peak, 1), "unit": "G warp-inst/s",
+            "frac": round(achieved / peak, 4), "warp_inst_per_ray": ipr,
+            "source": "profiles/k_wf_extend_stress.md (smsp__inst_executed.sum / rays)"}
+
+
 def cpu_sample_text(threads: int) -> str:
     rows = len(range(0, HEIGHT, CPU_ROW_STEP))
     return (f"{CPU_FRAMES} frames x every {CPU_ROW_STEP}th row ({rows} rows spread over the image) x {WIDTH} px of "
@@ -277,7 +302,7 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     device_ms = trace_ms = 0.0
-    rays = launches = trace_launches = errors = 0
+    rays = ext_rays = launches = trace_launches = errors = 0
     with ClockSampler(local_rank) as clocks:
         for _ in range(args.steps):
             ctx.set_camera(camera)
@@ -286,6 +311,7 @@ def run_ours(args):
             device_ms += st["device_ms"]
             trace_ms += st["trace_kernel_ms"]
             rays += st["extension_rays"] + st["shadow_rays"]
+            ext_rays += st["extension_rays"]
             launches += st["kernel_launches"]
             trace_launches += st["trace_launches"]
             errors |= st["error_flags"]
@@ -363,6 +389,8 @@ def run_ours(args):
         "device_error_flags": errors,
         "clocks": clocks.summary(),
     }
+    line["roofline"]["issue"] = issue_roofline(ext_rays, trace_ms / 1000.0, line["clocks"].get("sm_mhz"),
+                                               torch.cuda.get_device_properties(local_rank).multi_processor_count)
     if cpu:
         line["cpu_baseline"] = cpu
     if world == 1 and not args.no_nee:
@@ -512,14 +540,13 @@ def batch_metric(autotune: bool = False):
 
 def denoise_metric(ctx):
     """Second half of the metric: wall time to relMSE 0.01 (and 0.003) at 1920x1080 on the same scene,
-    denoised low-spp (committed U-Net weights, tcgen05 inference, per-tile fallback) vs plain path
-    tracing, both scored against a 4096-spp plain reference (the full 16384-spp run is
-    `python -m sparkle_gb300.eval_denoiser`)."""
+    denoised 1 / 4 / 16 spp (committed U-Net weights, tcgen05 inference, per-tile fallback) vs plain path
+    tracing at 1 .. 512 spp, both scored against a 16384-spp plain reference (about 70 s of the run)."""
     from sparkle_gb300 import denoise, eval_denoiser
     import os as _os
     if not _os.path.exists(denoise.WEIGHTS):
         return {"unavailable": "no trained weights at " + _os.path.relpath(denoise.WEIGHTS, ROOT)}
-    r = eval_denoiser.run(WIDTH, HEIGHT, ref_spp=4096, plain_max=512, den_spp=(1, 4), ctx=ctx)
+    r = eval_denoiser.run(WIDTH, HEIGHT, ref_spp=16384, plain_max=512, den_spp=(1, 4, 16), ctx=ctx)
     out = {"ref_spp": r["ref_spp"], "nee": True, "threshold": r["threshold"], "tile": r["tile"],
            "plain": [[p["spp"], round(p["relmse"], 6), p["wall_s"]] for p in r["plain"]],
            "denoised": [[d["spp"], round(d["relmse"], 6), d["wall_s"], d["fallback_tiles"]] for d in r["denoised"]]}
@@ -530,18 +557,21 @@ def denoise_metric(ctx):
 
 def run_profile_small(args):
     """The bench workload cut to 2 frames (stress scene, 127 MB of nodes + triangles, larger than L2, at
-    1920x1080): the case the ncu captures run on (one kernel, a few launches, ~0.6 GB on the device)."""
+    1920x1080; `--nee` turns next-event estimation on): the case the ncu captures run on (one kernel, a few
+    launches, ~0.6 GB on the device)."""
     from sparkle_gb300 import abi, native, scenes
     scene, cam_args = scenes.terrain_spheres(0)
     w, h = WIDTH, HEIGHT
     ctx = native.Context(0)
     ctx.set_scene(scene)
-    ctx.set_config(abi.make_config(w, h, spp=1, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS, kernel=args.kernel))
+    ctx.set_config(abi.make_config(w, h, spp=1, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS, kernel=args.kernel,
+                                   enable_nee=args.nee))
     ctx.set_camera(scenes.make_camera(cam_args, w, h))
     ctx.render(2)
     st = ctx.stats()
     assert st["error_flags"] == 0, st
-    print(json.dumps({"profile_small": True, "extension_rays": st["extension_rays"], "device_ms": st["device_ms"]}))
+    print(json.dumps({"profile_small": True, "nee": args.nee, "extension_rays": st["extension_rays"],
+                      "shadow_rays": st["shadow_rays"], "device_ms": st["device_ms"]}))
     ctx.close()
 
 
@@ -640,6 +670,7 @@ def main():
     ap.add_argument("--tune", default="", help="spk_tuning knobs, e.g. cuda_graph=0,material_sort=1,bvh_width=4")
     ap.add_argument("--profile-small", action="store_true",
                     help="ncu capture case: the bench workload cut to 2 frames, no timing output")
+    ap.add_argument("--nee", action="store_true", help="with --profile-small: next-event estimation on")
     ap.add_argument("--profile-unet", action="store_true",
                     help="ncu capture case: one 1080p U-Net inference and one training step")
     ap.add_argument("--profile-scene", action="store_true",

@@ -14,9 +14,10 @@
 //                  m * cout ...), committing each stage back to the producer;
 //   all 4 warps    epilogue: tcgen05.ld of the pixel rows (warp w owns TMEM lanes 32w..32w+31), bias,
 //                  ReLU or ReLU-backward mask, BF16 pack, 16-byte stores.
-// Wgrad (one CTA per (128 rows of (tap, ci), pixel range)): all threads gather and transpose the shifted
-// input and the output gradient into K-major (pixel-contiguous) swizzled tiles, thread 0 issues the MMAs,
-// and the FP32 partial sums are added to dw with atomics.
+// Wgrad (one CTA per (128 rows of (tap, ci), pixel range)): TMA loads of the shifted input and the output
+// gradient as they lie in NHWC memory (MN-major operands, 64-byte swizzle), MMAs that read them MN-major,
+// and the FP32 partial sums added to dw with atomics. (SPK_CONV_WGRAD_TMA=0 keeps the earlier form: all
+// threads gather and transpose both operands into K-major swizzled tiles.)
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -404,6 +405,142 @@ __global__ void __launch_bounds__(128, 1) k_conv_wgrad(WgradParams P) {
     }
 }
 
+// ------------------------------------------------------------------------------------------------
+// wgrad with TMA-fed MN-major operands
+// ------------------------------------------------------------------------------------------------
+// GEMM dw[g][co] = sum_p x[p + tap(g)][ci(g)] * dy[p][co], rows g = (tap, ci) in M tiles of 128, N = cout,
+// K = pixels in blocks of a tw x th = 64-pixel tile. In NHWC memory both operands have M (N) contiguous and
+// K strided, so they are loaded as they lie: per K block, warp 0 issues one 4-D TMA load per 32-row span of
+// the M tile (the input box {32 ch, tw, th, 1} of that span's channel chunk, shifted by its tap; zero fill
+// outside the image is the padding) and one per 32-channel span of dy (unshifted), each landing as 64 rows
+// (pixels) x 64 bytes in the 64-byte-swizzled layout; warp 1 issues four kind::f16 MMAs (K = 16 pixels
+// each) that read both tiles MN-major. The FP32 partial sums of the CTA's pixel range are then added to dw.
+constexpr uint32_t kWgtStages = 4;
+constexpr uint32_t kWgtPix = 64;                 // pixels per K block
+constexpr uint32_t kWgtSpanBytes = kWgtPix * 64;  // one 32-channel span of a K block: 64 rows x 64 B
+// Slack after the ring, before the barriers: every MMA read stays inside its stage for the descriptor
+// offsets above; the slack keeps it inside the CTA's shared memory even if the two offsets were read the
+// other way round (8-row groups 4 KB apart, spans 512 B apart).
+constexpr uint32_t kWgtSlack = 8192;
+
+struct WgradTmaParams {
+    uint32_t n, h, w, cin, cout;
+    uint32_t tw, th, tiles_x, tiles_y;  // K-block pixel tile and tiles per image row / column
+    uint32_t krows;                     // 9 * cin
+    uint32_t m_tiles;                   // ceil(krows / 128)
+    uint32_t kblocks;                   // K blocks (pixel tiles) per CTA
+    uint32_t ktotal;                    // pixel tiles in all images
+    uint32_t stages, stage_bytes;
+    float *dw;
+    uint32_t *err;
+};
+
+__host__ __device__ constexpr uint32_t wgt_stage_bytes(uint32_t cout) { return 4u * kWgtSpanBytes + (cout / 32u) * kWgtSpanBytes; }
+
+__global__ void __launch_bounds__(128, 1)
+    k_conv_wgrad_tma(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmdy, WgradTmaParams P) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = align1024(smem_raw);
+    const uint32_t nst = P.stages, stage_bytes = P.stage_bytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + nst * stage_bytes + kWgtSlack);
+    uint64_t *full = bars, *empty = bars + kWgtStages, *accum = bars + 2 * kWgtStages;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * kWgtStages + 1);
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t ncols = tmem_columns(P.cout);
+
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < nst; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accum, 1);
+        fence_mbar_init();
+        tma_prefetch_desc(&tmx);
+        tma_prefetch_desc(&tmdy);
+    }
+    if (warp == 0) tmem_alloc(tmem_slot, ncols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const uint32_t mtile = blockIdx.x % P.m_tiles, split = blockIdx.x / P.m_tiles;
+    const uint32_t kb0 = split * P.kblocks;
+    const uint32_t nkb = kb0 < P.ktotal ? min(P.kblocks, P.ktotal - kb0) : 0u;
+    const uint32_t cspans = P.cout / 32u;
+    // Spans of this M tile that hold rows < krows (the rest of the A tile is never loaded; its rows of the
+    // accumulator are not written out).
+    const uint32_t g_first = mtile * kTileM;
+    const uint32_t aspans = min(4u, (P.krows - g_first + 31u) / 32u);
+
+    if (warp == 0 && lane == 0) {
+        const uint32_t tx_bytes = (aspans + cspans) * kWgtSpanBytes;
+        for (uint32_t i = 0; i < nkb; ++i) {
+            const uint32_t s = i % nst, u = i / nst;
+            if (u > 0 && !mbar_wait(&empty[s], (u - 1) & 1u, P.err)) break;
+            uint32_t t = kb0 + i;
+            const uint32_t tx = t % P.tiles_x;
+            t /= P.tiles_x;
+            const uint32_t ty = t % P.tiles_y;
+            const int img = static_cast<int>(t / P.tiles_y);
+            const int x0 = static_cast<int>(tx * P.tw), y0 = static_cast<int>(ty * P.th);
+            uint8_t *a = smem + s * stage_bytes;
+            uint8_t *b = a + 4u * kWgtSpanBytes;
+            mbar_arrive_expect_tx(&full[s], tx_bytes);
+            for (uint32_t sp = 0; sp < aspans; ++sp) {
+                const uint32_t g0 = g_first + sp * 32u;
+                const uint32_t tap = g0 / P.cin, ci0 = g0 - tap * P.cin;
+                tma_load_4d(a + sp * kWgtSpanBytes, &tmx, &full[s], static_cast<int>(ci0),
+                            x0 + static_cast<int>(tap % 3u) - 1, y0 + static_cast<int>(tap / 3u) - 1, img);
+            }
+            for (uint32_t sp = 0; sp < cspans; ++sp)
+                tma_load_4d(b + sp * kWgtSpanBytes, &tmdy, &full[s], static_cast<int>(sp * 32u), x0, y0, img);
+        }
+    } else if (warp == 1 && lane == 0) {
+        const uint32_t idesc = idesc_bf16(kTileM, P.cout, true, true);
+        bool ok = true;
+        for (uint32_t i = 0; i < nkb; ++i) {
+            const uint32_t s = i % nst, u = i / nst;
+            if (!mbar_wait(&full[s], u & 1u, P.err)) {
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t a = smem_u32(smem + s * stage_bytes), b = a + 4u * kWgtSpanBytes;
+#pragma unroll
+            for (uint32_t k16 = 0; k16 < kWgtPix / 16u; ++k16)
+                mma_bf16(tmem, smem_desc_mn_sw64(a + k16 * 1024u, kWgtSpanBytes),
+                         smem_desc_mn_sw64(b + k16 * 1024u, kWgtSpanBytes), idesc, (i | k16) != 0u);
+            mma_commit(&empty[s]);
+        }
+        if (ok && nkb > 0) mma_commit(accum);
+    }
+    __syncwarp();
+
+    bool ready = nkb > 0 && mbar_wait(accum, 0, P.err);
+    ready = __all_sync(0xFFFFFFFFu, ready);
+    tc_fence_after();
+    if (ready) {
+        const uint32_t g = g_first + warp * 32u + lane;
+        for (uint32_t j = 0; j < P.cout / 16u; ++j) {
+            uint32_t v[16];
+            tmem_ld16(tmem + ((warp * 32u) << 16) + j * 16u, v);
+            if (g >= P.krows) continue;
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const float f = __uint_as_float(v[e]);
+                if (f != 0.f) atomicAdd(P.dw + static_cast<size_t>(j * 16u + e) * P.krows + g, f);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, ncols);
+    }
+}
+
 __global__ void k_transpose_weights(const __nv_bfloat16 *w, __nv_bfloat16 *wt, uint32_t cout, uint32_t cin) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;  // index into wt [cin][9][cout]
     if (i >= cout * cin * 9u) return;
@@ -583,11 +720,74 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
     return cudaGetLastError();
 }
 
+#ifndef SPK_CONV_WGRAD_TMA
+#define SPK_CONV_WGRAD_TMA 1  // 1: weight gradient from TMA-loaded MN-major operands; 0: thread-gathered K-major tiles
+#endif
+
+namespace {
+cudaError_t wgrad_tma(const NhwcView &x, const NhwcView &dy, float *dw, const ConvGeom &g, uint32_t *err,
+                      cudaStream_t stream) {
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return cudaErrorNotSupported;
+    WgradTmaParams P{};
+    P.n = g.n;
+    P.h = g.h;
+    P.w = g.w;
+    P.cin = x.channels;
+    P.cout = dy.channels;
+    P.tw = g.w >= 16u ? 16u : 8u;
+    P.th = kWgtPix / P.tw;
+    P.tiles_x = (g.w + P.tw - 1) / P.tw;
+    P.tiles_y = (g.h + P.th - 1) / P.th;
+    P.krows = 9u * P.cin;
+    P.m_tiles = (P.krows + kTileM - 1) / kTileM;
+    const unsigned long long ktotal = static_cast<unsigned long long>(P.tiles_x) * P.tiles_y * g.n;
+    if (ktotal > 0x7FFFFFFFull) return cudaErrorInvalidValue;
+    P.ktotal = static_cast<uint32_t>(ktotal);
+    P.dw = dw;
+    P.err = err;
+    P.stage_bytes = wgt_stage_bytes(P.cout);
+    P.stages = std::min<uint32_t>(kWgtStages, (200u * 1024u) / P.stage_bytes);
+    if (P.stages < 2) return cudaErrorInvalidConfiguration;
+    CUtensorMap tmx, tmdy;
+    const NhwcView *views[2] = {&x, &dy};
+    CUtensorMap *maps[2] = {&tmx, &tmdy};
+    for (int k = 0; k < 2; ++k) {
+        const NhwcView &v = *views[k];
+        const cuuint64_t dims[4] = {v.channels, g.w, g.h, g.n};
+        const cuuint64_t strides[3] = {static_cast<cuuint64_t>(v.ld) * 2u, static_cast<cuuint64_t>(v.ld) * 2u * g.w,
+                                       static_cast<cuuint64_t>(v.ld) * 2u * g.w * g.h};
+        const cuuint32_t box[4] = {32u, P.tw, P.th, 1u};
+        const cuuint32_t es[4] = {1u, 1u, 1u, 1u};
+        if (enc(maps[k], CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, v.ptr, dims, strides, box, es,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return cudaErrorInvalidValue;
+    }
+    // About two CTAs per SM in total, at least 8 K blocks each (fewer splits: fewer atomic partial sums).
+    static const int sms = device_sms();
+    unsigned long long splits = std::max<unsigned long long>(1ull, (2ull * sms) / P.m_tiles);
+    splits = std::min<unsigned long long>(splits, (ktotal + 7) / 8);
+    splits = std::max<unsigned long long>(splits, 1ull);
+    P.kblocks = static_cast<uint32_t>((ktotal + splits - 1) / splits);
+    splits = (ktotal + P.kblocks - 1) / P.kblocks;
+    const size_t smem = launch_smem(P.stages * P.stage_bytes + kWgtSlack + 1024 + 256, tmem_columns(P.cout));
+    if (smem == 0) return cudaErrorInvalidConfiguration;
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+        cudaFuncSetAttribute(k_conv_wgrad_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
+    });
+    k_conv_wgrad_tma<<<static_cast<unsigned>(splits * P.m_tiles), 128, smem, stream>>>(tmx, tmdy, P);
+    return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t conv3x3_wgrad(const NhwcView &x, const NhwcView &dy, float *dw, const ConvGeom &g, uint32_t *err,
                           cudaStream_t stream) {
     if (x.channels == 0 || x.channels % 32u || dy.channels == 0 || dy.channels % 32u || dy.channels > kMaxCout ||
         x.ld % 8u || dy.ld % 8u || !aligned16(x.ptr) || !aligned16(dy.ptr) || g.n == 0 || g.h == 0 || g.w == 0)
         return cudaErrorInvalidValue;
+    if (SPK_CONV_WGRAD_TMA) return wgrad_tma(x, dy, dw, g, err, stream);
     WgradParams P{};
     P.n = g.n;
     P.h = g.h;

@@ -2,13 +2,15 @@
 // time-bounded waits, TMA tiled loads, tcgen05 TMEM allocation / MMA issue / commit / loads, and the
 // shared-memory and instruction descriptors of tcgen05.mma kind::f16 (BF16 in, FP32 accumulate).
 //
-// Layout conventions (all operands K-major, 64-byte swizzle):
+// Layout conventions (operands K-major unless stated, 64-byte swizzle):
 //   * an operand tile is R rows x 32 BF16 (64 B per row) written by TMA with CU_TENSOR_MAP_SWIZZLE_64B or
 //     by threads applying the same XOR pattern (16-byte chunk c of row r lands at chunk c ^ ((r >> 1) & 3));
 //   * 8 rows form a 512-byte swizzle atom, so the descriptor's stride byte offset is 512 and every tile
 //     starts on a 1024-byte boundary;
 //   * one kind::f16 MMA consumes K = 16 (32 bytes of each row); the second K step of a tile starts 32 bytes
-//     further.
+//     further;
+//   * an MN-major operand (the weight gradient's) is the same 64-byte-row atom with the roles swapped: a row
+//     is 32 consecutive M (or N) elements, rows run along K, and one MMA's K = 16 rows span two atoms.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -193,13 +195,31 @@ __device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t saddr) {
     return d;
 }
 
-// Instruction descriptor of kind::f16: BF16 A and B (both K-major), FP32 D, M x N.
-__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n) {
-    return (1u << 4)            // D format F32
-           | (1u << 7)          // A format BF16
-           | (1u << 10)         // B format BF16
-           | ((n >> 3) << 17)   // N / 8
-           | ((m >> 4) << 24);  // M / 16
+// Shared-memory matrix descriptor of an MN-major operand, 64-byte swizzle: the tile is rows of 64 bytes
+// (32 consecutive BF16 of the M or N dimension), one row per K index; 8 consecutive K rows form a 512-byte
+// swizzle atom (stride byte offset = 512 between 8-row K groups) and 32-element M/N spans sit `span_bytes`
+// apart (leading byte offset). This is the layout a 64-byte-swizzled TMA box {32 channels, pixels} lands
+// in, with K = pixels.
+__device__ __forceinline__ uint64_t smem_desc_mn_sw64(uint32_t saddr, uint32_t span_bytes) {
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((saddr >> 4) & 0x3FFFu);              // start address
+    d |= static_cast<uint64_t>((span_bytes >> 4) & 0x3FFFu) << 16;   // leading byte offset: next M/N span
+    d |= static_cast<uint64_t>(512u >> 4) << 32;                     // stride byte offset: next 8 K rows
+    d |= static_cast<uint64_t>(1u) << 46;                            // descriptor version
+    d |= static_cast<uint64_t>(4u) << 61;                            // SWIZZLE_64B
+    return d;
+}
+
+// Instruction descriptor of kind::f16: BF16 A and B, FP32 D, M x N; A and B K-major unless `a_mn` /
+// `b_mn` select the MN-major (transposed) reading of that operand.
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n, bool a_mn = false, bool b_mn = false) {
+    return (1u << 4)                  // D format F32
+           | (1u << 7)                // A format BF16
+           | (1u << 10)               // B format BF16
+           | ((a_mn ? 1u : 0u) << 15)  // A major: MN
+           | ((b_mn ? 1u : 0u) << 16)  // B major: MN
+           | ((n >> 3) << 17)         // N / 8
+           | ((m >> 4) << 24);        // M / 16
 }
 
 // Byte offset of 16-byte chunk `chunk` (0..3) of row `row` in a 64-byte-swizzled K-major tile.

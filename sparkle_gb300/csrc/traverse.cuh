@@ -51,8 +51,15 @@ enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOve
 #ifndef SPK_WALK_MIN_BLOCKS
 #define SPK_WALK_MIN_BLOCKS 8  // resident 128-thread blocks per SM the walking kernels are compiled for
 #endif
+#ifndef SPK_SMEM_STACK
+#define SPK_SMEM_STACK 0  // top entries of each persistent walk's stack kept in shared memory (0: all local)
+#endif
+#ifndef SPK_STACK_REGTOP
+#define SPK_STACK_REGTOP 0  // 1: the top entry of each persistent walk's local stack cached in registers
+#endif
 
 constexpr int kStackSize = 48;
+constexpr int kWalkThreads = 128;  // threads per block of every persistent walking kernel
 constexpr uint32_t kMaxIterations = 1u << 20;
 constexpr int kPostponeLanes = SPK_POSTPONE_LANES;
 
@@ -166,6 +173,62 @@ __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint
     tgroup = make_uint2(n1.y, hitmask & 0x00FFFFFFu);
 }
 
+// Traversal stacks. Walker::push / pop address entry `i` (0 = bottom) of the current ray's stack.
+// LocalStack: the whole stack in local memory (one-thread walks).
+struct LocalStack {
+    uint2 e[kStackSize];
+    __device__ __forceinline__ void reset() {}
+    __device__ __forceinline__ void put(int i, uint2 v) { e[i] = v; }
+    __device__ __forceinline__ uint2 take(int i) { return e[i]; }
+};
+
+// SharedRingStack: the top K entries in a per-thread ring of shared memory, deeper entries in local memory.
+// Invariant: entries [max(0, sp - K), sp) are in the ring, entry i in slot i mod K; pushing entry i >= K
+// first moves entry i - K out to local memory, popping it brings entry i - K back into the freed slot. The
+// ring is a column of the block's array (slot k of thread t at k * kWalkThreads + t): the 16 lanes of a
+// half-warp touch 16 consecutive 8-byte words whatever their depths, so accesses are free of bank conflicts.
+template <int K>
+struct SharedRingStack {
+    static_assert(K > 0 && (K & (K - 1)) == 0 && K < kStackSize, "ring size: a power of two below the stack size");
+    uint2 *ring;  // this thread's slot 0
+    uint2 spill[kStackSize - K];
+    __device__ __forceinline__ void reset() {}
+    __device__ __forceinline__ void put(int i, uint2 v) {
+        uint2 *slot = ring + (i & (K - 1)) * kWalkThreads;
+        if (i >= K) spill[i - K] = *slot;
+        *slot = v;
+    }
+    __device__ __forceinline__ uint2 take(int i) {
+        uint2 *slot = ring + (i & (K - 1)) * kWalkThreads;
+        const uint2 v = *slot;
+        if (i >= K) *slot = spill[i - K];
+        return v;
+    }
+};
+
+// RegTopStack: a local stack whose top entry may live in registers instead (`cached`): a push moves the
+// cached entry out to local memory and caches the new one, a pop returns the cached entry when there is
+// one, so a push followed by its pop touches no memory.
+struct RegTopStack {
+    uint2 top;
+    bool cached = false;
+    uint2 e[kStackSize];
+    // A walk that ended early (an occlusion hit) may leave entries behind, the top one cached.
+    __device__ __forceinline__ void reset() { cached = false; }
+    __device__ __forceinline__ void put(int i, uint2 v) {
+        if (cached) e[i - 1] = top;
+        top = v;
+        cached = true;
+    }
+    __device__ __forceinline__ uint2 take(int i) {
+        if (cached) {
+            cached = false;
+            return top;
+        }
+        return e[i];
+    }
+};
+
 // Resumable two-level walk of one ray. init() starts it; step() advances by one node visit plus the
 // triangle tests it enables and returns true when the walk is over (result in `best`).
 template <int kMode, bool kCount>
@@ -206,15 +269,17 @@ struct Walker {
         return t == best.t && (inst < best.inst || (inst == best.inst && face < best.face));
     }
 
-    __device__ __forceinline__ void push(uint2 *stack, uint2 v, uint32_t &err) {
+    template <class Stack>
+    __device__ __forceinline__ void push(Stack &stack, uint2 v, uint32_t &err) {
         if (sp < kStackSize) {
-            stack[sp++] = v;
+            stack.put(sp++, v);
         } else {
             err |= kErrStackOverflow;
         }
     }
 
-    __device__ __forceinline__ bool step(const DevScene &S, uint2 *stack, uint32_t &err, TraceCounts *counts) {
+    template <class Stack>
+    __device__ __forceinline__ bool step(const DevScene &S, Stack &stack, uint32_t &err, TraceCounts *counts) {
         if (++iter > budget) {
             err |= kErrIterationBudget;
             return true;
@@ -348,7 +413,7 @@ struct Walker {
                 setup_level(ray, wo, wd);
             }
             if (sp == 0) return true;
-            ngroup = stack[--sp];
+            ngroup = stack.take(--sp);
         }
         return false;
     }
@@ -358,7 +423,7 @@ struct Walker {
 template <int kMode, bool kCount = false>
 __device__ __forceinline__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd, float tmax_occl, uint32_t &err,
                                                  TraceCounts *counts = nullptr) {
-    uint2 stack[kStackSize];
+    LocalStack stack;
     Walker<kMode, kCount> w;
     w.init(S, S.tlas_root, wo, wd, tmax_occl);
     while (!w.step(S, stack, err, counts)) {
@@ -370,7 +435,7 @@ __device__ __forceinline__ TraceResult trace_ray(const DevScene &S, f3 wo, f3 wd
 // ray has finished once fewer than `kRefillLanes` lanes are still walking. `fetch(i, o, d, tmax)` loads item
 // i's ray (tmax starts at the call's `tmax`; an occlusion walk may lower it per ray) and returns the TLAS
 // root of its scene; `finish(i, result)` stores its result. Every lane of every warp of the block must call
-// this.
+// this, and the block must have kWalkThreads threads (the shared stack rings are laid out for that many).
 constexpr int kRefillLanes = SPK_REFILL_LANES;
 
 template <int kMode, bool kCount, class Fetch, class Finish>
@@ -379,7 +444,15 @@ __device__ __forceinline__ void walk_persistent(const DevScene &S, unsigned long
                                                 Finish &&finish) {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt_mask = (1u << lane) - 1u;
-    uint2 stack[kStackSize];
+#if SPK_SMEM_STACK > 0
+    __shared__ uint2 rings[SPK_SMEM_STACK * kWalkThreads];
+    SharedRingStack<SPK_SMEM_STACK> stack;
+    stack.ring = rings + threadIdx.x;
+#elif SPK_STACK_REGTOP
+    RegTopStack stack;
+#else
+    LocalStack stack;
+#endif
     Walker<kMode, kCount> w;
     bool active = false, exhausted = false;
     unsigned long long item = 0;
@@ -399,6 +472,7 @@ __device__ __forceinline__ void walk_persistent(const DevScene &S, unsigned long
                     float tm = tmax;
                     const uint32_t root = fetch(q, o, d, tm);
                     w.init(S, root, o, d, tm);
+                    stack.reset();
                     active = true;
                 }
             }

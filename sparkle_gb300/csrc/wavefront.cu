@@ -296,14 +296,27 @@ __device__ __forceinline__ uint32_t item_pixel(uint32_t q, uint32_t w, uint32_t 
     return (ty * th + j / tw) * w + tx * tw + (j % tw);
 }
 
-// Slot `slot` starts sample item `item` = frame * pixels + q of the pass (pixel item_pixel(q)); the slot
-// records the sample's index frame * pixels + pixel, where its result is stored.
+#ifndef SPK_ITEM_ORDER
+#define SPK_ITEM_ORDER 1  // 1: frame fastest (a warp's items are consecutive frames of one pixel); 0: frame-major
+#endif
+
+// Slot `slot` starts sample item `item` of the pass (`total_items` = frames x pixels). Frame-fastest order:
+// item = q * frames + frame, pixel item_pixel(q), so the lanes of a warp trace samples of the same pixel in
+// consecutive frames (primary rays that differ only by their jitter and lens sample). Frame-major order:
+// item = frame * pixels + q. The slot records the sample's index frame * pixels + pixel, where its result
+// is stored; results never depend on the order (each sample keeps its pixel and seed).
 template <int kKind>
 __device__ __forceinline__ void start_item(const DevCamera &cam, const RenderParams &p, const WavefrontState &s,
                                            uint32_t slot, uint32_t item, uint32_t w, uint32_t h,
-                                           uint32_t frame_base) {
+                                           uint32_t frame_base, uint32_t total_items) {
     const uint32_t npix = w * h;
+#if SPK_ITEM_ORDER == 1
+    const uint32_t frames = total_items / npix;
+    const uint32_t q = item / frames, k = item - q * frames, pid = item_pixel(q, w, h);
+#else
+    (void)total_items;
     const uint32_t k = item / npix, pid = item_pixel(item - k * npix, w, h);
+#endif
     start_path<kKind>(cam, p, s, slot, pid % w, pid / w, w, h, s.frame_seed[frame_base + k]);
     s.slot_item[slot] = k * npix + pid;
     s.slot_state[slot] = 0u;
@@ -313,10 +326,10 @@ __device__ __forceinline__ void start_item(const DevCamera &cam, const RenderPar
 template <int kKind>
 __global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers fb, RenderParams p,
                                                      WavefrontState s, uint32_t frame_base, uint32_t initial,
-                                                     Counters *counters) {
+                                                     uint32_t total_items, Counters *counters) {
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= initial) return;
-    start_item<kKind>(cam, p, s, slot, slot, fb.width, fb.height, frame_base);
+    start_item<kKind>(cam, p, s, slot, slot, fb.width, fb.height, frame_base, total_items);
     s.queue[0][slot] = slot;
     if (slot == 0) {
         counters->queue_counters[kLen0] = initial;
@@ -367,7 +380,8 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_mf_shade(DevScene
             if (need) {
                 const unsigned long long item = base + __popc(need_mask & ((1u << lane) - 1u));
                 if (item < total_items) {
-                    start_item<kKind>(cam, p, s, slot, static_cast<uint32_t>(item), fb.width, fb.height, frame_base);
+                    start_item<kKind>(cam, p, s, slot, static_cast<uint32_t>(item), fb.width, fb.height, frame_base,
+                                      total_items);
                     push = true;
                 }
             }
@@ -582,11 +596,19 @@ __device__ __forceinline__ void start_item_batch(const DevScene &S, const BatchP
     const uint32_t r = find_request(b, item);
     const DevRequest &R = b.reqs[r];
     const unsigned long long local = item - R.item_base;
+#if SPK_ITEM_ORDER == 1
+    // frame fastest within the request, as start_item: a warp's items are consecutive frames of one pixel
+    const uint32_t q = static_cast<uint32_t>(local / R.spp);
+    const uint32_t k = static_cast<uint32_t>(local - static_cast<unsigned long long>(q) * R.spp);
+    const uint32_t pix = item_pixel(q, R.width, R.height);
+#else
     const uint32_t k = static_cast<uint32_t>(local / R.npix);
     const uint32_t pix = static_cast<uint32_t>(local - static_cast<unsigned long long>(k) * R.npix);
+#endif
     RenderParams p{k, R.bounce, b.rng, R.seed, 0u, b.enable_nee};
     start_path<kKind>(R.cam, p, s, slot, pix % R.width, pix / R.width, R.width, R.height, k);
-    s.slot_item[slot] = static_cast<uint32_t>(item);
+    // the sample's index in the frame-major sample buffer k_b_resolve reads
+    s.slot_item[slot] = static_cast<uint32_t>(R.item_base + static_cast<unsigned long long>(k) * R.npix + pix);
     s.slot_state[slot] = 0u;
     s.slot_req[slot] = r;
     s.slot_root[slot] = S.descs[R.scene].tlas_root;
@@ -725,7 +747,7 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_nee_accumulate(De
                     const unsigned long long item = base + __popc(need_mask & ((1u << lane) - 1u));
                     if (kMode == 1 && item < total_items) {
                         start_item<kKind>(cam, p, s, slot, static_cast<uint32_t>(item), fb.width, fb.height,
-                                          frame_base);
+                                          frame_base, total_items);
                         push = true;
                     } else if (kMode == 2 && item < b.total_items) {
                         start_item_batch<kKind>(S, b, s, slot, item);
@@ -1020,9 +1042,11 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
             std::min<uint64_t>({want, static_cast<uint64_t>(s.capacity), static_cast<uint64_t>(total_items)}));
         if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
         if (p.rng == 0) {
-            k_mf_generate<0><<<(initial + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, initial, counters);
+            k_mf_generate<0><<<(initial + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, initial, total_items,
+                                                                     counters);
         } else {
-            k_mf_generate<1><<<(initial + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, initial, counters);
+            k_mf_generate<1><<<(initial + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, initial, total_items,
+                                                                     counters);
         }
         ++nl;
         // One chunk: kChunk iterations of (reset the output queue, extend, shade).
