@@ -45,6 +45,9 @@ enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOve
 #ifndef SPK_MINMAX3
 #define SPK_MINMAX3 0  // 1: slab entry/exit with three-input min/max (exact, same results)
 #endif
+#ifndef SPK_META_SIMD
+#define SPK_META_SIMD 1  // 1: the four meta bytes of a half node decoded together with 32-bit SIMD-in-register ops
+#endif
 #ifndef SPK_MT_RCP
 #define SPK_MT_RCP 1  // 1: Moller-Trumbore's 1/det as a correctly rounded reciprocal (same bits as 1.f/det)
 #endif
@@ -146,9 +149,19 @@ __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint
         const uint32_t nx = (r.oct & 1u) ? hix : lox, fx = (r.oct & 1u) ? lox : hix;
         const uint32_t ny = (r.oct & 2u) ? hiy : loy, fy = (r.oct & 2u) ? loy : hiy;
         const uint32_t nz = (r.oct & 4u) ? hiz : loz, fz = (r.oct & 4u) ? loz : hiz;
+#if SPK_META_SIMD
+        // Per byte: an inner child has bits 3 and 4 of its meta set; its slot bit is xor-ed with the ray's
+        // octant. bit4 = the hit-mask bit index of each child, bits4 = the bits it sets there (0 for an
+        // empty slot, whose meta byte is 0, so empty slots need no test of their own).
+        const uint32_t inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
+        const uint32_t bit4 = (meta4 ^ ((inner4 >> 4) * r.oct)) & 0x1F1F1F1Fu;
+        const uint32_t bits4 = (meta4 >> 5) & 0x07070707u;
+#endif
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
+#if !SPK_META_SIMD
             const uint32_t m = (meta4 >> (8 * c)) & 0xFFu;
+#endif
             const float tnx = fmaf(byte_to_float(nx, c), ax, ox);
             const float tny = fmaf(byte_to_float(ny, c), ay, oy);
             const float tnz = fmaf(byte_to_float(nz, c), az, oz);
@@ -162,11 +175,15 @@ __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint
             const float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.f));
             const float t1 = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
 #endif
+#if SPK_META_SIMD
+            if (t0 <= t1) hitmask |= __byte_perm(bits4, 0u, 0x4440u | c) << __byte_perm(bit4, 0u, 0x4440u | c);
+#else
             if (m != 0u && t0 <= t1) {
                 uint32_t bit = m & 0x1Fu;
                 if ((m & 0x18u) == 0x18u) bit ^= r.oct;
                 hitmask |= ((m >> 5) & 7u) << bit;
             }
+#endif
         }
     }
     ngroup = make_uint2(n1.x, (hitmask & 0xFF000000u) | (n0.w >> 24));
