@@ -278,11 +278,30 @@ __global__ void k_adam(float *w, const float *g, float *m, float *v, size_t n, f
     w[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
 }
 
-// FP32 weights of a layer (param vector) -> BF16 copy [cout][9][cin].
-__global__ void k_weights_bf16(const float *wf, bf16 *wb, size_t n) {
-    const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i < n) wb[i] = __float2bfloat16_rn(wf[i]);
+// Every layer's weights in one launch: layer k covers the weight elements [first[k], first[k + 1]) of
+// the concatenated BF16 buffers.
+struct WeightTable {
+    uint32_t count;
+    uint32_t cin[kNumLayers], cout[kNumLayers];
+    unsigned long long w_off[kNumLayers], wb_off[kNumLayers], first[kNumLayers + 1];
+};
+
+// BF16 copy w_b[co][tap][ci] of each FP32 weight and the dgrad copy wt[ci][8 - tap][co] of the same
+// value (the layout conv3x3_transpose_weights writes), one thread per weight element of all layers.
+__global__ void k_refresh_weights(const __grid_constant__ WeightTable T, const float *params, bf16 *wb, bf16 *wt) {
+    const unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= T.first[T.count]) return;
+    uint32_t k = 0;
+    while (k + 1 < T.count && T.first[k + 1] <= i) ++k;
+    const unsigned long long j = i - T.first[k];  // (co * 9 + tap) * cin + ci within the layer
+    const uint32_t cin = T.cin[k], cout = T.cout[k];
+    const uint32_t ci = static_cast<uint32_t>(j % cin), tap = static_cast<uint32_t>((j / cin) % 9u);
+    const uint32_t co = static_cast<uint32_t>(j / (9ull * cin));
+    const bf16 v = __float2bfloat16_rn(params[T.w_off[k] + j]);
+    wb[T.wb_off[k] + j] = v;
+    wt[T.wb_off[k] + (static_cast<unsigned long long>(ci) * 9u + (8u - tap)) * cout + co] = v;
 }
+
 
 // OUT [n][hp][wp][32] -> rgb float4 [n][h][w] (expm1 of the log1p prediction).
 __global__ void k_decode(const bf16 *out, float4 *dst, uint32_t n, uint32_t h, uint32_t w, uint32_t hp, uint32_t wp) {
@@ -454,16 +473,23 @@ spk_status dn_cuda(spk_denoiser *dn, cudaError_t e, const char *what) {
         if (_e != cudaSuccess) return dn_cuda(dn, _e, what); \
     } while (0)
 
-// BF16 weight copies (and the transposed dgrad copies) from the FP32 master parameters.
+// BF16 weight copies (and the transposed dgrad copies) from the FP32 master parameters, one launch.
 cudaError_t refresh_weights(spk_denoiser *dn) {
-    cudaError_t e;
-    for (const Layer &L : dn->layers) {
-        const size_t n = static_cast<size_t>(L.cout) * 9 * L.cin;
-        k_weights_bf16<<<blocks_for(n, 256), 256, 0, dn->stream>>>(dn->params.p + L.w_off, dn->wb.p + L.wb_off, n);
-        if ((e = conv3x3_transpose_weights(dn->wb.p + L.wb_off, dn->wt.p + L.wb_off, L.cout, L.cin, dn->stream)) !=
-            cudaSuccess)
-            return e;
+    WeightTable T{};
+    T.count = static_cast<uint32_t>(dn->layers.size());
+    if (T.count > kNumLayers) return cudaErrorInvalidValue;
+    unsigned long long total = 0;
+    for (uint32_t k = 0; k < T.count; ++k) {
+        const Layer &L = dn->layers[k];
+        T.cin[k] = L.cin;
+        T.cout[k] = L.cout;
+        T.w_off[k] = L.w_off;
+        T.wb_off[k] = L.wb_off;
+        T.first[k] = total;
+        total += static_cast<unsigned long long>(L.cout) * 9u * L.cin;
     }
+    T.first[T.count] = total;
+    k_refresh_weights<<<blocks_for(total, 256), 256, 0, dn->stream>>>(T, dn->params.p, dn->wb.p, dn->wt.p);
     dn->weights_dirty = false;
     return cudaGetLastError();
 }
