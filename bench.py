@@ -381,6 +381,8 @@ def run_ours(args):
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "kernel": "k_wf_extend (closest-hit walk)" if args.kernel != 1 else "k_render_mega",
                      "algorithmic_bytes_per_ray": round(bytes_per_ray, 1),
+                     "nodes_per_ray": round(cs["node_visits"] / cs["extension_rays"], 2),
+                     "triangles_per_ray": round(cs["triangle_tests"] / cs["extension_rays"], 2),
                      "rays_per_launch": round(rays_per_launch, 1),
                      "traffic": (round(traffic_per_ray * rays_per_launch) if traffic_per_ray else None),
                      "traffic_unit": "DRAM bytes per launch (ncu per-ray figure x rays per launch)",

@@ -56,7 +56,48 @@ struct OutSpec {
     uint32_t relu;
     const __nv_bfloat16 *mask;
     uint32_t mask_ld;
+    __nv_bfloat16 *pool;  // dense [n][h/2][w/2][cout]: 2x2 average of the output, or null
 };
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+// 2x2 average pooling of the packed BF16 outputs (channels col0..col0+15) of the four pixels of a 2x2 block,
+// which sit in lanes l, l ^ 1 (next column) and l ^ tw, l ^ tw ^ 1 (next row) of the warp; every lane of the
+// warp calls it. The lane holding the block's top-left pixel writes the pooled channels when that pixel is
+// inside the image. Sum order per channel: top-left, top-right, bottom-left, bottom-right from 0, times 0.25,
+// rounded to BF16 -- the order and rounding of the pooling kernel it replaces.
+__device__ __forceinline__ void epilogue_pool(const OutSpec &O, const uint32_t (&pk)[8], uint32_t lane, uint32_t tw,
+                                              bool inb, uint32_t img, uint32_t px, uint32_t py, uint32_t h,
+                                              uint32_t w, uint32_t cout, uint32_t col0) {
+    uint32_t b[8], c[8], d[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        b[e] = __shfl_xor_sync(0xFFFFFFFFu, pk[e], 1);
+        c[e] = __shfl_xor_sync(0xFFFFFFFFu, pk[e], tw);
+        d[e] = __shfl_xor_sync(0xFFFFFFFFu, pk[e], tw ^ 1u);
+    }
+    if ((lane & 1u) || (lane & tw) || !inb) return;
+    uint32_t q[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        float lo = 0.f, hi = 0.f;
+        const uint32_t words[4] = {pk[e], b[e], c[e], d[e]};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162 *>(&words[k]);
+            lo += __low2float(v);
+            hi += __high2float(v);
+        }
+        q[e] = pack_bf16(0.25f * lo, 0.25f * hi);
+    }
+    const size_t dst = ((static_cast<size_t>(img) * (h / 2) + py / 2) * (w / 2) + px / 2) * cout + col0;
+    uint4 *op = reinterpret_cast<uint4 *>(O.pool + dst);
+    op[0] = make_uint4(q[0], q[1], q[2], q[3]);
+    op[1] = make_uint4(q[4], q[5], q[6], q[7]);
+}
 
 struct FwdParams {
     uint32_t n, h, w;
@@ -86,10 +127,6 @@ __device__ __forceinline__ uint8_t *align1024(uint8_t *raw) {
     return raw + (((a + 1023u) & ~1023u) - a);
 }
 
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-    return *reinterpret_cast<const uint32_t *>(&v);
-}
 
 // Output channels col0..col0+15 of pixel `pix` from 16 FP32 accumulator columns: + bias (`bias16`, or
 // none), then the ReLU-backward mask (keep where mask > 0; read only for pixels inside the image) or ReLU,
@@ -123,6 +160,7 @@ __device__ __forceinline__ void epilogue_pack(const OutSpec &O, const uint32_t (
 constexpr uint32_t kFwdThreads = 32u * SPK_CONV_EPI_WARPS;
 static_assert(SPK_CONV_EPI_WARPS == 4 || SPK_CONV_EPI_WARPS == 8, "4 or 8 warps");
 
+template <bool kPool>
 __global__ void __launch_bounds__(kFwdThreads, 1)
     k_conv_fwd(const __grid_constant__ CUtensorMap tmx, const __grid_constant__ CUtensorMap tmw,
                const __grid_constant__ CUtensorMap tmy, FwdParams P) {
@@ -229,6 +267,8 @@ __global__ void __launch_bounds__(kFwdThreads, 1)
             tmem_ld16(tmem + ((lgrp * 32u) << 16) + m * P.cout + j * 16u, v);
             epilogue_pack(P.out_spec, v, P.out_spec.bias ? P.out_spec.bias + j * 16u : nullptr, pix, j * 16u, inb,
                           pk);
+            if (kPool)
+                epilogue_pool(P.out_spec, pk, lane, P.tw, inb, img, px, py, P.h, P.w, P.cout, j * 16u);
             if (P.stage_out) {
                 uint8_t *region = smem + (m * chunks + (j >> 1)) * (kTileM * 64u);
                 const uint32_t c0 = (j & 1u) * 2u;
@@ -628,6 +668,7 @@ OutSpec out_spec(const NhwcView &y, const ConvEpilogue &epi) {
     o.relu = epi.relu ? 1u : 0u;
     o.mask = static_cast<const __nv_bfloat16 *>(epi.mask.ptr);
     o.mask_ld = epi.mask.ld;
+    o.pool = static_cast<__nv_bfloat16 *>(epi.pool);
     return o;
 }
 
@@ -646,6 +687,7 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
         return cudaErrorInvalidValue;
     if (epi.mask.ptr && (epi.mask.channels != cout || epi.mask.ld % 8u || !aligned16(epi.mask.ptr)))
         return cudaErrorInvalidValue;
+    if (epi.pool && ((g.h | g.w) & 1u || !aligned16(epi.pool))) return cudaErrorInvalidValue;
     EncodeTiledFn enc = encode_fn();
     if (!enc) return cudaErrorNotSupported;
     // Tiles of 16 x 8 pixels (8 x 16 below 16 columns): a multiple of 8 columns, so that the row taps'
@@ -710,13 +752,15 @@ cudaError_t conv3x3_forward(const NhwcView &x, const void *w, uint32_t cout, con
     P.err = err;
     static std::once_flag attr;
     std::call_once(attr, [] {
-        cudaFuncSetAttribute(k_conv_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
+        cudaFuncSetAttribute(k_conv_fwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
+        cudaFuncSetAttribute(k_conv_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem);
     });
     const unsigned long long tiles = static_cast<unsigned long long>(P.tiles_x) * P.tiles_y * g.n;
     if (tiles > 0x7FFFFFFFull) return cudaErrorInvalidValue;
     const size_t smem = launch_smem(P.stages * P.stage_bytes + 1024 + 256, tmem_columns(mt * cout));
     if (smem == 0) return cudaErrorInvalidConfiguration;
-    k_conv_fwd<<<static_cast<unsigned>(tiles), kFwdThreads, smem, stream>>>(tmx, tmw, tmy, P);
+    auto *kern = P.out_spec.pool ? k_conv_fwd<true> : k_conv_fwd<false>;
+    kern<<<static_cast<unsigned>(tiles), kFwdThreads, smem, stream>>>(tmx, tmw, tmy, P);
     return cudaGetLastError();
 }
 

@@ -31,6 +31,8 @@ struct ConvEpilogue {
     const float *bias = nullptr;  // cout floats or null
     bool relu = false;
     NhwcView mask{};              // optional: multiply by (mask > 0) (ReLU backward of the layer below)
+    // optional: also write the 2x2 average pooling of the (BF16) output, dense [n][h/2][w/2][cout] (h, w even)
+    void *pool = nullptr;
 };
 
 // y = conv3x3(x, w) over geometry g. `w` is bf16 [cout][9][cin]. `err` is a device word for error bits.

@@ -125,40 +125,6 @@ __global__ void k_input(const float *feat, bf16 *x0, uint32_t n, uint32_t h, uin
     *reinterpret_cast<uint4 *>(x0 + q * kInPad + grp * 8u) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
 }
 
-// 2x2 average pooling: src view [n][2h][2w] (ld_s) -> dst [n][h][w][c] (dense). One thread per (pixel,
-// 8-channel group): four 16-byte loads, one 16-byte store; per channel the sum runs in (dy, dx) order.
-__global__ void k_pool(const bf16 *src, uint32_t ld_s, bf16 *dst, uint32_t n, uint32_t h, uint32_t w, uint32_t c) {
-    const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;  // (pixel, channel group)
-    const uint32_t cg = c / 8;
-    const size_t total = static_cast<size_t>(n) * h * w * cg;
-    if (i >= total) return;
-    const uint32_t ch = static_cast<uint32_t>(i % cg) * 8;
-    const size_t q = i / cg;
-    const uint32_t x = static_cast<uint32_t>(q % w), y = static_cast<uint32_t>((q / w) % h);
-    const uint32_t img = static_cast<uint32_t>(q / (static_cast<size_t>(w) * h));
-    const uint32_t W2 = 2 * w;
-    float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (uint32_t dy = 0; dy < 2; ++dy)
-        for (uint32_t dx = 0; dx < 2; ++dx) {
-            const size_t p = (static_cast<size_t>(img) * 2 * h + 2 * y + dy) * W2 + 2 * x + dx;
-            const uint4 raw = *reinterpret_cast<const uint4 *>(src + p * ld_s + ch);
-            const uint32_t wv[4] = {raw.x, raw.y, raw.z, raw.w};
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const __nv_bfloat162 v = *reinterpret_cast<const __nv_bfloat162 *>(&wv[k]);
-                acc[2 * k] += __low2float(v);
-                acc[2 * k + 1] += __high2float(v);
-            }
-        }
-    uint32_t pk[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const __nv_bfloat162 v = __floats2bfloat162_rn(0.25f * acc[2 * k], 0.25f * acc[2 * k + 1]);
-        pk[k] = *reinterpret_cast<const uint32_t *>(&v);
-    }
-    *reinterpret_cast<uint4 *>(dst + q * c + ch) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-}
-
 // Nearest 2x upsampling: src [n][h][w][c] (dense) -> dst view [n][2h][2w] (ld_d, first c channels).
 __global__ void k_upsample(const bf16 *src, bf16 *dst, uint32_t ld_d, uint32_t n, uint32_t h, uint32_t w, uint32_t c) {
     const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;  // (fine pixel, 8-channel group)
@@ -551,11 +517,14 @@ NhwcView enc_out(spk_denoiser *dn, uint32_t l) {
     return view(dn->cat[l].p + kW[l + 1], kW[l], cat_channels(l));
 }
 
-cudaError_t conv_fwd(spk_denoiser *dn, uint32_t li, const NhwcView &x, const NhwcView &y, const ConvGeom &g) {
+// Forward of layer li; with `pool`, the epilogue also writes the 2x2 average pooling of the output there.
+cudaError_t conv_fwd(spk_denoiser *dn, uint32_t li, const NhwcView &x, const NhwcView &y, const ConvGeom &g,
+                     bf16 *pool = nullptr) {
     const Layer &L = dn->layers[li];
     ConvEpilogue epi;
     epi.bias = dn->params.p + L.b_off;
     epi.relu = L.relu;
+    epi.pool = pool;
     return conv3x3_forward(x, dn->wb.p + L.wb_off, L.cout, y, g, epi, dn->err.p, dn->stream);
 }
 
@@ -588,14 +557,11 @@ cudaError_t forward(spk_denoiser *dn, const float *feat, uint32_t n, uint32_t h,
     for (uint32_t l = 0; l < kLevels; ++l) {
         if ((e = conv_fwd(dn, enc_a(l), in, dense(dn->ea[l].p, kW[l]), G(l))) != cudaSuccess) return e;
         const NhwcView eo = enc_out(dn, l);
-        if ((e = conv_fwd(dn, enc_b(l), dense(dn->ea[l].p, kW[l]), eo, G(l))) != cudaSuccess) return e;
-        if (l < 4) {
-            const ConvGeom c = G(l + 1);
-            const size_t work = static_cast<size_t>(n) * c.h * c.w * (kW[l] / 8);
-            k_pool<<<blocks_for(work, 256), 256, 0, dn->stream>>>(static_cast<const bf16 *>(eo.ptr), eo.ld,
-                                                                   dn->pool[l].p, n, c.h, c.w, kW[l]);
-            in = dense(dn->pool[l].p, kW[l]);
-        }
+        // the encoder's second conv also writes the 2x2 average pooling of its output (the next level's input)
+        if ((e = conv_fwd(dn, enc_b(l), dense(dn->ea[l].p, kW[l]), eo, G(l), l < 4 ? dn->pool[l].p : nullptr)) !=
+            cudaSuccess)
+            return e;
+        if (l < 4) in = dense(dn->pool[l].p, kW[l]);
     }
     NhwcView up = dense(dn->eb4.p, kW[4]);
     for (int l = 3; l >= 0; --l) {
