@@ -11,7 +11,8 @@ cube with a baked sun). Rays = traced segments (extension + shadow).
 build here) on this machine's host cores over a bounded sample of the same workload.
 
 The line also carries `nee`: the same workload with next-event estimation on, the occlusion rays in the
-wavefront's shadow stage and walked inline (`--no-nee` skips it); `denoise`: the wall time to relMSE 0.01 / 0.003 at 1920x1080 on the same scene for
+wavefront's shadow stage and walked inline (`--no-nee` skips it); `spatial`: the same workload with the
+reference's default DenoisePass spatial fill on, multi-frame and frame by frame (`--no-spatial` skips it); `denoise`: the wall time to relMSE 0.01 / 0.003 at 1920x1080 on the same scene for
 denoised 1 / 4 / 16 spp rendering (the committed U-Net) vs plain path tracing, against a 16384-spp reference
 (`--no-denoise` skips it); and `batch`: 32 uneven render requests over 3 scenes in one batched wavefront
 against the same requests rendered one by one (`--no-batch` skips it, `--batch-autotune` adds a tuned run).
@@ -397,6 +398,8 @@ def run_ours(args):
         line["cpu_baseline"] = cpu
     if world == 1 and not args.no_nee:
         line["nee"] = nee_metric(ctx, camera)
+    if world == 1 and not args.no_spatial:
+        line["spatial"] = spatial_metric(ctx, camera)
     if world == 1 and not args.no_denoise:
         line["denoise"] = denoise_metric(ctx)
     if world == 1 and not args.no_batch:
@@ -435,6 +438,34 @@ def nee_metric(ctx, camera, steps: int = 3):
                      "error_flags": errors}
     ctx.set_tuning(shadow_stage=1)
     out["speedup"] = round(out["shadow_stage"]["mrays_s"] / out["inline"]["mrays_s"], 3)
+    return out
+
+
+def spatial_metric(ctx, camera, steps: int = 3):
+    """The same workload through the reference's default cpu pipeline, whose DenoisePass spatial fill is on
+    (RenderConfig.cpp:38): Mrays/s by device time with every frame of the call in one wavefront (the
+    default) and frame by frame (spk_tuning.multi_frame = 0)."""
+    from sparkle_gb300 import abi
+    cfg = abi.make_config(WIDTH, HEIGHT, spp=1, max_spp=4096, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS,
+                          seed=0, spatial_denoise=True)
+    ctx.set_config(cfg)
+    out = {"spp": SPP, "steps": steps}
+    for name, mf in (("multi_frame", 1), ("frame_by_frame", 0)):
+        ctx.set_tuning(multi_frame=mf)
+        ctx.set_camera(camera)
+        ctx.render(SPP)  # warm-up
+        ms = rays = 0.0
+        errors = 0
+        for _ in range(steps):
+            ctx.set_camera(camera)
+            ctx.render(SPP)
+            st = ctx.stats()
+            ms += st["device_ms"]
+            rays += st["extension_rays"] + st["shadow_rays"]
+            errors |= st["error_flags"]
+        out[name] = {"mrays_s": round(rays / (ms * 1e3), 1), "ms_per_step": round(ms / steps, 2), "error_flags": errors}
+    ctx.set_tuning(multi_frame=1)
+    out["speedup"] = round(out["multi_frame"]["mrays_s"] / out["frame_by_frame"]["mrays_s"], 3)
     return out
 
 
@@ -670,6 +701,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-denoise", action="store_true", help="skip the denoised-vs-plain time-to-relMSE leg")
     ap.add_argument("--no-nee", action="store_true", help="skip the next-event-estimation leg")
+    ap.add_argument("--no-spatial", action="store_true", help="skip the spatial-fill (default pipeline) leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-requests leg")
     ap.add_argument("--batch-autotune", action="store_true", help="autotune the batched leg's launch knobs")
     ap.add_argument("--no-scene-update", action="store_true", help="skip the scene build / incremental update leg")

@@ -223,6 +223,9 @@ typedef struct spk_tuning {
     uint32_t shadow_stage;         /* wavefront NEE: 1 (default) queues the light and sky occlusion rays of each
                                       light-sampling vertex for a persistent any-hit stage with lane refill, then adds
                                       their radiance in order; 0 walks them inline in the shade kernel, one per thread */
+    uint32_t multi_frame;          /* wavefront: 1 (default) renders all frames of a call in one regenerating wavefront
+                                      (16 B per sample of the call, 32 B with the spatial fill, in device memory);
+                                      0 renders frame by frame (one path per pixel, no per-sample buffers) */
 } spk_tuning;
 
 /* ------------------------------------------------------------------------------------------------ */

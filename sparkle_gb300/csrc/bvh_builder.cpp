@@ -366,8 +366,11 @@ WideBvh collapse_wide(const Bvh2 &bvh, int max_children) {
 
 namespace {
 
+#ifndef SPK_SAH_ITEM_COST
+#define SPK_SAH_ITEM_COST 0.3f  // cost of testing one leaf item relative to one wide-node visit
+#endif
 constexpr float kSahNodeCost = 1.0f;
-constexpr float kSahItemCost = 0.3f;
+constexpr float kSahItemCost = SPK_SAH_ITEM_COST;
 
 // Assigns the children of one wide node to octant slots (slot s = near-most child for rays whose sign
 // bits equal s) and writes its quantised boxes: the same assignment collapse_wide uses.

@@ -128,13 +128,6 @@ __global__ void __launch_bounds__(128) k_render_mega(DevScene S, DevCamera cam, 
 // ------------------------------------------------------------------------------------------------
 // DenoisePass + ToneMappingPass (CPURenderer.cpp:452-576) as one gather kernel.
 // ------------------------------------------------------------------------------------------------
-__constant__ int c_dirs[8][2] = {{1, 0}, {0, 1}, {-1, 0}, {0, -1}, {-1, -1}, {1, -1}, {-1, 1}, {1, 1}};
-
-__device__ __forceinline__ bool px_valid(const float4 &c) { return c.w > 0.f; }
-__device__ __forceinline__ bool px_sky(const float4 &c, const float4 &n) {
-    return px_valid(c) && fabsf(n.x) <= 1e-5f && fabsf(n.y) <= 1e-5f && fabsf(n.z) <= 1e-5f;
-}
-
 __device__ __forceinline__ float aces(float c, float exposure) {
     const float x = c * exposure;
     float y = (x * (x * 2.51f + 0.03f)) / (x * (x * 2.43f + 0.59f) + 0.14f);
@@ -147,41 +140,9 @@ __global__ void __launch_bounds__(256) k_resolve(FrameBuffers fb, float f, float
     const uint32_t i = blockIdx.x * 32u + (threadIdx.x & 31u);
     const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 5);
     if (i >= fb.width || j >= fb.height) return;
-    const int W = static_cast<int>(fb.width), H = static_cast<int>(fb.height);
     const size_t k = static_cast<size_t>(j) * fb.width + i;
     float4 in = fb.gcolor[k];
-    if (spatial && !px_valid(in)) {
-        // SpatialDenoisePixel as a gather: a valid, non-sky neighbour S fills this pixel when this pixel is
-        // the first of S's 8 directions that is in bounds, invalid and has normal similarity >= 0.99. Among
-        // several such S the one last in row-major order wins (the single-threaded order of the passes).
-        long best_writer = -1;
-        float4 best_color = in;
-        for (int dk = 0; dk < 8; ++dk) {
-            const int si = static_cast<int>(i) - c_dirs[dk][0], sj = static_cast<int>(j) - c_dirs[dk][1];
-            if (si < 0 || si >= W || sj < 0 || sj >= H) continue;
-            const size_t sk = static_cast<size_t>(sj) * fb.width + si;
-            const float4 sc = fb.gcolor[sk];
-            const float4 sn = fb.gnormal[sk];
-            if (!px_valid(sc) || px_sky(sc, sn)) continue;
-            const f3 wn = mk3(sn.x, sn.y, sn.z);
-            long target = -1;
-            for (int tk = 0; tk < 8; ++tk) {
-                const int ni = si + c_dirs[tk][0], nj = sj + c_dirs[tk][1];
-                if (ni < 0 || ni >= W || nj < 0 || nj >= H) continue;
-                const size_t nk = static_cast<size_t>(nj) * fb.width + ni;
-                if (fb.gcolor[nk].w > 0.f) continue;
-                const float4 nn = fb.gnormal[nk];
-                if (dot3(mk3(nn.x, nn.y, nn.z), wn) < 0.99f) continue;
-                target = static_cast<long>(nk);
-                break;
-            }
-            if (target == static_cast<long>(k) && static_cast<long>(sk) > best_writer) {
-                best_writer = static_cast<long>(sk);
-                best_color = make_float4(sc.x, sc.y, sc.z, 1.f);
-            }
-        }
-        in = best_color;
-    }
+    if (spatial) in = spatial_fill(fb.gcolor, fb.gnormal, i, j, fb.width, fb.height, in);
     float4 a = fb.fb[k];
     a = make_float4(in.x + (a.x - in.x) * f, in.y + (a.y - in.y) * f, in.z + (a.z - in.z) * f, in.w + (a.w - in.w) * f);
     fb.fb[k] = a;

@@ -60,6 +60,47 @@ struct LaunchEvents {
     }
 };
 
+// SpatialDenoisePixel (CPURenderer.cpp:452-504) for pixel (i, j) of one frame's G-buffer (`color`: rgb +
+// valid flag, `normal`: first-hit normal, rows of w pixels) as a gather: a valid, non-sky neighbour S fills
+// the pixel when it is the first of S's 8 directions that is in bounds, invalid and has normal similarity
+// >= 0.99; among several such S the one last in row-major order wins (the single-threaded order of the
+// passes). Returns the pixel's G-buffer colour after the fill (`in` itself when nothing fills it).
+__device__ __forceinline__ float4 spatial_fill(const float4 *color, const float4 *normal, uint32_t i, uint32_t j,
+                                               uint32_t w, uint32_t h, float4 in) {
+    constexpr int kDirs[8][2] = {{1, 0}, {0, 1}, {-1, 0}, {0, -1}, {-1, -1}, {1, -1}, {-1, 1}, {1, 1}};
+    if (in.w > 0.f) return in;
+    const int W = static_cast<int>(w), H = static_cast<int>(h);
+    const size_t k = static_cast<size_t>(j) * w + i;
+    long best_writer = -1;
+    float4 best = in;
+    for (int dk = 0; dk < 8; ++dk) {
+        const int si = static_cast<int>(i) - kDirs[dk][0], sj = static_cast<int>(j) - kDirs[dk][1];
+        if (si < 0 || si >= W || sj < 0 || sj >= H) continue;
+        const size_t sk = static_cast<size_t>(sj) * w + si;
+        const float4 sc = color[sk];
+        const float4 sn = normal[sk];
+        const bool sky = fabsf(sn.x) <= 1e-5f && fabsf(sn.y) <= 1e-5f && fabsf(sn.z) <= 1e-5f;
+        if (!(sc.w > 0.f) || sky) continue;
+        const f3 wn = mk3(sn.x, sn.y, sn.z);
+        long target = -1;
+        for (int tk = 0; tk < 8; ++tk) {
+            const int ni = si + kDirs[tk][0], nj = sj + kDirs[tk][1];
+            if (ni < 0 || ni >= W || nj < 0 || nj >= H) continue;
+            const size_t nk = static_cast<size_t>(nj) * w + ni;
+            if (color[nk].w > 0.f) continue;
+            const float4 nn = normal[nk];
+            if (dot3(mk3(nn.x, nn.y, nn.z), wn) < 0.99f) continue;
+            target = static_cast<long>(nk);
+            break;
+        }
+        if (target == static_cast<long>(k) && static_cast<long>(sk) > best_writer) {
+            best_writer = static_cast<long>(sk);
+            best = make_float4(sc.x, sc.y, sc.z, 1.f);
+        }
+    }
+    return best;
+}
+
 struct RenderParams {
     uint32_t frame_seed;
     uint32_t bounce;

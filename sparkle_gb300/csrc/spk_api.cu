@@ -1383,9 +1383,10 @@ static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
     if ((e = cudaMemsetAsync(ctx->counters, 0, sizeof(Counters), ctx->stream)) != cudaSuccess)
         return cuda_fail(ctx, e, "counter reset");
     if ((e = cudaEventRecord(ctx->ev_start, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "event");
-    if (wavefront && !ctx->cfg.spatial_denoise && num_frames > 0) {
+    if (wavefront && ctx->tuning.multi_frame && num_frames > 0) {
         // All frames in one regenerating wavefront: run the per-frame bookkeeping ahead on the host and hand
-        // the kernels each frame's weight and seed base.
+        // the kernels each frame's weight and seed base (the spatial fill, when on, runs per frame in the
+        // resolve over that frame's samples and first-hit normals).
         ctx->frame_weights.resize(num_frames);
         ctx->frame_seeds.resize(num_frames);
         bool clear = false;
@@ -1410,7 +1411,7 @@ static spk_status render_impl(spk_ctx *ctx, uint32_t num_frames) {
         if (clear &&
             (e = cudaMemsetAsync(ctx->fb.ptr, 0, ctx->fb.count * sizeof(float4), ctx->stream)) != cudaSuccess)
             return cuda_fail(ctx, e, "frame buffer clear");
-        RenderParams p{0u, ctx->cfg.bounce, ctx->cfg.rng, ctx->cfg.seed, 0u, ctx->cfg.enable_nee};
+        RenderParams p{0u, ctx->cfg.bounce, ctx->cfg.rng, ctx->cfg.seed, ctx->cfg.spatial_denoise, ctx->cfg.enable_nee};
         uint32_t launches = 0;
         ctx->chunk_graph.enabled = ctx->tuning.cuda_graph != 0;
         const uint32_t replays0 = ctx->chunk_graph.replays;
@@ -2142,6 +2143,7 @@ void spk_tuning_defaults(spk_tuning *out) {
     out->bvh_builder = 0;
     out->path_slots_per_pixel = 64;
     out->shadow_stage = 1;
+    out->multi_frame = 1;
 }
 
 spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
@@ -2158,7 +2160,8 @@ spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
     if (t->bvh_builder > 2) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "bvh_builder takes 0, 1 or 2");
     if (t->path_slots_per_pixel < 1 || t->path_slots_per_pixel > 64)
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "path_slots_per_pixel must be 1..64");
-    if (t->shadow_stage > 1) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "shadow_stage takes 0 or 1");
+    if (t->shadow_stage > 1 || t->multi_frame > 1)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "shadow_stage and multi_frame take 0 or 1");
     ctx->tuning = *t;
     return SPK_OK;
 }

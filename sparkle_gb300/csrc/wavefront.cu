@@ -100,7 +100,7 @@ enum : int { kNeeOff = 0, kNeeInline = 1, kNeeDeferred = 2 };
 template <int kKind, int kNee>
 __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontState &s, uint32_t pid,
                                            uint32_t bounce, float4 *gnormal, uint32_t &shadow, uint32_t &err,
-                                           uint32_t &nee_rays) {
+                                           uint32_t &nee_rays, size_t gnormal_index) {
     constexpr bool nee = kNee != kNeeOff;
     nee_rays = 0u;
     bool alive = false;
@@ -124,7 +124,8 @@ __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontSta
         const TraceResult h{hit4.x, hit4.y, hit4.z, inst, s.hit_face[pid]};
         const Surface surf = make_surface(S, h, o, d);
         const DevMaterial mat = resolve_material(S, S.materials[surf.material], surf.uv);
-        if (bounce == 0 && gnormal) gnormal[pid] = make_float4(surf.normal.x, surf.normal.y, surf.normal.z, 0.f);
+        if (bounce == 0 && gnormal)
+            gnormal[gnormal_index] = make_float4(surf.normal.x, surf.normal.y, surf.normal.z, 0.f);
         if (mat.is_emissive) {
             f3 c = cmul(mk3(mat.emissive[0], mat.emissive[1], mat.emissive[2]), thr);
             if (prev_pdf > 0.f) c = c * bsdf_hit_weight(S, prev_pdf, h, d);
@@ -255,7 +256,7 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_wf_shade(DevScene
         if (q < n) {
             pid = queue[q];
             alive = shade_path<kKind, kNee>(S, s, pid, bounce, p.spatial_denoise ? fb.gnormal : nullptr, shadow, err,
-                                             nee_rays);
+                                             nee_rays, pid);
         }
         if constexpr (kNee == kNeeDeferred) queue_nee(s, counters, pid, nee_rays, false);
         queue_push(s.queue[out_queue], &counters->queue_counters[out_queue], pid, alive && bounce + 1 < p.bounce);
@@ -320,6 +321,7 @@ __device__ __forceinline__ void start_item(const DevCamera &cam, const RenderPar
     start_path<kKind>(cam, p, s, slot, pid % w, pid / w, w, h, s.frame_seed[frame_base + k]);
     s.slot_item[slot] = k * npix + pid;
     s.slot_state[slot] = 0u;
+    if (p.spatial_denoise) s.sample_normals[k * npix + pid] = make_float4(0.f, 0.f, 0.f, 0.f);  // a miss: sky
 }
 
 // Starts the first `initial` sample items of the pass, item i in slot i.
@@ -356,7 +358,9 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_mf_shade(DevScene
         if (q < n) {
             slot = queue[q];
             const uint32_t bounce = s.slot_state[slot];
-            alive = shade_path<kKind, kNee>(S, s, slot, bounce, nullptr, shadow, err, nee_rays) && bounce + 1 < p.bounce;
+            alive = shade_path<kKind, kNee>(S, s, slot, bounce, p.spatial_denoise ? s.sample_normals : nullptr, shadow,
+                                            err, nee_rays, s.slot_item[slot]) &&
+                    bounce + 1 < p.bounce;
             if (alive) {
                 s.slot_state[slot] = bounce + 1u;
                 push = true;
@@ -552,13 +556,16 @@ __device__ __forceinline__ float aces_tonemap(float c, float exposure) {
 // DenoisePass temporal lerp of every sample of the pass, in frame order per pixel
 // (fb = new + (fb - new) * w_k, CPURenderer.cpp:534-543), then ToneMappingPass (:554-576).
 __global__ void __launch_bounds__(256) k_mf_resolve(FrameBuffers fb, WavefrontState s, uint32_t frame_base,
-                                                    uint32_t frames, float exposure) {
+                                                    uint32_t frames, float exposure, uint32_t spatial) {
     const uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t npix = fb.width * fb.height;
     if (pid >= npix) return;
     float4 a = fb.fb[pid];
     for (uint32_t k = 0; k < frames; ++k) {
-        const float4 n = s.samples[static_cast<size_t>(k) * npix + pid];
+        float4 n = s.samples[static_cast<size_t>(k) * npix + pid];
+        if (spatial)  // DenoisePass's spatial fill of frame k's G-buffer (CPURenderer.cpp:452-526)
+            n = spatial_fill(s.samples + static_cast<size_t>(k) * npix, s.sample_normals + static_cast<size_t>(k) * npix,
+                             pid % fb.width, pid / fb.width, fb.width, fb.height, n);
         const float f = s.frame_weight[frame_base + k];
         a = make_float4(n.x + (a.x - n.x) * f, n.y + (a.y - n.y) * f, n.z + (a.z - n.z) * f, n.w + (a.w - n.w) * f);
     }
@@ -645,7 +652,8 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_b_shade(DevScene 
             const DevRequest &R = b.reqs[s.slot_req[slot]];
             const DevScene Sv = scene_view(S, S.descs[R.scene]);
             const uint32_t bounce = s.slot_state[slot];
-            alive = shade_path<kKind, kNee>(Sv, s, slot, bounce, nullptr, shadow, err, nee_rays) && bounce + 1 < R.bounce;
+            alive = shade_path<kKind, kNee>(Sv, s, slot, bounce, nullptr, shadow, err, nee_rays, 0) &&
+                    bounce + 1 < R.bounce;
             if (alive) {
                 s.slot_state[slot] = bounce + 1u;
                 push = true;
@@ -917,7 +925,7 @@ void wavefront_free(WavefrontState &s) {
                     s.hit_face,   s.queue[0],  s.queue[1], s.sort_keys,   s.slot_state, s.slot_item,
                     s.samples,    s.frame_weight, s.frame_seed, s.prev_pdf, s.sort_hist, s.slot_req,
                     s.slot_root,  s.sort_keys2, s.shadow_o, s.shadow_d, s.nee_contrib, s.shadow_queue,
-                    s.nee_list};
+                    s.nee_list,   s.sample_normals};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (s.host_len) cudaFreeHost(s.host_len);
@@ -1022,6 +1030,13 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
         s.sample_capacity = 0;
         if ((e = dmalloc(s.samples, need)) != cudaSuccess) return e;
         s.sample_capacity = need;
+    }
+    if (p.spatial_denoise && s.normal_capacity < need) {
+        if (s.sample_normals) cudaFree(s.sample_normals);
+        s.sample_normals = nullptr;
+        s.normal_capacity = 0;
+        if ((e = dmalloc(s.sample_normals, need)) != cudaSuccess) return e;
+        s.normal_capacity = need;
     }
     if ((e = cudaMemcpyAsync(s.frame_weight, weights, num_frames * sizeof(float), cudaMemcpyHostToDevice, stream)) !=
             cudaSuccess ||
@@ -1181,7 +1196,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
             if (iter > max_iters) return cudaErrorLaunchFailure;  // cannot happen: every slot makes progress
         }
         t_site = "resolve";
-        k_mf_resolve<<<(npix + 255) / 256, 256, 0, stream>>>(fbuf, s, f0, frames, cam.exposure);
+        k_mf_resolve<<<(npix + 255) / 256, 256, 0, stream>>>(fbuf, s, f0, frames, cam.exposure, p.spatial_denoise);
         ++nl;
     }
     if (launches) *launches = nl;

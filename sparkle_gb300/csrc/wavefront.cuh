@@ -36,6 +36,8 @@ struct WavefrontState {
     uint32_t *slot_root = nullptr;            // batch mode: TLAS root of the slot's scene
     float4 *samples = nullptr;                // multi-frame mode: clamped result of each (frame, pixel) sample
     size_t sample_capacity = 0;               // float4 entries of `samples`
+    float4 *sample_normals = nullptr;         // multi-frame mode with the spatial fill: first-hit normal per sample
+    size_t normal_capacity = 0;               // float4 entries of `sample_normals`
     // multi-frame mode: per-frame constants, frame k of the call
     float *frame_weight = nullptr;      // DenoisePass moving-average weight of frame k
     uint32_t *frame_seed = nullptr;     // dispatched sample count at frame k (per-pixel seed base)
@@ -92,14 +94,15 @@ struct ChunkGraph {
 };
 void chunk_graph_free(ChunkGraph &g);
 
-// All `num_frames` frames of a call in one wavefront with path regeneration (valid when the spatial
-// DenoisePass is off, so pixels do not interact within a frame). Slots pull (frame, pixel) sample items
+// All `num_frames` frames of a call in one wavefront with path regeneration. Slots pull (frame, pixel) sample items
 // from a global counter in frame-major order; a slot whose path ends stores the sample's clamped result
 // and starts the next item, so every iteration keeps about one frame of paths in flight and only the
 // last few paths form a tail. A resolve pass then folds each pixel's samples into the frame buffer in
 // frame order with each frame's weight (CPURenderer.cpp:530-543), so the frame buffer is bit-identical
-// to rendering the frames one by one. `weights[k]` / `seeds[k]` are frame k's moving-average weight and
-// seed base. Ends with the tonemap of the final frame buffer.
+// to rendering the frames one by one. With the spatial DenoisePass on, every sample also keeps its first-hit
+// normal and the resolve applies the fill to each frame's samples before folding them (the fill reads only
+// the same frame's samples, so pixels still do not interact across frames). `weights[k]` / `seeds[k]` are
+// frame k's moving-average weight and seed base. Ends with the tonemap of the final frame buffer.
 cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam, const FrameBuffers &fbuf,
                                      const RenderParams &p, uint32_t num_frames, const float *weights,
                                      const uint32_t *seeds, bool count, Counters *counters, WavefrontState &s,

@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 DEFAULTS = dict(cuda_graph=1, material_sort=0, bvh_width=8, bvh_leaf_size=3, extend_blocks_per_sm=0,
                 shade_blocks_per_sm=8, batch_slots=0, ray_sort=0, bvh_collapse=0, bvh_builder=0,
-                path_slots_per_pixel=64, shadow_stage=1)
+                path_slots_per_pixel=64, shadow_stage=1, multi_frame=1)
 
 VARIANTS = [
     dict(cuda_graph=0),
@@ -34,6 +34,8 @@ VARIANTS = [
     dict(path_slots_per_pixel=3, material_sort=1),
     dict(shadow_stage=0),
     dict(shadow_stage=0, material_sort=1, path_slots_per_pixel=2),
+    dict(multi_frame=0),
+    dict(multi_frame=0, shadow_stage=0, material_sort=1),
 ]
 
 
@@ -61,19 +63,20 @@ def test_tuning_defaults_and_validation(ctx):
     assert ctx.tuning() == DEFAULTS
     for bad in [dict(bvh_width=1), dict(bvh_width=9), dict(bvh_leaf_size=0), dict(bvh_leaf_size=4),
                 dict(cuda_graph=2), dict(shade_blocks_per_sm=0), dict(extend_blocks_per_sm=33),
-                dict(path_slots_per_pixel=0), dict(path_slots_per_pixel=65), dict(shadow_stage=2)]:
+                dict(path_slots_per_pixel=0), dict(path_slots_per_pixel=65), dict(shadow_stage=2), dict(multi_frame=2)]:
         with pytest.raises(native.SpkError):
             ctx.set_tuning(**bad)
         assert ctx.tuning() == DEFAULTS  # a rejected setting leaves the previous one
 
 
-@pytest.mark.parametrize("kernel", [abi.SPK_KERNEL_WAVEFRONT, abi.SPK_KERNEL_MEGAKERNEL])
+@pytest.mark.parametrize("kernel,spatial", [(abi.SPK_KERNEL_WAVEFRONT, False), (abi.SPK_KERNEL_WAVEFRONT, True),
+                                            (abi.SPK_KERNEL_MEGAKERNEL, False)])
 @pytest.mark.parametrize("nee", [False, True])
-def test_knobs_render_identical_bits(ctx, small_terrain, kernel, nee):
+def test_knobs_render_identical_bits(ctx, small_terrain, kernel, spatial, nee):
     scene, cam_args = small_terrain
     W, H = 96, 64
     camera = scenes.make_camera(cam_args, W, H)
-    cfg = abi.make_config(W, H, spp=4, bounce=6, enable_nee=nee, seed=5, kernel=kernel)
+    cfg = abi.make_config(W, H, spp=4, bounce=6, enable_nee=nee, spatial_denoise=spatial, seed=5, kernel=kernel)
     # 70 frames: the multi-frame wavefront splits them into two passes (64 + 6), two chunk-graph keys
     base_hdr, base_out, _ = render(ctx, scene, camera, cfg, 70, {})
     for knobs in VARIANTS:
