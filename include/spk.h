@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define SPK_ABI_VERSION 3u
+#define SPK_ABI_VERSION 4u
 
 typedef int32_t spk_status;
 enum {
@@ -226,6 +226,9 @@ typedef struct spk_tuning {
     uint32_t multi_frame;          /* wavefront: 1 (default) renders all frames of a call in one regenerating wavefront
                                       (16 B per sample of the call, 32 B with the spatial fill, in device memory);
                                       0 renders frame by frame (one path per pixel, no per-sample buffers) */
+    uint32_t primary_packets;      /* wavefront: 1 (default) walks the primary rays of each pass (or frame) in packets of
+                                      32 consecutive samples, one warp testing one node for all of them; 0 walks every
+                                      ray on its own */
 } spk_tuning;
 
 /* ------------------------------------------------------------------------------------------------ */

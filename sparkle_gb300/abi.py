@@ -11,7 +11,7 @@ from typing import List, Optional
 
 import numpy as np
 
-SPK_ABI_VERSION = 3
+SPK_ABI_VERSION = 4
 SPK_INVALID_ID = 0xFFFFFFFF
 
 SPK_PRIM_MESH, SPK_PRIM_SPHERE = 0, 1
@@ -78,7 +78,7 @@ class spk_tuning(C.Structure):
     _fields_ = [("cuda_graph", _u32), ("material_sort", _u32), ("bvh_width", _u32), ("bvh_leaf_size", _u32),
                 ("extend_blocks_per_sm", _u32), ("shade_blocks_per_sm", _u32), ("batch_slots", _u32),
                 ("ray_sort", _u32), ("bvh_collapse", _u32), ("bvh_builder", _u32), ("path_slots_per_pixel", _u32),
-                ("shadow_stage", _u32), ("multi_frame", _u32)]
+                ("shadow_stage", _u32), ("multi_frame", _u32), ("primary_packets", _u32)]
 
 
 class spk_texture(C.Structure):

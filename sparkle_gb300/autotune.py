@@ -1,6 +1,7 @@
 """Autotuner for the path tracer's launch shapes and schedule (spk_tuning): queue capacity (batch path
 slots), CTAs per SM of the traversal and shading stages, BVH node width and leaf size, material sort on
-or off, CUDA-graph replay on or off, NEE occlusion rays in their own shadow stage or inline.
+or off, CUDA-graph replay on or off, NEE occlusion rays in their own shadow stage or inline, primary rays
+walked in warp packets or one by one.
 
 No knob changes a result (spk_tuning), so the tuner only measures: it runs a caller's workload under each
 candidate setting and keeps the fastest by device time. The search is coordinate descent from the
@@ -26,6 +27,7 @@ SPACE = {
     "bvh_collapse": [0, 1],
     "bvh_builder": [0, 1, 2],
     "shadow_stage": [1, 0],
+    "primary_packets": [1, 0],
 }
 SCENE_KNOBS = ("bvh_width", "bvh_leaf_size", "bvh_collapse", "bvh_builder")
 

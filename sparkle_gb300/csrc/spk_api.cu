@@ -1361,6 +1361,7 @@ static WfTuning wf_tuning(const spk_ctx *ctx) {
     t.ray_sort = ctx->tuning.ray_sort != 0;
     t.slots_per_pixel = ctx->tuning.path_slots_per_pixel;
     t.shadow_stage = ctx->tuning.shadow_stage != 0;
+    t.packets = ctx->tuning.primary_packets;
     return t;
 }
 
@@ -2144,6 +2145,7 @@ void spk_tuning_defaults(spk_tuning *out) {
     out->path_slots_per_pixel = 64;
     out->shadow_stage = 1;
     out->multi_frame = 1;
+    out->primary_packets = 1;
 }
 
 spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
@@ -2160,8 +2162,8 @@ spk_status spk_set_tuning(spk_ctx *ctx, const spk_tuning *t) {
     if (t->bvh_builder > 2) return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "bvh_builder takes 0, 1 or 2");
     if (t->path_slots_per_pixel < 1 || t->path_slots_per_pixel > 64)
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "path_slots_per_pixel must be 1..64");
-    if (t->shadow_stage > 1 || t->multi_frame > 1)
-        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "shadow_stage and multi_frame take 0 or 1");
+    if (t->shadow_stage > 1 || t->multi_frame > 1 || t->primary_packets > 1)
+        return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "shadow_stage, multi_frame and primary_packets take 0 or 1");
     ctx->tuning = *t;
     return SPK_OK;
 }

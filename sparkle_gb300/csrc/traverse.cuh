@@ -115,7 +115,9 @@ __device__ __forceinline__ float prune_limit(float best, f3 wo, f3 wd, float sce
 }
 
 // Slab test of the 8 children of one wide node; returns the next node group (inner children, permuted
-// slot bits 24..31 + imask in bits 0..7) and triangle group (leaf items, bits 0..23).
+// slot bits 24..31 + imask in bits 0..7) and triangle group (leaf items, bits 0..23). The ray's own octant
+// picks each slab's near and far planes; `order` (an octant) permutes the inner children's bits, which sets
+// the visiting order (a single-ray walk passes its own octant, a packet one octant shared by its lanes).
 // Three-input max / min (PTX max.f32 / min.f32 with three operands): the same value as the two-input
 // forms applied in turn, NaN operands ignored.
 __device__ __forceinline__ float max3f(float a, float b, float c) {
@@ -130,7 +132,7 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 }
 
 __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint32_t idx, const LevelRay &r,
-                                           float tmax, uint2 &ngroup, uint2 &tgroup) {
+                                           uint32_t order, float tmax, uint2 &ngroup, uint2 &tgroup) {
     const uint4 *np = nodes + static_cast<size_t>(idx) * 5;
     const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
     const float sx = __uint_as_float((n0.w & 0xFFu) << 23);
@@ -154,7 +156,7 @@ __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint
         // octant. bit4 = the hit-mask bit index of each child, bits4 = the bits it sets there (0 for an
         // empty slot, whose meta byte is 0, so empty slots need no test of their own).
         const uint32_t inner4 = (meta4 & (meta4 << 1)) & 0x10101010u;
-        const uint32_t bit4 = (meta4 ^ ((inner4 >> 4) * r.oct)) & 0x1F1F1F1Fu;
+        const uint32_t bit4 = (meta4 ^ ((inner4 >> 4) * order)) & 0x1F1F1F1Fu;
         const uint32_t bits4 = (meta4 >> 5) & 0x07070707u;
 #endif
 #pragma unroll
@@ -180,7 +182,7 @@ __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint
 #else
             if (m != 0u && t0 <= t1) {
                 uint32_t bit = m & 0x1Fu;
-                if ((m & 0x18u) == 0x18u) bit ^= r.oct;
+                if ((m & 0x18u) == 0x18u) bit ^= order;
                 hitmask |= ((m >> 5) & 7u) << bit;
             }
 #endif
@@ -188,6 +190,52 @@ __device__ __forceinline__ void visit_node(const uint4 *__restrict__ nodes, uint
     }
     ngroup = make_uint2(n1.x, (hitmask & 0xFF000000u) | (n0.w >> 24));
     tgroup = make_uint2(n1.y, hitmask & 0x00FFFFFFu);
+}
+
+// Möller–Trumbore (MeshRenderProxy.cpp:128-194) of triangle record `idx` in the level ray's (the instance's
+// local) space: true when the ray passes with local t > Eps, with (t, u, v) and the record's face index.
+__device__ __forceinline__ bool triangle_hit(const float4 *__restrict__ tris, uint32_t idx, const LevelRay &ray,
+                                             float &t, float &u, float &v, uint32_t &face) {
+    const float4 *tp = tris + static_cast<size_t>(idx) * 3;
+    const float4 a4 = __ldg(tp), b4 = __ldg(tp + 1), c4 = __ldg(tp + 2);
+    const f3 p0 = mk3(a4.x, a4.y, a4.z), e1 = mk3(a4.w, b4.x, b4.y), e2 = mk3(b4.z, b4.w, c4.x);
+    const f3 h = cross(ray.d, e2);
+    const float det = dot3(e1, h);
+    if (fabsf(det) < kEps) return false;
+    const f3 s = ray.o - p0;
+#if SPK_MT_RCP
+    const float f = __frcp_rn(det);
+#else
+    const float f = 1.f / det;
+#endif
+    u = f * dot3(s, h);
+    if (u < 0.f || u > 1.f) return false;
+    const f3 q = cross(s, e1);
+    v = f * dot3(ray.d, q);
+    if (v < 0.f || u + v > 1.f) return false;
+    t = f * dot3(e2, q);
+    face = __float_as_uint(c4.y);
+    return t > kEps;
+}
+
+// World t of a local hit at `t`, the reference's way: from the x component only (Ray::InverseAt, Ray.h:43-47).
+__device__ __forceinline__ float world_t(const DevInstance &I, const LevelRay &ray, float t, f3 wo, f3 wd) {
+    const f3 wp = xform_point(I.m, ray.o + ray.d * t);
+    return (wp.x - wo.x) / wd.x;
+}
+
+// SphereRenderProxy::IntersectInternal (SphereRenderProxy.cpp:5-38) in world space: false when the
+// discriminant is negative, else true with the root the reference takes (the near one from outside).
+__device__ __forceinline__ bool sphere_hit(const DevInstance &I, f3 wo, f3 wd, float &t) {
+    const f3 center = mk3(I.m[3], I.m[7], I.m[11]);
+    const f3 co = wo - center;
+    const float half_b = dot3(wd, co);
+    const float c = sqnorm(co) - I.radius * I.radius;
+    const float disc = half_b * half_b - 1.f * c;
+    if (disc < 0.f) return false;
+    const float sq = sqrtf(disc);
+    t = (-half_b + (c >= 0.f ? -sq : sq)) / 1.f;
+    return true;
 }
 
 // Traversal stacks. Walker::push / pop address entry `i` (0 = bottom) of the current ray's stack.
@@ -246,6 +294,13 @@ struct RegTopStack {
     }
 };
 
+// True when a hit at world t `t` on (inst, face) replaces `best`: a smaller t, or an exact tie on a smaller
+// (instance, face).
+__device__ __forceinline__ bool closer_hit(const TraceResult &best, float t, uint32_t inst, uint32_t face) {
+    if (t < best.t) return true;
+    return t == best.t && (inst < best.inst || (inst == best.inst && face < best.face));
+}
+
 // Resumable two-level walk of one ray. init() starts it; step() advances by one node visit plus the
 // triangle tests it enables and returns true when the walk is over (result in `best`).
 template <int kMode, bool kCount>
@@ -282,8 +337,7 @@ struct Walker {
     // a strict <), which depends on the visit order; this walk's order depends on warp composition, so an
     // exact tie goes to the smaller (instance, face) instead, making every hit independent of scheduling.
     __device__ __forceinline__ bool closer(float t, uint32_t inst, uint32_t face) const {
-        if (t < best.t) return true;
-        return t == best.t && (inst < best.inst || (inst == best.inst && face < best.face));
+        return closer_hit(best, t, inst, face);
     }
 
     template <class Stack>
@@ -307,7 +361,7 @@ struct Walker {
             const uint32_t slot = bit ^ ray.oct;
             const uint32_t node_idx = ngroup.x + __popc(ngroup.y & 0xFFu & ((1u << slot) - 1u));
             if (ngroup.y > 0x00FFFFFFu) push(stack, ngroup, err);
-            visit_node(S.nodes, node_idx, ray, tmax_box, ngroup, tgroup);
+            visit_node(S.nodes, node_idx, ray, ray.oct, tmax_box, ngroup, tgroup);
             if (kCount) ++counts->nodes;
             // Triangle postponing: when few lanes have triangles, keep walking nodes and test them later.
             const uint32_t want = __ballot_sync(__activemask(), tgroup.y != 0u);
@@ -334,27 +388,10 @@ struct Walker {
             tgroup.y &= tgroup.y - 1u;
             const uint32_t idx = tgroup.x + k;
             if (in_blas) {
-                // Möller–Trumbore (MeshRenderProxy.cpp:128-194) in the instance's local space.
                 if (kCount) ++counts->tris;
-                const float4 *tp = S.tris + static_cast<size_t>(idx) * 3;
-                const float4 a4 = __ldg(tp), b4 = __ldg(tp + 1), c4 = __ldg(tp + 2);
-                const f3 p0 = mk3(a4.x, a4.y, a4.z), e1 = mk3(a4.w, b4.x, b4.y), e2 = mk3(b4.z, b4.w, c4.x);
-                const f3 h = cross(ray.d, e2);
-                const float det = dot3(e1, h);
-                if (fabsf(det) < kEps) continue;
-                const f3 s = ray.o - p0;
-#if SPK_MT_RCP
-                const float f = __frcp_rn(det);
-#else
-                const float f = 1.f / det;
-#endif
-                const float u = f * dot3(s, h);
-                if (u < 0.f || u > 1.f) continue;
-                const f3 q = cross(s, e1);
-                const float v = f * dot3(ray.d, q);
-                if (v < 0.f || u + v > 1.f) continue;
-                const float t = f * dot3(e2, q);
-                if (!(t > kEps)) continue;
+                float t, u, v;
+                uint32_t face;
+                if (!triangle_hit(S.tris, idx, ray, t, u, v, face)) continue;
                 if (kMode == kTraceAnyRef) {
                     best.inst = cur_inst;
                     return true;
@@ -366,10 +403,7 @@ struct Walker {
                     }
                     continue;
                 }
-                const float *M = S.instances[cur_inst].m;
-                const f3 wp = xform_point(M, ray.o + ray.d * t);
-                const float wt = (wp.x - wo.x) / wd.x;
-                const uint32_t face = __float_as_uint(c4.y);
+                const float wt = world_t(S.instances[cur_inst], ray, t, wo, wd);
                 if (wt > 0.f && closer(wt, cur_inst, face)) {
                     best.t = wt;
                     best.u = u;
@@ -382,7 +416,8 @@ struct Walker {
                 const uint32_t inst = __ldg(S.tlas_items + idx);
                 const DevInstance &I = S.instances[inst];
                 if (I.type == 1u) {
-                    // SphereRenderProxy::IntersectInternal (SphereRenderProxy.cpp:5-38), world space.
+                    // SphereRenderProxy::IntersectInternal (SphereRenderProxy.cpp:5-38), world space: sphere_hit's
+                    // test, written out so the any-hit modes stop before the square root.
                     const f3 center = mk3(I.m[3], I.m[7], I.m[11]);
                     const f3 co = wo - center;
                     const float half_b = dot3(wd, co);
@@ -505,6 +540,145 @@ __device__ __forceinline__ void walk_persistent(const DevScene &S, unsigned long
             }
             if (!exhausted && __popc(__ballot_sync(__activemask(), active)) < kRefillLanes) break;
         }
+    }
+}
+
+// Closest-hit walk of coherent rays in packets (primary rays: the samples of one pixel, or neighbouring
+// pixels). Each warp takes 32 consecutive items of the work list and walks them together: one node or
+// triangle group at a time for the whole warp, every lane testing its own ray, in the order of lane 0's
+// octant. A lane only tests the children it hit itself (its own bits, kept beside each shared group on the
+// stack), against its own best t, so every box and triangle it tests is one its own walk would reach;
+// the warp visits the union of its rays' walks with all 32 lanes busy instead of each lane walking alone.
+// The closest hit never depends on the visiting order (exact ties go to the smaller (instance, face)), so
+// the results are walk_persistent's. The list must hold one scene: `fetch` returns the same TLAS root for
+// every item. `fetch(i, o, d, tmax)` and `finish(i, result)` as for walk_persistent; every lane of the warp
+// must call this.
+template <bool kCount, class Fetch, class Finish>
+__device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long long *cursor, unsigned long long n,
+                                             uint32_t &err, TraceCounts *counts, Fetch &&fetch, Finish &&finish) {
+    constexpr uint32_t kAll = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t budget = S.walk_budget ? S.walk_budget : kMaxIterations;
+    uint2 groups[kStackSize];  // the shared groups (the same in every lane)
+    uint32_t own[kStackSize];  // this lane's hit bits of each
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(cursor, 32ull);
+        base = __shfl_sync(kAll, base, 0);
+        if (base >= n) break;
+        const unsigned long long item = base + lane;
+        const bool valid = item < n;
+        f3 wo = mk3(0.f, 0.f, 0.f), wd = mk3(1.f, 1.f, 1.f);
+        uint32_t root = kInvalid;
+        if (valid) {
+            float tm = kFltMax;
+            root = fetch(item, wo, wd, tm);
+        }
+        root = __shfl_sync(kAll, root, 0);  // lane 0 always holds an item
+        LevelRay ray;
+        setup_level(ray, wo, wd);
+        const uint32_t top_order = __shfl_sync(kAll, ray.oct, 0);
+        uint32_t order = top_order;
+        TraceResult best{kFltMax, 0.f, 0.f, kInvalid, kInvalid};
+        float tmax_box = kFltMax;
+        uint2 ngroup = make_uint2(root, root == kInvalid ? 0u : (1u << 24)), tgroup = make_uint2(0u, 0u);
+        uint32_t nown = valid ? (1u << 24) : 0u, town = 0u;
+        int sp = 0, blas_sp = 0;
+        bool in_blas = false;
+        uint32_t cur_inst = 0, iter = 0;
+        auto push = [&](uint2 g, uint32_t mine) {
+            if (sp < kStackSize) {
+                groups[sp] = g;
+                own[sp] = mine;
+                ++sp;
+            } else {
+                err |= kErrStackOverflow;
+            }
+        };
+        for (;;) {
+            if (++iter > budget) {
+                err |= kErrIterationBudget;
+                break;
+            }
+            if (ngroup.y > 0x00FFFFFFu) {
+                const uint32_t bit = __ffs(ngroup.y >> 24) - 1;
+                const uint32_t keep = ~(1u << (bit + 24));
+                const bool mine = (nown >> (bit + 24)) & 1u;
+                ngroup.y &= keep;
+                nown &= keep;
+                const uint32_t slot = bit ^ order;
+                const uint32_t node_idx = ngroup.x + __popc(ngroup.y & 0xFFu & ((1u << slot) - 1u));
+                if (ngroup.y > 0x00FFFFFFu) push(ngroup, nown);
+                // A lane that did not reach this node tests its boxes against t <= -1: no hits.
+                visit_node(S.nodes, node_idx, ray, order, mine ? tmax_box : -1.f, ngroup, tgroup);
+                if (kCount && mine) ++counts->nodes;
+                nown = ngroup.y & 0xFF000000u;
+                town = tgroup.y;
+                const uint32_t any = __reduce_or_sync(kAll, nown | town);
+                ngroup.y = (any & 0xFF000000u) | (ngroup.y & 0xFFu);
+                tgroup.y = any & 0x00FFFFFFu;
+            } else {
+                tgroup = ngroup;
+                town = nown;
+                ngroup = make_uint2(0u, 0u);
+                nown = 0u;
+            }
+            while (tgroup.y != 0u) {
+                const uint32_t k = __ffs(tgroup.y) - 1;
+                tgroup.y &= tgroup.y - 1u;
+                const bool mine = (town >> k) & 1u;
+                const uint32_t idx = tgroup.x + k;
+                if (in_blas) {
+                    if (!mine) continue;
+                    if (kCount) ++counts->tris;
+                    float t, u, v;
+                    uint32_t face;
+                    if (!triangle_hit(S.tris, idx, ray, t, u, v, face)) continue;
+                    const float wt = world_t(S.instances[cur_inst], ray, t, wo, wd);
+                    if (wt > 0.f && closer_hit(best, wt, cur_inst, face)) {
+                        best = TraceResult{wt, u, v, cur_inst, face};
+                        tmax_box = prune_limit(best.t, wo, wd, S.scene_abs_x);
+                    }
+                } else {
+                    const uint32_t inst = __ldg(S.tlas_items + idx);
+                    const DevInstance &I = S.instances[inst];
+                    if (I.type == 1u) {
+                        float t;
+                        if (mine && sphere_hit(I, wo, wd, t) && t > 0.f && closer_hit(best, t, inst, kInvalid)) {
+                            best = TraceResult{t, 0.f, 0.f, inst, kInvalid};
+                            tmax_box = prune_limit(best.t, wo, wd, S.scene_abs_x);
+                        }
+                    } else if (I.blas_root != kInvalid) {
+                        // Enter the BLAS with every lane (those that did not reach it take no part); the
+                        // rest of this TLAS level waits on the stack.
+                        if (tgroup.y != 0u) push(tgroup, town);
+                        if (ngroup.y > 0x00FFFFFFu) push(ngroup, nown);
+                        blas_sp = sp;
+                        in_blas = true;
+                        cur_inst = inst;
+                        setup_level(ray, xform_point(I.minv, wo), xform_dir(I.minv, wd));
+                        const uint32_t entering = __ballot_sync(kAll, mine);  // not empty: the group had bit k
+                        order = __shfl_sync(kAll, ray.oct, __ffs(entering) - 1);
+                        ngroup = make_uint2(I.blas_root, 1u << 24);
+                        nown = mine ? (1u << 24) : 0u;
+                        tgroup.y = 0u;
+                        break;
+                    }
+                }
+            }
+            if (ngroup.y <= 0x00FFFFFFu) {
+                if (in_blas && sp == blas_sp) {
+                    in_blas = false;
+                    setup_level(ray, wo, wd);
+                    order = top_order;
+                }
+                if (sp == 0) break;
+                --sp;
+                ngroup = groups[sp];
+                nown = own[sp];
+            }
+        }
+        if (valid) finish(item, best);
     }
 }
 

@@ -22,6 +22,7 @@ constexpr int kCursor = 2;        // pop cursor of the running persistent stage
 constexpr int kShadowLen = 4;     // occlusion rays queued by the iteration's shade stage
 constexpr int kNeeLen = 5;        // light-sampling vertices of the iteration's shade stage
 constexpr int kShadowCursor = 6;  // pop cursor of the shadow stage
+constexpr int kPacketQueue = 7;   // nonzero: the extend queue is in item order (primary rays), walk it in packets
 
 template <int kKind>
 __device__ __forceinline__ void load_rng(const uint4 *rng, uint32_t pid, Rng &r) {
@@ -198,7 +199,7 @@ __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontSta
 // ------------------------------------------------------------------------------------------------
 template <int kKind>
 __global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers fb, RenderParams p, WavefrontState s,
-                                                     Counters *counters) {
+                                                     uint32_t packets, Counters *counters) {
     const uint32_t i = blockIdx.x * 16u + (threadIdx.x & 15u);
     const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 4);
     if (i >= fb.width || j >= fb.height) return;
@@ -206,33 +207,45 @@ __global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers
     start_path<kKind>(cam, p, s, pid, i, j, fb.width, fb.height, p.frame_seed);
     if (p.spatial_denoise) fb.gnormal[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
     s.queue[0][pid] = pid;
-    if (pid == 0) counters->queue_counters[kLen0] = static_cast<unsigned long long>(fb.width) * fb.height;
+    if (pid == 0) {
+        counters->queue_counters[kLen0] = static_cast<unsigned long long>(fb.width) * fb.height;
+        counters->queue_counters[kPacketQueue] = packets;
+    }
 }
 
 // Extend: persistent warps pull paths from the queue, refilling lanes whose walk has finished. With
-// kBatch each path traces in its own scene (the TLAS root its slot recorded at start).
-template <bool kCount, bool kBatch = false>
+// kBatch each path traces in its own scene (the TLAS root its slot recorded at start). kPackets walks a
+// queue still in item order (the primary rays a generate kernel just queued, flagged in kPacketQueue) in
+// packets of 32 consecutive paths instead: the samples of one pixel, or neighbouring pixels, take the same
+// nodes. Both forms are launched for a single-scene queue and the one the flag does not name returns at
+// once, so the choice needs no host round trip (and stays inside a replayed graph).
+template <bool kCount, bool kBatch = false, bool kPackets = false>
 __global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_wf_extend(DevScene S, WavefrontState s, int in_queue,
                                                       Counters *counters) {
+    static_assert(!(kBatch && kPackets), "packets hold one scene");
+    if (!kBatch && (counters->queue_counters[kPacketQueue] != 0u) != kPackets) return;
     uint32_t err = 0, done = 0;
     TraceCounts tc;
     const unsigned long long n = counters->queue_counters[in_queue];
     const uint32_t *queue = s.queue[in_queue];
     uint32_t pid = 0;
-    walk_persistent<kTraceClosest, kCount>(
-        S, &counters->queue_counters[kCursor], n, kFltMax, err, &tc,
-        [&](unsigned long long q, f3 &o, f3 &d, float &) {
-            pid = queue[q];
-            const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
-            o = mk3(o4.x, o4.y, o4.z);
-            d = mk3(d4.x, d4.y, d4.z);
-            return kBatch ? s.slot_root[pid] : S.tlas_root;
-        },
-        [&](unsigned long long, const TraceResult &h) {
-            s.hit[pid] = make_float4(h.t, h.u, h.v, __uint_as_float(h.inst));
-            s.hit_face[pid] = h.face;
-            ++done;
-        });
+    auto fetch = [&](unsigned long long q, f3 &o, f3 &d, float &) {
+        pid = queue[q];
+        const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
+        o = mk3(o4.x, o4.y, o4.z);
+        d = mk3(d4.x, d4.y, d4.z);
+        return kBatch ? s.slot_root[pid] : S.tlas_root;
+    };
+    auto finish = [&](unsigned long long, const TraceResult &h) {
+        s.hit[pid] = make_float4(h.t, h.u, h.v, __uint_as_float(h.inst));
+        s.hit_face[pid] = h.face;
+        ++done;
+    };
+    if constexpr (kPackets)
+        walk_packets<kCount>(S, &counters->queue_counters[kCursor], n, err, &tc, fetch, finish);
+    else
+        walk_persistent<kTraceClosest, kCount>(S, &counters->queue_counters[kCursor], n, kFltMax, err, &tc, fetch,
+                                               finish);
     warp_add_u64(&counters->extension_rays, done);
     if (kCount) {
         warp_add_u64(&counters->node_visits, tc.nodes);
@@ -247,6 +260,7 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_wf_shade(DevScene
     uint32_t shadow = 0, err = 0;
     const unsigned long long n = counters->queue_counters[in_queue];
     const int out_queue = in_queue ^ 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) counters->queue_counters[kPacketQueue] = 0u;  // the next queue is mixed
     const uint32_t *queue = s.queue[in_queue];
     for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
          q0 += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
@@ -328,7 +342,7 @@ __device__ __forceinline__ void start_item(const DevCamera &cam, const RenderPar
 template <int kKind>
 __global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers fb, RenderParams p,
                                                      WavefrontState s, uint32_t frame_base, uint32_t initial,
-                                                     uint32_t total_items, Counters *counters) {
+                                                     uint32_t total_items, uint32_t packets, Counters *counters) {
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= initial) return;
     start_item<kKind>(cam, p, s, slot, slot, fb.width, fb.height, frame_base, total_items);
@@ -336,6 +350,7 @@ __global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers
     if (slot == 0) {
         counters->queue_counters[kLen0] = initial;
         counters->queue_counters[kNextItem] = initial;
+        counters->queue_counters[kPacketQueue] = packets;
     }
 }
 
@@ -348,6 +363,7 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_mf_shade(DevScene
     uint32_t shadow = 0, err = 0;
     const unsigned long long n = counters->queue_counters[in_queue];
     const int out_queue = in_queue ^ 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) counters->queue_counters[kPacketQueue] = 0u;  // the next queue is mixed
     const uint32_t *queue = s.queue[in_queue];
     const uint32_t lane = threadIdx.x & 31u;
     for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
@@ -640,6 +656,7 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_b_shade(DevScene 
     uint32_t shadow = 0, err = 0;
     const unsigned long long n = counters->queue_counters[in_queue];
     const int out_queue = in_queue ^ 1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) counters->queue_counters[kPacketQueue] = 0u;  // the next queue is mixed
     const uint32_t *queue = s.queue[in_queue];
     const uint32_t lane = threadIdx.x & 31u;
     for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
@@ -818,15 +835,23 @@ unsigned extend_blocks(int num_sms, uint32_t per_sm_override) {
     return static_cast<unsigned>(num_sms) * n;
 }
 
+// Kernel launches of one extend stage: a single-scene queue gets the packet and the persistent form.
+constexpr uint32_t extend_launches(bool batch) { return batch ? 1u : 2u; }
+
 cudaError_t launch_extend(const DevScene &scene, const WavefrontState &s, int in, bool count, Counters *counters,
                           unsigned grid, cudaStream_t stream, LaunchEvents *ev, bool batch = false) {
     unsigned long long *qc = counters->queue_counters;
     cudaError_t e = cudaMemsetAsync(qc + kCursor, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     if (ev) ev->before(stream);
-    auto *kern = batch ? (count ? k_wf_extend<true, true> : k_wf_extend<false, true>)
-                       : (count ? k_wf_extend<true, false> : k_wf_extend<false, false>);
-    kern<<<grid, 128, 0, stream>>>(scene, s, in, counters);
+    if (batch) {
+        (count ? k_wf_extend<true, true> : k_wf_extend<false, true>)<<<grid, 128, 0, stream>>>(scene, s, in, counters);
+    } else {
+        (count ? k_wf_extend<true, false, true> : k_wf_extend<false, false, true>)<<<grid, 128, 0, stream>>>(
+            scene, s, in, counters);
+        (count ? k_wf_extend<true, false> : k_wf_extend<false, false>)<<<grid, 128, 0, stream>>>(scene, s, in,
+                                                                                                 counters);
+    }
     if (ev) ev->after(stream);
     return cudaSuccess;
 }
@@ -956,9 +981,9 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
     if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
     const dim3 ggrid((fbuf.width + 15) / 16, (fbuf.height + 7) / 8);
     if (p.rng == 0) {
-        k_wf_generate<0><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, counters);
+        k_wf_generate<0><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, tuning.packets, counters);
     } else {
-        k_wf_generate<1><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, counters);
+        k_wf_generate<1><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, tuning.packets, counters);
     }
     ++nl;
     const unsigned shade_blocks = static_cast<unsigned>(num_sms) * tuning.shade_blocks_per_sm;
@@ -972,7 +997,7 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
             nl += 3;
         }
         if ((e = launch_extend(scene, se, in, count, counters, extend_grid, stream, ev)) != cudaSuccess) return e;
-        ++nl;
+        nl += extend_launches(false);
         WavefrontState ss = se;
         if (tuning.material_sort) {
             ss = enqueue_material_sort(scene, se, in, counters, num_sms, stream);
@@ -1058,10 +1083,10 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
         if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
         if (p.rng == 0) {
             k_mf_generate<0><<<(initial + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, initial, total_items,
-                                                                     counters);
+                                                                     tuning.packets, counters);
         } else {
             k_mf_generate<1><<<(initial + 127) / 128, 128, 0, stream>>>(cam, fbuf, p, s, f0, initial, total_items,
-                                                                     counters);
+                                                                     tuning.packets, counters);
         }
         ++nl;
         // One chunk: kChunk iterations of (reset the output queue, extend, shade).
@@ -1176,7 +1201,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 return e;
             }
             iter += kChunk;
-            nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
+            nl += (1u + extend_launches(false) + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
                    (nee == kNeeDeferred ? 2u : 0u)) * kChunk;
             if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
                 cudaSuccess)
@@ -1248,8 +1273,8 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         iter += kChunk;
-        nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) + (nee == kNeeDeferred ? 2u : 0u)) *
-              kChunk;
+        nl += (1u + extend_launches(true) + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
+               (nee == kNeeDeferred ? 2u : 0u)) * kChunk;
         if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
             cudaSuccess)
             return e;

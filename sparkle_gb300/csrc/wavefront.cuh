@@ -76,6 +76,7 @@ struct WfTuning {
     uint32_t slots_per_pixel = 1;  // multi-frame schedule: path slots per pixel (bounded by the state's capacity)
     uint32_t batch_slots = 0;      // batch schedule: paths in flight (0 = the state's capacity)
     bool shadow_stage = true;      // NEE occlusion rays walked by their own persistent stage (false: inline in shade)
+    uint32_t packets = 1;          // 1: primary rays (the first extend of a pass or frame) walked in warp packets
 };
 
 // Allocates the shadow-stage buffers of `s` for its capacity (no-op when they are large enough).

@@ -5,7 +5,7 @@ from sparkle_gb300 import autotune as at
 
 DEFAULTS = dict(cuda_graph=1, material_sort=0, bvh_width=8, bvh_leaf_size=3, extend_blocks_per_sm=0,
                 shade_blocks_per_sm=8, batch_slots=0, ray_sort=0, bvh_collapse=0, bvh_builder=0,
-                path_slots_per_pixel=64, shadow_stage=1, multi_frame=1)
+                path_slots_per_pixel=64, shadow_stage=1, multi_frame=1, primary_packets=1)
 
 
 class FakeContext:

@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 
 DEFAULTS = dict(cuda_graph=1, material_sort=0, bvh_width=8, bvh_leaf_size=3, extend_blocks_per_sm=0,
                 shade_blocks_per_sm=8, batch_slots=0, ray_sort=0, bvh_collapse=0, bvh_builder=0,
-                path_slots_per_pixel=64, shadow_stage=1, multi_frame=1)
+                path_slots_per_pixel=64, shadow_stage=1, multi_frame=1, primary_packets=1)
 
 VARIANTS = [
     dict(cuda_graph=0),
@@ -36,6 +36,9 @@ VARIANTS = [
     dict(shadow_stage=0, material_sort=1, path_slots_per_pixel=2),
     dict(multi_frame=0),
     dict(multi_frame=0, shadow_stage=0, material_sort=1),
+    dict(primary_packets=0),
+    dict(primary_packets=0, multi_frame=0),
+    dict(bvh_width=4, bvh_leaf_size=1, ray_sort=1),  # packets over a sorted queue and a narrow tree
 ]
 
 
@@ -63,7 +66,8 @@ def test_tuning_defaults_and_validation(ctx):
     assert ctx.tuning() == DEFAULTS
     for bad in [dict(bvh_width=1), dict(bvh_width=9), dict(bvh_leaf_size=0), dict(bvh_leaf_size=4),
                 dict(cuda_graph=2), dict(shade_blocks_per_sm=0), dict(extend_blocks_per_sm=33),
-                dict(path_slots_per_pixel=0), dict(path_slots_per_pixel=65), dict(shadow_stage=2), dict(multi_frame=2)]:
+                dict(path_slots_per_pixel=0), dict(path_slots_per_pixel=65), dict(shadow_stage=2), dict(multi_frame=2),
+                dict(primary_packets=2)]:
         with pytest.raises(native.SpkError):
             ctx.set_tuning(**bad)
         assert ctx.tuning() == DEFAULTS  # a rejected setting leaves the previous one
