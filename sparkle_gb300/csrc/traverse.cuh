@@ -54,6 +54,9 @@ enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOve
 #ifndef SPK_WALK_MIN_BLOCKS
 #define SPK_WALK_MIN_BLOCKS 8  // resident 128-thread blocks per SM the walking kernels are compiled for
 #endif
+#ifndef SPK_PACKET_MIN_BLOCKS
+#define SPK_PACKET_MIN_BLOCKS 8  // resident 128-thread blocks per SM the packet walk is compiled for
+#endif
 #ifndef SPK_SMEM_STACK
 #define SPK_SMEM_STACK 0  // top entries of each persistent walk's stack kept in shared memory (0: all local)
 #endif
@@ -543,16 +546,102 @@ __device__ __forceinline__ void walk_persistent(const DevScene &S, unsigned long
     }
 }
 
+// Order-preserving map of a float to an int (and back) for warp min / max reductions.
+__device__ __forceinline__ int float_key(float x) {
+    const int b = __float_as_int(x);
+    return b ^ ((b >> 31) & 0x7FFFFFFF);
+}
+__device__ __forceinline__ float key_float(int k) { return __int_as_float(k ^ ((k >> 31) & 0x7FFFFFFF)); }
+__device__ __forceinline__ float warp_min(float x) { return key_float(__reduce_min_sync(0xFFFFFFFFu, float_key(x))); }
+__device__ __forceinline__ float warp_max(float x) { return key_float(__reduce_max_sync(0xFFFFFFFFu, float_key(x))); }
+
+// Bounds of a packet's level rays: origins and slab reciprocals per axis over the warp's 32 lanes.
+struct PacketFrustum {
+    f3 omin, omax, imin, imax;
+};
+
+// Fills `f` from every lane's level ray and returns true when the packet can be tested as one: every lane's
+// direction lies in octant `order` and no component is small enough for slab_inverse's 2^100 stand-in
+// (so every bound below stays finite). Every lane of the warp must call this.
+__device__ __forceinline__ bool make_frustum(const LevelRay &r, uint32_t order, PacketFrustum &f) {
+    const bool regular = fabsf(r.inv.x) < 0x1p24f && fabsf(r.inv.y) < 0x1p24f && fabsf(r.inv.z) < 0x1p24f;
+    if (!__all_sync(0xFFFFFFFFu, r.oct == order && regular)) return false;
+    f.omin = mk3(warp_min(r.o.x), warp_min(r.o.y), warp_min(r.o.z));
+    f.omax = mk3(warp_max(r.o.x), warp_max(r.o.y), warp_max(r.o.z));
+    f.imin = mk3(warp_min(r.inv.x), warp_min(r.inv.y), warp_min(r.inv.z));
+    f.imax = mk3(warp_max(r.inv.x), warp_max(r.inv.y), warp_max(r.inv.z));
+    return true;
+}
+
+// Bounds over the packet of one axis's slab terms: a = s * inv and o = (p - org) * inv, the two values
+// visit_node forms per ray (t = fma(q, a, o) for a plane byte q). Each is a product or difference of the
+// lanes' values, so rounding to nearest keeps them within the products and differences of the extremes.
+__device__ __forceinline__ void axis_bounds(float p, float s, float omin, float omax, float imin, float imax,
+                                            float &alo, float &ahi, float &olo, float &ohi) {
+    alo = s * imin;
+    ahi = s * imax;
+    const float nlo = p - omax, nhi = p - omin;
+    const float c0 = nlo * imin, c1 = nlo * imax, c2 = nhi * imin, c3 = nhi * imax;
+    olo = fminf(fminf(c0, c1), fminf(c2, c3));
+    ohi = fmaxf(fmaxf(c0, c1), fmaxf(c2, c3));
+}
+
+// visit_node for a whole packet at once: lane k tests child slot k mod 8 against the packet's bounds and the
+// warp ORs the results. fma(q, a, o) grows with a (q >= 0) and with o, so the lower bound of each near-plane
+// t and the upper bound of each far-plane t take the extremes of a and o: a child passes whenever it passes
+// for at least one lane's own ray with that lane's tmax (<= `tmax`), as visit_node computes it, and may pass
+// for none (the packet then visits a node that none of its rays needs, which only costs time). Every lane of
+// the warp must call this; the result is the same in every lane.
+__device__ __forceinline__ void visit_node_frustum(const uint4 *__restrict__ nodes, uint32_t idx,
+                                                   const PacketFrustum &f, uint32_t order, float tmax,
+                                                   uint2 &ngroup, uint2 &tgroup) {
+    const uint4 *np = nodes + static_cast<size_t>(idx) * 5;
+    const uint4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2), n3 = __ldg(np + 3), n4 = __ldg(np + 4);
+    float axlo, axhi, oxlo, oxhi, aylo, ayhi, oylo, oyhi, azlo, azhi, ozlo, ozhi;
+    axis_bounds(__uint_as_float(n0.x), __uint_as_float((n0.w & 0xFFu) << 23), f.omin.x, f.omax.x, f.imin.x,
+                f.imax.x, axlo, axhi, oxlo, oxhi);
+    axis_bounds(__uint_as_float(n0.y), __uint_as_float(((n0.w >> 8) & 0xFFu) << 23), f.omin.y, f.omax.y, f.imin.y,
+                f.imax.y, aylo, ayhi, oylo, oyhi);
+    axis_bounds(__uint_as_float(n0.z), __uint_as_float(((n0.w >> 16) & 0xFFu) << 23), f.omin.z, f.omax.z,
+                f.imin.z, f.imax.z, azlo, azhi, ozlo, ozhi);
+    const uint32_t slot = threadIdx.x & 7u, h = slot >> 2, c = slot & 3u;
+    const uint32_t meta4 = h ? n1.w : n1.z;
+    const uint32_t lox = h ? n2.y : n2.x, loy = h ? n2.w : n2.z, loz = h ? n3.y : n3.x;
+    const uint32_t hix = h ? n3.w : n3.z, hiy = h ? n4.y : n4.x, hiz = h ? n4.w : n4.z;
+    const uint32_t nx = (order & 1u) ? hix : lox, fx = (order & 1u) ? lox : hix;
+    const uint32_t ny = (order & 2u) ? hiy : loy, fy = (order & 2u) ? loy : hiy;
+    const uint32_t nz = (order & 4u) ? hiz : loz, fz = (order & 4u) ? loz : hiz;
+    const uint32_t sel = 0x4440u | c;
+    const float t0 = fmaxf(fmaxf(fmaf(static_cast<float>(__byte_perm(nx, 0u, sel)), axlo, oxlo),
+                                 fmaf(static_cast<float>(__byte_perm(ny, 0u, sel)), aylo, oylo)),
+                           fmaxf(fmaf(static_cast<float>(__byte_perm(nz, 0u, sel)), azlo, ozlo), 0.f));
+    const float t1 = fminf(fminf(fmaf(static_cast<float>(__byte_perm(fx, 0u, sel)), axhi, oxhi),
+                                 fmaf(static_cast<float>(__byte_perm(fy, 0u, sel)), ayhi, oyhi)),
+                           fminf(fmaf(static_cast<float>(__byte_perm(fz, 0u, sel)), azhi, ozhi), tmax));
+    const uint32_t m = __byte_perm(meta4, 0u, sel);
+    uint32_t bits = 0u;
+    if (m != 0u && t0 <= t1) {
+        uint32_t bit = m & 0x1Fu;
+        if ((m & 0x18u) == 0x18u) bit ^= order;
+        bits = ((m >> 5) & 7u) << bit;
+    }
+    const uint32_t any = __reduce_or_sync(0xFFFFFFFFu, bits);
+    ngroup = make_uint2(n1.x, (any & 0xFF000000u) | (n0.w >> 24));
+    tgroup = make_uint2(n1.y, any & 0x00FFFFFFu);
+}
+
 // Closest-hit walk of coherent rays in packets (primary rays: the samples of one pixel, or neighbouring
 // pixels). Each warp takes 32 consecutive items of the work list and walks them together: one node or
-// triangle group at a time for the whole warp, every lane testing its own ray, in the order of lane 0's
-// octant. A lane only tests the children it hit itself (its own bits, kept beside each shared group on the
-// stack), against its own best t, so every box and triangle it tests is one its own walk would reach;
-// the warp visits the union of its rays' walks with all 32 lanes busy instead of each lane walking alone.
-// The closest hit never depends on the visiting order (exact ties go to the smaller (instance, face)), so
-// the results are walk_persistent's. The list must hold one scene: `fetch` returns the same TLAS root for
-// every item. `fetch(i, o, d, tmax)` and `finish(i, result)` as for walk_persistent; every lane of the warp
-// must call this.
+// triangle group at a time for the whole warp, in the order of lane 0's octant, every lane testing its own
+// ray against each triangle. When all the packet's rays share that octant (checked per level, TLAS and each
+// BLAS), a node's 8 children are tested once for the whole packet (visit_node_frustum: one child per lane
+// against the bounds of the lanes' rays); otherwise every lane tests them with its own ray (visit_node) and
+// takes only the children it hit itself. Either way a lane tests every box and triangle its own walk would
+// reach, and prunes only beyond its own best t; it may test more. Its result is still the smallest world t
+// over every triangle and sphere its ray hits (exact ties to the smaller (instance, face)), which no visiting
+// order or extra test changes: the results are walk_persistent's. The list must hold one scene: `fetch`
+// returns the same TLAS root for every item. `fetch(i, o, d, tmax)` and `finish(i, result)` as for
+// walk_persistent; every lane of the warp must call this.
 template <bool kCount, class Fetch, class Finish>
 __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long long *cursor, unsigned long long n,
                                              uint32_t &err, TraceCounts *counts, Fetch &&fetch, Finish &&finish) {
@@ -574,15 +663,27 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
             float tm = kFltMax;
             root = fetch(item, wo, wd, tm);
         }
-        root = __shfl_sync(kAll, root, 0);  // lane 0 always holds an item
+        // Lane 0 always holds an item; lanes past the end of the list walk a copy of its ray (their results
+        // are dropped), which keeps the packet's bounds and octant those of its real rays.
+        root = __shfl_sync(kAll, root, 0);
+        {
+            const f3 o0 = mk3(__shfl_sync(kAll, wo.x, 0), __shfl_sync(kAll, wo.y, 0), __shfl_sync(kAll, wo.z, 0));
+            const f3 d0 = mk3(__shfl_sync(kAll, wd.x, 0), __shfl_sync(kAll, wd.y, 0), __shfl_sync(kAll, wd.z, 0));
+            if (!valid) {
+                wo = o0;
+                wd = d0;
+            }
+        }
         LevelRay ray;
         setup_level(ray, wo, wd);
         const uint32_t top_order = __shfl_sync(kAll, ray.oct, 0);
         uint32_t order = top_order;
+        PacketFrustum frustum;
+        bool packed = make_frustum(ray, order, frustum);  // the level's nodes are tested once for the packet
         TraceResult best{kFltMax, 0.f, 0.f, kInvalid, kInvalid};
         float tmax_box = kFltMax;
         uint2 ngroup = make_uint2(root, root == kInvalid ? 0u : (1u << 24)), tgroup = make_uint2(0u, 0u);
-        uint32_t nown = valid ? (1u << 24) : 0u, town = 0u;
+        uint32_t nown = 1u << 24, town = 0u;
         int sp = 0, blas_sp = 0;
         bool in_blas = false;
         uint32_t cur_inst = 0, iter = 0;
@@ -609,14 +710,23 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                 const uint32_t slot = bit ^ order;
                 const uint32_t node_idx = ngroup.x + __popc(ngroup.y & 0xFFu & ((1u << slot) - 1u));
                 if (ngroup.y > 0x00FFFFFFu) push(ngroup, nown);
-                // A lane that did not reach this node tests its boxes against t <= -1: no hits.
-                visit_node(S.nodes, node_idx, ray, order, mine ? tmax_box : -1.f, ngroup, tgroup);
                 if (kCount && mine) ++counts->nodes;
-                nown = ngroup.y & 0xFF000000u;
-                town = tgroup.y;
-                const uint32_t any = __reduce_or_sync(kAll, nown | town);
-                ngroup.y = (any & 0xFF000000u) | (ngroup.y & 0xFFu);
-                tgroup.y = any & 0x00FFFFFFu;
+                if (packed) {
+                    // One test for the packet against the largest tmax of the lanes that reached the node
+                    // (tmax_box is never negative); those lanes take every child it passes.
+                    const float tmax = __uint_as_float(__reduce_max_sync(kAll, mine ? __float_as_uint(tmax_box) : 0u));
+                    visit_node_frustum(S.nodes, node_idx, frustum, order, tmax, ngroup, tgroup);
+                    nown = mine ? (ngroup.y & 0xFF000000u) : 0u;
+                    town = mine ? tgroup.y : 0u;
+                } else {
+                    // A lane that did not reach this node tests its boxes against t <= -1: no hits.
+                    visit_node(S.nodes, node_idx, ray, order, mine ? tmax_box : -1.f, ngroup, tgroup);
+                    nown = ngroup.y & 0xFF000000u;
+                    town = tgroup.y;
+                    const uint32_t any = __reduce_or_sync(kAll, nown | town);
+                    ngroup.y = (any & 0xFF000000u) | (ngroup.y & 0xFFu);
+                    tgroup.y = any & 0x00FFFFFFu;
+                }
             } else {
                 tgroup = ngroup;
                 town = nown;
@@ -659,6 +769,7 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                         setup_level(ray, xform_point(I.minv, wo), xform_dir(I.minv, wd));
                         const uint32_t entering = __ballot_sync(kAll, mine);  // not empty: the group had bit k
                         order = __shfl_sync(kAll, ray.oct, __ffs(entering) - 1);
+                        packed = make_frustum(ray, order, frustum);
                         ngroup = make_uint2(I.blas_root, 1u << 24);
                         nown = mine ? (1u << 24) : 0u;
                         tgroup.y = 0u;
@@ -671,6 +782,7 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                     in_blas = false;
                     setup_level(ray, wo, wd);
                     order = top_order;
+                    if (sp != 0) packed = make_frustum(ray, order, frustum);
                 }
                 if (sp == 0) break;
                 --sp;

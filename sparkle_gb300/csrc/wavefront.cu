@@ -220,8 +220,8 @@ __global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers
 // nodes. Both forms are launched for a single-scene queue and the one the flag does not name returns at
 // once, so the choice needs no host round trip (and stays inside a replayed graph).
 template <bool kCount, bool kBatch = false, bool kPackets = false>
-__global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_wf_extend(DevScene S, WavefrontState s, int in_queue,
-                                                      Counters *counters) {
+__global__ void __launch_bounds__(128, kPackets ? SPK_PACKET_MIN_BLOCKS : SPK_WALK_MIN_BLOCKS)
+    k_wf_extend(DevScene S, WavefrontState s, int in_queue, Counters *counters) {
     static_assert(!(kBatch && kPackets), "packets hold one scene");
     if (!kBatch && (counters->queue_counters[kPacketQueue] != 0u) != kPackets) return;
     uint32_t err = 0, done = 0;
