@@ -285,9 +285,10 @@ def run_ours(args):
     ctx.set_config(cfg)
     ctx.set_camera(camera)
 
-    # Traffic accounting (untimed): count visited wide nodes and tested triangles over 2 frames.
+    # Traffic accounting (untimed): count visited wide nodes and tested triangles over one step's frames
+    # (a packet walk counts a node or triangle once per packet: one fetch serves its rays).
     ctx.set_instrumentation(True)
-    ctx.render(2)
+    ctx.render(SPP)
     cs = ctx.stats()
     ctx.set_instrumentation(False)
     bytes_per_ray = (NODE_BYTES * cs["node_visits"] + TRI_BYTES * cs["triangle_tests"]) / cs["extension_rays"] \
@@ -593,9 +594,10 @@ def denoise_metric(ctx):
 
 
 def run_profile_small(args):
-    """The bench workload cut to 2 frames (stress scene, 127 MB of nodes + triangles, larger than L2, at
-    1920x1080; `--nee` turns next-event estimation on): the case the ncu captures run on (one kernel, a few
-    launches, ~0.6 GB on the device)."""
+    """The bench workload cut to `--frames` frames (default 2; stress scene, 127 MB of nodes + triangles,
+    larger than L2, at 1920x1080; `--nee` turns next-event estimation on): the case the ncu captures run on
+    (one kernel, a few launches, ~0.3 GB on the device per frame). With F frames a packet of 32 primary rays
+    holds 32 / F pixels' samples (one pixel's at F >= 32, as in the 64-frame bench step)."""
     from sparkle_gb300 import abi, native, scenes
     scene, cam_args = scenes.terrain_spheres(0)
     w, h = WIDTH, HEIGHT
@@ -604,10 +606,11 @@ def run_profile_small(args):
     ctx.set_config(abi.make_config(w, h, spp=1, bounce=BOUNCE, rng=abi.SPK_RNG_XOSHIRO256SS, kernel=args.kernel,
                                    enable_nee=args.nee))
     ctx.set_camera(scenes.make_camera(cam_args, w, h))
-    ctx.render(2)
+    ctx.render(args.frames)
     st = ctx.stats()
     assert st["error_flags"] == 0, st
-    print(json.dumps({"profile_small": True, "nee": args.nee, "extension_rays": st["extension_rays"],
+    print(json.dumps({"profile_small": True, "frames": args.frames, "nee": args.nee,
+                      "extension_rays": st["extension_rays"],
                       "shadow_rays": st["shadow_rays"], "device_ms": st["device_ms"]}))
     ctx.close()
 
@@ -707,8 +710,9 @@ def main():
     ap.add_argument("--no-scene-update", action="store_true", help="skip the scene build / incremental update leg")
     ap.add_argument("--tune", default="", help="spk_tuning knobs, e.g. cuda_graph=0,material_sort=1,bvh_width=4")
     ap.add_argument("--profile-small", action="store_true",
-                    help="ncu capture case: the bench workload cut to 2 frames, no timing output")
+                    help="ncu capture case: the bench workload cut to --frames frames, no timing output")
     ap.add_argument("--nee", action="store_true", help="with --profile-small: next-event estimation on")
+    ap.add_argument("--frames", type=int, default=2, help="with --profile-small: frames rendered (1..64)")
     ap.add_argument("--profile-unet", action="store_true",
                     help="ncu capture case: one 1080p U-Net inference and one training step")
     ap.add_argument("--profile-scene", action="store_true",

@@ -573,7 +573,6 @@ __global__ void k_collapse_open(BinaryTree t, const uint32_t *jobs, uint32_t num
     const uint32_t b = jobs[j];
     uint32_t k[8];
     int nk = 0;
-    const uint32_t ml = static_cast<uint32_t>(max_leaf);
     if (b >= 2 * t.n - 1) {  // not a node: emit an empty job (the host then reports the item count mismatch)
         for (int q = 0; q < 8; ++q) kids[8ull * j + q] = kNone;
         inner_count[j] = item_count[j] = 0;
@@ -627,7 +626,6 @@ __global__ void k_collapse_emit(BinaryTree t, uint32_t num_jobs, int max_leaf, c
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= num_jobs) return;
     const uint32_t b = jobs[j];
-    const uint32_t ml = static_cast<uint32_t>(max_leaf);
     uint32_t k[8];
     int nk = 0;
     for (int q = 0; q < 8; ++q) {

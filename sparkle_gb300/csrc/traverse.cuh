@@ -57,6 +57,15 @@ enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOve
 #ifndef SPK_PACKET_MIN_BLOCKS
 #define SPK_PACKET_MIN_BLOCKS 8  // resident 128-thread blocks per SM the packet walk is compiled for
 #endif
+#ifndef SPK_FRUSTUM_SPREAD
+#define SPK_FRUSTUM_SPREAD 0.25f  // largest relative spread of a packet's slab reciprocals tested as one
+#endif
+#ifndef SPK_PACKET_FRUSTUM
+#define SPK_PACKET_FRUSTUM 1  // 1: packets of one octant test each node once for all rays (0: every lane its own ray)
+#endif
+#ifndef SPK_PACKET_SIBLINGS
+#define SPK_PACKET_SIBLINGS 4  // sibling nodes a packet tests at once (one per 8-lane group), 1..4
+#endif
 #ifndef SPK_SMEM_STACK
 #define SPK_SMEM_STACK 0  // top entries of each persistent walk's stack kept in shared memory (0: all local)
 #endif
@@ -68,6 +77,9 @@ constexpr int kStackSize = 48;
 constexpr int kWalkThreads = 128;  // threads per block of every persistent walking kernel
 constexpr uint32_t kMaxIterations = 1u << 20;
 constexpr int kPostponeLanes = SPK_POSTPONE_LANES;
+constexpr uint32_t kPacketSiblings = SPK_PACKET_SIBLINGS;
+constexpr uint32_t kPacketStack = 64;  // packet walks push up to 2 * kPacketSiblings - 1 groups per node step
+static_assert(kPacketSiblings >= 1 && kPacketSiblings <= 4, "one to four 8-lane groups");
 
 // Byte `c` of `word` as a float (exact for 0..255).
 __device__ __forceinline__ float byte_to_float(uint32_t word, int c) {
@@ -570,7 +582,13 @@ __device__ __forceinline__ bool make_frustum(const LevelRay &r, uint32_t order, 
     f.omax = mk3(warp_max(r.o.x), warp_max(r.o.y), warp_max(r.o.z));
     f.imin = mk3(warp_min(r.inv.x), warp_min(r.inv.y), warp_min(r.inv.z));
     f.imax = mk3(warp_max(r.inv.x), warp_max(r.inv.y), warp_max(r.inv.z));
-    return true;
+    // The bounds of (p - org) * inv widen with the spread of inv relative to its size: past a few tens of
+    // percent (a component near zero in some lanes) the packet test stops culling and walks far more nodes
+    // than its rays need, so such a packet tests with its own rays instead.
+    const float k = SPK_FRUSTUM_SPREAD;
+    return f.imax.x - f.imin.x <= k * fminf(fabsf(f.imin.x), fabsf(f.imax.x)) &&
+           f.imax.y - f.imin.y <= k * fminf(fabsf(f.imin.y), fabsf(f.imax.y)) &&
+           f.imax.z - f.imin.z <= k * fminf(fabsf(f.imin.z), fabsf(f.imax.z));
 }
 
 // Bounds over the packet of one axis's slab terms: a = s * inv and o = (p - org) * inv, the two values
@@ -586,12 +604,13 @@ __device__ __forceinline__ void axis_bounds(float p, float s, float omin, float 
     ohi = fmaxf(fmaxf(c0, c1), fmaxf(c2, c3));
 }
 
-// visit_node for a whole packet at once: lane k tests child slot k mod 8 against the packet's bounds and the
-// warp ORs the results. fma(q, a, o) grows with a (q >= 0) and with o, so the lower bound of each near-plane
-// t and the upper bound of each far-plane t take the extremes of a and o: a child passes whenever it passes
-// for at least one lane's own ray with that lane's tmax (<= `tmax`), as visit_node computes it, and may pass
-// for none (the packet then visits a node that none of its rays needs, which only costs time). Every lane of
-// the warp must call this; the result is the same in every lane.
+// visit_node for a whole packet at once: each 8-lane group of the warp visits node `idx` (its own: the groups
+// may visit different nodes), lane k testing child slot k mod 8 against the packet's bounds, and the group
+// ORs the results. fma(q, a, o) grows with a (q >= 0) and with o, so the lower bound of each near-plane t and
+// the upper bound of each far-plane t take the extremes of a and o: a child passes whenever it passes for at
+// least one lane's own ray with that lane's tmax (<= `tmax`), as visit_node computes it, and may pass for
+// none (the packet then visits a node that none of its rays needs, which only costs time). Every lane of the
+// warp must call this; the result is the same in every lane of a group.
 __device__ __forceinline__ void visit_node_frustum(const uint4 *__restrict__ nodes, uint32_t idx,
                                                    const PacketFrustum &f, uint32_t order, float tmax,
                                                    uint2 &ngroup, uint2 &tgroup) {
@@ -625,7 +644,9 @@ __device__ __forceinline__ void visit_node_frustum(const uint4 *__restrict__ nod
         if ((m & 0x18u) == 0x18u) bit ^= order;
         bits = ((m >> 5) & 7u) << bit;
     }
-    const uint32_t any = __reduce_or_sync(0xFFFFFFFFu, bits);
+    uint32_t any = bits | __shfl_xor_sync(0xFFFFFFFFu, bits, 1);
+    any |= __shfl_xor_sync(0xFFFFFFFFu, any, 2);
+    any |= __shfl_xor_sync(0xFFFFFFFFu, any, 4);
     ngroup = make_uint2(n1.x, (any & 0xFF000000u) | (n0.w >> 24));
     tgroup = make_uint2(n1.y, any & 0x00FFFFFFu);
 }
@@ -641,15 +662,16 @@ __device__ __forceinline__ void visit_node_frustum(const uint4 *__restrict__ nod
 // over every triangle and sphere its ray hits (exact ties to the smaller (instance, face)), which no visiting
 // order or extra test changes: the results are walk_persistent's. The list must hold one scene: `fetch`
 // returns the same TLAS root for every item. `fetch(i, o, d, tmax)` and `finish(i, result)` as for
-// walk_persistent; every lane of the warp must call this.
+// walk_persistent; every lane of the warp must call this. `counts` (kCount) takes each node and triangle once
+// per packet: one fetch serves the packet's rays.
 template <bool kCount, class Fetch, class Finish>
 __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long long *cursor, unsigned long long n,
                                              uint32_t &err, TraceCounts *counts, Fetch &&fetch, Finish &&finish) {
     constexpr uint32_t kAll = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t budget = S.walk_budget ? S.walk_budget : kMaxIterations;
-    uint2 groups[kStackSize];  // the shared groups (the same in every lane)
-    uint32_t own[kStackSize];  // this lane's hit bits of each
+    uint2 groups[kPacketStack];  // the shared groups (the same in every lane)
+    uint32_t own[kPacketStack];  // this lane's hit bits of each
     for (;;) {
         unsigned long long base = 0;
         if (lane == 0) base = atomicAdd(cursor, 32ull);
@@ -688,7 +710,7 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
         bool in_blas = false;
         uint32_t cur_inst = 0, iter = 0;
         auto push = [&](uint2 g, uint32_t mine) {
-            if (sp < kStackSize) {
+            if (sp < kPacketStack) {
                 groups[sp] = g;
                 own[sp] = mine;
                 ++sp;
@@ -701,7 +723,50 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                 err |= kErrIterationBudget;
                 break;
             }
-            if (ngroup.y > 0x00FFFFFFu) {
+            if (ngroup.y > 0x00FFFFFFu && packed && SPK_PACKET_FRUSTUM) {
+                // The nearest inner children of the group (up to kPacketSiblings, while the stack has room for
+                // their groups), one per 8-lane group, each tested once for the packet against the largest
+                // tmax of the lanes that reached any of them (tmax_box is never negative). A lane takes every
+                // child that passes in the nodes it reached.
+                const uint32_t imask = ngroup.y & 0xFFu, inner = ngroup.y >> 24;
+                const uint32_t room = sp + 2 * kPacketSiblings <= kPacketStack ? kPacketSiblings : 1u;
+                const uint32_t cnt = min(static_cast<uint32_t>(__popc(inner)), room);
+                const uint32_t grp = (threadIdx.x >> 3) & 3u;
+                uint32_t rest = inner, from = inner;
+                for (uint32_t k = 0; k < cnt; ++k) {
+                    if (k == grp) from = rest;
+                    rest &= rest - 1u;
+                }
+                const uint32_t slot = (__ffs(from) - 1) ^ order;  // groups past `cnt` repeat the first child
+                const uint32_t node_idx = ngroup.x + __popc(imask & ((1u << slot) - 1u));
+                const uint32_t taken = inner & ~rest;
+                const uint32_t mine_taken = (nown >> 24) & taken;
+                ngroup.y = (rest << 24) | imask;
+                nown &= ~(taken << 24);
+                if (rest) push(ngroup, nown);
+                if (kCount && lane == 0) counts->nodes += cnt;
+                const float tmax = __uint_as_float(__reduce_max_sync(kAll, mine_taken ? __float_as_uint(tmax_box) : 0u));
+                uint2 ng, tg;
+                visit_node_frustum(S.nodes, node_idx, frustum, order, tmax, ng, tg);
+                // Hand each child's groups out, farthest first onto the stack so the nearest comes back first.
+                uint32_t left = taken;
+                for (int g = static_cast<int>(cnt) - 1; g >= 0; --g) {
+                    const uint32_t b = 31 - __clz(left);
+                    left &= ~(1u << b);
+                    const bool mine = (mine_taken >> b) & 1u;
+                    const uint2 n_g = make_uint2(__shfl_sync(kAll, ng.x, 8 * g), __shfl_sync(kAll, ng.y, 8 * g));
+                    const uint2 t_g = make_uint2(__shfl_sync(kAll, tg.x, 8 * g), __shfl_sync(kAll, tg.y, 8 * g));
+                    if (g == 0) {
+                        ngroup = n_g;
+                        tgroup = t_g;
+                        nown = mine ? (n_g.y & 0xFF000000u) : 0u;
+                        town = mine ? t_g.y : 0u;
+                    } else {
+                        if (n_g.y > 0x00FFFFFFu) push(n_g, mine ? (n_g.y & 0xFF000000u) : 0u);
+                        if (t_g.y != 0u) push(t_g, mine ? t_g.y : 0u);
+                    }
+                }
+            } else if (ngroup.y > 0x00FFFFFFu) {
                 const uint32_t bit = __ffs(ngroup.y >> 24) - 1;
                 const uint32_t keep = ~(1u << (bit + 24));
                 const bool mine = (nown >> (bit + 24)) & 1u;
@@ -710,23 +775,15 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                 const uint32_t slot = bit ^ order;
                 const uint32_t node_idx = ngroup.x + __popc(ngroup.y & 0xFFu & ((1u << slot) - 1u));
                 if (ngroup.y > 0x00FFFFFFu) push(ngroup, nown);
-                if (kCount && mine) ++counts->nodes;
-                if (packed) {
-                    // One test for the packet against the largest tmax of the lanes that reached the node
-                    // (tmax_box is never negative); those lanes take every child it passes.
-                    const float tmax = __uint_as_float(__reduce_max_sync(kAll, mine ? __float_as_uint(tmax_box) : 0u));
-                    visit_node_frustum(S.nodes, node_idx, frustum, order, tmax, ngroup, tgroup);
-                    nown = mine ? (ngroup.y & 0xFF000000u) : 0u;
-                    town = mine ? tgroup.y : 0u;
-                } else {
-                    // A lane that did not reach this node tests its boxes against t <= -1: no hits.
-                    visit_node(S.nodes, node_idx, ray, order, mine ? tmax_box : -1.f, ngroup, tgroup);
-                    nown = ngroup.y & 0xFF000000u;
-                    town = tgroup.y;
-                    const uint32_t any = __reduce_or_sync(kAll, nown | town);
-                    ngroup.y = (any & 0xFF000000u) | (ngroup.y & 0xFFu);
-                    tgroup.y = any & 0x00FFFFFFu;
-                }
+                if (kCount && lane == 0) ++counts->nodes;
+                // Rays of several octants: every lane tests the node with its own ray; a lane that did not
+                // reach it tests against t <= -1 (no hits).
+                visit_node(S.nodes, node_idx, ray, order, mine ? tmax_box : -1.f, ngroup, tgroup);
+                nown = ngroup.y & 0xFF000000u;
+                town = tgroup.y;
+                const uint32_t any = __reduce_or_sync(kAll, nown | town);
+                ngroup.y = (any & 0xFF000000u) | (ngroup.y & 0xFFu);
+                tgroup.y = any & 0x00FFFFFFu;
             } else {
                 tgroup = ngroup;
                 town = nown;
@@ -739,8 +796,8 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                 const bool mine = (town >> k) & 1u;
                 const uint32_t idx = tgroup.x + k;
                 if (in_blas) {
+                    if (kCount && lane == 0) ++counts->tris;
                     if (!mine) continue;
-                    if (kCount) ++counts->tris;
                     float t, u, v;
                     uint32_t face;
                     if (!triangle_hit(S.tris, idx, ray, t, u, v, face)) continue;
