@@ -660,10 +660,10 @@ __device__ __forceinline__ void visit_node_frustum(const uint4 *__restrict__ nod
 // takes only the children it hit itself. Either way a lane tests every box and triangle its own walk would
 // reach, and prunes only beyond its own best t; it may test more. Its result is still the smallest world t
 // over every triangle and sphere its ray hits (exact ties to the smaller (instance, face)), which no visiting
-// order or extra test changes: the results are walk_persistent's. The list must hold one scene: `fetch`
-// returns the same TLAS root for every item. `fetch(i, o, d, tmax)` and `finish(i, result)` as for
-// walk_persistent; every lane of the warp must call this. `counts` (kCount) takes each node and triangle once
-// per packet: one fetch serves the packet's rays.
+// order or extra test changes: the results are walk_persistent's. `fetch(i, o, d, tmax)` and
+// `finish(i, result)` as for
+// walk_persistent (`fetch` may be called more than once for an item); every lane of the warp must call this.
+// `counts` (kCount) takes each node and triangle once per packet: one fetch serves the packet's rays.
 template <bool kCount, class Fetch, class Finish>
 __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long long *cursor, unsigned long long n,
                                              uint32_t &err, TraceCounts *counts, Fetch &&fetch, Finish &&finish) {
@@ -672,25 +672,37 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
     const uint32_t budget = S.walk_budget ? S.walk_budget : kMaxIterations;
     uint2 groups[kPacketStack];  // the shared groups (the same in every lane)
     uint32_t own[kPacketStack];  // this lane's hit bits of each
+    unsigned long long item = 0;
+    bool todo = false;  // this lane holds an item not walked yet
     for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(cursor, 32ull);
-        base = __shfl_sync(kAll, base, 0);
-        if (base >= n) break;
-        const unsigned long long item = base + lane;
-        const bool valid = item < n;
+        if (!__any_sync(kAll, todo)) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(cursor, 32ull);
+            base = __shfl_sync(kAll, base, 0);
+            if (base >= n) break;
+            item = base + lane;
+            todo = item < n;  // lane 0 always holds an item
+        }
+        // One packet per TLAS root among the lanes' items (a batch of requests holds several scenes; almost
+        // every warp has one). The packet is the lanes with the first pending lane's root; the others, and
+        // lanes past the end of the list, walk a copy of its leader's ray and drop their results, which keeps
+        // the packet's bounds and octant those of its real rays.
+        const int leader = __ffs(__ballot_sync(kAll, todo)) - 1;
         f3 wo = mk3(0.f, 0.f, 0.f), wd = mk3(1.f, 1.f, 1.f);
         uint32_t root = kInvalid;
-        if (valid) {
+        if (todo) {
             float tm = kFltMax;
             root = fetch(item, wo, wd, tm);
         }
-        // Lane 0 always holds an item; lanes past the end of the list walk a copy of its ray (their results
-        // are dropped), which keeps the packet's bounds and octant those of its real rays.
-        root = __shfl_sync(kAll, root, 0);
+        const uint32_t lroot = __shfl_sync(kAll, root, leader);
+        const bool valid = todo && root == lroot;
+        todo = todo && !valid;
+        root = lroot;
         {
-            const f3 o0 = mk3(__shfl_sync(kAll, wo.x, 0), __shfl_sync(kAll, wo.y, 0), __shfl_sync(kAll, wo.z, 0));
-            const f3 d0 = mk3(__shfl_sync(kAll, wd.x, 0), __shfl_sync(kAll, wd.y, 0), __shfl_sync(kAll, wd.z, 0));
+            const f3 o0 = mk3(__shfl_sync(kAll, wo.x, leader), __shfl_sync(kAll, wo.y, leader),
+                              __shfl_sync(kAll, wo.z, leader));
+            const f3 d0 = mk3(__shfl_sync(kAll, wd.x, leader), __shfl_sync(kAll, wd.y, leader),
+                              __shfl_sync(kAll, wd.z, leader));
             if (!valid) {
                 wo = o0;
                 wd = d0;
@@ -698,7 +710,7 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
         }
         LevelRay ray;
         setup_level(ray, wo, wd);
-        const uint32_t top_order = __shfl_sync(kAll, ray.oct, 0);
+        const uint32_t top_order = __shfl_sync(kAll, ray.oct, leader);
         uint32_t order = top_order;
         PacketFrustum frustum;
         bool packed = make_frustum(ray, order, frustum);  // the level's nodes are tested once for the packet

@@ -19,10 +19,13 @@ namespace {
 // queue_counters slots
 constexpr int kLen0 = 0;          // length of queue 0 (queue 1's length is slot 1)
 constexpr int kCursor = 2;        // pop cursor of the running persistent stage
+constexpr int kPacketCursor = 3;  // pop cursor of the packet walk (reset with kCursor)
 constexpr int kShadowLen = 4;     // occlusion rays queued by the iteration's shade stage
 constexpr int kNeeLen = 5;        // light-sampling vertices of the iteration's shade stage
 constexpr int kShadowCursor = 6;  // pop cursor of the shadow stage
-constexpr int kPacketQueue = 7;   // nonzero: the extend queue is in item order (primary rays), walk it in packets
+constexpr int kPacketQueue = 7;   // leading extend-queue entries walked in packets (primary rays queued in
+                                  // sample-item order, >= kPacketMinSamples of a pixel in a row); 0 after shade
+constexpr int kNextItem = 8;      // next (frame, pixel) sample item to hand out
 
 template <int kKind>
 __device__ __forceinline__ void load_rng(const uint4 *rng, uint32_t pid, Rng &r) {
@@ -199,7 +202,7 @@ __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontSta
 // ------------------------------------------------------------------------------------------------
 template <int kKind>
 __global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers fb, RenderParams p, WavefrontState s,
-                                                     uint32_t packets, Counters *counters) {
+                                                     Counters *counters) {
     const uint32_t i = blockIdx.x * 16u + (threadIdx.x & 15u);
     const uint32_t j = blockIdx.y * 8u + (threadIdx.x >> 4);
     if (i >= fb.width || j >= fb.height) return;
@@ -209,25 +212,27 @@ __global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers
     s.queue[0][pid] = pid;
     if (pid == 0) {
         counters->queue_counters[kLen0] = static_cast<unsigned long long>(fb.width) * fb.height;
-        counters->queue_counters[kPacketQueue] = packets;
+        counters->queue_counters[kPacketQueue] = 0u;  // one sample per pixel: no packets
     }
 }
 
 // Extend: persistent warps pull paths from the queue, refilling lanes whose walk has finished. With
-// kBatch each path traces in its own scene (the TLAS root its slot recorded at start). kPackets walks a
-// queue still in item order (the primary rays a generate kernel just queued, flagged in kPacketQueue) in
-// packets of 32 consecutive paths instead: the samples of one pixel, or neighbouring pixels, take the same
-// nodes. Both forms are launched for a single-scene queue and the one the flag does not name returns at
-// once, so the choice needs no host round trip (and stays inside a replayed graph).
+// kBatch each path traces in its own scene (the TLAS root its slot recorded at start). The first
+// kPacketQueue entries of a queue (primary rays a generate kernel queued in sample-item order: 32
+// consecutive paths are a pixel's samples, or a few neighbouring pixels') are walked by the kPackets form in
+// packets of 32 instead, the rest by the persistent form. Both forms are launched every stage and return at
+// once when they have nothing to walk, so the split needs no host round trip (and stays inside a replayed
+// graph).
 template <bool kCount, bool kBatch = false, bool kPackets = false>
 __global__ void __launch_bounds__(128, kPackets ? SPK_PACKET_MIN_BLOCKS : SPK_WALK_MIN_BLOCKS)
     k_wf_extend(DevScene S, WavefrontState s, int in_queue, Counters *counters) {
-    static_assert(!(kBatch && kPackets), "packets hold one scene");
-    if (!kBatch && (counters->queue_counters[kPacketQueue] != 0u) != kPackets) return;
+    const unsigned long long len = counters->queue_counters[in_queue];
+    const unsigned long long split = min(counters->queue_counters[kPacketQueue], len);
+    const unsigned long long first = kPackets ? 0ull : split, n = kPackets ? split : len - split;
+    if (n == 0) return;
     uint32_t err = 0, done = 0;
     TraceCounts tc;
-    const unsigned long long n = counters->queue_counters[in_queue];
-    const uint32_t *queue = s.queue[in_queue];
+    const uint32_t *queue = s.queue[in_queue] + first;
     uint32_t pid = 0;
     auto fetch = [&](unsigned long long q, f3 &o, f3 &d, float &) {
         pid = queue[q];
@@ -242,7 +247,7 @@ __global__ void __launch_bounds__(128, kPackets ? SPK_PACKET_MIN_BLOCKS : SPK_WA
         ++done;
     };
     if constexpr (kPackets)
-        walk_packets<kCount>(S, &counters->queue_counters[kCursor], n, err, &tc, fetch, finish);
+        walk_packets<kCount>(S, &counters->queue_counters[kPacketCursor], n, err, &tc, fetch, finish);
     else
         walk_persistent<kTraceClosest, kCount>(S, &counters->queue_counters[kCursor], n, kFltMax, err, &tc, fetch,
                                                finish);
@@ -289,7 +294,6 @@ __global__ void __launch_bounds__(256) k_wf_finish(FrameBuffers fb, WavefrontSta
 // ------------------------------------------------------------------------------------------------
 // Multi-frame schedule with path regeneration
 // ------------------------------------------------------------------------------------------------
-constexpr int kNextItem = 3;  // queue_counters slot: next (frame, pixel) sample item to hand out
 
 #ifndef SPK_ITEM_TILES
 #define SPK_ITEM_TILES 1  // 1: a frame's items walk the image in 32-pixel tiles (0: row by row)
@@ -350,7 +354,8 @@ __global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers
     if (slot == 0) {
         counters->queue_counters[kLen0] = initial;
         counters->queue_counters[kNextItem] = initial;
-        counters->queue_counters[kPacketQueue] = packets;
+        counters->queue_counters[kPacketQueue] =
+            SPK_ITEM_ORDER == 1 && packets && total_items / (fb.width * fb.height) >= kPacketMinSamples ? initial : 0u;
     }
 }
 
@@ -614,8 +619,9 @@ __device__ __forceinline__ uint32_t find_request(const BatchParams &b, unsigned 
 // Slot `slot` starts global item `item`: request r, frame k, pixel; the same seed, jitter and camera ray
 // as frame k of spk_render on that request alone (frame seed base k: one sample per frame).
 template <int kKind>
-__device__ __forceinline__ void start_item_batch(const DevScene &S, const BatchParams &b, const WavefrontState &s,
-                                                 uint32_t slot, unsigned long long item) {
+// Returns the item's request.
+__device__ __forceinline__ uint32_t start_item_batch(const DevScene &S, const BatchParams &b, const WavefrontState &s,
+                                                     uint32_t slot, unsigned long long item) {
     const uint32_t r = find_request(b, item);
     const DevRequest &R = b.reqs[r];
     const unsigned long long local = item - R.item_base;
@@ -635,18 +641,21 @@ __device__ __forceinline__ void start_item_batch(const DevScene &S, const BatchP
     s.slot_state[slot] = 0u;
     s.slot_req[slot] = r;
     s.slot_root[slot] = S.descs[R.scene].tlas_root;
+    return r;
 }
 
+// Starts the first `first` sample items, item i in slot i, queued at the position BatchParams lays out.
 template <int kKind>
 __global__ void __launch_bounds__(128) k_b_generate(DevScene S, BatchParams b, WavefrontState s, uint32_t first,
                                                     Counters *counters) {
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= first) return;
-    start_item_batch<kKind>(S, b, s, slot, slot);
-    s.queue[0][slot] = slot;
+    const DevRequest &R = b.reqs[start_item_batch<kKind>(S, b, s, slot, slot)];
+    s.queue[0][R.queue_base + static_cast<uint32_t>(slot - R.item_base)] = slot;
     if (slot == 0) {
         counters->queue_counters[kLen0] = first;
         counters->queue_counters[kNextItem] = first;
+        counters->queue_counters[kPacketQueue] = SPK_ITEM_ORDER == 1 ? min(b.packet_items, 1ull * first) : 0ull;
     }
 }
 
@@ -835,16 +844,19 @@ unsigned extend_blocks(int num_sms, uint32_t per_sm_override) {
     return static_cast<unsigned>(num_sms) * n;
 }
 
-// Kernel launches of one extend stage: a single-scene queue gets the packet and the persistent form.
-constexpr uint32_t extend_launches(bool batch) { return batch ? 1u : 2u; }
+// Kernel launches of one extend stage: the packet and the persistent form.
+constexpr uint32_t kExtendLaunches = 2u;
 
 cudaError_t launch_extend(const DevScene &scene, const WavefrontState &s, int in, bool count, Counters *counters,
                           unsigned grid, cudaStream_t stream, LaunchEvents *ev, bool batch = false) {
     unsigned long long *qc = counters->queue_counters;
-    cudaError_t e = cudaMemsetAsync(qc + kCursor, 0, sizeof(unsigned long long), stream);
+    static_assert(kPacketCursor == kCursor + 1, "one reset for both cursors");
+    cudaError_t e = cudaMemsetAsync(qc + kCursor, 0, 2 * sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     if (ev) ev->before(stream);
     if (batch) {
+        (count ? k_wf_extend<true, true, true> : k_wf_extend<false, true, true>)<<<grid, 128, 0, stream>>>(
+            scene, s, in, counters);
         (count ? k_wf_extend<true, true> : k_wf_extend<false, true>)<<<grid, 128, 0, stream>>>(scene, s, in, counters);
     } else {
         (count ? k_wf_extend<true, false, true> : k_wf_extend<false, false, true>)<<<grid, 128, 0, stream>>>(
@@ -981,9 +993,9 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
     if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
     const dim3 ggrid((fbuf.width + 15) / 16, (fbuf.height + 7) / 8);
     if (p.rng == 0) {
-        k_wf_generate<0><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, tuning.packets, counters);
+        k_wf_generate<0><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, counters);
     } else {
-        k_wf_generate<1><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, tuning.packets, counters);
+        k_wf_generate<1><<<ggrid, 128, 0, stream>>>(cam, fbuf, p, s, counters);
     }
     ++nl;
     const unsigned shade_blocks = static_cast<unsigned>(num_sms) * tuning.shade_blocks_per_sm;
@@ -997,7 +1009,7 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
             nl += 3;
         }
         if ((e = launch_extend(scene, se, in, count, counters, extend_grid, stream, ev)) != cudaSuccess) return e;
-        nl += extend_launches(false);
+        nl += kExtendLaunches;
         WavefrontState ss = se;
         if (tuning.material_sort) {
             ss = enqueue_material_sort(scene, se, in, counters, num_sms, stream);
@@ -1201,7 +1213,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 return e;
             }
             iter += kChunk;
-            nl += (1u + extend_launches(false) + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
+            nl += (1u + kExtendLaunches + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
                    (nee == kNeeDeferred ? 2u : 0u)) * kChunk;
             if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
                 cudaSuccess)
@@ -1273,7 +1285,7 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         iter += kChunk;
-        nl += (1u + extend_launches(true) + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
+        nl += (1u + kExtendLaunches + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
                (nee == kNeeDeferred ? 2u : 0u)) * kChunk;
         if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
             cudaSuccess)

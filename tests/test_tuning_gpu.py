@@ -134,3 +134,35 @@ def test_trace_hits_independent_of_bvh_shape(ctx, small_terrain, width, leaf, co
     for f in ("t", "u", "v", "prim", "face"):
         assert np.array_equal(got[f].view(np.uint32), ref[f].view(np.uint32)), f
     ctx.set_tuning(**DEFAULTS)
+
+
+@pytest.mark.parametrize("frames", [1, 4, 8, 64])
+def test_primary_packets_run_where_they_pay(ctx, small_terrain, frames):
+    """The packet walk takes the primary rays of a pass whose pixels give it >= 8 samples in a row (the
+    instrumented walk then counts each node once per packet, far fewer visits) and renders the same bits;
+    with fewer samples per pixel per pass the persistent walk keeps them (the same count)."""
+    scene, cam_args = small_terrain
+    W, H = 128, 96
+    camera = scenes.make_camera(cam_args, W, H)
+    cfg = abi.make_config(W, H, spp=1, bounce=1, seed=3)  # one segment per path: the primary rays alone
+    ctx.set_scene(scene)
+    visits = {}
+    for packets in (0, 1):
+        ctx.set_tuning(**{**DEFAULTS, "primary_packets": packets})
+        ctx.set_config(cfg)
+        ctx.set_camera(camera)
+        ctx.set_instrumentation(True)
+        ctx.render(frames)
+        ctx.set_instrumentation(False)
+        st = ctx.stats()
+        assert st["error_flags"] == 0 and st["extension_rays"] == W * H * frames
+        visits[packets] = st["node_visits"]
+        hdr, out = ctx.framebuffer()
+        if packets == 0:
+            base = (hdr, out)
+    assert np.array_equal(hdr.view(np.uint32), base[0].view(np.uint32)) and np.array_equal(out, base[1])
+    if frames >= 8:
+        assert visits[1] * 4 < visits[0], visits
+    else:
+        assert visits[1] == visits[0], visits
+    ctx.set_tuning(**DEFAULTS)
