@@ -51,11 +51,17 @@ enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOve
 #ifndef SPK_MT_RCP
 #define SPK_MT_RCP 1  // 1: Moller-Trumbore's 1/det as a correctly rounded reciprocal (same bits as 1.f/det)
 #endif
+#ifndef SPK_SLAB_RCP
+#define SPK_SLAB_RCP 0  // 1: the slab reciprocals as correctly rounded reciprocals (same bits as 1.f/x)
+#endif
 #ifndef SPK_WALK_MIN_BLOCKS
 #define SPK_WALK_MIN_BLOCKS 8  // resident 128-thread blocks per SM the walking kernels are compiled for
 #endif
 #ifndef SPK_PACKET_MIN_BLOCKS
 #define SPK_PACKET_MIN_BLOCKS 8  // resident 128-thread blocks per SM the packet walk is compiled for
+#endif
+#ifndef SPK_PACKET2_MIN_BLOCKS
+#define SPK_PACKET2_MIN_BLOCKS 6  // resident 128-thread blocks per SM the two-rays-per-lane packet walk is compiled for
 #endif
 #ifndef SPK_FRUSTUM_SPREAD
 #define SPK_FRUSTUM_SPREAD 0.25f  // largest relative spread of a packet's slab reciprocals tested as one
@@ -110,7 +116,11 @@ struct LevelRay {
 // Reciprocal for the slab test; a component with |d| <= FLT_EPSILON gets +-2^100 so that
 // (bound - o) * inv keeps its exact sign without overflowing (an exact containment test on that axis).
 __device__ __forceinline__ float slab_inverse(float x) {
+#if SPK_SLAB_RCP
+    return fabsf(x) <= 1.1920928955078125e-07f ? copysignf(0x1p100f, x) : __frcp_rn(x);  // the bits of 1.f / x
+#else
     return fabsf(x) <= 1.1920928955078125e-07f ? copysignf(0x1p100f, x) : 1.f / x;
+#endif
 }
 
 __device__ __forceinline__ void setup_level(LevelRay &r, f3 o, f3 d) {
@@ -572,18 +582,31 @@ struct PacketFrustum {
     f3 omin, omax, imin, imax;
 };
 
-// Fills `f` from every lane's level ray and returns true when the packet can be tested as one: every lane's
-// direction lies in octant `order` and no component is small enough for slab_inverse's 2^100 stand-in
-// (so every bound below stays finite). Every lane of the warp must call this.
-__device__ __forceinline__ bool make_frustum(const LevelRay &r, uint32_t order, PacketFrustum &f) {
-    const bool regular = fabsf(r.inv.x) < 0x1p24f && fabsf(r.inv.y) < 0x1p24f && fabsf(r.inv.z) < 0x1p24f;
-    if (!__all_sync(0xFFFFFFFFu, r.oct == order && regular)) return false;
-    f.omin = mk3(warp_min(r.o.x), warp_min(r.o.y), warp_min(r.o.z));
-    f.omax = mk3(warp_max(r.o.x), warp_max(r.o.y), warp_max(r.o.z));
-    f.imin = mk3(warp_min(r.inv.x), warp_min(r.inv.y), warp_min(r.inv.z));
-    f.imax = mk3(warp_max(r.inv.x), warp_max(r.inv.y), warp_max(r.inv.z));
+// Fills `f` from the level rays of every lane (kRays per lane) and returns true when the packet can be tested
+// as one: every ray's direction lies in octant `order` and no component is small enough for slab_inverse's
+// 2^100 stand-in (so every bound below stays finite). Every lane of the warp must call this.
+template <int kRays>
+__device__ __forceinline__ bool make_frustum(const LevelRay (&r)[kRays], uint32_t order, PacketFrustum &f) {
+    bool ok = true;
+    f3 omin = r[0].o, omax = r[0].o, imin = r[0].inv, imax = r[0].inv;
+#pragma unroll
+    for (int k = 0; k < kRays; ++k) {
+        ok = ok && r[k].oct == order && fabsf(r[k].inv.x) < 0x1p24f && fabsf(r[k].inv.y) < 0x1p24f &&
+             fabsf(r[k].inv.z) < 0x1p24f;
+        if (k > 0) {
+            omin = mk3(fminf(omin.x, r[k].o.x), fminf(omin.y, r[k].o.y), fminf(omin.z, r[k].o.z));
+            omax = mk3(fmaxf(omax.x, r[k].o.x), fmaxf(omax.y, r[k].o.y), fmaxf(omax.z, r[k].o.z));
+            imin = mk3(fminf(imin.x, r[k].inv.x), fminf(imin.y, r[k].inv.y), fminf(imin.z, r[k].inv.z));
+            imax = mk3(fmaxf(imax.x, r[k].inv.x), fmaxf(imax.y, r[k].inv.y), fmaxf(imax.z, r[k].inv.z));
+        }
+    }
+    if (!__all_sync(0xFFFFFFFFu, ok)) return false;
+    f.omin = mk3(warp_min(omin.x), warp_min(omin.y), warp_min(omin.z));
+    f.omax = mk3(warp_max(omax.x), warp_max(omax.y), warp_max(omax.z));
+    f.imin = mk3(warp_min(imin.x), warp_min(imin.y), warp_min(imin.z));
+    f.imax = mk3(warp_max(imax.x), warp_max(imax.y), warp_max(imax.z));
     // The bounds of (p - org) * inv widen with the spread of inv relative to its size: past a few tens of
-    // percent (a component near zero in some lanes) the packet test stops culling and walks far more nodes
+    // percent (a component near zero in some rays) the packet test stops culling and walks far more nodes
     // than its rays need, so such a packet tests with its own rays instead.
     const float k = SPK_FRUSTUM_SPREAD;
     return f.imax.x - f.imin.x <= k * fminf(fabsf(f.imin.x), fabsf(f.imax.x)) &&
@@ -652,71 +675,94 @@ __device__ __forceinline__ void visit_node_frustum(const uint4 *__restrict__ nod
 }
 
 // Closest-hit walk of coherent rays in packets (primary rays: the samples of one pixel, or neighbouring
-// pixels). Each warp takes 32 consecutive items of the work list and walks them together: one node or
-// triangle group at a time for the whole warp, in the order of lane 0's octant, every lane testing its own
-// ray against each triangle. When all the packet's rays share that octant (checked per level, TLAS and each
-// BLAS), a node's 8 children are tested once for the whole packet (visit_node_frustum: one child per lane
-// against the bounds of the lanes' rays); otherwise every lane tests them with its own ray (visit_node) and
-// takes only the children it hit itself. Either way a lane tests every box and triangle its own walk would
-// reach, and prunes only beyond its own best t; it may test more. Its result is still the smallest world t
-// over every triangle and sphere its ray hits (exact ties to the smaller (instance, face)), which no visiting
-// order or extra test changes: the results are walk_persistent's. `fetch(i, o, d, tmax)` and
-// `finish(i, result)` as for
-// walk_persistent (`fetch` may be called more than once for an item); every lane of the warp must call this.
-// `counts` (kCount) takes each node and triangle once per packet: one fetch serves the packet's rays.
-template <bool kCount, class Fetch, class Finish>
+// pixels). Each warp takes 32 * kRays consecutive items of the work list (lane l the items l, l + 32, ...)
+// and walks them together: one node or triangle group at a time for the whole warp, in the order of the
+// leader's octant, every lane testing its own rays against each triangle. When all the packet's rays share
+// that octant (checked per level, TLAS and each BLAS), a node's 8 children are tested once for the whole
+// packet (visit_node_frustum: one child per lane against the bounds of all its rays); otherwise every lane
+// tests them with its own rays (visit_node) and takes only the children they hit. Either way a ray is tested
+// against every box and triangle its own walk would reach, and pruned only beyond its own best t; it may be
+// tested against more. Its result is still the smallest world t over every triangle and sphere it hits
+// (exact ties to the smaller (instance, face)), which no visiting order or extra test changes: the results
+// are walk_persistent's. `fetch(i, o, d, tmax)` and `finish(i, result)` as for walk_persistent (`fetch` may
+// be called more than once for an item, `finish` must find the item from i alone); every lane of the warp
+// must call this. `counts` (kCount) takes each node and triangle once per packet: one fetch serves its rays.
+template <bool kCount, int kRays, class Fetch, class Finish>
 __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long long *cursor, unsigned long long n,
                                              uint32_t &err, TraceCounts *counts, Fetch &&fetch, Finish &&finish) {
+    static_assert(kRays == 1 || kRays == 2, "one or two rays per lane");
     constexpr uint32_t kAll = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t budget = S.walk_budget ? S.walk_budget : kMaxIterations;
     uint2 groups[kPacketStack];  // the shared groups (the same in every lane)
     uint32_t own[kPacketStack];  // this lane's hit bits of each
-    unsigned long long item = 0;
-    bool todo = false;  // this lane holds an item not walked yet
+    unsigned long long base = 0;
+    bool todo[kRays];  // this lane's items not walked yet
+#pragma unroll
+    for (int r = 0; r < kRays; ++r) todo[r] = false;
     for (;;) {
-        if (!__any_sync(kAll, todo)) {
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(cursor, 32ull);
-            base = __shfl_sync(kAll, base, 0);
+        bool any_todo = false;
+#pragma unroll
+        for (int r = 0; r < kRays; ++r) any_todo = any_todo || todo[r];
+        if (!__any_sync(kAll, any_todo)) {
+            unsigned long long b = 0;
+            if (lane == 0) b = atomicAdd(cursor, 32ull * kRays);
+            base = __shfl_sync(kAll, b, 0);
             if (base >= n) break;
-            item = base + lane;
-            todo = item < n;  // lane 0 always holds an item
+#pragma unroll
+            for (int r = 0; r < kRays; ++r) todo[r] = base + lane + 32u * r < n;  // lane 0's first always
+            any_todo = todo[0];
         }
-        // One packet per TLAS root among the lanes' items (a batch of requests holds several scenes; almost
-        // every warp has one). The packet is the lanes with the first pending lane's root; the others, and
-        // lanes past the end of the list, walk a copy of its leader's ray and drop their results, which keeps
-        // the packet's bounds and octant those of its real rays.
-        const int leader = __ffs(__ballot_sync(kAll, todo)) - 1;
-        f3 wo = mk3(0.f, 0.f, 0.f), wd = mk3(1.f, 1.f, 1.f);
-        uint32_t root = kInvalid;
-        if (todo) {
-            float tm = kFltMax;
-            root = fetch(item, wo, wd, tm);
-        }
-        const uint32_t lroot = __shfl_sync(kAll, root, leader);
-        const bool valid = todo && root == lroot;
-        todo = todo && !valid;
-        root = lroot;
-        {
-            const f3 o0 = mk3(__shfl_sync(kAll, wo.x, leader), __shfl_sync(kAll, wo.y, leader),
-                              __shfl_sync(kAll, wo.z, leader));
-            const f3 d0 = mk3(__shfl_sync(kAll, wd.x, leader), __shfl_sync(kAll, wd.y, leader),
-                              __shfl_sync(kAll, wd.z, leader));
-            if (!valid) {
-                wo = o0;
-                wd = d0;
+        // One packet per TLAS root among the items (a batch of requests holds several scenes; almost every
+        // warp has one). The packet is the rays with the leader's root (its lowest pending item's); the
+        // others, and items past the end of the list, walk a copy of that ray and drop their results, which
+        // keeps the packet's bounds and octant those of its real rays.
+        const int leader = __ffs(__ballot_sync(kAll, any_todo)) - 1;
+        f3 wo[kRays], wd[kRays];
+        uint32_t root[kRays];
+        bool valid[kRays];
+#pragma unroll
+        for (int r = 0; r < kRays; ++r) {
+            wo[r] = mk3(0.f, 0.f, 0.f);
+            wd[r] = mk3(1.f, 1.f, 1.f);
+            root[r] = kInvalid;
+            if (todo[r]) {
+                float tm = kFltMax;
+                root[r] = fetch(base + lane + 32u * r, wo[r], wd[r], tm);
             }
         }
-        LevelRay ray;
-        setup_level(ray, wo, wd);
-        const uint32_t top_order = __shfl_sync(kAll, ray.oct, leader);
+        uint32_t first_root = root[0];
+        f3 first_o = wo[0], first_d = wd[0];
+        if (kRays > 1 && !todo[0]) {
+            first_root = root[kRays - 1];
+            first_o = wo[kRays - 1];
+            first_d = wd[kRays - 1];
+        }
+        const uint32_t lroot = __shfl_sync(kAll, first_root, leader);
+        const f3 o0 = mk3(__shfl_sync(kAll, first_o.x, leader), __shfl_sync(kAll, first_o.y, leader),
+                          __shfl_sync(kAll, first_o.z, leader));
+        const f3 d0 = mk3(__shfl_sync(kAll, first_d.x, leader), __shfl_sync(kAll, first_d.y, leader),
+                          __shfl_sync(kAll, first_d.z, leader));
+        LevelRay ray[kRays];
+        TraceResult best[kRays];
+        float tmax_box[kRays];
+#pragma unroll
+        for (int r = 0; r < kRays; ++r) {
+            valid[r] = todo[r] && root[r] == lroot;
+            todo[r] = todo[r] && !valid[r];
+            if (!valid[r]) {
+                wo[r] = o0;
+                wd[r] = d0;
+            }
+            setup_level(ray[r], wo[r], wd[r]);
+            best[r] = TraceResult{kFltMax, 0.f, 0.f, kInvalid, kInvalid};
+            tmax_box[r] = kFltMax;
+        }
+        const uint32_t top_order = __shfl_sync(kAll, ray[0].oct, leader);  // the leader's ray: o0, d0
         uint32_t order = top_order;
         PacketFrustum frustum;
         bool packed = make_frustum(ray, order, frustum);  // the level's nodes are tested once for the packet
-        TraceResult best{kFltMax, 0.f, 0.f, kInvalid, kInvalid};
-        float tmax_box = kFltMax;
-        uint2 ngroup = make_uint2(root, root == kInvalid ? 0u : (1u << 24)), tgroup = make_uint2(0u, 0u);
+        uint2 ngroup = make_uint2(lroot, lroot == kInvalid ? 0u : (1u << 24)), tgroup = make_uint2(0u, 0u);
         uint32_t nown = 1u << 24, town = 0u;
         int sp = 0, blas_sp = 0;
         bool in_blas = false;
@@ -730,6 +776,12 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                 err |= kErrStackOverflow;
             }
         };
+        auto lane_tmax = [&]() {
+            float t = tmax_box[0];
+#pragma unroll
+            for (int r = 1; r < kRays; ++r) t = fmaxf(t, tmax_box[r]);
+            return t;
+        };
         for (;;) {
             if (++iter > budget) {
                 err |= kErrIterationBudget;
@@ -738,8 +790,8 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
             if (ngroup.y > 0x00FFFFFFu && packed && SPK_PACKET_FRUSTUM) {
                 // The nearest inner children of the group (up to kPacketSiblings, while the stack has room for
                 // their groups), one per 8-lane group, each tested once for the packet against the largest
-                // tmax of the lanes that reached any of them (tmax_box is never negative). A lane takes every
-                // child that passes in the nodes it reached.
+                // tmax of the rays of the lanes that reached any of them (tmax_box is never negative). A lane
+                // takes every child that passes in the nodes it reached.
                 const uint32_t imask = ngroup.y & 0xFFu, inner = ngroup.y >> 24;
                 const uint32_t room = sp + 2 * kPacketSiblings <= kPacketStack ? kPacketSiblings : 1u;
                 const uint32_t cnt = min(static_cast<uint32_t>(__popc(inner)), room);
@@ -757,7 +809,7 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                 nown &= ~(taken << 24);
                 if (rest) push(ngroup, nown);
                 if (kCount && lane == 0) counts->nodes += cnt;
-                const float tmax = __uint_as_float(__reduce_max_sync(kAll, mine_taken ? __float_as_uint(tmax_box) : 0u));
+                const float tmax = __uint_as_float(__reduce_max_sync(kAll, mine_taken ? __float_as_uint(lane_tmax()) : 0u));
                 uint2 ng, tg;
                 visit_node_frustum(S.nodes, node_idx, frustum, order, tmax, ng, tg);
                 // Hand each child's groups out, farthest first onto the stack so the nearest comes back first.
@@ -788,12 +840,21 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                 const uint32_t node_idx = ngroup.x + __popc(ngroup.y & 0xFFu & ((1u << slot) - 1u));
                 if (ngroup.y > 0x00FFFFFFu) push(ngroup, nown);
                 if (kCount && lane == 0) ++counts->nodes;
-                // Rays of several octants: every lane tests the node with its own ray; a lane that did not
+                // Rays of several octants: every lane tests the node with its own rays; a lane that did not
                 // reach it tests against t <= -1 (no hits).
-                visit_node(S.nodes, node_idx, ray, order, mine ? tmax_box : -1.f, ngroup, tgroup);
-                nown = ngroup.y & 0xFF000000u;
-                town = tgroup.y;
-                const uint32_t any = __reduce_or_sync(kAll, nown | town);
+                uint32_t hits = 0u;
+#pragma unroll
+                for (int r = 0; r < kRays; ++r) {
+                    uint2 ng, tg;
+                    visit_node(S.nodes, node_idx, ray[r], order, mine ? tmax_box[r] : -1.f, ng, tg);
+                    hits |= (ng.y & 0xFF000000u) | tg.y;
+                    ngroup.x = ng.x;
+                    tgroup.x = tg.x;
+                    ngroup.y = (ngroup.y & ~0xFFu) | (ng.y & 0xFFu);  // the child's imask
+                }
+                nown = hits & 0xFF000000u;
+                town = hits & 0x00FFFFFFu;
+                const uint32_t any = __reduce_or_sync(kAll, hits);
                 ngroup.y = (any & 0xFF000000u) | (ngroup.y & 0xFFu);
                 tgroup.y = any & 0x00FFFFFFu;
             } else {
@@ -810,22 +871,29 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                 if (in_blas) {
                     if (kCount && lane == 0) ++counts->tris;
                     if (!mine) continue;
-                    float t, u, v;
-                    uint32_t face;
-                    if (!triangle_hit(S.tris, idx, ray, t, u, v, face)) continue;
-                    const float wt = world_t(S.instances[cur_inst], ray, t, wo, wd);
-                    if (wt > 0.f && closer_hit(best, wt, cur_inst, face)) {
-                        best = TraceResult{wt, u, v, cur_inst, face};
-                        tmax_box = prune_limit(best.t, wo, wd, S.scene_abs_x);
+#pragma unroll
+                    for (int r = 0; r < kRays; ++r) {
+                        float t, u, v;
+                        uint32_t face;
+                        if (!triangle_hit(S.tris, idx, ray[r], t, u, v, face)) continue;
+                        const float wt = world_t(S.instances[cur_inst], ray[r], t, wo[r], wd[r]);
+                        if (wt > 0.f && closer_hit(best[r], wt, cur_inst, face)) {
+                            best[r] = TraceResult{wt, u, v, cur_inst, face};
+                            tmax_box[r] = prune_limit(wt, wo[r], wd[r], S.scene_abs_x);
+                        }
                     }
                 } else {
                     const uint32_t inst = __ldg(S.tlas_items + idx);
                     const DevInstance &I = S.instances[inst];
                     if (I.type == 1u) {
-                        float t;
-                        if (mine && sphere_hit(I, wo, wd, t) && t > 0.f && closer_hit(best, t, inst, kInvalid)) {
-                            best = TraceResult{t, 0.f, 0.f, inst, kInvalid};
-                            tmax_box = prune_limit(best.t, wo, wd, S.scene_abs_x);
+                        if (!mine) continue;
+#pragma unroll
+                        for (int r = 0; r < kRays; ++r) {
+                            float t;
+                            if (sphere_hit(I, wo[r], wd[r], t) && t > 0.f && closer_hit(best[r], t, inst, kInvalid)) {
+                                best[r] = TraceResult{t, 0.f, 0.f, inst, kInvalid};
+                                tmax_box[r] = prune_limit(t, wo[r], wd[r], S.scene_abs_x);
+                            }
                         }
                     } else if (I.blas_root != kInvalid) {
                         // Enter the BLAS with every lane (those that did not reach it take no part); the
@@ -835,9 +903,10 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                         blas_sp = sp;
                         in_blas = true;
                         cur_inst = inst;
-                        setup_level(ray, xform_point(I.minv, wo), xform_dir(I.minv, wd));
+#pragma unroll
+                        for (int r = 0; r < kRays; ++r) setup_level(ray[r], xform_point(I.minv, wo[r]), xform_dir(I.minv, wd[r]));
                         const uint32_t entering = __ballot_sync(kAll, mine);  // not empty: the group had bit k
-                        order = __shfl_sync(kAll, ray.oct, __ffs(entering) - 1);
+                        order = __shfl_sync(kAll, ray[0].oct, __ffs(entering) - 1);
                         packed = make_frustum(ray, order, frustum);
                         ngroup = make_uint2(I.blas_root, 1u << 24);
                         nown = mine ? (1u << 24) : 0u;
@@ -849,7 +918,8 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
             if (ngroup.y <= 0x00FFFFFFu) {
                 if (in_blas && sp == blas_sp) {
                     in_blas = false;
-                    setup_level(ray, wo, wd);
+#pragma unroll
+                    for (int r = 0; r < kRays; ++r) setup_level(ray[r], wo[r], wd[r]);
                     order = top_order;
                     if (sp != 0) packed = make_frustum(ray, order, frustum);
                 }
@@ -859,7 +929,9 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                 nown = own[sp];
             }
         }
-        if (valid) finish(item, best);
+#pragma unroll
+        for (int r = 0; r < kRays; ++r)
+            if (valid[r]) finish(base + lane + 32u * r, best[r]);
     }
 }
 

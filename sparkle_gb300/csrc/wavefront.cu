@@ -26,6 +26,7 @@ constexpr int kShadowCursor = 6;  // pop cursor of the shadow stage
 constexpr int kPacketQueue = 7;   // leading extend-queue entries walked in packets (primary rays queued in
                                   // sample-item order, >= kPacketMinSamples of a pixel in a row); 0 after shade
 constexpr int kNextItem = 8;      // next (frame, pixel) sample item to hand out
+constexpr int kPacketRays = 9;    // rays per lane of the packet walk (1 or 2) for the kPacketQueue entries
 
 template <int kKind>
 __device__ __forceinline__ void load_rng(const uint4 *rng, uint32_t pid, Rng &r) {
@@ -223,13 +224,15 @@ __global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers
 // packets of 32 instead, the rest by the persistent form. Both forms are launched every stage and return at
 // once when they have nothing to walk, so the split needs no host round trip (and stays inside a replayed
 // graph).
-template <bool kCount, bool kBatch = false, bool kPackets = false>
-__global__ void __launch_bounds__(128, kPackets ? SPK_PACKET_MIN_BLOCKS : SPK_WALK_MIN_BLOCKS)
+template <bool kCount, bool kBatch = false, int kPackets = 0>
+__global__ void __launch_bounds__(128, kPackets == 2   ? SPK_PACKET2_MIN_BLOCKS
+                                       : kPackets == 1 ? SPK_PACKET_MIN_BLOCKS
+                                                       : SPK_WALK_MIN_BLOCKS)
     k_wf_extend(DevScene S, WavefrontState s, int in_queue, Counters *counters) {
     const unsigned long long len = counters->queue_counters[in_queue];
     const unsigned long long split = min(counters->queue_counters[kPacketQueue], len);
     const unsigned long long first = kPackets ? 0ull : split, n = kPackets ? split : len - split;
-    if (n == 0) return;
+    if (n == 0 || (kPackets && counters->queue_counters[kPacketRays] != kPackets)) return;
     uint32_t err = 0, done = 0;
     TraceCounts tc;
     const uint32_t *queue = s.queue[in_queue] + first;
@@ -241,16 +244,18 @@ __global__ void __launch_bounds__(128, kPackets ? SPK_PACKET_MIN_BLOCKS : SPK_WA
         d = mk3(d4.x, d4.y, d4.z);
         return kBatch ? s.slot_root[pid] : S.tlas_root;
     };
-    auto finish = [&](unsigned long long, const TraceResult &h) {
-        s.hit[pid] = make_float4(h.t, h.u, h.v, __uint_as_float(h.inst));
-        s.hit_face[pid] = h.face;
+    auto store = [&](uint32_t p, const TraceResult &h) {
+        s.hit[p] = make_float4(h.t, h.u, h.v, __uint_as_float(h.inst));
+        s.hit_face[p] = h.face;
         ++done;
     };
-    if constexpr (kPackets)
-        walk_packets<kCount>(S, &counters->queue_counters[kPacketCursor], n, err, &tc, fetch, finish);
-    else
+    if constexpr (kPackets != 0) {
+        walk_packets<kCount, kPackets>(S, &counters->queue_counters[kPacketCursor], n, err, &tc, fetch,
+                                       [&](unsigned long long q, const TraceResult &h) { store(queue[q], h); });
+    } else {
         walk_persistent<kTraceClosest, kCount>(S, &counters->queue_counters[kCursor], n, kFltMax, err, &tc, fetch,
-                                               finish);
+                                               [&](unsigned long long, const TraceResult &h) { store(pid, h); });
+    }
     warp_add_u64(&counters->extension_rays, done);
     if (kCount) {
         warp_add_u64(&counters->node_visits, tc.nodes);
@@ -354,8 +359,10 @@ __global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers
     if (slot == 0) {
         counters->queue_counters[kLen0] = initial;
         counters->queue_counters[kNextItem] = initial;
+        const uint32_t frames = total_items / (fb.width * fb.height);
         counters->queue_counters[kPacketQueue] =
-            SPK_ITEM_ORDER == 1 && packets && total_items / (fb.width * fb.height) >= kPacketMinSamples ? initial : 0u;
+            SPK_ITEM_ORDER == 1 && packets && frames >= kPacketMinSamples ? initial : 0u;
+        counters->queue_counters[kPacketRays] = frames >= kPacket2MinSamples ? 2u : 1u;
     }
 }
 
@@ -656,6 +663,7 @@ __global__ void __launch_bounds__(128) k_b_generate(DevScene S, BatchParams b, W
         counters->queue_counters[kLen0] = first;
         counters->queue_counters[kNextItem] = first;
         counters->queue_counters[kPacketQueue] = SPK_ITEM_ORDER == 1 ? min(b.packet_items, 1ull * first) : 0ull;
+        counters->queue_counters[kPacketRays] = 1u;
     }
 }
 
@@ -844,8 +852,9 @@ unsigned extend_blocks(int num_sms, uint32_t per_sm_override) {
     return static_cast<unsigned>(num_sms) * n;
 }
 
-// Kernel launches of one extend stage: the packet and the persistent form.
-constexpr uint32_t kExtendLaunches = 2u;
+// Kernel launches of one extend stage: the packet forms (a batch: one ray per lane; otherwise one and two)
+// and the persistent form.
+constexpr uint32_t extend_launches(bool batch) { return batch ? 2u : 3u; }
 
 cudaError_t launch_extend(const DevScene &scene, const WavefrontState &s, int in, bool count, Counters *counters,
                           unsigned grid, cudaStream_t stream, LaunchEvents *ev, bool batch = false) {
@@ -855,12 +864,14 @@ cudaError_t launch_extend(const DevScene &scene, const WavefrontState &s, int in
     if (e != cudaSuccess) return e;
     if (ev) ev->before(stream);
     if (batch) {
-        (count ? k_wf_extend<true, true, true> : k_wf_extend<false, true, true>)<<<grid, 128, 0, stream>>>(
-            scene, s, in, counters);
+        (count ? k_wf_extend<true, true, 1> : k_wf_extend<false, true, 1>)<<<grid, 128, 0, stream>>>(scene, s, in,
+                                                                                                     counters);
         (count ? k_wf_extend<true, true> : k_wf_extend<false, true>)<<<grid, 128, 0, stream>>>(scene, s, in, counters);
     } else {
-        (count ? k_wf_extend<true, false, true> : k_wf_extend<false, false, true>)<<<grid, 128, 0, stream>>>(
-            scene, s, in, counters);
+        (count ? k_wf_extend<true, false, 1> : k_wf_extend<false, false, 1>)<<<grid, 128, 0, stream>>>(scene, s, in,
+                                                                                                       counters);
+        (count ? k_wf_extend<true, false, 2> : k_wf_extend<false, false, 2>)<<<grid, 128, 0, stream>>>(scene, s, in,
+                                                                                                       counters);
         (count ? k_wf_extend<true, false> : k_wf_extend<false, false>)<<<grid, 128, 0, stream>>>(scene, s, in,
                                                                                                  counters);
     }
@@ -1009,7 +1020,7 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
             nl += 3;
         }
         if ((e = launch_extend(scene, se, in, count, counters, extend_grid, stream, ev)) != cudaSuccess) return e;
-        nl += kExtendLaunches;
+        nl += extend_launches(false);
         WavefrontState ss = se;
         if (tuning.material_sort) {
             ss = enqueue_material_sort(scene, se, in, counters, num_sms, stream);
@@ -1213,7 +1224,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 return e;
             }
             iter += kChunk;
-            nl += (1u + kExtendLaunches + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
+            nl += (1u + extend_launches(false) + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
                    (nee == kNeeDeferred ? 2u : 0u)) * kChunk;
             if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
                 cudaSuccess)
@@ -1285,7 +1296,7 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         iter += kChunk;
-        nl += (1u + kExtendLaunches + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
+        nl += (1u + extend_launches(true) + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
                (nee == kNeeDeferred ? 2u : 0u)) * kChunk;
         if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
             cudaSuccess)

@@ -119,6 +119,12 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
 #define SPK_PACKET_MIN_SAMPLES 8
 #endif
 constexpr uint32_t kPacketMinSamples = SPK_PACKET_MIN_SAMPLES;
+// Fewest samples per pixel in a multi-frame pass for packets of two rays per lane (64 consecutive samples:
+// one pixel's at 64 frames), which share each node visit between twice the rays.
+#ifndef SPK_PACKET2_MIN_SAMPLES
+#define SPK_PACKET2_MIN_SAMPLES 64
+#endif
+constexpr uint32_t kPacket2MinSamples = SPK_PACKET2_MIN_SAMPLES;
 
 struct DevRequest {
     DevCamera cam;
