@@ -227,9 +227,10 @@ typedef struct spk_tuning {
                                       (16 B per sample of the call, 32 B with the spatial fill, in device memory);
                                       0 renders frame by frame (one path per pixel, no per-sample buffers) */
     uint32_t primary_packets;      /* wavefront: 1 (default) walks the primary rays of a multi-frame pass of >= 8 frames
-                                      (of batch requests of >= 8 spp) in packets of 32 consecutive samples, a pixel's
-                                      samples side by side, each node tested once for the packet; 0 walks every ray on
-                                      its own. Fewer samples per pixel are walked on their own either way */
+                                      (of batch requests of >= 8 spp) in packets of 32 consecutive samples (64 from 32
+                                      frames), a pixel's samples side by side, each node tested once for the packet; 0
+                                      walks every ray on its own. Fewer samples per pixel are walked on their own
+                                      either way */
 } spk_tuning;
 
 /* ------------------------------------------------------------------------------------------------ */
