@@ -852,26 +852,36 @@ unsigned extend_blocks(int num_sms, uint32_t per_sm_override) {
     return static_cast<unsigned>(num_sms) * n;
 }
 
-// Kernel launches of one extend stage: the packet forms (a batch: one ray per lane; otherwise one and two)
-// and the persistent form.
-constexpr uint32_t extend_launches(bool batch) { return batch ? 2u : 3u; }
+// Kernel launches of one extend stage: the persistent form, and the packet form of `packet_rays` rays per
+// lane (1 or 2; 0: none) where the stage may walk packets (a pass's first extend).
+constexpr uint32_t extend_launches(uint32_t packet_rays) { return packet_rays ? 2u : 1u; }
+
+// The packet form a multi-frame pass of `frames` frames per pixel walks its primary rays with (0: none); the
+// generate kernel sets the same in the queue counters, which the kernels follow.
+uint32_t pass_packet_rays(uint32_t frames, const WfTuning &tuning) {
+    if (SPK_ITEM_ORDER != 1 || !tuning.packets || frames < kPacketMinSamples) return 0u;
+    return frames >= kPacket2MinSamples ? 2u : 1u;
+}
 
 cudaError_t launch_extend(const DevScene &scene, const WavefrontState &s, int in, bool count, Counters *counters,
-                          unsigned grid, cudaStream_t stream, LaunchEvents *ev, bool batch = false) {
+                          unsigned grid, cudaStream_t stream, LaunchEvents *ev, bool batch, uint32_t packet_rays) {
     unsigned long long *qc = counters->queue_counters;
     static_assert(kPacketCursor == kCursor + 1, "one reset for both cursors");
     cudaError_t e = cudaMemsetAsync(qc + kCursor, 0, 2 * sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     if (ev) ev->before(stream);
     if (batch) {
-        (count ? k_wf_extend<true, true, 1> : k_wf_extend<false, true, 1>)<<<grid, 128, 0, stream>>>(scene, s, in,
-                                                                                                     counters);
+        if (packet_rays)
+            (count ? k_wf_extend<true, true, 1> : k_wf_extend<false, true, 1>)<<<grid, 128, 0, stream>>>(scene, s, in,
+                                                                                                         counters);
         (count ? k_wf_extend<true, true> : k_wf_extend<false, true>)<<<grid, 128, 0, stream>>>(scene, s, in, counters);
     } else {
-        (count ? k_wf_extend<true, false, 1> : k_wf_extend<false, false, 1>)<<<grid, 128, 0, stream>>>(scene, s, in,
-                                                                                                       counters);
-        (count ? k_wf_extend<true, false, 2> : k_wf_extend<false, false, 2>)<<<grid, 128, 0, stream>>>(scene, s, in,
-                                                                                                       counters);
+        if (packet_rays == 1)
+            (count ? k_wf_extend<true, false, 1> : k_wf_extend<false, false, 1>)<<<grid, 128, 0, stream>>>(
+                scene, s, in, counters);
+        if (packet_rays == 2)
+            (count ? k_wf_extend<true, false, 2> : k_wf_extend<false, false, 2>)<<<grid, 128, 0, stream>>>(
+                scene, s, in, counters);
         (count ? k_wf_extend<true, false> : k_wf_extend<false, false>)<<<grid, 128, 0, stream>>>(scene, s, in,
                                                                                                  counters);
     }
@@ -1019,8 +1029,9 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
             se = enqueue_ray_sort(scene, s, in, counters, num_sms, stream);
             nl += 3;
         }
-        if ((e = launch_extend(scene, se, in, count, counters, extend_grid, stream, ev)) != cudaSuccess) return e;
-        nl += extend_launches(false);
+        if ((e = launch_extend(scene, se, in, count, counters, extend_grid, stream, ev, false, 0u)) != cudaSuccess)
+            return e;
+        nl += extend_launches(0u);
         WavefrontState ss = se;
         if (tuning.material_sort) {
             ss = enqueue_material_sort(scene, se, in, counters, num_sms, stream);
@@ -1098,6 +1109,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
     static_assert(kChunk % 2 == 0, "a chunk must keep the queue parity, so one graph serves every chunk");
     for (uint32_t f0 = 0; f0 < num_frames; f0 += kFramesPerPass) {
         const uint32_t frames = std::min(kFramesPerPass, num_frames - f0);
+        const uint32_t packet_rays = pass_packet_rays(frames, tuning);
         const uint32_t total_items = frames * npix;
         // Paths in flight: slots_per_pixel x pixels, within the state's capacity and the pass's items.
         const uint64_t want = static_cast<uint64_t>(npix) * std::max(1u, tuning.slots_per_pixel);
@@ -1120,7 +1132,8 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 if ((ce = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return ce;
                 const WavefrontState se =
                     tuning.ray_sort ? enqueue_ray_sort(scene, s, in, counters, num_sms, stream) : s;
-                if ((ce = launch_extend(scene, se, in, count, counters, extend_grid, stream, chunk_ev)) != cudaSuccess)
+                if ((ce = launch_extend(scene, se, in, count, counters, extend_grid, stream, chunk_ev, false,
+                                        c == 0 ? packet_rays : 0u)) != cudaSuccess)
                     return ce;
                 const WavefrontState ss =
                     tuning.material_sort ? enqueue_material_sort(scene, se, in, counters, num_sms, stream) : se;
@@ -1147,7 +1160,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 uint32_t f0, total_items, count, num_sms;
                 Counters *counters;
                 cudaStream_t stream;
-                unsigned extend_grid, shade_grid, material_sort, ray_sort, nee_mode;
+                unsigned extend_grid, shade_grid, material_sort, ray_sort, nee_mode, packet_rays;
             } key;
             std::memset(static_cast<void *>(&key), 0, sizeof(key));  // padding too: the key is compared bytewise
             key.scene = scene;
@@ -1166,6 +1179,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
             key.material_sort = tuning.material_sort;
             key.ray_sort = tuning.ray_sort;
             key.nee_mode = static_cast<unsigned>(nee);
+            key.packet_rays = packet_rays;
             const auto *kb = reinterpret_cast<const unsigned char *>(&key);
             graph_ev.pairs = graph->events;
             graph_ev.capacity = static_cast<int>(kChunk);
@@ -1224,8 +1238,9 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 return e;
             }
             iter += kChunk;
-            nl += (1u + extend_launches(false) + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
-                   (nee == kNeeDeferred ? 2u : 0u)) * kChunk;
+            nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) + (nee == kNeeDeferred ? 2u : 0u)) *
+                      kChunk +
+                  extend_launches(packet_rays) - 1u;
             if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
                 cudaSuccess)
                 return e;
@@ -1279,12 +1294,14 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
     const unsigned long long max_iters = b.total_items * 64ull + kChunk;
     unsigned long long iter = 0;
     auto *shade = pick_b_shade(b.rng, nee);
+    const uint32_t packet_rays = SPK_ITEM_ORDER == 1 && b.packet_items ? 1u : 0u;  // the first extend of the batch
     for (;;) {
         for (uint32_t c = 0; c < kChunk; ++c) {
             const int in = static_cast<int>(c & 1u), out = in ^ 1;
             if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
             const WavefrontState se = tuning.ray_sort ? enqueue_ray_sort(scene, s, in, counters, num_sms, stream) : s;
-            if ((e = launch_extend(scene, se, in, count, counters, extend_grid, stream, ev, true)) != cudaSuccess)
+            if ((e = launch_extend(scene, se, in, count, counters, extend_grid, stream, ev, true,
+                                   c == 0 ? packet_rays : 0u)) != cudaSuccess)
                 return e;
             const WavefrontState ss =
                 tuning.material_sort ? enqueue_material_sort(scene, se, in, counters, num_sms, stream) : se;
@@ -1296,8 +1313,9 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         iter += kChunk;
-        nl += (1u + extend_launches(true) + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
-               (nee == kNeeDeferred ? 2u : 0u)) * kChunk;
+        nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) + (nee == kNeeDeferred ? 2u : 0u)) *
+                  kChunk +
+              extend_launches(packet_rays) - 1u;
         if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
             cudaSuccess)
             return e;

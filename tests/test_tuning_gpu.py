@@ -166,3 +166,21 @@ def test_primary_packets_run_where_they_pay(ctx, small_terrain, frames):
     else:
         assert visits[1] == visits[0], visits
     ctx.set_tuning(**DEFAULTS)
+
+
+@pytest.mark.parametrize("frames", [9, 40])
+def test_packets_with_ragged_ends(ctx, small_terrain, frames):
+    """Odd image sizes: packets straddle pixels (40 frames: two rays per lane, 64 items across two pixels;
+    9 frames: one ray per lane across four) and the last packet of the pass is partly empty (33 x 17 x 40 =
+    22440 items, not a multiple of 64). Full depth, NEE on: the same bits with packets as without."""
+    scene, cam_args = small_terrain
+    W, H = 33, 17
+    camera = scenes.make_camera(cam_args, W, H)
+    cfg = abi.make_config(W, H, spp=1, bounce=6, enable_nee=True, seed=11)
+    out = []
+    for packets in (1, 0):
+        hdr, img, st = render(ctx, scene, camera, cfg, frames, {"primary_packets": packets})
+        out.append((hdr, img))
+    assert np.array_equal(out[0][0].view(np.uint32), out[1][0].view(np.uint32))
+    assert np.array_equal(out[0][1], out[1][1])
+    ctx.set_tuning(**DEFAULTS)
