@@ -55,7 +55,10 @@ enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOve
 #define SPK_SLAB_RCP 0  // 1: the slab reciprocals as correctly rounded reciprocals (same bits as 1.f/x)
 #endif
 #ifndef SPK_WALK_MIN_BLOCKS
-#define SPK_WALK_MIN_BLOCKS 8  // resident 128-thread blocks per SM the walking kernels are compiled for
+#define SPK_WALK_MIN_BLOCKS 7  // resident 128-thread blocks per SM the closest-hit walks are compiled for (72 registers)
+#endif
+#ifndef SPK_SHADOW_MIN_BLOCKS
+#define SPK_SHADOW_MIN_BLOCKS 8  // the same for the occlusion walk of the shadow stage (64 registers)
 #endif
 #ifndef SPK_PACKET_MIN_BLOCKS
 #define SPK_PACKET_MIN_BLOCKS 8  // resident 128-thread blocks per SM the packet walk is compiled for

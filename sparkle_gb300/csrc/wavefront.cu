@@ -723,7 +723,7 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_b_shade(DevScene 
 // (lane refill as in extend), then the in-order addition of the unoccluded radiance.
 // ------------------------------------------------------------------------------------------------
 template <bool kBatch>
-__global__ void __launch_bounds__(128, SPK_WALK_MIN_BLOCKS) k_wf_shadow(DevScene S, WavefrontState s,
+__global__ void __launch_bounds__(128, SPK_SHADOW_MIN_BLOCKS) k_wf_shadow(DevScene S, WavefrontState s,
                                                                        Counters *counters) {
     uint32_t err = 0;
     const unsigned long long n = counters->queue_counters[kShadowLen];
@@ -844,6 +844,20 @@ unsigned extend_blocks(int num_sms, uint32_t per_sm_override) {
     static int per_sm = 0;
     if (per_sm == 0) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_extend<false>, 128, 0) != cudaSuccess ||
+            per_sm <= 0)
+            per_sm = 8;
+    }
+    const uint32_t n = per_sm_override ? std::min<uint32_t>(per_sm_override, static_cast<uint32_t>(per_sm))
+                                       : static_cast<uint32_t>(per_sm);
+    return static_cast<unsigned>(num_sms) * n;
+}
+
+// The shadow stage's persistent grid: SMs x its own occupancy (compiled for more blocks per SM than the
+// closest-hit walk), capped like the extend grid by spk_tuning.extend_blocks_per_sm.
+unsigned shadow_blocks(int num_sms, uint32_t per_sm_override) {
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wf_shadow<false>, 128, 0) != cudaSuccess ||
             per_sm <= 0)
             per_sm = 8;
     }
@@ -1021,6 +1035,7 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
     ++nl;
     const unsigned shade_blocks = static_cast<unsigned>(num_sms) * tuning.shade_blocks_per_sm;
     const unsigned extend_grid = extend_blocks(num_sms, tuning.extend_blocks_per_sm);
+    const unsigned shadow_grid = shadow_blocks(num_sms, tuning.extend_blocks_per_sm);
     for (uint32_t b = 0; b < p.bounce; ++b) {
         const int in = static_cast<int>(b & 1u), out = in ^ 1;
         if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
@@ -1041,7 +1056,7 @@ cudaError_t launch_render_wavefront(const DevScene &scene, const DevCamera &cam,
         pick_wf_shade(p.rng, nee)<<<shade_blocks, 128, 0, stream>>>(scene, fbuf, p, ss, in, b, counters);
         ++nl;
         if (nee == kNeeDeferred) {
-            enqueue_shadow_stage<0>(scene, cam, fbuf, p, BatchParams{}, ss, p.rng, out, 0u, 0u, counters, extend_grid,
+            enqueue_shadow_stage<0>(scene, cam, fbuf, p, BatchParams{}, ss, p.rng, out, 0u, 0u, counters, shadow_grid,
                                     shade_blocks, stream);
             nl += 2;
         }
@@ -1105,6 +1120,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
     unsigned long long *qc = counters->queue_counters;
     const unsigned shade_blocks = static_cast<unsigned>(num_sms) * tuning.shade_blocks_per_sm;
     const unsigned extend_grid = extend_blocks(num_sms, tuning.extend_blocks_per_sm);
+    const unsigned shadow_grid = shadow_blocks(num_sms, tuning.extend_blocks_per_sm);
     constexpr uint32_t kChunk = kChunkIterations;
     static_assert(kChunk % 2 == 0, "a chunk must keep the queue parity, so one graph serves every chunk");
     for (uint32_t f0 = 0; f0 < num_frames; f0 += kFramesPerPass) {
@@ -1142,7 +1158,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                                                                             total_items, counters);
                 if (nee == kNeeDeferred)
                     enqueue_shadow_stage<1>(scene, cam, fbuf, p, BatchParams{}, ss, p.rng, out, f0, total_items,
-                                            counters, extend_grid, shade_blocks, stream);
+                                            counters, shadow_grid, shade_blocks, stream);
             }
             return cudaGetLastError();
         };
@@ -1279,6 +1295,7 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
     unsigned long long *qc = counters->queue_counters;
     const unsigned shade_blocks = static_cast<unsigned>(num_sms) * tuning.shade_blocks_per_sm;
     const unsigned extend_grid = extend_blocks(num_sms, tuning.extend_blocks_per_sm);
+    const unsigned shadow_grid = shadow_blocks(num_sms, tuning.extend_blocks_per_sm);
     const unsigned long long want = tuning.batch_slots ? tuning.batch_slots : s.capacity;
     const uint32_t first = static_cast<uint32_t>(std::min<unsigned long long>({want, s.capacity, b.total_items}));
     if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
@@ -1309,7 +1326,7 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
             shade<<<shade_blocks, 128, 0, stream>>>(scene, b, ss, in, counters);
             if (nee == kNeeDeferred)
                 enqueue_shadow_stage<2>(scene, DevCamera{}, FrameBuffers{}, RenderParams{}, b, ss, b.rng, out, 0u, 0u,
-                                        counters, extend_grid, shade_blocks, stream);
+                                        counters, shadow_grid, shade_blocks, stream);
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         iter += kChunk;
