@@ -31,7 +31,7 @@ struct Counters {
     unsigned int pad;
     unsigned long long node_visits;
     unsigned long long tri_tests;
-    unsigned long long queue_counters[10];
+    unsigned long long queue_counters[12];
 };
 
 // Sum of a per-thread count over the active lanes of a warp, added once per warp.

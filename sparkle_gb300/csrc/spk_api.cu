@@ -2055,22 +2055,22 @@ spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t 
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "batch of %llu sample items: split it below 2^32", items);
     const uint32_t slots = static_cast<uint32_t>(
         std::min<unsigned long long>(items, ctx->tuning.batch_slots ? ctx->tuning.batch_slots : kMaxPathSlots));
-    // First-pass queue (items 0 .. slots-1): the items of requests with spp >= kPacketMinSamples first, walked
-    // in packets, then the others; each request's items stay in item order.
-    unsigned long long packet_items = 0;
-    for (const DevRequest &d : reqs) {
-        if (d.spp >= kPacketMinSamples)
-            packet_items += std::min<unsigned long long>(d.item_base + 1ull * d.npix * d.spp, slots) -
-                            std::min<unsigned long long>(d.item_base, slots);
-    }
+    // First-pass queue (items 0 .. slots-1), each request's items in item order: the requests with spp >=
+    // kPacket2MinSamples first (walked in packets of two rays per lane), then those with spp >=
+    // kPacketMinSamples (one ray per lane), then the others.
+    auto packet_class = [](uint32_t spp) { return spp >= kPacket2MinSamples ? 0 : spp >= kPacketMinSamples ? 1 : 2; };
+    unsigned long long class_items[3] = {0, 0, 0};
+    auto first_pass_items = [&](const DevRequest &d) {
+        return std::min<unsigned long long>(d.item_base + 1ull * d.npix * d.spp, slots) -
+               std::min<unsigned long long>(d.item_base, slots);
+    };
+    for (const DevRequest &d : reqs) class_items[packet_class(d.spp)] += first_pass_items(d);
     {
-        unsigned long long packed = 0, rest = packet_items;
+        unsigned long long pos[3] = {0, class_items[0], class_items[0] + class_items[1]};
         for (DevRequest &d : reqs) {
-            const unsigned long long n = std::min<unsigned long long>(d.item_base + 1ull * d.npix * d.spp, slots) -
-                                         std::min<unsigned long long>(d.item_base, slots);
-            unsigned long long &pos = d.spp >= kPacketMinSamples ? packed : rest;
-            d.queue_base = static_cast<uint32_t>(pos);
-            pos += n;
+            unsigned long long &p = pos[packet_class(d.spp)];
+            d.queue_base = static_cast<uint32_t>(p);
+            p += first_pass_items(d);
         }
     }
     cudaError_t e;
@@ -2101,7 +2101,8 @@ spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t 
     b.enable_nee = enable_nee ? 1u : 0u;
     b.total_items = items;
     b.total_pixels = pixels;
-    b.packet_items = ctx->tuning.primary_packets ? packet_items : 0ull;
+    b.packet_items = ctx->tuning.primary_packets ? class_items[0] + class_items[1] : 0ull;
+    b.packet2_items = ctx->tuning.primary_packets ? class_items[0] : 0ull;
     b.out_hdr = ctx->batch_hdr.ptr;
     b.out_image = ctx->batch_img.ptr;
     const bool count = (ctx->instrumentation & SPK_INSTR_COUNT_TRAFFIC) != 0;

@@ -18,15 +18,18 @@ namespace {
 
 // queue_counters slots
 constexpr int kLen0 = 0;          // length of queue 0 (queue 1's length is slot 1)
-constexpr int kCursor = 2;        // pop cursor of the running persistent stage
-constexpr int kPacketCursor = 3;  // pop cursor of the packet walk (reset with kCursor)
-constexpr int kShadowLen = 4;     // occlusion rays queued by the iteration's shade stage
-constexpr int kNeeLen = 5;        // light-sampling vertices of the iteration's shade stage
-constexpr int kShadowCursor = 6;  // pop cursor of the shadow stage
-constexpr int kPacketQueue = 7;   // leading extend-queue entries walked in packets (primary rays queued in
-                                  // sample-item order, >= kPacketMinSamples of a pixel in a row); 0 after shade
-constexpr int kNextItem = 8;      // next (frame, pixel) sample item to hand out
-constexpr int kPacketRays = 9;    // rays per lane of the packet walk (1 or 2) for the kPacketQueue entries
+constexpr int kCursor = 2;         // pop cursor of the running persistent stage
+constexpr int kPacketCursor = 3;   // pop cursors of the packet walks, one and two rays per lane (reset with
+constexpr int kPacket2Cursor = 4;  // kCursor)
+constexpr int kShadowLen = 5;      // occlusion rays queued by the iteration's shade stage
+constexpr int kNeeLen = 6;         // light-sampling vertices of the iteration's shade stage
+constexpr int kShadowCursor = 7;   // pop cursor of the shadow stage
+// Leading extend-queue entries walked in packets (primary rays queued in sample-item order, >= kPacketMinSamples
+// of a pixel in a row): the first kPacket2Queue with two rays per lane, the rest up to kPacketQueue with one.
+// Both 0 after shade.
+constexpr int kPacketQueue = 8;
+constexpr int kPacket2Queue = 9;
+constexpr int kNextItem = 10;  // next (frame, pixel) sample item to hand out
 
 template <int kKind>
 __device__ __forceinline__ void load_rng(const uint4 *rng, uint32_t pid, Rng &r) {
@@ -214,6 +217,7 @@ __global__ void __launch_bounds__(128) k_wf_generate(DevCamera cam, FrameBuffers
     if (pid == 0) {
         counters->queue_counters[kLen0] = static_cast<unsigned long long>(fb.width) * fb.height;
         counters->queue_counters[kPacketQueue] = 0u;  // one sample per pixel: no packets
+        counters->queue_counters[kPacket2Queue] = 0u;
     }
 }
 
@@ -230,9 +234,11 @@ __global__ void __launch_bounds__(128, kPackets == 2   ? SPK_PACKET2_MIN_BLOCKS
                                                        : SPK_WALK_MIN_BLOCKS)
     k_wf_extend(DevScene S, WavefrontState s, int in_queue, Counters *counters) {
     const unsigned long long len = counters->queue_counters[in_queue];
-    const unsigned long long split = min(counters->queue_counters[kPacketQueue], len);
-    const unsigned long long first = kPackets ? 0ull : split, n = kPackets ? split : len - split;
-    if (n == 0 || (kPackets && counters->queue_counters[kPacketRays] != kPackets)) return;
+    const unsigned long long p1 = min(counters->queue_counters[kPacketQueue], len);
+    const unsigned long long p2 = min(counters->queue_counters[kPacket2Queue], p1);
+    const unsigned long long first = kPackets == 2 ? 0ull : kPackets == 1 ? p2 : p1;
+    const unsigned long long n = (kPackets == 2 ? p2 : kPackets == 1 ? p1 : len) - first;
+    if (n == 0) return;
     uint32_t err = 0, done = 0;
     TraceCounts tc;
     const uint32_t *queue = s.queue[in_queue] + first;
@@ -250,7 +256,8 @@ __global__ void __launch_bounds__(128, kPackets == 2   ? SPK_PACKET2_MIN_BLOCKS
         ++done;
     };
     if constexpr (kPackets != 0) {
-        walk_packets<kCount, kPackets>(S, &counters->queue_counters[kPacketCursor], n, err, &tc, fetch,
+        walk_packets<kCount, kPackets>(S, &counters->queue_counters[kPackets == 2 ? kPacket2Cursor : kPacketCursor], n,
+                                       err, &tc, fetch,
                                        [&](unsigned long long q, const TraceResult &h) { store(queue[q], h); });
     } else {
         walk_persistent<kTraceClosest, kCount>(S, &counters->queue_counters[kCursor], n, kFltMax, err, &tc, fetch,
@@ -270,7 +277,10 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_wf_shade(DevScene
     uint32_t shadow = 0, err = 0;
     const unsigned long long n = counters->queue_counters[in_queue];
     const int out_queue = in_queue ^ 1;
-    if (blockIdx.x == 0 && threadIdx.x == 0) counters->queue_counters[kPacketQueue] = 0u;  // the next queue is mixed
+    if (blockIdx.x == 0 && threadIdx.x == 0) {  // the next queue is mixed
+        counters->queue_counters[kPacketQueue] = 0u;
+        counters->queue_counters[kPacket2Queue] = 0u;
+    }
     const uint32_t *queue = s.queue[in_queue];
     for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
          q0 += static_cast<unsigned long long>(gridDim.x) * blockDim.x) {
@@ -360,9 +370,9 @@ __global__ void __launch_bounds__(128) k_mf_generate(DevCamera cam, FrameBuffers
         counters->queue_counters[kLen0] = initial;
         counters->queue_counters[kNextItem] = initial;
         const uint32_t frames = total_items / (fb.width * fb.height);
-        counters->queue_counters[kPacketQueue] =
-            SPK_ITEM_ORDER == 1 && packets && frames >= kPacketMinSamples ? initial : 0u;
-        counters->queue_counters[kPacketRays] = frames >= kPacket2MinSamples ? 2u : 1u;
+        const bool pk = SPK_ITEM_ORDER == 1 && packets && frames >= kPacketMinSamples;
+        counters->queue_counters[kPacketQueue] = pk ? initial : 0u;
+        counters->queue_counters[kPacket2Queue] = pk && frames >= kPacket2MinSamples ? initial : 0u;
     }
 }
 
@@ -375,7 +385,10 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_mf_shade(DevScene
     uint32_t shadow = 0, err = 0;
     const unsigned long long n = counters->queue_counters[in_queue];
     const int out_queue = in_queue ^ 1;
-    if (blockIdx.x == 0 && threadIdx.x == 0) counters->queue_counters[kPacketQueue] = 0u;  // the next queue is mixed
+    if (blockIdx.x == 0 && threadIdx.x == 0) {  // the next queue is mixed
+        counters->queue_counters[kPacketQueue] = 0u;
+        counters->queue_counters[kPacket2Queue] = 0u;
+    }
     const uint32_t *queue = s.queue[in_queue];
     const uint32_t lane = threadIdx.x & 31u;
     for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
@@ -663,7 +676,7 @@ __global__ void __launch_bounds__(128) k_b_generate(DevScene S, BatchParams b, W
         counters->queue_counters[kLen0] = first;
         counters->queue_counters[kNextItem] = first;
         counters->queue_counters[kPacketQueue] = SPK_ITEM_ORDER == 1 ? min(b.packet_items, 1ull * first) : 0ull;
-        counters->queue_counters[kPacketRays] = 1u;
+        counters->queue_counters[kPacket2Queue] = SPK_ITEM_ORDER == 1 ? min(b.packet2_items, 1ull * first) : 0ull;
     }
 }
 
@@ -673,7 +686,10 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_b_shade(DevScene 
     uint32_t shadow = 0, err = 0;
     const unsigned long long n = counters->queue_counters[in_queue];
     const int out_queue = in_queue ^ 1;
-    if (blockIdx.x == 0 && threadIdx.x == 0) counters->queue_counters[kPacketQueue] = 0u;  // the next queue is mixed
+    if (blockIdx.x == 0 && threadIdx.x == 0) {  // the next queue is mixed
+        counters->queue_counters[kPacketQueue] = 0u;
+        counters->queue_counters[kPacket2Queue] = 0u;
+    }
     const uint32_t *queue = s.queue[in_queue];
     const uint32_t lane = threadIdx.x & 31u;
     for (unsigned long long q0 = static_cast<unsigned long long>(blockIdx.x) * blockDim.x; q0 < n;
@@ -866,35 +882,38 @@ unsigned shadow_blocks(int num_sms, uint32_t per_sm_override) {
     return static_cast<unsigned>(num_sms) * n;
 }
 
-// Kernel launches of one extend stage: the persistent form, and the packet form of `packet_rays` rays per
-// lane (1 or 2; 0: none) where the stage may walk packets (a pass's first extend).
-constexpr uint32_t extend_launches(uint32_t packet_rays) { return packet_rays ? 2u : 1u; }
+// Kernel launches of one extend stage: the persistent form, and the packet forms `packet_forms` names (bit 0:
+// one ray per lane, bit 1: two) where the stage may walk packets (a pass's first extend).
+constexpr uint32_t extend_launches(uint32_t packet_forms) { return 1u + (packet_forms & 1u) + (packet_forms >> 1); }
 
-// The packet form a multi-frame pass of `frames` frames per pixel walks its primary rays with (0: none); the
-// generate kernel sets the same in the queue counters, which the kernels follow.
-uint32_t pass_packet_rays(uint32_t frames, const WfTuning &tuning) {
+// The packet forms a multi-frame pass of `frames` frames per pixel walks its primary rays with; the generate
+// kernel sets the matching queue counters, which the kernels follow.
+uint32_t pass_packet_forms(uint32_t frames, const WfTuning &tuning) {
     if (SPK_ITEM_ORDER != 1 || !tuning.packets || frames < kPacketMinSamples) return 0u;
     return frames >= kPacket2MinSamples ? 2u : 1u;
 }
 
 cudaError_t launch_extend(const DevScene &scene, const WavefrontState &s, int in, bool count, Counters *counters,
-                          unsigned grid, cudaStream_t stream, LaunchEvents *ev, bool batch, uint32_t packet_rays) {
+                          unsigned grid, cudaStream_t stream, LaunchEvents *ev, bool batch, uint32_t packet_forms) {
     unsigned long long *qc = counters->queue_counters;
-    static_assert(kPacketCursor == kCursor + 1, "one reset for both cursors");
-    cudaError_t e = cudaMemsetAsync(qc + kCursor, 0, 2 * sizeof(unsigned long long), stream);
+    static_assert(kPacketCursor == kCursor + 1 && kPacket2Cursor == kCursor + 2, "one reset for the cursors");
+    cudaError_t e = cudaMemsetAsync(qc + kCursor, 0, 3 * sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
     if (ev) ev->before(stream);
     if (batch) {
-        if (packet_rays)
+        if (packet_forms & 2u)
+            (count ? k_wf_extend<true, true, 2> : k_wf_extend<false, true, 2>)<<<grid, 128, 0, stream>>>(scene, s, in,
+                                                                                                         counters);
+        if (packet_forms & 1u)
             (count ? k_wf_extend<true, true, 1> : k_wf_extend<false, true, 1>)<<<grid, 128, 0, stream>>>(scene, s, in,
                                                                                                          counters);
         (count ? k_wf_extend<true, true> : k_wf_extend<false, true>)<<<grid, 128, 0, stream>>>(scene, s, in, counters);
     } else {
-        if (packet_rays == 1)
-            (count ? k_wf_extend<true, false, 1> : k_wf_extend<false, false, 1>)<<<grid, 128, 0, stream>>>(
-                scene, s, in, counters);
-        if (packet_rays == 2)
+        if (packet_forms & 2u)
             (count ? k_wf_extend<true, false, 2> : k_wf_extend<false, false, 2>)<<<grid, 128, 0, stream>>>(
+                scene, s, in, counters);
+        if (packet_forms & 1u)
+            (count ? k_wf_extend<true, false, 1> : k_wf_extend<false, false, 1>)<<<grid, 128, 0, stream>>>(
                 scene, s, in, counters);
         (count ? k_wf_extend<true, false> : k_wf_extend<false, false>)<<<grid, 128, 0, stream>>>(scene, s, in,
                                                                                                  counters);
@@ -1125,7 +1144,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
     static_assert(kChunk % 2 == 0, "a chunk must keep the queue parity, so one graph serves every chunk");
     for (uint32_t f0 = 0; f0 < num_frames; f0 += kFramesPerPass) {
         const uint32_t frames = std::min(kFramesPerPass, num_frames - f0);
-        const uint32_t packet_rays = pass_packet_rays(frames, tuning);
+        const uint32_t packet_forms = pass_packet_forms(frames, tuning);
         const uint32_t total_items = frames * npix;
         // Paths in flight: slots_per_pixel x pixels, within the state's capacity and the pass's items.
         const uint64_t want = static_cast<uint64_t>(npix) * std::max(1u, tuning.slots_per_pixel);
@@ -1149,7 +1168,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 const WavefrontState se =
                     tuning.ray_sort ? enqueue_ray_sort(scene, s, in, counters, num_sms, stream) : s;
                 if ((ce = launch_extend(scene, se, in, count, counters, extend_grid, stream, chunk_ev, false,
-                                        c == 0 ? packet_rays : 0u)) != cudaSuccess)
+                                        c == 0 ? packet_forms : 0u)) != cudaSuccess)
                     return ce;
                 const WavefrontState ss =
                     tuning.material_sort ? enqueue_material_sort(scene, se, in, counters, num_sms, stream) : se;
@@ -1176,7 +1195,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 uint32_t f0, total_items, count, num_sms;
                 Counters *counters;
                 cudaStream_t stream;
-                unsigned extend_grid, shade_grid, material_sort, ray_sort, nee_mode, packet_rays;
+                unsigned extend_grid, shade_grid, material_sort, ray_sort, nee_mode, packet_forms;
             } key;
             std::memset(static_cast<void *>(&key), 0, sizeof(key));  // padding too: the key is compared bytewise
             key.scene = scene;
@@ -1195,7 +1214,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
             key.material_sort = tuning.material_sort;
             key.ray_sort = tuning.ray_sort;
             key.nee_mode = static_cast<unsigned>(nee);
-            key.packet_rays = packet_rays;
+            key.packet_forms = packet_forms;
             const auto *kb = reinterpret_cast<const unsigned char *>(&key);
             graph_ev.pairs = graph->events;
             graph_ev.capacity = static_cast<int>(kChunk);
@@ -1256,7 +1275,7 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
             iter += kChunk;
             nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) + (nee == kNeeDeferred ? 2u : 0u)) *
                       kChunk +
-                  extend_launches(packet_rays) - 1u;
+                  extend_launches(packet_forms) - 1u;
             if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
                 cudaSuccess)
                 return e;
@@ -1311,14 +1330,16 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
     const unsigned long long max_iters = b.total_items * 64ull + kChunk;
     unsigned long long iter = 0;
     auto *shade = pick_b_shade(b.rng, nee);
-    const uint32_t packet_rays = SPK_ITEM_ORDER == 1 && b.packet_items ? 1u : 0u;  // the first extend of the batch
+    // the first extend of the batch: two rays per lane for its first packet2_items entries, one for the rest
+    const uint32_t packet_forms =
+        SPK_ITEM_ORDER == 1 ? (b.packet2_items ? 2u : 0u) | (b.packet_items > b.packet2_items ? 1u : 0u) : 0u;
     for (;;) {
         for (uint32_t c = 0; c < kChunk; ++c) {
             const int in = static_cast<int>(c & 1u), out = in ^ 1;
             if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
             const WavefrontState se = tuning.ray_sort ? enqueue_ray_sort(scene, s, in, counters, num_sms, stream) : s;
             if ((e = launch_extend(scene, se, in, count, counters, extend_grid, stream, ev, true,
-                                   c == 0 ? packet_rays : 0u)) != cudaSuccess)
+                                   c == 0 ? packet_forms : 0u)) != cudaSuccess)
                 return e;
             const WavefrontState ss =
                 tuning.material_sort ? enqueue_material_sort(scene, se, in, counters, num_sms, stream) : se;
@@ -1332,7 +1353,7 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
         iter += kChunk;
         nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) + (nee == kNeeDeferred ? 2u : 0u)) *
                   kChunk +
-              extend_launches(packet_rays) - 1u;
+              extend_launches(packet_forms) - 1u;
         if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
             cudaSuccess)
             return e;

@@ -142,9 +142,10 @@ struct BatchParams {
     uint32_t rng, enable_nee;
     unsigned long long total_items;
     unsigned long long total_pixels;
-    // The first pass queues its items request by request, the requests with spp >= kPacketMinSamples first:
-    // the first packet_items queue entries are walked in packets (0: none).
-    unsigned long long packet_items;
+    // The first pass queues its items request by request: those of requests with spp >= kPacket2MinSamples
+    // first, walked in packets of two rays per lane (packet2_items entries), then those with spp >=
+    // kPacketMinSamples, in packets of one ray per lane (up to packet_items entries), then the rest.
+    unsigned long long packet_items, packet2_items;
     float4 *out_hdr;     // accumulated frame buffers of all requests, request after request
     ushort4 *out_image;  // tonemapped images (top row first per request)
 };
