@@ -2055,23 +2055,39 @@ spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t 
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "batch of %llu sample items: split it below 2^32", items);
     const uint32_t slots = static_cast<uint32_t>(
         std::min<unsigned long long>(items, ctx->tuning.batch_slots ? ctx->tuning.batch_slots : kMaxPathSlots));
-    // First-pass queue (items 0 .. slots-1), each request's items in item order: the requests with spp >=
-    // kPacket2MinSamples first (walked in packets of two rays per lane), then those with spp >=
-    // kPacketMinSamples (one ray per lane), then the others.
+    // Groups of consecutive whole requests of at most `slots` items (a larger request alone), each rendered as
+    // one wavefront that starts all its items at once. A group's first-pass queue holds each request's items in
+    // item order, the requests with spp >= kPacket2MinSamples first (walked in packets of two rays per lane),
+    // then those with spp >= kPacketMinSamples (one ray per lane), then the others.
     auto packet_class = [](uint32_t spp) { return spp >= kPacket2MinSamples ? 0 : spp >= kPacketMinSamples ? 1 : 2; };
-    unsigned long long class_items[3] = {0, 0, 0};
-    auto first_pass_items = [&](const DevRequest &d) {
-        return std::min<unsigned long long>(d.item_base + 1ull * d.npix * d.spp, slots) -
-               std::min<unsigned long long>(d.item_base, slots);
-    };
-    for (const DevRequest &d : reqs) class_items[packet_class(d.spp)] += first_pass_items(d);
-    {
+    std::vector<BatchGroup> groups;
+    auto close_group = [&](uint32_t r0, uint32_t r1, unsigned long long lo, unsigned long long hi) {
+        const unsigned long long first_end = lo + std::min<unsigned long long>(slots, hi - lo);
+        auto first_pass_items = [&](const DevRequest &d) {
+            return std::min<unsigned long long>(d.item_base + 1ull * d.npix * d.spp, first_end) -
+                   std::min<unsigned long long>(d.item_base, first_end);
+        };
+        unsigned long long class_items[3] = {0, 0, 0};
+        for (uint32_t r = r0; r < r1; ++r) class_items[packet_class(reqs[r].spp)] += first_pass_items(reqs[r]);
         unsigned long long pos[3] = {0, class_items[0], class_items[0] + class_items[1]};
-        for (DevRequest &d : reqs) {
-            unsigned long long &p = pos[packet_class(d.spp)];
-            d.queue_base = static_cast<uint32_t>(p);
-            p += first_pass_items(d);
+        for (uint32_t r = r0; r < r1; ++r) {
+            unsigned long long &q = pos[packet_class(reqs[r].spp)];
+            reqs[r].queue_base = static_cast<uint32_t>(q);
+            q += first_pass_items(reqs[r]);
         }
+        const bool pk = ctx->tuning.primary_packets != 0;
+        groups.push_back(BatchGroup{lo, hi, pk ? class_items[0] + class_items[1] : 0ull, pk ? class_items[0] : 0ull});
+    };
+    {
+        uint32_t r0 = 0;
+        for (uint32_t r = 1; r < num_requests; ++r) {
+            const DevRequest &d = reqs[r];
+            if (d.item_base + 1ull * d.npix * d.spp - reqs[r0].item_base > slots) {
+                close_group(r0, r, reqs[r0].item_base, d.item_base);
+                r0 = r;
+            }
+        }
+        close_group(r0, num_requests, reqs[r0].item_base, items);
     }
     cudaError_t e;
     WavefrontState &s = ctx->wf_batch;
@@ -2101,8 +2117,8 @@ spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t 
     b.enable_nee = enable_nee ? 1u : 0u;
     b.total_items = items;
     b.total_pixels = pixels;
-    b.packet_items = ctx->tuning.primary_packets ? class_items[0] + class_items[1] : 0ull;
-    b.packet2_items = ctx->tuning.primary_packets ? class_items[0] : 0ull;
+    b.item_lo = 0;
+    b.item_hi = items;
     b.out_hdr = ctx->batch_hdr.ptr;
     b.out_image = ctx->batch_img.ptr;
     const bool count = (ctx->instrumentation & SPK_INSTR_COUNT_TRAFFIC) != 0;
@@ -2114,7 +2130,8 @@ spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t 
     ctx->launch_events.capacity = 0;  // per-launch traversal timing is not recorded for batches
     WfTuning bt = wf_tuning(ctx);
     bt.batch_slots = slots;  // the state may be larger (it only grows): use the requested number of paths
-    e = launch_render_batch(ctx->scene, b, count, ctx->counters, s, ctx->num_sms, ctx->stream, &launches, nullptr, bt);
+    e = launch_render_batch(ctx->scene, b, groups, count, ctx->counters, s, ctx->num_sms, ctx->stream, &launches,
+                            nullptr, bt);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "batch wavefront");
     if ((e = cudaEventRecord(ctx->ev_stop, ctx->stream)) != cudaSuccess) return cuda_fail(ctx, e, "event");
     ctx->batch_host = reqs;

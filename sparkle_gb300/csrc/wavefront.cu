@@ -664,17 +664,19 @@ __device__ __forceinline__ uint32_t start_item_batch(const DevScene &S, const Ba
     return r;
 }
 
-// Starts the first `first` sample items, item i in slot i, queued at the position BatchParams lays out.
+// Starts the group's first `first` sample items, item item_lo + i in slot i, queued at the position
+// BatchParams lays out.
 template <int kKind>
 __global__ void __launch_bounds__(128) k_b_generate(DevScene S, BatchParams b, WavefrontState s, uint32_t first,
                                                     Counters *counters) {
     const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= first) return;
-    const DevRequest &R = b.reqs[start_item_batch<kKind>(S, b, s, slot, slot)];
-    s.queue[0][R.queue_base + static_cast<uint32_t>(slot - R.item_base)] = slot;
+    const unsigned long long item = b.item_lo + slot;
+    const DevRequest &R = b.reqs[start_item_batch<kKind>(S, b, s, slot, item)];
+    s.queue[0][R.queue_base + static_cast<uint32_t>(item - R.item_base)] = slot;
     if (slot == 0) {
         counters->queue_counters[kLen0] = first;
-        counters->queue_counters[kNextItem] = first;
+        counters->queue_counters[kNextItem] = b.item_lo + first;
         counters->queue_counters[kPacketQueue] = SPK_ITEM_ORDER == 1 ? min(b.packet_items, 1ull * first) : 0ull;
         counters->queue_counters[kPacket2Queue] = SPK_ITEM_ORDER == 1 ? min(b.packet2_items, 1ull * first) : 0ull;
     }
@@ -722,7 +724,7 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_b_shade(DevScene 
             base = __shfl_sync(0xFFFFFFFFu, base, __ffs(need_mask) - 1);
             if (need) {
                 const unsigned long long item = base + __popc(need_mask & ((1u << lane) - 1u));
-                if (item < b.total_items) {
+                if (item < b.item_hi) {
                     start_item_batch<kKind>(S, b, s, slot, item);
                     push = true;
                 }
@@ -807,7 +809,7 @@ __global__ void __launch_bounds__(128, SPK_SHADE_MIN_BLOCKS) k_nee_accumulate(De
                         start_item<kKind>(cam, p, s, slot, static_cast<uint32_t>(item), fb.width, fb.height,
                                           frame_base, total_items);
                         push = true;
-                    } else if (kMode == 2 && item < b.total_items) {
+                    } else if (kMode == 2 && item < b.item_hi) {
                         start_item_batch<kKind>(S, b, s, slot, item);
                         push = true;
                     }
@@ -1301,10 +1303,11 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
     return cudaGetLastError();
 }
 
-cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, bool count, Counters *counters,
-                                WavefrontState &s, int num_sms, cudaStream_t stream, uint32_t *launches,
-                                LaunchEvents *ev, const WfTuning &tuning) {
-    if (b.num_reqs == 0 || b.total_items == 0 || s.capacity == 0 || s.sample_capacity < b.total_items)
+cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, const std::vector<BatchGroup> &groups,
+                                bool count, Counters *counters, WavefrontState &s, int num_sms, cudaStream_t stream,
+                                uint32_t *launches, LaunchEvents *ev, const WfTuning &tuning) {
+    if (b.num_reqs == 0 || b.total_items == 0 || s.capacity == 0 || s.sample_capacity < b.total_items ||
+        groups.empty())
         return cudaErrorInvalidValue;
     if ((tuning.ray_sort || tuning.material_sort) && !sort_buffers_ok(s)) return cudaErrorInvalidValue;
     uint32_t nl = 0;
@@ -1316,50 +1319,61 @@ cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, boo
     const unsigned extend_grid = extend_blocks(num_sms, tuning.extend_blocks_per_sm);
     const unsigned shadow_grid = shadow_blocks(num_sms, tuning.extend_blocks_per_sm);
     const unsigned long long want = tuning.batch_slots ? tuning.batch_slots : s.capacity;
-    const uint32_t first = static_cast<uint32_t>(std::min<unsigned long long>({want, s.capacity, b.total_items}));
-    if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
-    if (b.rng == 0) {
-        k_b_generate<0><<<(first + 127) / 128, 128, 0, stream>>>(scene, b, s, first, counters);
-    } else {
-        k_b_generate<1><<<(first + 127) / 128, 128, 0, stream>>>(scene, b, s, first, counters);
-    }
-    ++nl;
-    constexpr uint32_t kChunk = kChunkIterations;
-    // A slot finishes an item within its request's bounce limit and no item starts twice, so
-    // total_items * 64 iterations (bounce < 64 in practice) is a loose guard against a runaway loop.
-    const unsigned long long max_iters = b.total_items * 64ull + kChunk;
-    unsigned long long iter = 0;
     auto *shade = pick_b_shade(b.rng, nee);
-    // the first extend of the batch: two rays per lane for its first packet2_items entries, one for the rest
-    const uint32_t packet_forms =
-        SPK_ITEM_ORDER == 1 ? (b.packet2_items ? 2u : 0u) | (b.packet_items > b.packet2_items ? 1u : 0u) : 0u;
-    for (;;) {
-        for (uint32_t c = 0; c < kChunk; ++c) {
-            const int in = static_cast<int>(c & 1u), out = in ^ 1;
-            if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
-            const WavefrontState se = tuning.ray_sort ? enqueue_ray_sort(scene, s, in, counters, num_sms, stream) : s;
-            if ((e = launch_extend(scene, se, in, count, counters, extend_grid, stream, ev, true,
-                                   c == 0 ? packet_forms : 0u)) != cudaSuccess)
-                return e;
-            const WavefrontState ss =
-                tuning.material_sort ? enqueue_material_sort(scene, se, in, counters, num_sms, stream) : se;
-            if (nee == kNeeDeferred && (e = reset_shadow_counters(counters, stream)) != cudaSuccess) return e;
-            shade<<<shade_blocks, 128, 0, stream>>>(scene, b, ss, in, counters);
-            if (nee == kNeeDeferred)
-                enqueue_shadow_stage<2>(scene, DevCamera{}, FrameBuffers{}, RenderParams{}, b, ss, b.rng, out, 0u, 0u,
-                                        counters, shadow_grid, shade_blocks, stream);
+    constexpr uint32_t kChunk = kChunkIterations;
+    for (const BatchGroup &grp : groups) {
+        if (grp.item_hi <= grp.item_lo || grp.item_hi > b.total_items) return cudaErrorInvalidValue;
+        BatchParams bg = b;
+        bg.item_lo = grp.item_lo;
+        bg.item_hi = grp.item_hi;
+        bg.packet_items = grp.packet_items;
+        bg.packet2_items = grp.packet2_items;
+        const uint32_t first =
+            static_cast<uint32_t>(std::min<unsigned long long>({want, s.capacity, grp.item_hi - grp.item_lo}));
+        if ((e = cudaMemsetAsync(qc, 0, sizeof(counters->queue_counters), stream)) != cudaSuccess) return e;
+        if (b.rng == 0) {
+            k_b_generate<0><<<(first + 127) / 128, 128, 0, stream>>>(scene, bg, s, first, counters);
+        } else {
+            k_b_generate<1><<<(first + 127) / 128, 128, 0, stream>>>(scene, bg, s, first, counters);
         }
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        iter += kChunk;
-        nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) + (nee == kNeeDeferred ? 2u : 0u)) *
-                  kChunk +
-              extend_launches(packet_forms) - 1u;
-        if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
-            cudaSuccess)
-            return e;
-        if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
-        if (*s.host_len == 0) break;
-        if (iter > max_iters) return cudaErrorLaunchFailure;
+        ++nl;
+        // A slot finishes an item within its request's bounce limit and no item starts twice, so
+        // items * 64 iterations (bounce < 64 in practice) is a loose guard against a runaway loop.
+        const unsigned long long max_iters = (grp.item_hi - grp.item_lo) * 64ull + kChunk;
+        unsigned long long iter = 0;
+        // the group's first extend: two rays per lane for its first packet2_items entries, one for the rest
+        const uint32_t packet_forms =
+            SPK_ITEM_ORDER == 1 ? (grp.packet2_items ? 2u : 0u) | (grp.packet_items > grp.packet2_items ? 1u : 0u)
+                                : 0u;
+        for (;;) {
+            for (uint32_t c = 0; c < kChunk; ++c) {
+                const int in = static_cast<int>(c & 1u), out = in ^ 1;
+                if ((e = cudaMemsetAsync(qc + out, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
+                const WavefrontState se =
+                    tuning.ray_sort ? enqueue_ray_sort(scene, s, in, counters, num_sms, stream) : s;
+                if ((e = launch_extend(scene, se, in, count, counters, extend_grid, stream, ev, true,
+                                       c == 0 ? packet_forms : 0u)) != cudaSuccess)
+                    return e;
+                const WavefrontState ss =
+                    tuning.material_sort ? enqueue_material_sort(scene, se, in, counters, num_sms, stream) : se;
+                if (nee == kNeeDeferred && (e = reset_shadow_counters(counters, stream)) != cudaSuccess) return e;
+                shade<<<shade_blocks, 128, 0, stream>>>(scene, bg, ss, in, counters);
+                if (nee == kNeeDeferred)
+                    enqueue_shadow_stage<2>(scene, DevCamera{}, FrameBuffers{}, RenderParams{}, bg, ss, b.rng, out, 0u,
+                                            0u, counters, shadow_grid, shade_blocks, stream);
+            }
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+            iter += kChunk;
+            nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
+                   (nee == kNeeDeferred ? 2u : 0u)) * kChunk +
+                  extend_launches(packet_forms) - 1u;
+            if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
+                cudaSuccess)
+                return e;
+            if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
+            if (*s.host_len == 0) break;
+            if (iter > max_iters) return cudaErrorLaunchFailure;
+        }
     }
     const unsigned blocks = static_cast<unsigned>((b.total_pixels + 255) / 256);
     k_b_resolve<<<blocks, 256, 0, stream>>>(b, s);

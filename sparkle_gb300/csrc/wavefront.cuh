@@ -142,19 +142,29 @@ struct BatchParams {
     uint32_t rng, enable_nee;
     unsigned long long total_items;
     unsigned long long total_pixels;
-    // The first pass queues its items request by request: those of requests with spp >= kPacket2MinSamples
-    // first, walked in packets of two rays per lane (packet2_items entries), then those with spp >=
-    // kPacketMinSamples, in packets of one ray per lane (up to packet_items entries), then the rest.
+    // The sample items of one group of whole requests, [item_lo, item_hi), run as one wavefront (set per group
+    // by launch_render_batch from BatchGroup). Its first pass queues them request by request: those of requests
+    // with spp >= kPacket2MinSamples first, walked in packets of two rays per lane (packet2_items entries), then
+    // those with spp >= kPacketMinSamples, in packets of one ray per lane (up to packet_items entries), then the
+    // rest (DevRequest::queue_base, relative to the group).
+    unsigned long long item_lo, item_hi;
     unsigned long long packet_items, packet2_items;
     float4 *out_hdr;     // accumulated frame buffers of all requests, request after request
     ushort4 *out_image;  // tonemapped images (top row first per request)
 };
 
-// All sample items of a batch in one regenerating wavefront over `s` (capacity = path slots), then the
-// ordered per-pixel resolve and tonemap into the batch outputs. `s.samples` must hold total_items entries.
-cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, bool count, Counters *counters,
-                                WavefrontState &s, int num_sms, cudaStream_t stream, uint32_t *launches,
-                                LaunchEvents *ev, const WfTuning &tuning);
+// A group of consecutive whole requests rendered as one wavefront: items [item_lo, item_hi), the first
+// packet2_items / packet_items of its first pass walked in packets (BatchParams).
+struct BatchGroup {
+    unsigned long long item_lo, item_hi, packet_items, packet2_items;
+};
+
+// All sample items of a batch, group after group: each group one regenerating wavefront over `s` (capacity =
+// path slots; a group that fits starts all its items at once), then the ordered per-pixel resolve and
+// tonemap into the batch outputs. `s.samples` must hold total_items entries.
+cudaError_t launch_render_batch(const DevScene &scene, const BatchParams &b, const std::vector<BatchGroup> &groups,
+                                bool count, Counters *counters, WavefrontState &s, int num_sms, cudaStream_t stream,
+                                uint32_t *launches, LaunchEvents *ev, const WfTuning &tuning);
 
 // Step of the last launch_render_multiframe call on this thread that returned an error (for messages).
 const char *wavefront_error_site();
