@@ -210,7 +210,8 @@ typedef struct spk_tuning {
     uint32_t bvh_leaf_size;        /* items per BVH leaf, 1..3 (default 3); used by the next spk_set_scene */
     uint32_t extend_blocks_per_sm; /* traversal CTAs per SM, 0 = the occupancy maximum (default 0) */
     uint32_t shade_blocks_per_sm;  /* shading CTAs per SM, 1..32 (default 8) */
-    uint32_t batch_slots;          /* path slots (queue capacity) of spk_render_batch, 0 = min(items, 2^27) */
+    uint32_t batch_slots;          /* path slots (queue capacity) of spk_render_batch, 0 = min(items, 2^27); also the
+                                      largest group of requests rendered as one wavefront */
     uint32_t ray_sort;             /* 1: order each extend queue by ray (direction octant, origin cell) (default 0) */
     uint32_t bvh_collapse;         /* 8-wide collapse: 0 greedy largest-area (default), 1 SAH-optimal; next spk_set_scene */
     uint32_t bvh_builder;          /* BLAS builder: 0 host binned SAH (default), 1 device LBVH (Karras radix tree over
@@ -416,10 +417,11 @@ typedef struct spk_request {
     spk_camera camera;
 } spk_request;
 
-/* No reference counterpart. Renders all requests in one regenerating wavefront: sample items (request,
- * frame, pixel) of every request are handed to path slots from one counter, so requests of uneven
- * resolution, sample count, depth and scene keep the GPU full together. `rng` and `enable_nee` apply to
- * the whole batch. Each request's frame buffer and tonemapped image are bit-identical to spk_set_config
+/* No reference counterpart. Renders the requests in groups of consecutive whole requests of at most the
+ * path slots' sample items (spk_tuning.batch_slots; a larger request alone), each group one regenerating
+ * wavefront: the sample items (request, frame, pixel) of its requests are handed to path slots from one
+ * counter, so requests of uneven resolution, sample count, depth and scene keep the GPU full together, and a
+ * group that fits starts all its samples at once. `rng` and `enable_nee` apply to the whole batch. Each request's frame buffer and tonemapped image are bit-identical to spk_set_config
  * ({width, height, spp = 1, max_spp >= spp, bounce, spatial_denoise = 0, enable_nee, rng, seed}) +
  * spk_set_camera + spk_render(spp) on its scene. Waits for completion; spk_get_stats reports the batch. */
 spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t num_requests, uint32_t rng,
