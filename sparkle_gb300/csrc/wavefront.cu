@@ -90,9 +90,8 @@ __device__ __forceinline__ void start_path(const DevCamera &cam, const RenderPar
     camera_ray<kKind>(cam, rng, u, v, o, d);
     s.ray_o[pid] = make_float4(o.x, o.y, o.z, 0.f);
     s.ray_d[pid] = make_float4(d.x, d.y, d.z, 0.f);
-    s.thr[pid] = make_float4(1.f, 1.f, 1.f, 0.f);
-    s.color[pid] = make_float4(0.f, 0.f, 0.f, 1.f);
-    s.prev_pdf[pid] = 0.f;
+    // Throughput 1, colour 0 with valid flag 1 and no previous light-sampling pdf: shade_path takes these
+    // at bounce 0 without reading them, so they are not stored here.
     store_rng<kKind>(s.rng, pid, rng);
 }
 
@@ -116,12 +115,14 @@ __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontSta
     const uint32_t inst = __float_as_uint(hit4.w);
     const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
     const f3 o = mk3(o4.x, o4.y, o4.z), d = mk3(d4.x, d4.y, d4.z);
-    const float4 c4 = s.color[pid];
+    // A path's first segment starts from throughput 1, colour 0, valid flag 1 and no light-sampling pdf
+    // (start_path leaves them unstored).
+    const float4 c4 = bounce == 0 ? make_float4(0.f, 0.f, 0.f, 1.f) : s.color[pid];
     f3 color = mk3(c4.x, c4.y, c4.z);
-    const float4 t4 = s.thr[pid];
+    const float4 t4 = bounce == 0 ? make_float4(1.f, 1.f, 1.f, 0.f) : s.thr[pid];
     f3 thr = mk3(t4.x, t4.y, t4.z);
     float valid = c4.w;
-    const float prev_pdf = nee ? s.prev_pdf[pid] : 0.f;
+    const float prev_pdf = nee && bounce > 0 ? s.prev_pdf[pid] : 0.f;
     if (inst == kInvalid) {
         if (S.sky_mode != 0u) {
             f3 c = cmul(sky_eval(S, d), thr);
