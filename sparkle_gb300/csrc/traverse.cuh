@@ -72,6 +72,9 @@ enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOve
 #ifndef SPK_PACKET_FRUSTUM
 #define SPK_PACKET_FRUSTUM 1  // 1: packets of one octant test each node once for all rays (0: every lane its own ray)
 #endif
+#ifndef SPK_PACKET_WORLD_SMEM
+#define SPK_PACKET_WORLD_SMEM 1  // 1: packet walks keep each lane's world rays in shared memory, not registers
+#endif
 #ifndef SPK_PACKET_SIBLINGS
 #define SPK_PACKET_SIBLINGS 4  // sibling nodes a packet tests at once (one per 8-lane group), 1..4
 #endif
@@ -699,6 +702,13 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
     const uint32_t budget = S.walk_budget ? S.walk_budget : kMaxIterations;
     uint2 groups[kPacketStack];  // the shared groups (the same in every lane)
     uint32_t own[kPacketStack];  // this lane's hit bits of each
+#if SPK_PACKET_WORLD_SMEM
+    // Each lane's world rays (origin, direction per ray) wait in shared memory, read only at a BLAS exit and
+    // for a candidate hit's world t: entry k of thread t at [k][t], consecutive lanes in consecutive words.
+    __shared__ float4 world[2 * kRays][kWalkThreads];
+    auto world_o = [&](int r) { const float4 v = world[2 * r][threadIdx.x]; return mk3(v.x, v.y, v.z); };
+    auto world_d = [&](int r) { const float4 v = world[2 * r + 1][threadIdx.x]; return mk3(v.x, v.y, v.z); };
+#endif
     unsigned long long base = 0;
     bool todo[kRays];  // this lane's items not walked yet
 #pragma unroll
@@ -760,6 +770,10 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
             setup_level(ray[r], wo[r], wd[r]);
             best[r] = TraceResult{kFltMax, 0.f, 0.f, kInvalid, kInvalid};
             tmax_box[r] = kFltMax;
+#if SPK_PACKET_WORLD_SMEM
+            world[2 * r][threadIdx.x] = make_float4(wo[r].x, wo[r].y, wo[r].z, 0.f);
+            world[2 * r + 1][threadIdx.x] = make_float4(wd[r].x, wd[r].y, wd[r].z, 0.f);
+#endif
         }
         const uint32_t top_order = __shfl_sync(kAll, ray[0].oct, leader);  // the leader's ray: o0, d0
         uint32_t order = top_order;
@@ -879,10 +893,15 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                         float t, u, v;
                         uint32_t face;
                         if (!triangle_hit(S.tris, idx, ray[r], t, u, v, face)) continue;
-                        const float wt = world_t(S.instances[cur_inst], ray[r], t, wo[r], wd[r]);
+#if SPK_PACKET_WORLD_SMEM
+                        const f3 ro = world_o(r), rd = world_d(r);
+#else
+                        const f3 ro = wo[r], rd = wd[r];
+#endif
+                        const float wt = world_t(S.instances[cur_inst], ray[r], t, ro, rd);
                         if (wt > 0.f && closer_hit(best[r], wt, cur_inst, face)) {
                             best[r] = TraceResult{wt, u, v, cur_inst, face};
-                            tmax_box[r] = prune_limit(wt, wo[r], wd[r], S.scene_abs_x);
+                            tmax_box[r] = prune_limit(wt, ro, rd, S.scene_abs_x);
                         }
                     }
                 } else {
@@ -893,9 +912,11 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
 #pragma unroll
                         for (int r = 0; r < kRays; ++r) {
                             float t;
-                            if (sphere_hit(I, wo[r], wd[r], t) && t > 0.f && closer_hit(best[r], t, inst, kInvalid)) {
+                            // (at the TLAS level the level ray is the world ray)
+                            if (sphere_hit(I, ray[r].o, ray[r].d, t) && t > 0.f &&
+                                closer_hit(best[r], t, inst, kInvalid)) {
                                 best[r] = TraceResult{t, 0.f, 0.f, inst, kInvalid};
-                                tmax_box[r] = prune_limit(t, wo[r], wd[r], S.scene_abs_x);
+                                tmax_box[r] = prune_limit(t, ray[r].o, ray[r].d, S.scene_abs_x);
                             }
                         }
                     } else if (I.blas_root != kInvalid) {
@@ -907,7 +928,8 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                         in_blas = true;
                         cur_inst = inst;
 #pragma unroll
-                        for (int r = 0; r < kRays; ++r) setup_level(ray[r], xform_point(I.minv, wo[r]), xform_dir(I.minv, wd[r]));
+                        for (int r = 0; r < kRays; ++r)
+                            setup_level(ray[r], xform_point(I.minv, ray[r].o), xform_dir(I.minv, ray[r].d));
                         const uint32_t entering = __ballot_sync(kAll, mine);  // not empty: the group had bit k
                         order = __shfl_sync(kAll, ray[0].oct, __ffs(entering) - 1);
                         packed = make_frustum(ray, order, frustum);
@@ -922,7 +944,13 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                 if (in_blas && sp == blas_sp) {
                     in_blas = false;
 #pragma unroll
-                    for (int r = 0; r < kRays; ++r) setup_level(ray[r], wo[r], wd[r]);
+                    for (int r = 0; r < kRays; ++r) {
+#if SPK_PACKET_WORLD_SMEM
+                        setup_level(ray[r], world_o(r), world_d(r));
+#else
+                        setup_level(ray[r], wo[r], wd[r]);
+#endif
+                    }
                     order = top_order;
                     if (sp != 0) packed = make_frustum(ray, order, frustum);
                 }
