@@ -55,7 +55,7 @@ enum : uint32_t { kErrStackOverflow = 1u, kErrIterationBudget = 2u, kErrQueueOve
 #define SPK_SLAB_RCP 0  // 1: the slab reciprocals as correctly rounded reciprocals (same bits as 1.f/x)
 #endif
 #ifndef SPK_WALK_MIN_BLOCKS
-#define SPK_WALK_MIN_BLOCKS 7  // resident 128-thread blocks per SM the closest-hit walks are compiled for (72 registers)
+#define SPK_WALK_MIN_BLOCKS 7  // resident 128-thread blocks per SM of the closest-hit walks (72 registers)
 #endif
 #ifndef SPK_SHADOW_MIN_BLOCKS
 #define SPK_SHADOW_MIN_BLOCKS 8  // the same for the occlusion walk of the shadow stage (64 registers)
@@ -826,7 +826,8 @@ __device__ __forceinline__ void walk_packets(const DevScene &S, unsigned long lo
                 nown &= ~(taken << 24);
                 if (rest) push(ngroup, nown);
                 if (kCount && lane == 0) counts->nodes += cnt;
-                const float tmax = __uint_as_float(__reduce_max_sync(kAll, mine_taken ? __float_as_uint(lane_tmax()) : 0u));
+                const float tmax =
+                    __uint_as_float(__reduce_max_sync(kAll, mine_taken ? __float_as_uint(lane_tmax()) : 0u));
                 uint2 ng, tg;
                 visit_node_frustum(S.nodes, node_idx, frustum, order, tmax, ng, tg);
                 // Hand each child's groups out, farthest first onto the stack so the nearest comes back first.

@@ -1276,8 +1276,8 @@ cudaError_t launch_render_multiframe(const DevScene &scene, const DevCamera &cam
                 return e;
             }
             iter += kChunk;
-            nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) + (nee == kNeeDeferred ? 2u : 0u)) *
-                      kChunk +
+            nl += (2u + (tuning.material_sort ? 3u : 0u) + (tuning.ray_sort ? 3u : 0u) +
+                   (nee == kNeeDeferred ? 2u : 0u)) * kChunk +
                   extend_launches(packet_forms) - 1u;
             if ((e = cudaMemcpyAsync(s.host_len, qc, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream)) !=
                 cudaSuccess)
