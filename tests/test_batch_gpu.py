@@ -1,7 +1,8 @@
 """Batched requests (spk_set_scenes + spk_render_batch): each request of a batch over several resident
 scenes renders bit-identically to the same request rendered alone through spk_set_scene / spk_set_config /
-spk_render (frame buffer and tonemapped image), for both RNG policies, with and without NEE; and every
-request matches the CPU oracle's render of it (parity tolerances of tests/parity.py)."""
+spk_render (frame buffer and tonemapped image), for both RNG policies, with and without NEE, in one group or
+in several groups of requests (a small slot budget); and every request matches the CPU oracle's render of it
+(parity tolerances of tests/parity.py)."""
 import numpy as np
 import pytest
 
@@ -27,10 +28,13 @@ def three_scenes(cornell, small_terrain):
     return [cornell, small_terrain, scenes.random_training_scene(5)]
 
 
-@pytest.mark.parametrize("rng,nee", [(abi.SPK_RNG_XOSHIRO256SS, False), (abi.SPK_RNG_XOSHIRO256SS, True),
-                                     (abi.SPK_RNG_XOSHIRO128P, True)])
-def test_batch_matches_single_renders(three_scenes, rng, nee):
+# batch_slots 0: every request in one group; 20000: groups of whole requests of at most 20000 items, and the
+# 268,800-item request alone in its group, regenerating its slots
+@pytest.mark.parametrize("rng,nee,slots", [(abi.SPK_RNG_XOSHIRO256SS, False, 0), (abi.SPK_RNG_XOSHIRO256SS, True, 0),
+                                           (abi.SPK_RNG_XOSHIRO128P, True, 0), (abi.SPK_RNG_XOSHIRO256SS, True, 20000)])
+def test_batch_matches_single_renders(three_scenes, rng, nee, slots):
     batch = native.Context(0)
+    batch.set_tuning(batch_slots=slots)
     batch.set_scenes([sc for sc, _ in three_scenes])
     requests = []
     for scene, w, h, spp, bounce, seed in REQS:
