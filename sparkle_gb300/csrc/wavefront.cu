@@ -75,6 +75,18 @@ __device__ __forceinline__ void queue_nee(const WavefrontState &s, Counters *cou
     queue_push(s.nee_list, &qc[kNeeLen], slot | (ended ? 0x80000000u : 0u), nee_rays != 0u);
 }
 
+// A path's next ray in 24 bytes: origin xyz and direction x in one 16-byte record, direction yz in another.
+__device__ __forceinline__ void store_ray(const WavefrontState &s, uint32_t pid, f3 o, f3 d) {
+    s.ray_a[pid] = make_float4(o.x, o.y, o.z, d.x);
+    s.ray_b[pid] = make_float2(d.y, d.z);
+}
+__device__ __forceinline__ void load_ray(const WavefrontState &s, uint32_t pid, f3 &o, f3 &d) {
+    const float4 a = s.ray_a[pid];
+    const float2 b = s.ray_b[pid];
+    o = mk3(a.x, a.y, a.z);
+    d = mk3(a.w, b.x, b.y);
+}
+
 // RenderPixel's start of a sample (CPURenderer.cpp:398-406, 436-444): reseed, jitter, camera ray.
 template <int kKind>
 __device__ __forceinline__ void start_path(const DevCamera &cam, const RenderParams &p, const WavefrontState &s,
@@ -88,8 +100,7 @@ __device__ __forceinline__ void start_path(const DevCamera &cam, const RenderPar
     const float v = (static_cast<float>(j) + rng_unit<kKind>(rng)) * ph;
     f3 o, d;
     camera_ray<kKind>(cam, rng, u, v, o, d);
-    s.ray_o[pid] = make_float4(o.x, o.y, o.z, 0.f);
-    s.ray_d[pid] = make_float4(d.x, d.y, d.z, 0.f);
+    store_ray(s, pid, o, d);
     // Throughput 1, colour 0 with valid flag 1 and no previous light-sampling pdf: shade_path takes these
     // at bounce 0 without reading them, so they are not stored here.
     store_rng<kKind>(s.rng, pid, rng);
@@ -103,7 +114,7 @@ enum : int { kNeeOff = 0, kNeeInline = 1, kNeeDeferred = 2 };
 // next-event estimation at diffuse-branch vertices with MIS on the emission the BSDF rays collect.
 // kNeeInline walks the two occlusion rays here; kNeeDeferred stores them with their radiance for the
 // shadow stage and returns in `nee_rays` which were queued (bit k: ray k), the colour still without them.
-// Returns whether the path continues (the next ray is then in s.ray_o / s.ray_d).
+// Returns whether the path continues (the next ray is then in s.ray_a / s.ray_b).
 template <int kKind, int kNee>
 __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontState &s, uint32_t pid,
                                            uint32_t bounce, float4 *gnormal, uint32_t &shadow, uint32_t &err,
@@ -113,8 +124,8 @@ __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontSta
     bool alive = false;
     const float4 hit4 = s.hit[pid];
     const uint32_t inst = __float_as_uint(hit4.w);
-    const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
-    const f3 o = mk3(o4.x, o4.y, o4.z), d = mk3(d4.x, d4.y, d4.z);
+    f3 o, d;
+    load_ray(s, pid, o, d);
     // A path's first segment starts from throughput 1, colour 0, valid flag 1 and no light-sampling pdf
     // (start_path leaves them unstored).
     const float4 c4 = bounce == 0 ? make_float4(0.f, 0.f, 0.f, 1.f) : s.color[pid];
@@ -188,8 +199,7 @@ __device__ __forceinline__ bool shade_path(const DevScene &S, const WavefrontSta
                 }
                 if (survive) {
                     const f3 no = surf.location + next_dir * kTolerance;
-                    s.ray_o[pid] = make_float4(no.x, no.y, no.z, 0.f);
-                    s.ray_d[pid] = make_float4(next_dir.x, next_dir.y, next_dir.z, 0.f);
+                    store_ray(s, pid, no, next_dir);
                     if (nee) s.prev_pdf[pid] = next_pdf;
                     alive = true;
                 }
@@ -246,9 +256,7 @@ __global__ void __launch_bounds__(128, kPackets == 2   ? SPK_PACKET2_MIN_BLOCKS
     uint32_t pid = 0;
     auto fetch = [&](unsigned long long q, f3 &o, f3 &d, float &) {
         pid = queue[q];
-        const float4 o4 = s.ray_o[pid], d4 = s.ray_d[pid];
-        o = mk3(o4.x, o4.y, o4.z);
-        d = mk3(d4.x, d4.y, d4.z);
+        load_ray(s, pid, o, d);
         return kBatch ? s.slot_root[pid] : S.tlas_root;
     };
     auto store = [&](uint32_t p, const TraceResult &h) {
@@ -452,7 +460,8 @@ __device__ __forceinline__ uint32_t spread3(uint32_t v) {  // bits b2 b1 b0 -> b
 }
 
 __device__ __forceinline__ uint32_t ray_key(const DevScene &S, const WavefrontState &s, uint32_t pid) {
-    const float4 o = s.ray_o[pid], d = s.ray_d[pid];
+    f3 o, d;
+    load_ray(s, pid, o, d);
     uint32_t c[3];
     const float ov[3] = {o.x, o.y, o.z};
 #pragma unroll
@@ -994,7 +1003,7 @@ cudaError_t wavefront_alloc_nee(WavefrontState &s) {
 cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
     wavefront_free(s);
     cudaError_t e;
-    if ((e = dmalloc(s.ray_o, capacity)) != cudaSuccess || (e = dmalloc(s.ray_d, capacity)) != cudaSuccess ||
+    if ((e = dmalloc(s.ray_a, capacity)) != cudaSuccess || (e = dmalloc(s.ray_b, capacity)) != cudaSuccess ||
         (e = dmalloc(s.thr, capacity)) != cudaSuccess || (e = dmalloc(s.color, capacity)) != cudaSuccess ||
         (e = dmalloc(s.rng, 2 * static_cast<size_t>(capacity))) != cudaSuccess ||
         (e = dmalloc(s.hit, capacity)) != cudaSuccess || (e = dmalloc(s.hit_face, capacity)) != cudaSuccess ||
@@ -1015,7 +1024,7 @@ cudaError_t wavefront_alloc(WavefrontState &s, uint32_t capacity) {
 }
 
 void wavefront_free(WavefrontState &s) {
-    void *ptrs[] = {s.ray_o,      s.ray_d,     s.thr,     s.color,        s.rng,        s.hit,
+    void *ptrs[] = {s.ray_a,      s.ray_b,     s.thr,     s.color,        s.rng,        s.hit,
                     s.hit_face,   s.queue[0],  s.queue[1], s.sort_keys,   s.slot_state, s.slot_item,
                     s.samples,    s.frame_weight, s.frame_seed, s.prev_pdf, s.sort_hist, s.slot_req,
                     s.slot_root,  s.sort_keys2, s.shadow_o, s.shadow_d, s.nee_contrib, s.shadow_queue,

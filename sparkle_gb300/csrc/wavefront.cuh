@@ -18,8 +18,8 @@ namespace spk {
 
 struct WavefrontState {
     uint32_t capacity = 0;
-    float4 *ray_o = nullptr;    // origin xyz, w = pixel index bits
-    float4 *ray_d = nullptr;    // direction xyz
+    float4 *ray_a = nullptr;    // next ray: origin xyz, direction x
+    float2 *ray_b = nullptr;    // next ray: direction y, z
     float4 *thr = nullptr;      // throughput xyz
     float4 *color = nullptr;    // radiance xyz, w = valid flag
     uint4 *rng = nullptr;       // 2 x uint4 per path (xoshiro256** needs 32 B)
