@@ -218,7 +218,7 @@ typedef struct spk_tuning {
                                       Morton order), 2 device PLOC clustering over Morton order; 1 and 2 use the greedy
                                       collapse (bvh_collapse ignored) and take milliseconds where the host takes seconds */
     uint32_t path_slots_per_pixel; /* multi-frame schedule: paths in flight per pixel, 1..64 (default 64: every sample
-                                      of a 64-frame call at once, at most 2^27 paths, ~152 B of state each). More paths
+                                      of a 64-frame call at once, at most 2^27 paths, ~144 B of state each). More paths
                                       per extend launch spread each launch's tail (its last, longest walks) over more
                                       rays; spk_render(1) uses one path per pixel whatever the setting */
     uint32_t shadow_stage;         /* wavefront NEE: 1 (default) queues the light and sky occlusion rays of each
