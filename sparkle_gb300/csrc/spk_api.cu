@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "../../include/spk.h"
+#include "batch_plan.h"
 #include "bvh_builder.h"
 #include "bvh_device.cuh"
 #include "fault.h"
@@ -2055,39 +2056,20 @@ spk_status spk_render_batch(spk_ctx *ctx, const spk_request *requests, uint32_t 
         return fail(ctx, SPK_ERR_INVALID_ARGUMENT, "batch of %llu sample items: split it below 2^32", items);
     const uint32_t slots = static_cast<uint32_t>(
         std::min<unsigned long long>(items, ctx->tuning.batch_slots ? ctx->tuning.batch_slots : kMaxPathSlots));
-    // Groups of consecutive whole requests of at most `slots` items (a larger request alone), each rendered as
-    // one wavefront that starts all its items at once. A group's first-pass queue holds each request's items in
-    // item order, the requests with spp >= kPacket2MinSamples first (walked in packets of two rays per lane),
-    // then those with spp >= kPacketMinSamples (one ray per lane), then the others.
-    auto packet_class = [](uint32_t spp) { return spp >= kPacket2MinSamples ? 0 : spp >= kPacketMinSamples ? 1 : 2; };
+    // Groups of consecutive whole requests, each one wavefront, and their first-pass queue layout (batch_plan.h).
     std::vector<BatchGroup> groups;
-    auto close_group = [&](uint32_t r0, uint32_t r1, unsigned long long lo, unsigned long long hi) {
-        const unsigned long long first_end = lo + std::min<unsigned long long>(slots, hi - lo);
-        auto first_pass_items = [&](const DevRequest &d) {
-            return std::min<unsigned long long>(d.item_base + 1ull * d.npix * d.spp, first_end) -
-                   std::min<unsigned long long>(d.item_base, first_end);
-        };
-        unsigned long long class_items[3] = {0, 0, 0};
-        for (uint32_t r = r0; r < r1; ++r) class_items[packet_class(reqs[r].spp)] += first_pass_items(reqs[r]);
-        unsigned long long pos[3] = {0, class_items[0], class_items[0] + class_items[1]};
-        for (uint32_t r = r0; r < r1; ++r) {
-            unsigned long long &q = pos[packet_class(reqs[r].spp)];
-            reqs[r].queue_base = static_cast<uint32_t>(q);
-            q += first_pass_items(reqs[r]);
+    {
+        std::vector<uint64_t> req_items(num_requests);
+        std::vector<uint32_t> req_spp(num_requests), queue_base(num_requests);
+        for (uint32_t r = 0; r < num_requests; ++r) {
+            req_items[r] = 1ull * reqs[r].npix * reqs[r].spp;
+            req_spp[r] = reqs[r].spp;
         }
         const bool pk = ctx->tuning.primary_packets != 0;
-        groups.push_back(BatchGroup{lo, hi, pk ? class_items[0] + class_items[1] : 0ull, pk ? class_items[0] : 0ull});
-    };
-    {
-        uint32_t r0 = 0;
-        for (uint32_t r = 1; r < num_requests; ++r) {
-            const DevRequest &d = reqs[r];
-            if (d.item_base + 1ull * d.npix * d.spp - reqs[r0].item_base > slots) {
-                close_group(r0, r, reqs[r0].item_base, d.item_base);
-                r0 = r;
-            }
-        }
-        close_group(r0, num_requests, reqs[r0].item_base, items);
+        for (const BatchPlanGroup &g : plan_batch(req_items.data(), req_spp.data(), num_requests, slots,
+                                                  kPacketMinSamples, kPacket2MinSamples, queue_base.data()))
+            groups.push_back(BatchGroup{g.item_lo, g.item_hi, pk ? g.packet_items : 0ull, pk ? g.packet2_items : 0ull});
+        for (uint32_t r = 0; r < num_requests; ++r) reqs[r].queue_base = queue_base[r];
     }
     cudaError_t e;
     WavefrontState &s = ctx->wf_batch;
